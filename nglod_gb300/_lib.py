@@ -1,0 +1,110 @@
+"""ctypes binding of the C ABI in include/nglod_gb300.h.
+
+The library is loaded from nglod_gb300/_build/libnglod_gb300.so (built by
+``nglod_gb300.build``).  There is no fallback: if it is missing, or a call is
+made with CPU tensors, a RuntimeError is raised.
+"""
+import ctypes
+import os
+
+import torch
+
+from . import build as _build
+
+MAX_LODS = 8
+F32 = 0
+BF16 = 1
+
+STATUS = {
+    0: "ok",
+    -1: "invalid argument",
+    -2: "unsupported configuration",
+    -3: "CUDA error",
+    -4: "capacity exceeded",
+    -5: "misaligned pointer",
+    -6: "device wait timed out",
+}
+
+_vp = ctypes.c_void_p
+_i64 = ctypes.c_int64
+_i32 = ctypes.c_int32
+
+
+class DenseModel(ctypes.Structure):
+    _fields_ = [
+        ("num_lods", _i32),
+        ("base_lod", _i32),
+        ("feature_dim", _i32),
+        ("hidden_dim", _i32),
+        ("grid_dtype", _i32),
+        ("reserved", _i32),
+        ("grid", _vp * MAX_LODS),
+        ("w0", _vp * MAX_LODS),
+        ("b0", _vp * MAX_LODS),
+        ("w1", _vp * MAX_LODS),
+        ("b1", _vp * MAX_LODS),
+    ]
+
+
+class TraceParams(ctypes.Structure):
+    _fields_ = [
+        ("num_steps", _i32),
+        ("min_dis", ctypes.c_float),
+        ("osc_dis", ctypes.c_float),
+        ("step_size", ctypes.c_float),
+        ("far_clip", ctypes.c_float),
+        ("lod", _i32),
+        ("want_normals", _i32),
+    ]
+
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "nglod_version": (ctypes.c_char_p, []),
+    "nglod_last_error": (ctypes.c_char_p, []),
+    "nglod_aabb": (ctypes.c_int, [_vp, _vp, _i64, _vp, _vp, _vp, _vp]),
+    "nglod_volume_sample": (ctypes.c_int, [_vp, _i32, _i32, _vp, _i64, _vp, _vp]),
+    "nglod_sdf_fwd": (ctypes.c_int, [ctypes.POINTER(DenseModel), _vp, _i64, _i32, _i32, _vp, _vp]),
+    "nglod_trace": (ctypes.c_int, [ctypes.POINTER(DenseModel), ctypes.POINTER(TraceParams), _vp, _vp, _i64,
+                                   _vp, _vp, _vp, _vp, _vp, _vp]),
+}
+
+_LIB = None
+
+
+def load():
+    """Load the library once and declare every signature; raises if absent."""
+    global _LIB
+    if _LIB is None:
+        path = _build.library_path()
+        if not os.path.exists(path):
+            raise RuntimeError(
+                f"nglod_gb300 CUDA library not found at {path}; build it with "
+                "`python -m nglod_gb300.build` (there is no CPU fallback)")
+        lib = ctypes.CDLL(path)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _LIB = lib
+    return _LIB
+
+
+def check(status, what):
+    if status != 0:
+        msg = load().nglod_last_error().decode(errors="replace")
+        raise RuntimeError(f"{what} failed ({STATUS.get(status, status)}): {msg}")
+
+
+def stream_ptr(device=None):
+    return ctypes.c_void_p(torch.cuda.current_stream(device).cuda_stream)
+
+
+def ptr(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else ctypes.c_void_p(0)
+
+
+def require_cuda(*tensors):
+    for t in tensors:
+        if not isinstance(t, torch.Tensor) or not t.is_cuda:
+            raise RuntimeError("nglod_gb300 runs on CUDA tensors only (no CPU fallback)")

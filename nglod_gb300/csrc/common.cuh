@@ -1,0 +1,42 @@
+// Shared helpers of the nglod_gb300 CUDA library: status reporting, launch
+// geometry, and small device utilities.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "nglod_gb300.h"
+
+namespace nglod {
+
+// Records a printf-style message as this host thread's last error.
+void set_error(const char *fmt, ...);
+
+// NGLOD_OK if e == cudaSuccess, else records "<where>: <cuda message>" and
+// returns NGLOD_ERR_CUDA.
+int cuda_status(cudaError_t e, const char *where);
+
+// Launch status of the last kernel launch on this thread.
+inline int launch_status(const char *where) { return cuda_status(cudaGetLastError(), where); }
+
+// Multiprocessor count of the current device (cached per device).
+int num_sms();
+
+inline bool aligned(const void *p, uintptr_t a) { return (reinterpret_cast<uintptr_t>(p) & (a - 1)) == 0; }
+
+}  // namespace nglod
+
+#define NGLOD_REQUIRE(cond, code, ...)        \
+    do {                                      \
+        if (!(cond)) {                        \
+            ::nglod::set_error(__VA_ARGS__);  \
+            return (code);                    \
+        }                                     \
+    } while (0)
+
+#define NGLOD_TRY(expr)            \
+    do {                           \
+        int _st = (expr);          \
+        if (_st != NGLOD_OK)       \
+            return _st;            \
+    } while (0)

@@ -1,0 +1,551 @@
+// Dense NGLOD path, float32: ray/box entry, fused LOD gather + decoder, and a
+// persistent sphere tracer.
+//
+// Layout: feature volume l is channel-last [s][s][s][C] (C = 32 floats =
+// 128 B per vertex), so each trilinear corner is eight 16-byte loads of one
+// cache line.  The decoder of one LOD is staged in shared memory as H rows of
+// 36 floats (35 weights of Linear(35, H) followed by its bias; the input
+// vector carries a trailing 1.0) plus the H weights and the bias of
+// Linear(H, 1).  Every thread evaluates whole points, reading the decoder
+// rows as warp-wide broadcasts.
+#include <math.h>
+
+#include "common.cuh"
+
+namespace nglod {
+
+constexpr int kC = 32;         // feature channels this library is built for
+constexpr int kRowF4 = 9;      // float4 per staged decoder row (35 weights + bias)
+
+// float4 count of one staged decoder with H hidden units.
+__host__ __device__ inline int decoder_f4(int H) { return H * kRowF4 + (H + 4) / 4; }
+
+__device__ __forceinline__ void stage_decoder(float4 *dst, const nglod_dense_model &m, int l) {
+    const int H = m.hidden_dim;
+    float *rows = reinterpret_cast<float *>(dst);
+    const float *__restrict__ w0 = m.w0[l];
+    const float *__restrict__ b0 = m.b0[l];
+    for (int i = threadIdx.x; i < H * 36; i += blockDim.x) {
+        const int j = i / 36, k = i - j * 36;
+        rows[i] = k < 35 ? w0[j * 35 + k] : b0[j];
+    }
+    float *w1s = rows + H * 36;
+    for (int j = threadIdx.x; j < H; j += blockDim.x) w1s[j] = m.w1[l][j];
+    if (threadIdx.x == 0) w1s[H] = m.b1[l][0];
+}
+
+// Adds the trilinear sample of one channel-last float32 volume (s vertices per
+// side) at point p to f.  Same arithmetic as PyTorch's 3-D grid sampler with
+// align_corners=True and padding_mode='border': u = ((p + 1) / 2) * (s - 1)
+// clamped to [0, s - 1], corner weights are products of distances to the
+// opposite corner, corners summed in tnw, tne, tsw, tse, bnw, bne, bsw, bse
+// order.  The far corner index is clamped to s - 1 where u = s - 1; its weight
+// is then exactly 0, as when PyTorch skips the out-of-range corner.
+__device__ __forceinline__ void gather_add_f32(const float *__restrict__ g, int s, float px, float py,
+                                               float pz, float (&f)[kC]) {
+    const float sm1 = (float)(s - 1);
+    float ix = ((px + 1.f) / 2.f) * sm1;
+    float iy = ((py + 1.f) / 2.f) * sm1;
+    float iz = ((pz + 1.f) / 2.f) * sm1;
+    ix = fminf(sm1, fmaxf(ix, 0.f));
+    iy = fminf(sm1, fmaxf(iy, 0.f));
+    iz = fminf(sm1, fmaxf(iz, 0.f));
+    const float x0 = floorf(ix), y0 = floorf(iy), z0 = floorf(iz);
+    const float wx1 = ix - x0, wx0 = (x0 + 1.f) - ix;
+    const float wy1 = iy - y0, wy0 = (y0 + 1.f) - iy;
+    const float wz1 = iz - z0, wz0 = (z0 + 1.f) - iz;
+    const int xi = (int)x0, yi = (int)y0, zi = (int)z0;
+    const int xj = min(xi + 1, s - 1), yj = min(yi + 1, s - 1), zj = min(zi + 1, s - 1);
+    const size_t sy = (size_t)s * kC, sz = (size_t)s * sy;
+    const float4 *c[8];
+    c[0] = reinterpret_cast<const float4 *>(g + zi * sz + yi * sy + xi * kC);
+    c[1] = reinterpret_cast<const float4 *>(g + zi * sz + yi * sy + xj * kC);
+    c[2] = reinterpret_cast<const float4 *>(g + zi * sz + yj * sy + xi * kC);
+    c[3] = reinterpret_cast<const float4 *>(g + zi * sz + yj * sy + xj * kC);
+    c[4] = reinterpret_cast<const float4 *>(g + zj * sz + yi * sy + xi * kC);
+    c[5] = reinterpret_cast<const float4 *>(g + zj * sz + yi * sy + xj * kC);
+    c[6] = reinterpret_cast<const float4 *>(g + zj * sz + yj * sy + xi * kC);
+    c[7] = reinterpret_cast<const float4 *>(g + zj * sz + yj * sy + xj * kC);
+    float w[8];
+    w[0] = wx0 * wy0 * wz0;
+    w[1] = wx1 * wy0 * wz0;
+    w[2] = wx0 * wy1 * wz0;
+    w[3] = wx1 * wy1 * wz0;
+    w[4] = wx0 * wy0 * wz1;
+    w[5] = wx1 * wy0 * wz1;
+    w[6] = wx0 * wy1 * wz1;
+    w[7] = wx1 * wy1 * wz1;
+#pragma unroll
+    for (int q = 0; q < kC / 4; ++q) {
+        float4 v[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) v[k] = __ldg(c[k] + q);
+        float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            a0 = fmaf(v[k].x, w[k], a0);
+            a1 = fmaf(v[k].y, w[k], a1);
+            a2 = fmaf(v[k].z, w[k], a2);
+            a3 = fmaf(v[k].w, w[k], a3);
+        }
+        f[4 * q + 0] += a0;
+        f[4 * q + 1] += a1;
+        f[4 * q + 2] += a2;
+        f[4 * q + 3] += a3;
+    }
+}
+
+// Linear(35, H) -> ReLU -> Linear(H, 1) on [p, f] with the staged decoder.
+__device__ __forceinline__ float decode_f32(const float4 *__restrict__ dec, int H, float px, float py,
+                                            float pz, const float (&f)[kC]) {
+    const float *__restrict__ w1 = reinterpret_cast<const float *>(dec + H * kRowF4);
+    float in[36];
+    in[0] = px;
+    in[1] = py;
+    in[2] = pz;
+#pragma unroll
+    for (int c = 0; c < kC; ++c) in[3 + c] = f[c];
+    in[35] = 1.f;
+    float out = 0.f;
+#pragma unroll 1
+    for (int j = 0; j < H; j += 2) {
+        const float4 *r0 = dec + j * kRowF4;
+        const float4 *r1 = r0 + kRowF4;
+        float a0 = 0.f, a1 = 0.f, b0 = 0.f, b1 = 0.f;
+#pragma unroll
+        for (int q = 0; q < kRowF4; ++q) {
+            const float4 u = r0[q];
+            const float4 v = r1[q];
+            if (q & 1) {
+                a1 = fmaf(u.x, in[4 * q + 0], a1);
+                a1 = fmaf(u.y, in[4 * q + 1], a1);
+                a1 = fmaf(u.z, in[4 * q + 2], a1);
+                a1 = fmaf(u.w, in[4 * q + 3], a1);
+                b1 = fmaf(v.x, in[4 * q + 0], b1);
+                b1 = fmaf(v.y, in[4 * q + 1], b1);
+                b1 = fmaf(v.z, in[4 * q + 2], b1);
+                b1 = fmaf(v.w, in[4 * q + 3], b1);
+            } else {
+                a0 = fmaf(u.x, in[4 * q + 0], a0);
+                a0 = fmaf(u.y, in[4 * q + 1], a0);
+                a0 = fmaf(u.z, in[4 * q + 2], a0);
+                a0 = fmaf(u.w, in[4 * q + 3], a0);
+                b0 = fmaf(v.x, in[4 * q + 0], b0);
+                b0 = fmaf(v.y, in[4 * q + 1], b0);
+                b0 = fmaf(v.z, in[4 * q + 2], b0);
+                b0 = fmaf(v.w, in[4 * q + 3], b0);
+            }
+        }
+        const float h0 = fmaxf(a0 + a1, 0.f);
+        const float h1 = fmaxf(b0 + b1, 0.f);
+        out = fmaf(w1[j], h0, out);
+        out = fmaf(w1[j + 1], h1, out);
+    }
+    return out + w1[H];
+}
+
+__device__ __forceinline__ int volume_side(const nglod_dense_model &m, int l) { return (1 << (l + m.base_lod)) + 1; }
+
+// Sum of the LOD 0..L samples at p, then decoder `dec`.
+__device__ __forceinline__ float eval_point_f32(const nglod_dense_model &m, int L, const float4 *dec, float px,
+                                                float py, float pz) {
+    float f[kC];
+#pragma unroll
+    for (int c = 0; c < kC; ++c) f[c] = 0.f;
+#pragma unroll 1
+    for (int l = 0; l <= L; ++l)
+        gather_add_f32(static_cast<const float *>(m.grid[l]), volume_side(m, l), px, py, pz, f);
+    return decode_f32(dec, m.hidden_dim, px, py, pz, f);
+}
+
+// ---------------------------------------------------------------------------
+// sdf forward
+// ---------------------------------------------------------------------------
+template <bool kAll>
+__global__ void __launch_bounds__(256) sdf_fwd_f32_kernel(const nglod_dense_model m, const float *__restrict__ x,
+                                                          int64_t n, int L, float *__restrict__ out) {
+    extern __shared__ float4 smem[];
+    const int H = m.hidden_dim;
+    const int dstride = decoder_f4(H);
+    const int first = kAll ? 0 : L;
+    for (int l = first; l <= L; ++l) stage_decoder(smem + (l - first) * dstride, m, l);
+    __syncthreads();
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const float px = x[3 * i], py = x[3 * i + 1], pz = x[3 * i + 2];
+        float f[kC];
+#pragma unroll
+        for (int c = 0; c < kC; ++c) f[c] = 0.f;
+#pragma unroll 1
+        for (int l = 0; l <= L; ++l) {
+            gather_add_f32(static_cast<const float *>(m.grid[l]), volume_side(m, l), px, py, pz, f);
+            if (kAll) out[(int64_t)l * n + i] = decode_f32(smem + l * dstride, H, px, py, pz, f);
+        }
+        if (!kAll) out[i] = decode_f32(smem, H, px, py, pz, f);
+    }
+}
+
+// One feature volume sampled at every point: out[n][C] (FeatureVolume.forward).
+__global__ void __launch_bounds__(256) volume_sample_f32_kernel(const float *__restrict__ g, int s,
+                                                                const float *__restrict__ x, int64_t n,
+                                                                float *__restrict__ out) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        float f[kC];
+#pragma unroll
+        for (int c = 0; c < kC; ++c) f[c] = 0.f;
+        gather_add_f32(g, s, x[3 * i], x[3 * i + 1], x[3 * i + 2], f);
+        float4 *o = reinterpret_cast<float4 *>(out + i * kC);
+#pragma unroll
+        for (int q = 0; q < kC / 4; ++q) o[q] = make_float4(f[4 * q], f[4 * q + 1], f[4 * q + 2], f[4 * q + 3]);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// ray vs [-1,1]^3 box
+// ---------------------------------------------------------------------------
+
+// Entry distance of a ray into the unit box, with the float arithmetic of
+// sol_nglod_kernel.cu:92-150: reciprocal direction in double then float,
+// slab distances (sgn - o) * invdir, entry-face tests with fmaf, the first
+// passing face in x, y, z order, accepted when t < 500.  Rays starting inside
+// the box return false.
+__device__ __forceinline__ bool box_entry(float ox, float oy, float oz, float dx, float dy, float dz, float &t) {
+    const float ivx = (float)(1.0 / (double)dx);
+    const float ivy = (float)(1.0 / (double)dy);
+    const float ivz = (float)(1.0 / (double)dz);
+    const float s0 = signbit(dx) ? 1.f : -1.f;
+    const float s1 = signbit(dy) ? 1.f : -1.f;
+    const float s2 = signbit(dz) ? 1.f : -1.f;
+    const float cmax = fmaxf(fmaxf(fabsf(ox), fabsf(oy)), fabsf(oz));
+    if (cmax < 1.f) return false;
+    const float d0 = __fmul_rn(__fsub_rn(s0, ox), ivx);
+    const float d1 = __fmul_rn(__fsub_rn(s1, oy), ivy);
+    const float d2 = __fmul_rn(__fsub_rn(s2, oz), ivz);
+    const bool t0 = (d0 >= 0.f) && (fabsf(fmaf(dy, d0, oy)) < 1.f) && (fabsf(fmaf(dz, d0, oz)) < 1.f);
+    const bool t1 = (d1 >= 0.f) && (fabsf(fmaf(dx, d1, ox)) < 1.f) && (fabsf(fmaf(dz, d1, oz)) < 1.f);
+    const bool t2 = (d2 >= 0.f) && (fabsf(fmaf(dx, d2, ox)) < 1.f) && (fabsf(fmaf(dy, d2, oy)) < 1.f);
+    const float d = t0 ? d0 : (t1 ? d1 : (t2 ? d2 : 0.f));
+    if ((t0 || t1 || t2) && d < 500.f) {
+        t = d;
+        return true;
+    }
+    return false;
+}
+
+__global__ void __launch_bounds__(256) aabb_kernel(const float *__restrict__ ro, const float *__restrict__ rd,
+                                                   int64_t n, float *__restrict__ x, float *__restrict__ t,
+                                                   uint8_t *__restrict__ hit) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const float ox = ro[3 * i], oy = ro[3 * i + 1], oz = ro[3 * i + 2];
+        const float dx = rd[3 * i], dy = rd[3 * i + 1], dz = rd[3 * i + 2];
+        float tt = 0.f;
+        const bool h = box_entry(ox, oy, oz, dx, dy, dz, tt);
+        x[3 * i + 0] = h ? fmaf(dx, tt, ox) : ox;
+        x[3 * i + 1] = h ? fmaf(dy, tt, oy) : oy;
+        x[3 * i + 2] = h ? fmaf(dz, tt, oz) : oz;
+        t[i] = h ? tt : 0.f;
+        hit[i] = h ? 1 : 0;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// persistent sphere tracer
+// ---------------------------------------------------------------------------
+struct TraceArgs {
+    nglod_dense_model m;
+    nglod_trace_params p;
+    int L;
+    const float *ray_o;
+    const float *ray_d;
+    int64_t n;
+    float *x;
+    float *t;
+    uint8_t *hit;
+    float *normal;
+    unsigned long long *counter;
+};
+
+enum : int { kNeed = 0, kEvalInit = 1, kMarch = 2, kTap0 = 3, kDone = 9, kGone = 10 };
+
+// One thread owns one ray at a time and every loop iteration evaluates exactly
+// one sdf point per thread: the ray's first point, its next march point, or
+// one of the six finite-difference taps of its normal.  A thread whose ray
+// finishes writes it out and takes the next ray index from a global counter;
+// the lanes of a warp that need rays in the same iteration share one
+// atomicAdd.  Per ray this runs SphereTracer.forward's state machine
+// (SphereTracer.py:74-130): hit = |t| < far is re-evaluated at the start of
+// every iteration, cond &= |d| > min_dis & |(d+dprev)/2| > osc_dis & hit,
+// x = o + dir*t, dprev = d, d = net(x) * step_size, t += d; after the march
+// hit &= all(|x| <= 1) and hit rays get normalize(central differences, h =
+// 1/192).  Rays never affect one another in the reference, so running each to
+// completion gives the same results as its global loop.
+__global__ void __launch_bounds__(128) trace_f32_kernel(const TraceArgs a) {
+    extern __shared__ float4 smem[];
+    stage_decoder(smem, a.m, a.L);
+    __syncthreads();
+
+    const unsigned FULL = 0xffffffffu;
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    const float h = 1.0f / 192.0f;
+    const float twoh = (float)(2.0 / 192.0);
+
+    int phase = kNeed, step = 0;
+    int64_t ray = 0;
+    float ox = 0.f, oy = 0.f, oz = 0.f, dx = 0.f, dy = 0.f, dz = 0.f;
+    float xx = 0.f, xy = 0.f, xz = 0.f, t = 0.f, d = 0.f, dprev = 0.f;
+    float g[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    float nx = 0.f, ny = 0.f, nz = 0.f;
+    bool cond = false, hitr = false, hitf = false;
+
+    auto finish = [&]() {
+        hitf = hitr && !(fabsf(xx) > 1.f || fabsf(xy) > 1.f || fabsf(xz) > 1.f);
+        phase = (hitf && a.p.want_normals) ? kTap0 : kDone;
+    };
+    // Start of march iteration `step` (SphereTracer.py:84-114).
+    auto march_decide = [&]() {
+        if (step >= a.p.num_steps) {
+            finish();
+            return;
+        }
+        hitr = fabsf(t) < a.p.far_clip;
+        cond = cond && (fabsf(d) > a.p.min_dis) && (fabsf((d + dprev) / 2.f) > a.p.osc_dis) && hitr;
+        if (!cond) {
+            finish();
+            return;
+        }
+        xx = __fadd_rn(ox, __fmul_rn(dx, t));
+        xy = __fadd_rn(oy, __fmul_rn(dy, t));
+        xz = __fadd_rn(oz, __fmul_rn(dz, t));
+        dprev = d;
+        phase = kMarch;
+    };
+
+    for (;;) {
+        for (;;) {
+            if (phase == kDone) {
+                a.x[3 * ray + 0] = xx;
+                a.x[3 * ray + 1] = xy;
+                a.x[3 * ray + 2] = xz;
+                a.t[ray] = t;
+                a.hit[ray] = hitf ? 1 : 0;
+                if (a.normal) {
+                    const bool hn = hitf && a.p.want_normals;
+                    a.normal[3 * ray + 0] = hn ? nx : 0.f;
+                    a.normal[3 * ray + 1] = hn ? ny : 0.f;
+                    a.normal[3 * ray + 2] = hn ? nz : 0.f;
+                }
+                phase = kNeed;
+            }
+            const unsigned need = __ballot_sync(FULL, phase == kNeed);
+            if (need == 0u) break;
+            const int leader = __ffs(need) - 1;
+            unsigned long long base = 0ull;
+            if ((int)lane == leader) base = atomicAdd(a.counter, (unsigned long long)__popc(need));
+            base = __shfl_sync(FULL, base, leader);
+            if (phase == kNeed) {
+                const unsigned long long r = base + (unsigned long long)__popc(need & lt_mask);
+                if (r >= (unsigned long long)a.n) {
+                    phase = kGone;
+                } else {
+                    ray = (int64_t)r;
+                    ox = a.ray_o[3 * ray];
+                    oy = a.ray_o[3 * ray + 1];
+                    oz = a.ray_o[3 * ray + 2];
+                    dx = a.ray_d[3 * ray];
+                    dy = a.ray_d[3 * ray + 1];
+                    dz = a.ray_d[3 * ray + 2];
+                    t = 0.f;
+                    cond = box_entry(ox, oy, oz, dx, dy, dz, t);
+                    xx = cond ? fmaf(dx, t, ox) : ox;
+                    xy = cond ? fmaf(dy, t, oy) : oy;
+                    xz = cond ? fmaf(dz, t, oz) : oz;
+                    step = 0;
+                    hitr = false;
+                    hitf = false;
+                    if (cond)
+                        phase = kEvalInit;
+                    else
+                        march_decide();
+                }
+            }
+        }
+        if (__all_sync(FULL, phase == kGone)) break;
+
+        float qx = xx, qy = xy, qz = xz;
+        if (phase >= kTap0 && phase < kDone) {
+            const int k = phase - kTap0;
+            const float e = (k & 1) ? -h : h;
+            if ((k >> 1) == 0) qx = __fadd_rn(xx, e);
+            else if ((k >> 1) == 1) qy = __fadd_rn(xy, e);
+            else qz = __fadd_rn(xz, e);
+        }
+        const float v = eval_point_f32(a.m, a.L, smem, qx, qy, qz);
+
+        if (phase == kEvalInit) {
+            d = v;
+            dprev = d;
+            march_decide();
+        } else if (phase == kMarch) {
+            d = v * a.p.step_size;
+            t = t + d;
+            ++step;
+            march_decide();
+        } else if (phase >= kTap0 && phase < kDone) {
+            const int k = phase - kTap0;
+#pragma unroll
+            for (int i = 0; i < 6; ++i)
+                if (i == k) g[i] = v;
+            if (k == 5) {
+                const float gx = (g[0] - g[1]) / twoh;
+                const float gy = (g[2] - g[3]) / twoh;
+                const float gz = (g[4] - g[5]) / twoh;
+                const float nrm = sqrtf(gx * gx + gy * gy + gz * gz);
+                const float den = fmaxf(nrm, 1e-5f);
+                nx = gx / den;
+                ny = gy / den;
+                nz = gz / den;
+                phase = kDone;
+            } else {
+                phase = phase + 1;
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+static int check_model(const nglod_dense_model *m, int L_max) {
+    NGLOD_REQUIRE(m != nullptr, NGLOD_ERR_INVALID, "model is null");
+    NGLOD_REQUIRE(m->num_lods >= 1 && m->num_lods <= NGLOD_MAX_LODS, NGLOD_ERR_INVALID,
+                  "num_lods=%d outside [1, %d]", m->num_lods, NGLOD_MAX_LODS);
+    NGLOD_REQUIRE(m->base_lod >= 0 && m->num_lods - 1 + m->base_lod <= 9, NGLOD_ERR_INVALID,
+                  "base_lod=%d with num_lods=%d gives volumes above 2^9+1 per side", m->base_lod, m->num_lods);
+    NGLOD_REQUIRE(m->feature_dim == kC, NGLOD_ERR_UNSUPPORTED, "feature_dim=%d not built (only %d)",
+                  m->feature_dim, kC);
+    NGLOD_REQUIRE(m->hidden_dim >= 2 && m->hidden_dim <= 256 && (m->hidden_dim % 2) == 0, NGLOD_ERR_UNSUPPORTED,
+                  "hidden_dim=%d not built (even, 2..256)", m->hidden_dim);
+    NGLOD_REQUIRE(m->grid_dtype == NGLOD_F32, NGLOD_ERR_UNSUPPORTED, "grid_dtype=%d: this entry point is float32",
+                  m->grid_dtype);
+    for (int l = 0; l <= L_max; ++l) {
+        NGLOD_REQUIRE(m->grid[l] && m->w0[l] && m->b0[l] && m->w1[l] && m->b1[l], NGLOD_ERR_INVALID,
+                      "lod %d has a null volume or decoder pointer", l);
+        NGLOD_REQUIRE(aligned(m->grid[l], 16), NGLOD_ERR_ALIGN, "volume %d is not 16-byte aligned", l);
+    }
+    return NGLOD_OK;
+}
+
+static int resolve_lod(const nglod_dense_model *m, int lod) {
+    return (lod < 0 || lod >= m->num_lods) ? m->num_lods - 1 : lod;
+}
+
+template <typename K>
+static int prepare_smem(K kernel, size_t smem) {
+    NGLOD_REQUIRE(smem <= 227 * 1024, NGLOD_ERR_UNSUPPORTED, "decoder staging needs %zu B of shared memory", smem);
+    return cuda_status(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                       "cudaFuncSetAttribute");
+}
+
+template <typename K>
+static int resident_blocks(K kernel, int threads, size_t smem) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    return per_sm * num_sms();
+}
+
+}  // namespace nglod
+
+using namespace nglod;
+
+extern "C" int nglod_aabb(const float *ray_o, const float *ray_d, int64_t n, float *x, float *t, uint8_t *hit,
+                          nglod_stream_t stream) {
+    NGLOD_REQUIRE(n >= 0, NGLOD_ERR_INVALID, "n=%lld is negative", (long long)n);
+    if (n == 0) return NGLOD_OK;
+    NGLOD_REQUIRE(ray_o && ray_d && x && t && hit, NGLOD_ERR_INVALID, "null pointer argument");
+    const int threads = 256;
+    const int64_t want = (n + threads - 1) / threads;
+    const int blocks = (int)(want < (int64_t)num_sms() * 16 ? want : (int64_t)num_sms() * 16);
+    aabb_kernel<<<blocks, threads, 0, (cudaStream_t)stream>>>(ray_o, ray_d, n, x, t, hit);
+    return launch_status("nglod_aabb");
+}
+
+extern "C" int nglod_volume_sample(const float *grid, int32_t side, int32_t feature_dim, const float *x,
+                                   int64_t n, float *out, nglod_stream_t stream) {
+    NGLOD_REQUIRE(feature_dim == kC, NGLOD_ERR_UNSUPPORTED, "feature_dim=%d not built (only %d)", feature_dim, kC);
+    NGLOD_REQUIRE(side >= 2 && side <= 1025, NGLOD_ERR_INVALID, "side=%d outside [2, 1025]", side);
+    NGLOD_REQUIRE(n >= 0, NGLOD_ERR_INVALID, "n=%lld is negative", (long long)n);
+    if (n == 0) return NGLOD_OK;
+    NGLOD_REQUIRE(grid && x && out, NGLOD_ERR_INVALID, "null pointer argument");
+    NGLOD_REQUIRE(aligned(grid, 16) && aligned(out, 16), NGLOD_ERR_ALIGN, "grid and out must be 16-byte aligned");
+    const int threads = 256;
+    const int64_t want = (n + threads - 1) / threads;
+    const int64_t cap = resident_blocks(volume_sample_f32_kernel, threads, 0);
+    volume_sample_f32_kernel<<<(int)(want < cap ? want : cap), threads, 0, (cudaStream_t)stream>>>(grid, side, x, n,
+                                                                                                   out);
+    return launch_status("nglod_volume_sample");
+}
+
+extern "C" int nglod_sdf_fwd(const nglod_dense_model *model, const float *x, int64_t n, int32_t lod,
+                             int32_t all_lods, float *out, nglod_stream_t stream) {
+    NGLOD_REQUIRE(model != nullptr, NGLOD_ERR_INVALID, "model is null");
+    const int L = all_lods ? model->num_lods - 1 : resolve_lod(model, lod);
+    NGLOD_TRY(check_model(model, L));
+    NGLOD_REQUIRE(n >= 0, NGLOD_ERR_INVALID, "n=%lld is negative", (long long)n);
+    if (n == 0) return NGLOD_OK;
+    NGLOD_REQUIRE(x && out, NGLOD_ERR_INVALID, "null pointer argument");
+    const int threads = 256;
+    const int ndec = all_lods ? L + 1 : 1;
+    const size_t smem = (size_t)ndec * decoder_f4(model->hidden_dim) * sizeof(float4);
+    const int64_t want = (n + threads - 1) / threads;
+    if (all_lods) {
+        auto k = sdf_fwd_f32_kernel<true>;
+        NGLOD_TRY(prepare_smem(k, smem));
+        const int64_t cap = resident_blocks(k, threads, smem);
+        k<<<(int)(want < cap ? want : cap), threads, smem, (cudaStream_t)stream>>>(*model, x, n, L, out);
+    } else {
+        auto k = sdf_fwd_f32_kernel<false>;
+        NGLOD_TRY(prepare_smem(k, smem));
+        const int64_t cap = resident_blocks(k, threads, smem);
+        k<<<(int)(want < cap ? want : cap), threads, smem, (cudaStream_t)stream>>>(*model, x, n, L, out);
+    }
+    return launch_status("nglod_sdf_fwd");
+}
+
+extern "C" int nglod_trace(const nglod_dense_model *model, const nglod_trace_params *params, const float *ray_o,
+                           const float *ray_d, int64_t n, float *x, float *t, uint8_t *hit, float *normal,
+                           int64_t *work_counter, nglod_stream_t stream) {
+    NGLOD_REQUIRE(model != nullptr && params != nullptr, NGLOD_ERR_INVALID, "model or params is null");
+    const int L = resolve_lod(model, params->lod);
+    NGLOD_TRY(check_model(model, L));
+    NGLOD_REQUIRE(n >= 0, NGLOD_ERR_INVALID, "n=%lld is negative", (long long)n);
+    NGLOD_REQUIRE(params->num_steps >= 0, NGLOD_ERR_INVALID, "num_steps=%d is negative", params->num_steps);
+    if (n == 0) return NGLOD_OK;
+    NGLOD_REQUIRE(ray_o && ray_d && x && t && hit && work_counter, NGLOD_ERR_INVALID, "null pointer argument");
+    NGLOD_REQUIRE(normal || !params->want_normals, NGLOD_ERR_INVALID, "normals requested with a null buffer");
+    NGLOD_REQUIRE(aligned(work_counter, 8), NGLOD_ERR_ALIGN, "work_counter is not 8-byte aligned");
+    TraceArgs a;
+    a.m = *model;
+    a.p = *params;
+    a.L = L;
+    a.ray_o = ray_o;
+    a.ray_d = ray_d;
+    a.n = n;
+    a.x = x;
+    a.t = t;
+    a.hit = hit;
+    a.normal = normal;
+    a.counter = reinterpret_cast<unsigned long long *>(work_counter);
+    const int threads = 128;
+    const size_t smem = (size_t)decoder_f4(model->hidden_dim) * sizeof(float4);
+    NGLOD_TRY(prepare_smem(trace_f32_kernel, smem));
+    const int64_t want = (n + threads - 1) / threads;
+    const int64_t cap = resident_blocks(trace_f32_kernel, threads, smem);
+    NGLOD_TRY(cuda_status(cudaMemsetAsync(work_counter, 0, sizeof(int64_t), (cudaStream_t)stream),
+                          "nglod_trace counter reset"));
+    trace_f32_kernel<<<(int)(want < cap ? want : cap), threads, smem, (cudaStream_t)stream>>>(a);
+    return launch_status("nglod_trace");
+}

@@ -1,0 +1,232 @@
+"""Generates the golden fixtures in tests/golden/ by running the reference's own
+Python code (sdf-net/lib) on seeded synthetic inputs, on the CPU.
+
+    python tests/golden/make_golden.py [REFERENCE_ROOT]
+
+REFERENCE_ROOT defaults to /root/reference (the read-only checkout of
+nv-tlabs/nglod).  Modules the reference imports but the hot path does not use
+(mesh2sdf, polyscope, PIL, cv2, tinyobjloader) are stubbed; the CUDA-only
+``sol_nglod.aabb`` is replaced by the bit-exact C restatement in
+oracle/nglod_oracle.c, and ``PerfTimer`` (which creates CUDA events) by a
+no-op.  Everything else -- OctreeSDF.sdf, SphereTracer.forward,
+diffutils.gradient, autograd through grid_sample, spc3d.SPC3D,
+geoutils.unique_corners -- is the reference's code.
+
+Fixtures:
+  dense_small.npz  OctreeSDF(num_lods=3, base_lod=1, C=32, H=128, seed 0):
+                   sdf at every lod, lod=None, lod >= num_lods, return_lst;
+                   parameter gradients of the 3-LOD L2 training loss.
+  trace_small.npz  OctreeSDF(num_lods=2, base_lod=3) set to a sphere-union SDF
+                   plus noise; SphereTracer.forward on 40x40 camera rays and
+                   edge-case rays, lod None and 0.
+  spc_small.npz    SPC3D octree of level 5 built from the voxels near the
+                   sphere-union surface: Morton codes, octree bytes, pyramid,
+                   decoded points; unique_corners of levels 2..5.
+"""
+import os
+import sys
+import types
+
+import numpy as np
+import torch
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, REPO)
+
+from nglod_gb300 import synthetic  # noqa: E402
+from nglod_gb300.analytic_init import init_from_sdf  # noqa: E402
+from nglod_gb300.octree_sdf import OctreeSDF as DropIn  # noqa: E402
+from nglod_gb300.options import default_args  # noqa: E402
+from oracle import cref  # noqa: E402
+
+
+class _NoTimer:
+    def __init__(self, *a, **k):
+        pass
+
+    def check(self, *a, **k):
+        return None
+
+    def reset(self):
+        pass
+
+
+def _cpu_aabb(ray_o, ray_d):
+    x, t, hit = cref.aabb(ray_o.detach().float().numpy(), ray_d.detach().float().numpy())
+    dt = ray_o.dtype
+    return [torch.from_numpy(x).to(dt), torch.from_numpy(t).to(dt), torch.from_numpy(hit)]
+
+
+def import_reference(ref_root):
+    sys.path.insert(0, os.path.join(ref_root, "sdf-net"))
+    for name in ["mesh2sdf", "polyscope", "cv2", "tinyobjloader"]:
+        sys.modules.setdefault(name, types.ModuleType(name))
+    pil = types.ModuleType("PIL")
+    pil.Image = types.ModuleType("PIL.Image")
+    sys.modules["PIL"] = pil
+    sys.modules["PIL.Image"] = pil.Image
+    sol = types.ModuleType("sol_nglod")
+    sol.aabb = _cpu_aabb
+    sys.modules["sol_nglod"] = sol
+    import lib.utils
+    lib.utils.PerfTimer = _NoTimer
+    from lib.models.OctreeSDF import OctreeSDF
+    import lib.tracer.SphereTracer  # noqa: F401
+    ST = sys.modules["lib.tracer.SphereTracer"]
+    ST.PerfTimer = _NoTimer
+    from lib.options import parse_options
+    from lib import spc3d, geoutils
+    return OctreeSDF, ST.SphereTracer, parse_options, spc3d, geoutils
+
+
+def ref_args(parse_options, **kw):
+    argv = ["--net", "OctreeSDF"]
+    for k, v in kw.items():
+        flag = "--" + k.replace("_", "-")
+        if isinstance(v, bool):
+            if v:
+                argv.append(flag)
+        elif isinstance(v, (list, tuple)):
+            argv += [flag] + [str(u) for u in v]
+        else:
+            argv += [flag, str(v)]
+    return parse_options(return_parser=True).parse_args(argv)
+
+
+def dense_small(OctreeSDF, parse_options):
+    args = ref_args(parse_options, num_lods=3, base_lod=1, feature_dim=32, hidden_dim=128)
+    torch.manual_seed(0)
+    net = OctreeSDF(args)
+    g = torch.Generator().manual_seed(11)
+    pts = torch.rand((600, 3), generator=g) * 2.2 - 1.1
+    special = torch.tensor([[-1, -1, -1], [1, 1, 1], [0, 0, 0], [1, -1, 0.5], [-1.5, 0.25, 2.0],
+                            [0.5, 0.5, 0.5], [-0.5, 1.0, -0.25], [0.999999, -0.999999, 1e-7]], dtype=torch.float32)
+    pts = torch.cat([pts, special])
+    out = {"points": pts.numpy()}
+    net.eval()
+    with torch.no_grad():
+        for lod in [0, 1, 2]:
+            out[f"sdf_lod{lod}"] = net.sdf(pts, lod=lod).numpy()
+        out["sdf_lodNone"] = net.sdf(pts).numpy()
+        out["sdf_lod7"] = net.sdf(pts, lod=7).numpy()
+        out["sdf_lst"] = np.stack([t.numpy() for t in net.sdf(pts, return_lst=True)])
+        net.lod = 1
+        out["forward_lod1"] = net(pts).numpy()
+        net.lod = None
+    for k, v in net.state_dict().items():
+        out["param/" + k] = v.numpy()
+    # Training loss of Trainer.step_geometry (trainer.py:317-339) over all LODs.
+    c, r = synthetic.sphere_union(1)
+    gts = torch.from_numpy(synthetic.sphere_union_sdf(pts.numpy(), c, r)).float()[:, None]
+    net.train()
+    net.zero_grad()
+    loss = 0
+    for lod in [0, 1, 2]:
+        loss = loss + ((net.sdf(pts, lod=lod) - gts) ** 2).sum()
+    loss = loss / pts.shape[0]
+    loss.backward()
+    out["train/gts"] = gts.numpy()
+    out["train/loss"] = np.array(loss.item())
+    for k, p in net.named_parameters():
+        out["grad/" + k] = p.grad.numpy()
+    np.savez_compressed(os.path.join(HERE, "dense_small.npz"), **out)
+
+
+def trace_small(OctreeSDF, SphereTracer, parse_options):
+    args = ref_args(parse_options, num_lods=2, base_lod=3, feature_dim=32, hidden_dim=128, num_steps=64,
+                    min_dis=0.0003, step_size=1.0, camera_clamp=[-5, 10], grad_method="finitediff")
+    c, r = synthetic.sphere_union(1)
+    torch.manual_seed(0)
+    dropin = DropIn(default_args(num_lods=2, base_lod=3))
+    init_from_sdf(dropin, lambda p: torch.from_numpy(synthetic.sphere_union_sdf(p.numpy(), c, r)), noise=2e-3,
+                  seed=5)
+    with torch.no_grad():
+        for fv in dropin.features:  # keep the fixture small: noise in channels 1-3 only
+            fv.fm[:, 4:] = 0
+    net = OctreeSDF(args)
+    net.load_state_dict(dropin.state_dict())
+    net.eval()
+    ro, rd = synthetic.look_at_rays(width=40, height=40)
+    extra_o = torch.tensor([[0, 0, 0], [0.5, 0.2, -0.3], [3, 3, 3], [0, 0, 4], [1, 0, 0], [0, 2, 0],
+                            [-0.2, 0.1, 1.0]], dtype=torch.float32)
+    extra_d = torch.tensor([[1, 0, 0], [0, 0, 1], [1, 0, 0], [0, 0, -1], [-1, 0, 0], [0, -1, 0],
+                            [0, 0, -1]], dtype=torch.float32)
+    ro = torch.cat([ro, extra_o])
+    rd = torch.cat([rd, extra_d])
+    out = {"ray_o": ro.numpy(), "ray_d": rd.numpy()}
+    tracer = SphereTracer(args)
+    for name, lod in [("lodNone", None), ("lod0", 0)]:
+        net.lod = lod
+        rb = tracer(net, ro, rd)
+        out[f"{name}/x"] = rb.x.detach().numpy()
+        out[f"{name}/depth"] = rb.depth.detach().numpy()
+        out[f"{name}/hit"] = rb.hit.numpy()
+        out[f"{name}/normal"] = rb.normal.detach().numpy()
+    net.lod = None
+    for k, v in net.state_dict().items():
+        out["param/" + k] = v.numpy()
+    out["trace/num_steps"] = np.array(64)
+    np.savez_compressed(os.path.join(HERE, "trace_small.npz"), **out)
+
+
+def coded_volume(s, channels=2):
+    c = torch.arange(channels, dtype=torch.float64).view(channels, 1, 1, 1)
+    z = torch.arange(s, dtype=torch.float64).view(1, s, 1, 1)
+    y = torch.arange(s, dtype=torch.float64).view(1, 1, s, 1)
+    x = torch.arange(s, dtype=torch.float64).view(1, 1, 1, s)
+    return (c * 1e6 + z * 1e4 + y * 1e2 + x)[None]
+
+
+def spc_small(spc3d, geoutils):
+    level = 5
+    res = 2 ** level
+    c, r = synthetic.sphere_union(1)
+    idx = np.stack(np.meshgrid(np.arange(res), np.arange(res), np.arange(res), indexing="ij"), -1).reshape(-1, 3)
+    centres = (idx + 0.5) / res * 2 - 1
+    keep = np.abs(synthetic.sphere_union_sdf(centres, c, r)) <= np.sqrt(3) * (2.0 / res)
+    vox = idx[keep].astype(np.uint16)
+    spc = spc3d.SPC3D(level)
+    for i in range(vox.shape[0]):
+        spc.mdata[i] = spc3d.to_morton(vox[i])
+        spc.psize += 1
+    spc.mdata[:spc.psize] = np.sort(spc.mdata[:spc.psize])
+    morton = spc.mdata[:spc.psize].copy()
+    spc.morton_to_point(spc.psize, spc.mdata, spc.pdata)
+    points_sorted = spc.pdata[:spc.psize].copy()
+    osize = spc.points_to_nodes()
+    octree = spc.oroot[:osize].copy()
+    pyramid = spc.pyramid[:level + 1].copy()
+    pyramid_sum = spc.pyramid_sum[:level + 1].copy()
+    dec = spc3d.SPC3D(level, nodebytes=octree.copy())
+    npts = dec.nodes_to_points()
+    out = {"voxels": vox, "morton": morton, "points_sorted": points_sorted, "octree": octree,
+           "pyramid": pyramid, "pyramid_sum": pyramid_sum, "decoded_leaf_points": dec.pdata[:npts].copy(),
+           "decoded_pyramid": dec.pyramid[:level + 1].copy(), "level": np.array(level)}
+    # unique_corners of each octree level's voxels (geoutils.py:60-77).  The
+    # feature volume encodes its own index, fm[0, c, z, y, x] =
+    # c*1e6 + z*1e4 + y*1e2 + x, so cf pins the gather order exactly.
+    for lv in range(2, level + 1):
+        shift = level - lv
+        vs = torch.unique(torch.from_numpy(points_sorted.astype(np.int64)) >> shift, dim=0)
+        out[f"corners/{lv}/voxels"] = vs.numpy()
+        corners, feats = geoutils.unique_corners(vs, coded_volume(2 ** lv + 1))
+        out[f"corners/{lv}/cc"] = corners.numpy()
+        out[f"corners/{lv}/cf"] = feats.numpy()
+    np.savez_compressed(os.path.join(HERE, "spc_small.npz"), **out)
+
+
+def main():
+    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    OctreeSDF, SphereTracer, parse_options, spc3d, geoutils = import_reference(ref_root)
+    torch.set_num_threads(max(1, os.cpu_count() or 1))
+    dense_small(OctreeSDF, parse_options)
+    trace_small(OctreeSDF, SphereTracer, parse_options)
+    spc_small(spc3d, geoutils)
+    for f in sorted(os.listdir(HERE)):
+        if f.endswith(".npz"):
+            print(f, os.path.getsize(os.path.join(HERE, f)))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,90 @@
+"""The C-ABI library loads, exports every entry point include/nglod_gb300.h
+declares, and its structs match the ctypes mirrors.  No CUDA work is issued:
+only argument-validation paths that return before touching the device."""
+import ctypes
+import os
+import re
+import subprocess
+
+import pytest
+
+from tests.conftest import ROOT
+
+HEADER = os.path.join(ROOT, "include", "nglod_gb300.h")
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(nglod_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_header_declares_entry_points():
+    names = declared_functions()
+    for required in ["nglod_aabb", "nglod_sdf_fwd", "nglod_trace", "nglod_volume_sample", "nglod_last_error"]:
+        assert required in names
+
+
+def test_library_exports_every_declared_symbol(built_library):
+    lib = ctypes.CDLL(built_library)
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, missing
+    from nglod_gb300 import _lib
+    assert set(_lib.SIGNATURES) <= set(declared_functions())
+    assert set(declared_functions()) <= set(_lib.SIGNATURES), "every declared symbol has a Python binding"
+
+
+def _c_layout(tmp_path, structs):
+    src = tmp_path / "layout.c"
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "nglod_gb300.h"', "int main(void) {"]
+    for s, fields in structs.items():
+        lines.append(f'printf("{s} %zu\\n", sizeof({s}));')
+        for f in fields:
+            lines.append(f'printf("{s}.{f} %zu\\n", offsetof({s}, {f}));')
+    lines.append("return 0; }")
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout
+    return {k: int(v) for k, v in (ln.split() for ln in out.strip().splitlines())}
+
+
+def test_struct_layouts_match_ctypes(tmp_path):
+    from nglod_gb300 import _lib
+    mirrors = {"nglod_dense_model": _lib.DenseModel, "nglod_trace_params": _lib.TraceParams}
+    mirrors.update({k: v for k, v in _lib.STRUCTS.items()} if hasattr(_lib, "STRUCTS") else {})
+    structs = {name: [f[0] for f in cls._fields_] for name, cls in mirrors.items()}
+    lay = _c_layout(tmp_path, structs)
+    for name, cls in mirrors.items():
+        assert lay[name] == ctypes.sizeof(cls), name
+        for f in cls._fields_:
+            assert lay[f"{name}.{f[0]}"] == getattr(cls, f[0]).offset, (name, f[0])
+
+
+def test_validation_errors_without_device(built_library):
+    from nglod_gb300 import _lib
+    lib = _lib.load()
+    assert lib.nglod_sdf_fwd(None, None, 0, 0, 0, None, None) == -1
+    assert b"model is null" in lib.nglod_last_error()
+    m = _lib.DenseModel()
+    m.num_lods, m.base_lod, m.feature_dim, m.hidden_dim = 2, 2, 16, 128
+    assert lib.nglod_sdf_fwd(m, None, 0, 0, 0, None, None) == -2
+    assert b"feature_dim=16" in lib.nglod_last_error()
+    m.feature_dim = 32
+    assert lib.nglod_sdf_fwd(m, None, 0, 0, 0, None, None) == -1  # null volume pointers
+    assert lib.nglod_aabb(None, None, 0, None, None, None, None) == 0  # empty input: no work
+    assert lib.nglod_aabb(None, None, -1, None, None, None, None) == -1
+    assert lib.nglod_trace(None, None, None, None, 0, None, None, None, None, None, None) == -1
+    p = _lib.TraceParams()
+    p.num_steps = -1
+    m.grid[0] = m.grid[1] = 256
+    for k in ("w0", "b0", "w1", "b1"):
+        getattr(m, k)[0] = getattr(m, k)[1] = 256
+    assert lib.nglod_trace(m, p, None, None, 0, None, None, None, None, None, None) == -1
+    assert b"num_steps" in lib.nglod_last_error()
+
+
+def test_python_shim_raises_on_status():
+    from nglod_gb300 import _lib
+    with pytest.raises(RuntimeError, match="invalid argument"):
+        _lib.check(_lib.load().nglod_aabb(None, None, -5, None, None, None, None), "nglod_aabb")

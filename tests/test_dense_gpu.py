@@ -1,0 +1,163 @@
+"""Parity of the dense float32 CUDA path with the oracle and the reference's
+golden vectors.  Tolerances follow the spec bar: 1e-5 abs on SDF
+values, 1e-4 on depth of hit rays, >= 99.99 % hit-mask agreement."""
+import numpy as np
+import pytest
+import torch
+import torch.nn.functional as F
+
+import nglod_gb300 as ng
+from nglod_gb300 import synthetic
+from nglod_gb300.analytic_init import init_from_sdf
+from nglod_gb300.options import default_args
+from oracle import cref, dense
+from tests.helpers import model_from_fixture, oracle_model, seeded_model
+
+pytestmark = pytest.mark.gpu
+
+SDF_TOL = 1e-5
+DEPTH_TOL = 1e-4
+
+
+def _rays(n, seed):
+    rng = np.random.default_rng(seed)
+    o = rng.uniform(-3, 3, (n, 3)).astype(np.float32)
+    d = rng.normal(size=(n, 3)).astype(np.float32)
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    d[:64, 1] = 0.0
+    d[64:96, :2] = 0.0
+    o[96:160] = rng.uniform(-0.9, 0.9, (64, 3))
+    o[160:200, 0] = 1.0
+    return o, d
+
+
+def test_aabb_bit_exact(cuda):
+    o, d = _rays(200_000, 1)
+    x, t, hit = ng.sol_nglod.aabb(torch.from_numpy(o).to(cuda), torch.from_numpy(d).to(cuda))
+    xo, to, ho = cref.aabb(o, d)
+    assert np.array_equal(hit.cpu().numpy(), ho)
+    assert np.array_equal(t.cpu().numpy().view(np.uint32), to.view(np.uint32))
+    assert np.array_equal(x.cpu().numpy().view(np.uint32), xo.view(np.uint32))
+
+
+def test_volume_sample_matches_grid_sample(cuda):
+    net = seeded_model(num_lods=3, seed=2).to(cuda)
+    x = torch.rand(50_000, 3, device=cuda) * 2.4 - 1.2
+    for fv in net.features:
+        got = fv(x)
+        ref = F.grid_sample(fv.fm.detach().double(), x.double().reshape(1, -1, 1, 1, 3), align_corners=True,
+                            padding_mode="border")[0, :, :, 0, 0].T
+        assert (got.double() - ref).abs().max().item() < 1e-6
+
+
+def test_sdf_matches_reference_golden(golden, cuda):
+    fx = golden("dense_small")
+    net = model_from_fixture(fx, 3, 1, device=cuda)
+    x = torch.from_numpy(fx["points"]).to(cuda)
+    with torch.no_grad():
+        for lod in [0, 1, 2]:
+            np.testing.assert_allclose(net.sdf(x, lod=lod).cpu().numpy(), fx[f"sdf_lod{lod}"], atol=SDF_TOL, rtol=0)
+        np.testing.assert_allclose(net.sdf(x).cpu().numpy(), fx["sdf_lodNone"], atol=SDF_TOL, rtol=0)
+        np.testing.assert_allclose(net.sdf(x, lod=7).cpu().numpy(), fx["sdf_lod7"], atol=SDF_TOL, rtol=0)
+        lst = net.sdf(x, return_lst=True)
+        np.testing.assert_allclose(torch.stack(lst).cpu().numpy(), fx["sdf_lst"], atol=SDF_TOL, rtol=0)
+        net.lod = 1
+        np.testing.assert_allclose(net(x, lod=0).cpu().numpy(), fx["forward_lod1"], atol=SDF_TOL, rtol=0)
+
+
+def test_sdf_full_architecture_vs_fp64_oracle(cuda):
+    """Config: 5 LODs (5^3..65^3), C=32, H=128, seed 0, 262,144 points U[-1,1]^3."""
+    net = seeded_model(num_lods=5, base_lod=2, seed=0).to(cuda)
+    x = synthetic.uniform_points(262_144, seed=0)
+    m = oracle_model(net.cpu(), np.float64)
+    net = net.to(cuda)
+    with torch.no_grad():
+        got = net.sdf(x.to(cuda), lod=4).cpu().numpy()
+    ref = dense.sdf(m, x.numpy(), lod=4)
+    assert np.abs(got - ref).max() < SDF_TOL
+    sub = x[:8192]
+    with torch.no_grad():
+        lst = [t.cpu().numpy() for t in net.sdf(sub.to(cuda), return_lst=True)]
+    ref_lst = dense.sdf(m, sub.numpy(), return_lst=True)
+    for lod in range(5):
+        assert np.abs(lst[lod] - ref_lst[lod]).max() < SDF_TOL
+
+
+def test_sdf_training_mode_keeps_loss_preds(cuda):
+    net = seeded_model(num_lods=3, seed=4).to(cuda)
+    net.train()
+    x = torch.rand(1000, 3, device=cuda) * 2 - 1
+    with torch.no_grad():
+        out = net.sdf(x)
+        assert isinstance(net.loss_preds, list) and len(net.loss_preds) == 3
+        assert torch.equal(out, net.loss_preds[-1])
+        net.loss_preds = None
+        net.sdf(x, lod=1)
+        assert net.loss_preds is None
+
+
+def test_empty_and_ragged_inputs(cuda):
+    net = seeded_model(num_lods=2, seed=1).to(cuda)
+    with torch.no_grad():
+        assert net.sdf(torch.zeros(0, 3, device=cuda)).shape == (0, 1)
+        for n in [1, 31, 33, 257, 1023]:
+            x = torch.rand(n, 3, device=cuda) * 2 - 1
+            got = net.sdf(x).cpu().numpy()
+            ref = dense.sdf(oracle_model(net.cpu()), x.cpu().numpy())
+            net.to(cuda)
+            assert np.abs(got - ref).max() < SDF_TOL
+    rb = ng.SphereTracer(default_args(num_steps=16))(net, torch.zeros(0, 3, device=cuda), torch.zeros(0, 3, device=cuda))
+    assert rb.x.shape == (0, 3)
+
+
+def _check_trace(rb, x, t, hit, normal):
+    h = rb.hit.cpu().numpy()
+    assert (h == hit).mean() >= 0.9999
+    both = h & hit
+    tt = rb.depth.cpu().numpy()
+    np.testing.assert_allclose(tt[both], t[both], atol=DEPTH_TOL, rtol=0)
+    np.testing.assert_allclose(tt[~both], t[~both], atol=DEPTH_TOL, rtol=1e-4)
+    np.testing.assert_allclose(rb.normal.cpu().numpy()[both], normal[both], atol=1e-3, rtol=0)
+    assert (rb.normal.cpu().numpy()[~h] == 0).all()
+
+
+@pytest.mark.parametrize("name,lod", [("lodNone", None), ("lod0", 0)])
+@pytest.mark.parametrize("tracer_cls", [ng.SphereTracer, ng.PlainSphereTracer])
+def test_trace_matches_reference_golden(golden, cuda, name, lod, tracer_cls):
+    fx = golden("trace_small")
+    net = model_from_fixture(fx, 2, 3, device=cuda)
+    net.lod = lod
+    tracer = tracer_cls(default_args(num_steps=int(fx["trace/num_steps"])))
+    rb = tracer(net, torch.from_numpy(fx["ray_o"]).to(cuda), torch.from_numpy(fx["ray_d"]).to(cuda))
+    _check_trace(rb, None, fx[f"{name}/depth"], fx[f"{name}/hit"], fx[f"{name}/normal"])
+    assert rb.hit[-7].item() and rb.depth[-7, 0].item() == 0.0
+
+
+def test_trace_full_model_vs_oracle(cuda):
+    """5-LOD network holding the seed-1 sphere union; 96x96 camera, 128 steps."""
+    c, r = synthetic.sphere_union(1)
+    torch.manual_seed(0)
+    net = ng.OctreeSDF(default_args(num_lods=5, base_lod=2))
+    init_from_sdf(net, lambda p: torch.from_numpy(synthetic.sphere_union_sdf(p.numpy(), c, r)), noise=1e-3, seed=2)
+    m = oracle_model(net, np.float32)
+    net = net.to(cuda).eval()
+    ro, rd = synthetic.look_at_rays(width=96, height=96)
+    rb = ng.SphereTracer(default_args(num_steps=128))(net, ro.to(cuda), rd.to(cuda))
+    x, t, hit, normal = dense.sphere_trace(m, ro.numpy(), rd.numpy(), num_steps=128, aabb_fn=cref.aabb)
+    assert hit.sum() > 1000
+    _check_trace(rb, x, t, hit, normal)
+    both = rb.hit.cpu().numpy() & hit
+    assert np.abs(rb.x.cpu().numpy()[both] - x[both]).max() < DEPTH_TOL
+
+
+def test_trace_matches_plain_tracer_at_scale(cuda):
+    c, r = synthetic.sphere_union(1)
+    torch.manual_seed(0)
+    net = ng.OctreeSDF(default_args(num_lods=5, base_lod=2))
+    init_from_sdf(net, lambda p: torch.from_numpy(synthetic.sphere_union_sdf(p.numpy(), c, r)), noise=1e-3, seed=2)
+    net = net.to(cuda).eval()
+    ro, rd = synthetic.look_at_rays(width=640, height=360)
+    a = default_args(num_steps=64)
+    fused = ng.SphereTracer(a)(net, ro.to(cuda), rd.to(cuda))
+    plain = ng.PlainSphereTracer(a)(net, ro.to(cuda), rd.to(cuda))
+    _check_trace(fused, None, plain.depth.cpu().numpy(), plain.hit.cpu().numpy(), plain.normal.cpu().numpy())
