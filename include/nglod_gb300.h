@@ -108,6 +108,61 @@ int nglod_trace(const nglod_dense_model *model, const nglod_trace_params *params
                 float *x, float *t, uint8_t *hit, float *normal,
                 int64_t *work_counter, nglod_stream_t stream);
 
+/* ------------------------------------------------------------------------
+ * Training: forward with saved features, hand-written backward, Adam.
+ * ------------------------------------------------------------------------ */
+
+/* Gradient buffers of a dense model, same layouts as the parameters
+ * (volumes channel-last).  Backward ADDS into them, as autograd accumulates
+ * into .grad; callers zero them first. */
+typedef struct nglod_dense_grads {
+    float *grid[NGLOD_MAX_LODS];
+    float *w0[NGLOD_MAX_LODS];
+    float *b0[NGLOD_MAX_LODS];
+    float *w1[NGLOD_MAX_LODS];
+    float *b1[NGLOD_MAX_LODS];
+} nglod_dense_grads;
+
+/* Forward of the LODs in lod_mask (bit l = LOD l) for training.  With
+ * L = highest set bit: preds[l][n] and feats[l][n][C] (the running feature
+ * sum that decoder l reads) are written for every l in the mask.  Same
+ * predictions as OctreeSDF.sdf(x, lod=l) for each l in the mask
+ * (OctreeSDF.py:94-146); with all bits set, as sdf(x, return_lst=True). */
+int nglod_sdf_fwd_train(const nglod_dense_model *model, const float *x, int64_t n, uint32_t lod_mask,
+                        float *preds, float *feats, nglod_stream_t stream);
+
+/* Backward of nglod_sdf_fwd_train.  grad_preds[l][n] = dLoss/dpred_l for l in
+ * lod_mask.  Adds the parameter gradients into `grads` and, when grad_x is
+ * not NULL, dLoss/dx into grad_x[n][3].  dfeat_scratch[L+1][n][C] is caller-
+ * provided scratch.  Replaces the autograd backward of OctreeSDF.sdf through
+ * nn.Linear and F.grid_sample (border padding, align_corners) that
+ * Trainer.step_geometry runs (sdf-net/lib/trainer.py:339): decoder weight
+ * gradients are per-block tile reductions, feature gradients a trilinear
+ * scatter-add (coarse volumes accumulated in shared memory, the rest with
+ * vector atomics). */
+int nglod_sdf_bwd(const nglod_dense_model *model, const float *x, int64_t n, uint32_t lod_mask,
+                  const float *grad_preds, const float *feats, float *dfeat_scratch,
+                  const nglod_dense_grads *grads, float *grad_x, nglod_stream_t stream);
+
+/* One tensor of a multi-tensor Adam step (device-resident table). */
+typedef struct nglod_adam_tensor {
+    float       *param;
+    const float *grad;
+    float       *exp_avg;
+    float       *exp_avg_sq;
+    int64_t      numel;
+} nglod_adam_tensor;
+
+/* Adam update of `count` tensors described by the device table `tensors`,
+ * step = the step number after increment (1 for the first step).  Same
+ * update order as torch.optim.Adam's single-tensor path with amsgrad=False,
+ * maximize=False (the optimizer of sdf-net/lib/trainer.py:184-185):
+ * m = lerp(m, g, 1-beta1); v = v*beta2 + (1-beta2)*g*g;
+ * p -= lr/(1-beta1^step) * m / (sqrt(v)/sqrt(1-beta2^step) + eps).
+ * weight_decay adds weight_decay*p to g first (0 in the reference). */
+int nglod_adam_step(const nglod_adam_tensor *tensors, int32_t count, int64_t max_numel, float lr, float beta1,
+                    float beta2, float eps, float weight_decay, int64_t step, nglod_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -11,10 +11,10 @@ all backed by the C-ABI library ``nglod_gb300/_build/libnglod_gb300.so``
 (include/nglod_gb300.h).  There is no CPU fallback: calls with CPU tensors or
 without the built library raise RuntimeError.
 """
-from . import sol_nglod
+from . import autograd, sol_nglod, trainer
 from ._lib import load as load_library
 from .octree_sdf import FeatureVolume, OctreeSDF, setparam
 from .tracer import BaseTracer, PlainSphereTracer, RenderBuffer, SphereTracer
 
 __all__ = ["OctreeSDF", "FeatureVolume", "SphereTracer", "PlainSphereTracer", "BaseTracer", "RenderBuffer",
-           "sol_nglod", "setparam", "load_library"]
+           "sol_nglod", "setparam", "load_library", "trainer", "autograd"]

@@ -58,6 +58,26 @@ class TraceParams(ctypes.Structure):
     ]
 
 
+class DenseGrads(ctypes.Structure):
+    _fields_ = [
+        ("grid", _vp * MAX_LODS),
+        ("w0", _vp * MAX_LODS),
+        ("b0", _vp * MAX_LODS),
+        ("w1", _vp * MAX_LODS),
+        ("b1", _vp * MAX_LODS),
+    ]
+
+
+class AdamTensor(ctypes.Structure):
+    _fields_ = [("param", _vp), ("grad", _vp), ("exp_avg", _vp), ("exp_avg_sq", _vp), ("numel", _i64)]
+
+
+# C struct name -> ctypes mirror (layouts are checked against the header by tests/test_abi.py)
+STRUCTS = {"nglod_dense_grads": DenseGrads, "nglod_adam_tensor": AdamTensor}
+
+_u32 = ctypes.c_uint32
+_f32 = ctypes.c_float
+
 # name -> (restype, argtypes)
 SIGNATURES = {
     "nglod_version": (ctypes.c_char_p, []),
@@ -67,6 +87,10 @@ SIGNATURES = {
     "nglod_sdf_fwd": (ctypes.c_int, [ctypes.POINTER(DenseModel), _vp, _i64, _i32, _i32, _vp, _vp]),
     "nglod_trace": (ctypes.c_int, [ctypes.POINTER(DenseModel), ctypes.POINTER(TraceParams), _vp, _vp, _i64,
                                    _vp, _vp, _vp, _vp, _vp, _vp]),
+    "nglod_sdf_fwd_train": (ctypes.c_int, [ctypes.POINTER(DenseModel), _vp, _i64, _u32, _vp, _vp, _vp]),
+    "nglod_sdf_bwd": (ctypes.c_int, [ctypes.POINTER(DenseModel), _vp, _i64, _u32, _vp, _vp, _vp,
+                                     ctypes.POINTER(DenseGrads), _vp, _vp]),
+    "nglod_adam_step": (ctypes.c_int, [_vp, _i32, _i64, _f32, _f32, _f32, _f32, _f32, _i64, _vp]),
 }
 
 _LIB = None

@@ -1,0 +1,101 @@
+"""torch.autograd.Function over the hand-written training kernels.
+
+``sdf_train(net, x, lod, all_lods)`` is what ``OctreeSDF.sdf`` calls when
+autograd needs gradients: forward ``nglod_sdf_fwd_train`` saves the per-LOD
+feature sums, backward ``nglod_sdf_bwd`` produces the gradients of every
+volume and decoder that the requested predictions depend on (and of x when x
+requires grad), replacing autograd through F.grid_sample and nn.Linear
+(sdf-net/lib/models/OctreeSDF.py:94-155).
+"""
+import torch
+
+from . import _lib
+from .octree_sdf import CL3D, _as_cl3d
+
+
+def _model_from_params(net, fms, decs):
+    m = _lib.DenseModel()
+    m.num_lods = net.num_lods
+    m.base_lod = net.base_lod
+    m.feature_dim = net.fdim
+    m.hidden_dim = net.hidden_dim
+    m.grid_dtype = _lib.F32
+    for i, fm in enumerate(fms):
+        m.grid[i] = fm.data_ptr()
+    for i, (w0, b0, w1, b1) in enumerate(decs):
+        m.w0[i], m.b0[i], m.w1[i], m.b1[i] = w0.data_ptr(), b0.data_ptr(), w1.data_ptr(), b1.data_ptr()
+    return m
+
+
+class _SdfTrain(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, x, mask, net, *params):
+        nl = net.num_lods
+        L = mask.bit_length() - 1
+        fms = [_as_cl3d(p.detach()) for p in params[:nl]]
+        decs = [tuple(p.detach().contiguous() for p in params[nl + 4 * i: nl + 4 * i + 4]) for i in range(nl)]
+        xd = x.detach().float().contiguous()
+        n = xd.shape[0]
+        dev = xd.device
+        preds = torch.zeros(L + 1, n, 1, device=dev, dtype=torch.float32)
+        feats = torch.empty(L + 1, n, net.fdim, device=dev, dtype=torch.float32)
+        m = _model_from_params(net, fms, decs)
+        _lib.check(_lib.load().nglod_sdf_fwd_train(m, _lib.ptr(xd), n, mask, _lib.ptr(preds), _lib.ptr(feats),
+                                                   _lib.stream_ptr(dev)), "nglod_sdf_fwd_train")
+        ctx.save_for_backward(xd, feats, *fms, *[p for d in decs for p in d])
+        ctx.mask = mask
+        ctx.net = net
+        ctx.L = L
+        ctx.x_needs_grad = x.requires_grad
+        return preds
+
+    @staticmethod
+    def backward(ctx, grad_preds):
+        net = ctx.net
+        nl = net.num_lods
+        L = ctx.L
+        saved = ctx.saved_tensors
+        xd, feats = saved[0], saved[1]
+        fms = saved[2:2 + nl]
+        flat = saved[2 + nl:]
+        decs = [tuple(flat[4 * i: 4 * i + 4]) for i in range(nl)]
+        n = xd.shape[0]
+        dev = xd.device
+        gp = grad_preds.detach().float().contiguous()
+        m = _model_from_params(net, fms, decs)
+        g = _lib.DenseGrads()
+        gfm = [None] * nl
+        gdec = [[None] * 4 for _ in range(nl)]
+        for i in range(L + 1):
+            gfm[i] = torch.zeros_like(fms[i], memory_format=CL3D)
+            g.grid[i] = gfm[i].data_ptr()
+            if (ctx.mask >> i) & 1:
+                gdec[i] = [torch.zeros_like(p) for p in decs[i]]
+                g.w0[i], g.b0[i], g.w1[i], g.b1[i] = [t.data_ptr() for t in gdec[i]]
+        dfeat = torch.empty_like(feats)
+        gx = torch.zeros(n, 3, device=dev, dtype=torch.float32) if ctx.x_needs_grad else None
+        _lib.check(_lib.load().nglod_sdf_bwd(m, _lib.ptr(xd), n, ctx.mask, _lib.ptr(gp), _lib.ptr(feats),
+                                             _lib.ptr(dfeat), g, _lib.ptr(gx), _lib.stream_ptr(dev)), "nglod_sdf_bwd")
+        out = [gx, None, None] + gfm + [t for d in gdec for t in d]
+        return tuple(out)
+
+
+def train_params(net):
+    ps = [fv.fm for fv in net.features]
+    for dec in net.louts:
+        ps += [dec[0].weight, dec[0].bias, dec[2].weight, dec[2].bias]
+    return ps
+
+
+def sdf_train(net, x, lod, all_lods):
+    """Differentiable predictions: [N, 1] at `lod` (finest if None), or the
+    list of every LOD's [N, 1] when all_lods."""
+    _lib.require_cuda(x, net.features[0].fm)
+    if x.dim() != 2 or x.shape[1] != 3:
+        raise NotImplementedError("OctreeSDF.sdf: only [N, 3] query points are supported")
+    L = net.num_lods - 1 if lod is None else lod
+    mask = ((1 << (L + 1)) - 1) if all_lods else (1 << L)
+    preds = _SdfTrain.apply(x, mask, net, *train_params(net))
+    if all_lods:
+        return [preds[i] for i in range(L + 1)]
+    return preds[L]

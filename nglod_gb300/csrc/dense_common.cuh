@@ -1,0 +1,205 @@
+// Device building blocks of the dense float32 path shared by the forward,
+// tracer and training kernels.
+//
+// Layout: feature volume l is channel-last [s][s][s][C] (C = 32 floats =
+// 128 B per vertex), so each trilinear corner is eight 16-byte loads of one
+// cache line.  The decoder of one LOD is staged in shared memory as H rows of
+// 36 floats (35 weights of Linear(35, H) followed by its bias; the input
+// vector carries a trailing 1.0) plus the H weights and the bias of
+// Linear(H, 1).  Every thread evaluates whole points, reading the decoder
+// rows as warp-wide broadcasts.
+#pragma once
+
+#include <math.h>
+
+#include "common.cuh"
+
+namespace nglod {
+
+constexpr int kC = 32;         // feature channels this library is built for
+constexpr int kRowF4 = 9;      // float4 per staged decoder row (35 weights + bias)
+
+// float4 count of one staged decoder with H hidden units.
+__host__ __device__ inline int decoder_f4(int H) { return H * kRowF4 + (H + 4) / 4; }
+
+__device__ __forceinline__ void stage_decoder(float4 *dst, const nglod_dense_model &m, int l) {
+    const int H = m.hidden_dim;
+    float *rows = reinterpret_cast<float *>(dst);
+    const float *__restrict__ w0 = m.w0[l];
+    const float *__restrict__ b0 = m.b0[l];
+    for (int i = threadIdx.x; i < H * 36; i += blockDim.x) {
+        const int j = i / 36, k = i - j * 36;
+        rows[i] = k < 35 ? w0[j * 35 + k] : b0[j];
+    }
+    float *w1s = rows + H * 36;
+    for (int j = threadIdx.x; j < H; j += blockDim.x) w1s[j] = m.w1[l][j];
+    if (threadIdx.x == 0) w1s[H] = m.b1[l][0];
+}
+
+// Adds the trilinear sample of one channel-last float32 volume (s vertices per
+// side) at point p to f.  Same arithmetic as PyTorch's 3-D grid sampler with
+// align_corners=True and padding_mode='border': u = ((p + 1) / 2) * (s - 1)
+// clamped to [0, s - 1], corner weights are products of distances to the
+// opposite corner, corners summed in tnw, tne, tsw, tse, bnw, bne, bsw, bse
+// order.  The far corner index is clamped to s - 1 where u = s - 1; its weight
+// is then exactly 0, as when PyTorch skips the out-of-range corner.
+__device__ __forceinline__ void gather_add_f32(const float *__restrict__ g, int s, float px, float py,
+                                               float pz, float (&f)[kC]) {
+    const float sm1 = (float)(s - 1);
+    float ix = ((px + 1.f) / 2.f) * sm1;
+    float iy = ((py + 1.f) / 2.f) * sm1;
+    float iz = ((pz + 1.f) / 2.f) * sm1;
+    ix = fminf(sm1, fmaxf(ix, 0.f));
+    iy = fminf(sm1, fmaxf(iy, 0.f));
+    iz = fminf(sm1, fmaxf(iz, 0.f));
+    const float x0 = floorf(ix), y0 = floorf(iy), z0 = floorf(iz);
+    const float wx1 = ix - x0, wx0 = (x0 + 1.f) - ix;
+    const float wy1 = iy - y0, wy0 = (y0 + 1.f) - iy;
+    const float wz1 = iz - z0, wz0 = (z0 + 1.f) - iz;
+    const int xi = (int)x0, yi = (int)y0, zi = (int)z0;
+    const int xj = min(xi + 1, s - 1), yj = min(yi + 1, s - 1), zj = min(zi + 1, s - 1);
+    const size_t sy = (size_t)s * kC, sz = (size_t)s * sy;
+    const float4 *c[8];
+    c[0] = reinterpret_cast<const float4 *>(g + zi * sz + yi * sy + xi * kC);
+    c[1] = reinterpret_cast<const float4 *>(g + zi * sz + yi * sy + xj * kC);
+    c[2] = reinterpret_cast<const float4 *>(g + zi * sz + yj * sy + xi * kC);
+    c[3] = reinterpret_cast<const float4 *>(g + zi * sz + yj * sy + xj * kC);
+    c[4] = reinterpret_cast<const float4 *>(g + zj * sz + yi * sy + xi * kC);
+    c[5] = reinterpret_cast<const float4 *>(g + zj * sz + yi * sy + xj * kC);
+    c[6] = reinterpret_cast<const float4 *>(g + zj * sz + yj * sy + xi * kC);
+    c[7] = reinterpret_cast<const float4 *>(g + zj * sz + yj * sy + xj * kC);
+    float w[8];
+    w[0] = wx0 * wy0 * wz0;
+    w[1] = wx1 * wy0 * wz0;
+    w[2] = wx0 * wy1 * wz0;
+    w[3] = wx1 * wy1 * wz0;
+    w[4] = wx0 * wy0 * wz1;
+    w[5] = wx1 * wy0 * wz1;
+    w[6] = wx0 * wy1 * wz1;
+    w[7] = wx1 * wy1 * wz1;
+#pragma unroll
+    for (int q = 0; q < kC / 4; ++q) {
+        float4 v[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) v[k] = __ldg(c[k] + q);
+        float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            a0 = fmaf(v[k].x, w[k], a0);
+            a1 = fmaf(v[k].y, w[k], a1);
+            a2 = fmaf(v[k].z, w[k], a2);
+            a3 = fmaf(v[k].w, w[k], a3);
+        }
+        f[4 * q + 0] += a0;
+        f[4 * q + 1] += a1;
+        f[4 * q + 2] += a2;
+        f[4 * q + 3] += a3;
+    }
+}
+
+// Linear(35, H) -> ReLU -> Linear(H, 1) on [p, f] with the staged decoder.
+__device__ __forceinline__ float decode_f32(const float4 *__restrict__ dec, int H, float px, float py,
+                                            float pz, const float (&f)[kC]) {
+    const float *__restrict__ w1 = reinterpret_cast<const float *>(dec + H * kRowF4);
+    float in[36];
+    in[0] = px;
+    in[1] = py;
+    in[2] = pz;
+#pragma unroll
+    for (int c = 0; c < kC; ++c) in[3 + c] = f[c];
+    in[35] = 1.f;
+    float out = 0.f;
+#pragma unroll 1
+    for (int j = 0; j < H; j += 2) {
+        const float4 *r0 = dec + j * kRowF4;
+        const float4 *r1 = r0 + kRowF4;
+        float a0 = 0.f, a1 = 0.f, b0 = 0.f, b1 = 0.f;
+#pragma unroll
+        for (int q = 0; q < kRowF4; ++q) {
+            const float4 u = r0[q];
+            const float4 v = r1[q];
+            if (q & 1) {
+                a1 = fmaf(u.x, in[4 * q + 0], a1);
+                a1 = fmaf(u.y, in[4 * q + 1], a1);
+                a1 = fmaf(u.z, in[4 * q + 2], a1);
+                a1 = fmaf(u.w, in[4 * q + 3], a1);
+                b1 = fmaf(v.x, in[4 * q + 0], b1);
+                b1 = fmaf(v.y, in[4 * q + 1], b1);
+                b1 = fmaf(v.z, in[4 * q + 2], b1);
+                b1 = fmaf(v.w, in[4 * q + 3], b1);
+            } else {
+                a0 = fmaf(u.x, in[4 * q + 0], a0);
+                a0 = fmaf(u.y, in[4 * q + 1], a0);
+                a0 = fmaf(u.z, in[4 * q + 2], a0);
+                a0 = fmaf(u.w, in[4 * q + 3], a0);
+                b0 = fmaf(v.x, in[4 * q + 0], b0);
+                b0 = fmaf(v.y, in[4 * q + 1], b0);
+                b0 = fmaf(v.z, in[4 * q + 2], b0);
+                b0 = fmaf(v.w, in[4 * q + 3], b0);
+            }
+        }
+        const float h0 = fmaxf(a0 + a1, 0.f);
+        const float h1 = fmaxf(b0 + b1, 0.f);
+        out = fmaf(w1[j], h0, out);
+        out = fmaf(w1[j + 1], h1, out);
+    }
+    return out + w1[H];
+}
+
+__device__ __forceinline__ int volume_side(const nglod_dense_model &m, int l) { return (1 << (l + m.base_lod)) + 1; }
+
+// Sum of the LOD 0..L samples at p, then decoder `dec`.
+__device__ __forceinline__ float eval_point_f32(const nglod_dense_model &m, int L, const float4 *dec, float px,
+                                                float py, float pz) {
+    float f[kC];
+#pragma unroll
+    for (int c = 0; c < kC; ++c) f[c] = 0.f;
+#pragma unroll 1
+    for (int l = 0; l <= L; ++l)
+        gather_add_f32(static_cast<const float *>(m.grid[l]), volume_side(m, l), px, py, pz, f);
+    return decode_f32(dec, m.hidden_dim, px, py, pz, f);
+}
+
+// ---------------------------------------------------------------------------
+// host helpers
+// ---------------------------------------------------------------------------
+inline int check_model(const nglod_dense_model *m, int L_max) {
+    NGLOD_REQUIRE(m != nullptr, NGLOD_ERR_INVALID, "model is null");
+    NGLOD_REQUIRE(m->num_lods >= 1 && m->num_lods <= NGLOD_MAX_LODS, NGLOD_ERR_INVALID,
+                  "num_lods=%d outside [1, %d]", m->num_lods, NGLOD_MAX_LODS);
+    NGLOD_REQUIRE(m->base_lod >= 0 && m->num_lods - 1 + m->base_lod <= 9, NGLOD_ERR_INVALID,
+                  "base_lod=%d with num_lods=%d gives volumes above 2^9+1 per side", m->base_lod, m->num_lods);
+    NGLOD_REQUIRE(m->feature_dim == kC, NGLOD_ERR_UNSUPPORTED, "feature_dim=%d not built (only %d)",
+                  m->feature_dim, kC);
+    NGLOD_REQUIRE(m->hidden_dim >= 2 && m->hidden_dim <= 256 && (m->hidden_dim % 2) == 0, NGLOD_ERR_UNSUPPORTED,
+                  "hidden_dim=%d not built (even, 2..256)", m->hidden_dim);
+    NGLOD_REQUIRE(m->grid_dtype == NGLOD_F32, NGLOD_ERR_UNSUPPORTED, "grid_dtype=%d: this entry point is float32",
+                  m->grid_dtype);
+    for (int l = 0; l <= L_max; ++l) {
+        NGLOD_REQUIRE(m->grid[l] && m->w0[l] && m->b0[l] && m->w1[l] && m->b1[l], NGLOD_ERR_INVALID,
+                      "lod %d has a null volume or decoder pointer", l);
+        NGLOD_REQUIRE(aligned(m->grid[l], 16), NGLOD_ERR_ALIGN, "volume %d is not 16-byte aligned", l);
+    }
+    return NGLOD_OK;
+}
+
+inline int resolve_lod(const nglod_dense_model *m, int lod) {
+    return (lod < 0 || lod >= m->num_lods) ? m->num_lods - 1 : lod;
+}
+
+template <typename K>
+inline int prepare_smem(K kernel, size_t smem) {
+    NGLOD_REQUIRE(smem <= 227 * 1024, NGLOD_ERR_UNSUPPORTED, "decoder staging needs %zu B of shared memory", smem);
+    return cuda_status(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                       "cudaFuncSetAttribute");
+}
+
+template <typename K>
+inline int resident_blocks(K kernel, int threads, size_t smem) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    return per_sm * num_sms();
+}
+
+}  // namespace nglod

@@ -1,0 +1,506 @@
+// Training kernels of the dense float32 path: forward with saved feature
+// sums, hand-written backward, multi-tensor Adam.
+//
+// Backward of one training batch (lod_mask = set of LODs with a loss term):
+//   1. sdf_bwd_decoder_kernel, one pass per LOD l in the mask: each thread
+//      owns one point of a 128-point tile, recomputes the decoder's hidden
+//      layer from the saved feature sum, writes dLoss/d(feature sum) for its
+//      point and stores its hidden activations in a shared tile; the block
+//      then reduces the tile into the weight gradients (thread j owns hidden
+//      row j: dW0[j][:], db0[j], dw1[j]), accumulating over all tiles it
+//      visits, and adds its totals to global memory once per LOD.
+//   2. sdf_bwd_scatter_kernel: per point, the gradient reaching volume i is
+//      the suffix sum over mask LODs l >= i of dLoss/d(feature sum l); it is
+//      scattered with the trilinear weights.  The coarsest volumes
+//      (5^3 and 9^3 vertices at base_lod 2) are accumulated in shared memory
+//      per block and flushed once; finer ones use red.global.add.v4.f32.
+#include "dense_common.cuh"
+
+namespace nglod {
+
+constexpr int kBT = 128;  // points per backward tile = threads per block
+
+// ---------------------------------------------------------------------------
+// forward for training
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) sdf_fwd_train_kernel(const nglod_dense_model m, const float *__restrict__ x,
+                                                            int64_t n, int L, uint32_t mask,
+                                                            float *__restrict__ preds, float *__restrict__ feats) {
+    extern __shared__ float4 smem[];
+    const int H = m.hidden_dim;
+    const int dstride = decoder_f4(H);
+    for (int l = 0; l <= L; ++l)
+        if ((mask >> l) & 1u) stage_decoder(smem + l * dstride, m, l);
+    __syncthreads();
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const float px = x[3 * i], py = x[3 * i + 1], pz = x[3 * i + 2];
+        float f[kC];
+#pragma unroll
+        for (int c = 0; c < kC; ++c) f[c] = 0.f;
+#pragma unroll 1
+        for (int l = 0; l <= L; ++l) {
+            gather_add_f32(static_cast<const float *>(m.grid[l]), volume_side(m, l), px, py, pz, f);
+            if ((mask >> l) & 1u) {
+                preds[(int64_t)l * n + i] = decode_f32(smem + l * dstride, H, px, py, pz, f);
+                float4 *o = reinterpret_cast<float4 *>(feats + ((int64_t)l * n + i) * kC);
+#pragma unroll
+                for (int q = 0; q < kC / 4; ++q)
+                    o[q] = make_float4(f[4 * q], f[4 * q + 1], f[4 * q + 2], f[4 * q + 3]);
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// backward 1: decoders
+// ---------------------------------------------------------------------------
+struct BwdArgs {
+    nglod_dense_model m;
+    nglod_dense_grads g;
+    const float *x;
+    int64_t n;
+    uint32_t mask;
+    int L;
+    const float *gpred;
+    const float *feats;
+    float *dfeat;
+    float *gx;
+};
+
+__host__ __device__ inline int bwd_ht_floats(int H) { return kBT * (H + 1); }
+// Shared layout (floats): decoder | H tile [kBT][H+1] | IN tile [kBT][36] | g [kBT] | acc [H][37]
+__host__ __device__ inline size_t bwd_decoder_smem(int H) {
+    size_t f = (size_t)decoder_f4(H) * 4 + bwd_ht_floats(H);
+    f = (f + 3) & ~(size_t)3;
+    return (f + kBT * 36 + kBT + (size_t)H * 37) * sizeof(float);
+}
+
+__global__ void __launch_bounds__(kBT) sdf_bwd_decoder_kernel(const BwdArgs a) {
+    extern __shared__ float4 smem[];
+    const int H = a.m.hidden_dim;
+    const int tid = threadIdx.x;
+    float4 *dec = smem;
+    float *Ht = reinterpret_cast<float *>(smem + decoder_f4(H));
+    size_t off = (size_t)decoder_f4(H) * 4 + bwd_ht_floats(H);
+    off = (off + 3) & ~(size_t)3;
+    float *INt = reinterpret_cast<float *>(smem) + off;
+    float *gt = INt + kBT * 36;
+    float *acc = gt + kBT;
+    const float *w1s = reinterpret_cast<const float *>(dec + H * kRowF4);
+
+    for (int l = 0; l <= a.L; ++l) {
+        if (!((a.mask >> l) & 1u)) continue;
+        __syncthreads();
+        stage_decoder(dec, a.m, l);
+        for (int i = tid; i < H * 37; i += kBT) acc[i] = 0.f;
+        float db1 = 0.f;
+        __syncthreads();
+        for (int64_t tile = blockIdx.x; tile * kBT < a.n; tile += gridDim.x) {
+            const int64_t p = tile * kBT + tid;
+            const bool valid = p < a.n;
+            float in[36];
+            float g = 0.f;
+            if (valid) {
+                in[0] = a.x[3 * p];
+                in[1] = a.x[3 * p + 1];
+                in[2] = a.x[3 * p + 2];
+                const float4 *fr = reinterpret_cast<const float4 *>(a.feats + ((int64_t)l * a.n + p) * kC);
+#pragma unroll
+                for (int q = 0; q < kC / 4; ++q) {
+                    const float4 v = fr[q];
+                    in[3 + 4 * q] = v.x;
+                    in[4 + 4 * q] = v.y;
+                    in[5 + 4 * q] = v.z;
+                    in[6 + 4 * q] = v.w;
+                }
+                in[35] = 1.f;
+                g = a.gpred[(int64_t)l * a.n + p];
+            } else {
+#pragma unroll
+                for (int k = 0; k < 36; ++k) in[k] = 0.f;
+            }
+            float din[36];
+#pragma unroll
+            for (int k = 0; k < 36; ++k) din[k] = 0.f;
+#pragma unroll 1
+            for (int j = 0; j < H; ++j) {
+                const float4 *r = dec + j * kRowF4;
+                float s0 = 0.f, s1 = 0.f;
+#pragma unroll
+                for (int q = 0; q < kRowF4; ++q) {
+                    const float4 w = r[q];
+                    if (q & 1) {
+                        s1 = fmaf(w.x, in[4 * q], s1);
+                        s1 = fmaf(w.y, in[4 * q + 1], s1);
+                        s1 = fmaf(w.z, in[4 * q + 2], s1);
+                        s1 = fmaf(w.w, in[4 * q + 3], s1);
+                    } else {
+                        s0 = fmaf(w.x, in[4 * q], s0);
+                        s0 = fmaf(w.y, in[4 * q + 1], s0);
+                        s0 = fmaf(w.z, in[4 * q + 2], s0);
+                        s0 = fmaf(w.w, in[4 * q + 3], s0);
+                    }
+                }
+                const float pre = s0 + s1;
+                const float h = fmaxf(pre, 0.f);
+                const float dh = pre > 0.f ? g * w1s[j] : 0.f;
+                Ht[tid * (H + 1) + j] = h;
+#pragma unroll
+                for (int q = 0; q < kRowF4; ++q) {
+                    const float4 w = r[q];
+                    din[4 * q] = fmaf(dh, w.x, din[4 * q]);
+                    din[4 * q + 1] = fmaf(dh, w.y, din[4 * q + 1]);
+                    din[4 * q + 2] = fmaf(dh, w.z, din[4 * q + 2]);
+                    din[4 * q + 3] = fmaf(dh, w.w, din[4 * q + 3]);
+                }
+            }
+            if (valid) {
+                float4 *o = reinterpret_cast<float4 *>(a.dfeat + ((int64_t)l * a.n + p) * kC);
+#pragma unroll
+                for (int q = 0; q < kC / 4; ++q)
+                    o[q] = make_float4(din[3 + 4 * q], din[4 + 4 * q], din[5 + 4 * q], din[6 + 4 * q]);
+                if (a.gx) {
+                    a.gx[3 * p] += din[0];
+                    a.gx[3 * p + 1] += din[1];
+                    a.gx[3 * p + 2] += din[2];
+                }
+            }
+            float4 *ir = reinterpret_cast<float4 *>(INt + tid * 36);
+#pragma unroll
+            for (int q = 0; q < 9; ++q) ir[q] = make_float4(in[4 * q], in[4 * q + 1], in[4 * q + 2], in[4 * q + 3]);
+            gt[tid] = g;
+            __syncthreads();
+            if (tid < H) {
+                const int j = tid;
+                const float w1j = w1s[j];
+                float r[36];
+#pragma unroll
+                for (int k = 0; k < 36; ++k) r[k] = 0.f;
+                float dw1 = 0.f;
+#pragma unroll 2
+                for (int q = 0; q < kBT; ++q) {
+                    const float h = Ht[q * (H + 1) + j];
+                    const float gq = gt[q];
+                    const float dh = h > 0.f ? gq * w1j : 0.f;
+                    dw1 = fmaf(gq, h, dw1);
+                    const float4 *row = reinterpret_cast<const float4 *>(INt + q * 36);
+#pragma unroll
+                    for (int k4 = 0; k4 < 9; ++k4) {
+                        const float4 v = row[k4];
+                        r[4 * k4] = fmaf(dh, v.x, r[4 * k4]);
+                        r[4 * k4 + 1] = fmaf(dh, v.y, r[4 * k4 + 1]);
+                        r[4 * k4 + 2] = fmaf(dh, v.z, r[4 * k4 + 2]);
+                        r[4 * k4 + 3] = fmaf(dh, v.w, r[4 * k4 + 3]);
+                    }
+                }
+#pragma unroll
+                for (int k = 0; k < 36; ++k) acc[j * 37 + k] += r[k];
+                acc[j * 37 + 36] += dw1;
+            }
+            if (tid < 32) {
+                float s = gt[tid] + gt[tid + 32] + gt[tid + 64] + gt[tid + 96];
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+                db1 += s;
+            }
+            __syncthreads();
+        }
+        if (tid < H) {
+            const int j = tid;
+            float *dw0 = a.g.w0[l] + (size_t)j * 35;
+            for (int k = 0; k < 35; ++k) atomicAdd(dw0 + k, acc[j * 37 + k]);
+            atomicAdd(a.g.b0[l] + j, acc[j * 37 + 35]);
+            atomicAdd(a.g.w1[l] + j, acc[j * 37 + 36]);
+        }
+        if (tid == 0) atomicAdd(a.g.b1[l], db1);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// backward 2: trilinear scatter into the volumes (+ optional dLoss/dx)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void red_add_v4(float *addr, float a, float b, float c, float d) {
+    asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(addr), "f"(a), "f"(b), "f"(c), "f"(d)
+                 : "memory");
+}
+
+// Volumes below `smem_levels` are accumulated in shared memory (offsets in
+// floats given by soff[l]); the rest go straight to global memory.
+struct ScatterArgs {
+    BwdArgs a;
+    int smem_levels;
+    int soff[NGLOD_MAX_LODS + 1];
+};
+
+template <bool kGradX>
+__global__ void __launch_bounds__(256) sdf_bwd_scatter_kernel(const ScatterArgs s) {
+    extern __shared__ float sacc[];
+    const BwdArgs &a = s.a;
+    const int stot = s.soff[s.smem_levels];
+    for (int i = threadIdx.x; i < stot; i += blockDim.x) sacc[i] = 0.f;
+    __syncthreads();
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < a.n; p += stride) {
+        const float px = a.x[3 * p], py = a.x[3 * p + 1], pz = a.x[3 * p + 2];
+        float G[kC];
+#pragma unroll
+        for (int c = 0; c < kC; ++c) G[c] = 0.f;
+        float gxx = 0.f, gxy = 0.f, gxz = 0.f;
+#pragma unroll 1
+        for (int l = a.L; l >= 0; --l) {
+            if ((a.mask >> l) & 1u) {
+                const float4 *dr = reinterpret_cast<const float4 *>(a.dfeat + ((int64_t)l * a.n + p) * kC);
+#pragma unroll
+                for (int q = 0; q < kC / 4; ++q) {
+                    const float4 v = dr[q];
+                    G[4 * q] += v.x;
+                    G[4 * q + 1] += v.y;
+                    G[4 * q + 2] += v.z;
+                    G[4 * q + 3] += v.w;
+                }
+            }
+            const int sd = volume_side(a.m, l);
+            const float sm1 = (float)(sd - 1);
+            const float rx = ((px + 1.f) / 2.f) * sm1;
+            const float ry = ((py + 1.f) / 2.f) * sm1;
+            const float rz = ((pz + 1.f) / 2.f) * sm1;
+            const float ix = fminf(sm1, fmaxf(rx, 0.f));
+            const float iy = fminf(sm1, fmaxf(ry, 0.f));
+            const float iz = fminf(sm1, fmaxf(rz, 0.f));
+            const float x0 = floorf(ix), y0 = floorf(iy), z0 = floorf(iz);
+            const float wx1 = ix - x0, wx0 = (x0 + 1.f) - ix;
+            const float wy1 = iy - y0, wy0 = (y0 + 1.f) - iy;
+            const float wz1 = iz - z0, wz0 = (z0 + 1.f) - iz;
+            const int xi = (int)x0, yi = (int)y0, zi = (int)z0;
+            const int xj = min(xi + 1, sd - 1), yj = min(yi + 1, sd - 1), zj = min(zi + 1, sd - 1);
+            int cidx[8];
+            cidx[0] = (zi * sd + yi) * sd + xi;
+            cidx[1] = (zi * sd + yi) * sd + xj;
+            cidx[2] = (zi * sd + yj) * sd + xi;
+            cidx[3] = (zi * sd + yj) * sd + xj;
+            cidx[4] = (zj * sd + yi) * sd + xi;
+            cidx[5] = (zj * sd + yi) * sd + xj;
+            cidx[6] = (zj * sd + yj) * sd + xi;
+            cidx[7] = (zj * sd + yj) * sd + xj;
+            float w[8];
+            w[0] = wx0 * wy0 * wz0;
+            w[1] = wx1 * wy0 * wz0;
+            w[2] = wx0 * wy1 * wz0;
+            w[3] = wx1 * wy1 * wz0;
+            w[4] = wx0 * wy0 * wz1;
+            w[5] = wx1 * wy0 * wz1;
+            w[6] = wx0 * wy1 * wz1;
+            w[7] = wx1 * wy1 * wz1;
+            if (l < s.smem_levels) {
+                float *base = sacc + s.soff[l];
+#pragma unroll
+                for (int k = 0; k < 8; ++k) {
+                    float *dst = base + cidx[k] * kC;
+#pragma unroll
+                    for (int c = 0; c < kC; ++c) atomicAdd(dst + c, G[c] * w[k]);
+                }
+            } else {
+                float *base = a.g.grid[l];
+#pragma unroll
+                for (int k = 0; k < 8; ++k) {
+                    float *dst = base + (size_t)cidx[k] * kC;
+#pragma unroll
+                    for (int q = 0; q < kC / 4; ++q)
+                        red_add_v4(dst + 4 * q, G[4 * q] * w[k], G[4 * q + 1] * w[k], G[4 * q + 2] * w[k],
+                                   G[4 * q + 3] * w[k]);
+                }
+            }
+            if (kGradX) {
+                // d(sample)/du per corner: -/+ the product of the other two axes' weights
+                // (PyTorch's grid_sampler_3d backward), times (s-1)/2, zero where clamped.
+                const float *g = static_cast<const float *>(a.m.grid[l]);
+                float dot[8];
+#pragma unroll
+                for (int k = 0; k < 8; ++k) {
+                    const float4 *v = reinterpret_cast<const float4 *>(g + (size_t)cidx[k] * kC);
+                    float sacc_k = 0.f;
+#pragma unroll
+                    for (int q = 0; q < kC / 4; ++q) {
+                        const float4 u = __ldg(v + q);
+                        sacc_k = fmaf(G[4 * q], u.x, sacc_k);
+                        sacc_k = fmaf(G[4 * q + 1], u.y, sacc_k);
+                        sacc_k = fmaf(G[4 * q + 2], u.z, sacc_k);
+                        sacc_k = fmaf(G[4 * q + 3], u.w, sacc_k);
+                    }
+                    dot[k] = sacc_k;
+                }
+                float gix = 0.f, giy = 0.f, giz = 0.f;
+                gix += -dot[0] * wy0 * wz0 + dot[1] * wy0 * wz0 - dot[2] * wy1 * wz0 + dot[3] * wy1 * wz0;
+                gix += -dot[4] * wy0 * wz1 + dot[5] * wy0 * wz1 - dot[6] * wy1 * wz1 + dot[7] * wy1 * wz1;
+                giy += -dot[0] * wx0 * wz0 - dot[1] * wx1 * wz0 + dot[2] * wx0 * wz0 + dot[3] * wx1 * wz0;
+                giy += -dot[4] * wx0 * wz1 - dot[5] * wx1 * wz1 + dot[6] * wx0 * wz1 + dot[7] * wx1 * wz1;
+                giz += -dot[0] * wx0 * wy0 - dot[1] * wx1 * wy0 - dot[2] * wx0 * wy1 - dot[3] * wx1 * wy1;
+                giz += dot[4] * wx0 * wy0 + dot[5] * wx1 * wy0 + dot[6] * wx0 * wy1 + dot[7] * wx1 * wy1;
+                const float half = sm1 / 2.f;
+                gxx += (rx <= 0.f || rx >= sm1) ? 0.f : gix * half;
+                gxy += (ry <= 0.f || ry >= sm1) ? 0.f : giy * half;
+                gxz += (rz <= 0.f || rz >= sm1) ? 0.f : giz * half;
+            }
+        }
+        if (kGradX) {
+            a.gx[3 * p] += gxx;
+            a.gx[3 * p + 1] += gxy;
+            a.gx[3 * p + 2] += gxz;
+        }
+    }
+    __syncthreads();
+    for (int l = 0; l < s.smem_levels; ++l) {
+        const int nl = s.soff[l + 1] - s.soff[l];
+        float *dst = a.g.grid[l];
+        const float *src = sacc + s.soff[l];
+        for (int i = threadIdx.x * 4; i < nl; i += blockDim.x * 4)
+            red_add_v4(dst + i, src[i], src[i + 1], src[i + 2], src[i + 3]);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Adam
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) adam_kernel(const nglod_adam_tensor *__restrict__ tab, float lr_over_bc1,
+                                                   float beta1, float beta2, float one_m_b1, float one_m_b2,
+                                                   float bc2_sqrt, float eps, float wd) {
+    const nglod_adam_tensor t = tab[blockIdx.y];
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < t.numel; i += stride) {
+        float g = t.grad[i];
+        float p = t.param[i];
+        if (wd != 0.f) g = g + wd * p;
+        float m = t.exp_avg[i];
+        // torch.lerp with weight < 0.5: m + w * (g - m)
+        m = m + one_m_b1 * (g - m);
+        float v = t.exp_avg_sq[i] * beta2;
+        v = v + (one_m_b2 * g) * g;
+        const float denom = sqrtf(v) / bc2_sqrt + eps;
+        p = p + (-lr_over_bc1) * (m / denom);
+        t.exp_avg[i] = m;
+        t.exp_avg_sq[i] = v;
+        t.param[i] = p;
+    }
+}
+
+}  // namespace nglod
+
+using namespace nglod;
+
+static int lod_mask_top(uint32_t mask) {
+    int L = -1;
+    for (int l = 0; l < NGLOD_MAX_LODS; ++l)
+        if ((mask >> l) & 1u) L = l;
+    return L;
+}
+
+extern "C" int nglod_sdf_fwd_train(const nglod_dense_model *model, const float *x, int64_t n, uint32_t lod_mask,
+                                   float *preds, float *feats, nglod_stream_t stream) {
+    NGLOD_REQUIRE(model != nullptr, NGLOD_ERR_INVALID, "model is null");
+    const int L = lod_mask_top(lod_mask);
+    NGLOD_REQUIRE(L >= 0 && L < model->num_lods && (lod_mask >> NGLOD_MAX_LODS) == 0, NGLOD_ERR_INVALID,
+                  "lod_mask=0x%x selects no LOD or a LOD >= num_lods=%d", lod_mask, model->num_lods);
+    NGLOD_TRY(check_model(model, L));
+    NGLOD_REQUIRE(n >= 0, NGLOD_ERR_INVALID, "n=%lld is negative", (long long)n);
+    if (n == 0) return NGLOD_OK;
+    NGLOD_REQUIRE(x && preds && feats, NGLOD_ERR_INVALID, "null pointer argument");
+    NGLOD_REQUIRE(aligned(feats, 16), NGLOD_ERR_ALIGN, "feats must be 16-byte aligned");
+    const int threads = 256;
+    const size_t smem = (size_t)(L + 1) * decoder_f4(model->hidden_dim) * sizeof(float4);
+    NGLOD_TRY(prepare_smem(sdf_fwd_train_kernel, smem));
+    const int64_t want = (n + threads - 1) / threads;
+    const int64_t cap = resident_blocks(sdf_fwd_train_kernel, threads, smem);
+    sdf_fwd_train_kernel<<<(int)(want < cap ? want : cap), threads, smem, (cudaStream_t)stream>>>(
+        *model, x, n, L, lod_mask, preds, feats);
+    return launch_status("nglod_sdf_fwd_train");
+}
+
+extern "C" int nglod_sdf_bwd(const nglod_dense_model *model, const float *x, int64_t n, uint32_t lod_mask,
+                             const float *grad_preds, const float *feats, float *dfeat_scratch,
+                             const nglod_dense_grads *grads, float *grad_x, nglod_stream_t stream) {
+    NGLOD_REQUIRE(model != nullptr && grads != nullptr, NGLOD_ERR_INVALID, "model or grads is null");
+    const int L = lod_mask_top(lod_mask);
+    NGLOD_REQUIRE(L >= 0 && L < model->num_lods && (lod_mask >> NGLOD_MAX_LODS) == 0, NGLOD_ERR_INVALID,
+                  "lod_mask=0x%x selects no LOD or a LOD >= num_lods=%d", lod_mask, model->num_lods);
+    NGLOD_TRY(check_model(model, L));
+    NGLOD_REQUIRE(model->hidden_dim <= kBT, NGLOD_ERR_UNSUPPORTED, "backward built for hidden_dim <= %d", kBT);
+    NGLOD_REQUIRE(n >= 0, NGLOD_ERR_INVALID, "n=%lld is negative", (long long)n);
+    if (n == 0) return NGLOD_OK;
+    NGLOD_REQUIRE(x && grad_preds && feats && dfeat_scratch, NGLOD_ERR_INVALID, "null pointer argument");
+    NGLOD_REQUIRE(aligned(feats, 16) && aligned(dfeat_scratch, 16), NGLOD_ERR_ALIGN,
+                  "feats and dfeat_scratch must be 16-byte aligned");
+    for (int l = 0; l <= L; ++l) {
+        NGLOD_REQUIRE(grads->grid[l] && aligned(grads->grid[l], 16), NGLOD_ERR_INVALID,
+                      "volume gradient %d is null or not 16-byte aligned", l);
+        if ((lod_mask >> l) & 1u)
+            NGLOD_REQUIRE(grads->w0[l] && grads->b0[l] && grads->w1[l] && grads->b1[l], NGLOD_ERR_INVALID,
+                          "decoder gradient %d has a null pointer", l);
+    }
+    BwdArgs a;
+    a.m = *model;
+    a.g = *grads;
+    a.x = x;
+    a.n = n;
+    a.mask = lod_mask;
+    a.L = L;
+    a.gpred = grad_preds;
+    a.feats = feats;
+    a.dfeat = dfeat_scratch;
+    a.gx = grad_x;
+
+    const size_t smem1 = bwd_decoder_smem(model->hidden_dim);
+    NGLOD_TRY(prepare_smem(sdf_bwd_decoder_kernel, smem1));
+    const int64_t tiles = (n + kBT - 1) / kBT;
+    const int64_t cap1 = resident_blocks(sdf_bwd_decoder_kernel, kBT, smem1);
+    sdf_bwd_decoder_kernel<<<(int)(tiles < cap1 ? tiles : cap1), kBT, smem1, (cudaStream_t)stream>>>(a);
+    NGLOD_TRY(launch_status("nglod_sdf_bwd (decoder)"));
+
+    ScatterArgs s;
+    s.a = a;
+    s.smem_levels = 0;
+    s.soff[0] = 0;
+    const int budget = 112 * 1024 / (int)sizeof(float);  // leave room for two blocks per SM
+    for (int l = 0; l <= L; ++l) {
+        const int side = (1 << (l + model->base_lod)) + 1;
+        const int cnt = side * side * side * kC;
+        if (s.soff[l] + cnt > budget) break;
+        s.soff[l + 1] = s.soff[l] + cnt;
+        s.smem_levels = l + 1;
+    }
+    const size_t smem2 = (size_t)s.soff[s.smem_levels] * sizeof(float);
+    const int threads = 256;
+    const int64_t want = (n + threads - 1) / threads;
+    if (grad_x) {
+        auto k = sdf_bwd_scatter_kernel<true>;
+        NGLOD_TRY(prepare_smem(k, smem2));
+        const int64_t cap = resident_blocks(k, threads, smem2);
+        k<<<(int)(want < cap ? want : cap), threads, smem2, (cudaStream_t)stream>>>(s);
+    } else {
+        auto k = sdf_bwd_scatter_kernel<false>;
+        NGLOD_TRY(prepare_smem(k, smem2));
+        const int64_t cap = resident_blocks(k, threads, smem2);
+        k<<<(int)(want < cap ? want : cap), threads, smem2, (cudaStream_t)stream>>>(s);
+    }
+    return launch_status("nglod_sdf_bwd (scatter)");
+}
+
+extern "C" int nglod_adam_step(const nglod_adam_tensor *tensors, int32_t count, int64_t max_numel, float lr,
+                               float beta1, float beta2, float eps, float weight_decay, int64_t step,
+                               nglod_stream_t stream) {
+    NGLOD_REQUIRE(count >= 0 && count <= 65535, NGLOD_ERR_INVALID, "count=%d outside [0, 65535]", count);
+    NGLOD_REQUIRE(step >= 1, NGLOD_ERR_INVALID, "step=%lld: the first step is 1", (long long)step);
+    if (count == 0 || max_numel <= 0) return NGLOD_OK;
+    NGLOD_REQUIRE(tensors != nullptr, NGLOD_ERR_INVALID, "tensor table is null");
+    const double bc1 = 1.0 - pow((double)beta1, (double)step);
+    const double bc2 = 1.0 - pow((double)beta2, (double)step);
+    const int threads = 256;
+    int64_t bx = (max_numel + threads - 1) / threads;
+    const int64_t cap = (int64_t)num_sms() * 8;
+    if (bx > cap) bx = cap;
+    dim3 grid((unsigned)bx, (unsigned)count);
+    adam_kernel<<<grid, threads, 0, (cudaStream_t)stream>>>(tensors, (float)((double)lr / bc1), beta1, beta2,
+                                                            (float)(1.0 - (double)beta1), (float)(1.0 - (double)beta2),
+                                                            (float)sqrt(bc2), eps, weight_decay);
+    return launch_status("nglod_adam_step");
+}

@@ -1,0 +1,97 @@
+"""Training step of the dense model on the nglod_gb300 kernels.
+
+``FusedAdam`` is a torch.optim.Optimizer whose step is one multi-tensor
+kernel launch (``nglod_adam_step``) with torch.optim.Adam's update rule.
+``step_geometry`` is Trainer.step_geometry (sdf-net/lib/trainer.py:294-340):
+L2 loss summed over the loss LODs and divided by the batch size, backward,
+optimizer step.  The loss is reduced in float64 on the GPU.
+"""
+import ctypes
+
+import torch
+
+from . import _lib
+
+
+class FusedAdam(torch.optim.Optimizer):
+    def __init__(self, params, lr=1e-3, betas=(0.9, 0.999), eps=1e-8, weight_decay=0.0):
+        super().__init__(params, dict(lr=lr, betas=betas, eps=eps, weight_decay=weight_decay))
+        self._host_table = None
+
+    @torch.no_grad()
+    def step(self, closure=None):
+        loss = None
+        if closure is not None:
+            with torch.enable_grad():
+                loss = closure()
+        for group in self.param_groups:
+            entries = []
+            dev = None
+            step_no = None
+            for p in group["params"]:
+                if p.grad is None:
+                    continue
+                _lib.require_cuda(p)
+                if p.dtype != torch.float32 or p.grad.dtype != torch.float32:
+                    raise RuntimeError("FusedAdam: float32 parameters and gradients required")
+                st = self.state[p]
+                if not st:
+                    st["step"] = 0
+                    st["exp_avg"] = torch.zeros_like(p, memory_format=torch.preserve_format)
+                    st["exp_avg_sq"] = torch.zeros_like(p, memory_format=torch.preserve_format)
+                st["step"] += 1
+                step_no = st["step"] if step_no is None else step_no
+                if st["step"] != step_no:
+                    raise RuntimeError("FusedAdam: parameters of a group must share their step count")
+                g = p.grad
+                if g.stride() != p.stride():
+                    g = _like(p, g)
+                    p.grad = g
+                entries.append((p, g, st["exp_avg"], st["exp_avg_sq"]))
+                dev = p.device
+            if not entries:
+                continue
+            tab = (_lib.AdamTensor * len(entries))()
+            for i, (p, g, m, v) in enumerate(entries):
+                tab[i].param, tab[i].grad = p.data_ptr(), g.data_ptr()
+                tab[i].exp_avg, tab[i].exp_avg_sq = m.data_ptr(), v.data_ptr()
+                tab[i].numel = p.numel()
+            raw = torch.frombuffer(bytearray(bytes(tab)), dtype=torch.uint8)
+            dtab = raw.to(dev, non_blocking=False)
+            b1, b2 = group["betas"]
+            _lib.check(_lib.load().nglod_adam_step(ctypes.c_void_p(dtab.data_ptr()), len(entries),
+                                                   max(p.numel() for p, *_ in entries), group["lr"], b1, b2,
+                                                   group["eps"], group["weight_decay"], step_no,
+                                                   _lib.stream_ptr(dev)), "nglod_adam_step")
+            group.setdefault("_tables", []).append(dtab)  # keep alive until the stream has used it
+            if len(group["_tables"]) > 4:
+                group["_tables"].pop(0)
+        return loss
+
+
+def _like(p, g):
+    """g copied into a tensor with p's strides (dense, same memory format)."""
+    out = torch.empty_like(p, memory_format=torch.preserve_format)
+    out.copy_(g)
+    return out
+
+
+def l2_loss(preds, gts, loss_lods, batch_size):
+    """sum over loss LODs of ((pred - gt)^2).sum() / batch_size (trainer.py:325-336)."""
+    loss = 0
+    for l in loss_lods:
+        loss = loss + ((preds[l] - gts) ** 2).sum()
+    return loss / batch_size
+
+
+def step_geometry(net, optimizer, pts, gts, loss_lods=None):
+    """One training step; returns the loss (float64, reduced on the GPU)."""
+    if loss_lods is None:
+        loss_lods = list(range(net.num_lods))
+    net.zero_grad()
+    preds = net.sdf(pts, return_lst=True)
+    loss = l2_loss(preds, gts, loss_lods, pts.shape[0])
+    loss.backward()
+    optimizer.step()
+    with torch.no_grad():
+        return sum(((preds[l].double() - gts.double()) ** 2).sum() for l in loss_lods) / pts.shape[0]

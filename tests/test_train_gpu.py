@@ -1,0 +1,156 @@
+"""Hand-written backward and Adam against the reference's autograd gradients,
+FP64 central finite differences and torch.optim.Adam."""
+import numpy as np
+import pytest
+import torch
+
+import nglod_gb300 as ng
+from nglod_gb300 import synthetic, trainer
+from oracle import dense
+from tests.helpers import model_from_fixture, oracle_model, seeded_model
+
+pytestmark = pytest.mark.gpu
+
+
+def _grads(net):
+    return {k: p.grad.detach().cpu().numpy() for k, p in net.named_parameters() if p.grad is not None}
+
+
+def test_backward_matches_reference_autograd(golden, cuda):
+    """Same loss as the fixture (Trainer.step_geometry over lods 0, 1, 2 with
+    separate sdf calls); gradients vs the reference's autograd on the CPU."""
+    fx = golden("dense_small")
+    net = model_from_fixture(fx, 3, 1, device=cuda).train()
+    x = torch.from_numpy(fx["points"]).to(cuda)
+    gts = torch.from_numpy(fx["train/gts"]).to(cuda)
+    net.zero_grad()
+    loss = 0
+    for lod in [0, 1, 2]:
+        loss = loss + ((net.sdf(x, lod=lod) - gts) ** 2).sum()
+    loss = loss / x.shape[0]
+    loss.backward()
+    assert abs(loss.item() - float(fx["train/loss"])) < 1e-5 * max(1.0, abs(float(fx["train/loss"])))
+    got = _grads(net)
+    for k, g in got.items():
+        ref = fx["grad/" + k]
+        scale = np.abs(ref).max() + 1e-12
+        err = np.abs(g - ref).max() / scale
+        assert err < 1e-4, (k, err)
+    assert set(got) == {k[len("grad/"):] for k in fx if k.startswith("grad/")}
+
+
+def test_return_lst_backward_equals_separate_calls(cuda):
+    net = seeded_model(num_lods=4, base_lod=2, seed=3).to(cuda).train()
+    x = torch.rand(3000, 3, device=cuda) * 2.2 - 1.1
+    gts = torch.rand(3000, 1, device=cuda) * 0.2 - 0.1
+    net.zero_grad()
+    preds = net.sdf(x, return_lst=True)
+    trainer.l2_loss(preds, gts, [0, 1, 2, 3], x.shape[0]).backward()
+    a = _grads(net)
+    net.zero_grad()
+    loss = sum(((net.sdf(x, lod=l) - gts) ** 2).sum() for l in range(4)) / x.shape[0]
+    loss.backward()
+    b = _grads(net)
+    for k in a:
+        scale = np.abs(b[k]).max() + 1e-12
+        assert np.abs(a[k] - b[k]).max() / scale < 1e-5, k
+
+
+def _fd_check(net, x, gts, lods, picks, h=1e-3):
+    """Gradient entries vs FP64 central differences of the oracle loss."""
+    m = oracle_model(net.cpu(), np.float64)
+    xn = x.cpu().numpy().astype(np.float64)
+    gn = gts.cpu().numpy().astype(np.float64)
+
+    def loss_of(mm):
+        return sum(((dense.sdf(mm, xn, lod=l) - gn) ** 2).sum() for l in lods) / xn.shape[0]
+
+    out = []
+    for name, idx in picks:
+        kind, i = name.split(":")
+        i = int(i)
+        arr = {"fm": m["fms"], "w0": m["w0"], "b0": m["b0"], "w1": m["w1"], "b1": m["b1"]}[kind][i]
+        base = arr[idx]
+        arr[idx] = base + h
+        lp = loss_of(m)
+        arr[idx] = base - h
+        lm = loss_of(m)
+        arr[idx] = base
+        out.append((lp - lm) / (2 * h))
+    return np.array(out)
+
+
+def test_backward_vs_fp64_finite_differences(cuda):
+    torch.manual_seed(7)
+    net = seeded_model(num_lods=2, base_lod=2, seed=7)
+    c, r = synthetic.sphere_union(1)
+    x, gts = synthetic.training_batch(512, c, r, seed=3)
+    net = net.to(cuda).train()
+    xd, gd = x.to(cuda), gts.to(cuda)
+    net.zero_grad()
+    trainer.l2_loss(net.sdf(xd, return_lst=True), gd, [0, 1], 512).backward()
+    grads = {"fm:0": net.features[0].fm.grad[0].cpu().numpy(), "fm:1": net.features[1].fm.grad[0].cpu().numpy(),
+             "w0:1": net.louts[1][0].weight.grad.cpu().numpy(), "b0:0": net.louts[0][0].bias.grad.cpu().numpy(),
+             "w1:1": net.louts[1][2].weight.grad.cpu().numpy(), "b1:0": net.louts[0][2].bias.grad.cpu().numpy()}
+    rng = np.random.default_rng(0)
+    picks = []
+    for name, g in grads.items():
+        flat = np.argsort(-np.abs(g).ravel())[:3]  # the largest entries (well above FD noise)
+        for f in list(flat) + [rng.integers(g.size)]:
+            picks.append((name, np.unravel_index(f, g.shape)))
+    fd = _fd_check(net, x, gts, [0, 1], picks)
+    got = np.array([grads[n][i] for n, i in picks])
+    big = np.abs(fd) > 1e-4
+    rel = np.abs(got - fd)[big] / np.abs(fd)[big]
+    assert big.sum() >= 12
+    assert rel.max() < 1e-3, rel.max()
+    assert np.abs(got - fd)[~big].max(initial=0) < 1e-6
+
+
+def test_grad_x_vs_finite_differences(cuda):
+    net = seeded_model(num_lods=3, base_lod=2, seed=9).to(cuda).eval()
+    x = (torch.rand(256, 3, device=cuda) * 1.8 - 0.9).requires_grad_(True)
+    y = net.sdf(x, lod=2)
+    (gx,) = torch.autograd.grad(y.sum(), x)
+    m = oracle_model(net.cpu(), np.float64)
+    xn = x.detach().cpu().numpy().astype(np.float64)
+    h = 1e-4
+    fd = np.zeros_like(xn)
+    for k in range(3):
+        e = np.zeros(3)
+        e[k] = h
+        fd[:, k] = (dense.sdf(m, xn + e, lod=2) - dense.sdf(m, xn - e, lod=2))[:, 0] / (2 * h)
+    np.testing.assert_allclose(gx.cpu().numpy(), fd, atol=2e-4, rtol=1e-3)
+
+
+def test_fused_adam_matches_torch_adam(cuda):
+    torch.manual_seed(0)
+    p1 = torch.randn(1000, 37, device=cuda)
+    p2 = p1.clone()
+    q1 = torch.randn(5, 32, 9, 9, 9, device=cuda).contiguous(memory_format=torch.channels_last_3d)
+    q2 = q1.clone()
+    a = trainer.FusedAdam([p1, q1], lr=1e-3)
+    b = torch.optim.Adam([p2, q2], lr=1e-3, foreach=False)
+    for p in (p1, p2, q1, q2):
+        p.requires_grad_(True)
+    for s in range(5):
+        g = torch.randn_like(p1)
+        h = torch.randn_like(q1)
+        p1.grad, p2.grad = g.clone(), g.clone()
+        q1.grad, q2.grad = h.clone(), h.clone()
+        a.step()
+        b.step()
+    assert (p1 - p2).abs().max().item() < 1e-6
+    assert (q1 - q2).abs().max().item() < 1e-6
+
+
+def test_training_reduces_loss(cuda):
+    c, r = synthetic.sphere_union(1)
+    net = seeded_model(num_lods=5, base_lod=2, seed=0).to(cuda).train()
+    opt = trainer.FusedAdam(net.parameters(), lr=1e-3)
+    losses = []
+    for it in range(60):
+        x, g = synthetic.training_batch(16384, c, r, seed=100 + it)
+        losses.append(trainer.step_geometry(net, opt, x.to(cuda), g.to(cuda)).item())
+    assert np.isfinite(losses).all()
+    assert losses[-1] < 0.5 * losses[0], losses[::10]
