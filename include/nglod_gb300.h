@@ -144,6 +144,24 @@ int nglod_sdf_bwd(const nglod_dense_model *model, const float *x, int64_t n, uin
                   const float *grad_preds, const float *feats, float *dfeat_scratch,
                   const nglod_dense_grads *grads, float *grad_x, nglod_stream_t stream);
 
+/* nglod_sdf_bwd for callers that cannot allocate device memory (a plugin
+ * whose GPU memory is owned by its host application, a process whose
+ * allocator is locked after start-up): the same backward, but the per-point
+ * scratch comes from a fixed array inside the library instead of a
+ * caller-provided buffer, and the call allocates nothing.  No counterpart in
+ * the reference.
+ * Limit: (highest LOD in lod_mask + 1) * n * feature_dim floats must fit in
+ * NGLOD_NOALLOC_SCRATCH_BYTES (16 MiB on every GPU that loads the library,
+ * held until exit): n <= 26,214 with 5 LODs, 131,072 with one; larger n
+ * returns NGLOD_ERR_CAPACITY.  The first call on each device looks up the
+ * array's device address (cudaGetSymbolAddress), so make that first call
+ * before any stream capture.  All calls share the array: calls that overlap
+ * on the GPU race and must be serialised by the caller. */
+#define NGLOD_NOALLOC_SCRATCH_BYTES (16u << 20)
+int nglod_sdf_bwd_noalloc(const nglod_dense_model *model, const float *x, int64_t n, uint32_t lod_mask,
+                          const float *grad_preds, const float *feats, const nglod_dense_grads *grads,
+                          float *grad_x, nglod_stream_t stream);
+
 /* One tensor of a multi-tensor Adam step (device-resident table). */
 typedef struct nglod_adam_tensor {
     float       *param;

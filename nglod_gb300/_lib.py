@@ -90,6 +90,8 @@ SIGNATURES = {
     "nglod_sdf_fwd_train": (ctypes.c_int, [ctypes.POINTER(DenseModel), _vp, _i64, _u32, _vp, _vp, _vp]),
     "nglod_sdf_bwd": (ctypes.c_int, [ctypes.POINTER(DenseModel), _vp, _i64, _u32, _vp, _vp, _vp,
                                      ctypes.POINTER(DenseGrads), _vp, _vp]),
+    "nglod_sdf_bwd_noalloc": (ctypes.c_int, [ctypes.POINTER(DenseModel), _vp, _i64, _u32, _vp, _vp,
+                                             ctypes.POINTER(DenseGrads), _vp, _vp]),
     "nglod_adam_step": (ctypes.c_int, [_vp, _i32, _i64, _f32, _f32, _f32, _f32, _f32, _i64, _vp]),
 }
 

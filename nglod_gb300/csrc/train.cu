@@ -14,6 +14,8 @@
 //      scattered with the trilinear weights.  The coarsest volumes
 //      (5^3 and 9^3 vertices at base_lod 2) are accumulated in shared memory
 //      per block and flushed once; finer ones use red.global.add.v4.f32.
+#include <mutex>
+
 #include "dense_common.cuh"
 
 namespace nglod {
@@ -503,4 +505,78 @@ extern "C" int nglod_adam_step(const nglod_adam_tensor *tensors, int32_t count, 
                                                             (float)(1.0 - (double)beta1), (float)(1.0 - (double)beta2),
                                                             (float)sqrt(bc2), eps, weight_decay);
     return launch_status("nglod_adam_step");
+}
+
+// ---------------------------------------------------------------------------
+// Backward for callers that cannot allocate device memory
+// ---------------------------------------------------------------------------
+// nglod_sdf_bwd needs a per-point scratch buffer (dLoss/d(feature sum) for
+// every point and LOD) that the caller allocates.  Some callers cannot call
+// cudaMalloc at all: a plugin or engine whose GPU memory belongs to a host
+// runtime that hands out only the buffers it manages (inputs and outputs),
+// or a process whose allocator is locked after start-up.  For them,
+// nglod_sdf_bwd_noalloc takes that scratch from a fixed array compiled into
+// this library, so the call needs nothing beyond its inputs and outputs and
+// itself calls no allocator.
+//
+// The array is 16 MiB on every GPU that loads the library and stays there
+// until the process exits.  It holds (L+1) * n * 32 floats, so one call
+// covers at most 131,072 point-LODs (26,214 points when all 5 LODs of the
+// reference architecture carry a loss); larger calls are rejected.  All calls
+// share the one array: calls that run at the same time on the GPU (different
+// streams, or different host threads on one device) overwrite each other's
+// scratch and must be serialised by the caller.  Nothing in the array has to
+// start at zero: each call writes every element it later reads.
+namespace nglod {
+
+constexpr size_t kNoAllocScratchFloats = (size_t)4 << 20;  // 16 MiB of float32
+
+static __device__ __align__(256) float g_bwd_noalloc_scratch[kNoAllocScratchFloats];
+
+constexpr int kNoAllocMaxDevices = 64;
+static float *g_bwd_noalloc_addr[kNoAllocMaxDevices] = {nullptr};
+static std::mutex g_bwd_noalloc_mutex;
+
+// Device address of the array on the current device, looked up on the first
+// call made on that device (the symbol's host-side name is not a device
+// address and must never be passed to a kernel).
+static int noalloc_scratch_address(float **out) {
+    int dev = -1;
+    NGLOD_TRY(cuda_status(cudaGetDevice(&dev), "nglod_sdf_bwd_noalloc: cudaGetDevice"));
+    NGLOD_REQUIRE(dev >= 0 && dev < kNoAllocMaxDevices, NGLOD_ERR_UNSUPPORTED,
+                  "nglod_sdf_bwd_noalloc: device %d beyond the %d supported", dev, kNoAllocMaxDevices);
+    std::lock_guard<std::mutex> lock(g_bwd_noalloc_mutex);
+    if (g_bwd_noalloc_addr[dev] == nullptr) {
+        void *p = nullptr;
+        NGLOD_TRY(cuda_status(cudaGetSymbolAddress(&p, g_bwd_noalloc_scratch),
+                              "nglod_sdf_bwd_noalloc: cudaGetSymbolAddress"));
+        g_bwd_noalloc_addr[dev] = static_cast<float *>(p);
+    }
+    *out = g_bwd_noalloc_addr[dev];
+    return NGLOD_OK;
+}
+
+}  // namespace nglod
+
+extern "C" int nglod_sdf_bwd_noalloc(const nglod_dense_model *model, const float *x, int64_t n,
+                                     uint32_t lod_mask, const float *grad_preds, const float *feats,
+                                     const nglod_dense_grads *grads, float *grad_x, nglod_stream_t stream) {
+    NGLOD_REQUIRE(model != nullptr && grads != nullptr, NGLOD_ERR_INVALID, "model or grads is null");
+    const int L = lod_mask_top(lod_mask);
+    NGLOD_REQUIRE(L >= 0 && L < model->num_lods && (lod_mask >> NGLOD_MAX_LODS) == 0, NGLOD_ERR_INVALID,
+                  "lod_mask=0x%x selects no LOD or a LOD >= num_lods=%d", lod_mask, model->num_lods);
+    NGLOD_REQUIRE(n >= 0, NGLOD_ERR_INVALID, "n=%lld is negative", (long long)n);
+    NGLOD_REQUIRE(model->feature_dim == kC, NGLOD_ERR_UNSUPPORTED, "feature_dim=%d not built (only %d)",
+                  model->feature_dim, kC);
+    const size_t per_point = (size_t)(L + 1) * kC;
+    NGLOD_REQUIRE((size_t)n <= kNoAllocScratchFloats / per_point, NGLOD_ERR_CAPACITY,
+                  "nglod_sdf_bwd_noalloc: n=%lld points x %d LODs needs %zu scratch floats, the built-in "
+                  "array holds %zu (16 MiB): at most %zu points for this lod_mask; use nglod_sdf_bwd with "
+                  "caller-provided scratch for larger batches",
+                  (long long)n, L + 1, (size_t)n * per_point, kNoAllocScratchFloats,
+                  kNoAllocScratchFloats / per_point);
+    if (n == 0) return NGLOD_OK;
+    float *scratch = nullptr;
+    NGLOD_TRY(noalloc_scratch_address(&scratch));
+    return nglod_sdf_bwd(model, x, n, lod_mask, grad_preds, feats, scratch, grads, grad_x, stream);
 }
