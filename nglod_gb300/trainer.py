@@ -16,7 +16,7 @@ from . import _lib
 class FusedAdam(torch.optim.Optimizer):
     def __init__(self, params, lr=1e-3, betas=(0.9, 0.999), eps=1e-8, weight_decay=0.0):
         super().__init__(params, dict(lr=lr, betas=betas, eps=eps, weight_decay=weight_decay))
-        self._host_table = None
+        self._tables = []  # device copies of recent step tables, kept alive until their kernels ran
 
     @torch.no_grad()
     def step(self, closure=None):
@@ -63,9 +63,9 @@ class FusedAdam(torch.optim.Optimizer):
                                                    max(p.numel() for p, *_ in entries), group["lr"], b1, b2,
                                                    group["eps"], group["weight_decay"], step_no,
                                                    _lib.stream_ptr(dev)), "nglod_adam_step")
-            group.setdefault("_tables", []).append(dtab)  # keep alive until the stream has used it
-            if len(group["_tables"]) > 4:
-                group["_tables"].pop(0)
+            self._tables.append(dtab)
+            if len(self._tables) > 8:
+                self._tables.pop(0)
         return loss
 
 
