@@ -181,6 +181,79 @@ typedef struct nglod_adam_tensor {
 int nglod_adam_step(const nglod_adam_tensor *tensors, int32_t count, int64_t max_numel, float lr, float beta1,
                     float beta2, float eps, float weight_decay, int64_t step, nglod_stream_t stream);
 
+/* ------------------------------------------------------------------------
+ * Structured point cloud (SPC) octree: build, decode, ray traversal.
+ *
+ * An octree of `level` levels is the sequence of child-occupancy bytes of
+ * every occupied node of levels 0..level-1, level by level, each level in
+ * Morton order (bit j of a node's byte = child j, j = 4*x + 2*y + z of the
+ * child's offset).  Points are int16 [psize][4] (x, y, z, 0), all levels
+ * concatenated (level 0 = the root).  pyramid is int32 [2][level+2]:
+ * row 0 = points per level (then 0), row 1 = exclusive prefix sums
+ * (row1[level+1] = psize).  Same formats as sol-renderer's SPC
+ * (include/spc/spc/SPC.h:65-138, SPC.cu:148-238) and spc3d.SPC3D.
+ * ------------------------------------------------------------------------ */
+
+/* Octree from leaf voxels: pts[n][3] uint16 at `level` (duplicates allowed,
+ * any order).  Writes octree bytes (capacity octree_cap), their count to
+ * *osize, and pyramid[2][level+2].  scratch: at least
+ * nglod_spc_build_scratch_bytes(level) bytes.  Bit-exact with
+ * spc3d.SPC3D.points_to_nodes after Morton sorting (sdf-net/lib/spc3d.py:224-255).
+ * Synchronises the stream once to return the sizes. */
+int64_t nglod_spc_build_scratch_bytes(int32_t level);
+int nglod_spc_build(const uint16_t *pts, int64_t n, int32_t level, uint8_t *octree, int64_t octree_cap,
+                    int64_t *osize, int32_t *pyramid_host, void *scratch, nglod_stream_t stream);
+
+/* SPC::SetGeometry (SPC.cu:148-238): octree bytes -> points[psize][4] int16
+ * (capacity points_cap), exclusive prefix sums of child counts
+ * prefix[osize+1] (prefix[k] = number of children of nodes before k; the
+ * table the traversal addresses children with), and pyramid[2][level+2].
+ * Synchronises the stream once to return the level sizes. */
+int nglod_spc_decode(const uint8_t *octree, int64_t osize, int16_t *points, int64_t points_cap,
+                     uint32_t *prefix, int32_t *pyramid_host, int32_t *level_out, nglod_stream_t stream);
+
+/* spc_raytrace (include/spc/spc/spc_raytrace_cuda.cpp:141-199,
+ * spc_raytrace_cuda_kernel.cu:194-265): level-by-level ray/voxel tests of
+ * rays org/dir [n][3] against the octree down to target_level, children
+ * expanded front to back.  Output: nuggets (ray index, level-local voxel
+ * index) of every voxel at target_level the ray's line passes through, per
+ * ray front to back, rays in order -- bit-exact with the reference.  All
+ * levels run on the device with no host round trip.
+ * nuggets_a/nuggets_b: two int32 [capacity][2] buffers; info, partials:
+ * uint32 [capacity] and [capacity/1024 + 2]; ctrl: int64
+ * [NGLOD_SPC_CTRL_WORDS] device.
+ * On return (the call synchronises once) *count = number of nuggets and
+ * *result_buffer = 0 (nuggets_a) or 1 (nuggets_b) holds them.  More than
+ * `capacity` nuggets at any level: NGLOD_ERR_CAPACITY (the reference
+ * truncated silently). */
+/* Exclusive prefix sums of child counts over all octree bytes:
+ * prefix[k] = sum of popcount(octree[i]) for i < k, k in [0, osize]; the
+ * table the reference recomputes on every spc_raytrace call with CUB
+ * (spc_raytrace_cuda_kernel.cu:226-227).  partials: uint32
+ * [osize/1024 + 2]; ctrl: int64 [2].  Asynchronous. */
+int nglod_spc_prefix(const uint8_t *octree, int64_t osize, uint32_t *prefix, uint32_t *partials, int64_t *ctrl,
+                     nglod_stream_t stream);
+
+#define NGLOD_SPC_CTRL_WORDS 20
+int nglod_spc_raytrace(const uint8_t *octree, const int16_t *points, const uint32_t *prefix,
+                       const int32_t *pyramid_host, int32_t level, int32_t target_level,
+                       const float *org, const float *dir, int64_t n_rays,
+                       int32_t *nuggets_a, int32_t *nuggets_b, int64_t capacity, uint32_t *info,
+                       uint32_t *partials, int64_t *ctrl, int64_t *count, int32_t *result_buffer,
+                       nglod_stream_t stream);
+
+/* d_MarkUniqueRays (sol-renderer/sdfRenderer.cu:108-120): info[i] = 1 where
+ * nugget i is its ray's first, else 0. */
+int nglod_spc_mark_first(const int32_t *nuggets, int64_t n, int32_t *info, nglod_stream_t stream);
+
+/* spc_generate_primary_rays (spc_raytrace_cuda.cpp:65-121, kernel
+ * spc_raytrace_cuda_kernel.cu:271-287): pinhole rays of a width x height
+ * image from the 4x4 inverse view-projection matrix inv_wvp (row-major,
+ * row-vector convention); directions are not normalised, as in the
+ * reference. */
+int nglod_spc_generate_rays(const float *inv_wvp_host, int32_t width, int32_t height, float *org, float *dir,
+                            nglod_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

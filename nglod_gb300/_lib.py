@@ -92,6 +92,14 @@ SIGNATURES = {
                                      ctypes.POINTER(DenseGrads), _vp, _vp]),
     "nglod_sdf_bwd_noalloc": (ctypes.c_int, [ctypes.POINTER(DenseModel), _vp, _i64, _u32, _vp, _vp,
                                              ctypes.POINTER(DenseGrads), _vp, _vp]),
+    "nglod_spc_build_scratch_bytes": (_i64, [_i32]),
+    "nglod_spc_build": (ctypes.c_int, [_vp, _i64, _i32, _vp, _i64, ctypes.POINTER(_i64), _vp, _vp, _vp]),
+    "nglod_spc_decode": (ctypes.c_int, [_vp, _i64, _vp, _i64, _vp, _vp, ctypes.POINTER(_i32), _vp]),
+    "nglod_spc_prefix": (ctypes.c_int, [_vp, _i64, _vp, _vp, _vp, _vp]),
+    "nglod_spc_raytrace": (ctypes.c_int, [_vp, _vp, _vp, _vp, _i32, _i32, _vp, _vp, _i64, _vp, _vp, _i64, _vp,
+                                          _vp, _vp, ctypes.POINTER(_i64), ctypes.POINTER(_i32), _vp]),
+    "nglod_spc_mark_first": (ctypes.c_int, [_vp, _i64, _vp, _vp]),
+    "nglod_spc_generate_rays": (ctypes.c_int, [_vp, _i32, _i32, _vp, _vp, _vp]),
     "nglod_adam_step": (ctypes.c_int, [_vp, _i32, _i64, _f32, _f32, _f32, _f32, _f32, _i64, _vp]),
 }
 

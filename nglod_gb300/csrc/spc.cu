@@ -1,0 +1,695 @@
+// Structured point cloud (SPC) octree: build from voxels, decode, and the
+// level-by-level ray/octree traversal of sol-renderer's spc_raytrace.
+//
+// Every variable-length step is a stream compaction done with "chunk scans":
+// a chunk is 1024 consecutive elements handled by one 1024-thread block
+// iteration; pass 1 reduces each chunk to a count, pass 2 (one block) turns
+// the counts into exclusive chunk offsets and the total, pass 3 rescans each
+// chunk and writes its survivors.  Element counts of every level live in a
+// small device control block, so the traversal of all levels is enqueued
+// without any host round trip; the host reads the result once at the end.
+#include <stdio.h>
+
+#include <vector>
+
+#include "common.cuh"
+
+namespace nglod {
+
+constexpr int kChunk = 1024;
+constexpr int kMaxSpcLevels = 15;
+constexpr int kCtrlStatus = 0;   // 0 ok, 1 capacity exceeded
+constexpr int kCtrlCount = 4;    // count of level l at kCtrlCount + l
+
+// ---------------------------------------------------------------------------
+// block scan helpers (blockDim.x == kChunk)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t *s_warp, uint32_t *total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) s_warp[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = s_warp[lane];
+        uint32_t wi = w;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, wi, o);
+            if (lane >= o) wi += y;
+        }
+        s_warp[lane] = wi - w;  // exclusive prefix of warp totals
+        if (lane == 31) s_warp[32] = wi;
+    }
+    __syncthreads();
+    const uint32_t r = s_warp[warp] + x - v;
+    *total = s_warp[32];
+    __syncthreads();
+    return r;
+}
+
+__device__ __forceinline__ uint32_t block_sum(uint32_t v, uint32_t *s_warp) {
+    uint32_t t;
+    block_exclusive_scan(v, s_warp, &t);
+    return t;
+}
+
+// Pass 2: exclusive scan of `nchunks` chunk counts in place, in one block.
+// The total goes to *total_out (and, if over `capacity`, raises the status).
+__global__ void __launch_bounds__(kChunk) scan_chunk_counts_kernel(uint32_t *partials, const int64_t *count_in,
+                                                                   int64_t *total_out, int64_t capacity,
+                                                                   int64_t *status) {
+    __shared__ uint32_t s_warp[33];
+    const int64_t count = *count_in;
+    const int64_t nchunks = (count + kChunk - 1) / kChunk;
+    uint64_t carry = 0;
+    for (int64_t base = 0; base < nchunks; base += kChunk) {
+        const int64_t i = base + threadIdx.x;
+        const uint32_t v = i < nchunks ? partials[i] : 0u;
+        uint32_t tot;
+        const uint32_t ex = block_exclusive_scan(v, s_warp, &tot);
+        if (i < nchunks) partials[i] = (uint32_t)(carry + ex);
+        carry += tot;
+    }
+    if (threadIdx.x == 0) {
+        *total_out = (int64_t)carry;
+        if ((int64_t)carry > capacity && status) *status = 1;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// front-to-back child order
+// ---------------------------------------------------------------------------
+// Children of a voxel visited by a ray whose origin lies in octant `code`
+// (4*[x > centre] + 2*[y > centre] + [z > centre]) come nearest first: sorted
+// by the Hamming distance of their octant index to `code`, ties by index.
+// This reproduces the Order table of spc_raytrace_cuda_kernel.cu:39-47.
+__host__ __device__ inline uint32_t child_order(uint32_t code, uint32_t rank) {
+    uint32_t seen = 0;
+    for (uint32_t dist = 0; dist <= 3; ++dist)
+        for (uint32_t j = 0; j < 8; ++j)
+            if ((uint32_t)__builtin_popcount(j ^ code) == dist) {
+                if (seen == rank) return j;
+                ++seen;
+            }
+    return 0;
+}
+
+struct OrderTable {
+    unsigned char o[8][8];
+};
+
+static OrderTable make_order_table() {
+    OrderTable t;
+    for (uint32_t c = 0; c < 8; ++c)
+        for (uint32_t r = 0; r < 8; ++r) t.o[c][r] = (unsigned char)child_order(c, r);
+    return t;
+}
+
+// ---------------------------------------------------------------------------
+// ray / voxel test (d_Decide, d_FaceEval of spc_raytrace_cuda_kernel.cu:85-138)
+// ---------------------------------------------------------------------------
+// The ray is mapped to [0,1]^3 (o' = o/2 + 1/2, d' = d/2); the voxel (i, j)
+// square of each coordinate plane is tested against the line's 2-D edge
+// function a*i + b*j + c at its four corners.  Arithmetic order: the
+// reference source compiled with nvcc's default contraction, i.e.
+// c0 = fma(a, i, b*j) + c, c1 = c0 + a, c2 = c0 + b, c3 = c1 + b, and
+// o' x d' with each component fma(u, v, -(w*z)).
+__device__ __forceinline__ bool face_straddles(float fi, float fj, float a, float b, float c) {
+    const float r0 = __fadd_rn(__fmaf_rn(a, fi, __fmul_rn(b, fj)), c);
+    const float r1 = __fadd_rn(r0, a);
+    const float r2 = __fadd_rn(r0, b);
+    const float r3 = __fadd_rn(r1, b);
+    float mn = 1.f, mx = -1.f;
+    mn = r0 < mn ? r0 : mn;
+    mx = r0 > mx ? r0 : mx;
+    mn = r1 < mn ? r1 : mn;
+    mx = r1 > mx ? r1 : mx;
+    mn = r2 < mn ? r2 : mn;
+    mx = r2 > mx ? r2 : mx;
+    mn = r3 < mn ? r3 : mn;
+    mx = r3 > mx ? r3 : mx;
+    return mn <= 0.f && mx >= 0.f;
+}
+
+__device__ __forceinline__ bool ray_hits_voxel(const float *__restrict__ org, const float *__restrict__ dir,
+                                               uint32_t ridx, short4 p, int level) {
+    const float ox = __fmaf_rn(0.5f, org[3 * ridx], 0.5f);
+    const float oy = __fmaf_rn(0.5f, org[3 * ridx + 1], 0.5f);
+    const float oz = __fmaf_rn(0.5f, org[3 * ridx + 2], 0.5f);
+    const float dx = __fmul_rn(0.5f, dir[3 * ridx]);
+    const float dy = __fmul_rn(0.5f, dir[3 * ridx + 1]);
+    const float dz = __fmul_rn(0.5f, dir[3 * ridx + 2]);
+    const float cx = __fmaf_rn(oy, dz, -__fmul_rn(dy, oz));
+    const float cy = __fmaf_rn(oz, dx, -__fmul_rn(dz, ox));
+    const float cz = __fmaf_rn(ox, dy, -__fmul_rn(dx, oy));
+    const float s1 = ldexpf(1.f, -level);
+    const float s2 = __fmul_rn(s1, s1);
+    const float px = (float)(unsigned short)p.x, py = (float)(unsigned short)p.y, pz = (float)(unsigned short)p.z;
+    return face_straddles(py, pz, __fmul_rn(-s2, dz), __fmul_rn(s2, dy), __fmul_rn(s1, cx)) &&
+           face_straddles(px, pz, __fmul_rn(s2, dz), __fmul_rn(-s2, dx), __fmul_rn(s1, cy)) &&
+           face_straddles(px, py, __fmul_rn(-s2, dy), __fmul_rn(s2, dx), __fmul_rn(s1, cz));
+}
+
+// Octant of the ray origin relative to the voxel centre (d_Subdivide,
+// spc_raytrace_cuda_kernel.cu:157-167): the reference forms
+// (0.5*o + 0.5) - scale*(p + 0.5) in double, so only the comparison matters.
+__device__ __forceinline__ uint32_t origin_octant(const float *__restrict__ org, uint32_t ridx, short4 p,
+                                                  int level) {
+    const double sc = ldexp(1.0, -level);
+    const double ax = (double)__fmaf_rn(0.5f, org[3 * ridx], 0.5f);
+    const double ay = (double)__fmaf_rn(0.5f, org[3 * ridx + 1], 0.5f);
+    const double az = (double)__fmaf_rn(0.5f, org[3 * ridx + 2], 0.5f);
+    uint32_t code = 0;
+    if ((float)(ax - sc * ((double)p.x + 0.5)) > 0.f) code = 4;
+    if ((float)(ay - sc * ((double)p.y + 0.5)) > 0.f) code += 2;
+    if ((float)(az - sc * ((double)p.z + 0.5)) > 0.f) code += 1;
+    return code;
+}
+
+// ---------------------------------------------------------------------------
+// traversal kernels
+// ---------------------------------------------------------------------------
+struct TraverseArgs {
+    const uint8_t *octree;
+    const short4 *points;  // all levels
+    const uint32_t *prefix;
+    const float *org;
+    const float *dir;
+    const int2 *in;  // nuggets of this level (unused at level 0)
+    int2 *out;
+    uint32_t *info;
+    uint32_t *partials;
+    int64_t *ctrl;
+    int64_t capacity;
+    int level;       // current level
+    int target;      // target level
+    int64_t off0;    // global point index of this level's first point
+    int64_t off1;    // ... of the next level's
+    OrderTable order;
+};
+
+__device__ __forceinline__ int2 nugget_at(const TraverseArgs &a, int64_t i) {
+    if (a.level == 0) return make_int2((int)i, 0);
+    return a.in[i];
+}
+
+__global__ void __launch_bounds__(kChunk) traverse_decide_kernel(const TraverseArgs a) {
+    __shared__ uint32_t s_warp[33];
+    if (a.ctrl[kCtrlStatus] != 0) return;
+    const int64_t count = a.ctrl[kCtrlCount + a.level];
+    const int64_t nchunks = (count + kChunk - 1) / kChunk;
+    for (int64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
+        const int64_t i = c * kChunk + threadIdx.x;
+        uint32_t v = 0;
+        if (i < count) {
+            const int2 nug = nugget_at(a, i);
+            const short4 p = a.points[a.off0 + nug.y];
+            if (ray_hits_voxel(a.org, a.dir, (uint32_t)nug.x, p, a.level))
+                v = a.level < a.target ? (uint32_t)__popc(a.octree[a.off0 + nug.y]) : 1u;
+            a.info[i] = v;
+        }
+        const uint32_t s = block_sum(v, s_warp);
+        if (threadIdx.x == 0) a.partials[c] = s;
+    }
+}
+
+__global__ void __launch_bounds__(kChunk) traverse_emit_kernel(const TraverseArgs a) {
+    __shared__ uint32_t s_warp[33];
+    if (a.ctrl[kCtrlStatus] != 0) return;
+    const int64_t count = a.ctrl[kCtrlCount + a.level];
+    const int64_t nchunks = (count + kChunk - 1) / kChunk;
+    for (int64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
+        const int64_t i = c * kChunk + threadIdx.x;
+        const uint32_t v = i < count ? a.info[i] : 0u;
+        uint32_t tot;
+        const uint32_t ex = block_exclusive_scan(v, s_warp, &tot);
+        if (v == 0) continue;
+        int64_t pos = (int64_t)a.partials[c] + ex;
+        const int2 nug = nugget_at(a, i);
+        if (a.level == a.target) {
+            a.out[pos] = nug;
+            continue;
+        }
+        const short4 p = a.points[a.off0 + nug.y];
+        const uint32_t o = a.octree[a.off0 + nug.y];
+        const uint32_t s = a.prefix[a.off0 + nug.y];
+        const uint32_t code = origin_octant(a.org, (uint32_t)nug.x, p, a.level);
+        for (int r = 0; r < 8; ++r) {
+            const uint32_t j = a.order.o[code][r];
+            if (o & (1u << j)) {
+                const uint32_t cnt = __popc(o & ((2u << j) - 1u));
+                a.out[pos++] = make_int2(nug.x, (int)((int64_t)s + cnt - a.off1));
+            }
+        }
+    }
+}
+
+__global__ void mark_first_kernel(const int2 *__restrict__ nug, int64_t n, int32_t *__restrict__ info) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+        info[i] = (i == 0 || nug[i - 1].x != nug[i].x) ? 1 : 0;
+}
+
+// ---------------------------------------------------------------------------
+// decode (SPC::SetGeometry)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kChunk) popc_chunk_kernel(const uint8_t *__restrict__ oct, const int64_t *count,
+                                                            uint32_t *partials) {
+    __shared__ uint32_t s_warp[33];
+    const int64_t n = *count;
+    const int64_t nchunks = (n + kChunk - 1) / kChunk;
+    for (int64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
+        const int64_t i = c * kChunk + threadIdx.x;
+        const uint32_t v = i < n ? (uint32_t)__popc(oct[i]) : 0u;
+        const uint32_t s = block_sum(v, s_warp);
+        if (threadIdx.x == 0) partials[c] = s;
+    }
+}
+
+// prefix[i] = children of nodes before i, for i in [0, n] (n + 1 entries; the
+// count passed covers n + 1 elements, byte n reads as 0).
+__global__ void __launch_bounds__(kChunk) popc_prefix_kernel(const uint8_t *__restrict__ oct, int64_t nbytes,
+                                                             const int64_t *count, const uint32_t *partials,
+                                                             uint32_t *prefix) {
+    __shared__ uint32_t s_warp[33];
+    const int64_t n = *count;
+    const int64_t nchunks = (n + kChunk - 1) / kChunk;
+    for (int64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
+        const int64_t i = c * kChunk + threadIdx.x;
+        const uint32_t v = i < nbytes ? (uint32_t)__popc(oct[i]) : 0u;
+        uint32_t tot;
+        const uint32_t ex = block_exclusive_scan(v, s_warp, &tot);
+        if (i < n) prefix[i] = partials[c] + ex;
+    }
+}
+
+// Level sizes from the prefix table: level 0 = the root; level l+1 has
+// prefix[end_l] - prefix[start_l] nodes.  out[0..levels] = counts,
+// out[kMaxSpcLevels+1] = number of levels (the leaf level index).
+__global__ void level_sizes_kernel(const uint32_t *prefix, int64_t osize, int64_t *out) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    int64_t start = 0, cnt = 1;
+    int l = 0;
+    out[0] = 1;
+    while (start < osize && l < kMaxSpcLevels) {
+        const int64_t end = start + cnt;
+        const int64_t next = (int64_t)prefix[end < osize ? end : osize] - (int64_t)prefix[start];
+        start = end;
+        cnt = next;
+        ++l;
+        out[l] = cnt;
+    }
+    out[kMaxSpcLevels + 1] = (start == osize) ? l : -1;
+}
+
+// Children Morton codes of one level's nodes; codes are staged in the points
+// buffer itself (8 bytes per point) and converted to coordinates at the end.
+__global__ void nodes_to_morton_kernel(const uint8_t *__restrict__ oct, const uint32_t *__restrict__ prefix,
+                                       uint64_t *codes, int64_t start, int64_t cnt) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < cnt; k += stride) {
+        const int64_t node = start + k;
+        const uint32_t bits = oct[node];
+        const uint64_t m = codes[node];
+        int64_t addr = 1 + (int64_t)prefix[node];
+        for (int j = 0; j < 8; ++j)
+            if (bits & (1u << j)) codes[addr++] = 8ull * m + (uint64_t)j;
+    }
+}
+
+__global__ void morton_to_points_kernel(uint64_t *codes_then_points, int64_t n) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const uint64_t m = codes_then_points[i];
+        uint32_t x = 0, y = 0, z = 0;
+        for (int b = 0; b < 16; ++b) {
+            x |= (uint32_t)((m >> (3 * b + 2)) & 1u) << b;
+            y |= (uint32_t)((m >> (3 * b + 1)) & 1u) << b;
+            z |= (uint32_t)((m >> (3 * b)) & 1u) << b;
+        }
+        short4 p = make_short4((short)x, (short)y, (short)z, 0);
+        reinterpret_cast<short4 *>(codes_then_points)[i] = p;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// build (points -> octree)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint64_t morton3(uint32_t x, uint32_t y, uint32_t z) {
+    uint64_t m = 0;
+    for (int b = 0; b < 16; ++b) {
+        m |= (uint64_t)((z >> b) & 1u) << (3 * b);
+        m |= (uint64_t)((y >> b) & 1u) << (3 * b + 1);
+        m |= (uint64_t)((x >> b) & 1u) << (3 * b + 2);
+    }
+    return m;
+}
+
+__global__ void mark_leaves_kernel(const uint16_t *__restrict__ pts, int64_t n, int level, uint8_t *occ,
+                                   int64_t *status) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const uint32_t lim = 1u << level;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const uint32_t x = pts[3 * i], y = pts[3 * i + 1], z = pts[3 * i + 2];
+        if (x >= lim || y >= lim || z >= lim) {
+            *status = 2;
+            continue;
+        }
+        occ[morton3(x, y, z)] = 1;
+    }
+}
+
+// Child-occupancy byte of every node of a level from the next level's bytes
+// (or leaf occupancy): byte[m] = sum_j [child 8m+j occupied] << j.
+__global__ void reduce_level_kernel(const uint8_t *__restrict__ child, int64_t nparents, uint8_t *__restrict__ bytes) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; m < nparents; m += stride) {
+        const uint2 c = reinterpret_cast<const uint2 *>(child)[m];  // 8 child entries
+        uint32_t b = 0;
+        for (int j = 0; j < 4; ++j) {
+            if ((c.x >> (8 * j)) & 0xffu) b |= 1u << j;
+            if ((c.y >> (8 * j)) & 0xffu) b |= 1u << (j + 4);
+        }
+        bytes[m] = (uint8_t)b;
+    }
+}
+
+__global__ void __launch_bounds__(kChunk) nonzero_chunk_kernel(const uint8_t *__restrict__ v, const int64_t *count,
+                                                               uint32_t *partials) {
+    __shared__ uint32_t s_warp[33];
+    const int64_t n = *count;
+    const int64_t nchunks = (n + kChunk - 1) / kChunk;
+    for (int64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
+        const int64_t i = c * kChunk + threadIdx.x;
+        const uint32_t f = (i < n && v[i]) ? 1u : 0u;
+        const uint32_t s = block_sum(f, s_warp);
+        if (threadIdx.x == 0) partials[c] = s;
+    }
+}
+
+__global__ void __launch_bounds__(kChunk) nonzero_emit_kernel(const uint8_t *__restrict__ v, const int64_t *count,
+                                                              const uint32_t *partials, uint8_t *out,
+                                                              int64_t out_cap, int64_t *status) {
+    __shared__ uint32_t s_warp[33];
+    const int64_t n = *count;
+    const int64_t nchunks = (n + kChunk - 1) / kChunk;
+    for (int64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
+        const int64_t i = c * kChunk + threadIdx.x;
+        const uint32_t f = (i < n && v[i]) ? 1u : 0u;
+        uint32_t tot;
+        const uint32_t ex = block_exclusive_scan(f, s_warp, &tot);
+        if (f) {
+            const int64_t pos = (int64_t)partials[c] + ex;
+            if (pos < out_cap)
+                out[pos] = v[i];
+            else
+                *status = 1;
+        }
+    }
+}
+
+inline int grid_for(int64_t chunks) {
+    const int64_t cap = (int64_t)num_sms() * 2;
+    if (chunks < 1) chunks = 1;
+    return (int)(chunks < cap ? chunks : cap);
+}
+
+inline int grid_elems(int64_t n, int threads = 256) {
+    const int64_t want = (n + threads - 1) / threads;
+    const int64_t cap = (int64_t)num_sms() * 16;
+    return (int)(want < 1 ? 1 : (want < cap ? want : cap));
+}
+
+}  // namespace nglod
+
+using namespace nglod;
+
+// Scratch layout of nglod_spc_build: one dense byte array per level l
+// (8^l entries, each array starting on a 256-byte boundary so that the
+// 8-children reads are aligned), then the chunk partials, then a control
+// block of 64 int64.
+static int64_t level_array_offset(int l) {
+    int64_t t = 0;
+    for (int k = 0; k < l; ++k) t += (((int64_t)1 << (3 * k)) + 255) & ~(int64_t)255;
+    return t;
+}
+static int64_t build_dense_bytes(int level) { return level_array_offset(level + 1); }
+
+extern "C" int64_t nglod_spc_build_scratch_bytes(int32_t level) {
+    if (level < 1 || level > 9) return -1;
+    const int64_t dense = build_dense_bytes(level);
+    const int64_t parts = ((int64_t)1 << (3 * level)) / kChunk + 2;
+    return dense + ((parts * 4 + 255) & ~(int64_t)255) + 64 * 8;
+}
+
+extern "C" int nglod_spc_build(const uint16_t *pts, int64_t n, int32_t level, uint8_t *octree, int64_t octree_cap,
+                               int64_t *osize, int32_t *pyramid_host, void *scratch, nglod_stream_t stream) {
+    NGLOD_REQUIRE(level >= 1 && level <= 9, NGLOD_ERR_UNSUPPORTED, "octree level=%d outside [1, 9]", level);
+    NGLOD_REQUIRE(n >= 1, NGLOD_ERR_INVALID, "n=%lld: an octree needs at least one voxel", (long long)n);
+    NGLOD_REQUIRE(pts && octree && osize && pyramid_host && scratch, NGLOD_ERR_INVALID, "null pointer argument");
+    NGLOD_REQUIRE(aligned(scratch, 256), NGLOD_ERR_ALIGN, "scratch must be 256-byte aligned");
+    cudaStream_t s = (cudaStream_t)stream;
+    const int64_t dense = build_dense_bytes(level);
+    uint8_t *base = static_cast<uint8_t *>(scratch);
+    // level l's dense array starts at off[l]; leaf level last
+    std::vector<int64_t> off(level + 1);
+    for (int l = 0; l <= level; ++l) off[l] = level_array_offset(l);
+    uint32_t *partials = reinterpret_cast<uint32_t *>(base + dense);
+    const int64_t parts = ((int64_t)1 << (3 * level)) / kChunk + 2;
+    int64_t *ctrl = reinterpret_cast<int64_t *>(base + dense + ((parts * 4 + 255) & ~(int64_t)255));
+    NGLOD_TRY(cuda_status(cudaMemsetAsync(base, 0, (size_t)dense, s), "nglod_spc_build memset"));
+    NGLOD_TRY(cuda_status(cudaMemsetAsync(ctrl, 0, 64 * sizeof(int64_t), s), "nglod_spc_build memset"));
+    mark_leaves_kernel<<<grid_elems(n), 256, 0, s>>>(pts, n, level, base + off[level], ctrl);
+    for (int l = level - 1; l >= 0; --l)
+        reduce_level_kernel<<<grid_elems((int64_t)1 << (3 * l)), 256, 0, s>>>(base + off[l + 1],
+                                                                            (int64_t)1 << (3 * l), base + off[l]);
+    NGLOD_TRY(launch_status("nglod_spc_build (levels)"));
+    // Compact each level's nonzero bytes in Morton order; counts of levels
+    // 0..level (level = occupied leaves) go to ctrl[8 + l].
+    int64_t *status = ctrl;
+    std::vector<int64_t> counts(level + 1);
+    int64_t written = 0;
+    for (int l = 0; l <= level; ++l) {
+        const int64_t n_l = (int64_t)1 << (3 * l);
+        NGLOD_TRY(cuda_status(cudaMemcpyAsync(ctrl + 2, &n_l, sizeof(int64_t), cudaMemcpyHostToDevice, s),
+                              "nglod_spc_build copy"));
+        const int64_t chunks = (n_l + kChunk - 1) / kChunk;
+        nonzero_chunk_kernel<<<grid_for(chunks), kChunk, 0, s>>>(base + off[l], ctrl + 2, partials);
+        scan_chunk_counts_kernel<<<1, kChunk, 0, s>>>(partials, ctrl + 2, ctrl + 8 + l, INT64_MAX, nullptr);
+        if (l < level)
+            nonzero_emit_kernel<<<grid_for(chunks), kChunk, 0, s>>>(base + off[l], ctrl + 2, partials,
+                                                                    octree + written, octree_cap - written, status);
+        NGLOD_TRY(launch_status("nglod_spc_build (compact)"));
+        NGLOD_TRY(cuda_status(cudaMemcpyAsync(&counts[l], ctrl + 8 + l, sizeof(int64_t), cudaMemcpyDeviceToHost, s),
+                              "nglod_spc_build copy"));
+        NGLOD_TRY(cuda_status(cudaStreamSynchronize(s), "nglod_spc_build sync"));
+        if (l < level) written += counts[l];
+        NGLOD_REQUIRE(written <= octree_cap, NGLOD_ERR_CAPACITY, "octree needs more than %lld bytes",
+                      (long long)octree_cap);
+    }
+    int64_t st = 0;
+    NGLOD_TRY(cuda_status(cudaMemcpy(&st, status, sizeof(int64_t), cudaMemcpyDeviceToHost), "nglod_spc_build copy"));
+    NGLOD_REQUIRE(st != 2, NGLOD_ERR_INVALID, "a voxel coordinate is >= 2^level");
+    NGLOD_REQUIRE(st == 0, NGLOD_ERR_CAPACITY, "octree capacity exceeded");
+    *osize = written;
+    int64_t sum = 0;
+    for (int l = 0; l <= level; ++l) {
+        pyramid_host[l] = (int32_t)counts[l];
+        pyramid_host[(level + 2) + l] = (int32_t)sum;
+        sum += counts[l];
+    }
+    pyramid_host[level + 1] = 0;
+    pyramid_host[(level + 2) + level + 1] = (int32_t)sum;
+    return NGLOD_OK;
+}
+
+extern "C" int nglod_spc_decode(const uint8_t *octree, int64_t osize, int16_t *points, int64_t points_cap,
+                                uint32_t *prefix, int32_t *pyramid_host, int32_t *level_out, nglod_stream_t stream) {
+    NGLOD_REQUIRE(osize >= 1, NGLOD_ERR_INVALID, "osize=%lld: empty octree", (long long)osize);
+    NGLOD_REQUIRE(octree && points && prefix && pyramid_host && level_out, NGLOD_ERR_INVALID,
+                  "null pointer argument");
+    NGLOD_REQUIRE(aligned(points, 8), NGLOD_ERR_ALIGN, "points must be 8-byte aligned");
+    cudaStream_t s = (cudaStream_t)stream;
+    // The scan's control block and chunk partials are staged in the points
+    // buffer (at least osize + 1 entries of 8 bytes), which is rewritten
+    // afterwards.
+    const int64_t nelem = osize + 1;
+    const int64_t chunks = (nelem + kChunk - 1) / kChunk;
+    NGLOD_REQUIRE(points_cap >= osize + 1 && points_cap * 8 >= (chunks + 2) * 4 + 64 * 8 + 8 * (kMaxSpcLevels + 2),
+                  NGLOD_ERR_CAPACITY, "points buffer of %lld entries is too small", (long long)points_cap);
+    uint8_t *tmp = reinterpret_cast<uint8_t *>(points);
+    int64_t *ctrl = reinterpret_cast<int64_t *>(tmp);
+    int64_t *sizes = ctrl + 8;
+    uint32_t *partials = reinterpret_cast<uint32_t *>(sizes + kMaxSpcLevels + 2);
+    NGLOD_TRY(cuda_status(cudaMemcpyAsync(ctrl, &nelem, sizeof(int64_t), cudaMemcpyHostToDevice, s), "decode copy"));
+    popc_chunk_kernel<<<grid_for(chunks), kChunk, 0, s>>>(octree, ctrl, partials);
+    scan_chunk_counts_kernel<<<1, kChunk, 0, s>>>(partials, ctrl, ctrl + 1, INT64_MAX, nullptr);
+    popc_prefix_kernel<<<grid_for(chunks), kChunk, 0, s>>>(octree, osize, ctrl, partials, prefix);
+    level_sizes_kernel<<<1, 32, 0, s>>>(prefix, osize, sizes);
+    NGLOD_TRY(launch_status("nglod_spc_decode (scan)"));
+    int64_t hs[kMaxSpcLevels + 2];
+    NGLOD_TRY(cuda_status(cudaMemcpyAsync(hs, sizes, sizeof(hs), cudaMemcpyDeviceToHost, s), "decode copy"));
+    NGLOD_TRY(cuda_status(cudaStreamSynchronize(s), "decode sync"));
+    const int64_t L = hs[kMaxSpcLevels + 1];
+    NGLOD_REQUIRE(L >= 1, NGLOD_ERR_INVALID, "octree bytes do not describe a complete tree of <= %d levels",
+                  kMaxSpcLevels);
+    int64_t psize = 0;
+    for (int l = 0; l <= L; ++l) psize += hs[l];
+    NGLOD_REQUIRE(psize <= points_cap, NGLOD_ERR_CAPACITY, "octree has %lld points, buffer holds %lld",
+                  (long long)psize, (long long)points_cap);
+    uint64_t *codes = reinterpret_cast<uint64_t *>(points);
+    NGLOD_TRY(cuda_status(cudaMemsetAsync(codes, 0, sizeof(uint64_t), s), "decode memset"));
+    int64_t start = 0;
+    for (int l = 0; l < L; ++l) {
+        nodes_to_morton_kernel<<<grid_elems(hs[l]), 256, 0, s>>>(octree, prefix, codes, start, hs[l]);
+        start += hs[l];
+    }
+    morton_to_points_kernel<<<grid_elems(psize), 256, 0, s>>>(codes, psize);
+    NGLOD_TRY(launch_status("nglod_spc_decode (points)"));
+    int64_t sum = 0;
+    for (int l = 0; l <= L; ++l) {
+        pyramid_host[l] = (int32_t)hs[l];
+        pyramid_host[(L + 2) + l] = (int32_t)sum;
+        sum += hs[l];
+    }
+    pyramid_host[L + 1] = 0;
+    pyramid_host[(L + 2) + L + 1] = (int32_t)sum;
+    *level_out = (int32_t)L;
+    return NGLOD_OK;
+}
+
+extern "C" int nglod_spc_raytrace(const uint8_t *octree, const int16_t *points, const uint32_t *prefix,
+                                  const int32_t *pyramid_host, int32_t level, int32_t target_level, const float *org,
+                                  const float *dir, int64_t n_rays, int32_t *nuggets_a, int32_t *nuggets_b,
+                                  int64_t capacity, uint32_t *info, uint32_t *partials, int64_t *ctrl, int64_t *count,
+                                  int32_t *result_buffer, nglod_stream_t stream) {
+    NGLOD_REQUIRE(level >= 1 && level < kMaxSpcLevels, NGLOD_ERR_INVALID, "level=%d outside [1, %d)", level,
+                  kMaxSpcLevels);
+    NGLOD_REQUIRE(target_level >= 0 && target_level <= level, NGLOD_ERR_INVALID,
+                  "target_level=%d outside [0, level=%d]", target_level, level);
+    NGLOD_REQUIRE(n_rays >= 0 && n_rays <= capacity && capacity <= ((int64_t)1 << 31) - 1, NGLOD_ERR_CAPACITY,
+                  "n_rays=%lld must not exceed capacity=%lld (< 2^31)", (long long)n_rays, (long long)capacity);
+    NGLOD_REQUIRE(pyramid_host && count && result_buffer, NGLOD_ERR_INVALID, "null pointer argument");
+    NGLOD_REQUIRE(pyramid_host[level + 1] == 0 && pyramid_host[level + 2] == 0, NGLOD_ERR_INVALID,
+                  "bad pyramid table (the reference's 'bad spc table3' check)");
+    *result_buffer = (target_level + 1) % 2;
+    *count = 0;
+    if (n_rays == 0) return NGLOD_OK;
+    NGLOD_REQUIRE(octree && points && prefix && org && dir && nuggets_a && nuggets_b && info && partials && ctrl,
+                  NGLOD_ERR_INVALID, "null pointer argument");
+    NGLOD_REQUIRE(aligned(points, 8) && aligned(nuggets_a, 8) && aligned(nuggets_b, 8) && aligned(ctrl, 8),
+                  NGLOD_ERR_ALIGN, "points, nuggets and ctrl must be 8-byte aligned");
+    cudaStream_t s = (cudaStream_t)stream;
+    int64_t init[kCtrlCount + 1] = {0, 0, 0, 0, n_rays};
+    NGLOD_TRY(cuda_status(cudaMemcpyAsync(ctrl, init, sizeof(init), cudaMemcpyHostToDevice, s), "raytrace copy"));
+    TraverseArgs a;
+    a.octree = octree;
+    a.points = reinterpret_cast<const short4 *>(points);
+    a.prefix = prefix;
+    a.org = org;
+    a.dir = dir;
+    a.info = info;
+    a.partials = partials;
+    a.ctrl = ctrl;
+    a.capacity = capacity;
+    a.target = target_level;
+    a.order = make_order_table();
+    const int32_t *psum = pyramid_host + (level + 2);
+    int2 *buf[2] = {reinterpret_cast<int2 *>(nuggets_a), reinterpret_cast<int2 *>(nuggets_b)};
+    const int grid = grid_for((capacity + kChunk - 1) / kChunk);
+    for (int l = 0; l <= target_level; ++l) {
+        a.level = l;
+        a.off0 = psum[l];
+        a.off1 = psum[l + 1];
+        a.in = buf[l % 2];
+        a.out = buf[(l + 1) % 2];
+        traverse_decide_kernel<<<grid, kChunk, 0, s>>>(a);
+        scan_chunk_counts_kernel<<<1, kChunk, 0, s>>>(partials, ctrl + kCtrlCount + l, ctrl + kCtrlCount + l + 1,
+                                                      capacity, ctrl + kCtrlStatus);
+        traverse_emit_kernel<<<grid, kChunk, 0, s>>>(a);
+    }
+    NGLOD_TRY(launch_status("nglod_spc_raytrace"));
+    int64_t res[kCtrlCount + kMaxSpcLevels + 1];
+    NGLOD_TRY(cuda_status(cudaMemcpyAsync(res, ctrl, sizeof(int64_t) * (kCtrlCount + target_level + 2),
+                                          cudaMemcpyDeviceToHost, s),
+                          "raytrace copy"));
+    NGLOD_TRY(cuda_status(cudaStreamSynchronize(s), "raytrace sync"));
+    NGLOD_REQUIRE(res[kCtrlStatus] == 0, NGLOD_ERR_CAPACITY,
+                  "spc_raytrace: more than capacity=%lld nuggets at some level", (long long)capacity);
+    *count = res[kCtrlCount + target_level + 1];
+    return NGLOD_OK;
+}
+
+extern "C" int nglod_spc_mark_first(const int32_t *nuggets, int64_t n, int32_t *info, nglod_stream_t stream) {
+    NGLOD_REQUIRE(n >= 0, NGLOD_ERR_INVALID, "n=%lld is negative", (long long)n);
+    if (n == 0) return NGLOD_OK;
+    NGLOD_REQUIRE(nuggets && info, NGLOD_ERR_INVALID, "null pointer argument");
+    mark_first_kernel<<<grid_elems(n), 256, 0, (cudaStream_t)stream>>>(reinterpret_cast<const int2 *>(nuggets), n,
+                                                                        info);
+    return launch_status("nglod_spc_mark_first");
+}
+
+namespace nglod {
+struct Mat4 {
+    float m[4][4];
+};
+
+// a (row vector) times M with the reference's mul4x4 arithmetic
+// (spc_math.h:102-110) compiled with default contraction:
+// fma(a.w, m3, fma(a.z, m2, fma(a.x, m0, a.y*m1))).
+__device__ __forceinline__ float4 row_times(float4 a, const Mat4 &M) {
+    float4 r;
+    r.x = __fmaf_rn(a.w, M.m[3][0], __fmaf_rn(a.z, M.m[2][0], __fmaf_rn(a.x, M.m[0][0], __fmul_rn(a.y, M.m[1][0]))));
+    r.y = __fmaf_rn(a.w, M.m[3][1], __fmaf_rn(a.z, M.m[2][1], __fmaf_rn(a.x, M.m[0][1], __fmul_rn(a.y, M.m[1][1]))));
+    r.z = __fmaf_rn(a.w, M.m[3][2], __fmaf_rn(a.z, M.m[2][2], __fmaf_rn(a.x, M.m[0][2], __fmul_rn(a.y, M.m[1][2]))));
+    r.w = __fmaf_rn(a.w, M.m[3][3], __fmaf_rn(a.z, M.m[2][3], __fmaf_rn(a.x, M.m[0][3], __fmul_rn(a.y, M.m[1][3]))));
+    return r;
+}
+
+__global__ void generate_rays_kernel(const Mat4 M, int width, int64_t n, float *org, float *dir) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const float px = (float)(uint32_t)(i % width), py = (float)(uint32_t)(i / width);
+        const float4 a = row_times(make_float4(0.f, 0.f, 1.f, 0.f), M);
+        const float4 b = row_times(make_float4(px, py, 0.f, 1.f), M);
+        org[3 * i] = a.x;
+        org[3 * i + 1] = a.y;
+        org[3 * i + 2] = a.z;
+        dir[3 * i] = b.x;
+        dir[3 * i + 1] = b.y;
+        dir[3 * i + 2] = b.z;
+    }
+}
+}  // namespace nglod
+
+extern "C" int nglod_spc_generate_rays(const float *inv_wvp_host, int32_t width, int32_t height, float *org,
+                                       float *dir, nglod_stream_t stream) {
+    NGLOD_REQUIRE(width > 0 && height > 0, NGLOD_ERR_INVALID, "image %dx%d is empty", width, height);
+    NGLOD_REQUIRE(inv_wvp_host && org && dir, NGLOD_ERR_INVALID, "null pointer argument");
+    Mat4 M;
+    for (int r = 0; r < 4; ++r)
+        for (int c = 0; c < 4; ++c) M.m[r][c] = inv_wvp_host[4 * r + c];
+    const int64_t n = (int64_t)width * height;
+    generate_rays_kernel<<<grid_elems(n), 256, 0, (cudaStream_t)stream>>>(M, width, n, org, dir);
+    return launch_status("nglod_spc_generate_rays");
+}
+
+extern "C" int nglod_spc_prefix(const uint8_t *octree, int64_t osize, uint32_t *prefix, uint32_t *partials,
+                                int64_t *ctrl, nglod_stream_t stream) {
+    NGLOD_REQUIRE(osize >= 0, NGLOD_ERR_INVALID, "osize=%lld is negative", (long long)osize);
+    NGLOD_REQUIRE(prefix && partials && ctrl && (octree || osize == 0), NGLOD_ERR_INVALID, "null pointer argument");
+    NGLOD_REQUIRE(aligned(ctrl, 8), NGLOD_ERR_ALIGN, "ctrl must be 8-byte aligned");
+    cudaStream_t s = (cudaStream_t)stream;
+    const int64_t nelem = osize + 1;
+    const int64_t chunks = (nelem + kChunk - 1) / kChunk;
+    NGLOD_TRY(cuda_status(cudaMemcpyAsync(ctrl, &nelem, sizeof(int64_t), cudaMemcpyHostToDevice, s), "prefix copy"));
+    popc_chunk_kernel<<<grid_for(chunks), kChunk, 0, s>>>(octree, ctrl, partials);
+    scan_chunk_counts_kernel<<<1, kChunk, 0, s>>>(partials, ctrl, ctrl + 1, INT64_MAX, nullptr);
+    popc_prefix_kernel<<<grid_for(chunks), kChunk, 0, s>>>(octree, osize, ctrl, partials, prefix);
+    return launch_status("nglod_spc_prefix");
+}

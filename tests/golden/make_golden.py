@@ -178,7 +178,19 @@ def coded_volume(s, channels=2):
     return (c * 1e6 + z * 1e4 + y * 1e2 + x)[None]
 
 
-def spc_small(spc3d, geoutils):
+def order_table(ref_root):
+    """The Order[8][8] child-order table of spc_raytrace_cuda_kernel.cu, read
+    from the source text."""
+    import re
+    path = os.path.join(ref_root, "sol-renderer", "include", "spc", "spc", "spc_raytrace_cuda_kernel.cu")
+    text = open(path).read()
+    body = text[text.index("Order[8][8]"):]
+    body = body[body.index("{") + 1:body.index("};")]
+    rows = re.findall(r"\{([^{}]*)\}", body)
+    return np.array([[int(v) for v in r.split(",")] for r in rows], dtype=np.uint8)
+
+
+def spc_small(spc3d, geoutils, ref_root):
     level = 5
     res = 2 ** level
     c, r = synthetic.sphere_union(1)
@@ -200,7 +212,8 @@ def spc_small(spc3d, geoutils):
     pyramid_sum = spc.pyramid_sum[:level + 1].copy()
     dec = spc3d.SPC3D(level, nodebytes=octree.copy())
     npts = dec.nodes_to_points()
-    out = {"voxels": vox, "morton": morton, "points_sorted": points_sorted, "octree": octree,
+    out = {"order_table": order_table(ref_root),
+           "voxels": vox, "morton": morton, "points_sorted": points_sorted, "octree": octree,
            "pyramid": pyramid, "pyramid_sum": pyramid_sum, "decoded_leaf_points": dec.pdata[:npts].copy(),
            "decoded_pyramid": dec.pyramid[:level + 1].copy(), "level": np.array(level)}
     # unique_corners of each octree level's voxels (geoutils.py:60-77).  The
@@ -222,7 +235,7 @@ def main():
     torch.set_num_threads(max(1, os.cpu_count() or 1))
     dense_small(OctreeSDF, parse_options)
     trace_small(OctreeSDF, SphereTracer, parse_options)
-    spc_small(spc3d, geoutils)
+    spc_small(spc3d, geoutils, ref_root)
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))
