@@ -254,6 +254,70 @@ int nglod_spc_mark_first(const int32_t *nuggets, int64_t n, int32_t *info, nglod
 int nglod_spc_generate_rays(const float *inv_wvp_host, int32_t width, int32_t height, float *org, float *dir,
                             nglod_stream_t stream);
 
+/* ------------------------------------------------------------------------
+ * Sparse SDF on an SPC octree (sol-renderer's SDF class, SDF.h:44-97).
+ *
+ * LOD i lives on octree level i + 2.  The features of the unique corners of
+ * the occupied voxels of every level are stored once (all levels
+ * concatenated, each level's corners in lexicographic (x, y, z) order, as
+ * SOL_NGLOD exports them: sdf-net/lib/models/SOL_NGLOD.py:68-75).  For every
+ * octree point of level >= 2, corner_idx[p][8] holds the global corner index
+ * of its 8 corners (corner j = (x + (j>>2&1), y + (j>>1&1), z + (j&1))) and
+ * parent[p] the global point index of its parent (-1 at level 2): the
+ * reference's Trinket {v[8], parent} (solr/util_structs.cuh:33-37).
+ * ------------------------------------------------------------------------ */
+typedef struct nglod_sparse_model {
+    int32_t num_lods;        /* decoders; octree levels 2 .. num_lods + 1 */
+    int32_t feature_dim;     /* 32 */
+    int32_t hidden_dim;      /* <= 256, even */
+    int32_t feat_dtype;      /* NGLOD_F32 or NGLOD_BF16 corner features */
+    const void    *corner_feats;  /* [ncorners][feature_dim], 16-byte aligned */
+    const int32_t *corner_idx;    /* [psize][8], 16-byte aligned */
+    const int32_t *parent;        /* [psize] */
+    const int16_t *points;        /* [psize][4] */
+    int64_t level_start[16];      /* global index of each octree level's first point */
+    const float *w0[NGLOD_MAX_LODS];
+    const float *b0[NGLOD_MAX_LODS];
+    const float *w1[NGLOD_MAX_LODS];
+    const float *b1[NGLOD_MAX_LODS];
+} nglod_sparse_model;
+
+/* SDF::initTrinkets + the corner export of SOL_NGLOD (SDF.cu:141-216,
+ * SOL_NGLOD.py:68-75): from a dense model whose LOD i volume has
+ * 2^(i+2)+1 vertices per side and an octree with at least num_lods + 1
+ * levels, writes corner features (corner_cap rows, dtype feat_dtype),
+ * corner_idx, parent, and corner_counts_host[num_lods] (corners per LOD).
+ * scratch: nglod_sparse_build_scratch_bytes(level) bytes.  Replaces the
+ * reference's O(points x corners) search (solr/sdf/index_trinket.cuh:31-98)
+ * with dense index grids.  Synchronises once. */
+int64_t nglod_sparse_build_scratch_bytes(int32_t level);
+int nglod_sparse_build(const nglod_dense_model *dense, const int16_t *points, const int32_t *pyramid_host,
+                       int32_t level, int32_t feat_dtype, void *corner_feats, int64_t corner_cap,
+                       int32_t *corner_idx, int32_t *parent, int64_t *corner_counts_host, void *scratch,
+                       nglod_stream_t stream);
+
+/* SDF::forward(x, lod) -- declared in SDF.h:52-54 but never defined in the
+ * reference: the sparse SDF at points x[n][3].  Each point's voxel at octree
+ * level lod+2 is found by descending the octree (spc3d.SPC3D.Identify,
+ * sdf-net/lib/spc3d.py:309-338); points outside every occupied voxel get
+ * NaN.  octree/prefix as from nglod_spc_decode. */
+int nglod_sparse_query(const nglod_sparse_model *model, const uint8_t *octree, const uint32_t *prefix, int32_t lod,
+                       const float *x, int64_t n, float *out, nglod_stream_t stream);
+
+/* SDF::sphereTrace (SDF.cu:297-472, kernels solr/sdf/sparse_grid_sample.cuh,
+ * solr/sdf/step.cuh, solr/gfx/ray_aabb.cuh, solr/common/normalize.cuh) in one
+ * persistent launch.  nuggets[m][2] from nglod_spc_raytrace at level lod+2;
+ * rays without nuggets are left untouched by the march (t = 0, x = ray_o,
+ * hit = 0, normal = (1,1,1)).  Per ray: voxel walk from ray_o, then up to
+ * num_steps sparse evaluations (t += d; hit = |d| < 3e-4 or
+ * |d + dprev|/2 < 1.5e-3; stop at t >= 5 or leaving the voxels, t = 100),
+ * normals of hit rays by central differences (1e-3) inside the last voxel.
+ * ray_first: int32 [n] scratch; work_counter: one int64. */
+int nglod_sparse_trace(const nglod_sparse_model *model, int32_t lod, int32_t num_steps, const float *ray_o,
+                       const float *ray_d, int64_t n, const int32_t *nuggets, int64_t n_nuggets,
+                       int32_t *ray_first, float *x, float *t, uint8_t *hit, float *normal, int64_t *work_counter,
+                       nglod_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -72,8 +72,26 @@ class AdamTensor(ctypes.Structure):
     _fields_ = [("param", _vp), ("grad", _vp), ("exp_avg", _vp), ("exp_avg_sq", _vp), ("numel", _i64)]
 
 
+class SparseModel(ctypes.Structure):
+    _fields_ = [
+        ("num_lods", _i32),
+        ("feature_dim", _i32),
+        ("hidden_dim", _i32),
+        ("feat_dtype", _i32),
+        ("corner_feats", _vp),
+        ("corner_idx", _vp),
+        ("parent", _vp),
+        ("points", _vp),
+        ("level_start", _i64 * 16),
+        ("w0", _vp * MAX_LODS),
+        ("b0", _vp * MAX_LODS),
+        ("w1", _vp * MAX_LODS),
+        ("b1", _vp * MAX_LODS),
+    ]
+
+
 # C struct name -> ctypes mirror (layouts are checked against the header by tests/test_abi.py)
-STRUCTS = {"nglod_dense_grads": DenseGrads, "nglod_adam_tensor": AdamTensor}
+STRUCTS = {"nglod_dense_grads": DenseGrads, "nglod_adam_tensor": AdamTensor, "nglod_sparse_model": SparseModel}
 
 _u32 = ctypes.c_uint32
 _f32 = ctypes.c_float
@@ -100,6 +118,12 @@ SIGNATURES = {
                                           _vp, _vp, ctypes.POINTER(_i64), ctypes.POINTER(_i32), _vp]),
     "nglod_spc_mark_first": (ctypes.c_int, [_vp, _i64, _vp, _vp]),
     "nglod_spc_generate_rays": (ctypes.c_int, [_vp, _i32, _i32, _vp, _vp, _vp]),
+    "nglod_sparse_build_scratch_bytes": (_i64, [_i32]),
+    "nglod_sparse_build": (ctypes.c_int, [ctypes.POINTER(DenseModel), _vp, _vp, _i32, _i32, _vp, _i64, _vp, _vp,
+                                          _vp, _vp, _vp]),
+    "nglod_sparse_query": (ctypes.c_int, [ctypes.POINTER(SparseModel), _vp, _vp, _i32, _vp, _i64, _vp, _vp]),
+    "nglod_sparse_trace": (ctypes.c_int, [ctypes.POINTER(SparseModel), _i32, _i32, _vp, _vp, _i64, _vp, _i64, _vp,
+                                          _vp, _vp, _vp, _vp, _vp, _vp]),
     "nglod_adam_step": (ctypes.c_int, [_vp, _i32, _i64, _f32, _f32, _f32, _f32, _f32, _i64, _vp]),
 }
 

@@ -22,18 +22,23 @@ constexpr int kRowF4 = 9;      // float4 per staged decoder row (35 weights + bi
 // float4 count of one staged decoder with H hidden units.
 __host__ __device__ inline int decoder_f4(int H) { return H * kRowF4 + (H + 4) / 4; }
 
-__device__ __forceinline__ void stage_decoder(float4 *dst, const nglod_dense_model &m, int l) {
-    const int H = m.hidden_dim;
+// Stages decoder (w0 [H][35], b0 [H], w1 [H], b1 [1]) into dst as H rows of
+// 36 floats (row weights then bias) followed by w1 and b1.
+__device__ __forceinline__ void stage_decoder_ptrs(float4 *dst, int H, const float *__restrict__ w0,
+                                                   const float *__restrict__ b0, const float *__restrict__ w1,
+                                                   const float *__restrict__ b1) {
     float *rows = reinterpret_cast<float *>(dst);
-    const float *__restrict__ w0 = m.w0[l];
-    const float *__restrict__ b0 = m.b0[l];
     for (int i = threadIdx.x; i < H * 36; i += blockDim.x) {
         const int j = i / 36, k = i - j * 36;
         rows[i] = k < 35 ? w0[j * 35 + k] : b0[j];
     }
     float *w1s = rows + H * 36;
-    for (int j = threadIdx.x; j < H; j += blockDim.x) w1s[j] = m.w1[l][j];
-    if (threadIdx.x == 0) w1s[H] = m.b1[l][0];
+    for (int j = threadIdx.x; j < H; j += blockDim.x) w1s[j] = w1[j];
+    if (threadIdx.x == 0) w1s[H] = b1[0];
+}
+
+__device__ __forceinline__ void stage_decoder(float4 *dst, const nglod_dense_model &m, int l) {
+    stage_decoder_ptrs(dst, m.hidden_dim, m.w0[l], m.b0[l], m.w1[l], m.b1[l]);
 }
 
 // Adds the trilinear sample of one channel-last float32 volume (s vertices per

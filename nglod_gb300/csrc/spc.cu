@@ -12,74 +12,13 @@
 
 #include <vector>
 
-#include "common.cuh"
+#include "scan.cuh"
 
 namespace nglod {
 
-constexpr int kChunk = 1024;
 constexpr int kMaxSpcLevels = 15;
 constexpr int kCtrlStatus = 0;   // 0 ok, 1 capacity exceeded
 constexpr int kCtrlCount = 4;    // count of level l at kCtrlCount + l
-
-// ---------------------------------------------------------------------------
-// block scan helpers (blockDim.x == kChunk)
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t *s_warp, uint32_t *total) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint32_t x = v;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= o) x += y;
-    }
-    if (lane == 31) s_warp[warp] = x;
-    __syncthreads();
-    if (warp == 0) {
-        uint32_t w = s_warp[lane];
-        uint32_t wi = w;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xffffffffu, wi, o);
-            if (lane >= o) wi += y;
-        }
-        s_warp[lane] = wi - w;  // exclusive prefix of warp totals
-        if (lane == 31) s_warp[32] = wi;
-    }
-    __syncthreads();
-    const uint32_t r = s_warp[warp] + x - v;
-    *total = s_warp[32];
-    __syncthreads();
-    return r;
-}
-
-__device__ __forceinline__ uint32_t block_sum(uint32_t v, uint32_t *s_warp) {
-    uint32_t t;
-    block_exclusive_scan(v, s_warp, &t);
-    return t;
-}
-
-// Pass 2: exclusive scan of `nchunks` chunk counts in place, in one block.
-// The total goes to *total_out (and, if over `capacity`, raises the status).
-__global__ void __launch_bounds__(kChunk) scan_chunk_counts_kernel(uint32_t *partials, const int64_t *count_in,
-                                                                   int64_t *total_out, int64_t capacity,
-                                                                   int64_t *status) {
-    __shared__ uint32_t s_warp[33];
-    const int64_t count = *count_in;
-    const int64_t nchunks = (count + kChunk - 1) / kChunk;
-    uint64_t carry = 0;
-    for (int64_t base = 0; base < nchunks; base += kChunk) {
-        const int64_t i = base + threadIdx.x;
-        const uint32_t v = i < nchunks ? partials[i] : 0u;
-        uint32_t tot;
-        const uint32_t ex = block_exclusive_scan(v, s_warp, &tot);
-        if (i < nchunks) partials[i] = (uint32_t)(carry + ex);
-        carry += tot;
-    }
-    if (threadIdx.x == 0) {
-        *total_out = (int64_t)carry;
-        if ((int64_t)carry > capacity && status) *status = 1;
-    }
-}
 
 // ---------------------------------------------------------------------------
 // front-to-back child order

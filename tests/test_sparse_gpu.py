@@ -1,0 +1,125 @@
+"""Sparse SDF (sol-renderer's SDF class) on the GPU against the numpy
+restatement of SDF::sphereTrace and against the dense model."""
+import numpy as np
+import pytest
+import torch
+
+import nglod_gb300 as ng
+from nglod_gb300 import spc, synthetic
+from nglod_gb300.analytic_init import init_from_sdf
+from nglod_gb300.options import default_args
+from nglod_gb300.sparse_sdf import SparseSDF
+from oracle import dense as odense
+from oracle import sparse as osparse
+from oracle import spc as ospc
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def scene(cuda):
+    c, r = synthetic.sphere_union(1)
+    torch.manual_seed(0)
+    net = ng.OctreeSDF(default_args(num_lods=4, base_lod=2))
+    init_from_sdf(net, lambda p: torch.from_numpy(synthetic.sphere_union_sdf(p.numpy(), c, r)), noise=1e-3, seed=3)
+    level = 5  # LODs 0..3 on octree levels 2..5
+    vox = ospc.voxels_near_surface(lambda p: synthetic.sphere_union_sdf(p, c, r), level)
+    s = spc.SPC.from_voxels(torch.from_numpy(vox.astype(np.int32)).to(cuda), level)
+    net = net.to(cuda).eval()
+    return net, s, (c, r)
+
+
+def _oracle_model(net, s, num_lods):
+    pts = s.GetPoints().cpu().numpy()
+    pyr = s.GetPyramid().numpy()
+    fms = [fv.fm.detach().cpu().numpy()[0].astype(np.float16).astype(np.float32) for fv in net.features]
+    m = osparse.build(fms, pts, pyr, num_lods)
+    decs = [tuple(t.detach().cpu().numpy().astype(np.float16).astype(np.float32).reshape(t.shape)
+                  for t in (d[0].weight, d[0].bias, d[2].weight, d[2].bias)) for d in net.louts]
+    return m, decs
+
+
+def test_build_matches_oracle(scene):
+    net, s, _ = scene
+    sp = SparseSDF.from_dense(net, s)
+    m, _ = _oracle_model(net, s, 4)
+    assert sp.corner_counts == m["counts"]
+    np.testing.assert_array_equal(sp.corner_feats.cpu().numpy(), m["cf"])
+    pyr = s.GetPyramid().numpy()
+    a = pyr[1, 2]
+    np.testing.assert_array_equal(sp.corner_idx.cpu().numpy()[a:], m["trink"][a:])
+    np.testing.assert_array_equal(sp.parent.cpu().numpy()[a:], m["parent"][a:])
+
+
+@pytest.mark.parametrize("lod", [0, 3])
+def test_query_equals_dense_inside_voxels(scene, lod):
+    """With float32 features and weights the sparse SDF equals the dense one
+    at points inside occupied voxels; outside it is NaN."""
+    net, s, (c, r) = scene
+    sp = SparseSDF.from_dense(net, s, precision="f32", half_weights=False)
+    x = synthetic.near_surface_query(20000, c, r, seed=4).to(s.GetOctree().device)
+    got = sp.forward(x, lod)
+    with torch.no_grad():
+        want = net.sdf(x, lod=lod)
+    inside = ~torch.isnan(got[:, 0])
+    assert inside.float().mean() > 0.3
+    assert (got[inside] - want[inside]).abs().max().item() < 1e-5
+    far = torch.tensor([[0.95, 0.95, 0.95], [2.0, 0.0, 0.0]], device=x.device)
+    assert torch.isnan(sp.forward(far, lod)).all()
+
+
+@pytest.mark.parametrize("precision", ["fp16", "bf16"])
+def test_sparse_trace_matches_oracle(scene, precision):
+    net, s, _ = scene
+    sp = SparseSDF.from_dense(net, s, precision=precision)
+    ro, rd = synthetic.look_at_rays(width=96, height=72)
+    dev = s.GetOctree().device
+    (x, t, hit, normal), nug = sp.render(ro.to(dev), rd.to(dev), lod=3, num_steps=50)
+    m, decs = _oracle_model(net, s, 4)
+    if precision == "bf16":
+        m["cf"] = sp.corner_feats.float().cpu().numpy()
+    xo, to, ho, no = osparse.sphere_trace(m, decs, 3, ro.numpy(), rd.numpy(), nug.cpu().numpy(), num_steps=50)
+    h = hit.cpu().numpy()
+    assert h.sum() > 500
+    assert (h == ho).mean() >= 0.999
+    both = h & ho
+    np.testing.assert_allclose(t.cpu().numpy()[both], to[both], atol=1e-4, rtol=0)
+    np.testing.assert_allclose(normal.cpu().numpy()[both], no[both], atol=2e-3, rtol=0)
+    nh = ~h & ~ho
+    assert (normal.cpu().numpy()[nh] == 1).all()
+
+
+def test_sparse_vs_dense_tracer(scene):
+    """The sparse trace (fp16 export, 50 steps) against the dense float32
+    tracer on the same network: same surface within a voxel's reach."""
+    net, s, _ = scene
+    sp = SparseSDF.from_dense(net, s)
+    ro, rd = synthetic.look_at_rays(width=128, height=96)
+    dev = s.GetOctree().device
+    net.lod = 3
+    (x, t, hit, normal), _ = sp.render(ro.to(dev), rd.to(dev), lod=3, num_steps=50)
+    rb = ng.SphereTracer(default_args(num_steps=128))(net, ro.to(dev), rd.to(dev))
+    net.lod = None
+    both = hit & rb.hit
+    agree = (hit == rb.hit).float().mean().item()
+    assert agree > 0.98, agree
+    assert (t[both] - rb.depth[both]).abs().median().item() < 2e-3
+    cosang = (normal[both] * rb.normal[both]).sum(-1)
+    assert cosang.median().item() > 0.99
+
+
+def test_npz_round_trip(scene, tmp_path):
+    net, s, _ = scene
+    sp = SparseSDF.from_dense(net, s)
+    path = tmp_path / "model.npz"
+    sp.save_npz(str(path))
+    z = np.load(str(path))
+    assert set(z.files) == {"octree", "cc", "cf", "w0", "b0", "w1", "b1", "pyramid"}
+    assert z["cc"].dtype == np.uint8 and z["cf"].dtype == np.float16 and z["w0"].shape == (4, 128, 35)
+    sp2 = SparseSDF.from_npz(str(path))
+    assert torch.equal(sp2.corner_idx, sp.corner_idx) and torch.equal(sp2.corner_feats, sp.corner_feats)
+    ro, rd = synthetic.look_at_rays(width=64, height=48)
+    dev = s.GetOctree().device
+    a, _ = sp.render(ro.to(dev), rd.to(dev), lod=3)
+    b, _ = sp2.render(ro.to(dev), rd.to(dev), lod=3)
+    assert torch.equal(a[1], b[1]) and torch.equal(a[2], b[2])

@@ -85,3 +85,38 @@ def test_traversal_visits_exactly_the_crossed_voxels_front_to_back(golden):
                 assert np.all(np.diff(t) > -1.5 * s), (r, t)
         assert mismatch <= 2, mismatch
         assert nug.shape[0] > 0
+
+
+def test_sparse_corner_export_matches_reference_unique_corners(golden):
+    """oracle.sparse.build's corners and features equal geoutils.unique_corners
+    of the reference on the coded volumes of the fixture."""
+    from oracle import sparse
+    fx = golden("spc_small")
+    pts, pyr, prefix = spc.set_geometry(fx["octree"])
+    level = int(fx["level"])
+    fms = []
+    for lv in range(2, level + 1):
+        s = 2 ** lv + 1
+        c = np.arange(2).reshape(2, 1, 1, 1)
+        z = np.arange(s).reshape(1, s, 1, 1)
+        y = np.arange(s).reshape(1, 1, s, 1)
+        x = np.arange(s).reshape(1, 1, 1, s)
+        fms.append((c * 1e6 + z * 1e4 + y * 1e2 + x).astype(np.float64))
+    m = sparse.build(fms, pts, pyr, level - 1, corner_dtype=np.float64)
+    o = 0
+    for i, lv in enumerate(range(2, level + 1)):
+        n = m["counts"][i]
+        assert np.array_equal(m["cc"][o:o + n], fx[f"corners/{lv}/cc"])
+        assert np.array_equal(m["cf"][o:o + n].astype(np.float64), fx[f"corners/{lv}/cf"].astype(np.float32))
+        o += n
+    # trinket corners really are the voxel's corners, parents contain their children
+    for lv in range(2, level + 1):
+        a, b = pyr[1, lv], pyr[1, lv + 1]
+        vox = pts[a:b, :3].astype(np.int64)
+        for j in range(8):
+            off = np.array([(j >> 2) & 1, (j >> 1) & 1, j & 1])
+            assert np.array_equal(m["cc"][m["trink"][a:b, j]], vox + off)
+        if lv > 2:
+            assert np.array_equal(pts[m["parent"][a:b], :3].astype(np.int64), vox >> 1)
+        else:
+            assert (m["parent"][a:b] == -1).all()
