@@ -64,8 +64,14 @@ def test_query_equals_dense_inside_voxels(scene, lod):
     inside = ~torch.isnan(got[:, 0])
     assert inside.float().mean() > 0.3
     assert (got[inside] - want[inside]).abs().max().item() < 1e-5
-    far = torch.tensor([[0.95, 0.95, 0.95], [2.0, 0.0, 0.0]], device=x.device)
-    assert torch.isnan(sp.forward(far, lod)).all()
+    # NaN exactly where the point's voxel at octree level lod+2 is unoccupied
+    res = 2 ** (lod + 2)
+    vox = ((x + 1) / 2 * res).floor().long().clamp(0, res - 1)
+    occ = torch.zeros(res, res, res, dtype=torch.bool, device=x.device)
+    lp = s.GetLevelPoints(lod + 2)[:, :3].long()
+    occ[lp[:, 0], lp[:, 1], lp[:, 2]] = True
+    assert torch.equal(inside, occ[vox[:, 0], vox[:, 1], vox[:, 2]])
+    assert torch.isnan(sp.forward(torch.tensor([[2.0, 0.0, 0.0]], device=x.device), lod)).all()
 
 
 @pytest.mark.parametrize("precision", ["fp16", "bf16"])
