@@ -109,6 +109,42 @@ int nglod_trace(const nglod_dense_model *model, const nglod_trace_params *params
                 int64_t *work_counter, nglod_stream_t stream);
 
 /* ------------------------------------------------------------------------
+ * BF16 form: bf16 feature volumes and a tcgen05 tensor-core decoder.
+ *
+ * The decoder's first layer runs as a 128-point x 128-hidden x 48 bf16 tile
+ * product with fp32 accumulation in tensor memory.  K order of the tile:
+ * k 0..31 = the 32 summed features, 32..34 = x, y, z rounded to bf16,
+ * 35..37 = the bf16 remainders x - bf16(x) (so positions keep ~16 bits),
+ * 38..47 = 0.  The first-layer bias b0, the ReLU and the second layer
+ * (w1, b1) are applied in fp32 after the product.
+ * ------------------------------------------------------------------------ */
+typedef struct nglod_bf16_model {
+    int32_t num_lods;
+    int32_t base_lod;
+    int32_t feature_dim;    /* 32 */
+    int32_t hidden_dim;     /* 128 */
+    const void  *grid[NGLOD_MAX_LODS];     /* bf16 channel-last [s][s][s][32], 16-byte aligned */
+    const void  *w0_tile[NGLOD_MAX_LODS];  /* NGLOD_BF16_TILE_BYTES from nglod_bf16_pack_decoder */
+    const float *b0[NGLOD_MAX_LODS];       /* [128] */
+    const float *w1[NGLOD_MAX_LODS];       /* [128] */
+    const float *b1[NGLOD_MAX_LODS];       /* [1] */
+} nglod_bf16_model;
+
+#define NGLOD_BF16_TILE_BYTES 12288
+
+/* Host-only: lays out w0 [128][35] (nn.Linear weight of louts[i][0]) as the
+ * bf16 B operand of the tensor-core tile (K-major, 8x8 core matrices, no
+ * swizzle), NGLOD_BF16_TILE_BYTES bytes.  No CUDA calls. */
+int nglod_bf16_pack_decoder(const float *w0_host, int32_t hidden_dim, int32_t in_dim, void *tile_host);
+
+/* OctreeSDF.sdf(x, lod) in the BF16 form: per-LOD bf16 trilinear gathers
+ * summed in fp32, decoder on tcgen05 tensor cores (see above).
+ * status: one device int32, set to nonzero if a bounded wait for the tensor
+ * core gave up (the call zeroes it first). */
+int nglod_sdf_fwd_bf16(const nglod_bf16_model *model, const float *x, int64_t n, int32_t lod, float *out,
+                       int32_t *status, nglod_stream_t stream);
+
+/* ------------------------------------------------------------------------
  * Training: forward with saved features, hand-written backward, Adam.
  * ------------------------------------------------------------------------ */
 

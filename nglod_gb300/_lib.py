@@ -90,8 +90,25 @@ class SparseModel(ctypes.Structure):
     ]
 
 
+class Bf16Model(ctypes.Structure):
+    _fields_ = [
+        ("num_lods", _i32),
+        ("base_lod", _i32),
+        ("feature_dim", _i32),
+        ("hidden_dim", _i32),
+        ("grid", _vp * MAX_LODS),
+        ("w0_tile", _vp * MAX_LODS),
+        ("b0", _vp * MAX_LODS),
+        ("w1", _vp * MAX_LODS),
+        ("b1", _vp * MAX_LODS),
+    ]
+
+
+BF16_TILE_BYTES = 12288
+
 # C struct name -> ctypes mirror (layouts are checked against the header by tests/test_abi.py)
-STRUCTS = {"nglod_dense_grads": DenseGrads, "nglod_adam_tensor": AdamTensor, "nglod_sparse_model": SparseModel}
+STRUCTS = {"nglod_dense_grads": DenseGrads, "nglod_adam_tensor": AdamTensor, "nglod_sparse_model": SparseModel,
+           "nglod_bf16_model": Bf16Model}
 
 _u32 = ctypes.c_uint32
 _f32 = ctypes.c_float
@@ -124,6 +141,8 @@ SIGNATURES = {
     "nglod_sparse_query": (ctypes.c_int, [ctypes.POINTER(SparseModel), _vp, _vp, _i32, _vp, _i64, _vp, _vp]),
     "nglod_sparse_trace": (ctypes.c_int, [ctypes.POINTER(SparseModel), _i32, _i32, _vp, _vp, _i64, _vp, _i64, _vp,
                                           _vp, _vp, _vp, _vp, _vp, _vp]),
+    "nglod_bf16_pack_decoder": (ctypes.c_int, [_vp, _i32, _i32, _vp]),
+    "nglod_sdf_fwd_bf16": (ctypes.c_int, [ctypes.POINTER(Bf16Model), _vp, _i64, _i32, _vp, _vp, _vp]),
     "nglod_adam_step": (ctypes.c_int, [_vp, _i32, _i64, _f32, _f32, _f32, _f32, _f32, _i64, _vp]),
 }
 

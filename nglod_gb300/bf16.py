@@ -1,0 +1,68 @@
+"""BF16 form of the dense OctreeSDF: bf16 feature volumes, tcgen05 decoder.
+
+``Bf16OctreeSDF(net)`` snapshots a float32 ``OctreeSDF`` for inference:
+volumes converted to bf16 (channel-last), each decoder's first layer packed
+once into the bf16 tensor-core tile layout (``nglod_bf16_pack_decoder``),
+b0 / w1 / b1 kept in float32.  ``sdf(x, lod)`` has the semantics of
+OctreeSDF.sdf(x, lod) (sdf-net/lib/models/OctreeSDF.py:94-146) with bf16
+storage and bf16 x bf16 -> fp32 products; its error against the FP64 oracle
+is measured per LOD by tests/test_bf16_gpu.py and bench.py.
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+
+
+def pack_decoder_tile(w0):
+    """[128, 35] float32 -> uint8 [12288] tile (host pack through the C ABI)."""
+    w = np.ascontiguousarray(w0.detach().cpu().numpy(), dtype=np.float32)
+    out = np.zeros(_lib.BF16_TILE_BYTES, dtype=np.uint8)
+    _lib.check(_lib.load().nglod_bf16_pack_decoder(w.ctypes.data_as(ctypes.c_void_p), w.shape[0], w.shape[1],
+                                                   out.ctypes.data_as(ctypes.c_void_p)), "nglod_bf16_pack_decoder")
+    return torch.from_numpy(out)
+
+
+class Bf16OctreeSDF:
+    def __init__(self, net):
+        _lib.require_cuda(net.features[0].fm)
+        dev = net.features[0].fm.device
+        self.num_lods = net.num_lods
+        self.base_lod = net.base_lod
+        self.lod = net.lod
+        self.grids = [fv.fm.detach().to(torch.bfloat16).contiguous(memory_format=torch.channels_last_3d)
+                      for fv in net.features]
+        self.tiles, self.b0, self.w1, self.b1 = [], [], [], []
+        for dec in net.louts:
+            self.tiles.append(pack_decoder_tile(dec[0].weight).to(dev))
+            self.b0.append(dec[0].bias.detach().float().contiguous())
+            self.w1.append(dec[2].weight.detach().float().reshape(-1).contiguous())
+            self.b1.append(dec[2].bias.detach().float().contiguous())
+        m = _lib.Bf16Model()
+        m.num_lods, m.base_lod, m.feature_dim, m.hidden_dim = self.num_lods, self.base_lod, net.fdim, net.hidden_dim
+        for i in range(self.num_lods):
+            m.grid[i] = self.grids[i].data_ptr()
+            m.w0_tile[i] = self.tiles[i].data_ptr()
+            m.b0[i], m.w1[i], m.b1[i] = self.b0[i].data_ptr(), self.w1[i].data_ptr(), self.b1[i].data_ptr()
+        self._m = m
+        self._status = torch.zeros(1, dtype=torch.int32, device=dev)
+
+    def sdf(self, x, lod=None):
+        if lod is None:
+            lod = self.lod
+        _lib.require_cuda(x)
+        x = x.detach().float().contiguous()
+        out = torch.empty(x.shape[0], 1, device=x.device)
+        _lib.check(_lib.load().nglod_sdf_fwd_bf16(self._m, _lib.ptr(x), x.shape[0], -1 if lod is None else lod,
+                                                  _lib.ptr(out), _lib.ptr(self._status), _lib.stream_ptr(x.device)),
+                   "nglod_sdf_fwd_bf16")
+        return out
+
+    def check_status(self):
+        """Raises if a tensor-core wait of the last launches gave up."""
+        if int(self._status.item()) != 0:
+            raise RuntimeError("nglod_sdf_fwd_bf16: a bounded tensor-core wait timed out")
+
+    __call__ = sdf

@@ -1,0 +1,263 @@
+// BF16 form of the dense path: bf16 channel-last feature volumes gathered by
+// four lanes per point (each lane owns 8 of the 32 channels of every corner,
+// one 16-byte load per corner), the LOD sum kept in fp32 and written as one
+// row of a bf16 tile in shared memory, and the decoder's 35 -> 128 layer run
+// by tcgen05.mma on 128-point tiles with the accumulator in tensor memory.
+// b0, ReLU and the 128 -> 1 layer are an fp32 epilogue on the TMEM rows.
+#include <cuda_bf16.h>
+#include <string.h>
+
+#include "common.cuh"
+#include "tc_common.cuh"
+
+namespace nglod {
+
+constexpr int kTP = 128;                 // points per tile = threads per block = UMMA M
+constexpr int kHid = 128;                // hidden units = UMMA N
+constexpr int kTK = 48;                  // tile K (3 steps of 16)
+constexpr int kKC = kTK / 8;             // core-matrix columns along K
+constexpr uint32_t kTileBytes = kTP * kTK * 2;
+constexpr uint32_t kLbo = 128, kSbo = kKC * 128;
+constexpr uint32_t kWaitPolls = 1u << 22;
+
+// Dynamic shared memory: A tile | B tile | b0[128] | w1[128] | mbarrier |
+// TMEM slot | abort flag, padded so that at most four blocks share an SM
+// (four x 128 TMEM columns fill the SM's 512).
+constexpr size_t kSmemA = 0;
+constexpr size_t kSmemB = kSmemA + kTileBytes;
+constexpr size_t kSmemB0 = kSmemB + kTileBytes;
+constexpr size_t kSmemW1 = kSmemB0 + kHid * 4;
+constexpr size_t kSmemBar = kSmemW1 + kHid * 4;
+constexpr size_t kSmemSlot = kSmemBar + 8;
+constexpr size_t kSmemAbort = kSmemSlot + 4;
+constexpr size_t kSmemBytes = 48 * 1024;
+
+__device__ __forceinline__ float bf_lo(uint32_t v) { return __uint_as_float(v << 16); }
+__device__ __forceinline__ float bf_hi(uint32_t v) { return __uint_as_float(v & 0xffff0000u); }
+
+__device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
+    const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);  // .x = a in the low half
+    return *reinterpret_cast<const uint32_t *>(&h);
+}
+
+// Adds this lane's 8 channels (8q .. 8q+7) of the trilinear sample of one
+// bf16 volume (s vertices per side) at p to acc; PyTorch grid_sample
+// arithmetic (align_corners, border clamp), corners in tnw..bse order.
+__device__ __forceinline__ void gather_bf16_quarter(const __nv_bfloat16 *__restrict__ g, int s, float px, float py,
+                                                    float pz, int q, float (&acc)[8]) {
+    const float sm1 = (float)(s - 1);
+    const float ix = fminf(sm1, fmaxf(((px + 1.f) / 2.f) * sm1, 0.f));
+    const float iy = fminf(sm1, fmaxf(((py + 1.f) / 2.f) * sm1, 0.f));
+    const float iz = fminf(sm1, fmaxf(((pz + 1.f) / 2.f) * sm1, 0.f));
+    const float x0 = floorf(ix), y0 = floorf(iy), z0 = floorf(iz);
+    const float wx1 = ix - x0, wx0 = (x0 + 1.f) - ix;
+    const float wy1 = iy - y0, wy0 = (y0 + 1.f) - iy;
+    const float wz1 = iz - z0, wz0 = (z0 + 1.f) - iz;
+    const int xi = (int)x0, yi = (int)y0, zi = (int)z0;
+    const int xj = min(xi + 1, s - 1), yj = min(yi + 1, s - 1), zj = min(zi + 1, s - 1);
+    const uint4 *base = reinterpret_cast<const uint4 *>(g) + q;  // 4 uint4 per vertex
+    const int64_t sy = (int64_t)s * 4, sz = (int64_t)s * sy;
+    const int64_t o[8] = {zi * sz + yi * sy + xi * 4, zi * sz + yi * sy + xj * 4, zi * sz + yj * sy + xi * 4,
+                          zi * sz + yj * sy + xj * 4, zj * sz + yi * sy + xi * 4, zj * sz + yi * sy + xj * 4,
+                          zj * sz + yj * sy + xi * 4, zj * sz + yj * sy + xj * 4};
+    const float w[8] = {wx0 * wy0 * wz0, wx1 * wy0 * wz0, wx0 * wy1 * wz0, wx1 * wy1 * wz0,
+                        wx0 * wy0 * wz1, wx1 * wy0 * wz1, wx0 * wy1 * wz1, wx1 * wy1 * wz1};
+    uint4 v[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) v[k] = __ldg(base + o[k]);
+    float a[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        a[0] = fmaf(bf_lo(v[k].x), w[k], a[0]);
+        a[1] = fmaf(bf_hi(v[k].x), w[k], a[1]);
+        a[2] = fmaf(bf_lo(v[k].y), w[k], a[2]);
+        a[3] = fmaf(bf_hi(v[k].y), w[k], a[3]);
+        a[4] = fmaf(bf_lo(v[k].z), w[k], a[4]);
+        a[5] = fmaf(bf_hi(v[k].z), w[k], a[5]);
+        a[6] = fmaf(bf_lo(v[k].w), w[k], a[6]);
+        a[7] = fmaf(bf_hi(v[k].w), w[k], a[7]);
+    }
+#pragma unroll
+    for (int c = 0; c < 8; ++c) acc[c] += a[c];
+}
+
+struct Bf16Args {
+    nglod_bf16_model m;
+    const float *x;
+    int64_t n;
+    int L;
+    float *out;
+    int *status;
+};
+
+__global__ void __launch_bounds__(kTP, 4) sdf_fwd_bf16_tc_kernel(const Bf16Args a) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    uint8_t *sA = smem + kSmemA;
+    uint8_t *sB = smem + kSmemB;
+    float *sb0 = reinterpret_cast<float *>(smem + kSmemB0);
+    float *sw1 = reinterpret_cast<float *>(smem + kSmemW1);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + kSmemBar);
+    uint32_t *slot = reinterpret_cast<uint32_t *>(smem + kSmemSlot);
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + kSmemAbort);
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const uint4 *bsrc = static_cast<const uint4 *>(a.m.w0_tile[a.L]);
+    for (int i = tid; i < (int)(kTileBytes / 16); i += kTP) reinterpret_cast<uint4 *>(sB)[i] = bsrc[i];
+    sb0[tid] = a.m.b0[a.L][tid];
+    sw1[tid] = a.m.w1[a.L][tid];
+    const float b1 = a.m.b1[a.L][0];
+    // K core-matrix column 5 (k 40..47) is always zero.
+    for (int i = tid; i < (kTP / 8) * 8; i += kTP) {
+        const int grp = i >> 3, r = i & 7;
+        *reinterpret_cast<uint4 *>(sA + (grp * kKC + 5) * 128 + r * 16) = make_uint4(0u, 0u, 0u, 0u);
+    }
+    if (warp == 0) tc::tmem_alloc(slot, kHid);
+    if (tid == 0) {
+        tc::mbar_init(bar, 1);
+        *abort_flag = 0;
+    }
+    tc::fence_proxy_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = *slot;
+    const uint32_t sa = tc::smem_addr(sA), sb = tc::smem_addr(sB);
+    const uint32_t idesc = tc::idesc_bf16_f32(kTP, kHid);
+    uint32_t phase = 0;
+    const int pp = lane >> 2, q = lane & 3;
+
+    for (int64_t tile = blockIdx.x; tile * kTP < a.n; tile += gridDim.x) {
+        // 1. gather: warp w fills rows 32w .. 32w+31, eight points per pass
+#pragma unroll 1
+        for (int pass = 0; pass < 4; ++pass) {
+            const int row = warp * 32 + pass * 8 + pp;
+            const int64_t gi = tile * kTP + row;
+            float px = 0.f, py = 0.f, pz = 0.f;
+            if (gi < a.n) {
+                px = a.x[3 * gi];
+                py = a.x[3 * gi + 1];
+                pz = a.x[3 * gi + 2];
+            }
+            float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll 1
+            for (int l = 0; l <= a.L; ++l)
+                gather_bf16_quarter(static_cast<const __nv_bfloat16 *>(a.m.grid[l]), (1 << (l + a.m.base_lod)) + 1,
+                                    px, py, pz, q, acc);
+            const uint4 f = make_uint4(pack_bf16x2(acc[0], acc[1]), pack_bf16x2(acc[2], acc[3]),
+                                       pack_bf16x2(acc[4], acc[5]), pack_bf16x2(acc[6], acc[7]));
+            *reinterpret_cast<uint4 *>(sA + tc::tile_offset(row, 8 * q, kKC)) = f;
+            if (q == 0) {
+                const float hx = __bfloat162float(__float2bfloat16_rn(px));
+                const float hy = __bfloat162float(__float2bfloat16_rn(py));
+                const float hz = __bfloat162float(__float2bfloat16_rn(pz));
+                const uint4 p = make_uint4(pack_bf16x2(hx, hy), pack_bf16x2(hz, px - hx), pack_bf16x2(py - hy, pz - hz),
+                                           0u);
+                *reinterpret_cast<uint4 *>(sA + tc::tile_offset(row, 32, kKC)) = p;
+            }
+        }
+        tc::fence_proxy_async_smem();
+        __syncthreads();
+        // 2. one thread issues the three K steps and commits to the barrier
+        if (tid == 0) {
+            tc::fence_after_sync();
+#pragma unroll
+            for (int ks = 0; ks < kTK / 16; ++ks) {
+                const uint64_t ad = tc::smem_desc(sa + ks * 256, kLbo, kSbo);
+                const uint64_t bd = tc::smem_desc(sb + ks * 256, kLbo, kSbo);
+                tc::mma_bf16(tmem, ad, bd, idesc, ks > 0 ? 1u : 0u);
+            }
+            tc::mma_commit(bar);
+            if (!tc::mbar_wait_bounded(bar, phase, kWaitPolls)) {
+                *abort_flag = 1;
+                atomicExch(a.status, 1);
+            }
+        }
+        __syncthreads();
+        if (*abort_flag) break;
+        phase ^= 1u;
+        tc::fence_after_sync();
+        // 3. epilogue: thread (w, lane) owns TMEM lane / tile row 32w + lane
+        float o = 0.f;
+#pragma unroll 1
+        for (int c = 0; c < kHid / 32; ++c) {
+            float v[32];
+            tc::tmem_load32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c * 32), v);
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+                const float h = fmaxf(v[j] + sb0[c * 32 + j], 0.f);
+                o = fmaf(sw1[c * 32 + j], h, o);
+            }
+        }
+        const int64_t gi = tile * kTP + warp * 32 + lane;
+        if (gi < a.n) a.out[gi] = o + b1;
+        tc::fence_before_sync();
+        __syncthreads();
+    }
+    if (*abort_flag && tid == 0) tc::mbar_wait_bounded(bar, phase, kWaitPolls);  // let an in-flight MMA finish
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if (warp == 0) tc::tmem_dealloc(tmem, kHid);
+}
+
+}  // namespace nglod
+
+using namespace nglod;
+
+extern "C" int nglod_bf16_pack_decoder(const float *w0_host, int32_t hidden_dim, int32_t in_dim, void *tile_host) {
+    NGLOD_REQUIRE(w0_host && tile_host, NGLOD_ERR_INVALID, "null pointer argument");
+    NGLOD_REQUIRE(hidden_dim == kHid && in_dim == 35, NGLOD_ERR_UNSUPPORTED,
+                  "bf16 decoder tile built for w0 [128][35], got [%d][%d]", hidden_dim, in_dim);
+    uint16_t *t = static_cast<uint16_t *>(tile_host);
+    memset(t, 0, kTileBytes);
+    for (int n = 0; n < kHid; ++n) {
+        for (int k = 0; k < kTK; ++k) {
+            float w = 0.f;
+            if (k < 32) w = w0_host[n * 35 + 3 + k];
+            else if (k < 35) w = w0_host[n * 35 + (k - 32)];
+            else if (k < 38) w = w0_host[n * 35 + (k - 35)];
+            const __nv_bfloat16 b = __float2bfloat16_rn(w);
+            uint16_t bits;
+            memcpy(&bits, &b, 2);
+            t[tc::tile_offset(n, k, kKC) / 2] = bits;
+        }
+    }
+    return NGLOD_OK;
+}
+
+extern "C" int nglod_sdf_fwd_bf16(const nglod_bf16_model *model, const float *x, int64_t n, int32_t lod, float *out,
+                                  int32_t *status, nglod_stream_t stream) {
+    NGLOD_REQUIRE(model != nullptr, NGLOD_ERR_INVALID, "model is null");
+    NGLOD_REQUIRE(model->num_lods >= 1 && model->num_lods <= NGLOD_MAX_LODS, NGLOD_ERR_INVALID, "num_lods=%d",
+                  model->num_lods);
+    NGLOD_REQUIRE(model->feature_dim == 32 && model->hidden_dim == kHid, NGLOD_ERR_UNSUPPORTED,
+                  "bf16 form built for feature_dim 32 and hidden_dim 128");
+    NGLOD_REQUIRE(model->base_lod >= 0 && model->num_lods - 1 + model->base_lod <= 9, NGLOD_ERR_INVALID,
+                  "base_lod=%d", model->base_lod);
+    const int L = (lod < 0 || lod >= model->num_lods) ? model->num_lods - 1 : lod;
+    for (int l = 0; l <= L; ++l)
+        NGLOD_REQUIRE(model->grid[l] && aligned(model->grid[l], 16), NGLOD_ERR_ALIGN,
+                      "bf16 volume %d is null or not 16-byte aligned", l);
+    NGLOD_REQUIRE(model->w0_tile[L] && aligned(model->w0_tile[L], 16) && model->b0[L] && model->w1[L] &&
+                      model->b1[L],
+                  NGLOD_ERR_INVALID, "decoder %d: null or misaligned tile/bias pointer", L);
+    NGLOD_REQUIRE(n >= 0, NGLOD_ERR_INVALID, "n=%lld is negative", (long long)n);
+    if (n == 0) return NGLOD_OK;
+    NGLOD_REQUIRE(x && out && status, NGLOD_ERR_INVALID, "null pointer argument");
+    cudaStream_t s = (cudaStream_t)stream;
+    NGLOD_TRY(cuda_status(cudaMemsetAsync(status, 0, sizeof(int32_t), s), "nglod_sdf_fwd_bf16 memset"));
+    Bf16Args a;
+    a.m = *model;
+    a.x = x;
+    a.n = n;
+    a.L = L;
+    a.out = out;
+    a.status = status;
+    NGLOD_TRY(cuda_status(
+        cudaFuncSetAttribute(sdf_fwd_bf16_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes),
+        "cudaFuncSetAttribute"));
+    const int64_t tiles = (n + kTP - 1) / kTP;
+    const int64_t cap = (int64_t)num_sms() * 4;
+    sdf_fwd_bf16_tc_kernel<<<(int)(tiles < cap ? tiles : cap), kTP, kSmemBytes, s>>>(a);
+    return launch_status("nglod_sdf_fwd_bf16");
+}
