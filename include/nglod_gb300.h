@@ -144,6 +144,15 @@ int nglod_bf16_pack_decoder(const float *w0_host, int32_t hidden_dim, int32_t in
 int nglod_sdf_fwd_bf16(const nglod_bf16_model *model, const float *x, int64_t n, int32_t lod, float *out,
                        int32_t *status, nglod_stream_t stream);
 
+/* SphereTracer.forward in the BF16 form: the persistent tracer of
+ * nglod_trace with every sdf evaluation (march points and normal taps) done
+ * by the bf16 tile kernel above, 128 rays per block evaluated together.
+ * Same outputs and march rules as nglod_trace.  status: one device int32,
+ * nonzero if a bounded tensor-core wait gave up. */
+int nglod_trace_bf16(const nglod_bf16_model *model, const nglod_trace_params *params, const float *ray_o,
+                     const float *ray_d, int64_t n, float *x, float *t, uint8_t *hit, float *normal,
+                     int64_t *work_counter, int32_t *status, nglod_stream_t stream);
+
 /* ------------------------------------------------------------------------
  * Training: forward with saved features, hand-written backward, Adam.
  * ------------------------------------------------------------------------ */

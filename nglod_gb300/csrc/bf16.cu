@@ -81,6 +81,32 @@ __device__ __forceinline__ void gather_bf16_quarter(const __nv_bfloat16 *__restr
     for (int c = 0; c < 8; ++c) acc[c] += a[c];
 }
 
+
+// Ray entry into [-1,1]^3 with sol_nglod_kernel.cu:92-150's float arithmetic
+// (same as the float32 path's box_entry).
+__device__ __forceinline__ bool box_entry_bf(float ox, float oy, float oz, float dx, float dy, float dz, float &t) {
+    const float ivx = (float)(1.0 / (double)dx);
+    const float ivy = (float)(1.0 / (double)dy);
+    const float ivz = (float)(1.0 / (double)dz);
+    const float s0 = signbit(dx) ? 1.f : -1.f;
+    const float s1 = signbit(dy) ? 1.f : -1.f;
+    const float s2 = signbit(dz) ? 1.f : -1.f;
+    const float cmax = fmaxf(fmaxf(fabsf(ox), fabsf(oy)), fabsf(oz));
+    if (cmax < 1.f) return false;
+    const float d0 = __fmul_rn(__fsub_rn(s0, ox), ivx);
+    const float d1 = __fmul_rn(__fsub_rn(s1, oy), ivy);
+    const float d2 = __fmul_rn(__fsub_rn(s2, oz), ivz);
+    const bool t0 = (d0 >= 0.f) && (fabsf(fmaf(dy, d0, oy)) < 1.f) && (fabsf(fmaf(dz, d0, oz)) < 1.f);
+    const bool t1 = (d1 >= 0.f) && (fabsf(fmaf(dx, d1, ox)) < 1.f) && (fabsf(fmaf(dz, d1, oz)) < 1.f);
+    const bool t2 = (d2 >= 0.f) && (fabsf(fmaf(dx, d2, ox)) < 1.f) && (fabsf(fmaf(dy, d2, oy)) < 1.f);
+    const float dd = t0 ? d0 : (t1 ? d1 : (t2 ? d2 : 0.f));
+    if ((t0 || t1 || t2) && dd < 500.f) {
+        t = dd;
+        return true;
+    }
+    return false;
+}
+
 struct Bf16Args {
     nglod_bf16_model m;
     const float *x;
@@ -200,6 +226,258 @@ __global__ void __launch_bounds__(kTP, 4) sdf_fwd_bf16_tc_kernel(const Bf16Args 
     if (warp == 0) tc::tmem_dealloc(tmem, kHid);
 }
 
+
+// ---------------------------------------------------------------------------
+// persistent BF16 sphere tracer
+// ---------------------------------------------------------------------------
+// 128 ray slots per block, one per thread.  Every iteration each slot
+// publishes one query point (the ray's next march point or one of its six
+// normal taps), the block gathers and decodes all 128 points as one tile
+// (above), and each thread advances its ray with SphereTracer.forward's state
+// machine (sdf-net/lib/tracer/SphereTracer.py:74-130, same rules as the float32
+// persistent tracer).  Finished slots write their ray out and take the next
+// ray index from a global counter, one atomicAdd per warp.
+struct Bf16TraceArgs {
+    nglod_bf16_model m;
+    nglod_trace_params p;
+    int L;
+    const float *ray_o;
+    const float *ray_d;
+    int64_t n;
+    float *x;
+    float *t;
+    uint8_t *hit;
+    float *normal;
+    unsigned long long *counter;
+    int *status;
+};
+
+constexpr size_t kSmemQ = (kSmemAbort + 4 + 15) & ~(size_t)15;  // float4 query points [128], 16-byte aligned
+static_assert(kSmemQ % 16 == 0 && kSmemQ + kTP * 16 <= kSmemBytes, "query-point array layout");
+static_assert(kSmemBar % 8 == 0 && kSmemB % 16 == 0, "barrier / tile alignment");
+
+enum : int { bNeed = 0, bEvalInit = 1, bMarch = 2, bTap0 = 3, bDone = 9, bGone = 10 };
+
+__global__ void __launch_bounds__(kTP, 4) trace_bf16_tc_kernel(const Bf16TraceArgs a) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    uint8_t *sA = smem + kSmemA;
+    uint8_t *sB = smem + kSmemB;
+    float *sb0 = reinterpret_cast<float *>(smem + kSmemB0);
+    float *sw1 = reinterpret_cast<float *>(smem + kSmemW1);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + kSmemBar);
+    uint32_t *slot = reinterpret_cast<uint32_t *>(smem + kSmemSlot);
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + kSmemAbort);
+    float4 *qpts = reinterpret_cast<float4 *>(smem + kSmemQ);
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const uint4 *bsrc = static_cast<const uint4 *>(a.m.w0_tile[a.L]);
+    for (int i = tid; i < (int)(kTileBytes / 16); i += kTP) reinterpret_cast<uint4 *>(sB)[i] = bsrc[i];
+    sb0[tid] = a.m.b0[a.L][tid];
+    sw1[tid] = a.m.w1[a.L][tid];
+    const float b1 = a.m.b1[a.L][0];
+    for (int i = tid; i < (kTP / 8) * 8; i += kTP) {
+        const int grp = i >> 3, r = i & 7;
+        *reinterpret_cast<uint4 *>(sA + (grp * kKC + 5) * 128 + r * 16) = make_uint4(0u, 0u, 0u, 0u);
+    }
+    if (warp == 0) tc::tmem_alloc(slot, kHid);
+    if (tid == 0) {
+        tc::mbar_init(bar, 1);
+        *abort_flag = 0;
+    }
+    tc::fence_proxy_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = *slot;
+    const uint32_t sa = tc::smem_addr(sA), sb = tc::smem_addr(sB);
+    const uint32_t idesc = tc::idesc_bf16_f32(kTP, kHid);
+    uint32_t mphase = 0;
+    const int pp = lane >> 2, q = lane & 3;
+
+    const unsigned FULL = 0xffffffffu;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    const float h = 1.0f / 192.0f;
+    const float twoh = (float)(2.0 / 192.0);
+    int phase = bNeed, step = 0;
+    int64_t ray = 0;
+    float ox = 0.f, oy = 0.f, oz = 0.f, dx = 0.f, dy = 0.f, dz = 0.f;
+    float xx = 0.f, xy = 0.f, xz = 0.f, t = 0.f, d = 0.f, dprev = 0.f;
+    float g[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    float nx = 0.f, ny = 0.f, nz = 0.f;
+    bool cond = false, hitr = false, hitf = false;
+
+    auto finish = [&]() {
+        hitf = hitr && !(fabsf(xx) > 1.f || fabsf(xy) > 1.f || fabsf(xz) > 1.f);
+        phase = (hitf && a.p.want_normals) ? bTap0 : bDone;
+    };
+    auto march_decide = [&]() {
+        if (step >= a.p.num_steps) {
+            finish();
+            return;
+        }
+        hitr = fabsf(t) < a.p.far_clip;
+        cond = cond && (fabsf(d) > a.p.min_dis) && (fabsf((d + dprev) / 2.f) > a.p.osc_dis) && hitr;
+        if (!cond) {
+            finish();
+            return;
+        }
+        xx = __fadd_rn(ox, __fmul_rn(dx, t));
+        xy = __fadd_rn(oy, __fmul_rn(dy, t));
+        xz = __fadd_rn(oz, __fmul_rn(dz, t));
+        dprev = d;
+        phase = bMarch;
+    };
+
+    for (;;) {
+        for (;;) {
+            if (phase == bDone) {
+                a.x[3 * ray + 0] = xx;
+                a.x[3 * ray + 1] = xy;
+                a.x[3 * ray + 2] = xz;
+                a.t[ray] = t;
+                a.hit[ray] = hitf ? 1 : 0;
+                if (a.normal) {
+                    const bool hn = hitf && a.p.want_normals;
+                    a.normal[3 * ray + 0] = hn ? nx : 0.f;
+                    a.normal[3 * ray + 1] = hn ? ny : 0.f;
+                    a.normal[3 * ray + 2] = hn ? nz : 0.f;
+                }
+                phase = bNeed;
+            }
+            const unsigned need = __ballot_sync(FULL, phase == bNeed);
+            if (need == 0u) break;
+            const int leader = __ffs(need) - 1;
+            unsigned long long base = 0ull;
+            if (lane == leader) base = atomicAdd(a.counter, (unsigned long long)__popc(need));
+            base = __shfl_sync(FULL, base, leader);
+            if (phase == bNeed) {
+                const unsigned long long r = base + (unsigned long long)__popc(need & lt_mask);
+                if (r >= (unsigned long long)a.n) {
+                    phase = bGone;
+                } else {
+                    ray = (int64_t)r;
+                    ox = a.ray_o[3 * ray];
+                    oy = a.ray_o[3 * ray + 1];
+                    oz = a.ray_o[3 * ray + 2];
+                    dx = a.ray_d[3 * ray];
+                    dy = a.ray_d[3 * ray + 1];
+                    dz = a.ray_d[3 * ray + 2];
+                    t = 0.f;
+                    cond = box_entry_bf(ox, oy, oz, dx, dy, dz, t);
+                    xx = cond ? fmaf(dx, t, ox) : ox;
+                    xy = cond ? fmaf(dy, t, oy) : oy;
+                    xz = cond ? fmaf(dz, t, oz) : oz;
+                    step = 0;
+                    hitr = false;
+                    hitf = false;
+                    if (cond)
+                        phase = bEvalInit;
+                    else
+                        march_decide();
+                }
+            }
+        }
+        if (__syncthreads_and(phase == bGone)) break;
+
+        float qx = xx, qy = xy, qz = xz;
+        if (phase >= bTap0 && phase < bDone) {
+            const int k = phase - bTap0;
+            const float e = (k & 1) ? -h : h;
+            if ((k >> 1) == 0) qx = __fadd_rn(xx, e);
+            else if ((k >> 1) == 1) qy = __fadd_rn(xy, e);
+            else qz = __fadd_rn(xz, e);
+        }
+        if (phase == bGone) qx = qy = qz = 0.f;
+        qpts[tid] = make_float4(qx, qy, qz, 0.f);
+        __syncthreads();
+#pragma unroll 1
+        for (int pass = 0; pass < 4; ++pass) {
+            const int row = warp * 32 + pass * 8 + pp;
+            const float4 pt = qpts[row];
+            float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll 1
+            for (int l = 0; l <= a.L; ++l)
+                gather_bf16_quarter(static_cast<const __nv_bfloat16 *>(a.m.grid[l]), (1 << (l + a.m.base_lod)) + 1,
+                                    pt.x, pt.y, pt.z, q, acc);
+            const uint4 f = make_uint4(pack_bf16x2(acc[0], acc[1]), pack_bf16x2(acc[2], acc[3]),
+                                       pack_bf16x2(acc[4], acc[5]), pack_bf16x2(acc[6], acc[7]));
+            *reinterpret_cast<uint4 *>(sA + tc::tile_offset(row, 8 * q, kKC)) = f;
+            if (q == 0) {
+                const float hx = __bfloat162float(__float2bfloat16_rn(pt.x));
+                const float hy = __bfloat162float(__float2bfloat16_rn(pt.y));
+                const float hz = __bfloat162float(__float2bfloat16_rn(pt.z));
+                const uint4 pp4 = make_uint4(pack_bf16x2(hx, hy), pack_bf16x2(hz, pt.x - hx),
+                                             pack_bf16x2(pt.y - hy, pt.z - hz), 0u);
+                *reinterpret_cast<uint4 *>(sA + tc::tile_offset(row, 32, kKC)) = pp4;
+            }
+        }
+        tc::fence_proxy_async_smem();
+        __syncthreads();
+        if (tid == 0) {
+            tc::fence_after_sync();
+#pragma unroll
+            for (int ks = 0; ks < kTK / 16; ++ks) {
+                const uint64_t ad = tc::smem_desc(sa + ks * 256, kLbo, kSbo);
+                const uint64_t bd = tc::smem_desc(sb + ks * 256, kLbo, kSbo);
+                tc::mma_bf16(tmem, ad, bd, idesc, ks > 0 ? 1u : 0u);
+            }
+            tc::mma_commit(bar);
+            if (!tc::mbar_wait_bounded(bar, mphase, kWaitPolls)) {
+                *abort_flag = 1;
+                atomicExch(a.status, 1);
+            }
+        }
+        __syncthreads();
+        if (*abort_flag) break;
+        mphase ^= 1u;
+        tc::fence_after_sync();
+        float v = 0.f;
+#pragma unroll 1
+        for (int c = 0; c < kHid / 32; ++c) {
+            float hv[32];
+            tc::tmem_load32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c * 32), hv);
+#pragma unroll
+            for (int j = 0; j < 32; ++j) v = fmaf(sw1[c * 32 + j], fmaxf(hv[j] + sb0[c * 32 + j], 0.f), v);
+        }
+        v += b1;
+        tc::fence_before_sync();
+
+        if (phase == bEvalInit) {
+            d = v;
+            dprev = d;
+            march_decide();
+        } else if (phase == bMarch) {
+            d = v * a.p.step_size;
+            t = t + d;
+            ++step;
+            march_decide();
+        } else if (phase >= bTap0 && phase < bDone) {
+            const int k = phase - bTap0;
+#pragma unroll
+            for (int i = 0; i < 6; ++i)
+                if (i == k) g[i] = v;
+            if (k == 5) {
+                const float gx = (g[0] - g[1]) / twoh;
+                const float gy = (g[2] - g[3]) / twoh;
+                const float gz = (g[4] - g[5]) / twoh;
+                const float nrm = sqrtf(gx * gx + gy * gy + gz * gz);
+                const float den = fmaxf(nrm, 1e-5f);
+                nx = gx / den;
+                ny = gy / den;
+                nz = gz / den;
+                phase = bDone;
+            } else {
+                phase = phase + 1;
+            }
+        }
+    }
+    if (*abort_flag && tid == 0) tc::mbar_wait_bounded(bar, mphase, kWaitPolls);
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if (warp == 0) tc::tmem_dealloc(tmem, kHid);
+}
+
 }  // namespace nglod
 
 using namespace nglod;
@@ -260,4 +538,53 @@ extern "C" int nglod_sdf_fwd_bf16(const nglod_bf16_model *model, const float *x,
     const int64_t cap = (int64_t)num_sms() * 4;
     sdf_fwd_bf16_tc_kernel<<<(int)(tiles < cap ? tiles : cap), kTP, kSmemBytes, s>>>(a);
     return launch_status("nglod_sdf_fwd_bf16");
+}
+
+extern "C" int nglod_trace_bf16(const nglod_bf16_model *model, const nglod_trace_params *params, const float *ray_o,
+                                const float *ray_d, int64_t n, float *x, float *t, uint8_t *hit, float *normal,
+                                int64_t *work_counter, int32_t *status, nglod_stream_t stream) {
+    NGLOD_REQUIRE(model != nullptr && params != nullptr, NGLOD_ERR_INVALID, "model or params is null");
+    NGLOD_REQUIRE(model->num_lods >= 1 && model->num_lods <= NGLOD_MAX_LODS, NGLOD_ERR_INVALID, "num_lods=%d",
+                  model->num_lods);
+    NGLOD_REQUIRE(model->feature_dim == 32 && model->hidden_dim == kHid, NGLOD_ERR_UNSUPPORTED,
+                  "bf16 form built for feature_dim 32 and hidden_dim 128");
+    NGLOD_REQUIRE(model->base_lod >= 0 && model->num_lods - 1 + model->base_lod <= 9, NGLOD_ERR_INVALID,
+                  "base_lod=%d", model->base_lod);
+    NGLOD_REQUIRE(params->num_steps >= 0, NGLOD_ERR_INVALID, "num_steps=%d is negative", params->num_steps);
+    const int L = (params->lod < 0 || params->lod >= model->num_lods) ? model->num_lods - 1 : params->lod;
+    for (int l = 0; l <= L; ++l)
+        NGLOD_REQUIRE(model->grid[l] && aligned(model->grid[l], 16), NGLOD_ERR_ALIGN,
+                      "bf16 volume %d is null or not 16-byte aligned", l);
+    NGLOD_REQUIRE(model->w0_tile[L] && aligned(model->w0_tile[L], 16) && model->b0[L] && model->w1[L] &&
+                      model->b1[L],
+                  NGLOD_ERR_INVALID, "decoder %d: null or misaligned tile/bias pointer", L);
+    NGLOD_REQUIRE(n >= 0, NGLOD_ERR_INVALID, "n=%lld is negative", (long long)n);
+    if (n == 0) return NGLOD_OK;
+    NGLOD_REQUIRE(ray_o && ray_d && x && t && hit && work_counter && status, NGLOD_ERR_INVALID,
+                  "null pointer argument");
+    NGLOD_REQUIRE(normal || !params->want_normals, NGLOD_ERR_INVALID, "normals requested with a null buffer");
+    NGLOD_REQUIRE(aligned(work_counter, 8), NGLOD_ERR_ALIGN, "work_counter is not 8-byte aligned");
+    cudaStream_t s = (cudaStream_t)stream;
+    NGLOD_TRY(cuda_status(cudaMemsetAsync(status, 0, sizeof(int32_t), s), "nglod_trace_bf16 memset"));
+    NGLOD_TRY(cuda_status(cudaMemsetAsync(work_counter, 0, sizeof(int64_t), s), "nglod_trace_bf16 memset"));
+    Bf16TraceArgs a;
+    a.m = *model;
+    a.p = *params;
+    a.L = L;
+    a.ray_o = ray_o;
+    a.ray_d = ray_d;
+    a.n = n;
+    a.x = x;
+    a.t = t;
+    a.hit = hit;
+    a.normal = normal;
+    a.counter = reinterpret_cast<unsigned long long *>(work_counter);
+    a.status = status;
+    NGLOD_TRY(cuda_status(
+        cudaFuncSetAttribute(trace_bf16_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes),
+        "cudaFuncSetAttribute"));
+    const int64_t want = (n + kTP - 1) / kTP;
+    const int64_t cap = (int64_t)num_sms() * 4;
+    trace_bf16_tc_kernel<<<(int)(want < cap ? want : cap), kTP, kSmemBytes, s>>>(a);
+    return launch_status("nglod_trace_bf16");
 }

@@ -105,17 +105,26 @@ class BaseTracer(object):
 
 
 def _check_net(net, grad_method):
-    if not isinstance(net, OctreeSDF):
-        raise TypeError("nglod_gb300.SphereTracer traces nglod_gb300.OctreeSDF networks")
+    from .bf16 import Bf16OctreeSDF
+    if not isinstance(net, (OctreeSDF, Bf16OctreeSDF)):
+        raise TypeError("nglod_gb300.SphereTracer traces nglod_gb300.OctreeSDF / Bf16OctreeSDF networks")
     if grad_method != "finitediff":
         raise NotImplementedError(f"grad_method={grad_method!r}: the fused tracer computes 'finitediff' normals")
 
 
 class SphereTracer(BaseTracer):
-    """Persistent fused sphere tracer (one kernel launch per call)."""
+    """Persistent fused sphere tracer (one kernel launch per call).
+
+    A float32 ``OctreeSDF`` is traced by ``nglod_trace``; a ``Bf16OctreeSDF``
+    (the BF16 form) by ``nglod_trace_bf16``, which evaluates 128 rays per
+    block on the tensor cores.
+    """
 
     def forward(self, net, ray_o, ray_d):
         _check_net(net, self.grad_method)
+        from .bf16 import Bf16OctreeSDF
+        if isinstance(net, Bf16OctreeSDF):
+            return self._forward_bf16(net, ray_o, ray_d)
         _lib.require_cuda(ray_o, ray_d)
         ray_o = ray_o.detach().float().contiguous()
         ray_d = ray_d.detach().float().contiguous()
@@ -131,6 +140,23 @@ class SphereTracer(BaseTracer):
         _lib.check(_lib.load().nglod_trace(m, p, _lib.ptr(ray_o), _lib.ptr(ray_d), n, _lib.ptr(x), _lib.ptr(t),
                                            _lib.ptr(hit), _lib.ptr(normal), _lib.ptr(counter),
                                            _lib.stream_ptr(dev)), "nglod_trace")
+        return RenderBuffer(x=x, depth=t, hit=hit, normal=normal)
+
+    def _forward_bf16(self, net, ray_o, ray_d):
+        _lib.require_cuda(ray_o, ray_d)
+        ray_o = ray_o.detach().float().contiguous()
+        ray_d = ray_d.detach().float().contiguous()
+        n = ray_o.shape[0]
+        dev = ray_o.device
+        x = torch.empty(n, 3, device=dev, dtype=torch.float32)
+        t = torch.empty(n, 1, device=dev, dtype=torch.float32)
+        hit = torch.empty(n, device=dev, dtype=torch.bool)
+        normal = torch.empty(n, 3, device=dev, dtype=torch.float32)
+        counter = torch.empty(1, device=dev, dtype=torch.int64)
+        p = self.trace_params(net)
+        _lib.check(_lib.load().nglod_trace_bf16(net._m, p, _lib.ptr(ray_o), _lib.ptr(ray_d), n, _lib.ptr(x),
+                                                _lib.ptr(t), _lib.ptr(hit), _lib.ptr(normal), _lib.ptr(counter),
+                                                _lib.ptr(net._status), _lib.stream_ptr(dev)), "nglod_trace_bf16")
         return RenderBuffer(x=x, depth=t, hit=hit, normal=normal)
 
 

@@ -90,3 +90,43 @@ def test_bf16_full_size_against_float32_path(nets):
     assert d.max().item() < 2e-2 and d.mean().item() < 2e-3
     bnet.check_status()
     assert bnet.sdf(torch.zeros(0, 3, device=dev)).shape == (0, 1)
+
+
+def test_bf16_trace_against_fp64_oracle(nets):
+    """BF16 served tracer vs the FP64 oracle trace: hit masks and depth."""
+    from oracle import cref
+    net, bnet, m32, m64, _ = nets
+    dev = net.features[0].fm.device
+    ro, rd = synthetic.look_at_rays(width=96, height=96)
+    tr = ng.SphereTracer(default_args(num_steps=128))
+    rb = tr(bnet, ro.to(dev), rd.to(dev))
+    bnet.check_status()
+    x, t, hit, normal = dense.sphere_trace(m64, ro.numpy().astype(np.float64), rd.numpy().astype(np.float64),
+                                           num_steps=128, aabb_fn=lambda o, d: tuple(
+                                               v.astype(np.float64) if v.dtype != bool else v
+                                               for v in cref.aabb(o.astype(np.float32), d.astype(np.float32))))
+    h = rb.hit.cpu().numpy()
+    assert hit.sum() > 1500
+    assert (h == hit).mean() > 0.995
+    both = h & hit
+    err = np.abs(rb.depth.cpu().numpy()[both] - t[both])
+    print(f"bf16 trace depth error vs fp64: mean {err.mean():.2e} p99 {np.percentile(err, 99):.2e} max {err.max():.2e}")
+    assert err.mean() < 1e-3 and np.percentile(err, 99) < 5e-3
+    cosang = (rb.normal.cpu().numpy()[both] * normal[both]).sum(-1)
+    assert np.median(cosang) > 0.999
+
+
+def test_bf16_trace_matches_fp32_trace_semantics(nets):
+    """Same rules as the float32 tracer: rays that start inside the box are
+    hits at depth 0, misses keep x = ray_o, normals of non-hits are 0."""
+    net, bnet, _, _, _ = nets
+    dev = net.features[0].fm.device
+    ro = torch.tensor([[0.0, 0.0, 0.0], [3.0, 3.0, 3.0], [0.0, 0.0, 4.0]], device=dev)
+    rd = torch.tensor([[1.0, 0.0, 0.0], [1.0, 0.0, 0.0], [0.0, 0.0, -1.0]], device=dev)
+    a = ng.SphereTracer(default_args(num_steps=64))
+    r16 = a(bnet, ro, rd)
+    r32 = a(net, ro, rd)
+    assert torch.equal(r16.hit, r32.hit)
+    assert r16.depth[0, 0].item() == 0.0 and torch.equal(r16.x[1], ro[1])
+    assert (r16.normal[~r16.hit] == 0).all()
+    assert abs(r16.depth[2, 0].item() - r32.depth[2, 0].item()) < 5e-3
