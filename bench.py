@@ -259,7 +259,7 @@ def run_ours(args):
 
     extras = {}
     if not args.no_extras:
-        extras["trace"] = bench_trace(net, dev, flush, stream)
+        extras["trace"] = bench_trace(net, bnet, dev, flush, stream)
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_extras:
@@ -287,7 +287,7 @@ def run_ours(args):
         print(json.dumps(line), flush=True)
 
 
-def bench_trace(net, dev, flush, stream):
+def bench_trace(net, bnet, dev, flush, stream):
     import nglod_gb300 as ng
     from nglod_gb300 import synthetic
     from nglod_gb300.options import default_args
@@ -303,6 +303,13 @@ def bench_trace(net, dev, flush, stream):
     reps = 10
     ms = time_steps(lambda: fused(net, ro, rd), reps, flush, stream) / reps
     hits = int(rb.hit.sum().item())
+    for _ in range(3):
+        rb16 = fused(bnet, ro, rd)
+    torch.cuda.synchronize()
+    ms16 = time_steps(lambda: fused(bnet, ro, rd), reps, flush, stream) / reps
+    bnet.check_status()
+    both = rb.hit & rb16.hit
+    derr = (rb.depth[both] - rb16.depth[both]).abs()
     plain(net, ro, rd)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -311,7 +318,11 @@ def bench_trace(net, dev, flush, stream):
     pms = (time.perf_counter() - t0) * 1e3
     return {"workload": f"SphereTracer {TRACE_W}x{TRACE_H}, {TRACE_STEPS} steps, lod=None (finest), camera (0,0,4) fov 30",
             "fused_f32_rays_per_s": n / (ms / 1e3), "fused_f32_ms": ms,
-            "plain_f32_rays_per_s": n / (pms / 1e3), "plain_f32_ms": pms, "hits": hits, "kernel_launches_fused": 2}
+            "fused_bf16_rays_per_s": n / (ms16 / 1e3), "fused_bf16_ms": ms16,
+            "bf16_vs_f32_hit_agreement": float((rb.hit == rb16.hit).float().mean().item()),
+            "bf16_vs_f32_depth_mean_abs": float(derr.mean().item()) if derr.numel() else None,
+            "plain_f32_rays_per_s": n / (pms / 1e3), "plain_f32_ms": pms, "hits": hits, "kernel_launches_fused": 2,
+            "bf16_over_plain_f32": (n / (ms16 / 1e3)) / (n / (pms / 1e3))}
 
 
 def cpu_baseline(net):
