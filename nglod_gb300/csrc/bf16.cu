@@ -60,23 +60,23 @@ __device__ __forceinline__ void gather_bf16_quarter(const __nv_bfloat16 *__restr
     const int64_t o[8] = {zi * sz + yi * sy + xi * 4, zi * sz + yi * sy + xj * 4, zi * sz + yj * sy + xi * 4,
                           zi * sz + yj * sy + xj * 4, zj * sz + yi * sy + xi * 4, zj * sz + yi * sy + xj * 4,
                           zj * sz + yj * sy + xi * 4, zj * sz + yj * sy + xj * 4};
-    const float w[8] = {wx0 * wy0 * wz0, wx1 * wy0 * wz0, wx0 * wy1 * wz0, wx1 * wy1 * wz0,
-                        wx0 * wy0 * wz1, wx1 * wy0 * wz1, wx0 * wy1 * wz1, wx1 * wy1 * wz1};
+    const float wxy[4] = {wx0 * wy0, wx1 * wy0, wx0 * wy1, wx1 * wy1};
+    const float w[8] = {wxy[0] * wz0, wxy[1] * wz0, wxy[2] * wz0, wxy[3] * wz0,
+                        wxy[0] * wz1, wxy[1] * wz1, wxy[2] * wz1, wxy[3] * wz1};
     uint4 v[8];
 #pragma unroll
     for (int k = 0; k < 8; ++k) v[k] = __ldg(base + o[k]);
-    float a[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    // Packed fp32 FMAs (two channels per instruction) on the unpacked bf16 pairs.
+    float2 a01 = make_float2(0.f, 0.f), a23 = a01, a45 = a01, a67 = a01;
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
-        a[0] = fmaf(bf_lo(v[k].x), w[k], a[0]);
-        a[1] = fmaf(bf_hi(v[k].x), w[k], a[1]);
-        a[2] = fmaf(bf_lo(v[k].y), w[k], a[2]);
-        a[3] = fmaf(bf_hi(v[k].y), w[k], a[3]);
-        a[4] = fmaf(bf_lo(v[k].z), w[k], a[4]);
-        a[5] = fmaf(bf_hi(v[k].z), w[k], a[5]);
-        a[6] = fmaf(bf_lo(v[k].w), w[k], a[6]);
-        a[7] = fmaf(bf_hi(v[k].w), w[k], a[7]);
+        const float2 w2 = make_float2(w[k], w[k]);
+        a01 = __ffma2_rn(make_float2(bf_lo(v[k].x), bf_hi(v[k].x)), w2, a01);
+        a23 = __ffma2_rn(make_float2(bf_lo(v[k].y), bf_hi(v[k].y)), w2, a23);
+        a45 = __ffma2_rn(make_float2(bf_lo(v[k].z), bf_hi(v[k].z)), w2, a45);
+        a67 = __ffma2_rn(make_float2(bf_lo(v[k].w), bf_hi(v[k].w)), w2, a67);
     }
+    const float a[8] = {a01.x, a01.y, a23.x, a23.y, a45.x, a45.y, a67.x, a67.y};
 #pragma unroll
     for (int c = 0; c < 8; ++c) acc[c] += a[c];
 }
