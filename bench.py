@@ -261,6 +261,9 @@ def run_ours(args):
     if not args.no_extras:
         extras["trace"] = bench_trace(net, bnet, dev, flush, stream)
 
+    if not args.no_extras:
+        extras["serve"] = bench_serve(dev)
+
     cpu = None
     if rank == 0 and ws == 1 and not args.no_extras:
         cpu = cpu_baseline(net)
@@ -323,6 +326,42 @@ def bench_trace(net, bnet, dev, flush, stream):
             "bf16_vs_f32_depth_mean_abs": float(derr.mean().item()) if derr.numel() else None,
             "plain_f32_rays_per_s": n / (pms / 1e3), "plain_f32_ms": pms, "hits": hits, "kernel_launches_fused": 2,
             "bf16_over_plain_f32": (n / (ms16 / 1e3)) / (n / (pms / 1e3))}
+
+
+def bench_serve(dev, duration_s=6.0, rate_hz=200.0, num_models=8):
+    """Serving: 8 resident BF16 models (the 16-sphere unions of seeds 2..9 held
+    through analytic_init), a seeded Poisson stream at 200 req/s of renders
+    (256^2, 512^2, 1280x720, 1920x1080, LOD 0-4) and point queries (1e4-1e6
+    points), admitted under a 16 GiB HBM budget on 8 streams."""
+    import nglod_gb300 as ng
+    from nglod_gb300 import serve, synthetic
+    from nglod_gb300.analytic_init import init_from_sdf
+    from nglod_gb300.bf16 import Bf16OctreeSDF
+    from nglod_gb300.options import default_args
+    models = []
+    for seed in range(2, 2 + num_models):
+        c, r = synthetic.sphere_union(seed)
+        torch.manual_seed(seed)
+        net = ng.OctreeSDF(default_args(num_lods=5, base_lod=2))
+        init_from_sdf(net, lambda p, c=c, r=r: torch.from_numpy(synthetic.sphere_union_sdf(p.numpy(), c, r)),
+                      noise=1e-3, seed=seed)
+        models.append(Bf16OctreeSDF(net.to(dev).eval()))
+    ex = serve.CudaExecutor(models, dev, num_streams=8)
+    gen = torch.Generator(device=dev)
+
+    def pts(spec):
+        gen.manual_seed(spec["seed"])
+        return torch.rand(spec["n"], 3, device=dev, generator=gen) * 2 - 1
+
+    warm = serve.Server(ex, 16 << 30)
+    serve.run_workload(warm, serve.poisson_workload(0.5, rate_hz, num_models, seed=99), pts)
+    torch.cuda.synchronize()
+    srv = serve.Server(ex, 16 << 30)
+    wl = serve.poisson_workload(duration_s, rate_hz, num_models, seed=7)
+    st = serve.run_workload(srv, wl, pts)
+    st["workload"] = (f"{len(wl)} requests, Poisson {rate_hz:.0f}/s for {duration_s:.0f} s, 8 resident BF16 models; "
+                      "renders 256^2/512^2/1280x720/1920x1080 at LOD 0-4, 64 steps; queries 1e4-1e6 points")
+    return st
 
 
 def cpu_baseline(net):

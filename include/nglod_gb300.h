@@ -108,6 +108,13 @@ int nglod_trace(const nglod_dense_model *model, const nglod_trace_params *params
                 float *x, float *t, uint8_t *hit, float *normal,
                 int64_t *work_counter, nglod_stream_t stream);
 
+/* Pinhole camera rays of the reference's look_at (sdf-net/lib/geoutils.py:
+ * 180-206, 'persp' mode) without the random pixel jitter of normalized_grid
+ * (geoutils.py:149-152): origins = eye, unit directions, ray i = ix*height + iy.
+ * eye/at/up are host float[3]. */
+int nglod_camera_rays(const float *eye, const float *at, const float *up, float fov_deg, int32_t width,
+                      int32_t height, float *org, float *dir, nglod_stream_t stream);
+
 /* ------------------------------------------------------------------------
  * BF16 form: bf16 feature volumes and a tcgen05 tensor-core decoder.
  *
@@ -115,8 +122,9 @@ int nglod_trace(const nglod_dense_model *model, const nglod_trace_params *params
  * product with fp32 accumulation in tensor memory.  K order of the tile:
  * k 0..31 = the 32 summed features, 32..34 = x, y, z rounded to bf16,
  * 35..37 = the bf16 remainders x - bf16(x) (so positions keep ~16 bits),
- * 38..47 = 0.  The first-layer bias b0, the ReLU and the second layer
- * (w1, b1) are applied in fp32 after the product.
+ * 38, 39 = 1.0 against the bf16 split b0 = hi + lo of the first-layer bias,
+ * 40..47 = 0.  The ReLU and the second layer (w1, b1) are applied in fp32
+ * after the product.
  * ------------------------------------------------------------------------ */
 typedef struct nglod_bf16_model {
     int32_t num_lods;
@@ -125,17 +133,18 @@ typedef struct nglod_bf16_model {
     int32_t hidden_dim;     /* 128 */
     const void  *grid[NGLOD_MAX_LODS];     /* bf16 channel-last [s][s][s][32], 16-byte aligned */
     const void  *w0_tile[NGLOD_MAX_LODS];  /* NGLOD_BF16_TILE_BYTES from nglod_bf16_pack_decoder */
-    const float *b0[NGLOD_MAX_LODS];       /* [128] */
+    const float *b0[NGLOD_MAX_LODS];       /* [128]; informational (b0 is folded into w0_tile) */
     const float *w1[NGLOD_MAX_LODS];       /* [128] */
     const float *b1[NGLOD_MAX_LODS];       /* [1] */
 } nglod_bf16_model;
 
 #define NGLOD_BF16_TILE_BYTES 12288
 
-/* Host-only: lays out w0 [128][35] (nn.Linear weight of louts[i][0]) as the
- * bf16 B operand of the tensor-core tile (K-major, 8x8 core matrices, no
- * swizzle), NGLOD_BF16_TILE_BYTES bytes.  No CUDA calls. */
-int nglod_bf16_pack_decoder(const float *w0_host, int32_t hidden_dim, int32_t in_dim, void *tile_host);
+/* Host-only: lays out w0 [128][35] and b0 [128] (louts[i][0]) as the bf16 B
+ * operand of the tensor-core tile (K-major, 8x8 core matrices, no swizzle),
+ * NGLOD_BF16_TILE_BYTES bytes.  No CUDA calls. */
+int nglod_bf16_pack_decoder(const float *w0_host, const float *b0_host, int32_t hidden_dim, int32_t in_dim,
+                            void *tile_host);
 
 /* OctreeSDF.sdf(x, lod) in the BF16 form: per-LOD bf16 trilinear gathers
  * summed in fp32, decoder on tcgen05 tensor cores (see above).

@@ -141,10 +141,11 @@ SIGNATURES = {
     "nglod_sparse_query": (ctypes.c_int, [ctypes.POINTER(SparseModel), _vp, _vp, _i32, _vp, _i64, _vp, _vp]),
     "nglod_sparse_trace": (ctypes.c_int, [ctypes.POINTER(SparseModel), _i32, _i32, _vp, _vp, _i64, _vp, _i64, _vp,
                                           _vp, _vp, _vp, _vp, _vp, _vp]),
-    "nglod_bf16_pack_decoder": (ctypes.c_int, [_vp, _i32, _i32, _vp]),
+    "nglod_bf16_pack_decoder": (ctypes.c_int, [_vp, _vp, _i32, _i32, _vp]),
     "nglod_sdf_fwd_bf16": (ctypes.c_int, [ctypes.POINTER(Bf16Model), _vp, _i64, _i32, _vp, _vp, _vp]),
     "nglod_trace_bf16": (ctypes.c_int, [ctypes.POINTER(Bf16Model), ctypes.POINTER(TraceParams), _vp, _vp, _i64,
                                         _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "nglod_camera_rays": (ctypes.c_int, [_vp, _vp, _vp, _f32, _i32, _i32, _vp, _vp, _vp]),
     "nglod_adam_step": (ctypes.c_int, [_vp, _i32, _i64, _f32, _f32, _f32, _f32, _f32, _i64, _vp]),
 }
 

@@ -5,7 +5,8 @@ volumes converted to bf16 (channel-last), each decoder's first layer packed
 once into the bf16 tensor-core tile layout (``nglod_bf16_pack_decoder``),
 b0 / w1 / b1 kept in float32.  ``sdf(x, lod)`` has the semantics of
 OctreeSDF.sdf(x, lod) (sdf-net/lib/models/OctreeSDF.py:94-146) with bf16
-storage and bf16 x bf16 -> fp32 products; its error against the FP64 oracle
+storage and bf16 x bf16 -> fp32 products (b0 enters the product as a bf16
+hi + lo pair); its error against the FP64 oracle
 is measured per LOD by tests/test_bf16_gpu.py and bench.py.
 """
 import ctypes
@@ -16,12 +17,14 @@ import torch
 from . import _lib
 
 
-def pack_decoder_tile(w0):
-    """[128, 35] float32 -> uint8 [12288] tile (host pack through the C ABI)."""
+def pack_decoder_tile(w0, b0):
+    """w0 [128, 35], b0 [128] float32 -> uint8 [12288] tile (host pack through the C ABI)."""
     w = np.ascontiguousarray(w0.detach().cpu().numpy(), dtype=np.float32)
+    b = np.ascontiguousarray(b0.detach().cpu().numpy(), dtype=np.float32)
     out = np.zeros(_lib.BF16_TILE_BYTES, dtype=np.uint8)
-    _lib.check(_lib.load().nglod_bf16_pack_decoder(w.ctypes.data_as(ctypes.c_void_p), w.shape[0], w.shape[1],
-                                                   out.ctypes.data_as(ctypes.c_void_p)), "nglod_bf16_pack_decoder")
+    _lib.check(_lib.load().nglod_bf16_pack_decoder(w.ctypes.data_as(ctypes.c_void_p), b.ctypes.data_as(ctypes.c_void_p),
+                                                   w.shape[0], w.shape[1], out.ctypes.data_as(ctypes.c_void_p)),
+               "nglod_bf16_pack_decoder")
     return torch.from_numpy(out)
 
 
@@ -36,7 +39,7 @@ class Bf16OctreeSDF:
                       for fv in net.features]
         self.tiles, self.b0, self.w1, self.b1 = [], [], [], []
         for dec in net.louts:
-            self.tiles.append(pack_decoder_tile(dec[0].weight).to(dev))
+            self.tiles.append(pack_decoder_tile(dec[0].weight, dec[0].bias).to(dev))
             self.b0.append(dec[0].bias.detach().float().contiguous())
             self.w1.append(dec[2].weight.detach().float().reshape(-1).contiguous())
             self.b1.append(dec[2].bias.detach().float().contiguous())

@@ -32,6 +32,8 @@ constexpr size_t kSmemSlot = kSmemBar + 8;
 constexpr size_t kSmemAbort = kSmemSlot + 4;
 constexpr size_t kSmemBytes = 48 * 1024;
 
+constexpr uint32_t kOneOne = 0x3F803F80u;  // two bf16 1.0: the b0 columns' inputs
+
 __device__ __forceinline__ float bf_lo(uint32_t v) { return __uint_as_float(v << 16); }
 __device__ __forceinline__ float bf_hi(uint32_t v) { return __uint_as_float(v & 0xffff0000u); }
 
@@ -56,10 +58,11 @@ __device__ __forceinline__ void gather_bf16_quarter(const __nv_bfloat16 *__restr
     const int xi = (int)x0, yi = (int)y0, zi = (int)z0;
     const int xj = min(xi + 1, s - 1), yj = min(yi + 1, s - 1), zj = min(zi + 1, s - 1);
     const uint4 *base = reinterpret_cast<const uint4 *>(g) + q;  // 4 uint4 per vertex
-    const int64_t sy = (int64_t)s * 4, sz = (int64_t)s * sy;
-    const int64_t o[8] = {zi * sz + yi * sy + xi * 4, zi * sz + yi * sy + xj * 4, zi * sz + yj * sy + xi * 4,
-                          zi * sz + yj * sy + xj * 4, zj * sz + yi * sy + xi * 4, zj * sz + yi * sy + xj * 4,
-                          zj * sz + yj * sy + xi * 4, zj * sz + yj * sy + xj * 4};
+    // uint4 offsets fit in 32 bits (volumes up to 513^3 x 64 B)
+    const int sy = s * 4, sz = s * sy;
+    const int o0 = zi * sz + yi * sy + xi * 4;
+    const int ox = (xj - xi) * 4, oy = (yj - yi) * sy, oz = (zj - zi) * sz;
+    const int o[8] = {o0, o0 + ox, o0 + oy, o0 + oy + ox, o0 + oz, o0 + oz + ox, o0 + oz + oy, o0 + oz + oy + ox};
     const float wxy[4] = {wx0 * wy0, wx1 * wy0, wx0 * wy1, wx1 * wy1};
     const float w[8] = {wxy[0] * wz0, wxy[1] * wz0, wxy[2] * wz0, wxy[3] * wz0,
                         wxy[0] * wz1, wxy[1] * wz1, wxy[2] * wz1, wxy[3] * wz1};
@@ -105,6 +108,22 @@ __device__ __forceinline__ bool box_entry_bf(float ox, float oy, float oz, float
         return true;
     }
     return false;
+}
+
+// Second decoder layer on this thread's TMEM row (b0 already inside the
+// product): sum_j w1[j] * relu(h[j]), two hidden units per packed FMA.
+__device__ __forceinline__ float relu_dot_w1(uint32_t taddr, const float *__restrict__ sw1) {
+    float2 acc = make_float2(0.f, 0.f);
+#pragma unroll 1
+    for (int c = 0; c < kHid / 32; ++c) {
+        float v[32];
+        tc::tmem_load32(taddr + (uint32_t)(c * 32), v);
+        const float2 *w2 = reinterpret_cast<const float2 *>(sw1 + c * 32);
+#pragma unroll
+        for (int j = 0; j < 16; ++j)
+            acc = __ffma2_rn(w2[j], make_float2(fmaxf(v[2 * j], 0.f), fmaxf(v[2 * j + 1], 0.f)), acc);
+    }
+    return acc.x + acc.y;
 }
 
 struct Bf16Args {
@@ -177,7 +196,7 @@ __global__ void __launch_bounds__(kTP, 4) sdf_fwd_bf16_tc_kernel(const Bf16Args 
                 const float hy = __bfloat162float(__float2bfloat16_rn(py));
                 const float hz = __bfloat162float(__float2bfloat16_rn(pz));
                 const uint4 p = make_uint4(pack_bf16x2(hx, hy), pack_bf16x2(hz, px - hx), pack_bf16x2(py - hy, pz - hz),
-                                           0u);
+                                           kOneOne);
                 *reinterpret_cast<uint4 *>(sA + tc::tile_offset(row, 32, kKC)) = p;
             }
         }
@@ -203,17 +222,7 @@ __global__ void __launch_bounds__(kTP, 4) sdf_fwd_bf16_tc_kernel(const Bf16Args 
         phase ^= 1u;
         tc::fence_after_sync();
         // 3. epilogue: thread (w, lane) owns TMEM lane / tile row 32w + lane
-        float o = 0.f;
-#pragma unroll 1
-        for (int c = 0; c < kHid / 32; ++c) {
-            float v[32];
-            tc::tmem_load32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c * 32), v);
-#pragma unroll
-            for (int j = 0; j < 32; ++j) {
-                const float h = fmaxf(v[j] + sb0[c * 32 + j], 0.f);
-                o = fmaf(sw1[c * 32 + j], h, o);
-            }
-        }
+        float o = relu_dot_w1(tmem + ((uint32_t)(warp * 32) << 16), sw1);
         const int64_t gi = tile * kTP + warp * 32 + lane;
         if (gi < a.n) a.out[gi] = o + b1;
         tc::fence_before_sync();
@@ -407,7 +416,7 @@ __global__ void __launch_bounds__(kTP, 4) trace_bf16_tc_kernel(const Bf16TraceAr
                 const float hy = __bfloat162float(__float2bfloat16_rn(pt.y));
                 const float hz = __bfloat162float(__float2bfloat16_rn(pt.z));
                 const uint4 pp4 = make_uint4(pack_bf16x2(hx, hy), pack_bf16x2(hz, pt.x - hx),
-                                             pack_bf16x2(pt.y - hy, pt.z - hz), 0u);
+                                             pack_bf16x2(pt.y - hy, pt.z - hz), kOneOne);
                 *reinterpret_cast<uint4 *>(sA + tc::tile_offset(row, 32, kKC)) = pp4;
             }
         }
@@ -431,15 +440,7 @@ __global__ void __launch_bounds__(kTP, 4) trace_bf16_tc_kernel(const Bf16TraceAr
         if (*abort_flag) break;
         mphase ^= 1u;
         tc::fence_after_sync();
-        float v = 0.f;
-#pragma unroll 1
-        for (int c = 0; c < kHid / 32; ++c) {
-            float hv[32];
-            tc::tmem_load32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c * 32), hv);
-#pragma unroll
-            for (int j = 0; j < 32; ++j) v = fmaf(sw1[c * 32 + j], fmaxf(hv[j] + sb0[c * 32 + j], 0.f), v);
-        }
-        v += b1;
+        float v = relu_dot_w1(tmem + ((uint32_t)(warp * 32) << 16), sw1) + b1;
         tc::fence_before_sync();
 
         if (phase == bEvalInit) {
@@ -482,8 +483,9 @@ __global__ void __launch_bounds__(kTP, 4) trace_bf16_tc_kernel(const Bf16TraceAr
 
 using namespace nglod;
 
-extern "C" int nglod_bf16_pack_decoder(const float *w0_host, int32_t hidden_dim, int32_t in_dim, void *tile_host) {
-    NGLOD_REQUIRE(w0_host && tile_host, NGLOD_ERR_INVALID, "null pointer argument");
+extern "C" int nglod_bf16_pack_decoder(const float *w0_host, const float *b0_host, int32_t hidden_dim, int32_t in_dim,
+                                       void *tile_host) {
+    NGLOD_REQUIRE(w0_host && b0_host && tile_host, NGLOD_ERR_INVALID, "null pointer argument");
     NGLOD_REQUIRE(hidden_dim == kHid && in_dim == 35, NGLOD_ERR_UNSUPPORTED,
                   "bf16 decoder tile built for w0 [128][35], got [%d][%d]", hidden_dim, in_dim);
     uint16_t *t = static_cast<uint16_t *>(tile_host);
@@ -494,6 +496,8 @@ extern "C" int nglod_bf16_pack_decoder(const float *w0_host, int32_t hidden_dim,
             if (k < 32) w = w0_host[n * 35 + 3 + k];
             else if (k < 35) w = w0_host[n * 35 + (k - 32)];
             else if (k < 38) w = w0_host[n * 35 + (k - 35)];
+            else if (k == 38) w = __bfloat162float(__float2bfloat16_rn(b0_host[n]));
+            else if (k == 39) w = b0_host[n] - __bfloat162float(__float2bfloat16_rn(b0_host[n]));
             const __nv_bfloat16 b = __float2bfloat16_rn(w);
             uint16_t bits;
             memcpy(&bits, &b, 2);

@@ -97,6 +97,36 @@ __global__ void __launch_bounds__(256) aabb_kernel(const float *__restrict__ ro,
 }
 
 // ---------------------------------------------------------------------------
+// pinhole camera rays (look_at of sdf-net/lib/geoutils.py:180-206, no jitter)
+// ---------------------------------------------------------------------------
+struct CameraArgs {
+    float eye[3], right[3], up[3], view[3];
+    float tan_half;
+    int width, height;
+};
+
+// Ray i = ix * height + iy (x-major, as torch.meshgrid(window_x, window_y)):
+// pixel = right * wx * tan + up * wy * tan + eye + view with
+// wx = (-1 + 2 ix / (W-1)) * W/H and wy = 1 - 2 iy / (H-1); origin = eye,
+// direction = normalize(pixel - eye).
+__global__ void camera_rays_kernel(const CameraArgs c, float *__restrict__ org, float *__restrict__ dir) {
+    const int64_t n = (int64_t)c.width * c.height;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const int ix = (int)(i / c.height), iy = (int)(i % c.height);
+        const float wx = (c.width > 1 ? -1.f + 2.f * ix / (float)(c.width - 1) : 0.f) * ((float)c.width / c.height);
+        const float wy = c.height > 1 ? 1.f - 2.f * iy / (float)(c.height - 1) : 0.f;
+        float d[3];
+        for (int k = 0; k < 3; ++k) d[k] = c.right[k] * wx * c.tan_half + c.up[k] * wy * c.tan_half + c.view[k];
+        const float inv = rsqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+        for (int k = 0; k < 3; ++k) {
+            org[3 * i + k] = c.eye[k];
+            dir[3 * i + k] = d[k] * inv;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // persistent sphere tracer
 // ---------------------------------------------------------------------------
 struct TraceArgs {
@@ -355,4 +385,44 @@ extern "C" int nglod_trace(const nglod_dense_model *model, const nglod_trace_par
                           "nglod_trace counter reset"));
     trace_f32_kernel<<<(int)(want < cap ? want : cap), threads, smem, (cudaStream_t)stream>>>(a);
     return launch_status("nglod_trace");
+}
+
+extern "C" int nglod_camera_rays(const float *eye, const float *at, const float *up, float fov_deg, int32_t width,
+                                 int32_t height, float *org, float *dir, nglod_stream_t stream) {
+    NGLOD_REQUIRE(eye && at && up && org && dir, NGLOD_ERR_INVALID, "null pointer argument");
+    NGLOD_REQUIRE(width > 0 && height > 0, NGLOD_ERR_INVALID, "image %dx%d is empty", width, height);
+    CameraArgs c;
+    double v[3], r[3], u[3], nv = 0, nr = 0, nu = 0;
+    for (int k = 0; k < 3; ++k) {
+        v[k] = (double)at[k] - eye[k];
+        nv += v[k] * v[k];
+    }
+    nv = sqrt(nv);
+    NGLOD_REQUIRE(nv > 0, NGLOD_ERR_INVALID, "eye and target coincide");
+    for (int k = 0; k < 3; ++k) v[k] /= nv;
+    r[0] = v[1] * up[2] - v[2] * up[1];
+    r[1] = v[2] * up[0] - v[0] * up[2];
+    r[2] = v[0] * up[1] - v[1] * up[0];
+    for (int k = 0; k < 3; ++k) nr += r[k] * r[k];
+    nr = sqrt(nr);
+    NGLOD_REQUIRE(nr > 0, NGLOD_ERR_INVALID, "up is parallel to the view direction");
+    for (int k = 0; k < 3; ++k) r[k] /= nr;
+    u[0] = r[1] * v[2] - r[2] * v[1];
+    u[1] = r[2] * v[0] - r[0] * v[2];
+    u[2] = r[0] * v[1] - r[1] * v[0];
+    for (int k = 0; k < 3; ++k) nu += u[k] * u[k];
+    nu = sqrt(nu);
+    for (int k = 0; k < 3; ++k) {
+        c.eye[k] = eye[k];
+        c.view[k] = (float)v[k];
+        c.right[k] = (float)r[k];
+        c.up[k] = (float)(u[k] / nu);
+    }
+    c.tan_half = (float)tan(fov_deg * 3.14159265358979323846 / 360.0);
+    c.width = width;
+    c.height = height;
+    const int64_t n = (int64_t)width * height;
+    const int64_t want = (n + 255) / 256, cap = (int64_t)num_sms() * 16;
+    camera_rays_kernel<<<(int)(want < cap ? want : cap), 256, 0, (cudaStream_t)stream>>>(c, org, dir);
+    return launch_status("nglod_camera_rays");
 }

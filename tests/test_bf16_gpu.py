@@ -26,8 +26,8 @@ def _bf16(a):
 
 def emulate(m, x, lod):
     """The BF16 form's arithmetic in numpy: bf16 volumes, fp32 LOD sum rounded
-    to bf16, positions as bf16 hi + lo, bf16 first-layer weights, products
-    accumulated in float64, b0 / ReLU / second layer in float32."""
+    to bf16, positions and b0 as bf16 hi + lo, bf16 first-layer weights,
+    products accumulated in float64, ReLU / second layer in float32."""
     x = x.astype(np.float32)
     acc = np.zeros((x.shape[0], 32), np.float32)
     for i in range(lod + 1):
@@ -36,8 +36,11 @@ def emulate(m, x, lod):
     hi = _bf16(x)
     lo = _bf16(x - hi)
     w0 = _bf16(m["w0"][lod].astype(np.float32)).astype(np.float64)
+    b0 = m["b0"][lod].astype(np.float32)
+    b0h = _bf16(b0)
+    b0l = _bf16(b0 - b0h)
     h = f.astype(np.float64) @ w0[:, 3:].T + hi.astype(np.float64) @ w0[:, :3].T + lo.astype(np.float64) @ w0[:, :3].T
-    h = np.maximum(h.astype(np.float32) + m["b0"][lod].astype(np.float32), 0)
+    h = np.maximum((h + b0h + b0l).astype(np.float32), 0)
     return (h @ m["w1"][lod].astype(np.float32).T + m["b1"][lod].astype(np.float32))
 
 
