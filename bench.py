@@ -264,6 +264,7 @@ def run_ours(args):
     if not args.no_extras:
         extras["serve"] = bench_serve(dev)
         extras["train"] = bench_train(dev, flush, stream)
+        extras["sparse"] = bench_sparse(net, dev, flush, stream)
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_extras:
@@ -432,6 +433,57 @@ def bench_train(dev, flush, stream, batch=524_288, steps=20, warm=3, train_steps
     with torch.no_grad():
         out["trained_f32_l1_vs_analytic_lod4"] = float((net.sdf(q[:262144], lod=4) - gt).abs().mean().item())
     return out
+
+
+def bench_sparse(net, dev, flush, stream, level=7, lod=4, steps=64):
+    """Sparse path (sol-renderer): SPC octree of level 7 built on the GPU from
+    the voxels whose centres lie within one voxel diagonal of the 16-sphere
+    surface (seed 1); per frame: ray/octree traversal to level lod+2 = 6,
+    first-nugget flags, sparse sphere trace (64 steps) with BF16 corner
+    features, 1920x1080.  Depth/normal maps against the dense float32
+    tracer on the same network."""
+    import nglod_gb300 as ng
+    from nglod_gb300 import spc, synthetic
+    from nglod_gb300.options import default_args
+    from nglod_gb300.sparse_sdf import SparseSDF
+    c, r = synthetic.sphere_union(1)
+    res = 2 ** level
+    idx = torch.stack(torch.meshgrid(torch.arange(res), torch.arange(res), torch.arange(res), indexing="ij"), -1)
+    idx = idx.reshape(-1, 3).to(dev)
+    centres = (idx.double() + 0.5) / res * 2 - 1
+    keep = synthetic.sphere_union_sdf(centres, c, r).abs() <= (3 ** 0.5) * (2.0 / res)
+    vox = idx[keep].int()
+    t0 = time.perf_counter()
+    s = spc.SPC.from_voxels(vox, level)
+    sp = SparseSDF.from_dense(net, s, precision="bf16")
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t0
+    ro, rd = synthetic.look_at_rays(width=TRACE_W, height=TRACE_H)
+    ro, rd = ro.to(dev), rd.to(dev)
+
+    def frame():
+        return sp.render(ro, rd, lod=lod, num_steps=steps)
+
+    for _ in range(3):
+        (x, t, hit, normal), nug = frame()
+    torch.cuda.synchronize()
+    reps = 10
+    ms = time_steps(frame, reps, flush, stream) / reps
+    ms_trav = time_steps(lambda: spc.spc_raytrace(s.GetOctree(), s.GetPoints(), s.GetPyramid(), ro, rd, lod + 2,
+                                                   prefix=s.GetPrefix()), reps, flush, stream) / reps
+    net.lod = lod
+    rb = ng.SphereTracer(default_args(num_steps=128))(net, ro, rd)
+    net.lod = None
+    both = hit & rb.hit
+    cosang = (normal[both] * rb.normal[both]).sum(-1)
+    return {"workload": f"octree level {level} ({int(s.GetPyramid()[0, level])} leaf voxels, {s.GetOSize()} bytes), "
+                        f"frame {TRACE_W}x{TRACE_H}: traversal to level {lod + 2}, sparse trace lod {lod}, "
+                        f"{steps} steps, bf16 corner features",
+            "frame_ms": ms, "rays_per_s": TRACE_W * TRACE_H / (ms / 1e3), "traversal_ms": ms_trav,
+            "nuggets": int(nug.shape[0]), "setup_s": setup_s,
+            "vs_dense_f32": {"hit_agreement": float((hit == rb.hit).float().mean().item()),
+                             "depth_median_abs": float((t[both] - rb.depth[both]).abs().median().item()),
+                             "normal_cos_median": float(cosang.median().item())}}
 
 
 def bench_serve(dev, duration_s=6.0, rate_hz=200.0, num_models=8):
