@@ -62,6 +62,8 @@ def parse():
     p.add_argument("--warmup", type=int, default=10)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--no-extras", action="store_true", help="skip the trace and CPU-baseline legs")
+    p.add_argument("--only", choices=["trace", "train", "sparse", "serve"], default=None,
+                   help="run one extra leg alone (profiling); prints its JSON")
     return p.parse_args()
 
 
@@ -402,6 +404,8 @@ def bench_train(dev, flush, stream, batch=524_288, steps=20, warm=3, train_steps
            "torch_ops_ms_per_step": ms_ref, "torch_ops_points_per_s": batch / (ms_ref / 1e3),
            "speedup_vs_torch_ops": ms_ref / ms_ours,
            "gradient_check": "tests/test_train_gpu.py: 1e-4 relative vs reference autograd, 1e-3 vs FP64 differences"}
+    if train_steps == 0:
+        return out
     # 2,000 steps of configuration 2 from seed 1 (fresh batches every step)
     torch.manual_seed(1)
     net = ng.OctreeSDF(default_args(num_lods=5, base_lod=2)).to(dev).train()
@@ -578,8 +582,31 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_only(args):
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    import nglod_gb300 as ng
+    from nglod_gb300.bf16 import Bf16OctreeSDF
+    ng.load_library()
+    net, _ = build_model(dev)
+    flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    if args.only == "trace":
+        out = bench_trace(net, Bf16OctreeSDF(net), dev, flush, stream)
+    elif args.only == "train":
+        out = bench_train(dev, flush, stream, steps=max(args.steps, 1), warm=max(args.warmup, 1), train_steps=0)
+    elif args.only == "sparse":
+        out = bench_sparse(net, dev, flush, stream)
+    else:
+        out = bench_serve(dev, duration_s=2.0)
+    print(json.dumps({"only": args.only, **out}), flush=True)
+
+
 def main():
     args = parse()
+    if args.only:
+        run_only(args)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:
