@@ -27,27 +27,19 @@ constexpr int kCtrlCount = 4;    // count of level l at kCtrlCount + l
 // (4*[x > centre] + 2*[y > centre] + [z > centre]) come nearest first: sorted
 // by the Hamming distance of their octant index to `code`, ties by index.
 // This reproduces the Order table of spc_raytrace_cuda_kernel.cu:39-47.
-__host__ __device__ inline uint32_t child_order(uint32_t code, uint32_t rank) {
-    uint32_t seen = 0;
+// The order of a code packed 3 bits per rank (rank 0 in the low bits).
+constexpr uint32_t popc3(uint32_t v) { return (v & 1u) + ((v >> 1) & 1u) + ((v >> 2) & 1u); }
+constexpr uint32_t order_word(uint32_t code) {
+    uint32_t w = 0, r = 0;
     for (uint32_t dist = 0; dist <= 3; ++dist)
         for (uint32_t j = 0; j < 8; ++j)
-            if ((uint32_t)__builtin_popcount(j ^ code) == dist) {
-                if (seen == rank) return j;
-                ++seen;
-            }
-    return 0;
+            if (popc3(j ^ code) == dist) w |= j << (3 * r++);
+    return w;
 }
-
-struct OrderTable {
-    unsigned char o[8][8];
-};
-
-static OrderTable make_order_table() {
-    OrderTable t;
-    for (uint32_t c = 0; c < 8; ++c)
-        for (uint32_t r = 0; r < 8; ++r) t.o[c][r] = (unsigned char)child_order(c, r);
-    return t;
-}
+static_assert(order_word(0) == (0u | 1u << 3 | 2u << 6 | 4u << 9 | 3u << 12 | 5u << 15 | 6u << 18 | 7u << 21),
+              "child order of octant 0");
+__constant__ uint32_t c_child_order[8] = {order_word(0), order_word(1), order_word(2), order_word(3),
+                                          order_word(4), order_word(5), order_word(6), order_word(7)};
 
 // ---------------------------------------------------------------------------
 // ray / voxel test (d_Decide, d_FaceEval of spc_raytrace_cuda_kernel.cu:85-138)
@@ -75,8 +67,13 @@ __device__ __forceinline__ bool face_straddles(float fi, float fj, float a, floa
     return mn <= 0.f && mx >= 0.f;
 }
 
-__device__ __forceinline__ bool ray_hits_voxel(const float *__restrict__ org, const float *__restrict__ dir,
-                                               uint32_t ridx, short4 p, int level) {
+// The three edge functions (a, b, c per plane) of one ray at one level.
+struct RayFaces {
+    float a0, b0, c0, a1, b1, c1, a2, b2, c2;
+};
+
+__device__ __forceinline__ RayFaces ray_faces(const float *__restrict__ org, const float *__restrict__ dir,
+                                              uint32_t ridx, int level) {
     const float ox = __fmaf_rn(0.5f, org[3 * ridx], 0.5f);
     const float oy = __fmaf_rn(0.5f, org[3 * ridx + 1], 0.5f);
     const float oz = __fmaf_rn(0.5f, org[3 * ridx + 2], 0.5f);
@@ -88,31 +85,61 @@ __device__ __forceinline__ bool ray_hits_voxel(const float *__restrict__ org, co
     const float cz = __fmaf_rn(ox, dy, -__fmul_rn(dx, oy));
     const float s1 = ldexpf(1.f, -level);
     const float s2 = __fmul_rn(s1, s1);
-    const float px = (float)(unsigned short)p.x, py = (float)(unsigned short)p.y, pz = (float)(unsigned short)p.z;
-    return face_straddles(py, pz, __fmul_rn(-s2, dz), __fmul_rn(s2, dy), __fmul_rn(s1, cx)) &&
-           face_straddles(px, pz, __fmul_rn(s2, dz), __fmul_rn(-s2, dx), __fmul_rn(s1, cy)) &&
-           face_straddles(px, py, __fmul_rn(-s2, dy), __fmul_rn(s2, dx), __fmul_rn(s1, cz));
+    RayFaces f;
+    f.a0 = __fmul_rn(-s2, dz);
+    f.b0 = __fmul_rn(s2, dy);
+    f.c0 = __fmul_rn(s1, cx);
+    f.a1 = __fmul_rn(s2, dz);
+    f.b1 = __fmul_rn(-s2, dx);
+    f.c1 = __fmul_rn(s1, cy);
+    f.a2 = __fmul_rn(-s2, dy);
+    f.b2 = __fmul_rn(s2, dx);
+    f.c2 = __fmul_rn(s1, cz);
+    return f;
+}
+
+// Voxel (px, py, pz) (integer coordinates at the faces' level, exact in float).
+__device__ __forceinline__ bool faces_hit(const RayFaces &f, float px, float py, float pz) {
+    return face_straddles(py, pz, f.a0, f.b0, f.c0) && face_straddles(px, pz, f.a1, f.b1, f.c1) &&
+           face_straddles(px, py, f.a2, f.b2, f.c2);
+}
+
+__device__ __forceinline__ bool ray_hits_voxel(const float *__restrict__ org, const float *__restrict__ dir,
+                                               uint32_t ridx, short4 p, int level) {
+    return faces_hit(ray_faces(org, dir, ridx, level), (float)(unsigned short)p.x, (float)(unsigned short)p.y,
+                     (float)(unsigned short)p.z);
 }
 
 // Octant of the ray origin relative to the voxel centre (d_Subdivide,
-// spc_raytrace_cuda_kernel.cu:157-167): the reference forms
-// (0.5*o + 0.5) - scale*(p + 0.5) in double, so only the comparison matters.
+// spc_raytrace_cuda_kernel.cu:157-167).  The reference forms
+// a - v = (0.5*o + 0.5) - scale*(p + 0.5) in double and tests the float of it
+// for > 0.  a is a float and v = 2^-level * (p + 0.5) is exact in float
+// (p < 2^15), both are multiples of 2^-149, so a - v is zero or at least
+// 2^-149 in magnitude: its float keeps its sign, and the test is a > v,
+// evaluated here in float (NaN origins compare false either way).
 __device__ __forceinline__ uint32_t origin_octant(const float *__restrict__ org, uint32_t ridx, short4 p,
                                                   int level) {
-    const double sc = ldexp(1.0, -level);
-    const double ax = (double)__fmaf_rn(0.5f, org[3 * ridx], 0.5f);
-    const double ay = (double)__fmaf_rn(0.5f, org[3 * ridx + 1], 0.5f);
-    const double az = (double)__fmaf_rn(0.5f, org[3 * ridx + 2], 0.5f);
-    uint32_t code = 0;
-    if ((float)(ax - sc * ((double)p.x + 0.5)) > 0.f) code = 4;
-    if ((float)(ay - sc * ((double)p.y + 0.5)) > 0.f) code += 2;
-    if ((float)(az - sc * ((double)p.z + 0.5)) > 0.f) code += 1;
-    return code;
+    const float ax = __fmaf_rn(0.5f, org[3 * ridx], 0.5f);
+    const float ay = __fmaf_rn(0.5f, org[3 * ridx + 1], 0.5f);
+    const float az = __fmaf_rn(0.5f, org[3 * ridx + 2], 0.5f);
+    const float vx = ldexpf((float)p.x + 0.5f, -level);
+    const float vy = ldexpf((float)p.y + 0.5f, -level);
+    const float vz = ldexpf((float)p.z + 0.5f, -level);
+    return (ax > vx ? 4u : 0u) + (ay > vy ? 2u : 0u) + (az > vz ? 1u : 0u);
 }
 
 // ---------------------------------------------------------------------------
 // traversal kernels
 // ---------------------------------------------------------------------------
+// Level l's pass turns the nuggets of level l (voxels the ray is known to
+// hit; at level 0 every ray with the root, tested here) into the nuggets of
+// level l+1: the children of each voxel that are occupied and hit by the
+// ray, nearest first.  "decide" tests the children and stores per nugget
+// the hit mask (bits 0-7, by child index) and the origin octant (bits 8-10);
+// "emit" writes the children of the mask in the octant's order.  Both
+// produce the reference's nuggets exactly: the reference emits every
+// occupied child and drops the missed ones at the next level, which leaves
+// the same children in the same order.
 struct TraverseArgs {
     const uint8_t *octree;
     const short4 *points;  // all levels
@@ -126,10 +153,9 @@ struct TraverseArgs {
     int64_t *ctrl;
     int64_t capacity;
     int level;       // current level
-    int target;      // target level
+    int target;      // target level (== level only for the root-only pass of target 0)
     int64_t off0;    // global point index of this level's first point
     int64_t off1;    // ... of the next level's
-    OrderTable order;
 };
 
 __device__ __forceinline__ int2 nugget_at(const TraverseArgs &a, int64_t i) {
@@ -147,10 +173,27 @@ __global__ void __launch_bounds__(kChunk) traverse_decide_kernel(const TraverseA
         uint32_t v = 0;
         if (i < count) {
             const int2 nug = nugget_at(a, i);
-            const short4 p = a.points[a.off0 + nug.y];
-            if (ray_hits_voxel(a.org, a.dir, (uint32_t)nug.x, p, a.level))
-                v = a.level < a.target ? (uint32_t)__popc(a.octree[a.off0 + nug.y]) : 1u;
-            a.info[i] = v;
+            const int64_t node = a.off0 + nug.y;
+            const short4 p = a.points[node];
+            uint32_t inf = 0;
+            if (a.level > 0 || ray_hits_voxel(a.org, a.dir, (uint32_t)nug.x, p, 0)) {
+                if (a.level == a.target) {
+                    inf = 1u;
+                } else {
+                    const uint32_t o = a.octree[node];
+                    const RayFaces f = ray_faces(a.org, a.dir, (uint32_t)nug.x, a.level + 1);
+                    const float bx = (float)(2 * (int)p.x), by = (float)(2 * (int)p.y), bz = (float)(2 * (int)p.z);
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) {
+                        if (!(o & (1u << j))) continue;
+                        if (faces_hit(f, bx + (float)((j >> 2) & 1), by + (float)((j >> 1) & 1), bz + (float)(j & 1)))
+                            inf |= 1u << j;
+                    }
+                    inf |= origin_octant(a.org, (uint32_t)nug.x, p, a.level) << 8;
+                }
+            }
+            a.info[i] = inf;
+            v = (uint32_t)__popc(inf & 0xffu);
         }
         const uint32_t s = block_sum(v, s_warp);
         if (threadIdx.x == 0) a.partials[c] = s;
@@ -159,12 +202,16 @@ __global__ void __launch_bounds__(kChunk) traverse_decide_kernel(const TraverseA
 
 __global__ void __launch_bounds__(kChunk) traverse_emit_kernel(const TraverseArgs a) {
     __shared__ uint32_t s_warp[33];
+    __shared__ uint32_t s_order[8];
+    if (threadIdx.x < 8) s_order[threadIdx.x] = c_child_order[threadIdx.x];
+    __syncthreads();
     if (a.ctrl[kCtrlStatus] != 0) return;
     const int64_t count = a.ctrl[kCtrlCount + a.level];
     const int64_t nchunks = (count + kChunk - 1) / kChunk;
     for (int64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
         const int64_t i = c * kChunk + threadIdx.x;
-        const uint32_t v = i < count ? a.info[i] : 0u;
+        const uint32_t inf = i < count ? a.info[i] : 0u;
+        const uint32_t v = (uint32_t)__popc(inf & 0xffu);
         uint32_t tot;
         const uint32_t ex = block_exclusive_scan(v, s_warp, &tot);
         if (v == 0) continue;
@@ -174,16 +221,14 @@ __global__ void __launch_bounds__(kChunk) traverse_emit_kernel(const TraverseArg
             a.out[pos] = nug;
             continue;
         }
-        const short4 p = a.points[a.off0 + nug.y];
-        const uint32_t o = a.octree[a.off0 + nug.y];
-        const uint32_t s = a.prefix[a.off0 + nug.y];
-        const uint32_t code = origin_octant(a.org, (uint32_t)nug.x, p, a.level);
-        for (int r = 0; r < 8; ++r) {
-            const uint32_t j = a.order.o[code][r];
-            if (o & (1u << j)) {
-                const uint32_t cnt = __popc(o & ((2u << j) - 1u));
-                a.out[pos++] = make_int2(nug.x, (int)((int64_t)s + cnt - a.off1));
-            }
+        const int64_t node = a.off0 + nug.y;
+        const uint32_t o = a.octree[node];
+        const int64_t first = (int64_t)a.prefix[node] - a.off1;
+        uint32_t ord = s_order[inf >> 8];
+#pragma unroll
+        for (int r = 0; r < 8; ++r, ord >>= 3) {
+            const uint32_t j = ord & 7u;
+            if (inf & (1u << j)) a.out[pos++] = make_int2(nug.x, (int)(first + __popc(o & ((2u << j) - 1u))));
         }
     }
 }
@@ -516,7 +561,10 @@ extern "C" int nglod_spc_raytrace(const uint8_t *octree, const int16_t *points, 
     NGLOD_REQUIRE(pyramid_host && count && result_buffer, NGLOD_ERR_INVALID, "null pointer argument");
     NGLOD_REQUIRE(pyramid_host[level + 1] == 0 && pyramid_host[level + 2] == 0, NGLOD_ERR_INVALID,
                   "bad pyramid table (the reference's 'bad spc table3' check)");
-    *result_buffer = (target_level + 1) % 2;
+    // Pass l writes level l+1's nuggets to buffer (l+1) % 2; target 0 runs one
+    // root-only pass (level 0, writing buffer 1).
+    const int passes = target_level == 0 ? 1 : target_level;
+    *result_buffer = passes % 2;
     *count = 0;
     if (n_rays == 0) return NGLOD_OK;
     NGLOD_REQUIRE(octree && points && prefix && org && dir && nuggets_a && nuggets_b && info && partials && ctrl,
@@ -537,11 +585,10 @@ extern "C" int nglod_spc_raytrace(const uint8_t *octree, const int16_t *points, 
     a.ctrl = ctrl;
     a.capacity = capacity;
     a.target = target_level;
-    a.order = make_order_table();
     const int32_t *psum = pyramid_host + (level + 2);
     int2 *buf[2] = {reinterpret_cast<int2 *>(nuggets_a), reinterpret_cast<int2 *>(nuggets_b)};
     const int grid = grid_for((capacity + kChunk - 1) / kChunk);
-    for (int l = 0; l <= target_level; ++l) {
+    for (int l = 0; l < passes; ++l) {
         a.level = l;
         a.off0 = psum[l];
         a.off1 = psum[l + 1];
@@ -560,7 +607,7 @@ extern "C" int nglod_spc_raytrace(const uint8_t *octree, const int16_t *points, 
     NGLOD_TRY(cuda_status(cudaStreamSynchronize(s), "raytrace sync"));
     NGLOD_REQUIRE(res[kCtrlStatus] == 0, NGLOD_ERR_CAPACITY,
                   "spc_raytrace: more than capacity=%lld nuggets at some level", (long long)capacity);
-    *count = res[kCtrlCount + target_level + 1];
+    *count = res[kCtrlCount + passes];
     return NGLOD_OK;
 }
 

@@ -173,7 +173,10 @@ def spc_raytrace(octree, points, pyramid, Org, Dir, targetLevel, prefix=None, ca
     if prefix is None:
         prefix = octree_prefix(octree)
     if capacity is None:
-        capacity = max(n, 1 << 22)
+        # four nuggets per ray covers typical frames in one pass (a frame of
+        # 1920x1080 rays against a level-7 sphere-union octree needs ~2.5 per
+        # ray at level 6); a larger count costs one retry with 4x the buffers.
+        capacity = max(4 * n, 1 << 22)
     capacity = max(capacity, n)
     lib = _lib.load()
     while True:
