@@ -9,19 +9,26 @@ points, half uniform in [-1,1]^3 and half within 0.02 of the 16-sphere-union
 surface (seed 1), in the BF16 form (bf16 volumes, tcgen05 decoder with fp32
 accumulation) -- the mixed-precision inference configuration.  One step =
 one pass over the batch.  ``value`` is queries/s with the points already
-resident in HBM; ``e2e`` is the same metric through the public API with the
-points copied from pinned host memory and the distances copied back inside
-the timed region.  ``fp32`` repeats the measurement for the float32 drop-in
-(``OctreeSDF.sdf``), which matches the reference to 1e-5.
+resident in HBM; ``e2e`` is the same metric through the public API with
+host buffers (``Bf16OctreeSDF.sdf_host`` -> ``nglod_sdf_fwd_bf16_host``): the
+points are copied from pinned host memory and the distances copied back inside
+the timed region, in 1M-point chunks whose copies overlap the kernels.
+``fp32`` repeats the measurement for the float32 drop-in (``OctreeSDF.sdf``),
+which matches the reference to 1e-5.
 
 The model holds the sphere-union SDF through ``analytic_init`` (deterministic
 and traced with real hits; throughput does not depend on the weights).
 Between timed steps an L2 flush (a 256 MiB write, larger than the 129 MB L2)
 runs outside the timed events.
 
-Extra keys: ``trace`` (fused float32 sphere tracer, 1920x1080, 64 steps, rays/s
-and the plain per-step tracer beside it), ``roofline``, ``cpu_baseline``,
-``clocks``, ``gpu_launches``.
+Extra keys: ``trace`` (sphere tracers at 1920x1080, 64 steps: fused BF16,
+fused float32 and the plain per-step float32 tracer), ``serve`` (the
+continuous-batching server under a Poisson request stream), ``train`` (the
+training step against the reference computation in stock PyTorch ops, then
+2,000 steps and the BF16 form on the trained weights), ``sparse`` (SPC octree
+traversal + sparse BF16 trace of a 1080p frame), ``roofline``,
+``cpu_baseline``, ``clocks``, ``gpu_launches``.  ``--only LEG`` runs one
+extra leg alone (for profiling).
 
 ``--impl reference`` times the reference's own CPU torch computation (the
 restatement in oracle/torch_port.py, same torch operators) on the host cores
@@ -215,11 +222,11 @@ def run_ours(args):
     steps32 = max(10, args.steps // 5)
     ms32 = max_over_ranks(time_steps(step32, steps32, flush, stream), ws, dev) / steps32
 
-    # e2e through the public API: pinned H2D, sdf, D2H, every step.
+    # e2e through the public API with host buffers: Bf16OctreeSDF.sdf_host ->
+    # nglod_sdf_fwd_bf16_host copies the pinned points in and the distances
+    # out every step, in 1M-point chunks whose copies overlap the kernels.
     def e2e_step():
-        xd = x_host.to(dev, non_blocking=True)
-        d = bnet.sdf(xd, lod=LOD)
-        out_host.copy_(d, non_blocking=True)
+        bnet.sdf_host(x_host, lod=LOD, out=out_host)
 
     e2e_steps = min(args.steps, 100)
     for _ in range(3):
@@ -409,18 +416,10 @@ def bench_train(dev, flush, stream, batch=524_288, steps=20, warm=3, train_steps
     # 2,000 steps of configuration 2 from seed 1 (fresh batches every step)
     torch.manual_seed(1)
     net = ng.OctreeSDF(default_args(num_lods=5, base_lod=2)).to(dev).train()
-    opt = trainer.FusedAdam(net.parameters(), lr=1e-3)
     t0 = time.perf_counter()
-    gen = torch.Generator().manual_seed(5)
     pool = [synthetic.training_batch(batch, c, r, seed=100 + k) for k in range(8)]
     pool = [(a.to(dev), b.to(dev)) for a, b in pool]
-    losses = []
-    for it in range(train_steps):
-        xb, gb = pool[it % len(pool)]
-        perm = torch.randperm(batch, device=dev)
-        l = trainer.step_geometry(net, opt, xb[perm], gb[perm])
-        if it % 500 == 0 or it == train_steps - 1:
-            losses.append(float(l.item()))
+    _, losses = trainer.fit(net, pool, train_steps, lr=1e-3, seed=5)
     torch.cuda.synchronize()
     out["train_2000_steps_s"] = time.perf_counter() - t0
     out["train_loss_trace"] = losses
@@ -494,7 +493,8 @@ def bench_serve(dev, duration_s=6.0, rate_hz=200.0, num_models=8):
     """Serving: 8 resident BF16 models (the 16-sphere unions of seeds 2..9 held
     through analytic_init), a seeded Poisson stream at 200 req/s of renders
     (256^2, 512^2, 1280x720, 1920x1080, LOD 0-4) and point queries (1e4-1e6
-    points), admitted under a 16 GiB HBM budget on 8 streams."""
+    points), admitted by the native scheduler (nglod_serve_*) under a 16 GiB
+    HBM budget on 8 slots."""
     import nglod_gb300 as ng
     from nglod_gb300 import serve, synthetic
     from nglod_gb300.analytic_init import init_from_sdf
@@ -517,10 +517,12 @@ def bench_serve(dev, duration_s=6.0, rate_hz=200.0, num_models=8):
 
     warm = serve.Server(ex, 16 << 30)
     serve.run_workload(warm, serve.poisson_workload(0.5, rate_hz, num_models, seed=99), pts)
+    warm.close()
     torch.cuda.synchronize()
     srv = serve.Server(ex, 16 << 30)
     wl = serve.poisson_workload(duration_s, rate_hz, num_models, seed=7)
     st = serve.run_workload(srv, wl, pts)
+    srv.close()
     st["workload"] = (f"{len(wl)} requests, Poisson {rate_hz:.0f}/s for {duration_s:.0f} s, 8 resident BF16 models; "
                       "renders 256^2/512^2/1280x720/1920x1080 at LOD 0-4, 64 steps; queries 1e4-1e6 points")
     return st

@@ -96,6 +96,20 @@ int nglod_volume_sample(const float *grid, int32_t side, int32_t feature_dim, co
 int nglod_sdf_fwd(const nglod_dense_model *model, const float *x, int64_t n,
                   int32_t lod, int32_t all_lods, float *out, nglod_stream_t stream);
 
+/* nglod_sdf_fwd with the points and results in HOST memory (pinned for the
+ * copies to overlap): x_host [n][3], out_host [n].  The points go through a
+ * device staging area in chunks of `chunk` points; chunk i's copy in,
+ * kernel and copy out run on one of three streams (the caller's and two
+ * library streams forked from and joined back into it), so the copies of
+ * one chunk overlap the kernels of the others.  scratch: device buffer of
+ * nglod_host_query_scratch_bytes(chunk) bytes, 256-byte aligned.  Queued on
+ * `stream` like every other call: out_host is complete when the work queued
+ * on `stream` is; x_host, out_host and scratch must stay valid until then.
+ * No reference counterpart (the reference takes device tensors only). */
+int64_t nglod_host_query_scratch_bytes(int64_t chunk);
+int nglod_sdf_fwd_host(const nglod_dense_model *model, const float *x_host, int64_t n, int32_t lod,
+                       float *out_host, int64_t chunk, void *scratch, nglod_stream_t stream);
+
 /* Persistent fused sphere tracer, float32: aabb prologue, march loop,
  * AABB cull and finite-difference normals in one launch.  Replaces
  * SphereTracer.forward (sdf-net/lib/tracer/SphereTracer.py:41-132) with
@@ -153,11 +167,16 @@ int nglod_bf16_pack_decoder(const float *w0_host, const float *b0_host, int32_t 
 int nglod_sdf_fwd_bf16(const nglod_bf16_model *model, const float *x, int64_t n, int32_t lod, float *out,
                        int32_t *status, nglod_stream_t stream);
 
+/* nglod_sdf_fwd_bf16 from host memory, pipelined as nglod_sdf_fwd_host. */
+int nglod_sdf_fwd_bf16_host(const nglod_bf16_model *model, const float *x_host, int64_t n, int32_t lod,
+                            float *out_host, int64_t chunk, void *scratch, int32_t *status, nglod_stream_t stream);
+
 /* SphereTracer.forward in the BF16 form: the persistent tracer of
  * nglod_trace with every sdf evaluation (march points and normal taps) done
  * by the bf16 tile kernel above, 128 rays per block evaluated together.
- * Same outputs and march rules as nglod_trace.  status: one device int32,
- * nonzero if a bounded tensor-core wait gave up. */
+ * Same outputs and march rules as nglod_trace, except that the ray
+ * parameter t is accumulated as a compensated fp32 sum (TwoSum per step).
+ * status: one device int32, nonzero if a bounded tensor-core wait gave up. */
 int nglod_trace_bf16(const nglod_bf16_model *model, const nglod_trace_params *params, const float *ray_o,
                      const float *ray_d, int64_t n, float *x, float *t, uint8_t *hit, float *normal,
                      int64_t *work_counter, int32_t *status, nglod_stream_t stream);
@@ -371,6 +390,128 @@ int nglod_sparse_trace(const nglod_sparse_model *model, int32_t lod, int32_t num
                        const float *ray_d, int64_t n, const int32_t *nuggets, int64_t n_nuggets,
                        int32_t *ray_first, float *x, float *t, uint8_t *hit, float *normal, int64_t *work_counter,
                        nglod_stream_t stream);
+
+/* ------------------------------------------------------------------------
+ * Serving: a continuous-batching request server over resident models.
+ *
+ * No reference counterpart: the reference renders one frame at a time in
+ * its viewer loop (sol-renderer/sdfRenderer.cpp:217-242) and answers point
+ * queries only through OctreeSDF.sdf.  The server keeps models resident and
+ * takes render and point-query requests as they arrive.  A request is
+ * admitted, in arrival order, as soon as (a) its device state fits in the
+ * server's pool of hbm_budget_bytes (first fit, 256-byte aligned regions)
+ * and (b) one of num_slots slots is free; each slot owns a CUDA stream, so
+ * admitted requests of different models, sizes and LODs run on the GPU at
+ * the same time.  Completion is detected by polling CUDA events (never a
+ * blocking device wait).  Every kernel computes each ray / point on its own,
+ * so a result is bitwise the same alone and in any mix.
+ *
+ * Ownership: the server owns its pool (allocated once at start), its streams
+ * and events.  Results live in the pool until nglod_serve_release.  Models
+ * and query points are the caller's device memory, borrowed: models until
+ * nglod_serve_destroy, points until their request has completed.
+ * Thread safety: every call locks the server; calls from several threads
+ * are serialised.
+ * ------------------------------------------------------------------------ */
+typedef struct nglod_server nglod_server; /* opaque */
+
+#define NGLOD_SERVE_RENDER 1
+#define NGLOD_SERVE_QUERY  2
+
+typedef struct nglod_serve_config {
+    int64_t hbm_budget_bytes; /* pool size: device state of requests on the GPU plus unreleased results */
+    int32_t num_slots;        /* requests on the GPU at once, one CUDA stream each, 1..64 */
+    int32_t reserved;
+} nglod_serve_config;
+
+typedef struct nglod_serve_request {
+    int32_t kind;                /* NGLOD_SERVE_RENDER or NGLOD_SERVE_QUERY */
+    int32_t model;               /* id from nglod_serve_add_model_* */
+    int32_t lod;                 /* LOD of every sdf evaluation; <0: finest */
+    int32_t width, height;       /* render: image size; rays as nglod_camera_rays */
+    float eye[3], at[3], up[3];  /* render: camera */
+    float fov_deg;               /* render */
+    nglod_trace_params trace;    /* render: march parameters (its lod field is ignored) */
+    const float *points;         /* query: device [n][3] float32 */
+    int64_t n;                   /* query: number of points */
+    int32_t has_ready_stream;    /* 1: the request's work first waits for the work queued on ready_stream */
+    int32_t reserved;            /*    at submit time (the stream that wrote `points`) */
+    nglod_stream_t ready_stream;
+} nglod_serve_request;
+
+typedef struct nglod_serve_result {
+    int64_t ticket;
+    int32_t kind;
+    int32_t status;         /* NGLOD_OK, or the error code of the request's launch or run */
+    double t_submit;        /* host monotonic clock (CLOCK_MONOTONIC), seconds */
+    double t_admit;
+    double t_done;          /* when a poll first saw the request finished */
+    int64_t units;          /* rays (render) or points (query) */
+    float *x;               /* render: [units][3] hit points (device, in the pool) */
+    float *t;               /* render: [units] depth */
+    uint8_t *hit;           /* render: [units] */
+    float *normal;          /* render: [units][3] */
+    float *sdf;             /* query: [units] distances */
+} nglod_serve_result;
+
+typedef struct nglod_serve_info {
+    int64_t budget_bytes, used_bytes, peak_used_bytes;
+    int32_t num_slots, pending, running, unpolled, held, max_concurrent;
+    int64_t submitted, completed;
+} nglod_serve_info;
+
+/* Device bytes a request takes from the pool (0 for an invalid request). */
+int64_t nglod_serve_request_bytes(const nglod_serve_request *request);
+
+/* Creates a server on the current CUDA device. */
+int nglod_serve_start(const nglod_serve_config *config, nglod_server **server);
+
+/* Registers a resident model (the descriptor is copied; the memory it points
+ * to stays the caller's).  *model_id: its index, from 0. */
+int nglod_serve_add_model_f32(nglod_server *server, const nglod_dense_model *model, int32_t *model_id);
+int nglod_serve_add_model_bf16(nglod_server *server, const nglod_bf16_model *model, int32_t *model_id);
+
+/* Queues a request.  t_arrival: its arrival time on the host monotonic clock
+ * (seconds; < 0: now), the start of its latency.  Admits whatever fits.
+ * NGLOD_ERR_CAPACITY if the request alone needs more than the whole pool. */
+int nglod_serve_submit(nglod_server *server, const nglod_serve_request *request, double t_arrival,
+                       int64_t *ticket);
+
+/* Retires finished requests, admits waiting ones, and returns up to
+ * max_results finished requests (each once, in completion order). */
+int nglod_serve_poll(nglod_server *server, nglod_serve_result *results, int32_t max_results, int32_t *count);
+
+/* Returns a polled request's region to the pool.  has_stream = 1: the region
+ * is reused only after the work queued on `stream` now (e.g. copies of the
+ * results) has finished. */
+int nglod_serve_release(nglod_server *server, int64_t ticket, int32_t has_stream, nglod_stream_t stream);
+
+int nglod_serve_get_info(nglod_server *server, nglod_serve_info *info);
+
+/* Bounded shutdown: drops the waiting requests, stops admitting, and polls
+ * the running ones for up to timeout_s seconds.  Finished requests stay
+ * pollable.  *unfinished: requests still on the GPU; *dropped: requests
+ * that never started. */
+int nglod_serve_stop(nglod_server *server, double timeout_s, int32_t *unfinished, int32_t *dropped);
+
+/* Waits for the server's streams, frees the pool, streams and events. */
+int nglod_serve_destroy(nglod_server *server);
+
+/* A server over caller-supplied launch / completion callbacks instead of
+ * CUDA (embedding in another runtime; scheduling tests on hosts without a
+ * GPU).  The pool is not allocated: regions are byte offsets, and result
+ * pointers are those offsets.  Callbacks run with the server locked and
+ * must not call the server. */
+typedef struct nglod_serve_executor {
+    void *ctx;
+    /* starts `request` in `slot` in pool region [region, region + bytes); 0 or an error code */
+    int32_t (*launch)(void *ctx, int64_t ticket, int32_t slot, const nglod_serve_request *request, int64_t region,
+                      int64_t bytes);
+    /* 1: the request in `slot` has finished; 0: still running; < 0: it failed with that code */
+    int32_t (*query)(void *ctx, int64_t ticket, int32_t slot);
+} nglod_serve_executor;
+int nglod_serve_start_custom(const nglod_serve_config *config, const nglod_serve_executor *executor,
+                             nglod_server **server);
 
 #ifdef __cplusplus
 }

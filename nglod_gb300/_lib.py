@@ -106,9 +106,80 @@ class Bf16Model(ctypes.Structure):
 
 BF16_TILE_BYTES = 12288
 
+SERVE_RENDER = 1
+SERVE_QUERY = 2
+
+
+class ServeConfig(ctypes.Structure):
+    _fields_ = [("hbm_budget_bytes", _i64), ("num_slots", _i32), ("reserved", _i32)]
+
+
+class ServeRequest(ctypes.Structure):
+    _fields_ = [
+        ("kind", _i32),
+        ("model", _i32),
+        ("lod", _i32),
+        ("width", _i32),
+        ("height", _i32),
+        ("eye", ctypes.c_float * 3),
+        ("at", ctypes.c_float * 3),
+        ("up", ctypes.c_float * 3),
+        ("fov_deg", ctypes.c_float),
+        ("trace", TraceParams),
+        ("points", _vp),
+        ("n", _i64),
+        ("has_ready_stream", _i32),
+        ("reserved", _i32),
+        ("ready_stream", _vp),
+    ]
+
+
+class ServeResult(ctypes.Structure):
+    _fields_ = [
+        ("ticket", _i64),
+        ("kind", _i32),
+        ("status", _i32),
+        ("t_submit", ctypes.c_double),
+        ("t_admit", ctypes.c_double),
+        ("t_done", ctypes.c_double),
+        ("units", _i64),
+        ("x", _vp),
+        ("t", _vp),
+        ("hit", _vp),
+        ("normal", _vp),
+        ("sdf", _vp),
+    ]
+
+
+class ServeInfo(ctypes.Structure):
+    _fields_ = [
+        ("budget_bytes", _i64),
+        ("used_bytes", _i64),
+        ("peak_used_bytes", _i64),
+        ("num_slots", _i32),
+        ("pending", _i32),
+        ("running", _i32),
+        ("unpolled", _i32),
+        ("held", _i32),
+        ("max_concurrent", _i32),
+        ("submitted", _i64),
+        ("completed", _i64),
+    ]
+
+
+SERVE_LAUNCH_FN = ctypes.CFUNCTYPE(_i32, _vp, _i64, _i32, ctypes.POINTER(ServeRequest), _i64, _i64)
+SERVE_QUERY_FN = ctypes.CFUNCTYPE(_i32, _vp, _i64, _i32)
+
+
+class ServeExecutor(ctypes.Structure):
+    _fields_ = [("ctx", _vp), ("launch", SERVE_LAUNCH_FN), ("query", SERVE_QUERY_FN)]
+
+
 # C struct name -> ctypes mirror (layouts are checked against the header by tests/test_abi.py)
 STRUCTS = {"nglod_dense_grads": DenseGrads, "nglod_adam_tensor": AdamTensor, "nglod_sparse_model": SparseModel,
-           "nglod_bf16_model": Bf16Model}
+           "nglod_bf16_model": Bf16Model, "nglod_serve_config": ServeConfig, "nglod_serve_request": ServeRequest,
+           "nglod_serve_result": ServeResult, "nglod_serve_info": ServeInfo,
+           "nglod_serve_executor": ServeExecutor}
 
 _u32 = ctypes.c_uint32
 _f32 = ctypes.c_float
@@ -147,6 +218,22 @@ SIGNATURES = {
                                         _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "nglod_camera_rays": (ctypes.c_int, [_vp, _vp, _vp, _f32, _i32, _i32, _vp, _vp, _vp]),
     "nglod_adam_step": (ctypes.c_int, [_vp, _i32, _i64, _f32, _f32, _f32, _f32, _f32, _i64, _vp]),
+    "nglod_host_query_scratch_bytes": (_i64, [_i64]),
+    "nglod_sdf_fwd_host": (ctypes.c_int, [ctypes.POINTER(DenseModel), _vp, _i64, _i32, _vp, _i64, _vp, _vp]),
+    "nglod_sdf_fwd_bf16_host": (ctypes.c_int, [ctypes.POINTER(Bf16Model), _vp, _i64, _i32, _vp, _i64, _vp, _vp,
+                                               _vp]),
+    "nglod_serve_request_bytes": (_i64, [ctypes.POINTER(ServeRequest)]),
+    "nglod_serve_start": (ctypes.c_int, [ctypes.POINTER(ServeConfig), ctypes.POINTER(_vp)]),
+    "nglod_serve_start_custom": (ctypes.c_int, [ctypes.POINTER(ServeConfig), ctypes.POINTER(ServeExecutor),
+                                                ctypes.POINTER(_vp)]),
+    "nglod_serve_add_model_f32": (ctypes.c_int, [_vp, ctypes.POINTER(DenseModel), ctypes.POINTER(_i32)]),
+    "nglod_serve_add_model_bf16": (ctypes.c_int, [_vp, ctypes.POINTER(Bf16Model), ctypes.POINTER(_i32)]),
+    "nglod_serve_submit": (ctypes.c_int, [_vp, ctypes.POINTER(ServeRequest), ctypes.c_double, ctypes.POINTER(_i64)]),
+    "nglod_serve_poll": (ctypes.c_int, [_vp, ctypes.POINTER(ServeResult), _i32, ctypes.POINTER(_i32)]),
+    "nglod_serve_release": (ctypes.c_int, [_vp, _i64, _i32, _vp]),
+    "nglod_serve_get_info": (ctypes.c_int, [_vp, ctypes.POINTER(ServeInfo)]),
+    "nglod_serve_stop": (ctypes.c_int, [_vp, ctypes.c_double, ctypes.POINTER(_i32), ctypes.POINTER(_i32)]),
+    "nglod_serve_destroy": (ctypes.c_int, [_vp]),
 }
 
 _LIB = None

@@ -63,6 +63,33 @@ class Bf16OctreeSDF:
                    "nglod_sdf_fwd_bf16")
         return out
 
+    def sdf_host(self, x_host, lod=None, out=None, chunk=1 << 20):
+        """sdf of points in host memory ([n, 3] float32; pinned for overlap)
+        into host memory ([n, 1] float32, returned): chunks are copied in,
+        evaluated and copied out on three streams joined into the current
+        one (nglod_sdf_fwd_bf16_host).  The result is complete once the
+        current stream's work is (e.g. after torch.cuda.synchronize())."""
+        if lod is None:
+            lod = self.lod
+        if x_host.is_cuda or x_host.dtype != torch.float32 or not x_host.is_contiguous():
+            raise RuntimeError("sdf_host takes a contiguous float32 CPU tensor (use sdf for device tensors)")
+        n = x_host.shape[0]
+        if out is None:
+            out = torch.empty(n, 1, pin_memory=True)
+        dev = self._status.device
+        scratch = self._host_scratch(chunk, dev)
+        _lib.check(_lib.load().nglod_sdf_fwd_bf16_host(self._m, _lib.ptr(x_host), n, -1 if lod is None else lod,
+                                                       _lib.ptr(out), chunk, _lib.ptr(scratch), _lib.ptr(self._status),
+                                                       _lib.stream_ptr(dev)), "nglod_sdf_fwd_bf16_host")
+        return out
+
+    def _host_scratch(self, chunk, dev):
+        nbytes = int(_lib.load().nglod_host_query_scratch_bytes(chunk))
+        cur = getattr(self, "_scratch", None)
+        if cur is None or cur.numel() < nbytes:
+            self._scratch = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+        return self._scratch
+
     def check_status(self):
         """Raises if a tensor-core wait of the last launches gave up."""
         if int(self._status.item()) != 0:

@@ -1,6 +1,6 @@
 // BF16 form of the dense path: bf16 channel-last feature volumes gathered by
-// four lanes per point (each lane owns 8 of the 32 channels of every corner,
-// one 16-byte load per corner), the LOD sum kept in fp32 and written as one
+// four lanes per point for point queries and two for the tracer (each lane
+// owns 8 or 16 of the 32 channels of every corner, 16-byte loads), the LOD sum kept in fp32 and written as one
 // row of a bf16 tile in shared memory, and the decoder's 35 -> 128 layer run
 // by tcgen05.mma on 128-point tiles with the accumulator in tensor memory.
 // b0, ReLU and the 128 -> 1 layer are an fp32 epilogue on the TMEM rows.
@@ -42,9 +42,65 @@ __device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
     return *reinterpret_cast<const uint32_t *>(&h);
 }
 
-// Adds this lane's 8 channels (8q .. 8q+7) of the trilinear sample of one
-// bf16 volume (s vertices per side) at p to acc; PyTorch grid_sample
-// arithmetic (align_corners, border clamp), corners in tnw..bse order.
+// Adds this lane's 16 channels (16h .. 16h+15) of the trilinear sample of
+// one bf16 volume (s vertices per side) at p to acc; PyTorch grid_sample
+// arithmetic (align_corners, border clamp), corners in tnw..bse order.  Two
+// lanes share a point: each loads 2 x 16 bytes per corner, and the corner
+// index / weight math is done once per 16 channels.
+__device__ __forceinline__ void gather_bf16_half(const __nv_bfloat16 *__restrict__ g, int s, float px, float py,
+                                                 float pz, int h, float (&acc)[16]) {
+    const float sm1 = (float)(s - 1);
+    const float ix = fminf(sm1, fmaxf(((px + 1.f) / 2.f) * sm1, 0.f));
+    const float iy = fminf(sm1, fmaxf(((py + 1.f) / 2.f) * sm1, 0.f));
+    const float iz = fminf(sm1, fmaxf(((pz + 1.f) / 2.f) * sm1, 0.f));
+    const float x0 = floorf(ix), y0 = floorf(iy), z0 = floorf(iz);
+    const float wx1 = ix - x0, wx0 = (x0 + 1.f) - ix;
+    const float wy1 = iy - y0, wy0 = (y0 + 1.f) - iy;
+    const float wz1 = iz - z0, wz0 = (z0 + 1.f) - iz;
+    const int xi = (int)x0, yi = (int)y0, zi = (int)z0;
+    const int xj = min(xi + 1, s - 1), yj = min(yi + 1, s - 1), zj = min(zi + 1, s - 1);
+    const uint4 *base = reinterpret_cast<const uint4 *>(g) + 2 * h;  // 4 uint4 per vertex
+    // uint4 offsets fit in 32 bits (volumes up to 513^3 x 64 B)
+    const int sy = s * 4, sz = s * sy;
+    const int o0 = zi * sz + yi * sy + xi * 4;
+    const int ox = (xj - xi) * 4, oy = (yj - yi) * sy, oz = (zj - zi) * sz;
+    const int o[8] = {o0, o0 + ox, o0 + oy, o0 + oy + ox, o0 + oz, o0 + oz + ox, o0 + oz + oy, o0 + oz + oy + ox};
+    const float wxy[4] = {wx0 * wy0, wx1 * wy0, wx0 * wy1, wx1 * wy1};
+    const float w[8] = {wxy[0] * wz0, wxy[1] * wz0, wxy[2] * wz0, wxy[3] * wz0,
+                        wxy[0] * wz1, wxy[1] * wz1, wxy[2] * wz1, wxy[3] * wz1};
+    uint4 v[8], u[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        v[k] = __ldg(base + o[k]);
+        u[k] = __ldg(base + o[k] + 1);
+    }
+    // Packed fp32 FMAs (two channels per instruction) on the unpacked bf16 pairs.
+    float2 a2[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) a2[c] = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const float2 w2 = make_float2(w[k], w[k]);
+        a2[0] = __ffma2_rn(make_float2(bf_lo(v[k].x), bf_hi(v[k].x)), w2, a2[0]);
+        a2[1] = __ffma2_rn(make_float2(bf_lo(v[k].y), bf_hi(v[k].y)), w2, a2[1]);
+        a2[2] = __ffma2_rn(make_float2(bf_lo(v[k].z), bf_hi(v[k].z)), w2, a2[2]);
+        a2[3] = __ffma2_rn(make_float2(bf_lo(v[k].w), bf_hi(v[k].w)), w2, a2[3]);
+        a2[4] = __ffma2_rn(make_float2(bf_lo(u[k].x), bf_hi(u[k].x)), w2, a2[4]);
+        a2[5] = __ffma2_rn(make_float2(bf_lo(u[k].y), bf_hi(u[k].y)), w2, a2[5]);
+        a2[6] = __ffma2_rn(make_float2(bf_lo(u[k].z), bf_hi(u[k].z)), w2, a2[6]);
+        a2[7] = __ffma2_rn(make_float2(bf_lo(u[k].w), bf_hi(u[k].w)), w2, a2[7]);
+    }
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+        acc[2 * c] += a2[c].x;
+        acc[2 * c + 1] += a2[c].y;
+    }
+}
+
+// Four lanes per point, 8 channels (8q .. 8q+7) each, one 16-byte load per
+// corner: a point's 64-byte vertex is read by one load instruction, which
+// keeps the distinct cache lines per instruction low when consecutive
+// points are far apart (unsorted point queries).
 __device__ __forceinline__ void gather_bf16_quarter(const __nv_bfloat16 *__restrict__ g, int s, float px, float py,
                                                     float pz, int q, float (&acc)[8]) {
     const float sm1 = (float)(s - 1);
@@ -58,7 +114,6 @@ __device__ __forceinline__ void gather_bf16_quarter(const __nv_bfloat16 *__restr
     const int xi = (int)x0, yi = (int)y0, zi = (int)z0;
     const int xj = min(xi + 1, s - 1), yj = min(yi + 1, s - 1), zj = min(zi + 1, s - 1);
     const uint4 *base = reinterpret_cast<const uint4 *>(g) + q;  // 4 uint4 per vertex
-    // uint4 offsets fit in 32 bits (volumes up to 513^3 x 64 B)
     const int sy = s * 4, sz = s * sy;
     const int o0 = zi * sz + yi * sy + xi * 4;
     const int ox = (xj - xi) * 4, oy = (yj - yi) * sy, oz = (zj - zi) * sz;
@@ -69,7 +124,6 @@ __device__ __forceinline__ void gather_bf16_quarter(const __nv_bfloat16 *__restr
     uint4 v[8];
 #pragma unroll
     for (int k = 0; k < 8; ++k) v[k] = __ldg(base + o[k]);
-    // Packed fp32 FMAs (two channels per instruction) on the unpacked bf16 pairs.
     float2 a01 = make_float2(0.f, 0.f), a23 = a01, a45 = a01, a67 = a01;
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
@@ -84,6 +138,47 @@ __device__ __forceinline__ void gather_bf16_quarter(const __nv_bfloat16 *__restr
     for (int c = 0; c < 8; ++c) acc[c] += a[c];
 }
 
+// Gathers all LODs 0..L of a point for one lane (LPP lanes per point; lane
+// part `part` owns channels part*32/LPP ..), summing in fp32.
+template <int LPP>
+__device__ __forceinline__ void gather_point(const nglod_bf16_model &m, int L, float px, float py, float pz, int part,
+                                             float (&acc)[32 / LPP]) {
+#pragma unroll
+    for (int c = 0; c < 32 / LPP; ++c) acc[c] = 0.f;
+#pragma unroll 1
+    for (int l = 0; l <= L; ++l) {
+        const __nv_bfloat16 *g = static_cast<const __nv_bfloat16 *>(m.grid[l]);
+        const int s = (1 << (l + m.base_lod)) + 1;
+        if constexpr (LPP == 4)
+            gather_bf16_quarter(g, s, px, py, pz, part, acc);
+        else
+            gather_bf16_half(g, s, px, py, pz, part, acc);
+    }
+}
+
+// Writes a point's tile row: this lane's 32/LPP summed features (bf16, K
+// columns from part*32/LPP) and, from part 0, the position / bias columns
+// 32..39.
+template <int LPP>
+__device__ __forceinline__ void write_tile_row(uint8_t *sA, int row, int h, const float (&acc)[32 / LPP], float px,
+                                               float py, float pz) {
+    constexpr int kCh = 32 / LPP;
+#pragma unroll
+    for (int j = 0; j < kCh / 8; ++j) {
+        const uint4 f = make_uint4(pack_bf16x2(acc[8 * j], acc[8 * j + 1]), pack_bf16x2(acc[8 * j + 2], acc[8 * j + 3]),
+                                   pack_bf16x2(acc[8 * j + 4], acc[8 * j + 5]),
+                                   pack_bf16x2(acc[8 * j + 6], acc[8 * j + 7]));
+        *reinterpret_cast<uint4 *>(sA + tc::tile_offset(row, kCh * h + 8 * j, kKC)) = f;
+    }
+    if (h == 0) {
+        const float hx = __bfloat162float(__float2bfloat16_rn(px));
+        const float hy = __bfloat162float(__float2bfloat16_rn(py));
+        const float hz = __bfloat162float(__float2bfloat16_rn(pz));
+        const uint4 p = make_uint4(pack_bf16x2(hx, hy), pack_bf16x2(hz, px - hx), pack_bf16x2(py - hy, pz - hz),
+                                   kOneOne);
+        *reinterpret_cast<uint4 *>(sA + tc::tile_offset(row, 32, kKC)) = p;
+    }
+}
 
 // Ray entry into [-1,1]^3 with sol_nglod_kernel.cu:92-150's float arithmetic
 // (same as the float32 path's box_entry).
@@ -169,13 +264,15 @@ __global__ void __launch_bounds__(kTP, 4) sdf_fwd_bf16_tc_kernel(const Bf16Args 
     const uint32_t sa = tc::smem_addr(sA), sb = tc::smem_addr(sB);
     const uint32_t idesc = tc::idesc_bf16_f32(kTP, kHid);
     uint32_t phase = 0;
-    const int pp = lane >> 2, q = lane & 3;
+    // unsorted query points: four lanes per point (one load instruction per vertex)
+    constexpr int kLPP = 4;
+    const int pp = lane / kLPP, h = lane % kLPP;
 
     for (int64_t tile = blockIdx.x; tile * kTP < a.n; tile += gridDim.x) {
-        // 1. gather: warp w fills rows 32w .. 32w+31, eight points per pass
+        // 1. gather: warp w fills rows 32w .. 32w+31, 32/kLPP points per pass
 #pragma unroll 1
-        for (int pass = 0; pass < 4; ++pass) {
-            const int row = warp * 32 + pass * 8 + pp;
+        for (int pass = 0; pass < kLPP; ++pass) {
+            const int row = warp * 32 + pass * (32 / kLPP) + pp;
             const int64_t gi = tile * kTP + row;
             float px = 0.f, py = 0.f, pz = 0.f;
             if (gi < a.n) {
@@ -183,22 +280,9 @@ __global__ void __launch_bounds__(kTP, 4) sdf_fwd_bf16_tc_kernel(const Bf16Args 
                 py = a.x[3 * gi + 1];
                 pz = a.x[3 * gi + 2];
             }
-            float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-#pragma unroll 1
-            for (int l = 0; l <= a.L; ++l)
-                gather_bf16_quarter(static_cast<const __nv_bfloat16 *>(a.m.grid[l]), (1 << (l + a.m.base_lod)) + 1,
-                                    px, py, pz, q, acc);
-            const uint4 f = make_uint4(pack_bf16x2(acc[0], acc[1]), pack_bf16x2(acc[2], acc[3]),
-                                       pack_bf16x2(acc[4], acc[5]), pack_bf16x2(acc[6], acc[7]));
-            *reinterpret_cast<uint4 *>(sA + tc::tile_offset(row, 8 * q, kKC)) = f;
-            if (q == 0) {
-                const float hx = __bfloat162float(__float2bfloat16_rn(px));
-                const float hy = __bfloat162float(__float2bfloat16_rn(py));
-                const float hz = __bfloat162float(__float2bfloat16_rn(pz));
-                const uint4 p = make_uint4(pack_bf16x2(hx, hy), pack_bf16x2(hz, px - hx), pack_bf16x2(py - hy, pz - hz),
-                                           kOneOne);
-                *reinterpret_cast<uint4 *>(sA + tc::tile_offset(row, 32, kKC)) = p;
-            }
+            float acc[32 / kLPP];
+            gather_point<kLPP>(a.m, a.L, px, py, pz, h, acc);
+            write_tile_row<kLPP>(sA, row, h, acc, px, py, pz);
         }
         tc::fence_proxy_async_smem();
         __syncthreads();
@@ -301,7 +385,10 @@ __global__ void __launch_bounds__(kTP, 4) trace_bf16_tc_kernel(const Bf16TraceAr
     const uint32_t sa = tc::smem_addr(sA), sb = tc::smem_addr(sB);
     const uint32_t idesc = tc::idesc_bf16_f32(kTP, kHid);
     uint32_t mphase = 0;
-    const int pp = lane >> 2, q = lane & 3;
+    // neighbouring rays query nearby points: two lanes per point (half the
+    // corner index / weight work; the lines of a load instruction are shared)
+    constexpr int kLPP = 2;
+    const int pp = lane / kLPP, hh = lane % kLPP;
 
     const unsigned FULL = 0xffffffffu;
     const unsigned lt_mask = (1u << lane) - 1u;
@@ -310,7 +397,11 @@ __global__ void __launch_bounds__(kTP, 4) trace_bf16_tc_kernel(const Bf16TraceAr
     int phase = bNeed, step = 0;
     int64_t ray = 0;
     float ox = 0.f, oy = 0.f, oz = 0.f, dx = 0.f, dy = 0.f, dz = 0.f;
-    float xx = 0.f, xy = 0.f, xz = 0.f, t = 0.f, d = 0.f, dprev = 0.f;
+    // t is carried as an unevaluated sum t + tc: each step adds d with
+    // Knuth's TwoSum and keeps the rounding error in tc (compensated
+    // summation), so 64+ steps of small d do not drift; te = t + tc is the
+    // depth used for positions, the far-clip test and the output.
+    float xx = 0.f, xy = 0.f, xz = 0.f, t = 0.f, tc = 0.f, te = 0.f, d = 0.f, dprev = 0.f;
     float g[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     float nx = 0.f, ny = 0.f, nz = 0.f;
     bool cond = false, hitr = false, hitf = false;
@@ -324,15 +415,15 @@ __global__ void __launch_bounds__(kTP, 4) trace_bf16_tc_kernel(const Bf16TraceAr
             finish();
             return;
         }
-        hitr = fabsf(t) < a.p.far_clip;
+        hitr = fabsf(te) < a.p.far_clip;
         cond = cond && (fabsf(d) > a.p.min_dis) && (fabsf((d + dprev) / 2.f) > a.p.osc_dis) && hitr;
         if (!cond) {
             finish();
             return;
         }
-        xx = __fadd_rn(ox, __fmul_rn(dx, t));
-        xy = __fadd_rn(oy, __fmul_rn(dy, t));
-        xz = __fadd_rn(oz, __fmul_rn(dz, t));
+        xx = __fadd_rn(ox, __fmul_rn(dx, te));
+        xy = __fadd_rn(oy, __fmul_rn(dy, te));
+        xz = __fadd_rn(oz, __fmul_rn(dz, te));
         dprev = d;
         phase = bMarch;
     };
@@ -343,7 +434,7 @@ __global__ void __launch_bounds__(kTP, 4) trace_bf16_tc_kernel(const Bf16TraceAr
                 a.x[3 * ray + 0] = xx;
                 a.x[3 * ray + 1] = xy;
                 a.x[3 * ray + 2] = xz;
-                a.t[ray] = t;
+                a.t[ray] = te;
                 a.hit[ray] = hitf ? 1 : 0;
                 if (a.normal) {
                     const bool hn = hitf && a.p.want_normals;
@@ -373,6 +464,8 @@ __global__ void __launch_bounds__(kTP, 4) trace_bf16_tc_kernel(const Bf16TraceAr
                     dz = a.ray_d[3 * ray + 2];
                     t = 0.f;
                     cond = box_entry_bf(ox, oy, oz, dx, dy, dz, t);
+                    tc = 0.f;
+                    te = t;
                     xx = cond ? fmaf(dx, t, ox) : ox;
                     xy = cond ? fmaf(dy, t, oy) : oy;
                     xz = cond ? fmaf(dz, t, oz) : oz;
@@ -400,25 +493,12 @@ __global__ void __launch_bounds__(kTP, 4) trace_bf16_tc_kernel(const Bf16TraceAr
         qpts[tid] = make_float4(qx, qy, qz, 0.f);
         __syncthreads();
 #pragma unroll 1
-        for (int pass = 0; pass < 4; ++pass) {
-            const int row = warp * 32 + pass * 8 + pp;
+        for (int pass = 0; pass < kLPP; ++pass) {
+            const int row = warp * 32 + pass * (32 / kLPP) + pp;
             const float4 pt = qpts[row];
-            float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-#pragma unroll 1
-            for (int l = 0; l <= a.L; ++l)
-                gather_bf16_quarter(static_cast<const __nv_bfloat16 *>(a.m.grid[l]), (1 << (l + a.m.base_lod)) + 1,
-                                    pt.x, pt.y, pt.z, q, acc);
-            const uint4 f = make_uint4(pack_bf16x2(acc[0], acc[1]), pack_bf16x2(acc[2], acc[3]),
-                                       pack_bf16x2(acc[4], acc[5]), pack_bf16x2(acc[6], acc[7]));
-            *reinterpret_cast<uint4 *>(sA + tc::tile_offset(row, 8 * q, kKC)) = f;
-            if (q == 0) {
-                const float hx = __bfloat162float(__float2bfloat16_rn(pt.x));
-                const float hy = __bfloat162float(__float2bfloat16_rn(pt.y));
-                const float hz = __bfloat162float(__float2bfloat16_rn(pt.z));
-                const uint4 pp4 = make_uint4(pack_bf16x2(hx, hy), pack_bf16x2(hz, pt.x - hx),
-                                             pack_bf16x2(pt.y - hy, pt.z - hz), kOneOne);
-                *reinterpret_cast<uint4 *>(sA + tc::tile_offset(row, 32, kKC)) = pp4;
-            }
+            float acc[32 / kLPP];
+            gather_point<kLPP>(a.m, a.L, pt.x, pt.y, pt.z, hh, acc);
+            write_tile_row<kLPP>(sA, row, hh, acc, pt.x, pt.y, pt.z);
         }
         tc::fence_proxy_async_smem();
         __syncthreads();
@@ -449,7 +529,12 @@ __global__ void __launch_bounds__(kTP, 4) trace_bf16_tc_kernel(const Bf16TraceAr
             march_decide();
         } else if (phase == bMarch) {
             d = v * a.p.step_size;
-            t = t + d;
+            const float tsum = __fadd_rn(t, d);
+            const float bp = __fsub_rn(tsum, t);
+            const float err = __fadd_rn(__fsub_rn(t, __fsub_rn(tsum, bp)), __fsub_rn(d, bp));
+            t = tsum;
+            tc = __fadd_rn(tc, err);
+            te = __fadd_rn(t, tc);
             ++step;
             march_decide();
         } else if (phase >= bTap0 && phase < bDone) {
@@ -507,8 +592,10 @@ extern "C" int nglod_bf16_pack_decoder(const float *w0_host, const float *b0_hos
     return NGLOD_OK;
 }
 
-extern "C" int nglod_sdf_fwd_bf16(const nglod_bf16_model *model, const float *x, int64_t n, int32_t lod, float *out,
-                                  int32_t *status, nglod_stream_t stream) {
+// zero_status: reset *status on the stream first (the public call); the
+// host-memory pipeline resets it once for all of its chunks.
+static int sdf_fwd_bf16_impl(const nglod_bf16_model *model, const float *x, int64_t n, int32_t lod, float *out,
+                             int32_t *status, cudaStream_t s, bool zero_status) {
     NGLOD_REQUIRE(model != nullptr, NGLOD_ERR_INVALID, "model is null");
     NGLOD_REQUIRE(model->num_lods >= 1 && model->num_lods <= NGLOD_MAX_LODS, NGLOD_ERR_INVALID, "num_lods=%d",
                   model->num_lods);
@@ -526,8 +613,8 @@ extern "C" int nglod_sdf_fwd_bf16(const nglod_bf16_model *model, const float *x,
     NGLOD_REQUIRE(n >= 0, NGLOD_ERR_INVALID, "n=%lld is negative", (long long)n);
     if (n == 0) return NGLOD_OK;
     NGLOD_REQUIRE(x && out && status, NGLOD_ERR_INVALID, "null pointer argument");
-    cudaStream_t s = (cudaStream_t)stream;
-    NGLOD_TRY(cuda_status(cudaMemsetAsync(status, 0, sizeof(int32_t), s), "nglod_sdf_fwd_bf16 memset"));
+    if (zero_status)
+        NGLOD_TRY(cuda_status(cudaMemsetAsync(status, 0, sizeof(int32_t), s), "nglod_sdf_fwd_bf16 memset"));
     Bf16Args a;
     a.m = *model;
     a.x = x;
@@ -542,6 +629,36 @@ extern "C" int nglod_sdf_fwd_bf16(const nglod_bf16_model *model, const float *x,
     const int64_t cap = (int64_t)num_sms() * 4;
     sdf_fwd_bf16_tc_kernel<<<(int)(tiles < cap ? tiles : cap), kTP, kSmemBytes, s>>>(a);
     return launch_status("nglod_sdf_fwd_bf16");
+}
+
+extern "C" int nglod_sdf_fwd_bf16(const nglod_bf16_model *model, const float *x, int64_t n, int32_t lod, float *out,
+                                  int32_t *status, nglod_stream_t stream) {
+    return sdf_fwd_bf16_impl(model, x, n, lod, out, status, (cudaStream_t)stream, true);
+}
+
+namespace {
+struct Bf16HostCtx {
+    const nglod_bf16_model *model;
+    int32_t lod;
+    int32_t *status;
+};
+int bf16_host_chunk(const void *ctx, const float *x, int64_t m, float *out, cudaStream_t s) {
+    const Bf16HostCtx *c = static_cast<const Bf16HostCtx *>(ctx);
+    return sdf_fwd_bf16_impl(c->model, x, m, c->lod, out, c->status, s, false);
+}
+}  // namespace
+
+extern "C" int nglod_sdf_fwd_bf16_host(const nglod_bf16_model *model, const float *x_host, int64_t n, int32_t lod,
+                                       float *out_host, int64_t chunk, void *scratch, int32_t *status,
+                                       nglod_stream_t stream) {
+    NGLOD_TRY(sdf_fwd_bf16_impl(model, nullptr, 0, lod, nullptr, nullptr, nullptr, false));  // validates the model
+    NGLOD_REQUIRE(n >= 0, NGLOD_ERR_INVALID, "n=%lld is negative", (long long)n);
+    if (n == 0) return NGLOD_OK;
+    NGLOD_REQUIRE(status, NGLOD_ERR_INVALID, "null pointer argument");
+    cudaStream_t s = (cudaStream_t)stream;
+    NGLOD_TRY(cuda_status(cudaMemsetAsync(status, 0, sizeof(int32_t), s), "nglod_sdf_fwd_bf16_host memset"));
+    const Bf16HostCtx ctx{model, lod, status};
+    return host_query_pipeline(x_host, n, out_host, chunk, scratch, s, bf16_host_chunk, &ctx);
 }
 
 extern "C" int nglod_trace_bf16(const nglod_bf16_model *model, const nglod_trace_params *params, const float *ray_o,

@@ -24,6 +24,19 @@ int num_sms();
 
 inline bool aligned(const void *p, uintptr_t a) { return (reinterpret_cast<uintptr_t>(p) & (a - 1)) == 0; }
 
+// Host-memory queries: points [n][3] and results [n] in host memory, in
+// chunks through a device staging area of kHostStages buffers; chunk i runs
+// H2D -> kernel -> D2H on stage i % kHostStages, whose stream is the
+// caller's (stage 0) or one of the library's helper streams of the current
+// device, forked from and joined back into the caller's stream, so that the
+// copies of one chunk overlap the kernels of the others.
+constexpr int kHostStages = 3;
+int64_t host_stage_bytes(int64_t chunk);
+// launch(x_dev, m, out_dev, stream) queues one chunk's kernel.
+using HostChunkLaunch = int (*)(const void *ctx, const float *x, int64_t m, float *out, cudaStream_t s);
+int host_query_pipeline(const float *x_host, int64_t n, float *out_host, int64_t chunk, void *scratch,
+                        cudaStream_t stream, HostChunkLaunch launch, const void *ctx);
+
 }  // namespace nglod
 
 #define NGLOD_REQUIRE(cond, code, ...)        \

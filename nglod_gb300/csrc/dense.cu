@@ -352,6 +352,24 @@ extern "C" int nglod_sdf_fwd(const nglod_dense_model *model, const float *x, int
     return launch_status("nglod_sdf_fwd");
 }
 
+namespace {
+struct F32HostCtx {
+    const nglod_dense_model *model;
+    int32_t lod;
+};
+int f32_host_chunk(const void *ctx, const float *x, int64_t m, float *out, cudaStream_t s) {
+    const F32HostCtx *c = static_cast<const F32HostCtx *>(ctx);
+    return nglod_sdf_fwd(c->model, x, m, c->lod, 0, out, (nglod_stream_t)s);
+}
+}  // namespace
+
+extern "C" int nglod_sdf_fwd_host(const nglod_dense_model *model, const float *x_host, int64_t n, int32_t lod,
+                                  float *out_host, int64_t chunk, void *scratch, nglod_stream_t stream) {
+    NGLOD_TRY(nglod_sdf_fwd(model, nullptr, 0, lod, 0, nullptr, stream));  // validates the model
+    const F32HostCtx ctx{model, lod};
+    return host_query_pipeline(x_host, n, out_host, chunk, scratch, (cudaStream_t)stream, f32_host_chunk, &ctx);
+}
+
 extern "C" int nglod_trace(const nglod_dense_model *model, const nglod_trace_params *params, const float *ray_o,
                            const float *ray_d, int64_t n, float *x, float *t, uint8_t *hit, float *normal,
                            int64_t *work_counter, nglod_stream_t stream) {

@@ -3,6 +3,8 @@
 #include <stdarg.h>
 #include <stdio.h>
 
+#include <mutex>
+
 #include "common.cuh"
 
 namespace nglod {
@@ -34,7 +36,77 @@ int num_sms() {
     return cache[dev];
 }
 
+// Helper streams of one device (created on first use, kept for the life of
+// the process) and the fork / join events of the pipeline.  The mutex keeps
+// one pipeline's event record / wait pairs from interleaving with another's.
+struct HostStages {
+    std::mutex mu;
+    bool ready = false;
+    cudaStream_t aux[kHostStages - 1] = {};
+    cudaEvent_t fork = nullptr;
+    cudaEvent_t join[kHostStages - 1] = {};
+};
+static HostStages g_stages[64];
+
+int64_t host_stage_bytes(int64_t chunk) {
+    const int64_t xs = (chunk * 12 + 255) & ~(int64_t)255, os = (chunk * 4 + 255) & ~(int64_t)255;
+    return kHostStages * (xs + os);
+}
+
+int host_query_pipeline(const float *x_host, int64_t n, float *out_host, int64_t chunk, void *scratch,
+                        cudaStream_t stream, HostChunkLaunch launch, const void *ctx) {
+    NGLOD_REQUIRE(n >= 0 && chunk >= 1, NGLOD_ERR_INVALID, "n=%lld, chunk=%lld", (long long)n, (long long)chunk);
+    if (n == 0) return NGLOD_OK;
+    NGLOD_REQUIRE(x_host && out_host && scratch, NGLOD_ERR_INVALID, "null pointer argument");
+    NGLOD_REQUIRE(aligned(scratch, 256), NGLOD_ERR_ALIGN, "scratch must be 256-byte aligned");
+    int dev = 0;
+    NGLOD_TRY(cuda_status(cudaGetDevice(&dev), "host query: device"));
+    NGLOD_REQUIRE(dev >= 0 && dev < 64, NGLOD_ERR_UNSUPPORTED, "device %d", dev);
+    HostStages &hs = g_stages[dev];
+    std::lock_guard<std::mutex> g(hs.mu);
+    if (!hs.ready) {
+        for (int i = 0; i < kHostStages - 1; ++i) {
+            NGLOD_TRY(cuda_status(cudaStreamCreateWithFlags(&hs.aux[i], cudaStreamNonBlocking), "host query: stream"));
+            NGLOD_TRY(cuda_status(cudaEventCreateWithFlags(&hs.join[i], cudaEventDisableTiming), "host query: event"));
+        }
+        NGLOD_TRY(cuda_status(cudaEventCreateWithFlags(&hs.fork, cudaEventDisableTiming), "host query: event"));
+        hs.ready = true;
+    }
+    cudaStream_t st[kHostStages];
+    st[0] = stream;
+    for (int i = 1; i < kHostStages; ++i) st[i] = hs.aux[i - 1];
+    const int64_t xs = (chunk * 12 + 255) & ~(int64_t)255, os = (chunk * 4 + 255) & ~(int64_t)255;
+    char *base = static_cast<char *>(scratch);
+    NGLOD_TRY(cuda_status(cudaEventRecord(hs.fork, stream), "host query: fork"));
+    for (int i = 1; i < kHostStages; ++i)
+        NGLOD_TRY(cuda_status(cudaStreamWaitEvent(st[i], hs.fork, 0), "host query: fork"));
+    int status = NGLOD_OK;
+    int64_t k = 0;
+    for (int64_t c = 0; c < n && status == NGLOD_OK; c += chunk, ++k) {
+        const int64_t m = n - c < chunk ? n - c : chunk;
+        const int b = (int)(k % kHostStages);
+        float *xd = reinterpret_cast<float *>(base + b * (xs + os));
+        float *od = reinterpret_cast<float *>(base + b * (xs + os) + xs);
+        status = cuda_status(cudaMemcpyAsync(xd, x_host + 3 * c, (size_t)m * 12, cudaMemcpyHostToDevice, st[b]),
+                             "host query: copy in");
+        if (status == NGLOD_OK) status = launch(ctx, xd, m, od, st[b]);
+        if (status == NGLOD_OK)
+            status = cuda_status(cudaMemcpyAsync(out_host + c, od, (size_t)m * 4, cudaMemcpyDeviceToHost, st[b]),
+                                 "host query: copy out");
+    }
+    // join every helper stream back into the caller's, also after an error
+    for (int i = 1; i < kHostStages; ++i) {
+        const int e1 = cuda_status(cudaEventRecord(hs.join[i - 1], st[i]), "host query: join");
+        const int e2 = e1 == NGLOD_OK ? cuda_status(cudaStreamWaitEvent(stream, hs.join[i - 1], 0), "host query: join")
+                                      : e1;
+        if (status == NGLOD_OK) status = e2;
+    }
+    return status;
+}
+
 }  // namespace nglod
+
+extern "C" int64_t nglod_host_query_scratch_bytes(int64_t chunk) { return chunk >= 1 ? nglod::host_stage_bytes(chunk) : -1; }
 
 extern "C" const char *nglod_version(void) { return "nglod_gb300 0.1 (sm_103a)"; }
 

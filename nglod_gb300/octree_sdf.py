@@ -146,6 +146,29 @@ class OctreeSDF(nn.Module):
             self.loss_preds = preds
         return preds if return_lst else preds[-1]
 
+    @torch.no_grad()
+    def sdf_host(self, x_host, lod=None, out=None, chunk=1 << 20):
+        """Inference sdf of points in host memory ([n, 3] float32; pinned for
+        overlap) into host memory ([n, 1], returned), pipelined in chunks on
+        three streams joined into the current one (nglod_sdf_fwd_host).  The
+        result is complete once the current stream's work is."""
+        if lod is None:
+            lod = self.lod
+        if x_host.is_cuda or x_host.dtype != torch.float32 or not x_host.is_contiguous():
+            raise RuntimeError("sdf_host takes a contiguous float32 CPU tensor (use sdf for device tensors)")
+        n = x_host.shape[0]
+        if out is None:
+            out = torch.empty(n, 1, pin_memory=True)
+        dev = self.features[0].fm.device
+        _lib.require_cuda(self.features[0].fm)
+        nbytes = int(_lib.load().nglod_host_query_scratch_bytes(chunk))
+        scratch = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+        m = self.dense_model()
+        in_range = lod is not None and 0 <= lod < self.num_lods
+        _lib.check(_lib.load().nglod_sdf_fwd_host(m, _lib.ptr(x_host), n, lod if in_range else -1, _lib.ptr(out), chunk,
+                                                  _lib.ptr(scratch), _lib.stream_ptr(dev)), "nglod_sdf_fwd_host")
+        return out
+
     # -- kernel plumbing ------------------------------------------------------
     def dense_model(self):
         """The ``nglod_dense_model`` descriptor of the current parameters."""

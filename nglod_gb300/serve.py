@@ -9,23 +9,28 @@ models resident on the GPU and serves two request kinds as they arrive:
                     RenderBuffer (x, depth, hit, normal) on the device
     QueryRequest    SDF values of a point batch at a LOD -> [N, 1]
 
-Scheduling.  Requests wait in arrival order until (a) their device memory
-(ray state and outputs, counted in bytes) fits under the HBM budget next to
-the requests already running and (b) a stream is free.  Each admitted
-request is enqueued on its own CUDA stream, so requests of different models,
-resolutions and LODs run on the GPU at the same time; a request that arrives
-while others are on the GPU is admitted as soon as budget and a stream free
-up.  Completion is detected by polling CUDA events, never by blocking the
-device.  Results are bit-identical to serving the same request alone: every
-kernel computes each ray / point independently of the others in its launch.
+Scheduling is native (``nglod_serve_*``, csrc/serve.cu): requests wait in
+arrival order until (a) their device state (ray state and results, counted
+in bytes) fits in the server's pool of ``hbm_budget_bytes`` next to the
+requests already there and (b) a slot (one CUDA stream each) is free.
+Admitted requests of different models, resolutions and LODs run on the GPU
+at the same time; a request that arrives while others run is admitted as
+soon as memory and a slot free up.  Completion is detected by polling CUDA
+events, never by blocking the device.  Results are bit-identical to serving
+the same request alone: every kernel computes each ray / point
+independently of the others in its launch.
 
 ``stats()`` reports p50 / p99 latency (arrival to completion, host
 monotonic clock) beside rays/s and queries/s.  ``stop(timeout)`` waits for
 running work with a bounded wait and reports what did not finish.
+
+Executors: ``CudaExecutor`` (resident models on one device) runs requests
+with the library's kernels.  Any other object with ``launch(ticket, slot)``
+and ``done(ticket)`` methods is driven through the same native scheduler by
+callbacks (used to test the scheduling on hosts without a GPU).
 """
-import collections
+import ctypes
 import dataclasses
-import itertools
 import math
 import time
 from typing import Optional
@@ -33,8 +38,7 @@ from typing import Optional
 import numpy as np
 import torch
 
-RENDER_BYTES_PER_RAY = 12 + 12 + 12 + 4 + 1 + 12  # org, dir, x, t, hit, normal
-QUERY_BYTES_PER_POINT = 12 + 4
+from . import _lib
 
 
 @dataclasses.dataclass
@@ -49,8 +53,23 @@ class RenderRequest:
     fov: float = 30.0
     num_steps: int = 64
 
+    def native(self, trace_params=None):
+        r = _lib.ServeRequest()
+        r.kind = _lib.SERVE_RENDER
+        r.model = self.model
+        r.lod = -1 if self.lod is None else int(self.lod)
+        r.width, r.height = self.width, self.height
+        r.eye[:], r.at[:], r.up[:] = [float(v) for v in self.eye], [float(v) for v in self.at], \
+            [float(v) for v in self.up]
+        r.fov_deg = float(self.fov)
+        if trace_params is not None:
+            r.trace = trace_params
+        r.trace.num_steps = int(self.num_steps)
+        return r
+
     def nbytes(self):
-        return self.width * self.height * RENDER_BYTES_PER_RAY + 64
+        """Device bytes the server's pool holds for this request."""
+        return int(_lib.load().nglod_serve_request_bytes(ctypes.byref(self.native())))
 
     def units(self):
         return self.width * self.height
@@ -62,8 +81,18 @@ class QueryRequest:
     points: torch.Tensor
     lod: Optional[int] = None
 
+    def native(self, points_ptr=None):
+        r = _lib.ServeRequest()
+        r.kind = _lib.SERVE_QUERY
+        r.model = self.model
+        r.lod = -1 if self.lod is None else int(self.lod)
+        r.n = int(self.points.shape[0])
+        # any non-null address sizes the request; submit passes the real one
+        r.points = points_ptr if points_ptr is not None else (self.points.data_ptr() or 16)
+        return r
+
     def nbytes(self):
-        return self.points.shape[0] * QUERY_BYTES_PER_POINT + 64
+        return int(_lib.load().nglod_serve_request_bytes(ctypes.byref(self.native())))
 
     def units(self):
         return self.points.shape[0]
@@ -76,76 +105,100 @@ class Ticket:
     t_arrival: float
     t_admit: float = math.nan
     t_done: float = math.nan
-    stream: object = None
+    status: int = 0
+    error: Optional[str] = None
     handle: object = None
     result: object = None
+    inputs: object = None
+    region: Optional[tuple] = None  # (offset, bytes) of its pool region while admitted
 
     @property
     def latency_ms(self):
         return (self.t_done - self.t_arrival) * 1e3
 
 
+class _DeviceArray:
+    """__cuda_array_interface__ view of a finished result in the server's pool."""
+
+    def __init__(self, ptr, shape, typestr):
+        self.__cuda_array_interface__ = {"shape": tuple(shape), "typestr": typestr, "data": (int(ptr), False),
+                                         "version": 3, "strides": None, "stream": None}
+
+
+def _pool_tensor(ptr, shape, typestr, device):
+    return torch.as_tensor(_DeviceArray(ptr, shape, typestr), device=device).clone()
+
+
 class CudaExecutor:
-    """Launches requests on CUDA streams with the nglod_gb300 kernels."""
+    """Resident models (``OctreeSDF`` float32 or ``Bf16OctreeSDF``) on one
+    device, run by the library's kernels; ``num_streams`` slots."""
 
     def __init__(self, models, device, num_streams, tracer_args=None):
         from .options import default_args
-        from .tracer import SphereTracer
         self.models = models
-        self.device = device
-        self.streams = [torch.cuda.Stream(device=device) for _ in range(num_streams)]
+        self.device = torch.device(device)
+        self.streams = [None] * num_streams
         self.tracer_args = tracer_args or default_args()
 
-        self._tracer_cls = SphereTracer
+    def trace_params(self):
+        a = self.tracer_args
+        p = _lib.TraceParams()
+        p.num_steps = int(a.num_steps)
+        p.min_dis = float(np.float32(a.min_dis))
+        p.osc_dis = float(np.float32(a.min_dis * 3))
+        p.step_size = float(np.float32(a.step_size))
+        p.far_clip = float(np.float32(a.camera_clamp[1]))
+        p.lod = -1
+        p.want_normals = 1
+        return p
 
-    def launch(self, ticket, stream_index):
-        from . import _lib
-        req = ticket.request
-        s = self.streams[stream_index]
-        model = self.models[req.model]
-        with torch.cuda.stream(s):
-            if isinstance(req, RenderRequest):
-                n = req.width * req.height
-                org = torch.empty(n, 3, device=self.device)
-                dr = torch.empty(n, 3, device=self.device)
-                e = np.asarray(req.eye, np.float32)
-                a = np.asarray(req.at, np.float32)
-                u = np.asarray(req.up, np.float32)
-                _lib.check(_lib.load().nglod_camera_rays(e.ctypes.data_as(_lib.ctypes.c_void_p),
-                                                         a.ctypes.data_as(_lib.ctypes.c_void_p),
-                                                         u.ctypes.data_as(_lib.ctypes.c_void_p), req.fov, req.width,
-                                                         req.height, _lib.ptr(org), _lib.ptr(dr),
-                                                         _lib.ctypes.c_void_p(s.cuda_stream)), "nglod_camera_rays")
-                tracer = self._tracer_cls(self.tracer_args, num_steps=req.num_steps)
-                old = model.lod
-                model.lod = req.lod
-                rb = tracer(model, org, dr)
-                model.lod = old
-                ticket.result = rb
+    def start(self, config):
+        from .bf16 import Bf16OctreeSDF
+        lib = _lib.load()
+        h = ctypes.c_void_p()
+        with torch.cuda.device(self.device):
+            _lib.check(lib.nglod_serve_start(ctypes.byref(config), ctypes.byref(h)), "nglod_serve_start")
+        keep = []
+        for m in self.models:
+            mid = ctypes.c_int32()
+            if isinstance(m, Bf16OctreeSDF):
+                st = lib.nglod_serve_add_model_bf16(h, ctypes.byref(m._m), ctypes.byref(mid))
             else:
-                pts = req.points
-                if not pts.is_cuda:
-                    pts = pts.to(self.device, non_blocking=True)
-                if hasattr(model, "tiles"):  # BF16 form
-                    out = model.sdf(pts, lod=req.lod)
-                else:
-                    with torch.no_grad():
-                        out = model.sdf(pts, lod=req.lod)
-                ticket.result = out
-            ev = torch.cuda.Event()
-            ev.record(s)
-        ticket.handle = ev
+                dm = m.dense_model()
+                keep.append(dm)
+                st = lib.nglod_serve_add_model_f32(h, ctypes.byref(dm), ctypes.byref(mid))
+            if st != 0:
+                lib.nglod_serve_destroy(h)
+                _lib.check(st, "nglod_serve_add_model")
+        return h, keep
 
-    def done(self, ticket):
-        return ticket.handle.query()
+    def prepare(self, request):
+        """(native request, tensors to keep alive until completion)."""
+        if isinstance(request, RenderRequest):
+            return request.native(self.trace_params()), None
+        pts = request.points
+        if not pts.is_cuda or pts.device != self.device:
+            pts = pts.to(self.device, non_blocking=True)
+        pts = pts.detach().float().contiguous()
+        r = request.native(pts.data_ptr() or 16)
+        r.has_ready_stream = 1
+        r.ready_stream = torch.cuda.current_stream(self.device).cuda_stream
+        return r, pts
 
-    def wait(self, ticket, timeout):
-        t0 = time.monotonic()
-        while not ticket.handle.query():
-            if time.monotonic() - t0 > timeout:
-                return False
-            time.sleep(1e-4)
-        return True
+    def collect(self, res, request):
+        n, dev = res.units, self.device
+        if isinstance(request, RenderRequest):
+            from .tracer import RenderBuffer
+            return RenderBuffer(x=_pool_tensor(res.x, (n, 3), "<f4", dev),
+                                depth=_pool_tensor(res.t, (n, 1), "<f4", dev),
+                                hit=_pool_tensor(res.hit, (n,), "|u1", dev).view(torch.bool),
+                                normal=_pool_tensor(res.normal, (n, 3), "<f4", dev))
+        if n == 0:
+            return torch.empty(0, 1, device=dev)
+        return _pool_tensor(res.sdf, (n, 1), "<f4", dev)
+
+    def release_stream(self):
+        return torch.cuda.current_stream(self.device).cuda_stream
 
 
 class Server:
@@ -153,24 +206,66 @@ class Server:
         self.ex = executor
         self.budget = int(hbm_budget_bytes)
         self.num_streams = num_streams or len(getattr(executor, "streams", [None] * 8))
-        self.pending = collections.deque()
-        self.running = {}
-        self.free_streams = list(range(self.num_streams))
         self.finished = []
-        self.used = 0
-        self.peak_used = 0
-        self.max_concurrent = 0
-        self._ids = itertools.count()
+        self._live = {}       # native ticket -> Ticket, submitted and not yet polled
+        self._incoming = None  # the Ticket being submitted (launch callbacks may see it first)
         self._t_first = None
         self._t_last = None
+        self._lib = _lib.load()
+        cfg = _lib.ServeConfig(self.budget, self.num_streams, 0)
+        self._native = isinstance(executor, CudaExecutor)
+        self._keep = []
+        if self._native:
+            self._h, self._keep = executor.start(cfg)
+        else:
+            self._h = ctypes.c_void_p()
+            self._cb = (_lib.SERVE_LAUNCH_FN(self._launch_cb), _lib.SERVE_QUERY_FN(self._query_cb))
+            exs = _lib.ServeExecutor(None, *self._cb)
+            _lib.check(self._lib.nglod_serve_start_custom(ctypes.byref(cfg), ctypes.byref(exs), ctypes.byref(self._h)),
+                       "nglod_serve_start_custom")
+
+    # -- callbacks of a non-CUDA executor ----------------------------------------
+    def _ticket(self, rid):
+        tk = self._live.get(rid)
+        if tk is None:
+            tk = self._incoming
+            tk.rid = rid
+        return tk
+
+    def _launch_cb(self, ctx, rid, slot, req, region, nbytes):
+        try:
+            tk = self._ticket(rid)
+            tk.region = (region, nbytes)
+            self.ex.launch(tk, slot)
+            return 0
+        except Exception:  # noqa: BLE001 - reported as a failed request
+            return -1
+
+    def _query_cb(self, ctx, rid, slot):
+        try:
+            return 1 if self.ex.done(self._ticket(rid)) else 0
+        except Exception:  # noqa: BLE001
+            return -1
 
     # -- submission -------------------------------------------------------------
     def submit(self, request, t_arrival=None):
-        if request.nbytes() > self.budget:
-            raise ValueError(f"request needs {request.nbytes()} B, more than the whole budget {self.budget} B")
         t = time.monotonic() if t_arrival is None else t_arrival
-        tk = Ticket(next(self._ids), request, t)
-        self.pending.append(tk)
+        if self._native:
+            req, inputs = self.ex.prepare(request)
+        else:
+            req, inputs = request.native(), None
+        tk = Ticket(-1, request, t, inputs=inputs)
+        rid = ctypes.c_int64(-1)
+        self._incoming = tk
+        try:
+            st = self._lib.nglod_serve_submit(self._h, ctypes.byref(req), float(t), ctypes.byref(rid))
+        finally:
+            self._incoming = None
+        if st == -4:
+            raise ValueError(f"request needs {request.nbytes()} B, more than the whole budget {self.budget} B")
+        _lib.check(st, "nglod_serve_submit")
+        tk.rid = rid.value
+        self._live[tk.rid] = tk
         if self._t_first is None:
             self._t_first = t
         return tk
@@ -178,34 +273,47 @@ class Server:
     # -- progress ---------------------------------------------------------------
     def poll(self):
         """Retire finished requests, admit waiting ones; returns newly finished tickets."""
-        now = time.monotonic()
         done = []
-        for rid, (tk, si) in list(self.running.items()):
-            if self.ex.done(tk):
-                tk.t_done = now
-                self.used -= tk.request.nbytes()
-                self.free_streams.append(si)
-                del self.running[rid]
+        buf = (_lib.ServeResult * 64)()
+        cnt = ctypes.c_int32()
+        while True:
+            _lib.check(self._lib.nglod_serve_poll(self._h, buf, 64, ctypes.byref(cnt)), "nglod_serve_poll")
+            for res in buf[:cnt.value]:
+                tk = self._live.pop(res.ticket)
+                tk.t_admit, tk.t_done, tk.status = res.t_admit, res.t_done, res.status
+                if res.status == 0:
+                    if self._native:
+                        tk.result = self.ex.collect(res, tk.request)
+                else:
+                    tk.error = _lib.STATUS.get(res.status, str(res.status))
+                tk.inputs = None
+                if self._native:
+                    st = self._lib.nglod_serve_release(self._h, res.ticket, 1,
+                                                       ctypes.c_void_p(self.ex.release_stream()))
+                else:
+                    st = self._lib.nglod_serve_release(self._h, res.ticket, 0, None)
+                _lib.check(st, "nglod_serve_release")
                 done.append(tk)
                 self.finished.append(tk)
-                self._t_last = now
-        while self.pending and self.free_streams:
-            tk = self.pending[0]
-            need = tk.request.nbytes()
-            if self.used + need > self.budget:
-                break
-            self.pending.popleft()
-            si = self.free_streams.pop(0)
-            tk.t_admit = time.monotonic()
-            self.used += need
-            self.peak_used = max(self.peak_used, self.used)
-            self.ex.launch(tk, si)
-            self.running[tk.rid] = (tk, si)
-            self.max_concurrent = max(self.max_concurrent, len(self.running))
-        return done
+                self._t_last = tk.t_done
+            if cnt.value < 64:
+                return done
+
+    def info(self):
+        i = _lib.ServeInfo()
+        _lib.check(self._lib.nglod_serve_get_info(self._h, ctypes.byref(i)), "nglod_serve_get_info")
+        return {f[0]: getattr(i, f[0]) for f in i._fields_}
+
+    @property
+    def peak_used(self):
+        return self.info()["peak_used_bytes"]
+
+    @property
+    def max_concurrent(self):
+        return self.info()["max_concurrent"]
 
     def idle(self):
-        return not self.pending and not self.running
+        return not self._live
 
     def drain(self, timeout=60.0):
         t0 = time.monotonic()
@@ -219,14 +327,23 @@ class Server:
     def stop(self, timeout=10.0):
         """Bounded shutdown: waits up to `timeout` for running requests, drops
         the waiting ones, returns (finished, unfinished_running, dropped)."""
-        dropped = list(self.pending)
-        self.pending.clear()
-        t0 = time.monotonic()
-        for rid, (tk, _) in list(self.running.items()):
-            left = max(0.0, timeout - (time.monotonic() - t0))
-            self.ex.wait(tk, left)
+        unfinished, dropped = ctypes.c_int32(), ctypes.c_int32()
+        _lib.check(self._lib.nglod_serve_stop(self._h, float(timeout), ctypes.byref(unfinished), ctypes.byref(dropped)),
+                   "nglod_serve_stop")
         self.poll()
-        return len(self.finished), len(self.running), len(dropped)
+        return len(self.finished), unfinished.value, dropped.value
+
+    def close(self):
+        """Waits for the server's streams and frees its pool (nglod_serve_destroy)."""
+        if getattr(self, "_h", None) and self._h.value:
+            h, self._h = self._h, ctypes.c_void_p()
+            _lib.check(self._lib.nglod_serve_destroy(h), "nglod_serve_destroy")
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # noqa: BLE001 - interpreter shutdown
+            pass
 
     # -- statistics -------------------------------------------------------------
     def stats(self):
@@ -240,12 +357,14 @@ class Server:
             key = f"render_{r.width}x{r.height}" if isinstance(r, RenderRequest) else "query"
             by_kind.setdefault(key, []).append(t.latency_ms)
         pct = lambda a, q: float(np.percentile(a, q)) if len(a) else None
+        info = self.info()
         return {
             "requests": len(self.finished),
+            "failed": sum(1 for t in self.finished if t.status != 0),
             "p50_ms": pct(lat, 50), "p99_ms": pct(lat, 99), "max_ms": float(lat.max()) if len(lat) else None,
             "rays_per_s": rays / span if span > 0 else None, "queries_per_s": pts / span if span > 0 else None,
-            "span_s": span, "peak_budget_bytes": self.peak_used, "budget_bytes": self.budget,
-            "max_concurrent": self.max_concurrent,
+            "span_s": span, "peak_budget_bytes": info["peak_used_bytes"], "budget_bytes": self.budget,
+            "max_concurrent": info["max_concurrent"],
             "by_kind": {k: {"n": len(v), "p50_ms": pct(v, 50), "p99_ms": pct(v, 99)} for k, v in by_kind.items()},
         }
 

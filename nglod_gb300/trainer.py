@@ -95,3 +95,23 @@ def step_geometry(net, optimizer, pts, gts, loss_lods=None):
     optimizer.step()
     with torch.no_grad():
         return sum(((preds[l].double() - gts.double()) ** 2).sum() for l in loss_lods) / pts.shape[0]
+
+
+def fit(net, batches, steps, lr=1e-3, loss_lods=None, seed=0, log_every=500):
+    """``steps`` calls of step_geometry with a FusedAdam(lr) optimizer,
+    cycling through ``batches`` (device (pts, gts) pairs), each batch in a
+    fresh random order (a device permutation from ``seed``).  Returns the
+    optimizer and the losses of every ``log_every``-th and of the last step."""
+    net.train()
+    opt = FusedAdam(net.parameters(), lr=lr)
+    dev = batches[0][0].device
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(seed)
+    losses = []
+    for it in range(steps):
+        xb, gb = batches[it % len(batches)]
+        perm = torch.randperm(xb.shape[0], device=dev, generator=gen)
+        l = step_geometry(net, opt, xb[perm], gb[perm], loss_lods)
+        if it % log_every == 0 or it == steps - 1:
+            losses.append(float(l.item()))
+    return opt, losses

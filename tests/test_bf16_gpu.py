@@ -133,3 +133,23 @@ def test_bf16_trace_matches_fp32_trace_semantics(nets):
     assert r16.depth[0, 0].item() == 0.0 and torch.equal(r16.x[1], ro[1])
     assert (r16.normal[~r16.hit] == 0).all()
     assert abs(r16.depth[2, 0].item() - r32.depth[2, 0].item()) < 5e-3
+
+
+@pytest.mark.parametrize("n,chunk", [(0, 1000), (1, 1000), (9999, 1000), (300_001, 65_536), (1_048_576, 1 << 20)])
+def test_host_memory_queries_equal_device_queries(nets, n, chunk):
+    """sdf_host (host points in, host distances out, chunks pipelined on three
+    streams) gives bitwise the device path's values, BF16 and float32 forms."""
+    net, bnet, _, _, _ = nets
+    dev = net.features[0].fm.device
+    x = (torch.rand(n, 3) * 2.2 - 1.1).pin_memory()
+    got16 = bnet.sdf_host(x, lod=4, chunk=chunk)
+    got32 = net.sdf_host(x, lod=3, chunk=chunk)
+    torch.cuda.synchronize()
+    bnet.check_status()
+    assert got16.shape == (n, 1) and got32.shape == (n, 1)
+    assert torch.equal(got16, bnet.sdf(x.to(dev), lod=4).cpu())
+    with torch.no_grad():
+        assert torch.equal(got32, net.sdf(x.to(dev), lod=3).cpu())
+    if n:
+        with pytest.raises(RuntimeError, match="CPU tensor"):
+            bnet.sdf_host(x.to(dev))

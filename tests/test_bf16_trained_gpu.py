@@ -1,0 +1,73 @@
+"""BF16 form on trained weights: the network of 2,000 training steps from
+seed 1 (batch 524,288 of the 16-sphere union, L2 over LOD 0..4, Adam 1e-3,
+trained by this library's own forward/backward kernels), then the BF16
+form's error against the FP64 oracle per LOD on half-uniform / half
+near-surface points, and its traced depth against the FP64 oracle trace."""
+import numpy as np
+import pytest
+import torch
+
+import nglod_gb300 as ng
+from nglod_gb300 import synthetic, trainer
+from nglod_gb300.bf16 import Bf16OctreeSDF
+from nglod_gb300.options import default_args
+from oracle import cref, dense
+from tests.helpers import oracle_model
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def trained(cuda):
+    c, r = synthetic.sphere_union(1)
+    torch.manual_seed(1)
+    net = ng.OctreeSDF(default_args(num_lods=5, base_lod=2)).to(cuda)
+    pool = [synthetic.training_batch(524_288, c, r, seed=100 + k) for k in range(8)]
+    pool = [(a.to(cuda), b.to(cuda)) for a, b in pool]
+    _, losses = trainer.fit(net, pool, 2000, lr=1e-3, seed=5)
+    assert losses[-1] < 0.05 * losses[0], losses
+    net.eval()
+    return net, Bf16OctreeSDF(net), oracle_model(net, np.float64), (c, r)
+
+
+def test_bf16_error_per_lod_vs_fp64_oracle(trained):
+    net, bnet, m64, (c, r) = trained
+    x = synthetic.near_surface_query(32768, c, r, seed=1)
+    xd = x.to(net.features[0].fm.device)
+    report = {}
+    for lod in range(5):
+        ref = dense.sdf(m64, x.numpy().astype(np.float64), lod=lod)
+        got16 = bnet.sdf(xd, lod=lod).cpu().numpy().astype(np.float64)
+        with torch.no_grad():
+            got32 = net.sdf(xd, lod=lod).cpu().numpy().astype(np.float64)
+        e16 = np.abs(got16 - ref)
+        e32 = np.abs(got32 - ref)
+        report[lod] = {"bf16_max": e16.max(), "bf16_mean": e16.mean(), "f32_max": e32.max()}
+        # float32 drop-in: the reference's tolerance; BF16: bounded and stated
+        assert e32.max() < 1e-5, (lod, e32.max())
+        assert e16.max() < 2e-2 and e16.mean() < 2e-3, (lod, e16.max(), e16.mean())
+    bnet.check_status()
+    print("trained weights, error vs FP64 oracle per LOD:",
+          {k: {kk: f"{vv:.2e}" for kk, vv in v.items()} for k, v in report.items()})
+
+
+def test_bf16_trace_depth_vs_fp64_oracle_trained(trained):
+    """Depth of the BF16 tracer (compensated t) on the trained network against
+    the FP64 oracle trace: mean error <= 1e-3 on rays both call hits."""
+    net, bnet, m64, _ = trained
+    dev = net.features[0].fm.device
+    ro, rd = synthetic.look_at_rays(width=96, height=96)
+    rb = ng.SphereTracer(default_args(num_steps=128))(bnet, ro.to(dev), rd.to(dev))
+    bnet.check_status()
+    x, t, hit, normal = dense.sphere_trace(m64, ro.numpy().astype(np.float64), rd.numpy().astype(np.float64),
+                                           num_steps=128, aabb_fn=lambda o, d: tuple(
+                                               v.astype(np.float64) if v.dtype != bool else v
+                                               for v in cref.aabb(o.astype(np.float32), d.astype(np.float32))))
+    h = rb.hit.cpu().numpy()
+    assert hit.sum() > 1000
+    assert (h == hit).mean() > 0.995
+    both = h & hit
+    err = np.abs(rb.depth.cpu().numpy()[both] - t[both])
+    print(f"trained bf16 trace depth error vs fp64: mean {err.mean():.2e} median {np.median(err):.2e} "
+          f"p99 {np.percentile(err, 99):.2e}")
+    assert err.mean() <= 1e-3
