@@ -70,15 +70,25 @@ struct BwdArgs {
     float *gx;
 };
 
-__host__ __device__ inline int bwd_ht_floats(int H) { return kBT * (H + 1); }
-// Shared layout (floats): decoder | H tile [kBT][H+1] | IN tile [kBT][36] | g [kBT] | acc [H][37]
+// Backward tile: kBP points per tile, kBThreads threads per block.  Phase 1
+// (per point): four threads per point, each recomputing a quarter of the
+// hidden units (j = part, part+4, ...) and its share of dLoss/d(input); the
+// four partial input gradients are summed with shuffles.  Phase 2 (per
+// hidden unit): thread (j, half) reduces half of the tile's points into
+// dW0[j][:], db0[j], dw1[j]; the two halves are added in turn.
+constexpr int kBP = 64;
+constexpr int kBThreads = 256;
+static_assert(kBThreads == 4 * kBP && kBThreads == 2 * kBT, "backward tile shape");
+
+__host__ __device__ inline int bwd_ht_floats(int H) { return kBP * (H + 1); }
+// Shared layout (floats): decoder | H tile [kBP][H+1] | IN tile [kBP][36] | g [kBP] | acc [H][37]
 __host__ __device__ inline size_t bwd_decoder_smem(int H) {
     size_t f = (size_t)decoder_f4(H) * 4 + bwd_ht_floats(H);
     f = (f + 3) & ~(size_t)3;
-    return (f + kBT * 36 + kBT + (size_t)H * 37) * sizeof(float);
+    return (f + kBP * 36 + kBP + (size_t)H * 37) * sizeof(float);
 }
 
-__global__ void __launch_bounds__(kBT) sdf_bwd_decoder_kernel(const BwdArgs a) {
+__global__ void __launch_bounds__(kBThreads, 2) sdf_bwd_decoder_kernel(const BwdArgs a) {
     extern __shared__ float4 smem[];
     const int H = a.m.hidden_dim;
     const int tid = threadIdx.x;
@@ -87,19 +97,21 @@ __global__ void __launch_bounds__(kBT) sdf_bwd_decoder_kernel(const BwdArgs a) {
     size_t off = (size_t)decoder_f4(H) * 4 + bwd_ht_floats(H);
     off = (off + 3) & ~(size_t)3;
     float *INt = reinterpret_cast<float *>(smem) + off;
-    float *gt = INt + kBT * 36;
-    float *acc = gt + kBT;
+    float *gt = INt + kBP * 36;
+    float *acc = gt + kBP;
     const float *w1s = reinterpret_cast<const float *>(dec + H * kRowF4);
+    const int pl = tid >> 2, part = tid & 3;      // phase 1: point of the tile, quarter
+    const int jr = tid & (kBT - 1), half = tid / kBT;  // phase 2: hidden unit, half of the points
 
     for (int l = 0; l <= a.L; ++l) {
         if (!((a.mask >> l) & 1u)) continue;
         __syncthreads();
         stage_decoder(dec, a.m, l);
-        for (int i = tid; i < H * 37; i += kBT) acc[i] = 0.f;
+        for (int i = tid; i < H * 37; i += kBThreads) acc[i] = 0.f;
         float db1 = 0.f;
         __syncthreads();
-        for (int64_t tile = blockIdx.x; tile * kBT < a.n; tile += gridDim.x) {
-            const int64_t p = tile * kBT + tid;
+        for (int64_t tile = blockIdx.x; tile * kBP < a.n; tile += gridDim.x) {
+            const int64_t p = tile * kBP + pl;
             const bool valid = p < a.n;
             float in[36];
             float g = 0.f;
@@ -126,7 +138,7 @@ __global__ void __launch_bounds__(kBT) sdf_bwd_decoder_kernel(const BwdArgs a) {
 #pragma unroll
             for (int k = 0; k < 36; ++k) din[k] = 0.f;
 #pragma unroll 1
-            for (int j = 0; j < H; ++j) {
+            for (int j = part; j < H; j += 4) {
                 const float4 *r = dec + j * kRowF4;
                 float s0 = 0.f, s1 = 0.f;
 #pragma unroll
@@ -147,7 +159,7 @@ __global__ void __launch_bounds__(kBT) sdf_bwd_decoder_kernel(const BwdArgs a) {
                 const float pre = s0 + s1;
                 const float h = fmaxf(pre, 0.f);
                 const float dh = pre > 0.f ? g * w1s[j] : 0.f;
-                Ht[tid * (H + 1) + j] = h;
+                Ht[pl * (H + 1) + j] = h;
 #pragma unroll
                 for (int q = 0; q < kRowF4; ++q) {
                     const float4 w = r[q];
@@ -157,32 +169,39 @@ __global__ void __launch_bounds__(kBT) sdf_bwd_decoder_kernel(const BwdArgs a) {
                     din[4 * q + 3] = fmaf(dh, w.w, din[4 * q + 3]);
                 }
             }
+            // the point's four quarters are lanes 4i .. 4i+3 of one warp
+#pragma unroll
+            for (int k = 0; k < 35; ++k) {
+                din[k] += __shfl_xor_sync(0xffffffffu, din[k], 1);
+                din[k] += __shfl_xor_sync(0xffffffffu, din[k], 2);
+            }
             if (valid) {
                 float4 *o = reinterpret_cast<float4 *>(a.dfeat + ((int64_t)l * a.n + p) * kC);
 #pragma unroll
                 for (int q = 0; q < kC / 4; ++q)
-                    o[q] = make_float4(din[3 + 4 * q], din[4 + 4 * q], din[5 + 4 * q], din[6 + 4 * q]);
-                if (a.gx) {
+                    if ((q >> 1) == part)
+                        o[q] = make_float4(din[3 + 4 * q], din[4 + 4 * q], din[5 + 4 * q], din[6 + 4 * q]);
+                if (a.gx && part == 0) {
                     a.gx[3 * p] += din[0];
                     a.gx[3 * p + 1] += din[1];
                     a.gx[3 * p + 2] += din[2];
                 }
             }
-            float4 *ir = reinterpret_cast<float4 *>(INt + tid * 36);
+            float4 *ir = reinterpret_cast<float4 *>(INt + pl * 36);
 #pragma unroll
-            for (int q = 0; q < 9; ++q) ir[q] = make_float4(in[4 * q], in[4 * q + 1], in[4 * q + 2], in[4 * q + 3]);
-            gt[tid] = g;
+            for (int q = 0; q < 9; ++q)
+                if ((q & 3) == part) ir[q] = make_float4(in[4 * q], in[4 * q + 1], in[4 * q + 2], in[4 * q + 3]);
+            if (part == 0) gt[pl] = g;
             __syncthreads();
-            if (tid < H) {
-                const int j = tid;
-                const float w1j = w1s[j];
-                float r[36];
+            float r[36];
 #pragma unroll
-                for (int k = 0; k < 36; ++k) r[k] = 0.f;
-                float dw1 = 0.f;
+            for (int k = 0; k < 36; ++k) r[k] = 0.f;
+            float dw1 = 0.f;
+            if (jr < H) {
+                const float w1j = w1s[jr];
 #pragma unroll 2
-                for (int q = 0; q < kBT; ++q) {
-                    const float h = Ht[q * (H + 1) + j];
+                for (int q = half * (kBP / 2); q < (half + 1) * (kBP / 2); ++q) {
+                    const float h = Ht[q * (H + 1) + jr];
                     const float gq = gt[q];
                     const float dh = h > 0.f ? gq * w1j : 0.f;
                     dw1 = fmaf(gq, h, dw1);
@@ -196,15 +215,21 @@ __global__ void __launch_bounds__(kBT) sdf_bwd_decoder_kernel(const BwdArgs a) {
                         r[4 * k4 + 3] = fmaf(dh, v.w, r[4 * k4 + 3]);
                     }
                 }
+            }
+#pragma unroll 1
+            for (int turn = 0; turn < 2; ++turn) {
+                if (half == turn && jr < H) {
 #pragma unroll
-                for (int k = 0; k < 36; ++k) acc[j * 37 + k] += r[k];
-                acc[j * 37 + 36] += dw1;
+                    for (int k = 0; k < 36; ++k) acc[jr * 37 + k] += r[k];
+                    acc[jr * 37 + 36] += dw1;
+                }
+                __syncthreads();
             }
             if (tid < 32) {
-                float s = gt[tid] + gt[tid + 32] + gt[tid + 64] + gt[tid + 96];
+                float sg = gt[tid] + gt[tid + 32];
 #pragma unroll
-                for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-                db1 += s;
+                for (int o = 16; o > 0; o >>= 1) sg += __shfl_xor_sync(0xffffffffu, sg, o);
+                db1 += sg;
             }
             __syncthreads();
         }
@@ -228,7 +253,11 @@ __device__ __forceinline__ void red_add_v4(float *addr, float a, float b, float 
 }
 
 // Volumes below `smem_levels` are accumulated in shared memory (offsets in
-// floats given by soff[l]); the rest go straight to global memory.
+// floats given by soff[l]); the rest go straight to global memory.  A shared
+// vertex takes kSV = 33 floats: with 32 the channel-c atomics of all lanes
+// of a warp fell in bank c (32-way conflicts); with 33 lanes at different
+// vertices use different banks.
+constexpr int kSV = kC + 1;
 struct ScatterArgs {
     BwdArgs a;
     int smem_levels;
@@ -298,7 +327,7 @@ __global__ void __launch_bounds__(256) sdf_bwd_scatter_kernel(const ScatterArgs 
                 float *base = sacc + s.soff[l];
 #pragma unroll
                 for (int k = 0; k < 8; ++k) {
-                    float *dst = base + cidx[k] * kC;
+                    float *dst = base + cidx[k] * kSV;
 #pragma unroll
                     for (int c = 0; c < kC; ++c) atomicAdd(dst + c, G[c] * w[k]);
                 }
@@ -353,11 +382,14 @@ __global__ void __launch_bounds__(256) sdf_bwd_scatter_kernel(const ScatterArgs 
     }
     __syncthreads();
     for (int l = 0; l < s.smem_levels; ++l) {
-        const int nl = s.soff[l + 1] - s.soff[l];
+        const int nq = (s.soff[l + 1] - s.soff[l]) / kSV * (kC / 4);  // vertices x channel quads
         float *dst = a.g.grid[l];
         const float *src = sacc + s.soff[l];
-        for (int i = threadIdx.x * 4; i < nl; i += blockDim.x * 4)
-            red_add_v4(dst + i, src[i], src[i + 1], src[i + 2], src[i + 3]);
+        for (int i = threadIdx.x; i < nq; i += blockDim.x) {
+            const int v = i / (kC / 4), c = 4 * (i % (kC / 4));
+            const float *r = src + v * kSV + c;
+            red_add_v4(dst + (size_t)v * kC + c, r[0], r[1], r[2], r[3]);
+        }
     }
 }
 
@@ -453,9 +485,9 @@ extern "C" int nglod_sdf_bwd(const nglod_dense_model *model, const float *x, int
 
     const size_t smem1 = bwd_decoder_smem(model->hidden_dim);
     NGLOD_TRY(prepare_smem(sdf_bwd_decoder_kernel, smem1));
-    const int64_t tiles = (n + kBT - 1) / kBT;
-    const int64_t cap1 = resident_blocks(sdf_bwd_decoder_kernel, kBT, smem1);
-    sdf_bwd_decoder_kernel<<<(int)(tiles < cap1 ? tiles : cap1), kBT, smem1, (cudaStream_t)stream>>>(a);
+    const int64_t tiles = (n + kBP - 1) / kBP;
+    const int64_t cap1 = resident_blocks(sdf_bwd_decoder_kernel, kBThreads, smem1);
+    sdf_bwd_decoder_kernel<<<(int)(tiles < cap1 ? tiles : cap1), kBThreads, smem1, (cudaStream_t)stream>>>(a);
     NGLOD_TRY(launch_status("nglod_sdf_bwd (decoder)"));
 
     ScatterArgs s;
@@ -465,7 +497,7 @@ extern "C" int nglod_sdf_bwd(const nglod_dense_model *model, const float *x, int
     const int budget = 112 * 1024 / (int)sizeof(float);  // leave room for two blocks per SM
     for (int l = 0; l <= L; ++l) {
         const int side = (1 << (l + model->base_lod)) + 1;
-        const int cnt = side * side * side * kC;
+        const int cnt = side * side * side * kSV;
         if (s.soff[l] + cnt > budget) break;
         s.soff[l + 1] = s.soff[l] + cnt;
         s.smem_levels = l + 1;
