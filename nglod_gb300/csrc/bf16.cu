@@ -1,6 +1,7 @@
-// BF16 form of the dense path: bf16 channel-last feature volumes gathered by
-// four lanes per point for point queries and two for the tracer (each lane
-// owns 8 or 16 of the 32 channels of every corner, 16-byte loads), the LOD sum kept in fp32 and written as one
+// BF16 form of the dense path: bf16 channel-last feature volumes gathered
+// with 16-byte loads (point queries: each lane computes its own point's
+// corner offsets and weights and four lanes per point load the corners, 8
+// channels each; the tracer: two lanes per point, 16 channels each), the LOD sum kept in fp32 and written as one
 // row of a bf16 tile in shared memory, and the decoder's 35 -> 128 layer run
 // by tcgen05.mma on 128-point tiles with the accumulator in tensor memory.
 // b0, ReLU and the 128 -> 1 layer are an fp32 epilogue on the TMEM rows.
@@ -42,6 +43,124 @@ __device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
     return *reinterpret_cast<const uint32_t *>(&h);
 }
 
+// Corner set of one point in one bf16 volume (s vertices per side) with
+// PyTorch grid_sample arithmetic (align_corners, border clamp): the vertex
+// index of corner 0 in bits 0..27 and whether the x / y / z neighbour
+// differs from it (not clamped) in bits 28..30; the eight trilinear weights
+// in tnw..bse order.
+__device__ __forceinline__ void corner_set(int s, float px, float py, float pz, uint32_t &packed, float (&w)[8]) {
+    const float sm1 = (float)(s - 1);
+    const float ix = fminf(sm1, fmaxf(((px + 1.f) / 2.f) * sm1, 0.f));
+    const float iy = fminf(sm1, fmaxf(((py + 1.f) / 2.f) * sm1, 0.f));
+    const float iz = fminf(sm1, fmaxf(((pz + 1.f) / 2.f) * sm1, 0.f));
+    const float x0 = floorf(ix), y0 = floorf(iy), z0 = floorf(iz);
+    const float wx1 = ix - x0, wx0 = (x0 + 1.f) - ix;
+    const float wy1 = iy - y0, wy0 = (y0 + 1.f) - iy;
+    const float wz1 = iz - z0, wz0 = (z0 + 1.f) - iz;
+    const int xi = (int)x0, yi = (int)y0, zi = (int)z0;
+    // vertex index < 513^3 < 2^28 for the volumes the model check admits
+    packed = (uint32_t)((zi * s + yi) * s + xi) | ((uint32_t)(xi + 1 < s) << 28) | ((uint32_t)(yi + 1 < s) << 29) |
+             ((uint32_t)(zi + 1 < s) << 30);
+    const float wxy[4] = {wx0 * wy0, wx1 * wy0, wx0 * wy1, wx1 * wy1};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        w[k] = wxy[k] * wz0;
+        w[k + 4] = wxy[k] * wz1;
+    }
+}
+
+// Sum over LODs 0..L of the trilinear samples of the 32 points of a warp
+// (lane i owns point i's position).  Each lane computes its own point's
+// corner set once per LOD; the loads are then done by LPP lanes per point
+// (each owning 32/LPP channels, one 16-byte load per 8 channels and corner),
+// which fetch the corner set from the point's lane with shuffles.  Pass p
+// covers points p*(32/LPP) .. +32/LPP-1; acc[p] are this lane's channels
+// (part = lane % LPP) of point p*(32/LPP) + lane / LPP, in fp32: per LOD the
+// eight weighted corners are summed in order from zero with packed FMAs and
+// the sample is added to the running sum.
+template <int LPP>
+__device__ __forceinline__ void gather_warp_rows(const nglod_bf16_model &m, int L, float px, float py, float pz,
+                                                 int lane, float2 (&acc)[LPP][16 / LPP]) {
+    constexpr int kQ = 16 / LPP;  // float2 per lane per point
+    constexpr int kU = kQ / 4;    // 16-byte loads per corner
+    const unsigned FULL = 0xffffffffu;
+    const int part = lane % LPP;
+#pragma unroll
+    for (int p = 0; p < LPP; ++p)
+#pragma unroll
+        for (int c = 0; c < kQ; ++c) acc[p][c] = make_float2(0.f, 0.f);
+#pragma unroll 1
+    for (int l = 0; l <= L; ++l) {
+        const uint4 *g = static_cast<const uint4 *>(m.grid[l]);  // 4 uint4 per vertex
+        const int s = (1 << (l + m.base_lod)) + 1;
+        const int sy = s * 4, sz = s * sy;
+        uint32_t pk;
+        float w[8];
+        corner_set(s, px, py, pz, pk, w);
+#pragma unroll
+        for (int p = 0; p < LPP; ++p) {
+            const int src = p * (32 / LPP) + lane / LPP;
+            const uint32_t q = __shfl_sync(FULL, pk, src);
+            float ws[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) ws[k] = __shfl_sync(FULL, w[k], src);
+            const int o0 = (int)(q & 0x0FFFFFFFu) * 4 + part * kU;
+            const int ox = ((q >> 28) & 1u) ? 4 : 0;
+            const int oy = ((q >> 29) & 1u) ? sy : 0;
+            const int oz = ((q >> 30) & 1u) ? sz : 0;
+            const int o[8] = {o0, o0 + ox, o0 + oy, o0 + oy + ox, o0 + oz, o0 + oz + ox, o0 + oz + oy, o0 + oz + oy + ox};
+#pragma unroll
+            for (int u = 0; u < kU; ++u) {
+                uint4 v[8];
+#pragma unroll
+                for (int k = 0; k < 8; ++k) v[k] = __ldg(g + o[k] + u);
+                float2 a2[4] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f),
+                                make_float2(0.f, 0.f)};
+#pragma unroll
+                for (int k = 0; k < 8; ++k) {
+                    const float2 w2 = make_float2(ws[k], ws[k]);
+                    a2[0] = __ffma2_rn(make_float2(bf_lo(v[k].x), bf_hi(v[k].x)), w2, a2[0]);
+                    a2[1] = __ffma2_rn(make_float2(bf_lo(v[k].y), bf_hi(v[k].y)), w2, a2[1]);
+                    a2[2] = __ffma2_rn(make_float2(bf_lo(v[k].z), bf_hi(v[k].z)), w2, a2[2]);
+                    a2[3] = __ffma2_rn(make_float2(bf_lo(v[k].w), bf_hi(v[k].w)), w2, a2[3]);
+                }
+#pragma unroll
+                for (int c = 0; c < 4; ++c) acc[p][4 * u + c] = __fadd2_rn(acc[p][4 * u + c], a2[c]);
+            }
+        }
+    }
+}
+
+// Writes the warp's 32 tile rows (32w .. 32w+31): every lane its 32/LPP bf16
+// features of each pass's point, and lane i the position / bias columns
+// 32..39 of row 32w + i.
+template <int LPP>
+__device__ __forceinline__ void write_warp_rows(uint8_t *sA, int warp, int lane, const float2 (&acc)[LPP][16 / LPP],
+                                                float px, float py, float pz) {
+    constexpr int kQ = 16 / LPP;
+    const int part = lane % LPP;
+#pragma unroll
+    for (int p = 0; p < LPP; ++p) {
+        const int row = warp * 32 + p * (32 / LPP) + lane / LPP;
+#pragma unroll
+        for (int j = 0; j < kQ / 4; ++j) {
+            const uint4 f = make_uint4(pack_bf16x2(acc[p][4 * j].x, acc[p][4 * j].y),
+                                       pack_bf16x2(acc[p][4 * j + 1].x, acc[p][4 * j + 1].y),
+                                       pack_bf16x2(acc[p][4 * j + 2].x, acc[p][4 * j + 2].y),
+                                       pack_bf16x2(acc[p][4 * j + 3].x, acc[p][4 * j + 3].y));
+            *reinterpret_cast<uint4 *>(sA + tc::tile_offset(row, 2 * kQ * part + 8 * j, kKC)) = f;
+        }
+    }
+    const float hx = __bfloat162float(__float2bfloat16_rn(px));
+    const float hy = __bfloat162float(__float2bfloat16_rn(py));
+    const float hz = __bfloat162float(__float2bfloat16_rn(pz));
+    const uint4 pp = make_uint4(pack_bf16x2(hx, hy), pack_bf16x2(hz, px - hx), pack_bf16x2(py - hy, pz - hz), kOneOne);
+    *reinterpret_cast<uint4 *>(sA + tc::tile_offset(warp * 32 + lane, 32, kKC)) = pp;
+}
+
+// The tracer's gather: two lanes per point, each computing the corner set
+// itself (neighbouring rays keep the lines of a load instruction shared; the
+// tracer's own ray state leaves no registers for the warp-wide corner sets).
 // Adds this lane's 16 channels (16h .. 16h+15) of the trilinear sample of
 // one bf16 volume (s vertices per side) at p to acc; PyTorch grid_sample
 // arithmetic (align_corners, border clamp), corners in tnw..bse order.  Two
@@ -97,72 +216,12 @@ __device__ __forceinline__ void gather_bf16_half(const __nv_bfloat16 *__restrict
     }
 }
 
-// Four lanes per point, 8 channels (8q .. 8q+7) each, one 16-byte load per
-// corner: a point's 64-byte vertex is read by one load instruction, which
-// keeps the distinct cache lines per instruction low when consecutive
-// points are far apart (unsorted point queries).
-__device__ __forceinline__ void gather_bf16_quarter(const __nv_bfloat16 *__restrict__ g, int s, float px, float py,
-                                                    float pz, int q, float (&acc)[8]) {
-    const float sm1 = (float)(s - 1);
-    const float ix = fminf(sm1, fmaxf(((px + 1.f) / 2.f) * sm1, 0.f));
-    const float iy = fminf(sm1, fmaxf(((py + 1.f) / 2.f) * sm1, 0.f));
-    const float iz = fminf(sm1, fmaxf(((pz + 1.f) / 2.f) * sm1, 0.f));
-    const float x0 = floorf(ix), y0 = floorf(iy), z0 = floorf(iz);
-    const float wx1 = ix - x0, wx0 = (x0 + 1.f) - ix;
-    const float wy1 = iy - y0, wy0 = (y0 + 1.f) - iy;
-    const float wz1 = iz - z0, wz0 = (z0 + 1.f) - iz;
-    const int xi = (int)x0, yi = (int)y0, zi = (int)z0;
-    const int xj = min(xi + 1, s - 1), yj = min(yi + 1, s - 1), zj = min(zi + 1, s - 1);
-    const uint4 *base = reinterpret_cast<const uint4 *>(g) + q;  // 4 uint4 per vertex
-    const int sy = s * 4, sz = s * sy;
-    const int o0 = zi * sz + yi * sy + xi * 4;
-    const int ox = (xj - xi) * 4, oy = (yj - yi) * sy, oz = (zj - zi) * sz;
-    const int o[8] = {o0, o0 + ox, o0 + oy, o0 + oy + ox, o0 + oz, o0 + oz + ox, o0 + oz + oy, o0 + oz + oy + ox};
-    const float wxy[4] = {wx0 * wy0, wx1 * wy0, wx0 * wy1, wx1 * wy1};
-    const float w[8] = {wxy[0] * wz0, wxy[1] * wz0, wxy[2] * wz0, wxy[3] * wz0,
-                        wxy[0] * wz1, wxy[1] * wz1, wxy[2] * wz1, wxy[3] * wz1};
-    uint4 v[8];
-#pragma unroll
-    for (int k = 0; k < 8; ++k) v[k] = __ldg(base + o[k]);
-    float2 a01 = make_float2(0.f, 0.f), a23 = a01, a45 = a01, a67 = a01;
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-        const float2 w2 = make_float2(w[k], w[k]);
-        a01 = __ffma2_rn(make_float2(bf_lo(v[k].x), bf_hi(v[k].x)), w2, a01);
-        a23 = __ffma2_rn(make_float2(bf_lo(v[k].y), bf_hi(v[k].y)), w2, a23);
-        a45 = __ffma2_rn(make_float2(bf_lo(v[k].z), bf_hi(v[k].z)), w2, a45);
-        a67 = __ffma2_rn(make_float2(bf_lo(v[k].w), bf_hi(v[k].w)), w2, a67);
-    }
-    const float a[8] = {a01.x, a01.y, a23.x, a23.y, a45.x, a45.y, a67.x, a67.y};
-#pragma unroll
-    for (int c = 0; c < 8; ++c) acc[c] += a[c];
-}
-
-// Gathers all LODs 0..L of a point for one lane (LPP lanes per point; lane
-// part `part` owns channels part*32/LPP ..), summing in fp32.
-template <int LPP>
-__device__ __forceinline__ void gather_point(const nglod_bf16_model &m, int L, float px, float py, float pz, int part,
-                                             float (&acc)[32 / LPP]) {
-#pragma unroll
-    for (int c = 0; c < 32 / LPP; ++c) acc[c] = 0.f;
-#pragma unroll 1
-    for (int l = 0; l <= L; ++l) {
-        const __nv_bfloat16 *g = static_cast<const __nv_bfloat16 *>(m.grid[l]);
-        const int s = (1 << (l + m.base_lod)) + 1;
-        if constexpr (LPP == 4)
-            gather_bf16_quarter(g, s, px, py, pz, part, acc);
-        else
-            gather_bf16_half(g, s, px, py, pz, part, acc);
-    }
-}
-
-// Writes a point's tile row: this lane's 32/LPP summed features (bf16, K
-// columns from part*32/LPP) and, from part 0, the position / bias columns
-// 32..39.
-template <int LPP>
-__device__ __forceinline__ void write_tile_row(uint8_t *sA, int row, int h, const float (&acc)[32 / LPP], float px,
-                                               float py, float pz) {
-    constexpr int kCh = 32 / LPP;
+// Writes a point's tile row from one of its two lanes: this lane's 16
+// summed features (bf16, K columns 16h .. 16h+15) and, from h == 0, the
+// position / bias columns 32..39.
+__device__ __forceinline__ void write_tile_row_half(uint8_t *sA, int row, int h, const float (&acc)[16], float px,
+                                                    float py, float pz) {
+    constexpr int kCh = 16;
 #pragma unroll
     for (int j = 0; j < kCh / 8; ++j) {
         const uint4 f = make_uint4(pack_bf16x2(acc[8 * j], acc[8 * j + 1]), pack_bf16x2(acc[8 * j + 2], acc[8 * j + 3]),
@@ -264,25 +323,23 @@ __global__ void __launch_bounds__(kTP, 4) sdf_fwd_bf16_tc_kernel(const Bf16Args 
     const uint32_t sa = tc::smem_addr(sA), sb = tc::smem_addr(sB);
     const uint32_t idesc = tc::idesc_bf16_f32(kTP, kHid);
     uint32_t phase = 0;
-    // unsorted query points: four lanes per point (one load instruction per vertex)
+    // unsorted query points: four lanes per point load (one load instruction
+    // covers a point's 64-byte vertex)
     constexpr int kLPP = 4;
-    const int pp = lane / kLPP, h = lane % kLPP;
 
     for (int64_t tile = blockIdx.x; tile * kTP < a.n; tile += gridDim.x) {
-        // 1. gather: warp w fills rows 32w .. 32w+31, 32/kLPP points per pass
-#pragma unroll 1
-        for (int pass = 0; pass < kLPP; ++pass) {
-            const int row = warp * 32 + pass * (32 / kLPP) + pp;
-            const int64_t gi = tile * kTP + row;
+        // 1. gather: warp w fills rows 32w .. 32w+31; lane i owns point 32w + i
+        {
+            const int64_t gi = tile * kTP + warp * 32 + lane;
             float px = 0.f, py = 0.f, pz = 0.f;
             if (gi < a.n) {
                 px = a.x[3 * gi];
                 py = a.x[3 * gi + 1];
                 pz = a.x[3 * gi + 2];
             }
-            float acc[32 / kLPP];
-            gather_point<kLPP>(a.m, a.L, px, py, pz, h, acc);
-            write_tile_row<kLPP>(sA, row, h, acc, px, py, pz);
+            float2 acc[kLPP][16 / kLPP];
+            gather_warp_rows<kLPP>(a.m, a.L, px, py, pz, lane, acc);
+            write_warp_rows<kLPP>(sA, warp, lane, acc, px, py, pz);
         }
         tc::fence_proxy_async_smem();
         __syncthreads();
@@ -385,10 +442,9 @@ __global__ void __launch_bounds__(kTP, 4) trace_bf16_tc_kernel(const Bf16TraceAr
     const uint32_t sa = tc::smem_addr(sA), sb = tc::smem_addr(sB);
     const uint32_t idesc = tc::idesc_bf16_f32(kTP, kHid);
     uint32_t mphase = 0;
-    // neighbouring rays query nearby points: two lanes per point (half the
-    // corner index / weight work; the lines of a load instruction are shared)
+    // neighbouring rays query nearby points: two lanes per point (the cache
+    // lines of a load instruction are shared by neighbouring points)
     constexpr int kLPP = 2;
-    const int pp = lane / kLPP, hh = lane % kLPP;
 
     const unsigned FULL = 0xffffffffu;
     const unsigned lt_mask = (1u << lane) - 1u;
@@ -494,11 +550,16 @@ __global__ void __launch_bounds__(kTP, 4) trace_bf16_tc_kernel(const Bf16TraceAr
         __syncthreads();
 #pragma unroll 1
         for (int pass = 0; pass < kLPP; ++pass) {
-            const int row = warp * 32 + pass * (32 / kLPP) + pp;
+            const int row = warp * 32 + pass * (32 / kLPP) + lane / kLPP;
             const float4 pt = qpts[row];
-            float acc[32 / kLPP];
-            gather_point<kLPP>(a.m, a.L, pt.x, pt.y, pt.z, hh, acc);
-            write_tile_row<kLPP>(sA, row, hh, acc, pt.x, pt.y, pt.z);
+            float acc[16];
+#pragma unroll
+            for (int c = 0; c < 16; ++c) acc[c] = 0.f;
+#pragma unroll 1
+            for (int l = 0; l <= a.L; ++l)
+                gather_bf16_half(static_cast<const __nv_bfloat16 *>(a.m.grid[l]), (1 << (l + a.m.base_lod)) + 1, pt.x,
+                                 pt.y, pt.z, lane % kLPP, acc);
+            write_tile_row_half(sA, row, lane % kLPP, acc, pt.x, pt.y, pt.z);
         }
         tc::fence_proxy_async_smem();
         __syncthreads();
