@@ -74,6 +74,14 @@ def parse():
     return p.parse_args()
 
 
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of
+# sdf_fwd_bf16_tc_kernel on this workload, from the ncu capture summarised in
+# profiles/sdf_fwd_bf16_tc_4M.md (the algorithmic bytes of a launch are
+# 67.1 MB of points and results plus 20.2 MB of bf16 volumes).
+NCU_TRAFFIC_BYTES = 70_620_416 + 5_572_352
+NCU_TRAFFIC_SOURCE = "ncu --set full capture of one launch, 4,194,304 points (profiles/sdf_fwd_bf16_tc_4M.md)"
+
+
 def peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -247,7 +255,8 @@ def run_ours(args):
     sec = ms_per_step / 1e3
     roofline = {
         "bound": "hbm", "achieved": hbm_bytes / sec / 1e9, "peak": pk["hbm_gbs"], "unit": "GB/s",
-        "frac": hbm_bytes / sec / 1e9 / pk["hbm_gbs"], "traffic": None,
+        "frac": hbm_bytes / sec / 1e9 / pk["hbm_gbs"], "traffic": NCU_TRAFFIC_BYTES,
+        "traffic_source": NCU_TRAFFIC_SOURCE, "algorithmic_bytes": hbm_bytes,
         "peak_source": f"{pk['source']} hbm_gbs (burst copy)",
         "kernel": "sdf_fwd_bf16_tc_kernel",
         "per_query": {"hbm_bytes": 16, "gathered_bytes": (LOD + 1) * 8 * 32 * 2, "tensor_flop": 2 * 35 * 128,
@@ -443,8 +452,9 @@ def bench_sparse(net, dev, flush, stream, level=7, lod=4, steps=64):
     the voxels whose centres lie within one voxel diagonal of the 16-sphere
     surface (seed 1); per frame: ray/octree traversal to level lod+2 = 6,
     first-nugget flags, sparse sphere trace (64 steps) with BF16 corner
-    features, 1920x1080.  Depth/normal maps against the dense float32
-    tracer on the same network."""
+    features and the tensor-core BF16 decoder, 1920x1080 (the same frame
+    with the float32 decoder beside it).  Depth/normal maps against the
+    dense float32 tracer on the same network."""
     import nglod_gb300 as ng
     from nglod_gb300 import spc, synthetic
     from nglod_gb300.options import default_args
@@ -458,9 +468,10 @@ def bench_sparse(net, dev, flush, stream, level=7, lod=4, steps=64):
     vox = idx[keep].int()
     t0 = time.perf_counter()
     s = spc.SPC.from_voxels(vox, level)
-    sp = SparseSDF.from_dense(net, s, precision="bf16")
+    sp = SparseSDF.from_dense(net, s, precision="bf16")  # tensor-core decoder
     torch.cuda.synchronize()
     setup_s = time.perf_counter() - t0
+    sp32 = SparseSDF.from_dense(net, s, precision="bf16", decoder="f32")
     ro, rd = synthetic.look_at_rays(width=TRACE_W, height=TRACE_H)
     ro, rd = ro.to(dev), rd.to(dev)
 
@@ -474,6 +485,9 @@ def bench_sparse(net, dev, flush, stream, level=7, lod=4, steps=64):
     ms = time_steps(frame, reps, flush, stream) / reps
     ms_trav = time_steps(lambda: spc.spc_raytrace(s.GetOctree(), s.GetPoints(), s.GetPyramid(), ro, rd, lod + 2,
                                                    prefix=s.GetPrefix()), reps, flush, stream) / reps
+    sp.check_status()
+    sp32.render(ro, rd, lod=lod, num_steps=steps)
+    ms32 = time_steps(lambda: sp32.render(ro, rd, lod=lod, num_steps=steps), reps, flush, stream) / reps
     net.lod = lod
     rb = ng.SphereTracer(default_args(num_steps=128))(net, ro, rd)
     net.lod = None
@@ -481,8 +495,9 @@ def bench_sparse(net, dev, flush, stream, level=7, lod=4, steps=64):
     cosang = (normal[both] * rb.normal[both]).sum(-1)
     return {"workload": f"octree level {level} ({int(s.GetPyramid()[0, level])} leaf voxels, {s.GetOSize()} bytes), "
                         f"frame {TRACE_W}x{TRACE_H}: traversal to level {lod + 2}, sparse trace lod {lod}, "
-                        f"{steps} steps, bf16 corner features",
+                        f"{steps} steps, bf16 corner features, tcgen05 bf16 decoder",
             "frame_ms": ms, "rays_per_s": TRACE_W * TRACE_H / (ms / 1e3), "traversal_ms": ms_trav,
+            "frame_ms_f32_decoder": ms32,
             "nuggets": int(nug.shape[0]), "setup_s": setup_s,
             "vs_dense_f32": {"hit_agreement": float((hit == rb.hit).float().mean().item()),
                              "depth_median_abs": float((t[both] - rb.depth[both]).abs().median().item()),

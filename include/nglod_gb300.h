@@ -353,6 +353,9 @@ typedef struct nglod_sparse_model {
     const float *b0[NGLOD_MAX_LODS];
     const float *w1[NGLOD_MAX_LODS];
     const float *b1[NGLOD_MAX_LODS];
+    /* optional: NGLOD_BF16_TILE_BYTES decoder tiles (nglod_bf16_pack_decoder)
+     * for nglod_sparse_trace_tc; unused by the other calls */
+    const void *w0_tile[NGLOD_MAX_LODS];
 } nglod_sparse_model;
 
 /* SDF::initTrinkets + the corner export of SOL_NGLOD (SDF.cu:141-216,
@@ -390,6 +393,79 @@ int nglod_sparse_trace(const nglod_sparse_model *model, int32_t lod, int32_t num
                        const float *ray_d, int64_t n, const int32_t *nuggets, int64_t n_nuggets,
                        int32_t *ray_first, float *x, float *t, uint8_t *hit, float *normal, int64_t *work_counter,
                        nglod_stream_t stream);
+
+/* nglod_sparse_trace with bf16 corner features and the BF16 decoder of
+ * nglod_sdf_fwd_bf16: every sdf evaluation of 128 rays is one tcgen05 tile
+ * product (model->w0_tile[lod] required; feature_dim 32, hidden_dim 128).
+ * Same march, walk and normal rules as nglod_sparse_trace.  status: one
+ * device int32, nonzero if a bounded tensor-core wait gave up.  No reference
+ * counterpart (the reference decodes with cuBLAS in float32, SDF.cu:420-421). */
+int nglod_sparse_trace_tc(const nglod_sparse_model *model, int32_t lod, int32_t num_steps, const float *ray_o,
+                          const float *ray_d, int64_t n, const int32_t *nuggets, int64_t n_nuggets,
+                          int32_t *ray_first, float *x, float *t, uint8_t *hit, float *normal, int64_t *work_counter,
+                          int32_t *status, nglod_stream_t stream);
+
+/* ------------------------------------------------------------------------
+ * Shading passes on a traced render buffer (Renderer.render / shade_tensor,
+ * sdf-net/lib/renderer.py:118-223; geoutils.py:237-276).  Buffers are the
+ * tracer's: x [n][3], t [n], hit [n], normal [n][3]; images are [W][H]
+ * with ray i = w * H + h (nglod_camera_rays' order).
+ * ------------------------------------------------------------------------ */
+
+/* Lowest y of the hit points, as an order-preserving uint32 key in *out_key
+ * (device): key = bits | 0x80000000 for y >= 0, ~bits for y < 0;
+ * 0xFFFFFFFF when nothing was hit.  (renderer.py:76-86 takes the ground
+ * height from the lowest surface sample.) */
+int nglod_shade_min_hit_y(const float *x, const uint8_t *hit, int64_t n, uint32_t *out_key, nglod_stream_t stream);
+
+/* Ground plane y = min_y (renderer.py:131-150): where the plane is nearer than
+ * the surface (0 < t_plane < min(500, t)), x / t / normal become the plane's
+ * and hit is cleared; plane_hit [n] marks those rays. */
+int nglod_shade_ground(const float *ray_o, const float *ray_d, int64_t n, float min_y, float *x, float *t,
+                       uint8_t *hit, float *normal, uint8_t *plane_hit, nglod_stream_t stream);
+
+/* Shadow rays (renderer.py:152-161): origin x + 0.1 normal, direction
+ * normalize(noise + light - origin) with the caller's N(0, 0.01^2) noise
+ * [n][3]; light_host float[3] (the reference's (-1.5, 4.5, -1.5));
+ * light_hit = direction . normal > 0.  Trace them with nglod_trace(_bf16). */
+int nglod_shade_shadow_rays(const float *x, const float *normal, const float *noise, int64_t n,
+                            const float *light_host, float *shadow_o, float *shadow_d, uint8_t *light_hit,
+                            nglod_stream_t stream);
+
+/* Ambient occlusion (renderer.py:184-208) in three calls: _ao_select writes
+ * the indices of the shaded rays (hit, or plane_hit when given; plane_hit may
+ * be NULL) to idx [n] and their number to *count (host; the call waits for
+ * it; partials [n/1024 + 2], ctrl [2] int64 scratch); _ao_taps writes the 40
+ * tap points x + normal * d_i of each selected ray to taps [count*40][3],
+ * d_i = 0.025 ((i+1)/41)^1.6; the caller evaluates the sdf at the taps (any
+ * nglod_sdf_fwd* call) into r [count*40]; _ao_reduce writes ao [n] =
+ * clamp(1 - sum_i 3.5 relu(d_i - r_i - 0.0015), 0.1, 1)^2 (1 for rays not
+ * selected; a plane ray's r_i is min(r_i, d_i)). */
+int nglod_shade_ao_select(const uint8_t *hit, const uint8_t *plane_hit, int64_t n, int32_t *idx, uint32_t *partials,
+                          int64_t *ctrl, int64_t *count, nglod_stream_t stream);
+int nglod_shade_ao_taps(const float *x, const float *normal, const int32_t *idx, int64_t count, float *taps,
+                        nglod_stream_t stream);
+int nglod_shade_ao_reduce(const float *r, const int32_t *idx, int64_t count, const uint8_t *plane_hit, int64_t n,
+                          float *ao, nglod_stream_t stream);
+
+/* Matcap colour (renderer.py:262-279 with geoutils.spherical_envmap and a
+ * bilinear matcap_sampler): rgb [n][3] in [0, 1] for hit rays, 1 elsewhere.
+ * view = ray directions; texture float32 [tex_w][tex_h][3] in 0..255 (the
+ * reference's image transposed to (width, height)). */
+int nglod_shade_matcap(const float *view, const float *normal, const uint8_t *hit, int64_t n, const float *texture,
+                       int32_t tex_w, int32_t tex_h, float *rgb, nglod_stream_t stream);
+
+/* Shadow map (renderer.py:283-286): shadow [rows*cols] = shadow_hit &
+ * light_hit; map = gaussian_filter(clamp(1 - shadow + 0.9, 0, 1), sigma)
+ * (scipy.ndimage, mode 'reflect', truncate 4) over the [rows][cols] image;
+ * scratch: rows*cols floats. */
+int nglod_shade_shadow_map(const uint8_t *shadow_hit, const uint8_t *light_hit, int32_t rows, int32_t cols,
+                           float sigma, float *map, float *scratch, uint8_t *shadow, nglod_stream_t stream);
+
+/* rgb *= shadow_map (if given) * ao (if given); relative_depth (if given) =
+ * clamp(t, 0, far_clip) / far_clip (renderer.py:167). */
+int nglod_shade_compose(float *rgb, int64_t n, const float *shadow_map, const float *ao, const float *t,
+                        float far_clip, float *relative_depth, nglod_stream_t stream);
 
 /* ------------------------------------------------------------------------
  * Serving: a continuous-batching request server over resident models.

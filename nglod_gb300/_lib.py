@@ -87,6 +87,7 @@ class SparseModel(ctypes.Structure):
         ("b0", _vp * MAX_LODS),
         ("w1", _vp * MAX_LODS),
         ("b1", _vp * MAX_LODS),
+        ("w0_tile", _vp * MAX_LODS),
     ]
 
 
@@ -212,6 +213,8 @@ SIGNATURES = {
     "nglod_sparse_query": (ctypes.c_int, [ctypes.POINTER(SparseModel), _vp, _vp, _i32, _vp, _i64, _vp, _vp]),
     "nglod_sparse_trace": (ctypes.c_int, [ctypes.POINTER(SparseModel), _i32, _i32, _vp, _vp, _i64, _vp, _i64, _vp,
                                           _vp, _vp, _vp, _vp, _vp, _vp]),
+    "nglod_sparse_trace_tc": (ctypes.c_int, [ctypes.POINTER(SparseModel), _i32, _i32, _vp, _vp, _i64, _vp, _i64,
+                                             _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "nglod_bf16_pack_decoder": (ctypes.c_int, [_vp, _vp, _i32, _i32, _vp]),
     "nglod_sdf_fwd_bf16": (ctypes.c_int, [ctypes.POINTER(Bf16Model), _vp, _i64, _i32, _vp, _vp, _vp]),
     "nglod_trace_bf16": (ctypes.c_int, [ctypes.POINTER(Bf16Model), ctypes.POINTER(TraceParams), _vp, _vp, _i64,
@@ -222,6 +225,15 @@ SIGNATURES = {
     "nglod_sdf_fwd_host": (ctypes.c_int, [ctypes.POINTER(DenseModel), _vp, _i64, _i32, _vp, _i64, _vp, _vp]),
     "nglod_sdf_fwd_bf16_host": (ctypes.c_int, [ctypes.POINTER(Bf16Model), _vp, _i64, _i32, _vp, _i64, _vp, _vp,
                                                _vp]),
+    "nglod_shade_min_hit_y": (ctypes.c_int, [_vp, _vp, _i64, _vp, _vp]),
+    "nglod_shade_ground": (ctypes.c_int, [_vp, _vp, _i64, _f32, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "nglod_shade_shadow_rays": (ctypes.c_int, [_vp, _vp, _vp, _i64, _vp, _vp, _vp, _vp, _vp]),
+    "nglod_shade_ao_select": (ctypes.c_int, [_vp, _vp, _i64, _vp, _vp, _vp, ctypes.POINTER(_i64), _vp]),
+    "nglod_shade_ao_taps": (ctypes.c_int, [_vp, _vp, _vp, _i64, _vp, _vp]),
+    "nglod_shade_ao_reduce": (ctypes.c_int, [_vp, _vp, _i64, _vp, _i64, _vp, _vp]),
+    "nglod_shade_matcap": (ctypes.c_int, [_vp, _vp, _vp, _i64, _vp, _i32, _i32, _vp, _vp]),
+    "nglod_shade_shadow_map": (ctypes.c_int, [_vp, _vp, _i32, _i32, _f32, _vp, _vp, _vp, _vp]),
+    "nglod_shade_compose": (ctypes.c_int, [_vp, _i64, _vp, _vp, _vp, _f32, _vp, _vp]),
     "nglod_serve_request_bytes": (_i64, [ctypes.POINTER(ServeRequest)]),
     "nglod_serve_start": (ctypes.c_int, [ctypes.POINTER(ServeConfig), ctypes.POINTER(_vp)]),
     "nglod_serve_start_custom": (ctypes.c_int, [ctypes.POINTER(ServeConfig), ctypes.POINTER(ServeExecutor),

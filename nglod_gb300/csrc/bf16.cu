@@ -8,40 +8,9 @@
 #include <cuda_bf16.h>
 #include <string.h>
 
-#include "common.cuh"
-#include "tc_common.cuh"
+#include "bf16_tile.cuh"
 
 namespace nglod {
-
-constexpr int kTP = 128;                 // points per tile = threads per block = UMMA M
-constexpr int kHid = 128;                // hidden units = UMMA N
-constexpr int kTK = 48;                  // tile K (3 steps of 16)
-constexpr int kKC = kTK / 8;             // core-matrix columns along K
-constexpr uint32_t kTileBytes = kTP * kTK * 2;
-constexpr uint32_t kLbo = 128, kSbo = kKC * 128;
-constexpr uint32_t kWaitPolls = 1u << 22;
-
-// Dynamic shared memory: A tile | B tile | b0[128] | w1[128] | mbarrier |
-// TMEM slot | abort flag, padded so that at most four blocks share an SM
-// (four x 128 TMEM columns fill the SM's 512).
-constexpr size_t kSmemA = 0;
-constexpr size_t kSmemB = kSmemA + kTileBytes;
-constexpr size_t kSmemB0 = kSmemB + kTileBytes;
-constexpr size_t kSmemW1 = kSmemB0 + kHid * 4;
-constexpr size_t kSmemBar = kSmemW1 + kHid * 4;
-constexpr size_t kSmemSlot = kSmemBar + 8;
-constexpr size_t kSmemAbort = kSmemSlot + 4;
-constexpr size_t kSmemBytes = 48 * 1024;
-
-constexpr uint32_t kOneOne = 0x3F803F80u;  // two bf16 1.0: the b0 columns' inputs
-
-__device__ __forceinline__ float bf_lo(uint32_t v) { return __uint_as_float(v << 16); }
-__device__ __forceinline__ float bf_hi(uint32_t v) { return __uint_as_float(v & 0xffff0000u); }
-
-__device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
-    const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);  // .x = a in the low half
-    return *reinterpret_cast<const uint32_t *>(&h);
-}
 
 // Corner set of one point in one bf16 volume (s vertices per side) with
 // PyTorch grid_sample arithmetic (align_corners, border clamp): the vertex
@@ -151,11 +120,7 @@ __device__ __forceinline__ void write_warp_rows(uint8_t *sA, int warp, int lane,
             *reinterpret_cast<uint4 *>(sA + tc::tile_offset(row, 2 * kQ * part + 8 * j, kKC)) = f;
         }
     }
-    const float hx = __bfloat162float(__float2bfloat16_rn(px));
-    const float hy = __bfloat162float(__float2bfloat16_rn(py));
-    const float hz = __bfloat162float(__float2bfloat16_rn(pz));
-    const uint4 pp = make_uint4(pack_bf16x2(hx, hy), pack_bf16x2(hz, px - hx), pack_bf16x2(py - hy, pz - hz), kOneOne);
-    *reinterpret_cast<uint4 *>(sA + tc::tile_offset(warp * 32 + lane, 32, kKC)) = pp;
+    *reinterpret_cast<uint4 *>(sA + tc::tile_offset(warp * 32 + lane, 32, kKC)) = position_columns(px, py, pz);
 }
 
 // The tracer's gather: two lanes per point, each computing the corner set
@@ -229,14 +194,7 @@ __device__ __forceinline__ void write_tile_row_half(uint8_t *sA, int row, int h,
                                    pack_bf16x2(acc[8 * j + 6], acc[8 * j + 7]));
         *reinterpret_cast<uint4 *>(sA + tc::tile_offset(row, kCh * h + 8 * j, kKC)) = f;
     }
-    if (h == 0) {
-        const float hx = __bfloat162float(__float2bfloat16_rn(px));
-        const float hy = __bfloat162float(__float2bfloat16_rn(py));
-        const float hz = __bfloat162float(__float2bfloat16_rn(pz));
-        const uint4 p = make_uint4(pack_bf16x2(hx, hy), pack_bf16x2(hz, px - hx), pack_bf16x2(py - hy, pz - hz),
-                                   kOneOne);
-        *reinterpret_cast<uint4 *>(sA + tc::tile_offset(row, 32, kKC)) = p;
-    }
+    if (h == 0) *reinterpret_cast<uint4 *>(sA + tc::tile_offset(row, 32, kKC)) = position_columns(px, py, pz);
 }
 
 // Ray entry into [-1,1]^3 with sol_nglod_kernel.cu:92-150's float arithmetic
@@ -262,22 +220,6 @@ __device__ __forceinline__ bool box_entry_bf(float ox, float oy, float oz, float
         return true;
     }
     return false;
-}
-
-// Second decoder layer on this thread's TMEM row (b0 already inside the
-// product): sum_j w1[j] * relu(h[j]), two hidden units per packed FMA.
-__device__ __forceinline__ float relu_dot_w1(uint32_t taddr, const float *__restrict__ sw1) {
-    float2 acc = make_float2(0.f, 0.f);
-#pragma unroll 1
-    for (int c = 0; c < kHid / 32; ++c) {
-        float v[32];
-        tc::tmem_load32(taddr + (uint32_t)(c * 32), v);
-        const float2 *w2 = reinterpret_cast<const float2 *>(sw1 + c * 32);
-#pragma unroll
-        for (int j = 0; j < 16; ++j)
-            acc = __ffma2_rn(w2[j], make_float2(fmaxf(v[2 * j], 0.f), fmaxf(v[2 * j + 1], 0.f)), acc);
-    }
-    return acc.x + acc.y;
 }
 
 struct Bf16Args {
@@ -401,10 +343,6 @@ struct Bf16TraceArgs {
     unsigned long long *counter;
     int *status;
 };
-
-constexpr size_t kSmemQ = (kSmemAbort + 4 + 15) & ~(size_t)15;  // float4 query points [128], 16-byte aligned
-static_assert(kSmemQ % 16 == 0 && kSmemQ + kTP * 16 <= kSmemBytes, "query-point array layout");
-static_assert(kSmemBar % 8 == 0 && kSmemB % 16 == 0, "barrier / tile alignment");
 
 enum : int { bNeed = 0, bEvalInit = 1, bMarch = 2, bTap0 = 3, bDone = 9, bGone = 10 };
 

@@ -8,9 +8,8 @@
 // reference reads from its cc table (solr/sdf/sparse_grid_sample.cuh:52-107).
 #include <vector>
 
+#include "bf16_tile.cuh"
 #include "dense_common.cuh"
-#include <cuda_bf16.h>
-
 #include "scan.cuh"
 
 namespace nglod {
@@ -290,6 +289,293 @@ __global__ void __launch_bounds__(128) sparse_trace_kernel(const SparseTraceArgs
 }
 
 // ---------------------------------------------------------------------------
+// persistent sparse tracer with the BF16 tensor-core decoder
+// ---------------------------------------------------------------------------
+// This lane's 8 channels (8q .. 8q+7) of sparse_features<NGLOD_BF16>: the
+// same corners, weights and per-channel fmaf order.
+__device__ __forceinline__ void sparse_features_quarter(const nglod_sparse_model &m, int lod, int64_t g, float px,
+                                                        float py, float pz, int q, float (&f)[8]) {
+#pragma unroll
+    for (int c = 0; c < 8; ++c) f[c] = 0.f;
+    const float nx = fmaf(px, 0.5f, 0.5f), ny = fmaf(py, 0.5f, 0.5f), nz = fmaf(pz, 0.5f, 0.5f);
+    const uint4 *feats = static_cast<const uint4 *>(m.corner_feats) + q;  // 4 uint4 per corner row
+#pragma unroll 1
+    for (int lv = lod + 2; lv >= 2; --lv) {
+        if (lv != lod + 2) g = m.parent[g];
+        const float res = (float)(1 << lv);
+        const float ux = nx * res, uy = ny * res, uz = nz * res;
+        const short4 p = reinterpret_cast<const short4 *>(m.points)[g];
+        const float x0 = (float)p.x, y0 = (float)p.y, z0 = (float)p.z;
+        const float wx[2] = {(x0 + 1.f) - ux, ux - x0};
+        const float wy[2] = {(y0 + 1.f) - uy, uy - y0};
+        const float wz[2] = {(z0 + 1.f) - uz, uz - z0};
+        const int4 ca = __ldg(reinterpret_cast<const int4 *>(m.corner_idx) + 2 * g);
+        const int4 cb = __ldg(reinterpret_cast<const int4 *>(m.corner_idx) + 2 * g + 1);
+        const int ci[8] = {ca.x, ca.y, ca.z, ca.w, cb.x, cb.y, cb.z, cb.w};
+        uint4 v[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const int bx = k & 1, by = (k >> 1) & 1, bz = k >> 2;
+            v[k] = __ldg(feats + (int64_t)ci[4 * bx + 2 * by + bz] * 4);
+        }
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const int bx = k & 1, by = (k >> 1) & 1, bz = k >> 2;
+            const float w = (wz[bz] * wy[by]) * wx[bx];
+            f[0] = fmaf(bf16_lo(v[k].x), w, f[0]);
+            f[1] = fmaf(bf16_hi(v[k].x), w, f[1]);
+            f[2] = fmaf(bf16_lo(v[k].y), w, f[2]);
+            f[3] = fmaf(bf16_hi(v[k].y), w, f[3]);
+            f[4] = fmaf(bf16_lo(v[k].z), w, f[4]);
+            f[5] = fmaf(bf16_hi(v[k].z), w, f[5]);
+            f[6] = fmaf(bf16_lo(v[k].w), w, f[6]);
+            f[7] = fmaf(bf16_hi(v[k].w), w, f[7]);
+        }
+    }
+}
+
+struct SparseTcArgs {
+    SparseTraceArgs t;
+    int *status;
+};
+
+// The state machine of sparse_trace_kernel (step_kernel rules, nugget walk,
+// getNormal taps) with every sdf evaluation done for 128 rays at once: each
+// slot publishes its query point and voxel, the block gathers the 128 rows'
+// corner features into the bf16 tile, one thread issues the tcgen05 product
+// and each thread reads its row's hidden layer back for the fp32 epilogue.
+__global__ void __launch_bounds__(kTP, 4) sparse_trace_tc_kernel(const SparseTcArgs args) {
+    const SparseTraceArgs &a = args.t;
+    // the block's dynamic shared memory, as bytes (the float32 kernels of this
+    // file declare it as float4)
+    extern __shared__ __align__(1024) uint8_t smem_tc[];
+    uint8_t *sA = smem_tc + kSmemA;
+    uint8_t *sB = smem_tc + kSmemB;
+    float *sw1 = reinterpret_cast<float *>(smem_tc + kSmemW1);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem_tc + kSmemBar);
+    uint32_t *slot = reinterpret_cast<uint32_t *>(smem_tc + kSmemSlot);
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(smem_tc + kSmemAbort);
+    float4 *qpts = reinterpret_cast<float4 *>(smem_tc + kSmemQ);
+
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const unsigned lane = threadIdx.x & 31u;
+    const uint4 *bsrc = static_cast<const uint4 *>(a.m.w0_tile[a.lod]);
+    for (int i = tid; i < (int)(kTileBytes / 16); i += kTP) reinterpret_cast<uint4 *>(sB)[i] = bsrc[i];
+    sw1[tid] = a.m.w1[a.lod][tid];
+    const float b1 = a.m.b1[a.lod][0];
+    for (int i = tid; i < (kTP / 8) * 8; i += kTP) {
+        const int grp = i >> 3, r = i & 7;
+        *reinterpret_cast<uint4 *>(sA + (grp * kKC + 5) * 128 + r * 16) = make_uint4(0u, 0u, 0u, 0u);
+    }
+    if (warp == 0) tc::tmem_alloc(slot, kHid);
+    if (tid == 0) {
+        tc::mbar_init(bar, 1);
+        *abort_flag = 0;
+    }
+    tc::fence_proxy_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = *slot;
+    const uint32_t sa = tc::smem_addr(sA), sb = tc::smem_addr(sB);
+    const uint32_t idesc = tc::idesc_bf16_f32(kTP, kHid);
+    uint32_t mphase = 0;
+
+    const unsigned FULL = 0xffffffffu;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    const int level = a.lod + 2;
+    const int64_t lstart = a.m.level_start[level];
+    const float r = (float)(1.0 / (double)(1 << level));
+    const float eps = 0.001f;
+
+    int phase = sNeed, it = 0;
+    int64_t ray = 0, pidx = 0;
+    int first = -1;
+    float ox = 0.f, oy = 0.f, oz = 0.f, dx = 0.f, dy = 0.f, dz = 0.f, ivx = 0.f, ivy = 0.f, ivz = 0.f;
+    float sx = 0.f, sy = 0.f, sz = 0.f;
+    float xx = 0.f, xy = 0.f, xz = 0.f, t = 0.f, dprev = 0.f;
+    float g[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    float nx = 1.f, ny = 1.f, nz = 1.f;
+    bool cond = false, hitf = false;
+
+    auto walk = [&](float qx, float qy, float qz) {
+        bool found = false;
+        int64_t i = first;
+        do {
+            const int pid = a.nug[i].y;
+            const short4 p = reinterpret_cast<const short4 *>(a.m.points)[lstart + pid];
+            const float cx = __fmaf_rn(r, __fmaf_rn(2.f, (float)p.x, 1.f), -1.f);
+            const float cy = __fmaf_rn(r, __fmaf_rn(2.f, (float)p.y, 1.f), -1.f);
+            const float cz = __fmaf_rn(r, __fmaf_rn(2.f, (float)p.z, 1.f), -1.f);
+            const float dd = voxel_entry(qx, qy, qz, dx, dy, dz, ivx, ivy, ivz, sx, sy, sz, cx, cy, cz, r);
+            if (dd != 0.f) {
+                found = true;
+                pidx = lstart + pid;
+                cond = true;
+                if (dd > 0.f) {
+                    t = t + dd;
+                    xx = __fmaf_rn(dx, t, ox);
+                    xy = __fmaf_rn(dy, t, oy);
+                    xz = __fmaf_rn(dz, t, oz);
+                }
+            }
+            ++i;
+        } while (i < a.n_nug && a.nug[i].x == (int)ray && !found);
+        if (!found) {
+            cond = false;
+            t = 100.f;
+            xx = __fmaf_rn(dx, t, ox);
+            xy = __fmaf_rn(dy, t, oy);
+            xz = __fmaf_rn(dz, t, oz);
+        }
+    };
+
+    for (;;) {
+        for (;;) {
+            if (phase == sDone) {
+                a.x[3 * ray + 0] = xx;
+                a.x[3 * ray + 1] = xy;
+                a.x[3 * ray + 2] = xz;
+                a.t[ray] = t;
+                a.hit[ray] = hitf ? 1 : 0;
+                if (a.normal) {
+                    a.normal[3 * ray + 0] = hitf ? nx : 1.f;
+                    a.normal[3 * ray + 1] = hitf ? ny : 1.f;
+                    a.normal[3 * ray + 2] = hitf ? nz : 1.f;
+                }
+                phase = sNeed;
+            }
+            const unsigned need = __ballot_sync(FULL, phase == sNeed);
+            if (need == 0u) break;
+            const int leader = __ffs(need) - 1;
+            unsigned long long base = 0ull;
+            if ((int)lane == leader) base = atomicAdd(a.counter, (unsigned long long)__popc(need));
+            base = __shfl_sync(FULL, base, leader);
+            if (phase == sNeed) {
+                const unsigned long long rr = base + (unsigned long long)__popc(need & lt_mask);
+                if (rr >= (unsigned long long)a.n) {
+                    phase = sGone;
+                    continue;
+                }
+                ray = (int64_t)rr;
+                ox = a.ray_o[3 * ray];
+                oy = a.ray_o[3 * ray + 1];
+                oz = a.ray_o[3 * ray + 2];
+                dx = a.ray_d[3 * ray];
+                dy = a.ray_d[3 * ray + 1];
+                dz = a.ray_d[3 * ray + 2];
+                xx = ox;
+                xy = oy;
+                xz = oz;
+                t = 0.f;
+                dprev = 0.f;
+                it = 0;
+                cond = false;
+                hitf = false;
+                first = a.ray_first[ray];
+                if (first < 0) {
+                    phase = sDone;
+                    continue;
+                }
+                ivx = __fdiv_rn(1.f, dx);
+                ivy = __fdiv_rn(1.f, dy);
+                ivz = __fdiv_rn(1.f, dz);
+                sx = signbit(dx) ? 1.f : -1.f;
+                sy = signbit(dy) ? 1.f : -1.f;
+                sz = signbit(dz) ? 1.f : -1.f;
+                walk(ox, oy, oz);
+                phase = (cond && a.num_steps > 0) ? sMarch : sDone;
+            }
+        }
+        if (__syncthreads_and(phase == sGone)) break;
+
+        float qx = xx, qy = xy, qz = xz;
+        if (phase >= sTap0 && phase < sDone) {
+            const int k = phase - sTap0;
+            const float e = (k & 1) ? -eps : eps;
+            if ((k >> 1) == 0) qx = __fadd_rn(xx, e);
+            else if ((k >> 1) == 1) qy = __fadd_rn(xy, e);
+            else qz = __fadd_rn(xz, e);
+        }
+        if (phase == sGone) qx = qy = qz = 0.f;
+        qpts[tid] = make_float4(qx, qy, qz, __int_as_float((int)(phase == sGone ? lstart : pidx)));
+        __syncthreads();
+        // gather: warp w fills rows 32w .. 32w+31, eight points per pass
+#pragma unroll 1
+        for (int pass = 0; pass < 4; ++pass) {
+            const int row = warp * 32 + pass * 8 + (int)(lane >> 2), q = (int)(lane & 3u);
+            const float4 pt = qpts[row];
+            float f[8];
+            sparse_features_quarter(a.m, a.lod, (int64_t)__float_as_int(pt.w), pt.x, pt.y, pt.z, q, f);
+            *reinterpret_cast<uint4 *>(sA + tc::tile_offset(row, 8 * q, kKC)) =
+                make_uint4(pack_bf16x2(f[0], f[1]), pack_bf16x2(f[2], f[3]), pack_bf16x2(f[4], f[5]),
+                           pack_bf16x2(f[6], f[7]));
+            if (q == 0)
+                *reinterpret_cast<uint4 *>(sA + tc::tile_offset(row, 32, kKC)) = position_columns(pt.x, pt.y, pt.z);
+        }
+        tc::fence_proxy_async_smem();
+        __syncthreads();
+        if (tid == 0) {
+            tc::fence_after_sync();
+#pragma unroll
+            for (int ks = 0; ks < kTK / 16; ++ks) {
+                const uint64_t ad = tc::smem_desc(sa + ks * 256, kLbo, kSbo);
+                const uint64_t bd = tc::smem_desc(sb + ks * 256, kLbo, kSbo);
+                tc::mma_bf16(tmem, ad, bd, idesc, ks > 0 ? 1u : 0u);
+            }
+            tc::mma_commit(bar);
+            if (!tc::mbar_wait_bounded(bar, mphase, kWaitPolls)) {
+                *abort_flag = 1;
+                atomicExch(args.status, 1);
+            }
+        }
+        __syncthreads();
+        if (*abort_flag) break;
+        mphase ^= 1u;
+        tc::fence_after_sync();
+        const float v = relu_dot_w1(tmem + ((uint32_t)(warp * 32) << 16), sw1) + b1;
+        tc::fence_before_sync();
+
+        if (phase == sMarch) {
+            // step_kernel (solr/sdf/step.cuh:48-85); thresholds compared in double
+            const float d = v;
+            t = t + d;
+            hitf = ((double)fabsf(d) < 0.0003) || ((double)fabsf(d + dprev) * 0.5 < 0.0015);
+            cond = ((double)t < 5.0) && !hitf;
+            xx = __fmaf_rn(dx, t, ox);
+            xy = __fmaf_rn(dy, t, oy);
+            xz = __fmaf_rn(dz, t, oz);
+            dprev = d;
+            ++it;
+            if (cond) walk(xx, xy, xz);
+            if (!cond || it >= a.num_steps) phase = hitf ? sTap0 : sDone;
+        } else if (phase >= sTap0 && phase < sDone) {
+            const int k = phase - sTap0;
+#pragma unroll
+            for (int i = 0; i < 6; ++i)
+                if (i == k) g[i] = v;
+            if (k == 5) {
+                const float gx = g[0] - g[1], gy = g[2] - g[3], gz = g[4] - g[5];
+                const float nrm = norm3df(gx, gy, gz);
+                nx = gx / nrm;
+                ny = gy / nrm;
+                nz = gz / nrm;
+                phase = sDone;
+            } else {
+                phase = phase + 1;
+            }
+        }
+        // the next iteration's gather overwrites the A tile only after every
+        // thread has read its TMEM row (the __syncthreads_and above)
+    }
+    if (*abort_flag && tid == 0) tc::mbar_wait_bounded(bar, mphase, kWaitPolls);  // let an in-flight MMA finish
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if (warp == 0) tc::tmem_dealloc(tmem, kHid);
+}
+
+// ---------------------------------------------------------------------------
 // point query (SDF::forward)
 // ---------------------------------------------------------------------------
 template <int DT>
@@ -563,6 +849,57 @@ extern "C" int nglod_sparse_query(const nglod_sparse_model *model, const uint8_t
                                                                                    out);
     }
     return launch_status("nglod_sparse_query");
+}
+
+extern "C" int nglod_sparse_trace_tc(const nglod_sparse_model *model, int32_t lod, int32_t num_steps,
+                                     const float *ray_o, const float *ray_d, int64_t n, const int32_t *nuggets,
+                                     int64_t n_nuggets, int32_t *ray_first, float *x, float *t, uint8_t *hit,
+                                     float *normal, int64_t *work_counter, int32_t *status, nglod_stream_t stream) {
+    NGLOD_TRY(check_sparse_model(model, lod));
+    NGLOD_REQUIRE(model->feat_dtype == NGLOD_BF16 && model->feature_dim == kC && model->hidden_dim == kHid,
+                  NGLOD_ERR_UNSUPPORTED, "tensor-core sparse trace built for bf16 corner features, C=32, H=128");
+    NGLOD_REQUIRE(model->w0_tile[lod] && aligned(model->w0_tile[lod], 16) && aligned(model->corner_feats, 16),
+                  NGLOD_ERR_ALIGN, "decoder tile %d / corner features null or not 16-byte aligned", lod);
+    NGLOD_REQUIRE(n >= 0 && n_nuggets >= 0 && num_steps >= 0, NGLOD_ERR_INVALID, "negative size");
+    // global voxel indices travel as int32 through shared memory: the level's
+    // first index plus its at most 8^level voxels must stay below 2^31
+    NGLOD_REQUIRE(lod + 2 <= 9 && model->level_start[lod + 2] + ((int64_t)1 << (3 * (lod + 2))) < ((int64_t)1 << 31),
+                  NGLOD_ERR_UNSUPPORTED, "voxel indices of level %d must fit 31 bits", lod + 2);
+    if (n == 0) return NGLOD_OK;
+    NGLOD_REQUIRE(ray_o && ray_d && ray_first && x && t && hit && work_counter && status && (nuggets || n_nuggets == 0),
+                  NGLOD_ERR_INVALID, "null pointer argument");
+    NGLOD_REQUIRE(aligned(work_counter, 8) && (n_nuggets == 0 || aligned(nuggets, 8)), NGLOD_ERR_ALIGN,
+                  "work_counter and nuggets must be 8-byte aligned");
+    cudaStream_t st = (cudaStream_t)stream;
+    NGLOD_TRY(cuda_status(cudaMemsetAsync(status, 0, sizeof(int32_t), st), "sparse trace memset"));
+    NGLOD_TRY(cuda_status(cudaMemsetAsync(ray_first, 0xff, (size_t)n * sizeof(int32_t), st), "sparse trace memset"));
+    if (n_nuggets > 0)
+        ray_first_kernel<<<sgrid(n_nuggets), 256, 0, st>>>(reinterpret_cast<const int2 *>(nuggets), n_nuggets,
+                                                           ray_first);
+    NGLOD_TRY(cuda_status(cudaMemsetAsync(work_counter, 0, sizeof(int64_t), st), "sparse trace memset"));
+    SparseTcArgs a;
+    a.t.m = *model;
+    a.t.lod = lod;
+    a.t.num_steps = num_steps;
+    a.t.ray_o = ray_o;
+    a.t.ray_d = ray_d;
+    a.t.n = n;
+    a.t.nug = reinterpret_cast<const int2 *>(nuggets);
+    a.t.n_nug = n_nuggets;
+    a.t.ray_first = ray_first;
+    a.t.x = x;
+    a.t.t = t;
+    a.t.hit = hit;
+    a.t.normal = normal;
+    a.t.counter = reinterpret_cast<unsigned long long *>(work_counter);
+    a.status = status;
+    NGLOD_TRY(cuda_status(
+        cudaFuncSetAttribute(sparse_trace_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes),
+        "cudaFuncSetAttribute"));
+    const int64_t want = (n + kTP - 1) / kTP;
+    const int64_t cap = (int64_t)num_sms() * 4;
+    sparse_trace_tc_kernel<<<(int)(want < cap ? want : cap), kTP, kSmemBytes, st>>>(a);
+    return launch_status("nglod_sparse_trace_tc");
 }
 
 extern "C" int nglod_sparse_trace(const nglod_sparse_model *model, int32_t lod, int32_t num_steps, const float *ray_o,

@@ -12,7 +12,11 @@
 LOD i lives on octree level i + 2.  Corner features are stored float32
 (``precision='fp16'`` rounds them through float16 as the reference's export
 does, ``'f32'`` keeps the dense values) or bfloat16 (``'bf16'``).  Decoder
-weights are rounded through float16 by default, like the export.
+weights are rounded through float16 by default, like the export.  With
+bfloat16 features the sphere trace decodes on the tensor cores by default
+(``decoder='tc'``: the BF16 decoder tile of the dense BF16 form,
+nglod_sparse_trace_tc); ``decoder='f32'`` keeps the reference's float32
+decoder arithmetic.
 """
 import ctypes
 
@@ -31,7 +35,12 @@ def _u(t):
 
 
 class SparseSDF:
-    def __init__(self, spc, corner_feats, corner_idx, parent, corner_counts, decoders, feat_dtype):
+    def __init__(self, spc, corner_feats, corner_idx, parent, corner_counts, decoders, feat_dtype, decoder=None):
+        if decoder is None:
+            decoder = "tc" if feat_dtype == _lib.BF16 else "f32"
+        if decoder not in ("tc", "f32") or (decoder == "tc" and feat_dtype != _lib.BF16):
+            raise ValueError("decoder must be 'f32', or 'tc' with bf16 corner features")
+        self.decoder = decoder
         self.spc = spc
         self.corner_feats = corner_feats
         self.corner_idx = corner_idx
@@ -41,11 +50,17 @@ class SparseSDF:
         self.feat_dtype = feat_dtype
         self.num_lods = len(decoders)
         self.hidden_dim = decoders[0][0].shape[0]
+        self.tiles = []
+        if decoder == "tc":
+            from .bf16 import pack_decoder_tile
+            dev = corner_feats.device
+            self.tiles = [pack_decoder_tile(w0, b0).to(dev) for w0, b0, _, _ in decoders]
+        self._status = torch.zeros(1, dtype=torch.int32, device=corner_feats.device)
         self._m = self._descriptor()
 
     # -- construction ----------------------------------------------------------
     @classmethod
-    def from_dense(cls, net, spc, precision="fp16", half_weights=True):
+    def from_dense(cls, net, spc, precision="fp16", half_weights=True, decoder=None):
         """Corner features of every occupied voxel of octree levels 2..num_lods+1
         taken from net's feature volumes, and net's decoders."""
         if precision not in ("fp16", "f32", "bf16"):
@@ -64,10 +79,10 @@ class SparseSDF:
             if half_weights:
                 ws = [w.half().float() for w in ws]
             decs.append(tuple(w.contiguous() for w in ws))
-        return cls._build(spc, vols, decs, net.base_lod, _lib.BF16 if precision == "bf16" else _lib.F32)
+        return cls._build(spc, vols, decs, net.base_lod, _lib.BF16 if precision == "bf16" else _lib.F32, decoder)
 
     @classmethod
-    def _build(cls, spc, vols, decs, base_lod, feat_dtype):
+    def _build(cls, spc, vols, decs, base_lod, feat_dtype, decoder=None):
         nl = len(vols)
         dev = spc.GetOctree().device
         level = spc.GetLevel()
@@ -102,10 +117,10 @@ class SparseSDF:
             cf = feats[:total * 32].view(total, 32).clone()
         else:
             cf = feats.view(torch.bfloat16)[:total * 32].view(total, 32).clone()
-        return cls(spc, cf, corner_idx, parent, list(counts), decs, feat_dtype)
+        return cls(spc, cf, corner_idx, parent, list(counts), decs, feat_dtype, decoder)
 
     @classmethod
-    def from_npz(cls, path, device="cuda", precision="f32"):
+    def from_npz(cls, path, device="cuda", precision="f32", decoder=None):
         """Load the reference's export (keys octree, cc, cf, w0, b0, w1, b1, pyramid)."""
         z = np.load(path)
         spc = SPC(torch.from_numpy(np.ascontiguousarray(z["octree"], dtype=np.uint8)).to(device))
@@ -127,7 +142,7 @@ class SparseSDF:
             ws[1] = ws[1].reshape(-1)
             ws[3] = ws[3].reshape(-1)
             decs.append(tuple(w.contiguous() for w in ws))
-        return cls._build(spc, vols, decs, 2, _lib.BF16 if precision == "bf16" else _lib.F32)
+        return cls._build(spc, vols, decs, 2, _lib.BF16 if precision == "bf16" else _lib.F32, decoder)
 
     def corner_coords(self, lod):
         """[count, 3] corner coordinates of LOD lod, in their stored order."""
@@ -158,7 +173,14 @@ class SparseSDF:
             m.level_start[l] = int(pyr[1, l])
         for i, (w0, b0, w1, b1) in enumerate(self.decoders):
             m.w0[i], m.b0[i], m.w1[i], m.b1[i] = w0.data_ptr(), b0.data_ptr(), w1.data_ptr(), b1.data_ptr()
+        for i, tile in enumerate(self.tiles):
+            m.w0_tile[i] = tile.data_ptr()
         return m
+
+    def check_status(self):
+        """Raises if a bounded tensor-core wait of the tensor-core trace gave up."""
+        if int(self._status.item()) != 0:
+            raise RuntimeError("nglod_sparse_trace_tc: a bounded tensor-core wait timed out")
 
     # -- evaluation ---------------------------------------------------------------
     def forward(self, x, lod):
@@ -189,9 +211,15 @@ class SparseSDF:
         normal = torch.empty(n, 3, device=dev)
         first = torch.empty(n, dtype=torch.int32, device=dev)
         counter = torch.empty(1, dtype=torch.int64, device=dev)
-        _lib.check(_lib.load().nglod_sparse_trace(self._m, lod, num_steps, _u(ray_o), _u(ray_d), n, _u(nuggets),
-                                                  nuggets.shape[0], _u(first), _u(x), _u(t), _u(hit), _u(normal),
-                                                  _u(counter), _lib.stream_ptr(dev)), "nglod_sparse_trace")
+        if self.decoder == "tc":
+            _lib.check(_lib.load().nglod_sparse_trace_tc(self._m, lod, num_steps, _u(ray_o), _u(ray_d), n,
+                                                         _u(nuggets), nuggets.shape[0], _u(first), _u(x), _u(t),
+                                                         _u(hit), _u(normal), _u(counter), _u(self._status),
+                                                         _lib.stream_ptr(dev)), "nglod_sparse_trace_tc")
+        else:
+            _lib.check(_lib.load().nglod_sparse_trace(self._m, lod, num_steps, _u(ray_o), _u(ray_d), n, _u(nuggets),
+                                                      nuggets.shape[0], _u(first), _u(x), _u(t), _u(hit), _u(normal),
+                                                      _u(counter), _lib.stream_ptr(dev)), "nglod_sparse_trace")
         return [x, t, hit, normal]
 
     def render(self, ray_o, ray_d, lod=None, num_steps=50):

@@ -95,6 +95,32 @@ def decode(dec, x, feats):
     return (h @ w1.T + b1).astype(f32)[:, 0]
 
 
+def _bf16(a):
+    """float32 -> bfloat16 (round to nearest even), returned as float32."""
+    a = np.ascontiguousarray(a, dtype=f32)
+    u = a.view(np.uint32).astype(np.uint64)
+    return (((u + 0x7FFF + ((u >> 16) & 1)) >> 16) << 16).astype(np.uint32).view(f32)
+
+
+def decode_bf16_tile(dec, x, feats):
+    """The BF16 decoder tile of the tensor-core trace (not a reference
+    computation; it restates the tile's arithmetic to check the kernel):
+    features and first-layer weights rounded to bf16, positions and b0 as
+    bf16 hi + lo, products summed in float64 (the tensor core sums in fp32),
+    ReLU and the second layer in float32."""
+    w0, b0, w1, b1 = dec
+    x = x.astype(f32)
+    f = _bf16(feats).astype(np.float64)
+    hi = _bf16(x)
+    lo = _bf16(x - hi)
+    wb = _bf16(w0).astype(np.float64)
+    b0h = _bf16(b0)
+    b0l = _bf16(b0 - b0h)
+    h = f @ wb[:, 3:].T + hi.astype(np.float64) @ wb[:, :3].T + lo.astype(np.float64) @ wb[:, :3].T
+    h = np.maximum((h + b0h.astype(np.float64) + b0l.astype(np.float64)).astype(f32), 0)
+    return (h @ w1.astype(f32).T + b1.astype(f32)).astype(f32)[:, 0]
+
+
 def _voxel_entry(q, d, inv, sgn, vc, r):
     o = (q - vc).astype(f32)
     cmax = np.abs(o).max(axis=1)
@@ -108,8 +134,11 @@ def _voxel_entry(q, d, inv, sgn, vc, r):
     return np.where(wind < 0, wind, dist).astype(f32)
 
 
-def sphere_trace(m, decs, lod, ray_o, ray_d, nuggets, num_steps=50):
-    """SDF::sphereTrace: (x [n,3], t [n,1], hit [n], normal [n,3])."""
+def sphere_trace(m, decs, lod, ray_o, ray_d, nuggets, num_steps=50, decoder=decode):
+    """SDF::sphereTrace: (x [n,3], t [n,1], hit [n], normal [n,3]).
+    ``decoder``: decode (the reference's float32 decoder) or
+    decode_bf16_tile."""
+    decode_fn = decoder
     o = ray_o.astype(f32)
     dr = ray_d.astype(f32)
     n = o.shape[0]
@@ -167,7 +196,7 @@ def sphere_trace(m, decs, lod, ray_o, ray_d, nuggets, num_steps=50):
         act = np.flatnonzero(cond)
         if act.size == 0:
             break
-        d = decode(decs[lod], x[act], features(m, lod, pidx[act], x[act]))
+        d = decode_fn(decs[lod], x[act], features(m, lod, pidx[act], x[act]))
         t[act] = (t[act] + d).astype(f32)
         h = (np.abs(d).astype(np.float64) < 0.0003) | (np.abs((d + dprev[act]).astype(f32)).astype(np.float64) * 0.5
                                                        < 0.0015)
@@ -184,8 +213,8 @@ def sphere_trace(m, decs, lod, ray_o, ray_d, nuggets, num_steps=50):
             e[k] = f32(0.001)
             xf = (x[hi] + e).astype(f32)
             xb = (x[hi] - e).astype(f32)
-            df = decode(decs[lod], xf, features(m, lod, pidx[hi], xf))
-            db = decode(decs[lod], xb, features(m, lod, pidx[hi], xb))
+            df = decode_fn(decs[lod], xf, features(m, lod, pidx[hi], xf))
+            db = decode_fn(decs[lod], xb, features(m, lod, pidx[hi], xb))
             normal[hi, k] = (df - db).astype(f32)
         nrm = np.sqrt((normal[hi].astype(np.float64) ** 2).sum(1)).astype(f32)
         normal[hi] = (normal[hi] / nrm[:, None]).astype(f32)
