@@ -462,8 +462,8 @@ int nglod_shade_matcap(const float *view, const float *normal, const uint8_t *hi
 int nglod_shade_shadow_map(const uint8_t *shadow_hit, const uint8_t *light_hit, int32_t rows, int32_t cols,
                            float sigma, float *map, float *scratch, uint8_t *shadow, nglod_stream_t stream);
 
-/* rgb *= shadow_map (if given) * ao (if given); relative_depth (if given) =
- * clamp(t, 0, far_clip) / far_clip (renderer.py:167). */
+/* rgb (if given) *= shadow_map (if given) * ao (if given); relative_depth
+ * (if given) = clamp(t, 0, far_clip) / far_clip (renderer.py:167). */
 int nglod_shade_compose(float *rgb, int64_t n, const float *shadow_map, const float *ao, const float *t,
                         float far_clip, float *relative_depth, nglod_stream_t stream);
 

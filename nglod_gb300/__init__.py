@@ -15,6 +15,7 @@ from . import autograd, sol_nglod, trainer
 from ._lib import load as load_library
 from .octree_sdf import FeatureVolume, OctreeSDF, setparam
 from .tracer import BaseTracer, PlainSphereTracer, RenderBuffer, SphereTracer
+from .renderer import Renderer
 
-__all__ = ["OctreeSDF", "FeatureVolume", "SphereTracer", "PlainSphereTracer", "BaseTracer", "RenderBuffer",
+__all__ = ["OctreeSDF", "FeatureVolume", "SphereTracer", "PlainSphereTracer", "BaseTracer", "RenderBuffer", "Renderer",
            "sol_nglod", "setparam", "load_library", "trainer", "autograd"]

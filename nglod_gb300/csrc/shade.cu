@@ -253,12 +253,14 @@ __global__ void compose_kernel(float *rgb, int64_t n, const float *__restrict__ 
                                const float *__restrict__ t, float far_clip, float *rel_depth) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        if (rgb) {
 #pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            float v = rgb[3 * i + c];
-            if (smap) v = __fmul_rn(v, smap[i]);
-            if (ao) v = __fmul_rn(v, ao[i]);
-            rgb[3 * i + c] = v;
+            for (int c = 0; c < 3; ++c) {
+                float v = rgb[3 * i + c];
+                if (smap) v = __fmul_rn(v, smap[i]);
+                if (ao) v = __fmul_rn(v, ao[i]);
+                rgb[3 * i + c] = v;
+            }
         }
         if (rel_depth) rel_depth[i] = __fdiv_rn(fminf(fmaxf(t[i], 0.f), far_clip), far_clip);
     }
@@ -403,7 +405,8 @@ extern "C" int nglod_shade_compose(float *rgb, int64_t n, const float *shadow_ma
                                    float far_clip, float *relative_depth, nglod_stream_t stream) {
     NGLOD_REQUIRE(n >= 0, NGLOD_ERR_INVALID, "n=%lld is negative", (long long)n);
     if (n == 0) return NGLOD_OK;
-    NGLOD_REQUIRE(rgb && (!relative_depth || (t && far_clip > 0.f)), NGLOD_ERR_INVALID, "bad argument");
+    NGLOD_REQUIRE((rgb || relative_depth) && (!relative_depth || (t && far_clip > 0.f)), NGLOD_ERR_INVALID,
+                  "bad argument");
     compose_kernel<<<shade_grid(n), 256, 0, (cudaStream_t)stream>>>(rgb, n, shadow_map, ao, t, far_clip,
                                                                     relative_depth);
     return launch_status("nglod_shade_compose");

@@ -20,7 +20,8 @@ DEFAULTS = dict(
     # renderer (options.py:191-232)
     sol=False, render_res=[512, 512], render_batch=0, camera_origin=[-2.8, 2.8, -2.8], camera_lookat=[0, 0, 0],
     camera_fov=30, camera_proj="persp", camera_clamp=[-5, 10], lod=None, interpolate=None, render_every=1,
-    num_steps=256, step_size=1.0, min_dis=0.0003, tracer="SphereTracer",
+    num_steps=256, step_size=1.0, min_dis=0.0003, tracer="SphereTracer", matcap_path="data/matcap/green.png",
+    ground_height=None, ao=False, shadow=False, shading_mode="matcap", perf=False,
 )
 
 

@@ -127,3 +127,21 @@ def look_at_rays(eye=(0.0, 0.0, 4.0), at=(0.0, 0.0, 0.0), width=128, height=128,
     d /= np.linalg.norm(d, axis=-1, keepdims=True)
     o = np.broadcast_to(eye, d.shape).copy()
     return torch.from_numpy(o).float(), torch.from_numpy(d).float()
+
+
+def matcap_texture(size=64):
+    """uint8 [size, size, 3] matcap image (rows = image y, as an image file
+    decodes): a lit green sphere filling the square, standing in for the
+    reference's data/matcap/green.png, which is not distributed with it."""
+    u = (np.arange(size) + 0.5) / size * 2 - 1
+    xx, yy = np.meshgrid(u, -u)  # image rows run top to bottom
+    rr = xx * xx + yy * yy
+    nz = np.sqrt(np.clip(1 - rr, 0, 1))
+    light = np.array([-0.4, 0.5, 0.77])
+    light = light / np.linalg.norm(light)
+    lam = np.clip(xx * light[0] + yy * light[1] + nz * light[2], 0, 1)
+    spec = lam ** 24
+    base = np.array([0.18, 0.62, 0.32])
+    col = base[None, None, :] * (0.15 + 0.85 * lam[..., None]) + 0.5 * spec[..., None]
+    col = np.where((rr <= 1)[..., None], col, base[None, None, :] * 0.15)
+    return np.clip(np.round(col * 255), 0, 255).astype(np.uint8)

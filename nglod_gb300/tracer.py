@@ -66,8 +66,22 @@ class RenderBuffer:
     def float(self):
         return self._apply(lambda t: t.float())
 
-    def exr_dict(self):
-        return {f.name: getattr(self, f.name) for f in fields(self) if getattr(self, f.name) is not None}
+    def reshape(self, *dims):
+        return self._apply(lambda t: t.reshape(*dims))
+
+    def transpose(self):
+        """[W, H, C] images -> [H, W, C] (RenderBuffer.py:86-88)."""
+        return self._apply(lambda t: t.permute(1, 0, 2))
+
+    def numpy(self):
+        return self._apply(lambda t: t.numpy())
+
+    def exrdict(self):
+        """The set fields, rgb renamed 'default' (RenderBuffer.py:98-104)."""
+        d = {f.name: getattr(self, f.name) for f in fields(self) if getattr(self, f.name) is not None}
+        if "rgb" in d:
+            d["default"] = d.pop("rgb")
+        return d
 
 
 class BaseTracer(object):

@@ -22,6 +22,13 @@ Fixtures:
   spc_small.npz    SPC3D octree of level 5 built from the voxels near the
                    sphere-union surface: Morton codes, octree bytes, pyramid,
                    decoded points; unique_corners of levels 2..5.
+  shade_small.npz  Renderer.shade_tensor with a ground plane, shadow rays and
+                   ambient occlusion on trace_small's network, 48x40 rays,
+                   matcap shading with nglod_gb300.synthetic.matcap_texture
+                   (served through the stubbed PIL.Image.open), shadow-ray
+                   noise from torch.manual_seed(7); torch.Tensor.cuda is made
+                   a no-op for the call (the reference moves its images to the
+                   GPU).
 """
 import os
 import sys
@@ -133,20 +140,24 @@ def dense_small(OctreeSDF, parse_options):
     np.savez_compressed(os.path.join(HERE, "dense_small.npz"), **out)
 
 
-def trace_small(OctreeSDF, SphereTracer, parse_options):
+def trace_small_net(OctreeSDF, parse_options, **extra):
     args = ref_args(parse_options, num_lods=2, base_lod=3, feature_dim=32, hidden_dim=128, num_steps=64,
-                    min_dis=0.0003, step_size=1.0, camera_clamp=[-5, 10], grad_method="finitediff")
+                    min_dis=0.0003, step_size=1.0, camera_clamp=[-5, 10], grad_method="finitediff", **extra)
     c, r = synthetic.sphere_union(1)
     torch.manual_seed(0)
     dropin = DropIn(default_args(num_lods=2, base_lod=3))
     init_from_sdf(dropin, lambda p: torch.from_numpy(synthetic.sphere_union_sdf(p.numpy(), c, r)), noise=2e-3,
                   seed=5)
     with torch.no_grad():
-        for fv in dropin.features:  # keep the fixture small: noise in channels 1-3 only
-            fv.fm[:, 4:] = 0
+        for fv in dropin.features:
+            fv.fm[:, 4:] = 0  # keep the fixtures small: noise in channels 1-3 only
     net = OctreeSDF(args)
     net.load_state_dict(dropin.state_dict())
-    net.eval()
+    return net.eval(), args
+
+
+def trace_small(OctreeSDF, SphereTracer, parse_options):
+    net, args = trace_small_net(OctreeSDF, parse_options)
     ro, rd = synthetic.look_at_rays(width=40, height=40)
     extra_o = torch.tensor([[0, 0, 0], [0.5, 0.2, -0.3], [3, 3, 3], [0, 0, 4], [1, 0, 0], [0, 2, 0],
                             [-0.2, 0.1, 1.0]], dtype=torch.float32)
@@ -168,6 +179,37 @@ def trace_small(OctreeSDF, SphereTracer, parse_options):
         out["param/" + k] = v.numpy()
     out["trace/num_steps"] = np.array(64)
     np.savez_compressed(os.path.join(HERE, "trace_small.npz"), **out)
+
+
+def shade_small(OctreeSDF, SphereTracer, parse_options):
+    import lib.renderer as R
+    W, H = 48, 40
+    net, args = trace_small_net(OctreeSDF, parse_options, render_res=[W, H], shadow=True, ao=True,
+                                ground_height=-0.7, shading_mode="matcap", matcap_path="synthetic")
+    tex = synthetic.matcap_texture(64)
+    sys.modules["PIL.Image"].open = lambda path: tex
+    R.PerfTimer = _NoTimer
+    ro, rd = synthetic.look_at_rays(eye=(1.2, 1.6, 3.2), at=(0.0, -0.2, 0.0), width=W, height=H, fov=40.0)
+    tracer = SphereTracer(args)
+    renderer = R.Renderer(tracer, args=args)
+    renderer.render_lookat = lambda net_, f=None, t=None, fov=None, camera_proj=None, device=None, mm=None: \
+        renderer.render(net_, ro, rd)
+    cuda = torch.Tensor.cuda
+    torch.Tensor.cuda = lambda self, *a, **k: self
+    try:
+        torch.manual_seed(7)
+        rb = renderer.shade_tensor(net)
+    finally:
+        torch.Tensor.cuda = cuda
+    torch.manual_seed(7)
+    noise = torch.zeros(W * H, 3).normal_(0.0, 0.01)
+    out = {"ray_o": ro.numpy(), "ray_d": rd.numpy(), "noise": noise.numpy(), "matcap": tex,
+           "ground_height": np.array(-0.7, np.float32), "width": np.array(W), "height": np.array(H)}
+    for k in ("x", "depth", "hit", "normal", "rgb", "shadow", "ao", "relative_depth"):
+        v = getattr(rb, k)
+        out[k] = v.detach().numpy().reshape(W * H, -1)
+    # the network's parameters are trace_small.npz's (same construction)
+    np.savez_compressed(os.path.join(HERE, "shade_small.npz"), **out)
 
 
 def coded_volume(s, channels=2):
@@ -236,6 +278,7 @@ def main():
     dense_small(OctreeSDF, parse_options)
     trace_small(OctreeSDF, SphereTracer, parse_options)
     spc_small(spc3d, geoutils, ref_root)
+    shade_small(OctreeSDF, SphereTracer, parse_options)
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))
