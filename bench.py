@@ -26,7 +26,9 @@ fused float32 and the plain per-step float32 tracer), ``serve`` (the
 continuous-batching server under a Poisson request stream), ``train`` (the
 training step against the reference computation in stock PyTorch ops, then
 2,000 steps and the BF16 form on the trained weights), ``sparse`` (SPC octree
-traversal + sparse BF16 trace of a 1080p frame), ``roofline``,
+traversal + sparse BF16 trace of a 1080p frame), ``shade`` (a shaded 1080p
+frame: trace, ground plane, shadow rays, ambient occlusion, matcap),
+``roofline``,
 ``cpu_baseline``, ``clocks``, ``gpu_launches``.  ``--only LEG`` runs one
 extra leg alone (for profiling).
 
@@ -69,7 +71,7 @@ def parse():
     p.add_argument("--warmup", type=int, default=10)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--no-extras", action="store_true", help="skip the trace and CPU-baseline legs")
-    p.add_argument("--only", choices=["trace", "train", "sparse", "serve"], default=None,
+    p.add_argument("--only", choices=["trace", "train", "sparse", "serve", "shade"], default=None,
                    help="run one extra leg alone (profiling); prints its JSON")
     return p.parse_args()
 
@@ -283,6 +285,7 @@ def run_ours(args):
         extras["serve"] = bench_serve(dev)
         extras["train"] = bench_train(dev, flush, stream)
         extras["sparse"] = bench_sparse(net, dev, flush, stream)
+        extras["shade"] = bench_shade(net, bnet, dev, flush, stream)
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_extras:
@@ -346,6 +349,34 @@ def bench_trace(net, bnet, dev, flush, stream):
             "bf16_vs_f32_depth_mean_abs": float(derr.mean().item()) if derr.numel() else None,
             "plain_f32_rays_per_s": n / (pms / 1e3), "plain_f32_ms": pms, "hits": hits, "kernel_launches_fused": 2,
             "bf16_over_plain_f32": (n / (ms16 / 1e3)) / (n / (pms / 1e3))}
+
+
+def bench_shade(net, bnet, dev, flush, stream):
+    """Shaded frame (Renderer.shade_tensor with a ground plane, shadow rays and
+    ambient occlusion, matcap colour): 1920x1080, 64 steps, camera (1.6, 1.4,
+    3.4) looking at (0, -0.1, 0), fov 35, for the BF16 and float32 networks;
+    the primary trace, the shadow-ray trace and 40 sdf taps per shaded pixel
+    are the bulk of it."""
+    from nglod_gb300.options import default_args
+    from nglod_gb300.renderer import Renderer
+    import nglod_gb300 as ng
+    tr = ng.SphereTracer(default_args(num_steps=TRACE_STEPS))
+    r = Renderer(tr, args=default_args(render_res=[TRACE_W, TRACE_H], shadow=True, ao=True, ground_height=-0.75))
+    f, t, fov = (1.6, 1.4, 3.4), (0.0, -0.1, 0.0), 35.0
+    out = {"workload": f"Renderer.shade_tensor {TRACE_W}x{TRACE_H}: trace ({TRACE_STEPS} steps) + ground plane + "
+                       "shadow rays + AO (40 taps) + matcap, camera (1.6, 1.4, 3.4) -> (0, -0.1, 0) fov 35"}
+    for name, m in (("bf16", bnet), ("f32", net)):
+        for _ in range(2):
+            rb = r.shade_tensor(m, f=f, t=t, fov=fov)
+        torch.cuda.synchronize()
+        reps = 5
+        ms = time_steps(lambda: r.shade_tensor(m, f=f, t=t, fov=fov), reps, flush, stream) / reps
+        out[f"{name}_frame_ms"] = ms
+        out[f"{name}_hit_fraction"] = float(rb.hit.float().mean().item())
+        out[f"{name}_shaded_fraction"] = float((rb.ao < 1).float().mean().item())
+    if hasattr(bnet, "check_status"):
+        bnet.check_status()
+    return out
 
 
 class _TorchOpsOctreeSDF(torch.nn.Module):
@@ -614,6 +645,8 @@ def run_only(args):
         out = bench_train(dev, flush, stream, steps=max(args.steps, 1), warm=max(args.warmup, 1), train_steps=0)
     elif args.only == "sparse":
         out = bench_sparse(net, dev, flush, stream)
+    elif args.only == "shade":
+        out = bench_shade(net, Bf16OctreeSDF(net), dev, flush, stream)
     else:
         out = bench_serve(dev, duration_s=2.0)
     print(json.dumps({"only": args.only, **out}), flush=True)
