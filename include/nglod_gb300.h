@@ -319,6 +319,21 @@ int nglod_spc_raytrace(const uint8_t *octree, const int16_t *points, const uint3
  * nugget i is its ray's first, else 0. */
 int nglod_spc_mark_first(const int32_t *nuggets, int64_t n, int32_t *info, nglod_stream_t stream);
 
+/* Octree from a field (the purpose of voxel_sparsify,
+ * sdf-net/lib/renderutils.py:56-73, as SOL_NGLOD.py:50 uses it):
+ * _voxel_centres writes the centres float32 [count][3] of voxels
+ * [start, start + count) of the 2^level grid over [-1, 1]^3, linear index
+ * (x * res + y) * res + z; after the caller evaluates the field there,
+ * _select_band appends the uint16 (x, y, z) of the voxels with |value| <= band
+ * to voxels[base ..], fails with NGLOD_ERR_CAPACITY past `capacity`, and
+ * returns their number in *selected (host; the call waits for it).
+ * partials: n/1024 + 2 uint32; ctrl: 3 int64.  The voxels feed
+ * nglod_spc_build.  No reference counterpart for the band rule itself. */
+int nglod_voxel_centres(int32_t level, int64_t start, int64_t count, float *out, nglod_stream_t stream);
+int nglod_select_band(const float *values, int64_t n, float band, int32_t level, int64_t start, uint16_t *voxels,
+                      int64_t base, int64_t capacity, uint32_t *partials, int64_t *ctrl, int64_t *selected,
+                      nglod_stream_t stream);
+
 /* spc_generate_primary_rays (spc_raytrace_cuda.cpp:65-121, kernel
  * spc_raytrace_cuda_kernel.cu:271-287): pinhole rays of a width x height
  * image from the 4x4 inverse view-projection matrix inv_wvp (row-major,

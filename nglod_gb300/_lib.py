@@ -206,6 +206,9 @@ SIGNATURES = {
     "nglod_spc_raytrace": (ctypes.c_int, [_vp, _vp, _vp, _vp, _i32, _i32, _vp, _vp, _i64, _vp, _vp, _i64, _vp,
                                           _vp, _vp, ctypes.POINTER(_i64), ctypes.POINTER(_i32), _vp]),
     "nglod_spc_mark_first": (ctypes.c_int, [_vp, _i64, _vp, _vp]),
+    "nglod_voxel_centres": (ctypes.c_int, [_i32, _i64, _i64, _vp, _vp]),
+    "nglod_select_band": (ctypes.c_int, [_vp, _i64, _f32, _i32, _i64, _vp, _i64, _i64, _vp, _vp,
+                                         ctypes.POINTER(_i64), _vp]),
     "nglod_spc_generate_rays": (ctypes.c_int, [_vp, _i32, _i32, _vp, _vp, _vp]),
     "nglod_sparse_build_scratch_bytes": (_i64, [_i32]),
     "nglod_sparse_build": (ctypes.c_int, [ctypes.POINTER(DenseModel), _vp, _vp, _i32, _i32, _vp, _i64, _vp, _vp,

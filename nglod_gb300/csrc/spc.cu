@@ -397,6 +397,65 @@ __global__ void __launch_bounds__(kChunk) nonzero_emit_kernel(const uint8_t *__r
     }
 }
 
+// ---------------------------------------------------------------------------
+// octree from a field: voxel centres and band selection
+// ---------------------------------------------------------------------------
+// Centres of voxels [start, start + count) of a 2^level grid in [-1, 1]^3,
+// linear index (x * res + y) * res + z.
+__global__ void voxel_centres_kernel(int level, int64_t start, int64_t count, float *out) {
+    const int64_t res = (int64_t)1 << level;
+    const float inv = 2.f / (float)res;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < count; k += stride) {
+        const int64_t v = start + k;
+        const int64_t x = v / (res * res), y = (v / res) % res, z = v % res;
+        out[3 * k] = ((float)x + 0.5f) * inv - 1.f;
+        out[3 * k + 1] = ((float)y + 0.5f) * inv - 1.f;
+        out[3 * k + 2] = ((float)z + 0.5f) * inv - 1.f;
+    }
+}
+
+__global__ void __launch_bounds__(kChunk) band_chunk_kernel(const float *__restrict__ d, const int64_t *count,
+                                                            float band, uint32_t *partials) {
+    __shared__ uint32_t s_warp[33];
+    const int64_t n = *count;
+    const int64_t nchunks = (n + kChunk - 1) / kChunk;
+    for (int64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
+        const int64_t i = c * kChunk + threadIdx.x;
+        const uint32_t f = (i < n && fabsf(d[i]) <= band) ? 1u : 0u;
+        const uint32_t s = block_sum(f, s_warp);
+        if (threadIdx.x == 0) partials[c] = s;
+    }
+}
+
+// Writes the grid coordinates (uint16 x, y, z) of the selected voxels after
+// `base` already selected ones.
+__global__ void __launch_bounds__(kChunk) band_emit_kernel(const float *__restrict__ d, const int64_t *count,
+                                                           float band, const uint32_t *__restrict__ partials,
+                                                           int level, int64_t start, uint16_t *out, int64_t base,
+                                                           int64_t cap, int64_t *status) {
+    __shared__ uint32_t s_warp[33];
+    const int64_t n = *count;
+    const int64_t res = (int64_t)1 << level;
+    const int64_t nchunks = (n + kChunk - 1) / kChunk;
+    for (int64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
+        const int64_t i = c * kChunk + threadIdx.x;
+        const uint32_t f = (i < n && fabsf(d[i]) <= band) ? 1u : 0u;
+        uint32_t tot;
+        const uint32_t ex = block_exclusive_scan(f, s_warp, &tot);
+        if (!f) continue;
+        const int64_t pos = base + (int64_t)partials[c] + ex;
+        if (pos >= cap) {
+            *status = 1;
+            continue;
+        }
+        const int64_t v = start + i;
+        out[3 * pos] = (uint16_t)(v / (res * res));
+        out[3 * pos + 1] = (uint16_t)((v / res) % res);
+        out[3 * pos + 2] = (uint16_t)(v % res);
+    }
+}
+
 inline int grid_for(int64_t chunks) {
     const int64_t cap = (int64_t)num_sms() * 2;
     if (chunks < 1) chunks = 1;
@@ -678,4 +737,40 @@ extern "C" int nglod_spc_prefix(const uint8_t *octree, int64_t osize, uint32_t *
     scan_chunk_counts_kernel<<<1, kChunk, 0, s>>>(partials, ctrl, ctrl + 1, INT64_MAX, nullptr);
     popc_prefix_kernel<<<grid_for(chunks), kChunk, 0, s>>>(octree, osize, ctrl, partials, prefix);
     return launch_status("nglod_spc_prefix");
+}
+
+extern "C" int nglod_voxel_centres(int32_t level, int64_t start, int64_t count, float *out, nglod_stream_t stream) {
+    NGLOD_REQUIRE(level >= 1 && level <= 15 && start >= 0 && count >= 0 &&
+                      start + count <= ((int64_t)1 << (3 * level)),
+                  NGLOD_ERR_INVALID, "voxels [%lld, +%lld) outside the 2^%d grid", (long long)start,
+                  (long long)count, level);
+    if (count == 0) return NGLOD_OK;
+    NGLOD_REQUIRE(out, NGLOD_ERR_INVALID, "null pointer argument");
+    voxel_centres_kernel<<<grid_elems(count), 256, 0, (cudaStream_t)stream>>>(level, start, count, out);
+    return launch_status("nglod_voxel_centres");
+}
+
+extern "C" int nglod_select_band(const float *values, int64_t n, float band, int32_t level, int64_t start,
+                                 uint16_t *voxels, int64_t base, int64_t capacity, uint32_t *partials, int64_t *ctrl,
+                                 int64_t *selected, nglod_stream_t stream) {
+    NGLOD_REQUIRE(n >= 0 && level >= 1 && level <= 15 && base >= 0 && selected, NGLOD_ERR_INVALID, "bad argument");
+    *selected = 0;
+    if (n == 0) return NGLOD_OK;
+    NGLOD_REQUIRE(values && voxels && partials && ctrl, NGLOD_ERR_INVALID, "null pointer argument");
+    NGLOD_REQUIRE(aligned(ctrl, 8), NGLOD_ERR_ALIGN, "ctrl must be 8-byte aligned");
+    cudaStream_t s = (cudaStream_t)stream;
+    const int64_t init[3] = {n, 0, 0};  // count, total, status
+    NGLOD_TRY(cuda_status(cudaMemcpyAsync(ctrl, init, sizeof(init), cudaMemcpyHostToDevice, s), "band copy"));
+    const int grid = grid_for((n + kChunk - 1) / kChunk);
+    band_chunk_kernel<<<grid, kChunk, 0, s>>>(values, ctrl, band, partials);
+    scan_chunk_counts_kernel<<<1, kChunk, 0, s>>>(partials, ctrl, ctrl + 1, INT64_MAX, nullptr);
+    band_emit_kernel<<<grid, kChunk, 0, s>>>(values, ctrl, band, partials, level, start, voxels, base, capacity,
+                                             ctrl + 2);
+    NGLOD_TRY(launch_status("nglod_select_band"));
+    int64_t res[3];
+    NGLOD_TRY(cuda_status(cudaMemcpyAsync(res, ctrl, sizeof(res), cudaMemcpyDeviceToHost, s), "band copy"));
+    NGLOD_TRY(cuda_status(cudaStreamSynchronize(s), "band sync"));
+    NGLOD_REQUIRE(res[2] == 0, NGLOD_ERR_CAPACITY, "more than %lld voxels selected", (long long)(capacity - base));
+    *selected = res[1];
+    return NGLOD_OK;
 }
