@@ -28,6 +28,7 @@ training step against the reference computation in stock PyTorch ops, then
 2,000 steps and the BF16 form on the trained weights), ``sparse`` (SPC octree
 traversal + sparse BF16 trace of a 1080p frame), ``shade`` (a shaded 1080p
 frame: trace, ground plane, shadow rays, ambient occlusion, matcap),
+``mesh`` (mesh signed distance of 1M points against 20,480 triangles),
 ``roofline``,
 ``cpu_baseline``, ``clocks``, ``gpu_launches``.  ``--only LEG`` runs one
 extra leg alone (for profiling).
@@ -71,7 +72,7 @@ def parse():
     p.add_argument("--warmup", type=int, default=10)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--no-extras", action="store_true", help="skip the trace and CPU-baseline legs")
-    p.add_argument("--only", choices=["trace", "train", "sparse", "serve", "shade"], default=None,
+    p.add_argument("--only", choices=["trace", "train", "sparse", "serve", "shade", "mesh"], default=None,
                    help="run one extra leg alone (profiling); prints its JSON")
     return p.parse_args()
 
@@ -286,6 +287,7 @@ def run_ours(args):
         extras["train"] = bench_train(dev, flush, stream)
         extras["sparse"] = bench_sparse(net, dev, flush, stream)
         extras["shade"] = bench_shade(net, bnet, dev, flush, stream)
+        extras["mesh"] = bench_mesh(dev, flush, stream)
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_extras:
@@ -377,6 +379,27 @@ def bench_shade(net, bnet, dev, flush, stream):
     if hasattr(bnet, "check_status"):
         bnet.check_status()
     return out
+
+
+def bench_mesh(dev, flush, stream):
+    """Mesh signed distance (compute_sdf): 1,048,576 points uniform in
+    [-1.2, 1.2]^3 against an icosphere of 20,480 triangles; the unit is one
+    point-triangle test (distance + 13 line crossings)."""
+    from nglod_gb300 import mesh, synthetic
+    V, F = synthetic.icosphere(5)
+    Vd = torch.from_numpy(V).float().to(dev)
+    Fd = torch.from_numpy(F).to(dev)
+    rec = mesh.triangle_records(Vd, Fd)
+    n = 1 << 20
+    pts = (torch.rand(n, 3, device=dev, generator=torch.Generator(device=dev).manual_seed(0)) * 2.4 - 1.2)
+    for _ in range(2):
+        mesh.mesh_sdf(rec, pts)
+    torch.cuda.synchronize()
+    reps = 3
+    ms = time_steps(lambda: mesh.mesh_sdf(rec, pts), reps, flush, stream) / reps
+    pairs = n * F.shape[0]
+    return {"workload": f"compute_sdf: {n} points x {F.shape[0]} triangles (icosphere, 5 subdivisions)",
+            "ms": ms, "points_per_s": n / (ms / 1e3), "point_triangle_tests_per_s": pairs / (ms / 1e3)}
 
 
 class _TorchOpsOctreeSDF(torch.nn.Module):
@@ -647,6 +670,8 @@ def run_only(args):
         out = bench_sparse(net, dev, flush, stream)
     elif args.only == "shade":
         out = bench_shade(net, Bf16OctreeSDF(net), dev, flush, stream)
+    elif args.only == "mesh":
+        out = bench_mesh(dev, flush, stream)
     else:
         out = bench_serve(dev, duration_s=2.0)
     print(json.dumps({"only": args.only, **out}), flush=True)

@@ -421,6 +421,25 @@ int nglod_sparse_trace_tc(const nglod_sparse_model *model, int32_t lod, int32_t 
                           int32_t *status, nglod_stream_t stream);
 
 /* ------------------------------------------------------------------------
+ * Mesh data path: signed distance of points to a triangle mesh
+ * (compute_sdf -> mesh2sdf.mesh2sdf_gpu, sdf-net/lib/torchgp/compute_sdf.py:
+ * 26-40; the algorithm of sdf-net/lib/extensions/mesh2sdf_cuda/
+ * mesh2sdf_kernel.cu:307-617: minimum point-triangle distance, negative when
+ * each of 13 fixed lines through the point crosses the mesh on both sides).
+ * ------------------------------------------------------------------------ */
+
+/* Floats per triangle record (nglod_mesh_prepare's output stride). */
+int64_t nglod_mesh_record_floats(void);
+
+/* triangles float32 [m][3][3] (vertices of each face) -> records
+ * [m][nglod_mesh_record_floats()], 16-byte aligned. */
+int nglod_mesh_prepare(const float *triangles, int64_t m, float *records, nglod_stream_t stream);
+
+/* out[n] = signed distance of points [n][3] to the mesh of m records. */
+int nglod_mesh_sdf(const float *records, int64_t m, const float *points, int64_t n, float *out,
+                   nglod_stream_t stream);
+
+/* ------------------------------------------------------------------------
  * Shading passes on a traced render buffer (Renderer.render / shade_tensor,
  * sdf-net/lib/renderer.py:118-223; geoutils.py:237-276).  Buffers are the
  * tracer's: x [n][3], t [n], hit [n], normal [n][3]; images are [W][H]

@@ -228,6 +228,9 @@ SIGNATURES = {
     "nglod_sdf_fwd_host": (ctypes.c_int, [ctypes.POINTER(DenseModel), _vp, _i64, _i32, _vp, _i64, _vp, _vp]),
     "nglod_sdf_fwd_bf16_host": (ctypes.c_int, [ctypes.POINTER(Bf16Model), _vp, _i64, _i32, _vp, _i64, _vp, _vp,
                                                _vp]),
+    "nglod_mesh_record_floats": (_i64, []),
+    "nglod_mesh_prepare": (ctypes.c_int, [_vp, _i64, _vp, _vp]),
+    "nglod_mesh_sdf": (ctypes.c_int, [_vp, _i64, _vp, _i64, _vp, _vp]),
     "nglod_shade_min_hit_y": (ctypes.c_int, [_vp, _vp, _i64, _vp, _vp]),
     "nglod_shade_ground": (ctypes.c_int, [_vp, _vp, _i64, _f32, _vp, _vp, _vp, _vp, _vp, _vp]),
     "nglod_shade_shadow_rays": (ctypes.c_int, [_vp, _vp, _vp, _i64, _vp, _vp, _vp, _vp, _vp]),

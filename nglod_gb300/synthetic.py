@@ -145,3 +145,53 @@ def matcap_texture(size=64):
     col = base[None, None, :] * (0.15 + 0.85 * lam[..., None]) + 0.5 * spec[..., None]
     col = np.where((rr <= 1)[..., None], col, base[None, None, :] * 0.15)
     return np.clip(np.round(col * 255), 0, 255).astype(np.uint8)
+
+
+def icosphere(subdivisions=3, radius=1.0, centre=(0.0, 0.0, 0.0)):
+    """Closed triangle mesh of a sphere: [V float64 [#V, 3], F int64 [#F, 3]],
+    an icosahedron subdivided `subdivisions` times (each face into four,
+    new vertices pushed onto the sphere), faces wound outward."""
+    t = (1.0 + 5 ** 0.5) / 2.0
+    V = [(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t), (0, -1, -t), (0, 1, -t),
+         (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)]
+    V = [np.array(v, float) / np.linalg.norm(v) for v in V]
+    F = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2), (10, 7, 6),
+         (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5), (2, 4, 11), (6, 2, 10),
+         (8, 6, 7), (9, 8, 1)]
+    for _ in range(subdivisions):
+        cache = {}
+
+        def mid(a, b):
+            key = (min(a, b), max(a, b))
+            if key not in cache:
+                m = V[a] + V[b]
+                V.append(m / np.linalg.norm(m))
+                cache[key] = len(V) - 1
+            return cache[key]
+        nf = []
+        for a, b, c in F:
+            ab, bc, ca = mid(a, b), mid(b, c), mid(c, a)
+            nf += [(a, ab, ca), (b, bc, ab), (c, ca, bc), (ab, bc, ca)]
+        F = nf
+    V = np.array(V) * radius + np.asarray(centre, float)
+    return V, np.array(F, dtype=np.int64)
+
+
+def torus(R=0.6, r=0.25, n_major=48, n_minor=24):
+    """Closed triangle mesh of a torus around the y axis: [V, F]."""
+    u = np.arange(n_major) * 2 * np.pi / n_major
+    v = np.arange(n_minor) * 2 * np.pi / n_minor
+    uu, vv = np.meshgrid(u, v, indexing="ij")
+    x = (R + r * np.cos(vv)) * np.cos(uu)
+    z = (R + r * np.cos(vv)) * np.sin(uu)
+    y = r * np.sin(vv)
+    V = np.stack([x, y, z], -1).reshape(-1, 3)
+    F = []
+    for i in range(n_major):
+        for j in range(n_minor):
+            a = i * n_minor + j
+            b = ((i + 1) % n_major) * n_minor + j
+            c = ((i + 1) % n_major) * n_minor + (j + 1) % n_minor
+            d = i * n_minor + (j + 1) % n_minor
+            F += [(a, d, b), (b, d, c)]
+    return V, np.array(F, dtype=np.int64)

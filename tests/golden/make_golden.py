@@ -22,6 +22,9 @@ Fixtures:
   spc_small.npz    SPC3D octree of level 5 built from the voxels near the
                    sphere-union surface: Morton codes, octree bytes, pyramid,
                    decoded points; unique_corners of levels 2..5.
+  mesh_small.npz   torchgp.normalize, per_face_normals and point_sample
+                   (['trace', 'near', 'rand'], torch seed 3) on a procedural
+                   icosphere.
   shade_small.npz  Renderer.shade_tensor with a ground plane, shadow rays and
                    ambient occlusion on trace_small's network, 48x40 rays,
                    matcap shading with nglod_gb300.synthetic.matcap_texture
@@ -212,6 +215,21 @@ def shade_small(OctreeSDF, SphereTracer, parse_options):
     np.savez_compressed(os.path.join(HERE, "shade_small.npz"), **out)
 
 
+def mesh_small():
+    """The reference's torchgp normalize, per_face_normals and point_sample on
+    a procedural icosphere (the reference's meshes are not distributed)."""
+    from lib.torchgp import normalize, per_face_normals, point_sample
+    V, F = synthetic.icosphere(2, radius=0.8, centre=(0.1, -0.05, 0.2))
+    V = torch.from_numpy(V).float()
+    F = torch.from_numpy(F)
+    Vn, Fn = normalize(V, F)
+    torch.manual_seed(3)
+    pts = point_sample(Vn, Fn, ["trace", "near", "rand"], 300)
+    out = {"V": V.numpy(), "F": F.numpy(), "V_normalized": Vn.numpy(), "face_normals": per_face_normals(Vn, Fn).numpy(),
+           "point_sample": pts.numpy()}
+    np.savez_compressed(os.path.join(HERE, "mesh_small.npz"), **out)
+
+
 def coded_volume(s, channels=2):
     c = torch.arange(channels, dtype=torch.float64).view(channels, 1, 1, 1)
     z = torch.arange(s, dtype=torch.float64).view(1, s, 1, 1)
@@ -279,6 +297,7 @@ def main():
     trace_small(OctreeSDF, SphereTracer, parse_options)
     spc_small(spc3d, geoutils, ref_root)
     shade_small(OctreeSDF, SphereTracer, parse_options)
+    mesh_small()
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))
