@@ -80,8 +80,9 @@ def parse():
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of
 # sdf_fwd_bf16_tc_kernel on this workload, from the ncu capture summarised in
 # profiles/sdf_fwd_bf16_tc_4M.md (the algorithmic bytes of a launch are
-# 67.1 MB of points and results plus 20.2 MB of bf16 volumes).
-NCU_TRAFFIC_BYTES = 70_620_416 + 5_572_352
+# 67.1 MB of points and results plus 40.4 MB of bf16 pair volumes; the
+# results still in L2 when the kernel ends are written back later).
+NCU_TRAFFIC_BYTES = 90_623_232 + 10_336_512
 NCU_TRAFFIC_SOURCE = "ncu --set full capture of one launch, 4,194,304 points (profiles/sdf_fwd_bf16_tc_4M.md)"
 
 
@@ -252,7 +253,8 @@ def run_ours(args):
 
     pk = peaks()
     grid_bytes = sum(fv.fm.numel() * 2 for fv in net.features)
-    hbm_bytes = N_POINTS * (12 + 4) + grid_bytes
+    pair_bytes = sum(pv.numel() * 2 for pv in bnet.pairs) or grid_bytes  # what the launch reads
+    hbm_bytes = N_POINTS * (12 + 4) + pair_bytes
     gather_bytes = N_POINTS * (LOD + 1) * 8 * 32 * 2
     tc_flop = N_POINTS * 2 * 35 * 128
     sec = ms_per_step / 1e3
@@ -267,9 +269,10 @@ def run_ours(args):
         "gather_gbs": gather_bytes / sec / 1e9,
         "tensor_tflops": tc_flop / sec / 1e12,
         "tensor_frac_of_bf16_peak": tc_flop / sec / 1e12 / pk["bf16_tflops"],
-        "note": "one launch reads each point once and the 20.2 MB of bf16 volumes from HBM; the corner "
-                "gathers (2,560 B/query) are served by L2/L1 and bind the kernel; the 35x128 decoder "
-                "layer runs on tcgen05 tensor cores and is a small share of the time",
+        "note": "one launch reads each point once and the 40.4 MB of bf16 pair volumes (each vertex beside "
+                "its +x neighbour, 128-byte lines) from HBM; the corner gathers (2,560 B/query, four whole "
+                "lines per LOD) are served by L2/L1 and bind the kernel; the 35x128 decoder layer runs on "
+                "tcgen05 tensor cores and is a small share of the time",
     }
     sec32 = ms32 / 1e3
     fp32 = {"value": ws * N_POINTS / sec32, "unit": UNIT, "ms_per_step": ms32, "steps": steps32,

@@ -150,7 +150,18 @@ typedef struct nglod_bf16_model {
     const float *b0[NGLOD_MAX_LODS];       /* [128]; informational (b0 is folded into w0_tile) */
     const float *w1[NGLOD_MAX_LODS];       /* [128] */
     const float *b1[NGLOD_MAX_LODS];       /* [1] */
+    /* Optional pair volumes from nglod_bf16_build_pairs (32-byte aligned):
+     * when set for every LOD a query reads, nglod_sdf_fwd_bf16 reads these
+     * (one 128-byte line per vertex and its +x neighbour) instead of grid;
+     * results are identical.  NULL: grid is read. */
+    const void  *grid_pairs[NGLOD_MAX_LODS];
 } nglod_bf16_model;
+
+/* Pair volume of one bf16 volume grid [s][s][s][32]: pairs [s][s][s][2][32]
+ * bf16, 128 bytes per vertex: four 32-byte units [v(z,y,x) channels 8c..8c+7
+ * | v(z,y,min(x+1,s-1)) channels 8c..8c+7].  grid 16-byte aligned, pairs
+ * 32-byte aligned, s in 2..1025. */
+int nglod_bf16_build_pairs(const void *grid, int32_t s, void *pairs, nglod_stream_t stream);
 
 #define NGLOD_BF16_TILE_BYTES 12288
 

@@ -102,6 +102,7 @@ class Bf16Model(ctypes.Structure):
         ("b0", _vp * MAX_LODS),
         ("w1", _vp * MAX_LODS),
         ("b1", _vp * MAX_LODS),
+        ("grid_pairs", _vp * MAX_LODS),
     ]
 
 
@@ -219,6 +220,7 @@ SIGNATURES = {
     "nglod_sparse_trace_tc": (ctypes.c_int, [ctypes.POINTER(SparseModel), _i32, _i32, _vp, _vp, _i64, _vp, _i64,
                                              _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "nglod_bf16_pack_decoder": (ctypes.c_int, [_vp, _vp, _i32, _i32, _vp]),
+    "nglod_bf16_build_pairs": (ctypes.c_int, [_vp, _i32, _vp, _vp]),
     "nglod_sdf_fwd_bf16": (ctypes.c_int, [ctypes.POINTER(Bf16Model), _vp, _i64, _i32, _vp, _vp, _vp]),
     "nglod_trace_bf16": (ctypes.c_int, [ctypes.POINTER(Bf16Model), ctypes.POINTER(TraceParams), _vp, _vp, _i64,
                                         _vp, _vp, _vp, _vp, _vp, _vp, _vp]),

@@ -29,7 +29,11 @@ def pack_decoder_tile(w0, b0):
 
 
 class Bf16OctreeSDF:
-    def __init__(self, net):
+    """pairs: also keep each volume as a pair volume (every vertex beside
+    its +x neighbour, nglod_bf16_build_pairs; twice the volume bytes), which
+    point queries read with whole 128-byte lines; results are identical."""
+
+    def __init__(self, net, pairs=True):
         _lib.require_cuda(net.features[0].fm)
         dev = net.features[0].fm.device
         self.num_lods = net.num_lods
@@ -49,6 +53,16 @@ class Bf16OctreeSDF:
             m.grid[i] = self.grids[i].data_ptr()
             m.w0_tile[i] = self.tiles[i].data_ptr()
             m.b0[i], m.w1[i], m.b1[i] = self.b0[i].data_ptr(), self.w1[i].data_ptr(), self.b1[i].data_ptr()
+        self.pairs = []
+        if pairs:
+            lib = _lib.load()
+            for i, g in enumerate(self.grids):
+                s = g.shape[-1]
+                pv = torch.empty(s, s, s, 2, g.shape[1], dtype=torch.bfloat16, device=dev)
+                _lib.check(lib.nglod_bf16_build_pairs(g.data_ptr(), s, pv.data_ptr(), _lib.stream_ptr(dev)),
+                           "nglod_bf16_build_pairs")
+                self.pairs.append(pv)
+                m.grid_pairs[i] = pv.data_ptr()
         self._m = m
         self._status = torch.zeros(1, dtype=torch.int32, device=dev)
 

@@ -1,7 +1,9 @@
 // BF16 form of the dense path: bf16 channel-last feature volumes gathered
 // with 16-byte loads (point queries: each lane computes its own point's
 // corner offsets and weights and four lanes per point load the corners, 8
-// channels each; the tracer: two lanes per point, 16 channels each), the LOD sum kept in fp32 and written as one
+// channels each, or with 32-byte loads from pair volumes that hold each
+// vertex beside its +x neighbour; the tracer: two lanes per point, 16
+// channels each), the LOD sum kept in fp32 and written as one
 // row of a bf16 tile in shared memory, and the decoder's 35 -> 128 layer run
 // by tcgen05.mma on 128-point tiles with the accumulator in tensor memory.
 // b0, ReLU and the 128 -> 1 layer are an fp32 epilogue on the TMEM rows.
@@ -97,6 +99,112 @@ __device__ __forceinline__ void gather_warp_rows(const nglod_bf16_model &m, int 
                 for (int c = 0; c < 4; ++c) acc[p][4 * u + c] = __fadd2_rn(acc[p][4 * u + c], a2[c]);
             }
         }
+    }
+}
+
+// Pair lines: vertex (z, y, x) of a volume stored beside its +x neighbour
+// (x + 1 clamped to s - 1) as one 128-byte line of four 32-byte units, unit c
+// = [v(z, y, x) channels 8c..8c+7 | v(z, y, x+1) channels 8c..8c+7].
+struct alignas(32) PairUnit {
+    uint32_t w[8];
+};
+
+// 256-bit read-only load (sm_100+); pair volumes are 32-byte aligned.
+__device__ __forceinline__ PairUnit ld_pair_unit(const PairUnit *p) {
+    PairUnit r;
+    asm("ld.global.nc.v8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=r"(r.w[0]), "=r"(r.w[1]), "=r"(r.w[2]), "=r"(r.w[3]), "=r"(r.w[4]), "=r"(r.w[5]), "=r"(r.w[6]),
+          "=r"(r.w[7])
+        : "l"(p));
+    return r;
+}
+
+// gather_warp_rows<4> over pair volumes for the warp's 8 * NP points (lane
+// i and every lane i + 8 * NP hold point i's position): the four lanes of a
+// point (4j .. 4j + 3) each read one 32-byte unit of each of the point's
+// four (y, z) lines, so a load instruction covers eight whole 128-byte lines
+// (the vertex layout covers eight half lines) and each quarter warp two.
+// (Lane i reading unit i / 8 of point i % 8 instead spreads a quarter warp
+// over eight lines and made the kernel twice as slow.)  Each lane holds both x corners of its 8
+// channels, and the eight weighted corners are summed in the same order
+// (tnw..bse) as gather_warp_rows, so the two give identical sums.
+template <int NP>
+__device__ __forceinline__ void gather_warp_pairs(const nglod_bf16_model &m, int L, float px, float py, float pz,
+                                                  int lane, float2 (&acc)[NP][4]) {
+    const unsigned FULL = 0xffffffffu;
+    const int part = lane & 3;
+#pragma unroll
+    for (int p = 0; p < NP; ++p)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) acc[p][c] = make_float2(0.f, 0.f);
+#pragma unroll 1
+    for (int l = 0; l <= L; ++l) {
+        const PairUnit *g = static_cast<const PairUnit *>(m.grid_pairs[l]) + part;  // 4 units per line
+        const int s = (1 << (l + m.base_lod)) + 1;
+        const int sy = s * 4, sz = s * sy;
+        uint32_t pk;
+        float w[8];
+        corner_set(s, px, py, pz, pk, w);
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+            const int src = p * 8 + (lane >> 2);
+            const uint32_t q = __shfl_sync(FULL, pk, src);
+            float ws[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) ws[k] = __shfl_sync(FULL, w[k], src);
+            const int o0 = (int)(q & 0x0FFFFFFFu) * 4;
+            const int oy = ((q >> 29) & 1u) ? sy : 0;
+            const int oz = ((q >> 30) & 1u) ? sz : 0;
+            const int o[4] = {o0, o0 + oy, o0 + oz, o0 + oz + oy};
+            PairUnit v[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) v[j] = ld_pair_unit(g + o[j]);
+            float2 a2[4] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f),
+                            make_float2(0.f, 0.f)};
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+#pragma unroll
+                for (int x = 0; x < 2; ++x) {
+                    const float2 w2 = make_float2(ws[2 * j + x], ws[2 * j + x]);
+#pragma unroll
+                    for (int c = 0; c < 4; ++c)
+                        a2[c] = __ffma2_rn(make_float2(bf_lo(v[j].w[4 * x + c]), bf_hi(v[j].w[4 * x + c])), w2, a2[c]);
+                }
+            }
+#pragma unroll
+            for (int c = 0; c < 4; ++c) acc[p][c] = __fadd2_rn(acc[p][c], a2[c]);
+        }
+    }
+}
+
+// Writes the tile rows row0 .. row0 + 8 * NP - 1 of gather_warp_pairs<NP>:
+// every lane its 8 bf16 features of each pass's point, and lane i < 8 * NP
+// the position / bias columns 32..39 of row row0 + i.
+template <int NP>
+__device__ __forceinline__ void write_pair_rows(uint8_t *sA, int row0, int lane, const float2 (&acc)[NP][4], float px,
+                                                float py, float pz) {
+    const int part = lane & 3;
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+        const int row = row0 + p * 8 + (lane >> 2);
+        const uint4 f = make_uint4(pack_bf16x2(acc[p][0].x, acc[p][0].y), pack_bf16x2(acc[p][1].x, acc[p][1].y),
+                                   pack_bf16x2(acc[p][2].x, acc[p][2].y), pack_bf16x2(acc[p][3].x, acc[p][3].y));
+        *reinterpret_cast<uint4 *>(sA + tc::tile_offset(row, 8 * part, kKC)) = f;
+    }
+    if (lane < 8 * NP)
+        *reinterpret_cast<uint4 *>(sA + tc::tile_offset(row0 + lane, 32, kKC)) = position_columns(px, py, pz);
+}
+
+// Pair volume of a bf16 volume (s vertices per side), in 16-byte units:
+// unit 8v + 2c + h of the pair volume is unit 4v' + c of the volume, v' = v
+// for h = 0 and the +x neighbour (clamped) for h = 1.
+__global__ void build_pairs_kernel(const uint4 *__restrict__ grid, int s, int64_t units, uint4 *__restrict__ pairs) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < units; i += stride) {
+        const int64_t v = i >> 3;
+        const int c = (int)((i >> 1) & 3), h = (int)(i & 1);
+        const int64_t src = v + ((h && (v % s) + 1 < s) ? 1 : 0);
+        pairs[i] = grid[4 * src + c];
     }
 }
 
@@ -231,6 +339,11 @@ struct Bf16Args {
     int *status;
 };
 
+// One 128-point tile per block of four warps: warp w gathers rows 32w ..
+// 32w + 31 (from the vertex volumes, or from pair volumes when kPairs), one
+// thread issues the MMA, and thread (w, lane) runs the epilogue of TMEM lane
+// / row 32w + lane.
+template <bool kPairs>
 __global__ void __launch_bounds__(kTP, 4) sdf_fwd_bf16_tc_kernel(const Bf16Args a) {
     extern __shared__ __align__(1024) uint8_t smem[];
     uint8_t *sA = smem + kSmemA;
@@ -266,7 +379,7 @@ __global__ void __launch_bounds__(kTP, 4) sdf_fwd_bf16_tc_kernel(const Bf16Args 
     const uint32_t idesc = tc::idesc_bf16_f32(kTP, kHid);
     uint32_t phase = 0;
     // unsorted query points: four lanes per point load (one load instruction
-    // covers a point's 64-byte vertex)
+    // covers a point's 64-byte vertex, or its 128-byte pair line)
     constexpr int kLPP = 4;
 
     for (int64_t tile = blockIdx.x; tile * kTP < a.n; tile += gridDim.x) {
@@ -279,9 +392,15 @@ __global__ void __launch_bounds__(kTP, 4) sdf_fwd_bf16_tc_kernel(const Bf16Args 
                 py = a.x[3 * gi + 1];
                 pz = a.x[3 * gi + 2];
             }
-            float2 acc[kLPP][16 / kLPP];
-            gather_warp_rows<kLPP>(a.m, a.L, px, py, pz, lane, acc);
-            write_warp_rows<kLPP>(sA, warp, lane, acc, px, py, pz);
+            if constexpr (kPairs) {
+                float2 acc[4][4];
+                gather_warp_pairs<4>(a.m, a.L, px, py, pz, lane, acc);
+                write_pair_rows<4>(sA, warp * 32, lane, acc, px, py, pz);
+            } else {
+                float2 acc[kLPP][16 / kLPP];
+                gather_warp_rows<kLPP>(a.m, a.L, px, py, pz, lane, acc);
+                write_warp_rows<kLPP>(sA, warp, lane, acc, px, py, pz);
+            }
         }
         tc::fence_proxy_async_smem();
         __syncthreads();
@@ -305,9 +424,11 @@ __global__ void __launch_bounds__(kTP, 4) sdf_fwd_bf16_tc_kernel(const Bf16Args 
         phase ^= 1u;
         tc::fence_after_sync();
         // 3. epilogue: thread (w, lane) owns TMEM lane / tile row 32w + lane
-        float o = relu_dot_w1(tmem + ((uint32_t)(warp * 32) << 16), sw1);
-        const int64_t gi = tile * kTP + warp * 32 + lane;
-        if (gi < a.n) a.out[gi] = o + b1;
+        {
+            float o = relu_dot_w1(tmem + ((uint32_t)(warp * 32) << 16), sw1);
+            const int64_t gi = tile * kTP + warp * 32 + lane;
+            if (gi < a.n) a.out[gi] = o + b1;
+        }
         tc::fence_before_sync();
         __syncthreads();
     }
@@ -612,6 +733,12 @@ static int sdf_fwd_bf16_impl(const nglod_bf16_model *model, const float *x, int6
     NGLOD_REQUIRE(n >= 0, NGLOD_ERR_INVALID, "n=%lld is negative", (long long)n);
     if (n == 0) return NGLOD_OK;
     NGLOD_REQUIRE(x && out && status, NGLOD_ERR_INVALID, "null pointer argument");
+    bool pairs = true;
+    for (int l = 0; l <= L; ++l) {
+        NGLOD_REQUIRE(!model->grid_pairs[l] || aligned(model->grid_pairs[l], 32), NGLOD_ERR_ALIGN,
+                      "bf16 pair volume %d is not 32-byte aligned", l);
+        pairs = pairs && model->grid_pairs[l] != nullptr;
+    }
     if (zero_status)
         NGLOD_TRY(cuda_status(cudaMemsetAsync(status, 0, sizeof(int32_t), s), "nglod_sdf_fwd_bf16 memset"));
     Bf16Args a;
@@ -621,13 +748,25 @@ static int sdf_fwd_bf16_impl(const nglod_bf16_model *model, const float *x, int6
     a.L = L;
     a.out = out;
     a.status = status;
-    NGLOD_TRY(cuda_status(
-        cudaFuncSetAttribute(sdf_fwd_bf16_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes),
-        "cudaFuncSetAttribute"));
+    auto kernel = pairs ? sdf_fwd_bf16_tc_kernel<true> : sdf_fwd_bf16_tc_kernel<false>;
+    NGLOD_TRY(cuda_status(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes),
+                          "cudaFuncSetAttribute"));
     const int64_t tiles = (n + kTP - 1) / kTP;
     const int64_t cap = (int64_t)num_sms() * 4;
-    sdf_fwd_bf16_tc_kernel<<<(int)(tiles < cap ? tiles : cap), kTP, kSmemBytes, s>>>(a);
+    kernel<<<(int)(tiles < cap ? tiles : cap), kTP, kSmemBytes, s>>>(a);
     return launch_status("nglod_sdf_fwd_bf16");
+}
+
+extern "C" int nglod_bf16_build_pairs(const void *grid, int32_t s, void *pairs, nglod_stream_t stream) {
+    NGLOD_REQUIRE(grid && pairs, NGLOD_ERR_INVALID, "null pointer argument");
+    NGLOD_REQUIRE(s >= 2 && s <= 1025, NGLOD_ERR_INVALID, "s=%d", s);
+    NGLOD_REQUIRE(aligned(grid, 16) && aligned(pairs, 32), NGLOD_ERR_ALIGN,
+                  "grid must be 16-byte and pairs 32-byte aligned");
+    const int64_t units = (int64_t)s * s * s * 8;
+    const int64_t want = (units + 255) / 256, cap = (int64_t)num_sms() * 16;
+    build_pairs_kernel<<<(int)(want < cap ? want : cap), 256, 0, (cudaStream_t)stream>>>(
+        static_cast<const uint4 *>(grid), s, units, static_cast<uint4 *>(pairs));
+    return launch_status("nglod_bf16_build_pairs");
 }
 
 extern "C" int nglod_sdf_fwd_bf16(const nglod_bf16_model *model, const float *x, int64_t n, int32_t lod, float *out,

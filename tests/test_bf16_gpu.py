@@ -153,3 +153,34 @@ def test_host_memory_queries_equal_device_queries(nets, n, chunk):
     if n:
         with pytest.raises(RuntimeError, match="CPU tensor"):
             bnet.sdf_host(x.to(dev))
+
+
+def test_pair_volumes_are_built_and_give_identical_results(nets):
+    """nglod_bf16_build_pairs against a torch construction of the pair layout,
+    and queries through pair volumes equal to queries through the vertex
+    volumes bit for bit (same corner order), including points outside the
+    box (border clamp) and exactly on the last vertex plane (x0 = s - 1)."""
+    net, bnet, m32, _, _ = nets
+    dev = net.features[0].fm.device
+    assert len(bnet.pairs) == bnet.num_lods
+    for g, pv in zip(bnet.grids, bnet.pairs):
+        s = g.shape[-1]
+        v = g[0].permute(1, 2, 3, 0)  # [z][y][x][32]
+        nx = torch.cat([v[:, :, 1:], v[:, :, -1:]], dim=2)
+        want = torch.stack([v.reshape(s, s, s, 4, 8), nx.reshape(s, s, s, 4, 8)], dim=4)  # [.., unit, x, 8]
+        assert torch.equal(pv.reshape(s, s, s, 4, 2, 8), want)
+    plain = Bf16OctreeSDF(net, pairs=False)
+    assert not plain.pairs
+    gen = torch.Generator().manual_seed(9)
+    x = torch.rand(70001, 3, generator=gen) * 2.4 - 1.2
+    x[:300] = torch.tensor([1.0, 1.0, 1.0])
+    x[300:600, 0] = 1.0
+    x[600:900, 1] = -1.0
+    x = x.to(dev)
+    for lod in range(bnet.num_lods):
+        a = bnet.sdf(x, lod=lod)
+        b = plain.sdf(x, lod=lod)
+        assert torch.equal(a, b), (lod, (a - b).abs().max().item())
+    np.testing.assert_allclose(a.cpu().numpy(), emulate(m32, x.cpu().numpy(), bnet.num_lods - 1), atol=2e-4, rtol=0)
+    bnet.check_status()
+    plain.check_status()
