@@ -211,22 +211,38 @@ typedef struct nglod_dense_grads {
  * L = highest set bit: preds[l][n] and feats[l][n][C] (the running feature
  * sum that decoder l reads) are written for every l in the mask.  Same
  * predictions as OctreeSDF.sdf(x, lod=l) for each l in the mask
- * (OctreeSDF.py:94-146); with all bits set, as sdf(x, return_lst=True). */
+ * (OctreeSDF.py:94-146); with all bits set, as sdf(x, return_lst=True).
+ * relu_masks (optional, 16-byte aligned): relu_masks[l][n][(H+31)/32] gets
+ * the decoder's ReLU mask (bit j of word j/32: hidden unit j was positive),
+ * which nglod_sdf_bwd takes as the ReLU derivative, as autograd takes the
+ * forward's saved activation. */
 int nglod_sdf_fwd_train(const nglod_dense_model *model, const float *x, int64_t n, uint32_t lod_mask,
-                        float *preds, float *feats, nglod_stream_t stream);
+                        float *preds, float *feats, uint32_t *relu_masks, nglod_stream_t stream);
 
 /* Backward of nglod_sdf_fwd_train.  grad_preds[l][n] = dLoss/dpred_l for l in
  * lod_mask.  Adds the parameter gradients into `grads` and, when grad_x is
  * not NULL, dLoss/dx into grad_x[n][3].  dfeat_scratch[L+1][n][C] is caller-
  * provided scratch.  Replaces the autograd backward of OctreeSDF.sdf through
  * nn.Linear and F.grid_sample (border padding, align_corners) that
- * Trainer.step_geometry runs (sdf-net/lib/trainer.py:339): decoder weight
- * gradients are per-block tile reductions, feature gradients a trilinear
+ * Trainer.step_geometry runs (sdf-net/lib/trainer.py:339).  With
+ * hidden_dim 128 and the forward's relu_masks, the decoder part runs on
+ * tcgen05 tensor cores (three products per 128-point tile, each as three
+ * bf16 MMAs over hi / lo splits, fp32 accumulation: relative error about
+ * 2^-16 per product, ReLU derivative from relu_masks); otherwise (relu_masks
+ * NULL, or other widths) float32 tile reductions that recompute the hidden
+ * layer in the forward's order.  Feature gradients are a trilinear
  * scatter-add (coarse volumes accumulated in shared memory, the rest with
- * vector atomics). */
+ * vector atomics).  A tensor-core wait that gives up is reported by
+ * nglod_train_status. */
 int nglod_sdf_bwd(const nglod_dense_model *model, const float *x, int64_t n, uint32_t lod_mask,
-                  const float *grad_preds, const float *feats, float *dfeat_scratch,
+                  const float *grad_preds, const float *feats, const uint32_t *relu_masks, float *dfeat_scratch,
                   const nglod_dense_grads *grads, float *grad_x, nglod_stream_t stream);
+
+/* Reads and clears the backward's device status on the current device
+ * (synchronous): *status_out = 1 if a bounded tensor-core wait of a
+ * nglod_sdf_bwd / nglod_sdf_bwd_noalloc call since the last read gave up
+ * (its gradients are incomplete), else 0. */
+int nglod_train_status(int32_t *status_out);
 
 /* nglod_sdf_bwd for callers that cannot allocate device memory (a plugin
  * whose GPU memory is owned by its host application, a process whose
@@ -243,8 +259,8 @@ int nglod_sdf_bwd(const nglod_dense_model *model, const float *x, int64_t n, uin
  * on the GPU race and must be serialised by the caller. */
 #define NGLOD_NOALLOC_SCRATCH_BYTES (16u << 20)
 int nglod_sdf_bwd_noalloc(const nglod_dense_model *model, const float *x, int64_t n, uint32_t lod_mask,
-                          const float *grad_preds, const float *feats, const nglod_dense_grads *grads,
-                          float *grad_x, nglod_stream_t stream);
+                          const float *grad_preds, const float *feats, const uint32_t *relu_masks,
+                          const nglod_dense_grads *grads, float *grad_x, nglod_stream_t stream);
 
 /* One tensor of a multi-tensor Adam step (device-resident table). */
 typedef struct nglod_adam_tensor {

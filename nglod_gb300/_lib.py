@@ -195,10 +195,11 @@ SIGNATURES = {
     "nglod_sdf_fwd": (ctypes.c_int, [ctypes.POINTER(DenseModel), _vp, _i64, _i32, _i32, _vp, _vp]),
     "nglod_trace": (ctypes.c_int, [ctypes.POINTER(DenseModel), ctypes.POINTER(TraceParams), _vp, _vp, _i64,
                                    _vp, _vp, _vp, _vp, _vp, _vp]),
-    "nglod_sdf_fwd_train": (ctypes.c_int, [ctypes.POINTER(DenseModel), _vp, _i64, _u32, _vp, _vp, _vp]),
-    "nglod_sdf_bwd": (ctypes.c_int, [ctypes.POINTER(DenseModel), _vp, _i64, _u32, _vp, _vp, _vp,
+    "nglod_sdf_fwd_train": (ctypes.c_int, [ctypes.POINTER(DenseModel), _vp, _i64, _u32, _vp, _vp, _vp, _vp]),
+    "nglod_train_status": (ctypes.c_int, [ctypes.POINTER(_i32)]),
+    "nglod_sdf_bwd": (ctypes.c_int, [ctypes.POINTER(DenseModel), _vp, _i64, _u32, _vp, _vp, _vp, _vp,
                                      ctypes.POINTER(DenseGrads), _vp, _vp]),
-    "nglod_sdf_bwd_noalloc": (ctypes.c_int, [ctypes.POINTER(DenseModel), _vp, _i64, _u32, _vp, _vp,
+    "nglod_sdf_bwd_noalloc": (ctypes.c_int, [ctypes.POINTER(DenseModel), _vp, _i64, _u32, _vp, _vp, _vp,
                                              ctypes.POINTER(DenseGrads), _vp, _vp]),
     "nglod_spc_build_scratch_bytes": (_i64, [_i32]),
     "nglod_spc_build": (ctypes.c_int, [_vp, _i64, _i32, _vp, _i64, ctypes.POINTER(_i64), _vp, _vp, _vp]),

@@ -7,6 +7,8 @@ volume and decoder that the requested predictions depend on (and of x when x
 requires grad), replacing autograd through F.grid_sample and nn.Linear
 (sdf-net/lib/models/OctreeSDF.py:94-155).
 """
+import ctypes
+
 import torch
 
 from . import _lib
@@ -39,9 +41,14 @@ class _SdfTrain(torch.autograd.Function):
         dev = xd.device
         preds = torch.zeros(L + 1, n, 1, device=dev, dtype=torch.float32)
         feats = torch.empty(L + 1, n, net.fdim, device=dev, dtype=torch.float32)
+        # ReLU masks of the forward: the tensor-core backward (hidden_dim 128) takes them as the
+        # ReLU derivative; other widths recompute the hidden layer
+        relu = (torch.empty(L + 1, n, net.hidden_dim // 32, device=dev, dtype=torch.int32)
+                if net.hidden_dim == 128 else None)
         m = _model_from_params(net, fms, decs)
         _lib.check(_lib.load().nglod_sdf_fwd_train(m, _lib.ptr(xd), n, mask, _lib.ptr(preds), _lib.ptr(feats),
-                                                   _lib.stream_ptr(dev)), "nglod_sdf_fwd_train")
+                                                   _lib.ptr(relu), _lib.stream_ptr(dev)), "nglod_sdf_fwd_train")
+        ctx.relu = relu
         ctx.save_for_backward(xd, feats, *fms, *[p for d in decs for p in d])
         ctx.mask = mask
         ctx.net = net
@@ -75,7 +82,9 @@ class _SdfTrain(torch.autograd.Function):
         dfeat = torch.empty_like(feats)
         gx = torch.zeros(n, 3, device=dev, dtype=torch.float32) if ctx.x_needs_grad else None
         _lib.check(_lib.load().nglod_sdf_bwd(m, _lib.ptr(xd), n, ctx.mask, _lib.ptr(gp), _lib.ptr(feats),
-                                             _lib.ptr(dfeat), g, _lib.ptr(gx), _lib.stream_ptr(dev)), "nglod_sdf_bwd")
+                                             _lib.ptr(ctx.relu), _lib.ptr(dfeat), g, _lib.ptr(gx),
+                                             _lib.stream_ptr(dev)), "nglod_sdf_bwd")
+        ctx.relu = None
         out = [gx, None, None] + gfm + [t for d in gdec for t in d]
         return tuple(out)
 
@@ -99,3 +108,13 @@ def sdf_train(net, x, lod, all_lods):
     if all_lods:
         return [preds[i] for i in range(L + 1)]
     return preds[L]
+
+
+def check_backward_status():
+    """Raises if a bounded tensor-core wait of a backward since the last
+    check gave up (its gradients would be incomplete).  Synchronises the
+    device (nglod_train_status)."""
+    v = ctypes.c_int32(0)
+    _lib.check(_lib.load().nglod_train_status(ctypes.byref(v)), "nglod_train_status")
+    if v.value:
+        raise RuntimeError("nglod_sdf_bwd: a bounded tensor-core wait timed out; gradients are incomplete")

@@ -103,8 +103,11 @@ __device__ __forceinline__ void gather_add_f32(const float *__restrict__ g, int 
 }
 
 // Linear(35, H) -> ReLU -> Linear(H, 1) on [p, f] with the staged decoder.
+// kMask: also store the ReLU mask (bit j of word j / 32 = hidden unit j was
+// positive) to mask_out[0 .. (H + 31) / 32 - 1].
+template <bool kMask = false>
 __device__ __forceinline__ float decode_f32(const float4 *__restrict__ dec, int H, float px, float py,
-                                            float pz, const float (&f)[kC]) {
+                                            float pz, const float (&f)[kC], uint32_t *mask_out = nullptr) {
     const float *__restrict__ w1 = reinterpret_cast<const float *>(dec + H * kRowF4);
     float in[36];
     in[0] = px;
@@ -114,6 +117,7 @@ __device__ __forceinline__ float decode_f32(const float4 *__restrict__ dec, int 
     for (int c = 0; c < kC; ++c) in[3 + c] = f[c];
     in[35] = 1.f;
     float out = 0.f;
+    uint32_t bits = 0u;
 #pragma unroll 1
     for (int j = 0; j < H; j += 2) {
         const float4 *r0 = dec + j * kRowF4;
@@ -147,6 +151,13 @@ __device__ __forceinline__ float decode_f32(const float4 *__restrict__ dec, int 
         const float h1 = fmaxf(b0 + b1, 0.f);
         out = fmaf(w1[j], h0, out);
         out = fmaf(w1[j + 1], h1, out);
+        if (kMask) {
+            bits |= ((uint32_t)(h0 > 0.f) << (j & 31)) | ((uint32_t)(h1 > 0.f) << ((j + 1) & 31));
+            if (((j + 2) & 31) == 0 || j + 2 >= H) {
+                mask_out[j >> 5] = bits;
+                bits = 0u;
+            }
+        }
     }
     return out + w1[H];
 }

@@ -14,9 +14,12 @@
 //      scattered with the trilinear weights.  The coarsest volumes
 //      (5^3 and 9^3 vertices at base_lod 2) are accumulated in shared memory
 //      per block and flushed once; finer ones use red.global.add.v4.f32.
+#include <cuda_bf16.h>
+
 #include <mutex>
 
 #include "dense_common.cuh"
+#include "tc_common.cuh"
 
 namespace nglod {
 
@@ -27,7 +30,8 @@ constexpr int kBT = 128;  // points per backward tile = threads per block
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) sdf_fwd_train_kernel(const nglod_dense_model m, const float *__restrict__ x,
                                                             int64_t n, int L, uint32_t mask,
-                                                            float *__restrict__ preds, float *__restrict__ feats) {
+                                                            float *__restrict__ preds, float *__restrict__ feats,
+                                                            uint32_t *__restrict__ relu) {
     extern __shared__ float4 smem[];
     const int H = m.hidden_dim;
     const int dstride = decoder_f4(H);
@@ -44,7 +48,9 @@ __global__ void __launch_bounds__(256) sdf_fwd_train_kernel(const nglod_dense_mo
         for (int l = 0; l <= L; ++l) {
             gather_add_f32(static_cast<const float *>(m.grid[l]), volume_side(m, l), px, py, pz, f);
             if ((mask >> l) & 1u) {
-                preds[(int64_t)l * n + i] = decode_f32(smem + l * dstride, H, px, py, pz, f);
+                const int64_t row = (int64_t)l * n + i;
+                preds[row] = relu ? decode_f32<true>(smem + l * dstride, H, px, py, pz, f, relu + row * ((H + 31) / 32))
+                                  : decode_f32(smem + l * dstride, H, px, py, pz, f);
                 float4 *o = reinterpret_cast<float4 *>(feats + ((int64_t)l * n + i) * kC);
 #pragma unroll
                 for (int q = 0; q < kC / 4; ++q)
@@ -66,6 +72,7 @@ struct BwdArgs {
     int L;
     const float *gpred;
     const float *feats;
+    const uint32_t *relu;  // forward ReLU masks [L+1][n][H/32] (tensor-core form)
     float *dfeat;
     float *gx;
 };
@@ -242,6 +249,331 @@ __global__ void __launch_bounds__(kBThreads, 2) sdf_bwd_decoder_kernel(const Bwd
         }
         if (tid == 0) atomicAdd(a.g.b1[l], db1);
     }
+}
+
+// ---------------------------------------------------------------------------
+// backward 1, tensor-core form (hidden_dim 128): three GEMMs per 128-point
+// tile on tcgen05, each product as three bf16 MMAs over hi / lo splits
+// (a*b ~ ah*bh + ah*bl + al*bh, relative error about 2^-16 before the fp32
+// accumulation), accumulators in TMEM:
+//   P   [128 pts x 128 hid] = IN [pts x 48] . W^T          (TMEM cols 0..127)
+//   dIN [128 pts x 48]      = dH [pts x 128 hid] . W        (cols 128..175)
+//   dW  [128 hid x 48]     += dH^T [hid x pts] . IN         (cols 192..239,
+//                              summed over all tiles of a LOD)
+// IN row of a point: x y z, the 32 summed features, 1 (the b0 column),
+// zeros; W row j: w0[j][0..34], b0[j], zeros; dH = (P > 0) * g * w1.
+// Each shared tile is written once in the K-major core-matrix layout and
+// read by the second product with an MN-major descriptor (the same 8 x 16 B
+// core matrices: for a no-swizzle MN-major operand LBO is the stride between
+// K-adjacent core matrices and SBO the stride between MN-adjacent ones).
+// dw1[j] = sum_pts g * relu(P) and db1 = sum g stay in registers per thread
+// across tiles and are reduced once per LOD.
+// ---------------------------------------------------------------------------
+namespace bwdtc {
+constexpr int kTP = 128, kH = 128, kK1 = 48, kKC1 = kK1 / 8, kKCH = kH / 8;
+constexpr int kThreads = 256;
+constexpr uint32_t kInBytes = kTP * kK1 * 2;   // 12 KB
+constexpr uint32_t kWBytes = kH * kK1 * 2;     // 12 KB
+constexpr uint32_t kDhBytes = kTP * kH * 2;    // 32 KB
+constexpr size_t kInH = 0, kInL = kInH + kInBytes, kWH = kInL + kInBytes, kWL = kWH + kWBytes;
+constexpr size_t kDH = kWL + kWBytes, kDL = kDH + kDhBytes;
+constexpr size_t kW1 = kDL + kDhBytes;          // w1 [128] f32
+constexpr size_t kDw1 = kW1 + kH * 4;           // dw1 LOD totals [128] f32
+constexpr size_t kBar = kDw1 + kH * 4;
+constexpr size_t kSlot = kBar + 8, kAbort = kSlot + 4;
+constexpr size_t kSmem = kAbort + 12;
+constexpr uint32_t kColP = 0, kColDin = 128, kColDw = 192, kCols = 256;
+constexpr uint32_t kPolls = 1u << 22;
+static_assert(kDH % 1024 == 0 && kBar % 8 == 0, "shared layout alignment");
+static_assert(kSmem <= 227 * 1024, "shared layout fits one block");
+}  // namespace bwdtc
+
+__device__ int32_t g_train_status;  // nonzero: a tensor-core wait of a backward gave up
+
+__device__ __forceinline__ uint32_t bf16x2_bits(__nv_bfloat162 h) { return *reinterpret_cast<uint32_t *>(&h); }
+
+// bf16 hi / lo split of two floats (a in the low half).
+__device__ __forceinline__ void split_bf16x2(float a, float b, uint32_t &hi, uint32_t &lo) {
+    const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    const float2 hf = __bfloat1622float2(h);
+    hi = bf16x2_bits(h);
+    lo = bf16x2_bits(__floats2bfloat162_rn(a - hf.x, b - hf.y));
+}
+
+// Column c (0..47, a compile-time index after unrolling) of a point's IN row.
+__device__ __forceinline__ float in_column(int c, const float (&xf)[3], const float4 (&fr)[8]) {
+    if (c < 3) return xf[c];
+    if (c < 35) {
+        const float4 v = fr[(c - 3) >> 2];
+        const int k = (c - 3) & 3;
+        return k == 0 ? v.x : k == 1 ? v.y : k == 2 ? v.z : v.w;
+    }
+    return c == 35 ? 1.f : 0.f;
+}
+
+// Columns 24 HALF .. 24 HALF + 23 of IN row r (hi and lo tiles); rows of
+// points past the end are zero.
+template <int HALF>
+__device__ __forceinline__ void fill_in_row(uint8_t *smem, int r, const float (&xf)[3], const float4 (&fr)[8],
+                                            bool valid) {
+#pragma unroll
+    for (int cc = 0; cc < 3; ++cc) {
+        const int c0 = HALF * 24 + cc * 8;
+        uint32_t h[4], lo[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const float v0 = valid ? in_column(c0 + 2 * k, xf, fr) : 0.f;
+            const float v1 = valid ? in_column(c0 + 2 * k + 1, xf, fr) : 0.f;
+            split_bf16x2(v0, v1, h[k], lo[k]);
+        }
+        const uint32_t off = tc::tile_offset(r, c0, bwdtc::kKC1);
+        *reinterpret_cast<uint4 *>(smem + bwdtc::kInH + off) = make_uint4(h[0], h[1], h[2], h[3]);
+        *reinterpret_cast<uint4 *>(smem + bwdtc::kInL + off) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
+    }
+}
+
+// Thread 0 issues the three-term product D (+)= A . B over `ksteps` K steps
+// of 16 (A, B descriptors advanced by a_step / b_step bytes per step).
+__device__ __forceinline__ void mma3(uint32_t d, const uint32_t (&a)[2], const uint32_t (&b)[2], uint32_t a_lbo,
+                                     uint32_t a_sbo, uint32_t a_step, uint32_t b_lbo, uint32_t b_sbo,
+                                     uint32_t b_step, int ksteps, uint32_t idesc, bool accumulate) {
+    const int ta[3] = {0, 0, 1}, tb[3] = {0, 1, 0};  // hi.hi, hi.lo, lo.hi
+#pragma unroll 1
+    for (int t = 0; t < 3; ++t)
+#pragma unroll 1
+        for (int ks = 0; ks < ksteps; ++ks) {
+            const uint64_t ad = tc::smem_desc(a[ta[t]] + ks * a_step, a_lbo, a_sbo);
+            const uint64_t bd = tc::smem_desc(b[tb[t]] + ks * b_step, b_lbo, b_sbo);
+            tc::mma_bf16(d, ad, bd, idesc, (accumulate || t > 0 || ks > 0) ? 1u : 0u);
+        }
+}
+
+// Commit and wait (thread 0); false if the bounded wait gave up.
+__device__ __forceinline__ bool commit_wait(uint64_t *bar, uint32_t &phase) {
+    tc::mma_commit(bar);
+    const bool ok = tc::mbar_wait_bounded(bar, phase, bwdtc::kPolls);
+    phase ^= 1u;
+    return ok;
+}
+
+__global__ void __launch_bounds__(bwdtc::kThreads, 1) sdf_bwd_decoder_tc_kernel(const BwdArgs a) {
+    using namespace bwdtc;
+    extern __shared__ __align__(1024) uint8_t smem_tc[];
+    uint8_t *smem = smem_tc;
+    float *w1s = reinterpret_cast<float *>(smem + kW1);
+    float *dw1s = reinterpret_cast<float *>(smem + kDw1);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + kBar);
+    uint32_t *slot = reinterpret_cast<uint32_t *>(smem + kSlot);
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + kAbort);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int sp = warp & 3, hf = warp >> 2;  // TMEM lane quarter, column half
+    const int ql = sp * 32 + lane;            // tile row (point) of this thread's TMEM lane
+
+    if (warp == 0) tc::tmem_alloc(slot, kCols);
+    if (tid == 0) {
+        tc::mbar_init(bar, 1);
+        *abort_flag = 0;
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = *slot;
+    const uint32_t sbase = tc::smem_addr(smem);
+    const uint32_t in_t[2] = {sbase + (uint32_t)kInH, sbase + (uint32_t)kInL};
+    const uint32_t w_t[2] = {sbase + (uint32_t)kWH, sbase + (uint32_t)kWL};
+    const uint32_t dh_t[2] = {sbase + (uint32_t)kDH, sbase + (uint32_t)kDL};
+    const uint32_t id1 = tc::idesc_bf16_f32(kTP, kH);
+    const uint32_t id2 = tc::idesc_bf16_f32(kTP, kK1) | (1u << 16);              // B MN-major
+    const uint32_t id3 = tc::idesc_bf16_f32(kH, kK1) | (1u << 15) | (1u << 16);  // A, B MN-major
+    const uint32_t trow = (uint32_t)(sp * 32) << 16;
+    uint32_t phase = 0;
+
+#pragma unroll 1
+    for (int l = 0; l <= a.L && !*abort_flag; ++l) {
+        if (!((a.mask >> l) & 1u)) continue;
+        // stage W (hi / lo) and w1 for this LOD
+        for (int u = tid; u < kH * kKC1; u += kThreads) {
+            const int j = u / kKC1, cc = u % kKC1;
+            float v[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                const int c = cc * 8 + k;
+                v[k] = c < 35 ? a.m.w0[l][j * 35 + c] : c == 35 ? a.m.b0[l][j] : 0.f;
+            }
+            uint32_t h[4], lo[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) split_bf16x2(v[2 * k], v[2 * k + 1], h[k], lo[k]);
+            const uint32_t off = tc::tile_offset(j, cc * 8, kKC1);
+            *reinterpret_cast<uint4 *>(smem + kWH + off) = make_uint4(h[0], h[1], h[2], h[3]);
+            *reinterpret_cast<uint4 *>(smem + kWL + off) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
+        }
+        if (tid < kH) {
+            w1s[tid] = a.m.w1[l][tid];
+            dw1s[tid] = 0.f;
+        }
+        float hg[64];  // sum over this thread's rows of g * relu(P) for columns 64 hf .. 64 hf + 63
+#pragma unroll
+        for (int i = 0; i < 64; ++i) hg[i] = 0.f;
+        float gsum = 0.f;
+        bool first = true;
+        tc::fence_proxy_async_smem();
+        __syncthreads();
+
+#pragma unroll 1
+        for (int64_t tile = blockIdx.x; tile * kTP < a.n; tile += gridDim.x) {
+            // a. IN rows: thread (r, half) fills columns 24 half .. 24 half + 23 of row r
+            {
+                const int r = tid & (kTP - 1), half = tid >> 7;
+                const int64_t q = tile * kTP + r;
+                const bool valid = q < a.n;
+                float xf[3] = {0.f, 0.f, 0.f};
+                float4 fr[8];
+#pragma unroll
+                for (int k = 0; k < 8; ++k) fr[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (valid) {
+                    xf[0] = a.x[3 * q];
+                    xf[1] = a.x[3 * q + 1];
+                    xf[2] = a.x[3 * q + 2];
+                    const float4 *src = reinterpret_cast<const float4 *>(a.feats + ((int64_t)l * a.n + q) * kC);
+#pragma unroll
+                    for (int k = 0; k < 8; ++k) fr[k] = src[k];
+                }
+                if (half == 0)
+                    fill_in_row<0>(smem, r, xf, fr, valid);
+                else
+                    fill_in_row<1>(smem, r, xf, fr, valid);
+            }
+            const int64_t qg = tile * kTP + ql;
+            const float g = qg < a.n ? a.gpred[(int64_t)l * a.n + qg] : 0.f;
+            tc::fence_proxy_async_smem();
+            tc::fence_before_sync();
+            __syncthreads();
+            // b. P = IN . W^T
+            if (tid == 0) {
+                tc::fence_after_sync();
+                mma3(tmem + kColP, in_t, w_t, 128, kKC1 * 128, 256, 128, kKC1 * 128, 256, kK1 / 16, id1, false);
+                if (!commit_wait(bar, phase)) {
+                    *abort_flag = 1;
+                    atomicExch(&g_train_status, 1);
+                }
+            }
+            __syncthreads();
+            if (*abort_flag) break;
+            tc::fence_after_sync();
+            // c. dH rows and the dw1 / db1 sums: thread (sp, hf) row ql, columns
+            // 64 hf .. +63; the ReLU derivative is the forward's mask
+            uint2 rm = make_uint2(0u, 0u);
+            if (qg < a.n) rm = reinterpret_cast<const uint2 *>(a.relu + ((int64_t)l * a.n + qg) * (kH / 32))[hf];
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                const int j0 = 64 * hf + 32 * k;
+                const uint32_t bits = k == 0 ? rm.x : rm.y;
+                float v[32];
+                tc::tmem_load32(tmem + trow + kColP + (uint32_t)j0, v);
+                uint32_t h[16], lo[16];
+#pragma unroll
+                for (int i = 0; i < 16; ++i) {
+                    const float p0 = v[2 * i], p1 = v[2 * i + 1];
+                    hg[32 * k + 2 * i] = fmaf(g, fmaxf(p0, 0.f), hg[32 * k + 2 * i]);
+                    hg[32 * k + 2 * i + 1] = fmaf(g, fmaxf(p1, 0.f), hg[32 * k + 2 * i + 1]);
+                    const float d0 = ((bits >> (2 * i)) & 1u) ? g * w1s[j0 + 2 * i] : 0.f;
+                    const float d1 = ((bits >> (2 * i + 1)) & 1u) ? g * w1s[j0 + 2 * i + 1] : 0.f;
+                    split_bf16x2(d0, d1, h[i], lo[i]);
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const uint32_t off = tc::tile_offset(ql, j0 + 8 * u, kKCH);
+                    *reinterpret_cast<uint4 *>(smem + kDH + off) = make_uint4(h[4 * u], h[4 * u + 1], h[4 * u + 2], h[4 * u + 3]);
+                    *reinterpret_cast<uint4 *>(smem + kDL + off) =
+                        make_uint4(lo[4 * u], lo[4 * u + 1], lo[4 * u + 2], lo[4 * u + 3]);
+                }
+            }
+            if (hf == 0) gsum += g;
+            tc::fence_proxy_async_smem();
+            tc::fence_before_sync();
+            __syncthreads();
+            // d. dIN = dH . W and dW += dH^T . IN
+            if (tid == 0) {
+                tc::fence_after_sync();
+                mma3(tmem + kColDin, dh_t, w_t, 128, kKCH * 128, 256, kKC1 * 128, 128, 2 * kKC1 * 128, kH / 16, id2,
+                     false);
+                mma3(tmem + kColDw, dh_t, in_t, kKCH * 128, 128, 2 * kKCH * 128, kKC1 * 128, 128, 2 * kKC1 * 128,
+                     kTP / 16, id3, !first);
+                if (!commit_wait(bar, phase)) {
+                    *abort_flag = 1;
+                    atomicExch(&g_train_status, 1);
+                }
+            }
+            __syncthreads();
+            if (*abort_flag) break;
+            first = false;
+            tc::fence_after_sync();
+            // e. dLoss/d(feature sum) and the decoder's dLoss/dx of row ql
+            {
+                float v[32];
+                tc::tmem_load32(tmem + trow + kColDin + (uint32_t)(32 * hf), v);
+                if (qg < a.n) {
+                    float *o = a.dfeat + ((int64_t)l * a.n + qg) * kC;
+                    if (hf == 0) {
+                        if (a.gx) {
+                            a.gx[3 * qg] += v[0];
+                            a.gx[3 * qg + 1] += v[1];
+                            a.gx[3 * qg + 2] += v[2];
+                        }
+#pragma unroll
+                        for (int k = 0; k < 7; ++k)
+                            reinterpret_cast<float4 *>(o)[k] =
+                                make_float4(v[3 + 4 * k], v[4 + 4 * k], v[5 + 4 * k], v[6 + 4 * k]);
+                        o[28] = v[31];
+                    } else {
+                        o[29] = v[0];
+                        o[30] = v[1];
+                        o[31] = v[2];
+                    }
+                }
+            }
+            tc::fence_before_sync();
+            __syncthreads();
+        }
+        if (*abort_flag) break;
+        // LOD totals: dW0 / db0 from TMEM rows (row j = ql), dw1 and db1 from registers
+        if (!first) {
+            tc::fence_after_sync();
+            float v[32];
+            tc::tmem_load32(tmem + trow + kColDw + (uint32_t)(32 * hf), v);
+            const int j = ql;
+            if (hf == 0) {
+#pragma unroll 4
+                for (int c = 0; c < 32; ++c) atomicAdd(a.g.w0[l] + j * 35 + c, v[c]);
+            } else {
+                atomicAdd(a.g.w0[l] + j * 35 + 32, v[0]);
+                atomicAdd(a.g.w0[l] + j * 35 + 33, v[1]);
+                atomicAdd(a.g.w0[l] + j * 35 + 34, v[2]);
+                atomicAdd(a.g.b0[l] + j, v[3]);
+            }
+#pragma unroll
+            for (int i = 0; i < 64; ++i) {
+                float t = hg[i];
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+                if (lane == 0) atomicAdd(dw1s + 64 * hf + i, t);
+            }
+            if (hf == 0) {
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) gsum += __shfl_xor_sync(0xffffffffu, gsum, o);
+                if (lane == 0) atomicAdd(a.g.b1[l], gsum);
+            }
+            __syncthreads();
+            if (tid < kH) atomicAdd(a.g.w1[l] + tid, dw1s[tid]);
+        }
+        tc::fence_before_sync();
+        __syncthreads();
+    }
+    if (*abort_flag && tid == 0) tc::mbar_wait_bounded(bar, phase, kPolls);  // let an in-flight MMA finish
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if (warp == 0) tc::tmem_dealloc(tmem, kCols);
 }
 
 // ---------------------------------------------------------------------------
@@ -430,7 +762,7 @@ static int lod_mask_top(uint32_t mask) {
 }
 
 extern "C" int nglod_sdf_fwd_train(const nglod_dense_model *model, const float *x, int64_t n, uint32_t lod_mask,
-                                   float *preds, float *feats, nglod_stream_t stream) {
+                                   float *preds, float *feats, uint32_t *relu_masks, nglod_stream_t stream) {
     NGLOD_REQUIRE(model != nullptr, NGLOD_ERR_INVALID, "model is null");
     const int L = lod_mask_top(lod_mask);
     NGLOD_REQUIRE(L >= 0 && L < model->num_lods && (lod_mask >> NGLOD_MAX_LODS) == 0, NGLOD_ERR_INVALID,
@@ -440,19 +772,21 @@ extern "C" int nglod_sdf_fwd_train(const nglod_dense_model *model, const float *
     if (n == 0) return NGLOD_OK;
     NGLOD_REQUIRE(x && preds && feats, NGLOD_ERR_INVALID, "null pointer argument");
     NGLOD_REQUIRE(aligned(feats, 16), NGLOD_ERR_ALIGN, "feats must be 16-byte aligned");
+    NGLOD_REQUIRE(!relu_masks || aligned(relu_masks, 16), NGLOD_ERR_ALIGN, "relu_masks must be 16-byte aligned");
     const int threads = 256;
     const size_t smem = (size_t)(L + 1) * decoder_f4(model->hidden_dim) * sizeof(float4);
     NGLOD_TRY(prepare_smem(sdf_fwd_train_kernel, smem));
     const int64_t want = (n + threads - 1) / threads;
     const int64_t cap = resident_blocks(sdf_fwd_train_kernel, threads, smem);
     sdf_fwd_train_kernel<<<(int)(want < cap ? want : cap), threads, smem, (cudaStream_t)stream>>>(
-        *model, x, n, L, lod_mask, preds, feats);
+        *model, x, n, L, lod_mask, preds, feats, relu_masks);
     return launch_status("nglod_sdf_fwd_train");
 }
 
 extern "C" int nglod_sdf_bwd(const nglod_dense_model *model, const float *x, int64_t n, uint32_t lod_mask,
-                             const float *grad_preds, const float *feats, float *dfeat_scratch,
-                             const nglod_dense_grads *grads, float *grad_x, nglod_stream_t stream) {
+                             const float *grad_preds, const float *feats, const uint32_t *relu_masks,
+                             float *dfeat_scratch, const nglod_dense_grads *grads, float *grad_x,
+                             nglod_stream_t stream) {
     NGLOD_REQUIRE(model != nullptr && grads != nullptr, NGLOD_ERR_INVALID, "model or grads is null");
     const int L = lod_mask_top(lod_mask);
     NGLOD_REQUIRE(L >= 0 && L < model->num_lods && (lod_mask >> NGLOD_MAX_LODS) == 0, NGLOD_ERR_INVALID,
@@ -464,6 +798,7 @@ extern "C" int nglod_sdf_bwd(const nglod_dense_model *model, const float *x, int
     NGLOD_REQUIRE(x && grad_preds && feats && dfeat_scratch, NGLOD_ERR_INVALID, "null pointer argument");
     NGLOD_REQUIRE(aligned(feats, 16) && aligned(dfeat_scratch, 16), NGLOD_ERR_ALIGN,
                   "feats and dfeat_scratch must be 16-byte aligned");
+    NGLOD_REQUIRE(!relu_masks || aligned(relu_masks, 16), NGLOD_ERR_ALIGN, "relu_masks must be 16-byte aligned");
     for (int l = 0; l <= L; ++l) {
         NGLOD_REQUIRE(grads->grid[l] && aligned(grads->grid[l], 16), NGLOD_ERR_INVALID,
                       "volume gradient %d is null or not 16-byte aligned", l);
@@ -480,14 +815,24 @@ extern "C" int nglod_sdf_bwd(const nglod_dense_model *model, const float *x, int
     a.L = L;
     a.gpred = grad_preds;
     a.feats = feats;
+    a.relu = relu_masks;
     a.dfeat = dfeat_scratch;
     a.gx = grad_x;
 
-    const size_t smem1 = bwd_decoder_smem(model->hidden_dim);
-    NGLOD_TRY(prepare_smem(sdf_bwd_decoder_kernel, smem1));
-    const int64_t tiles = (n + kBP - 1) / kBP;
-    const int64_t cap1 = resident_blocks(sdf_bwd_decoder_kernel, kBThreads, smem1);
-    sdf_bwd_decoder_kernel<<<(int)(tiles < cap1 ? tiles : cap1), kBThreads, smem1, (cudaStream_t)stream>>>(a);
+    if (model->hidden_dim == bwdtc::kH && relu_masks) {
+        // tensor-core form: one block of 256 threads per SM
+        NGLOD_TRY(prepare_smem(sdf_bwd_decoder_tc_kernel, bwdtc::kSmem));
+        const int64_t tiles = (n + bwdtc::kTP - 1) / bwdtc::kTP;
+        const int64_t cap1 = num_sms();
+        sdf_bwd_decoder_tc_kernel<<<(int)(tiles < cap1 ? tiles : cap1), bwdtc::kThreads, bwdtc::kSmem,
+                                    (cudaStream_t)stream>>>(a);
+    } else {
+        const size_t smem1 = bwd_decoder_smem(model->hidden_dim);
+        NGLOD_TRY(prepare_smem(sdf_bwd_decoder_kernel, smem1));
+        const int64_t tiles = (n + kBP - 1) / kBP;
+        const int64_t cap1 = resident_blocks(sdf_bwd_decoder_kernel, kBThreads, smem1);
+        sdf_bwd_decoder_kernel<<<(int)(tiles < cap1 ? tiles : cap1), kBThreads, smem1, (cudaStream_t)stream>>>(a);
+    }
     NGLOD_TRY(launch_status("nglod_sdf_bwd (decoder)"));
 
     ScatterArgs s;
@@ -592,7 +937,8 @@ static int noalloc_scratch_address(float **out) {
 
 extern "C" int nglod_sdf_bwd_noalloc(const nglod_dense_model *model, const float *x, int64_t n,
                                      uint32_t lod_mask, const float *grad_preds, const float *feats,
-                                     const nglod_dense_grads *grads, float *grad_x, nglod_stream_t stream) {
+                                     const uint32_t *relu_masks, const nglod_dense_grads *grads, float *grad_x,
+                                     nglod_stream_t stream) {
     NGLOD_REQUIRE(model != nullptr && grads != nullptr, NGLOD_ERR_INVALID, "model or grads is null");
     const int L = lod_mask_top(lod_mask);
     NGLOD_REQUIRE(L >= 0 && L < model->num_lods && (lod_mask >> NGLOD_MAX_LODS) == 0, NGLOD_ERR_INVALID,
@@ -610,5 +956,15 @@ extern "C" int nglod_sdf_bwd_noalloc(const nglod_dense_model *model, const float
     if (n == 0) return NGLOD_OK;
     float *scratch = nullptr;
     NGLOD_TRY(noalloc_scratch_address(&scratch));
-    return nglod_sdf_bwd(model, x, n, lod_mask, grad_preds, feats, scratch, grads, grad_x, stream);
+    return nglod_sdf_bwd(model, x, n, lod_mask, grad_preds, feats, relu_masks, scratch, grads, grad_x, stream);
+}
+
+extern "C" int nglod_train_status(int32_t *status_out) {
+    NGLOD_REQUIRE(status_out != nullptr, NGLOD_ERR_INVALID, "null pointer argument");
+    int32_t v = 0;
+    const int32_t zero = 0;
+    NGLOD_TRY(cuda_status(cudaMemcpyFromSymbol(&v, g_train_status, sizeof(v)), "nglod_train_status: read"));
+    NGLOD_TRY(cuda_status(cudaMemcpyToSymbol(g_train_status, &zero, sizeof(zero)), "nglod_train_status: reset"));
+    *status_out = v;
+    return NGLOD_OK;
 }

@@ -11,6 +11,7 @@ import ctypes
 import torch
 
 from . import _lib
+from .autograd import check_backward_status
 
 
 class FusedAdam(torch.optim.Optimizer):
@@ -114,4 +115,5 @@ def fit(net, batches, steps, lr=1e-3, loss_lods=None, seed=0, log_every=500):
         l = step_geometry(net, opt, xb[perm], gb[perm], loss_lods)
         if it % log_every == 0 or it == steps - 1:
             losses.append(float(l.item()))
+    check_backward_status()
     return opt, losses

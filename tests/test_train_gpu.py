@@ -6,6 +6,7 @@ import torch
 
 import nglod_gb300 as ng
 from nglod_gb300 import synthetic, trainer
+from nglod_gb300.autograd import check_backward_status
 from oracle import dense
 from tests.helpers import model_from_fixture, oracle_model, seeded_model
 
@@ -37,6 +38,7 @@ def test_backward_matches_reference_autograd(golden, cuda):
         err = np.abs(g - ref).max() / scale
         assert err < 1e-4, (k, err)
     assert set(got) == {k[len("grad/"):] for k in fx if k.startswith("grad/")}
+    check_backward_status()
 
 
 def test_return_lst_backward_equals_separate_calls(cuda):
@@ -168,3 +170,62 @@ def test_training_reduces_loss(cuda):
         losses.append(trainer.step_geometry(net, opt, x.to(cuda), g.to(cuda)).item())
     assert np.isfinite(losses).all()
     assert losses[-1] < 0.5 * losses[0], losses[::10]
+
+
+def _torch_reference_grads(net, x, gts, lods):
+    """Plain PyTorch fp32 on the GPU (grid_sample + Linear + autograd, TF32
+    off) of the same loss: sum over `lods` of ((sdf_l - gts)^2).sum() / n."""
+    import torch.nn.functional as F
+    assert not torch.backends.cuda.matmul.allow_tf32
+    fms = [fv.fm.detach().clone().contiguous().requires_grad_(True) for fv in net.features]
+    decs = [[p.detach().clone().requires_grad_(True) for p in (d[0].weight, d[0].bias, d[2].weight, d[2].bias)]
+            for d in net.louts]
+    n = x.shape[0]
+    acc, loss = None, 0.0
+    for i in range(max(lods) + 1):
+        s = F.grid_sample(fms[i], x.reshape(1, n, 1, 1, 3), align_corners=True,
+                          padding_mode="border")[0, :, :, 0, 0].transpose(0, 1)
+        acc = s if acc is None else acc + s
+        if i in lods:
+            w0, b0, w1, b1 = decs[i]
+            d = F.linear(F.relu(F.linear(torch.cat([x, acc], -1), w0, b0)), w1, b1)
+            loss = loss + ((d - gts) ** 2).sum()
+    (loss / n).backward()
+    out = {f"features.{i}.fm": fms[i].grad for i in range(len(fms))}
+    for i, d in enumerate(decs):
+        for name, p in zip(("0.weight", "0.bias", "2.weight", "2.bias"), d):
+            out[f"louts.{i}.{name}"] = p.grad
+    return out
+
+
+@pytest.mark.parametrize("hidden,lods,n", [(128, [0, 1, 2, 3, 4], 100_003), (128, [1, 3], 40_000),
+                                           (128, [4], 131), (64, [0, 2, 4], 30_001)])
+def test_backward_matches_torch_fp32_at_size(cuda, hidden, lods, n):
+    """The backward (tensor-core decoder part at hidden 128, float32 tile
+    reductions otherwise) against PyTorch fp32 autograd on the GPU, with many
+    tiles per block, a ragged last tile and LOD masks with gaps.  Bar: max
+    |g - ref| / max |ref| < 1e-4 per tensor (the bf16 hi / lo products are
+    good to about 2^-16 relative)."""
+    from nglod_gb300.options import default_args
+    torch.manual_seed(5)
+    net = ng.OctreeSDF(default_args(num_lods=5, base_lod=2, hidden_dim=hidden)).to(cuda).train()
+    with torch.no_grad():
+        for fv in net.features:
+            fv.fm.normal_(0.0, 0.05)
+    c, r = synthetic.sphere_union(1)
+    x, gts = synthetic.training_batch(n, c, r, seed=11)
+    x, gts = x.to(cuda), gts.to(cuda)
+    ref = _torch_reference_grads(net, x, gts, lods)
+    net.zero_grad()
+    preds = net.sdf(x, return_lst=True)
+    trainer.l2_loss(preds, gts, lods, n).backward()
+    check_backward_status()
+    params = dict(net.named_parameters())
+    for k, want in ref.items():
+        got = params[k].grad
+        scale = 0.0 if want is None else want.abs().max().item()
+        if scale == 0.0:
+            assert got is None or got.abs().max().item() == 0.0, k
+            continue
+        err = (got - want).abs().max().item() / scale
+        assert err < 1e-4, (k, err)

@@ -33,11 +33,12 @@ def _forward(net, n, mask, seed, dev):
     m = net.dense_model()
     preds = torch.zeros(L + 1, n, device=dev)
     feats = torch.empty(L + 1, n, 32, device=dev)
+    relu = torch.empty(L + 1, n, 4, device=dev, dtype=torch.int32)
     lib = _lib.load()
-    _lib.check(lib.nglod_sdf_fwd_train(m, _lib.ptr(x), n, mask, _lib.ptr(preds), _lib.ptr(feats),
+    _lib.check(lib.nglod_sdf_fwd_train(m, _lib.ptr(x), n, mask, _lib.ptr(preds), _lib.ptr(feats), _lib.ptr(relu),
                                        _lib.stream_ptr(dev)), "nglod_sdf_fwd_train")
     gp = (torch.randn(L + 1, n, generator=g) * 1e-2).to(dev)
-    return x, m, preds, feats, gp
+    return x, m, preds, feats, relu, gp
 
 
 def _grad_buffers(net, mask):
@@ -55,33 +56,38 @@ def _grad_buffers(net, mask):
     return g, bufs
 
 
-def _run(net, x, m, feats, gp, mask, noalloc):
+def _run(net, x, m, feats, relu, gp, mask, noalloc):
     dev = x.device
     n = x.shape[0]
     g, bufs = _grad_buffers(net, mask)
     gx = torch.zeros(n, 3, device=dev)
     lib = _lib.load()
     if noalloc:
-        st = lib.nglod_sdf_bwd_noalloc(m, _lib.ptr(x), n, mask, _lib.ptr(gp), _lib.ptr(feats), g, _lib.ptr(gx),
-                                       _lib.stream_ptr(dev))
+        st = lib.nglod_sdf_bwd_noalloc(m, _lib.ptr(x), n, mask, _lib.ptr(gp), _lib.ptr(feats), _lib.ptr(relu), g,
+                                       _lib.ptr(gx), _lib.stream_ptr(dev))
     else:
         scratch = torch.empty_like(feats)
-        st = lib.nglod_sdf_bwd(m, _lib.ptr(x), n, mask, _lib.ptr(gp), _lib.ptr(feats), _lib.ptr(scratch), g,
-                               _lib.ptr(gx), _lib.stream_ptr(dev))
+        st = lib.nglod_sdf_bwd(m, _lib.ptr(x), n, mask, _lib.ptr(gp), _lib.ptr(feats), _lib.ptr(relu),
+                               _lib.ptr(scratch), g, _lib.ptr(gx), _lib.stream_ptr(dev))
     _lib.check(st, "nglod_sdf_bwd_noalloc" if noalloc else "nglod_sdf_bwd")
     torch.cuda.synchronize()
     bufs["x"] = gx
     return {k: v.cpu().numpy() for k, v in bufs.items()}
 
 
-def test_noalloc_backward_matches_allocating_backward_twice(cuda):
+@pytest.mark.parametrize("with_masks", [True, False])
+def test_noalloc_backward_matches_allocating_backward_twice(cuda, with_masks):
+    """with_masks: the tensor-core decoder backward (forward ReLU masks);
+    without: the float32 one."""
     net = seeded_model(num_lods=5, base_lod=2, seed=21).to(cuda)
     # Two calls in a row: a large 5-LOD batch, then a smaller 3-LOD batch on
     # other points, so the second call starts from the first call's scratch.
     for n, mask, seed in [(20_000, 0b11111, 1), (7_001, 0b00111, 2)]:
-        x, m, preds, feats, gp = _forward(net, n, mask, seed, cuda)
-        want = _run(net, x, m, feats, gp, mask, noalloc=False)
-        got = _run(net, x, m, feats, gp, mask, noalloc=True)
+        x, m, preds, feats, relu, gp = _forward(net, n, mask, seed, cuda)
+        if not with_masks:
+            relu = None
+        want = _run(net, x, m, feats, relu, gp, mask, noalloc=False)
+        got = _run(net, x, m, feats, relu, gp, mask, noalloc=True)
         assert set(got) == set(want)
         for k in want:
             scale = np.abs(want[k]).max()
@@ -97,7 +103,7 @@ def test_noalloc_refuses_batches_beyond_its_array(cuda):
     g, _ = _grad_buffers(net, 0b11111)
     n = (16 << 20) // (5 * 32 * 4) + 1  # one point more than 5 LODs x 32 floats fit in 16 MiB
     dummy = torch.zeros(4, device=cuda)
-    st = lib.nglod_sdf_bwd_noalloc(m, _lib.ptr(dummy), n, 0b11111, _lib.ptr(dummy), _lib.ptr(dummy), g, None,
+    st = lib.nglod_sdf_bwd_noalloc(m, _lib.ptr(dummy), n, 0b11111, _lib.ptr(dummy), _lib.ptr(dummy), None, g, None,
                                    _lib.stream_ptr(cuda))
     assert st == -4
     msg = lib.nglod_last_error().decode()
