@@ -226,7 +226,7 @@ int nglod_sdf_fwd_train(const nglod_dense_model *model, const float *x, int64_t 
  * nn.Linear and F.grid_sample (border padding, align_corners) that
  * Trainer.step_geometry runs (sdf-net/lib/trainer.py:339).  With
  * hidden_dim 128 and the forward's relu_masks, the decoder part runs on
- * tcgen05 tensor cores (three products per 128-point tile, each as three
+ * tcgen05 tensor cores (two products per 128-point tile, each as three
  * bf16 MMAs over hi / lo splits, fp32 accumulation: relative error about
  * 2^-16 per product, ReLU derivative from relu_masks); otherwise (relu_masks
  * NULL, or other widths) float32 tile reductions that recompute the hidden

@@ -252,39 +252,47 @@ __global__ void __launch_bounds__(kBThreads, 2) sdf_bwd_decoder_kernel(const Bwd
 }
 
 // ---------------------------------------------------------------------------
-// backward 1, tensor-core form (hidden_dim 128): three GEMMs per 128-point
-// tile on tcgen05, each product as three bf16 MMAs over hi / lo splits
-// (a*b ~ ah*bh + ah*bl + al*bh, relative error about 2^-16 before the fp32
-// accumulation), accumulators in TMEM:
-//   P   [128 pts x 128 hid] = IN [pts x 48] . W^T          (TMEM cols 0..127)
-//   dIN [128 pts x 48]      = dH [pts x 128 hid] . W        (cols 128..175)
-//   dW  [128 hid x 48]     += dH^T [hid x pts] . IN         (cols 192..239,
-//                              summed over all tiles of a LOD)
-// IN row of a point: x y z, the 32 summed features, 1 (the b0 column),
-// zeros; W row j: w0[j][0..34], b0[j], zeros; dH = (P > 0) * g * w1.
-// Each shared tile is written once in the K-major core-matrix layout and
-// read by the second product with an MN-major descriptor (the same 8 x 16 B
-// core matrices: for a no-swizzle MN-major operand LBO is the stride between
-// K-adjacent core matrices and SBO the stride between MN-adjacent ones).
-// dw1[j] = sum_pts g * relu(P) and db1 = sum g stay in registers per thread
-// across tiles and are reduced once per LOD.
+// backward 1, tensor-core form (hidden_dim 128, forward ReLU masks given).
+// With mask[q][j] = (hidden unit j of point q was positive in the forward)
+// and g[q] = dLoss/dpred, the decoder's backward is
+//   dh[q][j]  = g[q] mask[q][j] w1[j]
+//   dIN[q][c] = sum_j dh[q][j] W[j][c]  = sum_j M[q][j] W1[j][c]
+//   dW[j][c]  = sum_q dh[q][j] IN[q][c] = w1[j] E[j][c]
+//   dw1[j]    = sum_q g[q] relu(P[q][j]) = sum_c W[j][c] E[j][c]
+// with M[q][j] = g[q] mask[q][j], W1[j][c] = w1[j] W[j][c] and
+// E[j][c] = sum_q M[q][j] IN[q][c]; IN row of a point = x y z, the 32
+// summed features, 1 (the b0 column), zeros; W row j = w0[j][0..34], b0[j].
+// So per 128-point tile two products run on tcgen05, each as three bf16
+// MMAs over hi / lo splits (a*b ~ ah*bh + ah*bl + al*bh, relative error
+// about 2^-16 before the fp32 accumulation in TMEM):
+//   dIN [128 pts x 48]  = M [pts x 128 hid] . W1          (TMEM cols 0..47)
+//   E   [128 hid x 48] += M^T [hid x pts] . IN            (cols 64..111,
+//                         summed over all tiles of a LOD)
+// and the hidden layer is never recomputed.  M and IN tiles are written
+// once in the K-major core-matrix layout and read by the second product
+// through MN-major descriptors (the same 8 x 16 B core matrices: for a
+// no-swizzle MN-major operand LBO is the stride between K-adjacent core
+// matrices and SBO the stride between MN-adjacent ones).  Both are double
+// buffered: the next tile's rows (its feature sums staged by cp.async) are
+// written while the tensor core works on this tile's.
 // ---------------------------------------------------------------------------
 namespace bwdtc {
 constexpr int kTP = 128, kH = 128, kK1 = 48, kKC1 = kK1 / 8, kKCH = kH / 8;
 constexpr int kThreads = 256;
 constexpr uint32_t kInBytes = kTP * kK1 * 2;   // 12 KB
 constexpr uint32_t kWBytes = kH * kK1 * 2;     // 12 KB
-constexpr uint32_t kDhBytes = kTP * kH * 2;    // 32 KB
-constexpr size_t kInH = 0, kInL = kInH + kInBytes, kWH = kInL + kInBytes, kWL = kWH + kWBytes;
-constexpr size_t kDH = kWL + kWBytes, kDL = kDH + kDhBytes;
-constexpr size_t kW1 = kDL + kDhBytes;          // w1 [128] f32
-constexpr size_t kDw1 = kW1 + kH * 4;           // dw1 LOD totals [128] f32
-constexpr size_t kBar = kDw1 + kH * 4;
-constexpr size_t kSlot = kBar + 8, kAbort = kSlot + 4;
+constexpr uint32_t kMBytes = kTP * kH * 2;     // 32 KB
+constexpr size_t kIn = 0;                      // IN: buffer b hi at kIn + 2b * kInBytes, lo after it
+constexpr size_t kM = kIn + 4 * kInBytes;      // M: buffer b hi at kM + 2b * kMBytes, lo after it
+constexpr size_t kWH = kM + 4 * kMBytes, kWL = kWH + kWBytes;  // W1 hi / lo
+constexpr size_t kStage = kWL + kWBytes;       // next tile's feature sums [128][32] f32
+constexpr size_t kStageX = kStage + kTP * 32 * 4;  // and positions [128][3] f32
+constexpr size_t kBarD = kStageX + kTP * 3 * 4;
+constexpr size_t kSlot = kBarD + 8, kAbort = kSlot + 4;
 constexpr size_t kSmem = kAbort + 12;
-constexpr uint32_t kColP = 0, kColDin = 128, kColDw = 192, kCols = 256;
+constexpr uint32_t kColDin = 0, kColE = 64, kCols = 128;
 constexpr uint32_t kPolls = 1u << 22;
-static_assert(kDH % 1024 == 0 && kBar % 8 == 0, "shared layout alignment");
+static_assert(kM % 1024 == 0 && kWH % 1024 == 0 && kBarD % 8 == 0, "shared layout alignment");
 static_assert(kSmem <= 227 * 1024, "shared layout fits one block");
 }  // namespace bwdtc
 
@@ -314,8 +322,8 @@ __device__ __forceinline__ float in_column(int c, const float (&xf)[3], const fl
 // Columns 24 HALF .. 24 HALF + 23 of IN row r (hi and lo tiles); rows of
 // points past the end are zero.
 template <int HALF>
-__device__ __forceinline__ void fill_in_row(uint8_t *smem, int r, const float (&xf)[3], const float4 (&fr)[8],
-                                            bool valid) {
+__device__ __forceinline__ void fill_in_row(uint8_t *in_hi, uint8_t *in_lo, int r, const float (&xf)[3],
+                                            const float4 (&fr)[8], bool valid) {
 #pragma unroll
     for (int cc = 0; cc < 3; ++cc) {
         const int c0 = HALF * 24 + cc * 8;
@@ -327,51 +335,119 @@ __device__ __forceinline__ void fill_in_row(uint8_t *smem, int r, const float (&
             split_bf16x2(v0, v1, h[k], lo[k]);
         }
         const uint32_t off = tc::tile_offset(r, c0, bwdtc::kKC1);
-        *reinterpret_cast<uint4 *>(smem + bwdtc::kInH + off) = make_uint4(h[0], h[1], h[2], h[3]);
-        *reinterpret_cast<uint4 *>(smem + bwdtc::kInL + off) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
+        *reinterpret_cast<uint4 *>(in_hi + off) = make_uint4(h[0], h[1], h[2], h[3]);
+        *reinterpret_cast<uint4 *>(in_lo + off) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
     }
 }
 
-// Thread 0 issues the three-term product D (+)= A . B over `ksteps` K steps
-// of 16 (A, B descriptors advanced by a_step / b_step bytes per step).
-__device__ __forceinline__ void mma3(uint32_t d, const uint32_t (&a)[2], const uint32_t (&b)[2], uint32_t a_lbo,
-                                     uint32_t a_sbo, uint32_t a_step, uint32_t b_lbo, uint32_t b_sbo,
-                                     uint32_t b_step, int ksteps, uint32_t idesc, bool accumulate) {
-    const int ta[3] = {0, 0, 1}, tb[3] = {0, 1, 0};  // hi.hi, hi.lo, lo.hi
-#pragma unroll 1
-    for (int t = 0; t < 3; ++t)
-#pragma unroll 1
-        for (int ks = 0; ks < ksteps; ++ks) {
-            const uint64_t ad = tc::smem_desc(a[ta[t]] + ks * a_step, a_lbo, a_sbo);
-            const uint64_t bd = tc::smem_desc(b[tb[t]] + ks * b_step, b_lbo, b_sbo);
-            tc::mma_bf16(d, ad, bd, idesc, (accumulate || t > 0 || ks > 0) ? 1u : 0u);
+__device__ __forceinline__ void cp_async16(void *dst, const void *src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(tc::smem_addr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async4(void *dst, const void *src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(tc::smem_addr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// Starts the copies of `tile`'s feature sums and positions into the staging
+// rows: thread (r, half) copies float4s 4 half .. 4 half + 3 of row r, and
+// half 0 the row's x y z.  Rows past the end are not copied.
+__device__ __forceinline__ void stage_tile(const BwdArgs &a, int l, int64_t tile, uint8_t *smem, int tid) {
+    using namespace bwdtc;
+    const int r = tid & (kTP - 1), half = tid >> 7;
+    const int64_t q = tile * kTP + r;
+    if (q < a.n) {
+        const float4 *src = reinterpret_cast<const float4 *>(a.feats + ((int64_t)l * a.n + q) * kC);
+        float4 *dst = reinterpret_cast<float4 *>(smem + kStage) + r * 8;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) cp_async16(dst + 4 * half + k, src + 4 * half + k);
+        if (half == 0) {
+            float *dx = reinterpret_cast<float *>(smem + kStageX) + r * 3;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) cp_async4(dx + k, a.x + 3 * q + k);
         }
+    }
+    cp_async_commit();
 }
 
-// Commit and wait (thread 0); false if the bounded wait gave up.
-__device__ __forceinline__ bool commit_wait(uint64_t *bar, uint32_t &phase) {
-    tc::mma_commit(bar);
-    const bool ok = tc::mbar_wait_bounded(bar, phase, bwdtc::kPolls);
-    phase ^= 1u;
-    return ok;
+// IN rows of `tile` (staged by stage_tile, copies complete and visible) into
+// IN buffer `buf`: thread (r, half) fills columns 24 half .. 24 half + 23 of
+// row r.
+__device__ __forceinline__ void fill_in_tile(const BwdArgs &a, int64_t tile, uint8_t *smem, int buf, int tid) {
+    using namespace bwdtc;
+    const int r = tid & (kTP - 1), half = tid >> 7;
+    const bool valid = tile * kTP + r < a.n;
+    const float *sx = reinterpret_cast<const float *>(smem + kStageX) + r * 3;
+    const float xf[3] = {sx[0], sx[1], sx[2]};
+    float4 fr[8];
+    const float4 *sf = reinterpret_cast<const float4 *>(smem + kStage) + r * 8;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) fr[k] = sf[k];
+    uint8_t *hi = smem + kIn + (size_t)(2 * buf) * kInBytes, *lo = hi + kInBytes;
+    if (half == 0)
+        fill_in_row<0>(hi, lo, r, xf, fr, valid);
+    else
+        fill_in_row<1>(hi, lo, r, xf, fr, valid);
+}
+
+// M row `row` (columns 64 hf .. 64 hf + 63) of buffer `buf`: g where the
+// 64 mask bits `bits` are set, else 0, as bf16 hi / lo.
+__device__ __forceinline__ void fill_m_row(uint8_t *smem, int buf, int row, int hf, float g, uint2 bits) {
+    using namespace bwdtc;
+    const __nv_bfloat16 gh = __float2bfloat16_rn(g);
+    const __nv_bfloat16 gl = __float2bfloat16_rn(g - __bfloat162float(gh));
+    const uint32_t uh = *reinterpret_cast<const uint16_t *>(&gh), ul = *reinterpret_cast<const uint16_t *>(&gl);
+    uint8_t *mh = smem + kM + (size_t)(2 * buf) * kMBytes, *ml = mh + kMBytes;
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {  // 8 columns per 16-byte store
+        const uint32_t b8 = ((u < 4 ? bits.x : bits.y) >> (8 * (u & 3))) & 0xFFu;
+        uint32_t h[4], lo[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const uint32_t m0 = (b8 >> (2 * k)) & 1u, m1 = (b8 >> (2 * k + 1)) & 1u;
+            h[k] = (m0 ? uh : 0u) | (m1 ? uh << 16 : 0u);
+            lo[k] = (m0 ? ul : 0u) | (m1 ? ul << 16 : 0u);
+        }
+        const uint32_t off = tc::tile_offset(row, 64 * hf + 8 * u, kKCH);
+        *reinterpret_cast<uint4 *>(mh + off) = make_uint4(h[0], h[1], h[2], h[3]);
+        *reinterpret_cast<uint4 *>(ml + off) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
+    }
+}
+
+// Thread 0 issues the three-term product D (+)= A . B over KSTEPS K steps
+// of 16 (A, B descriptors advanced by a_step / b_step bytes per step); the
+// descriptors of hi and lo differ only in their start address.
+template <int KSTEPS>
+__device__ __forceinline__ void mma3(uint32_t d, uint32_t a_hi, uint32_t a_lo, uint32_t b_hi, uint32_t b_lo,
+                                     uint32_t a_lbo, uint32_t a_sbo, uint32_t a_step, uint32_t b_lbo,
+                                     uint32_t b_sbo, uint32_t b_step, uint32_t idesc, bool accumulate) {
+    const uint64_t ah = tc::smem_desc(a_hi, a_lbo, a_sbo), al = tc::smem_desc(a_lo, a_lbo, a_sbo);
+    const uint64_t bh = tc::smem_desc(b_hi, b_lbo, b_sbo), bl = tc::smem_desc(b_lo, b_lbo, b_sbo);
+#pragma unroll
+    for (int t = 0; t < 3; ++t)
+#pragma unroll
+        for (int ks = 0; ks < KSTEPS; ++ks) {
+            // start address >> 4 sits in the descriptor's low bits
+            const uint64_t ad = (t == 2 ? al : ah) + (uint64_t)((ks * a_step) >> 4);
+            const uint64_t bd = (t == 1 ? bl : bh) + (uint64_t)((ks * b_step) >> 4);
+            tc::mma_bf16(d, ad, bd, idesc, (accumulate || t > 0 || ks > 0) ? 1u : 0u);
+        }
 }
 
 __global__ void __launch_bounds__(bwdtc::kThreads, 1) sdf_bwd_decoder_tc_kernel(const BwdArgs a) {
     using namespace bwdtc;
     extern __shared__ __align__(1024) uint8_t smem_tc[];
     uint8_t *smem = smem_tc;
-    float *w1s = reinterpret_cast<float *>(smem + kW1);
-    float *dw1s = reinterpret_cast<float *>(smem + kDw1);
-    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + kBar);
+    uint64_t *barD = reinterpret_cast<uint64_t *>(smem + kBarD);
     uint32_t *slot = reinterpret_cast<uint32_t *>(smem + kSlot);
     volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + kAbort);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int sp = warp & 3, hf = warp >> 2;  // TMEM lane quarter, column half
-    const int ql = sp * 32 + lane;            // tile row (point) of this thread's TMEM lane
+    const int ql = sp * 32 + lane;            // tile row (point, or hidden unit for E) of this thread's TMEM lane
 
     if (warp == 0) tc::tmem_alloc(slot, kCols);
     if (tid == 0) {
-        tc::mbar_init(bar, 1);
+        tc::mbar_init(barD, 1);
         *abort_flag = 0;
     }
     tc::fence_before_sync();
@@ -379,26 +455,25 @@ __global__ void __launch_bounds__(bwdtc::kThreads, 1) sdf_bwd_decoder_tc_kernel(
     tc::fence_after_sync();
     const uint32_t tmem = *slot;
     const uint32_t sbase = tc::smem_addr(smem);
-    const uint32_t in_t[2] = {sbase + (uint32_t)kInH, sbase + (uint32_t)kInL};
-    const uint32_t w_t[2] = {sbase + (uint32_t)kWH, sbase + (uint32_t)kWL};
-    const uint32_t dh_t[2] = {sbase + (uint32_t)kDH, sbase + (uint32_t)kDL};
-    const uint32_t id1 = tc::idesc_bf16_f32(kTP, kH);
     const uint32_t id2 = tc::idesc_bf16_f32(kTP, kK1) | (1u << 16);              // B MN-major
     const uint32_t id3 = tc::idesc_bf16_f32(kH, kK1) | (1u << 15) | (1u << 16);  // A, B MN-major
     const uint32_t trow = (uint32_t)(sp * 32) << 16;
-    uint32_t phase = 0;
+    uint32_t phD = 0;
 
 #pragma unroll 1
     for (int l = 0; l <= a.L && !*abort_flag; ++l) {
         if (!((a.mask >> l) & 1u)) continue;
-        // stage W (hi / lo) and w1 for this LOD
+        int64_t tile = blockIdx.x;
+        if (tile * kTP >= a.n) continue;
+        // W1 = w1[j] * W[j][c] (hi / lo) for this LOD, and the first tile's rows
         for (int u = tid; u < kH * kKC1; u += kThreads) {
             const int j = u / kKC1, cc = u % kKC1;
+            const float w1j = a.m.w1[l][j];
             float v[8];
 #pragma unroll
             for (int k = 0; k < 8; ++k) {
                 const int c = cc * 8 + k;
-                v[k] = c < 35 ? a.m.w0[l][j * 35 + c] : c == 35 ? a.m.b0[l][j] : 0.f;
+                v[k] = w1j * (c < 35 ? a.m.w0[l][j * 35 + c] : c == 35 ? a.m.b0[l][j] : 0.f);
             }
             uint32_t h[4], lo[4];
 #pragma unroll
@@ -407,109 +482,74 @@ __global__ void __launch_bounds__(bwdtc::kThreads, 1) sdf_bwd_decoder_tc_kernel(
             *reinterpret_cast<uint4 *>(smem + kWH + off) = make_uint4(h[0], h[1], h[2], h[3]);
             *reinterpret_cast<uint4 *>(smem + kWL + off) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
         }
-        if (tid < kH) {
-            w1s[tid] = a.m.w1[l][tid];
-            dw1s[tid] = 0.f;
-        }
-        float hg[64];  // sum over this thread's rows of g * relu(P) for columns 64 hf .. 64 hf + 63
-#pragma unroll
-        for (int i = 0; i < 64; ++i) hg[i] = 0.f;
         float gsum = 0.f;
-        bool first = true;
-        tc::fence_proxy_async_smem();
+        stage_tile(a, l, tile, smem, tid);
+        {
+            const int64_t qg = tile * kTP + ql;
+            float g = 0.f;
+            uint2 rm = make_uint2(0u, 0u);
+            if (qg < a.n) {
+                g = a.gpred[(int64_t)l * a.n + qg];
+                rm = reinterpret_cast<const uint2 *>(a.relu + ((int64_t)l * a.n + qg) * (kH / 32))[hf];
+            }
+            fill_m_row(smem, 0, ql, hf, g, rm);
+            if (hf == 0) gsum += g;
+        }
+        cp_async_wait_all();
         __syncthreads();
+        fill_in_tile(a, tile, smem, 0, tid);
+        bool first = true;
+        int buf = 0;
 
 #pragma unroll 1
-        for (int64_t tile = blockIdx.x; tile * kTP < a.n; tile += gridDim.x) {
-            // a. IN rows: thread (r, half) fills columns 24 half .. 24 half + 23 of row r
-            {
-                const int r = tid & (kTP - 1), half = tid >> 7;
-                const int64_t q = tile * kTP + r;
-                const bool valid = q < a.n;
-                float xf[3] = {0.f, 0.f, 0.f};
-                float4 fr[8];
-#pragma unroll
-                for (int k = 0; k < 8; ++k) fr[k] = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (valid) {
-                    xf[0] = a.x[3 * q];
-                    xf[1] = a.x[3 * q + 1];
-                    xf[2] = a.x[3 * q + 2];
-                    const float4 *src = reinterpret_cast<const float4 *>(a.feats + ((int64_t)l * a.n + q) * kC);
-#pragma unroll
-                    for (int k = 0; k < 8; ++k) fr[k] = src[k];
-                }
-                if (half == 0)
-                    fill_in_row<0>(smem, r, xf, fr, valid);
-                else
-                    fill_in_row<1>(smem, r, xf, fr, valid);
-            }
-            const int64_t qg = tile * kTP + ql;
-            const float g = qg < a.n ? a.gpred[(int64_t)l * a.n + qg] : 0.f;
+        for (; tile * kTP < a.n; tile += gridDim.x, buf ^= 1) {
+            const int64_t next = tile + gridDim.x;
+            const bool has_next = next * kTP < a.n;
+            // 1. rows of this tile are in buffer `buf`: dIN = M . W1, E += M^T . IN
             tc::fence_proxy_async_smem();
             tc::fence_before_sync();
             __syncthreads();
-            // b. P = IN . W^T
             if (tid == 0) {
                 tc::fence_after_sync();
-                mma3(tmem + kColP, in_t, w_t, 128, kKC1 * 128, 256, 128, kKC1 * 128, 256, kK1 / 16, id1, false);
-                if (!commit_wait(bar, phase)) {
-                    *abort_flag = 1;
-                    atomicExch(&g_train_status, 1);
-                }
+                const uint32_t mh = sbase + (uint32_t)(kM + 2 * buf * kMBytes), ml = mh + kMBytes;
+                const uint32_t ih = sbase + (uint32_t)(kIn + 2 * buf * kInBytes), il = ih + kInBytes;
+                mma3<kH / 16>(tmem + kColDin, mh, ml, sbase + (uint32_t)kWH, sbase + (uint32_t)kWL, 128, kKCH * 128,
+                              256, kKC1 * 128, 128, 2 * kKC1 * 128, id2, false);
+                mma3<kTP / 16>(tmem + kColE, mh, ml, ih, il, kKCH * 128, 128, 2 * kKCH * 128, kKC1 * 128, 128,
+                               2 * kKC1 * 128, id3, !first);
+                tc::mma_commit(barD);
             }
-            __syncthreads();
-            if (*abort_flag) break;
-            tc::fence_after_sync();
-            // c. dH rows and the dw1 / db1 sums: thread (sp, hf) row ql, columns
-            // 64 hf .. +63; the ReLU derivative is the forward's mask
-            uint2 rm = make_uint2(0u, 0u);
-            if (qg < a.n) rm = reinterpret_cast<const uint2 *>(a.relu + ((int64_t)l * a.n + qg) * (kH / 32))[hf];
-#pragma unroll
-            for (int k = 0; k < 2; ++k) {
-                const int j0 = 64 * hf + 32 * k;
-                const uint32_t bits = k == 0 ? rm.x : rm.y;
-                float v[32];
-                tc::tmem_load32(tmem + trow + kColP + (uint32_t)j0, v);
-                uint32_t h[16], lo[16];
-#pragma unroll
-                for (int i = 0; i < 16; ++i) {
-                    const float p0 = v[2 * i], p1 = v[2 * i + 1];
-                    hg[32 * k + 2 * i] = fmaf(g, fmaxf(p0, 0.f), hg[32 * k + 2 * i]);
-                    hg[32 * k + 2 * i + 1] = fmaf(g, fmaxf(p1, 0.f), hg[32 * k + 2 * i + 1]);
-                    const float d0 = ((bits >> (2 * i)) & 1u) ? g * w1s[j0 + 2 * i] : 0.f;
-                    const float d1 = ((bits >> (2 * i + 1)) & 1u) ? g * w1s[j0 + 2 * i + 1] : 0.f;
-                    split_bf16x2(d0, d1, h[i], lo[i]);
-                }
-#pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    const uint32_t off = tc::tile_offset(ql, j0 + 8 * u, kKCH);
-                    *reinterpret_cast<uint4 *>(smem + kDH + off) = make_uint4(h[4 * u], h[4 * u + 1], h[4 * u + 2], h[4 * u + 3]);
-                    *reinterpret_cast<uint4 *>(smem + kDL + off) =
-                        make_uint4(lo[4 * u], lo[4 * u + 1], lo[4 * u + 2], lo[4 * u + 3]);
-                }
-            }
-            if (hf == 0) gsum += g;
-            tc::fence_proxy_async_smem();
-            tc::fence_before_sync();
-            __syncthreads();
-            // d. dIN = dH . W and dW += dH^T . IN
-            if (tid == 0) {
-                tc::fence_after_sync();
-                mma3(tmem + kColDin, dh_t, w_t, 128, kKCH * 128, 256, kKC1 * 128, 128, 2 * kKC1 * 128, kH / 16, id2,
-                     false);
-                mma3(tmem + kColDw, dh_t, in_t, kKCH * 128, 128, 2 * kKCH * 128, kKC1 * 128, 128, 2 * kKC1 * 128,
-                     kTP / 16, id3, !first);
-                if (!commit_wait(bar, phase)) {
-                    *abort_flag = 1;
-                    atomicExch(&g_train_status, 1);
-                }
-            }
-            __syncthreads();
-            if (*abort_flag) break;
             first = false;
+            // 2. the next tile's rows into the other buffer while those run
+            if (has_next) {
+                stage_tile(a, l, next, smem, tid);
+                const int64_t qn = next * kTP + ql;
+                float g = 0.f;
+                uint2 rm = make_uint2(0u, 0u);
+                if (qn < a.n) {
+                    g = a.gpred[(int64_t)l * a.n + qn];
+                    rm = reinterpret_cast<const uint2 *>(a.relu + ((int64_t)l * a.n + qn) * (kH / 32))[hf];
+                }
+                fill_m_row(smem, buf ^ 1, ql, hf, g, rm);
+                if (hf == 0) gsum += g;
+                cp_async_wait_all();
+                __syncthreads();
+                fill_in_tile(a, next, smem, buf ^ 1, tid);
+            }
+            // 3. wait for the products, then dLoss/d(feature sum) and the
+            // decoder's dLoss/dx of row ql
+            if (tid == 0) {
+                if (!tc::mbar_wait_bounded(barD, phD, kPolls)) {
+                    *abort_flag = 1;
+                    atomicExch(&g_train_status, 1);
+                }
+                phD ^= 1u;
+            }
+            __syncthreads();
+            if (*abort_flag) break;
             tc::fence_after_sync();
-            // e. dLoss/d(feature sum) and the decoder's dLoss/dx of row ql
             {
+                const int64_t qg = tile * kTP + ql;
                 float v[32];
                 tc::tmem_load32(tmem + trow + kColDin + (uint32_t)(32 * hf), v);
                 if (qg < a.n) {
@@ -532,44 +572,46 @@ __global__ void __launch_bounds__(bwdtc::kThreads, 1) sdf_bwd_decoder_tc_kernel(
                     }
                 }
             }
-            tc::fence_before_sync();
-            __syncthreads();
         }
         if (*abort_flag) break;
-        // LOD totals: dW0 / db0 from TMEM rows (row j = ql), dw1 and db1 from registers
-        if (!first) {
-            tc::fence_after_sync();
+        // LOD totals from E (TMEM row j = ql): dW0 = w1 E, db0 = w1 E[:, 35],
+        // dw1 = sum_c W E; db1 = sum g
+        {
             float v[32];
-            tc::tmem_load32(tmem + trow + kColDw + (uint32_t)(32 * hf), v);
+            tc::tmem_load32(tmem + trow + kColE + (uint32_t)(32 * hf), v);
             const int j = ql;
+            const float w1j = a.m.w1[l][j];
+            const float *w0r = a.m.w0[l] + j * 35;
+            float dw1 = 0.f;
             if (hf == 0) {
 #pragma unroll 4
-                for (int c = 0; c < 32; ++c) atomicAdd(a.g.w0[l] + j * 35 + c, v[c]);
+                for (int c = 0; c < 32; ++c) {
+                    atomicAdd(a.g.w0[l] + j * 35 + c, w1j * v[c]);
+                    dw1 = fmaf(w0r[c], v[c], dw1);
+                }
             } else {
-                atomicAdd(a.g.w0[l] + j * 35 + 32, v[0]);
-                atomicAdd(a.g.w0[l] + j * 35 + 33, v[1]);
-                atomicAdd(a.g.w0[l] + j * 35 + 34, v[2]);
-                atomicAdd(a.g.b0[l] + j, v[3]);
-            }
 #pragma unroll
-            for (int i = 0; i < 64; ++i) {
-                float t = hg[i];
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-                if (lane == 0) atomicAdd(dw1s + 64 * hf + i, t);
+                for (int c = 0; c < 3; ++c) {
+                    atomicAdd(a.g.w0[l] + j * 35 + 32 + c, w1j * v[c]);
+                    dw1 = fmaf(w0r[32 + c], v[c], dw1);
+                }
+                atomicAdd(a.g.b0[l] + j, w1j * v[3]);
+                dw1 = fmaf(a.m.b0[l][j], v[3], dw1);
             }
+            atomicAdd(a.g.w1[l] + j, dw1);
             if (hf == 0) {
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) gsum += __shfl_xor_sync(0xffffffffu, gsum, o);
                 if (lane == 0) atomicAdd(a.g.b1[l], gsum);
             }
-            __syncthreads();
-            if (tid < kH) atomicAdd(a.g.w1[l] + tid, dw1s[tid]);
         }
         tc::fence_before_sync();
         __syncthreads();
     }
-    if (*abort_flag && tid == 0) tc::mbar_wait_bounded(bar, phase, kPolls);  // let an in-flight MMA finish
+    if (*abort_flag && tid == 0) {  // let in-flight MMAs finish before the columns are freed
+        tc::mma_commit(barD);
+        tc::mbar_wait_bounded(barD, phD, kPolls);
+    }
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();

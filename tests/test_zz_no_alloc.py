@@ -89,9 +89,15 @@ def test_noalloc_backward_matches_allocating_backward_twice(cuda, with_masks):
         want = _run(net, x, m, feats, relu, gp, mask, noalloc=False)
         got = _run(net, x, m, feats, relu, gp, mask, noalloc=True)
         assert set(got) == set(want)
+        gpn = gp.cpu().numpy()
         for k in want:
             scale = np.abs(want[k]).max()
             assert scale > 0, k
+            if k.startswith("b1"):
+                # db1 = sum of n random-sign dLoss/dpred values: the total is
+                # about sqrt(n) times smaller than the sum of its terms, so the
+                # atomic-order bound is taken against the sum of |terms|
+                scale = np.abs(gpn[int(k[2:])]).sum()
             err = np.abs(got[k] - want[k]).max() / scale
             assert err < REL_TOL, (n, k, err)
 
