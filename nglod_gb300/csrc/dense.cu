@@ -7,6 +7,10 @@ namespace nglod {
 // ---------------------------------------------------------------------------
 // sdf forward
 // ---------------------------------------------------------------------------
+// Each warp evaluates 32 points at a time (lane i owns point base + i): the
+// LOD sums are gathered cooperatively (gather_warp_add_f32), handed to the
+// point owners through a per-warp shared buffer placed after the staged
+// decoders, and each lane decodes its own point.
 template <bool kAll>
 __global__ void __launch_bounds__(256) sdf_fwd_f32_kernel(const nglod_dense_model m, const float *__restrict__ x,
                                                           int64_t n, int L, float *__restrict__ out) {
@@ -15,19 +19,36 @@ __global__ void __launch_bounds__(256) sdf_fwd_f32_kernel(const nglod_dense_mode
     const int dstride = decoder_f4(H);
     const int first = kAll ? 0 : L;
     for (int l = first; l <= L; ++l) stage_decoder(smem + (l - first) * dstride, m, l);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float *sT = reinterpret_cast<float *>(smem + (L - first + 1) * dstride) + warp * 32 * kTRow;
     __syncthreads();
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        const float px = x[3 * i], py = x[3 * i + 1], pz = x[3 * i + 2];
-        float f[kC];
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x + warp * 32; base < n; base += stride) {
+        const int64_t i = base + lane;
+        float px = 0.f, py = 0.f, pz = 0.f;
+        if (i < n) {
+            px = x[3 * i];
+            py = x[3 * i + 1];
+            pz = x[3 * i + 2];
+        }
+        float4 acc[8];
 #pragma unroll
-        for (int c = 0; c < kC; ++c) f[c] = 0.f;
+        for (int p = 0; p < 8; ++p) acc[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+        float f[kC];
 #pragma unroll 1
         for (int l = 0; l <= L; ++l) {
-            gather_add_f32(static_cast<const float *>(m.grid[l]), volume_side(m, l), px, py, pz, f);
-            if (kAll) out[(int64_t)l * n + i] = decode_f32(smem + l * dstride, H, px, py, pz, f);
+            gather_warp_add_f32(static_cast<const float *>(m.grid[l]), volume_side(m, l), px, py, pz, lane, acc);
+            if (kAll) {
+                warp_sums_to_points(sT, lane, acc, f);
+                const float o = decode_f32(smem + l * dstride, H, px, py, pz, f);
+                if (i < n) out[(int64_t)l * n + i] = o;
+            }
         }
-        if (!kAll) out[i] = decode_f32(smem, H, px, py, pz, f);
+        if (!kAll) {
+            warp_sums_to_points(sT, lane, acc, f);
+            const float o = decode_f32(smem, H, px, py, pz, f);
+            if (i < n) out[i] = o;
+        }
     }
 }
 
@@ -336,7 +357,9 @@ extern "C" int nglod_sdf_fwd(const nglod_dense_model *model, const float *x, int
     NGLOD_REQUIRE(x && out, NGLOD_ERR_INVALID, "null pointer argument");
     const int threads = 256;
     const int ndec = all_lods ? L + 1 : 1;
-    const size_t smem = (size_t)ndec * decoder_f4(model->hidden_dim) * sizeof(float4);
+    // staged decoders, then one [32][kTRow] float transpose buffer per warp
+    const size_t smem = (size_t)ndec * decoder_f4(model->hidden_dim) * sizeof(float4) +
+                        (size_t)threads * kTRow * sizeof(float);
     const int64_t want = (n + threads - 1) / threads;
     if (all_lods) {
         auto k = sdf_fwd_f32_kernel<true>;

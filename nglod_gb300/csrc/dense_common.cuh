@@ -102,9 +102,101 @@ __device__ __forceinline__ void gather_add_f32(const float *__restrict__ g, int 
     }
 }
 
+// Warp-cooperative form of gather_add_f32 for the warp's 32 points (lane i
+// owns point i's position).  Each lane computes its own point's corner set
+// (vertex index of corner 0, which neighbours are not clamped, the eight
+// weights); in pass p the eight lanes 8j .. 8j + 7 load the corners of
+// point 4p + j, one float4 (channels 4 (lane % 8) .. +3) each, fetching the
+// corner set by shuffles.  A load instruction then reads four whole 128-byte
+// vertices instead of 16 bytes of 32 different ones.  acc[p] += this lane's
+// four channels of point 4p + lane / 8, with gather_add_f32's arithmetic
+// (same weights, corners summed in the same order), so the sums are
+// identical.
+__device__ __forceinline__ void gather_warp_add_f32(const float *__restrict__ g, int s, float px, float py, float pz,
+                                                    int lane, float4 (&acc)[8]) {
+    const unsigned FULL = 0xffffffffu;
+    const float sm1 = (float)(s - 1);
+    float ix = ((px + 1.f) / 2.f) * sm1;
+    float iy = ((py + 1.f) / 2.f) * sm1;
+    float iz = ((pz + 1.f) / 2.f) * sm1;
+    ix = fminf(sm1, fmaxf(ix, 0.f));
+    iy = fminf(sm1, fmaxf(iy, 0.f));
+    iz = fminf(sm1, fmaxf(iz, 0.f));
+    const float x0 = floorf(ix), y0 = floorf(iy), z0 = floorf(iz);
+    const float wx1 = ix - x0, wx0 = (x0 + 1.f) - ix;
+    const float wy1 = iy - y0, wy0 = (y0 + 1.f) - iy;
+    const float wz1 = iz - z0, wz0 = (z0 + 1.f) - iz;
+    const int xi = (int)x0, yi = (int)y0, zi = (int)z0;
+    // vertex index < 513^3 < 2^28; bits 28..30: x / y / z neighbour not clamped
+    const uint32_t pk = (uint32_t)((zi * s + yi) * s + xi) | ((uint32_t)(xi + 1 < s) << 28) |
+                        ((uint32_t)(yi + 1 < s) << 29) | ((uint32_t)(zi + 1 < s) << 30);
+    float w[8];
+    w[0] = wx0 * wy0 * wz0;
+    w[1] = wx1 * wy0 * wz0;
+    w[2] = wx0 * wy1 * wz0;
+    w[3] = wx1 * wy1 * wz0;
+    w[4] = wx0 * wy0 * wz1;
+    w[5] = wx1 * wy0 * wz1;
+    w[6] = wx0 * wy1 * wz1;
+    w[7] = wx1 * wy1 * wz1;
+    const float4 *g4 = reinterpret_cast<const float4 *>(g) + (lane & 7);  // 8 float4 per vertex
+    const int sy = s * 8, sz = s * sy;
+#pragma unroll
+    for (int p = 0; p < 8; ++p) {
+        const int src = 4 * p + (lane >> 3);
+        const uint32_t q = __shfl_sync(FULL, pk, src);
+        float ws[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) ws[k] = __shfl_sync(FULL, w[k], src);
+        const int o0 = (int)(q & 0x0FFFFFFFu) * 8;
+        const int ox = ((q >> 28) & 1u) ? 8 : 0;
+        const int oy = ((q >> 29) & 1u) ? sy : 0;
+        const int oz = ((q >> 30) & 1u) ? sz : 0;
+        const int o[8] = {o0, o0 + ox, o0 + oy, o0 + oy + ox, o0 + oz, o0 + oz + ox, o0 + oz + oy, o0 + oz + oy + ox};
+        float4 v[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) v[k] = __ldg(g4 + o[k]);
+        float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            a0 = fmaf(v[k].x, ws[k], a0);
+            a1 = fmaf(v[k].y, ws[k], a1);
+            a2 = fmaf(v[k].z, ws[k], a2);
+            a3 = fmaf(v[k].w, ws[k], a3);
+        }
+        acc[p].x += a0;
+        acc[p].y += a1;
+        acc[p].z += a2;
+        acc[p].w += a3;
+    }
+}
+
+// Row stride (floats) of the per-warp transpose buffer: 36, so that the
+// float4 reads of eight consecutive rows fall in different banks.
+constexpr int kTRow = 36;
+
+// Hands the cooperative sums back to the point owners through the warp's
+// shared buffer sT [32][kTRow]: f = the 32 channels of point `lane`.
+__device__ __forceinline__ void warp_sums_to_points(float *sT, int lane, const float4 (&acc)[8], float (&f)[kC]) {
+#pragma unroll
+    for (int p = 0; p < 8; ++p)
+        *reinterpret_cast<float4 *>(sT + (4 * p + (lane >> 3)) * kTRow + 4 * (lane & 7)) = acc[p];
+    __syncwarp();
+#pragma unroll
+    for (int q = 0; q < kC / 4; ++q) {
+        const float4 v = *reinterpret_cast<const float4 *>(sT + lane * kTRow + 4 * q);
+        f[4 * q] = v.x;
+        f[4 * q + 1] = v.y;
+        f[4 * q + 2] = v.z;
+        f[4 * q + 3] = v.w;
+    }
+    __syncwarp();
+}
+
 // Linear(35, H) -> ReLU -> Linear(H, 1) on [p, f] with the staged decoder.
 // kMask: also store the ReLU mask (bit j of word j / 32 = hidden unit j was
-// positive) to mask_out[0 .. (H + 31) / 32 - 1].
+// positive) to mask_out[0 .. (H + 31) / 32 - 1] (nothing when mask_out is
+// null).
 template <bool kMask = false>
 __device__ __forceinline__ float decode_f32(const float4 *__restrict__ dec, int H, float px, float py,
                                             float pz, const float (&f)[kC], uint32_t *mask_out = nullptr) {
@@ -154,7 +246,7 @@ __device__ __forceinline__ float decode_f32(const float4 *__restrict__ dec, int 
         if (kMask) {
             bits |= ((uint32_t)(h0 > 0.f) << (j & 31)) | ((uint32_t)(h1 > 0.f) << ((j + 1) & 31));
             if (((j + 2) & 31) == 0 || j + 2 >= H) {
-                mask_out[j >> 5] = bits;
+                if (mask_out) mask_out[j >> 5] = bits;
                 bits = 0u;
             }
         }

@@ -28,33 +28,52 @@ constexpr int kBT = 128;  // points per backward tile = threads per block
 // ---------------------------------------------------------------------------
 // forward for training
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) sdf_fwd_train_kernel(const nglod_dense_model m, const float *__restrict__ x,
-                                                            int64_t n, int L, uint32_t mask,
-                                                            float *__restrict__ preds, float *__restrict__ feats,
-                                                            uint32_t *__restrict__ relu) {
+// Each warp evaluates 32 points at a time (lane i owns point base + i):
+// cooperative LOD gathers (gather_warp_add_f32); after each LOD in the mask
+// the running sums are written to feats straight from the cooperative layout
+// (four whole rows per store instruction), handed to the point owners
+// through the warp's shared buffer, and decoded by each lane.
+constexpr int kFwdTrainThreads = 512;  // 16 warps share the staged decoders of all LODs
+
+template <bool kRelu>
+__global__ void __launch_bounds__(kFwdTrainThreads, 1)
+    sdf_fwd_train_kernel(const nglod_dense_model m, const float *__restrict__ x, int64_t n, int L, uint32_t mask,
+                         float *__restrict__ preds, float *__restrict__ feats, uint32_t *__restrict__ relu) {
     extern __shared__ float4 smem[];
     const int H = m.hidden_dim;
     const int dstride = decoder_f4(H);
     for (int l = 0; l <= L; ++l)
         if ((mask >> l) & 1u) stage_decoder(smem + l * dstride, m, l);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float *sT = reinterpret_cast<float *>(smem + (L + 1) * dstride) + warp * 32 * kTRow;
     __syncthreads();
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        const float px = x[3 * i], py = x[3 * i + 1], pz = x[3 * i + 2];
-        float f[kC];
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x + warp * 32; base < n; base += stride) {
+        const int64_t i = base + lane;
+        float px = 0.f, py = 0.f, pz = 0.f;
+        if (i < n) {
+            px = x[3 * i];
+            py = x[3 * i + 1];
+            pz = x[3 * i + 2];
+        }
+        float4 acc[8];
 #pragma unroll
-        for (int c = 0; c < kC; ++c) f[c] = 0.f;
+        for (int p = 0; p < 8; ++p) acc[p] = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll 1
         for (int l = 0; l <= L; ++l) {
-            gather_add_f32(static_cast<const float *>(m.grid[l]), volume_side(m, l), px, py, pz, f);
+            gather_warp_add_f32(static_cast<const float *>(m.grid[l]), volume_side(m, l), px, py, pz, lane, acc);
             if ((mask >> l) & 1u) {
-                const int64_t row = (int64_t)l * n + i;
-                preds[row] = relu ? decode_f32<true>(smem + l * dstride, H, px, py, pz, f, relu + row * ((H + 31) / 32))
-                                  : decode_f32(smem + l * dstride, H, px, py, pz, f);
-                float4 *o = reinterpret_cast<float4 *>(feats + ((int64_t)l * n + i) * kC);
 #pragma unroll
-                for (int q = 0; q < kC / 4; ++q)
-                    o[q] = make_float4(f[4 * q], f[4 * q + 1], f[4 * q + 2], f[4 * q + 3]);
+                for (int p = 0; p < 8; ++p) {
+                    const int64_t ip = base + 4 * p + (lane >> 3);
+                    if (ip < n) reinterpret_cast<float4 *>(feats + ((int64_t)l * n + ip) * kC)[lane & 7] = acc[p];
+                }
+                float f[kC];
+                warp_sums_to_points(sT, lane, acc, f);
+                const int64_t row = (int64_t)l * n + i;
+                const float o = decode_f32<kRelu>(smem + l * dstride, H, px, py, pz, f,
+                                                  kRelu && i < n ? relu + row * ((H + 31) / 32) : nullptr);
+                if (i < n) preds[row] = o;
             }
         }
     }
@@ -815,13 +834,16 @@ extern "C" int nglod_sdf_fwd_train(const nglod_dense_model *model, const float *
     NGLOD_REQUIRE(x && preds && feats, NGLOD_ERR_INVALID, "null pointer argument");
     NGLOD_REQUIRE(aligned(feats, 16), NGLOD_ERR_ALIGN, "feats must be 16-byte aligned");
     NGLOD_REQUIRE(!relu_masks || aligned(relu_masks, 16), NGLOD_ERR_ALIGN, "relu_masks must be 16-byte aligned");
-    const int threads = 256;
-    const size_t smem = (size_t)(L + 1) * decoder_f4(model->hidden_dim) * sizeof(float4);
-    NGLOD_TRY(prepare_smem(sdf_fwd_train_kernel, smem));
+    const int threads = kFwdTrainThreads;
+    // staged decoders, then one [32][kTRow] float transpose buffer per warp
+    const size_t smem = (size_t)(L + 1) * decoder_f4(model->hidden_dim) * sizeof(float4) +
+                        (size_t)threads * kTRow * sizeof(float);
+    auto k = relu_masks ? sdf_fwd_train_kernel<true> : sdf_fwd_train_kernel<false>;
+    NGLOD_TRY(prepare_smem(k, smem));
     const int64_t want = (n + threads - 1) / threads;
-    const int64_t cap = resident_blocks(sdf_fwd_train_kernel, threads, smem);
-    sdf_fwd_train_kernel<<<(int)(want < cap ? want : cap), threads, smem, (cudaStream_t)stream>>>(
-        *model, x, n, L, lod_mask, preds, feats, relu_masks);
+    const int64_t cap = resident_blocks(k, threads, smem);
+    k<<<(int)(want < cap ? want : cap), threads, smem, (cudaStream_t)stream>>>(*model, x, n, L, lod_mask, preds,
+                                                                             feats, relu_masks);
     return launch_status("nglod_sdf_fwd_train");
 }
 
