@@ -167,7 +167,7 @@ struct TraceArgs {
 enum : int { kNeed = 0, kEvalInit = 1, kMarch = 2, kTap0 = 3, kDone = 9, kGone = 10 };
 
 // One thread owns one ray at a time and every loop iteration evaluates exactly
-// one sdf point per thread: the ray's first point, its next march point, or
+// one sdf point per thread (the warp gathers its 32 points cooperatively): the ray's first point, its next march point, or
 // one of the six finite-difference taps of its normal.  A thread whose ray
 // finishes writes it out and takes the next ray index from a global counter;
 // the lanes of a warp that need rays in the same iteration share one
@@ -181,6 +181,7 @@ enum : int { kNeed = 0, kEvalInit = 1, kMarch = 2, kTap0 = 3, kDone = 9, kGone =
 __global__ void __launch_bounds__(128) trace_f32_kernel(const TraceArgs a) {
     extern __shared__ float4 smem[];
     stage_decoder(smem, a.m, a.L);
+    float *sT = reinterpret_cast<float *>(smem + decoder_f4(a.m.hidden_dim)) + (threadIdx.x >> 5) * 32 * kTRow;
     __syncthreads();
 
     const unsigned FULL = 0xffffffffu;
@@ -279,7 +280,18 @@ __global__ void __launch_bounds__(128) trace_f32_kernel(const TraceArgs a) {
             else if ((k >> 1) == 1) qy = __fadd_rn(xy, e);
             else qz = __fadd_rn(xz, e);
         }
-        const float v = eval_point_f32(a.m, a.L, smem, qx, qy, qz);
+        // every lane of the warp is here: the LOD sums of the warp's 32
+        // points are gathered cooperatively, then each lane decodes its own
+        float4 acc[8];
+#pragma unroll
+        for (int p = 0; p < 8; ++p) acc[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll 1
+        for (int l = 0; l <= a.L; ++l)
+            gather_warp_add_f32(static_cast<const float *>(a.m.grid[l]), volume_side(a.m, l), qx, qy, qz, (int)lane,
+                                acc);
+        float f[kC];
+        warp_sums_to_points(sT, (int)lane, acc, f);
+        const float v = decode_f32(smem, a.m.hidden_dim, qx, qy, qz, f);
 
         if (phase == kEvalInit) {
             d = v;
@@ -418,7 +430,8 @@ extern "C" int nglod_trace(const nglod_dense_model *model, const nglod_trace_par
     a.normal = normal;
     a.counter = reinterpret_cast<unsigned long long *>(work_counter);
     const int threads = 128;
-    const size_t smem = (size_t)decoder_f4(model->hidden_dim) * sizeof(float4);
+    // staged decoder, then one [32][kTRow] float transpose buffer per warp
+    const size_t smem = (size_t)decoder_f4(model->hidden_dim) * sizeof(float4) + (size_t)threads * kTRow * sizeof(float);
     NGLOD_TRY(prepare_smem(trace_f32_kernel, smem));
     const int64_t want = (n + threads - 1) / threads;
     const int64_t cap = resident_blocks(trace_f32_kernel, threads, smem);

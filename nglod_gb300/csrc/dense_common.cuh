@@ -256,17 +256,6 @@ __device__ __forceinline__ float decode_f32(const float4 *__restrict__ dec, int 
 
 __device__ __forceinline__ int volume_side(const nglod_dense_model &m, int l) { return (1 << (l + m.base_lod)) + 1; }
 
-// Sum of the LOD 0..L samples at p, then decoder `dec`.
-__device__ __forceinline__ float eval_point_f32(const nglod_dense_model &m, int L, const float4 *dec, float px,
-                                                float py, float pz) {
-    float f[kC];
-#pragma unroll
-    for (int c = 0; c < kC; ++c) f[c] = 0.f;
-#pragma unroll 1
-    for (int l = 0; l <= L; ++l)
-        gather_add_f32(static_cast<const float *>(m.grid[l]), volume_side(m, l), px, py, pz, f);
-    return decode_f32(dec, m.hidden_dim, px, py, pz, f);
-}
 
 // ---------------------------------------------------------------------------
 // host helpers
