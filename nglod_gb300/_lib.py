@@ -197,6 +197,7 @@ SIGNATURES = {
                                    _vp, _vp, _vp, _vp, _vp, _vp]),
     "nglod_sdf_fwd_train": (ctypes.c_int, [ctypes.POINTER(DenseModel), _vp, _i64, _u32, _vp, _vp, _vp, _vp]),
     "nglod_train_status": (ctypes.c_int, [ctypes.POINTER(_i32)]),
+    "nglod_l2_loss": (ctypes.c_int, [_vp, _vp, _i64, _i32, _u32, _vp, _vp, _vp]),
     "nglod_sdf_bwd": (ctypes.c_int, [ctypes.POINTER(DenseModel), _vp, _i64, _u32, _vp, _vp, _vp, _vp,
                                      ctypes.POINTER(DenseGrads), _vp, _vp]),
     "nglod_sdf_bwd_noalloc": (ctypes.c_int, [ctypes.POINTER(DenseModel), _vp, _i64, _u32, _vp, _vp, _vp,

@@ -96,6 +96,15 @@ def train_params(net):
     return ps
 
 
+def sdf_train_stacked(net, x):
+    """Differentiable predictions of every LOD as one [num_lods, N, 1] tensor
+    (the rows sdf_train(net, x, None, True) returns as a list)."""
+    _lib.require_cuda(x, net.features[0].fm)
+    if x.dim() != 2 or x.shape[1] != 3:
+        raise NotImplementedError("OctreeSDF.sdf: only [N, 3] query points are supported")
+    return _SdfTrain.apply(x, (1 << net.num_lods) - 1, net, *train_params(net))
+
+
 def sdf_train(net, x, lod, all_lods):
     """Differentiable predictions: [N, 1] at `lod` (finest if None), or the
     list of every LOD's [N, 1] when all_lods."""

@@ -647,9 +647,16 @@ __device__ __forceinline__ void red_add_v4(float *addr, float a, float b, float 
 
 // Volumes below `smem_levels` are accumulated in shared memory (offsets in
 // floats given by soff[l]); the rest go straight to global memory.  A shared
-// vertex takes kSV = 33 floats: with 32 the channel-c atomics of all lanes
-// of a warp fell in bank c (32-way conflicts); with 33 lanes at different
-// vertices use different banks.
+// vertex takes kSV = 33 floats (32 channels and a pad word).
+//
+// Each warp handles 32 points at a time, cooperatively: the eight lanes
+// 8j .. 8j + 7 of pass p own channels 4 (lane % 8) .. +3 of point 4p + j.
+// A point's gradient G (suffix sum over the mask LODs l >= i of
+// dLoss/d(feature sum l)) is loaded as whole 128-byte rows, and each
+// corner's 32-channel update is one 128-byte vector reduction
+// (red.global.add.v4.f32 from eight lanes) or 32 consecutive shared-memory
+// atomics.  Corner sets come from the point's own lane by shuffles; the
+// weights are formed as (wx * wy) * wz, as in the forward.
 constexpr int kSV = kC + 1;
 struct ScatterArgs {
     BwdArgs a;
@@ -661,29 +668,43 @@ template <bool kGradX>
 __global__ void __launch_bounds__(256) sdf_bwd_scatter_kernel(const ScatterArgs s) {
     extern __shared__ float sacc[];
     const BwdArgs &a = s.a;
+    const unsigned FULL = 0xffffffffu;
     const int stot = s.soff[s.smem_levels];
     for (int i = threadIdx.x; i < stot; i += blockDim.x) sacc[i] = 0.f;
     __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, part = lane & 7;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < a.n; p += stride) {
-        const float px = a.x[3 * p], py = a.x[3 * p + 1], pz = a.x[3 * p + 2];
-        float G[kC];
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x + warp * 32; base < a.n; base += stride) {
+        const int64_t i = base + lane;
+        float px = 0.f, py = 0.f, pz = 0.f;
+        if (i < a.n) {
+            px = a.x[3 * i];
+            py = a.x[3 * i + 1];
+            pz = a.x[3 * i + 2];
+        }
+        float4 G[8];
+        float gxv[8][3];
 #pragma unroll
-        for (int c = 0; c < kC; ++c) G[c] = 0.f;
-        float gxx = 0.f, gxy = 0.f, gxz = 0.f;
+        for (int p = 0; p < 8; ++p) {
+            G[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+            gxv[p][0] = gxv[p][1] = gxv[p][2] = 0.f;
+        }
 #pragma unroll 1
         for (int l = a.L; l >= 0; --l) {
             if ((a.mask >> l) & 1u) {
-                const float4 *dr = reinterpret_cast<const float4 *>(a.dfeat + ((int64_t)l * a.n + p) * kC);
 #pragma unroll
-                for (int q = 0; q < kC / 4; ++q) {
-                    const float4 v = dr[q];
-                    G[4 * q] += v.x;
-                    G[4 * q + 1] += v.y;
-                    G[4 * q + 2] += v.z;
-                    G[4 * q + 3] += v.w;
+                for (int p = 0; p < 8; ++p) {
+                    const int64_t ip = base + 4 * p + (lane >> 3);
+                    if (ip < a.n) {
+                        const float4 v = reinterpret_cast<const float4 *>(a.dfeat + ((int64_t)l * a.n + ip) * kC)[part];
+                        G[p].x += v.x;
+                        G[p].y += v.y;
+                        G[p].z += v.z;
+                        G[p].w += v.w;
+                    }
                 }
             }
+            // this lane's own point: corner set at LOD l
             const int sd = volume_side(a.m, l);
             const float sm1 = (float)(sd - 1);
             const float rx = ((px + 1.f) / 2.f) * sm1;
@@ -693,84 +714,90 @@ __global__ void __launch_bounds__(256) sdf_bwd_scatter_kernel(const ScatterArgs 
             const float iy = fminf(sm1, fmaxf(ry, 0.f));
             const float iz = fminf(sm1, fmaxf(rz, 0.f));
             const float x0 = floorf(ix), y0 = floorf(iy), z0 = floorf(iz);
-            const float wx1 = ix - x0, wx0 = (x0 + 1.f) - ix;
-            const float wy1 = iy - y0, wy0 = (y0 + 1.f) - iy;
-            const float wz1 = iz - z0, wz0 = (z0 + 1.f) - iz;
+            const float wv[6] = {(x0 + 1.f) - ix, ix - x0, (y0 + 1.f) - iy, iy - y0, (z0 + 1.f) - iz, iz - z0};
             const int xi = (int)x0, yi = (int)y0, zi = (int)z0;
-            const int xj = min(xi + 1, sd - 1), yj = min(yi + 1, sd - 1), zj = min(zi + 1, sd - 1);
-            int cidx[8];
-            cidx[0] = (zi * sd + yi) * sd + xi;
-            cidx[1] = (zi * sd + yi) * sd + xj;
-            cidx[2] = (zi * sd + yj) * sd + xi;
-            cidx[3] = (zi * sd + yj) * sd + xj;
-            cidx[4] = (zj * sd + yi) * sd + xi;
-            cidx[5] = (zj * sd + yi) * sd + xj;
-            cidx[6] = (zj * sd + yj) * sd + xi;
-            cidx[7] = (zj * sd + yj) * sd + xj;
-            float w[8];
-            w[0] = wx0 * wy0 * wz0;
-            w[1] = wx1 * wy0 * wz0;
-            w[2] = wx0 * wy1 * wz0;
-            w[3] = wx1 * wy1 * wz0;
-            w[4] = wx0 * wy0 * wz1;
-            w[5] = wx1 * wy0 * wz1;
-            w[6] = wx0 * wy1 * wz1;
-            w[7] = wx1 * wy1 * wz1;
-            if (l < s.smem_levels) {
-                float *base = sacc + s.soff[l];
+            // vertex index < 2^28; bits 28..30: x / y / z neighbour not clamped
+            // (the clamp flags of dLoss/dx travel in `edge`)
+            const uint32_t pk = (uint32_t)((zi * sd + yi) * sd + xi) | ((uint32_t)(xi + 1 < sd) << 28) |
+                                ((uint32_t)(yi + 1 < sd) << 29) | ((uint32_t)(zi + 1 < sd) << 30);
+            const uint32_t edge = (uint32_t)(rx <= 0.f || rx >= sm1) | ((uint32_t)(ry <= 0.f || ry >= sm1) << 1) |
+                                  ((uint32_t)(rz <= 0.f || rz >= sm1) << 2);
+            const bool in_smem = l < s.smem_levels;
+            float *gbase = in_smem ? sacc + s.soff[l] : a.g.grid[l];
+            const int vstride = in_smem ? kSV : kC;
+            const float4 *fm = reinterpret_cast<const float4 *>(a.m.grid[l]);
 #pragma unroll
-                for (int k = 0; k < 8; ++k) {
-                    float *dst = base + cidx[k] * kSV;
+            for (int p = 0; p < 8; ++p) {
+                const int src = 4 * p + (lane >> 3);
+                const uint32_t q = __shfl_sync(FULL, pk, src);
+                float w6[6];
 #pragma unroll
-                    for (int c = 0; c < kC; ++c) atomicAdd(dst + c, G[c] * w[k]);
-                }
-            } else {
-                float *base = a.g.grid[l];
+                for (int k = 0; k < 6; ++k) w6[k] = __shfl_sync(FULL, wv[k], src);
+                const float w[8] = {w6[0] * w6[2] * w6[4], w6[1] * w6[2] * w6[4], w6[0] * w6[3] * w6[4],
+                                    w6[1] * w6[3] * w6[4], w6[0] * w6[2] * w6[5], w6[1] * w6[2] * w6[5],
+                                    w6[0] * w6[3] * w6[5], w6[1] * w6[3] * w6[5]};
+                const int v0 = (int)(q & 0x0FFFFFFFu);
+                const int ox = ((q >> 28) & 1u) ? 1 : 0;
+                const int oy = ((q >> 29) & 1u) ? sd : 0;
+                const int oz = ((q >> 30) & 1u) ? sd * sd : 0;
+                const int vtx[8] = {v0, v0 + ox, v0 + oy, v0 + oy + ox, v0 + oz, v0 + oz + ox, v0 + oz + oy, v0 + oz + oy + ox};
+                const bool valid = base + src < a.n;
+                if (valid) {
 #pragma unroll
-                for (int k = 0; k < 8; ++k) {
-                    float *dst = base + (size_t)cidx[k] * kC;
-#pragma unroll
-                    for (int q = 0; q < kC / 4; ++q)
-                        red_add_v4(dst + 4 * q, G[4 * q] * w[k], G[4 * q + 1] * w[k], G[4 * q + 2] * w[k],
-                                   G[4 * q + 3] * w[k]);
-                }
-            }
-            if (kGradX) {
-                // d(sample)/du per corner: -/+ the product of the other two axes' weights
-                // (PyTorch's grid_sampler_3d backward), times (s-1)/2, zero where clamped.
-                const float *g = static_cast<const float *>(a.m.grid[l]);
-                float dot[8];
-#pragma unroll
-                for (int k = 0; k < 8; ++k) {
-                    const float4 *v = reinterpret_cast<const float4 *>(g + (size_t)cidx[k] * kC);
-                    float sacc_k = 0.f;
-#pragma unroll
-                    for (int q = 0; q < kC / 4; ++q) {
-                        const float4 u = __ldg(v + q);
-                        sacc_k = fmaf(G[4 * q], u.x, sacc_k);
-                        sacc_k = fmaf(G[4 * q + 1], u.y, sacc_k);
-                        sacc_k = fmaf(G[4 * q + 2], u.z, sacc_k);
-                        sacc_k = fmaf(G[4 * q + 3], u.w, sacc_k);
+                    for (int k = 0; k < 8; ++k) {
+                        float *dst = gbase + (size_t)vtx[k] * vstride + 4 * part;
+                        if (in_smem) {
+                            atomicAdd(dst, G[p].x * w[k]);
+                            atomicAdd(dst + 1, G[p].y * w[k]);
+                            atomicAdd(dst + 2, G[p].z * w[k]);
+                            atomicAdd(dst + 3, G[p].w * w[k]);
+                        } else {
+                            red_add_v4(dst, G[p].x * w[k], G[p].y * w[k], G[p].z * w[k], G[p].w * w[k]);
+                        }
                     }
-                    dot[k] = sacc_k;
                 }
-                float gix = 0.f, giy = 0.f, giz = 0.f;
-                gix += -dot[0] * wy0 * wz0 + dot[1] * wy0 * wz0 - dot[2] * wy1 * wz0 + dot[3] * wy1 * wz0;
-                gix += -dot[4] * wy0 * wz1 + dot[5] * wy0 * wz1 - dot[6] * wy1 * wz1 + dot[7] * wy1 * wz1;
-                giy += -dot[0] * wx0 * wz0 - dot[1] * wx1 * wz0 + dot[2] * wx0 * wz0 + dot[3] * wx1 * wz0;
-                giy += -dot[4] * wx0 * wz1 - dot[5] * wx1 * wz1 + dot[6] * wx0 * wz1 + dot[7] * wx1 * wz1;
-                giz += -dot[0] * wx0 * wy0 - dot[1] * wx1 * wy0 - dot[2] * wx0 * wy1 - dot[3] * wx1 * wy1;
-                giz += dot[4] * wx0 * wy0 + dot[5] * wx1 * wy0 + dot[6] * wx0 * wy1 + dot[7] * wx1 * wy1;
-                const float half = sm1 / 2.f;
-                gxx += (rx <= 0.f || rx >= sm1) ? 0.f : gix * half;
-                gxy += (ry <= 0.f || ry >= sm1) ? 0.f : giy * half;
-                gxz += (rz <= 0.f || rz >= sm1) ? 0.f : giz * half;
+                if (kGradX) {
+                    // d(sample)/du per corner: -/+ the product of the other two axes' weights
+                    // (PyTorch's grid_sampler_3d backward), times (s-1)/2, zero where clamped.
+                    float dot[8];
+#pragma unroll
+                    for (int k = 0; k < 8; ++k) {
+                        const float4 u = __ldg(fm + (size_t)vtx[k] * (kC / 4) + part);
+                        float t = G[p].x * u.x;
+                        t = fmaf(G[p].y, u.y, t);
+                        t = fmaf(G[p].z, u.z, t);
+                        t = fmaf(G[p].w, u.w, t);
+                        t += __shfl_xor_sync(FULL, t, 1);
+                        t += __shfl_xor_sync(FULL, t, 2);
+                        t += __shfl_xor_sync(FULL, t, 4);
+                        dot[k] = t;
+                    }
+                    const float wx0 = w6[0], wx1 = w6[1], wy0 = w6[2], wy1 = w6[3], wz0 = w6[4], wz1 = w6[5];
+                    float gix = 0.f, giy = 0.f, giz = 0.f;
+                    gix += -dot[0] * wy0 * wz0 + dot[1] * wy0 * wz0 - dot[2] * wy1 * wz0 + dot[3] * wy1 * wz0;
+                    gix += -dot[4] * wy0 * wz1 + dot[5] * wy0 * wz1 - dot[6] * wy1 * wz1 + dot[7] * wy1 * wz1;
+                    giy += -dot[0] * wx0 * wz0 - dot[1] * wx1 * wz0 + dot[2] * wx0 * wz0 + dot[3] * wx1 * wz0;
+                    giy += -dot[4] * wx0 * wz1 - dot[5] * wx1 * wz1 + dot[6] * wx0 * wz1 + dot[7] * wx1 * wz1;
+                    giz += -dot[0] * wx0 * wy0 - dot[1] * wx1 * wy0 - dot[2] * wx0 * wy1 - dot[3] * wx1 * wy1;
+                    giz += dot[4] * wx0 * wy0 + dot[5] * wx1 * wy0 + dot[6] * wx0 * wy1 + dot[7] * wx1 * wy1;
+                    const float half = sm1 / 2.f;
+                    const uint32_t e = __shfl_sync(FULL, edge, src);
+                    gxv[p][0] += (e & 1u) ? 0.f : gix * half;
+                    gxv[p][1] += (e & 2u) ? 0.f : giy * half;
+                    gxv[p][2] += (e & 4u) ? 0.f : giz * half;
+                }
             }
         }
-        if (kGradX) {
-            a.gx[3 * p] += gxx;
-            a.gx[3 * p + 1] += gxy;
-            a.gx[3 * p + 2] += gxz;
+        if (kGradX && part == 0) {
+#pragma unroll
+            for (int p = 0; p < 8; ++p) {
+                const int64_t ip = base + 4 * p + (lane >> 3);
+                if (ip < a.n) {
+                    a.gx[3 * ip] += gxv[p][0];
+                    a.gx[3 * ip + 1] += gxv[p][1];
+                    a.gx[3 * ip + 2] += gxv[p][2];
+                }
+            }
         }
     }
     __syncthreads();
@@ -783,6 +810,43 @@ __global__ void __launch_bounds__(256) sdf_bwd_scatter_kernel(const ScatterArgs 
             const float *r = src + v * kSV + c;
             red_add_v4(dst + (size_t)v * kC + c, r[0], r[1], r[2], r[3]);
         }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// L2 loss of Trainer.step_geometry and its gradient in one pass
+// ---------------------------------------------------------------------------
+// preds [rows][n], gts [n]: loss = sum over l in mask, q of (preds - gts)^2
+// / n, accumulated in float64 (block partial sums, one double atomic per
+// block); grad[l][q] = 2 (preds - gts) / n for l in mask, else 0.
+__global__ void __launch_bounds__(256) l2_loss_kernel(const float *__restrict__ preds, const float *__restrict__ gts,
+                                                      int64_t n, int rows, uint32_t mask, double *loss,
+                                                      float *__restrict__ grad) {
+    __shared__ double part[8];
+    const float scale = 2.f / (float)n;
+    double acc = 0.0;
+    const int64_t total = (int64_t)rows * n;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += stride) {
+        const int l = (int)(e / n);
+        const int64_t q = e - (int64_t)l * n;
+        const bool on = (mask >> l) & 1u;
+        const float p = preds[e], g = gts[q];
+        if (on) {
+            const double d = (double)p - (double)g;
+            acc += d * d;
+        }
+        grad[e] = on ? (p - g) * scale : 0.f;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    const int warp = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) part[warp] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += part[w];
+        atomicAdd(loss, t / (double)n);
     }
 }
 
@@ -1031,4 +1095,21 @@ extern "C" int nglod_train_status(int32_t *status_out) {
     NGLOD_TRY(cuda_status(cudaMemcpyToSymbol(g_train_status, &zero, sizeof(zero)), "nglod_train_status: reset"));
     *status_out = v;
     return NGLOD_OK;
+}
+
+extern "C" int nglod_l2_loss(const float *preds, const float *gts, int64_t n, int32_t rows, uint32_t lod_mask,
+                             double *loss_out, float *grad_preds, nglod_stream_t stream) {
+    NGLOD_REQUIRE(n >= 0 && rows >= 1 && rows <= NGLOD_MAX_LODS, NGLOD_ERR_INVALID, "n=%lld rows=%d",
+                  (long long)n, rows);
+    NGLOD_REQUIRE(loss_out != nullptr, NGLOD_ERR_INVALID, "loss_out is null");
+    cudaStream_t s = (cudaStream_t)stream;
+    NGLOD_TRY(cuda_status(cudaMemsetAsync(loss_out, 0, sizeof(double), s), "nglod_l2_loss memset"));
+    if (n == 0) return NGLOD_OK;
+    NGLOD_REQUIRE(preds && gts && grad_preds, NGLOD_ERR_INVALID, "null pointer argument");
+    const int threads = 256;
+    const int64_t total = (int64_t)rows * n;
+    const int64_t want = (total + threads - 1) / threads, cap = (int64_t)num_sms() * 8;
+    l2_loss_kernel<<<(int)(want < cap ? want : cap), threads, 0, s>>>(preds, gts, n, rows, lod_mask, loss_out,
+                                                                      grad_preds);
+    return launch_status("nglod_l2_loss");
 }

@@ -11,13 +11,16 @@ import ctypes
 import torch
 
 from . import _lib
-from .autograd import check_backward_status
+from .autograd import check_backward_status, sdf_train_stacked
 
 
 class FusedAdam(torch.optim.Optimizer):
     def __init__(self, params, lr=1e-3, betas=(0.9, 0.999), eps=1e-8, weight_decay=0.0):
         super().__init__(params, dict(lr=lr, betas=betas, eps=eps, weight_decay=weight_decay))
-        self._tables = []  # device copies of recent step tables, kept alive until their kernels ran
+        # step tables go host -> device asynchronously through a ring of pinned
+        # buffers; an event per slot marks when its copy has been consumed
+        self._ring = []
+        self._ring_pos = 0
 
     @torch.no_grad()
     def step(self, closure=None):
@@ -57,17 +60,30 @@ class FusedAdam(torch.optim.Optimizer):
                 tab[i].param, tab[i].grad = p.data_ptr(), g.data_ptr()
                 tab[i].exp_avg, tab[i].exp_avg_sq = m.data_ptr(), v.data_ptr()
                 tab[i].numel = p.numel()
-            raw = torch.frombuffer(bytearray(bytes(tab)), dtype=torch.uint8)
-            dtab = raw.to(dev, non_blocking=False)
+            dtab = self._upload(tab, dev)
             b1, b2 = group["betas"]
             _lib.check(_lib.load().nglod_adam_step(ctypes.c_void_p(dtab.data_ptr()), len(entries),
                                                    max(p.numel() for p, *_ in entries), group["lr"], b1, b2,
                                                    group["eps"], group["weight_decay"], step_no,
                                                    _lib.stream_ptr(dev)), "nglod_adam_step")
-            self._tables.append(dtab)
-            if len(self._tables) > 8:
-                self._tables.pop(0)
+            self._ring[self._ring_pos - 1][2].record(torch.cuda.current_stream(dev))
         return loss
+
+    def _upload(self, tab, dev, slots=4):
+        """Device copy of the step table through the next pinned ring slot
+        (non-blocking; waits only if that slot's previous step has not run)."""
+        nbytes = ctypes.sizeof(tab)
+        if len(self._ring) < slots:
+            self._ring.append([None, None, torch.cuda.Event()])
+        slot = self._ring[self._ring_pos % len(self._ring)]
+        self._ring_pos = self._ring_pos % len(self._ring) + 1
+        slot[2].synchronize()
+        if slot[0] is None or slot[0].numel() < nbytes or slot[1].device != dev:
+            slot[0] = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+            slot[1] = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+        ctypes.memmove(slot[0].data_ptr(), ctypes.addressof(tab), nbytes)
+        slot[1][:nbytes].copy_(slot[0][:nbytes], non_blocking=True)
+        return slot[1]
 
 
 def _like(p, g):
@@ -85,17 +101,36 @@ def l2_loss(preds, gts, loss_lods, batch_size):
     return loss / batch_size
 
 
+def fused_l2_loss(preds, gts, loss_lods):
+    """l2_loss over stacked predictions [rows, n, 1] in one launch
+    (nglod_l2_loss): returns the loss (float64, 0-dim, on the device) and
+    its gradient with respect to preds."""
+    preds = preds.detach().contiguous()
+    gts = gts.detach().float().contiguous()
+    n = preds.shape[1]
+    mask = 0
+    for l in loss_lods:
+        mask |= 1 << l
+    loss = torch.empty((), dtype=torch.float64, device=preds.device)
+    grad = torch.empty_like(preds)
+    _lib.check(_lib.load().nglod_l2_loss(_lib.ptr(preds), _lib.ptr(gts), n, preds.shape[0], mask, _lib.ptr(loss),
+                                         _lib.ptr(grad), _lib.stream_ptr(preds.device)), "nglod_l2_loss")
+    return loss, grad
+
+
 def step_geometry(net, optimizer, pts, gts, loss_lods=None):
-    """One training step; returns the loss (float64, reduced on the GPU)."""
+    """One training step; returns the loss (float64, reduced on the GPU).
+    The loss and its gradient come from one kernel (fused_l2_loss) and
+    enter the backward as the gradient of the stacked predictions, with the
+    same values as l2_loss(...).backward()."""
     if loss_lods is None:
         loss_lods = list(range(net.num_lods))
     net.zero_grad()
-    preds = net.sdf(pts, return_lst=True)
-    loss = l2_loss(preds, gts, loss_lods, pts.shape[0])
-    loss.backward()
+    preds = sdf_train_stacked(net, pts)
+    loss, grad = fused_l2_loss(preds, gts, loss_lods)
+    preds.backward(grad)
     optimizer.step()
-    with torch.no_grad():
-        return sum(((preds[l].double() - gts.double()) ** 2).sum() for l in loss_lods) / pts.shape[0]
+    return loss
 
 
 def fit(net, batches, steps, lr=1e-3, loss_lods=None, seed=0, log_every=500):

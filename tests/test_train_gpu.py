@@ -229,3 +229,22 @@ def test_backward_matches_torch_fp32_at_size(cuda, hidden, lods, n):
             continue
         err = (got - want).abs().max().item() / scale
         assert err < 1e-4, (k, err)
+
+
+def test_fused_l2_loss_matches_autograd_loss(cuda):
+    """nglod_l2_loss: the loss of l2_loss in float64 and the gradient that
+    l2_loss(...).backward() gives its predictions, for a LOD subset."""
+    torch.manual_seed(3)
+    n = 70_001
+    preds = torch.randn(5, n, 1, device=cuda, dtype=torch.float32) * 0.1
+    gts = torch.randn(n, 1, device=cuda, dtype=torch.float32) * 0.1
+    lods = [0, 2, 4]
+    loss, grad = trainer.fused_l2_loss(preds, gts, lods)
+    p = preds.clone().requires_grad_(True)
+    ref = trainer.l2_loss([p[i] for i in range(5)], gts, lods, n)
+    ref.backward()
+    want = sum(((preds[l].double() - gts.double()) ** 2).sum() for l in lods).item() / n
+    assert abs(loss.item() - want) <= 1e-12 * max(1.0, abs(want))
+    assert abs(loss.item() - ref.item()) <= 1e-5 * abs(want)
+    np.testing.assert_allclose(grad.cpu().numpy(), p.grad.cpu().numpy(), rtol=1e-6, atol=1e-12)
+    assert (grad[1] == 0).all() and (grad[3] == 0).all()
