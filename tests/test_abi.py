@@ -88,3 +88,34 @@ def test_python_shim_raises_on_status():
     from nglod_gb300 import _lib
     with pytest.raises(RuntimeError, match="invalid argument"):
         _lib.check(_lib.load().nglod_aabb(None, None, -5, None, None, None, None), "nglod_aabb")
+
+
+def test_bf16_and_training_validation_without_device(built_library):
+    """Argument checks of the pair-volume, loss and training entry points
+    that run before any CUDA call (fake device addresses, no GPU)."""
+    from nglod_gb300 import _lib
+    lib = _lib.load()
+    b = _lib.Bf16Model()
+    b.num_lods, b.base_lod, b.feature_dim, b.hidden_dim = 2, 2, 32, 128
+    for i in range(2):
+        b.grid[i] = b.w0_tile[i] = b.b0[i] = b.w1[i] = b.b1[i] = 4096 * (i + 1)
+    b.grid_pairs[0] = 4096
+    b.grid_pairs[1] = 4096 + 16  # 16-byte but not 32-byte aligned
+    fake = ctypes.c_void_p(1 << 20)
+    assert lib.nglod_sdf_fwd_bf16(b, fake, 10, 1, fake, fake, None) == -5
+    assert b"pair volume 1" in lib.nglod_last_error()
+    assert lib.nglod_bf16_build_pairs(fake, 1, fake, None) == -1  # s < 2
+    assert lib.nglod_bf16_build_pairs(ctypes.c_void_p(4096 + 8), 5, fake, None) == -5
+    assert lib.nglod_l2_loss(fake, fake, 10, 0, 1, fake, fake, None) == -1  # rows = 0
+    assert lib.nglod_l2_loss(fake, fake, 10, 1, 1, None, fake, None) == -1  # no loss_out
+    m = _lib.DenseModel()
+    m.num_lods, m.base_lod, m.feature_dim, m.hidden_dim = 2, 2, 32, 128
+    for i in range(2):
+        m.grid[i] = m.w0[i] = m.b0[i] = m.w1[i] = m.b1[i] = 4096 * (i + 1)
+    mis = ctypes.c_void_p((1 << 20) + 4)  # not 16-byte aligned
+    assert lib.nglod_sdf_fwd_train(m, fake, 10, 0b11, fake, fake, mis, None) == -5
+    assert b"relu_masks" in lib.nglod_last_error()
+    g = _lib.DenseGrads()
+    for i in range(2):
+        g.grid[i] = g.w0[i] = g.b0[i] = g.w1[i] = g.b1[i] = 4096 * (i + 1)
+    assert lib.nglod_sdf_bwd(m, fake, 10, 0b11, fake, fake, mis, fake, g, None, None) == -5
