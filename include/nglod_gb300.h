@@ -407,6 +407,12 @@ typedef struct nglod_sparse_model {
     /* optional: NGLOD_BF16_TILE_BYTES decoder tiles (nglod_bf16_pack_decoder)
      * for nglod_sparse_trace_tc; unused by the other calls */
     const void *w0_tile[NGLOD_MAX_LODS];
+    /* optional, per lod: corner_chain[lod][v][k][8] = corner_idx of the
+     * level-(lod+2-k) ancestor of voxel v of level lod+2 (k = 0..lod), from
+     * nglod_sparse_build_chain, 16-byte aligned.  When set,
+     * nglod_sparse_trace_tc reads a voxel's corners of every level from its
+     * own row instead of walking `parent` (identical results). */
+    const int32_t *corner_chain[NGLOD_MAX_LODS];
 } nglod_sparse_model;
 
 /* SDF::initTrinkets + the corner export of SOL_NGLOD (SDF.cu:141-216,
@@ -444,6 +450,13 @@ int nglod_sparse_trace(const nglod_sparse_model *model, int32_t lod, int32_t num
                        const float *ray_d, int64_t n, const int32_t *nuggets, int64_t n_nuggets,
                        int32_t *ray_first, float *x, float *t, uint8_t *hit, float *normal, int64_t *work_counter,
                        nglod_stream_t stream);
+
+/* Fills chain [count][lod+1][8] int32 (count = level_start[lod+3] -
+ * level_start[lod+2] voxels of level lod+2) for model->corner_chain[lod]:
+ * row v, block k = corner_idx of the voxel reached from voxel v by k parent
+ * steps.  Needs corner_idx and parent of the model. */
+int nglod_sparse_build_chain(const nglod_sparse_model *model, int32_t lod, int64_t count, int32_t *chain,
+                             nglod_stream_t stream);
 
 /* nglod_sparse_trace with bf16 corner features and the BF16 decoder of
  * nglod_sdf_fwd_bf16: every sdf evaluation of 128 rays is one tcgen05 tile

@@ -88,6 +88,7 @@ class SparseModel(ctypes.Structure):
         ("w1", _vp * MAX_LODS),
         ("b1", _vp * MAX_LODS),
         ("w0_tile", _vp * MAX_LODS),
+        ("corner_chain", _vp * MAX_LODS),
     ]
 
 
@@ -219,6 +220,7 @@ SIGNATURES = {
     "nglod_sparse_query": (ctypes.c_int, [ctypes.POINTER(SparseModel), _vp, _vp, _i32, _vp, _i64, _vp, _vp]),
     "nglod_sparse_trace": (ctypes.c_int, [ctypes.POINTER(SparseModel), _i32, _i32, _vp, _vp, _i64, _vp, _i64, _vp,
                                           _vp, _vp, _vp, _vp, _vp, _vp]),
+    "nglod_sparse_build_chain": (ctypes.c_int, [ctypes.POINTER(SparseModel), _i32, _i64, _vp, _vp]),
     "nglod_sparse_trace_tc": (ctypes.c_int, [ctypes.POINTER(SparseModel), _i32, _i32, _vp, _vp, _i64, _vp, _i64,
                                              _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "nglod_bf16_pack_decoder": (ctypes.c_int, [_vp, _vp, _i32, _i32, _vp]),

@@ -288,29 +288,72 @@ __global__ void __launch_bounds__(128) sparse_trace_kernel(const SparseTraceArgs
     }
 }
 
+// corner_chain rows of the level-(lod+2) voxels start .. start+count-1: row
+// v, block k = corner_idx of the voxel k parent steps above voxel start+v.
+__global__ void chain_build_kernel(const int4 *__restrict__ corner_idx, const int32_t *__restrict__ parent,
+                                   int64_t start, int64_t count, int lod, int4 *__restrict__ chain) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < count; v += stride) {
+        int64_t g = start + v;
+        int4 *row = chain + v * (lod + 1) * 2;
+        for (int k = 0; k <= lod; ++k) {
+            if (k > 0) g = parent[g];
+            row[2 * k] = corner_idx[2 * g];
+            row[2 * k + 1] = corner_idx[2 * g + 1];
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------
 // persistent sparse tracer with the BF16 tensor-core decoder
 // ---------------------------------------------------------------------------
 // This lane's 8 channels (8q .. 8q+7) of sparse_features<NGLOD_BF16>: the
-// same corners, weights and per-channel fmaf order.
+// same corners, weights and per-channel fmaf order.  kChain: the corner
+// indices of every level come from the voxel's own corner_chain row and the
+// ancestors' coordinates are the voxel's shifted right (an octree parent is
+// the voxel at half the coordinates), so no load waits on a parent index.
+template <bool kChain>
 __device__ __forceinline__ void sparse_features_quarter(const nglod_sparse_model &m, int lod, int64_t g, float px,
                                                         float py, float pz, int q, float (&f)[8]) {
 #pragma unroll
     for (int c = 0; c < 8; ++c) f[c] = 0.f;
     const float nx = fmaf(px, 0.5f, 0.5f), ny = fmaf(py, 0.5f, 0.5f), nz = fmaf(pz, 0.5f, 0.5f);
     const uint4 *feats = static_cast<const uint4 *>(m.corner_feats) + q;  // 4 uint4 per corner row
+    const short4 pf = reinterpret_cast<const short4 *>(m.points)[g];
+    const int4 *chain =
+        kChain ? reinterpret_cast<const int4 *>(m.corner_chain[lod]) + (g - m.level_start[lod + 2]) * (lod + 1) * 2
+               : nullptr;
+    // kChain: the next level's corner indices are loaded one level ahead
+    int4 na = make_int4(0, 0, 0, 0), nb = na;
+    if (kChain) {
+        na = __ldg(chain);
+        nb = __ldg(chain + 1);
+    }
 #pragma unroll 1
     for (int lv = lod + 2; lv >= 2; --lv) {
-        if (lv != lod + 2) g = m.parent[g];
+        const int k = lod + 2 - lv;
+        short4 p;
+        int4 ca, cb;
+        if (kChain) {
+            p = make_short4((short)(pf.x >> k), (short)(pf.y >> k), (short)(pf.z >> k), 0);
+            ca = na;
+            cb = nb;
+            if (k < lod) {
+                na = __ldg(chain + 2 * k + 2);
+                nb = __ldg(chain + 2 * k + 3);
+            }
+        } else {
+            if (lv != lod + 2) g = m.parent[g];
+            p = lv == lod + 2 ? pf : reinterpret_cast<const short4 *>(m.points)[g];
+            ca = __ldg(reinterpret_cast<const int4 *>(m.corner_idx) + 2 * g);
+            cb = __ldg(reinterpret_cast<const int4 *>(m.corner_idx) + 2 * g + 1);
+        }
         const float res = (float)(1 << lv);
         const float ux = nx * res, uy = ny * res, uz = nz * res;
-        const short4 p = reinterpret_cast<const short4 *>(m.points)[g];
         const float x0 = (float)p.x, y0 = (float)p.y, z0 = (float)p.z;
         const float wx[2] = {(x0 + 1.f) - ux, ux - x0};
         const float wy[2] = {(y0 + 1.f) - uy, uy - y0};
         const float wz[2] = {(z0 + 1.f) - uz, uz - z0};
-        const int4 ca = __ldg(reinterpret_cast<const int4 *>(m.corner_idx) + 2 * g);
-        const int4 cb = __ldg(reinterpret_cast<const int4 *>(m.corner_idx) + 2 * g + 1);
         const int ci[8] = {ca.x, ca.y, ca.z, ca.w, cb.x, cb.y, cb.z, cb.w};
         uint4 v[8];
 #pragma unroll
@@ -344,6 +387,7 @@ struct SparseTcArgs {
 // slot publishes its query point and voxel, the block gathers the 128 rows'
 // corner features into the bf16 tile, one thread issues the tcgen05 product
 // and each thread reads its row's hidden layer back for the fp32 epilogue.
+template <bool kChain>
 __global__ void __launch_bounds__(kTP, 4) sparse_trace_tc_kernel(const SparseTcArgs args) {
     const SparseTraceArgs &a = args.t;
     // the block's dynamic shared memory, as bytes (the float32 kernels of this
@@ -506,7 +550,7 @@ __global__ void __launch_bounds__(kTP, 4) sparse_trace_tc_kernel(const SparseTcA
             const int row = warp * 32 + pass * 8 + (int)(lane >> 2), q = (int)(lane & 3u);
             const float4 pt = qpts[row];
             float f[8];
-            sparse_features_quarter(a.m, a.lod, (int64_t)__float_as_int(pt.w), pt.x, pt.y, pt.z, q, f);
+            sparse_features_quarter<kChain>(a.m, a.lod, (int64_t)__float_as_int(pt.w), pt.x, pt.y, pt.z, q, f);
             *reinterpret_cast<uint4 *>(sA + tc::tile_offset(row, 8 * q, kKC)) =
                 make_uint4(pack_bf16x2(f[0], f[1]), pack_bf16x2(f[2], f[3]), pack_bf16x2(f[4], f[5]),
                            pack_bf16x2(f[6], f[7]));
@@ -865,6 +909,8 @@ extern "C" int nglod_sparse_trace_tc(const nglod_sparse_model *model, int32_t lo
     // first index plus its at most 8^level voxels must stay below 2^31
     NGLOD_REQUIRE(lod + 2 <= 9 && model->level_start[lod + 2] + ((int64_t)1 << (3 * (lod + 2))) < ((int64_t)1 << 31),
                   NGLOD_ERR_UNSUPPORTED, "voxel indices of level %d must fit 31 bits", lod + 2);
+    NGLOD_REQUIRE(!model->corner_chain[lod] || aligned(model->corner_chain[lod], 16), NGLOD_ERR_ALIGN,
+                  "corner_chain %d is not 16-byte aligned", lod);
     if (n == 0) return NGLOD_OK;
     NGLOD_REQUIRE(ray_o && ray_d && ray_first && x && t && hit && work_counter && status && (nuggets || n_nuggets == 0),
                   NGLOD_ERR_INVALID, "null pointer argument");
@@ -893,13 +939,30 @@ extern "C" int nglod_sparse_trace_tc(const nglod_sparse_model *model, int32_t lo
     a.t.normal = normal;
     a.t.counter = reinterpret_cast<unsigned long long *>(work_counter);
     a.status = status;
-    NGLOD_TRY(cuda_status(
-        cudaFuncSetAttribute(sparse_trace_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes),
-        "cudaFuncSetAttribute"));
+    auto kernel = model->corner_chain[lod] ? sparse_trace_tc_kernel<true> : sparse_trace_tc_kernel<false>;
+    NGLOD_TRY(cuda_status(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes),
+                          "cudaFuncSetAttribute"));
     const int64_t want = (n + kTP - 1) / kTP;
     const int64_t cap = (int64_t)num_sms() * 4;
-    sparse_trace_tc_kernel<<<(int)(want < cap ? want : cap), kTP, kSmemBytes, st>>>(a);
+    kernel<<<(int)(want < cap ? want : cap), kTP, kSmemBytes, st>>>(a);
     return launch_status("nglod_sparse_trace_tc");
+}
+
+extern "C" int nglod_sparse_build_chain(const nglod_sparse_model *model, int32_t lod, int64_t count, int32_t *chain,
+                                        nglod_stream_t stream) {
+    NGLOD_REQUIRE(model != nullptr, NGLOD_ERR_INVALID, "model is null");
+    NGLOD_REQUIRE(lod >= 0 && lod < model->num_lods && lod + 3 < 16, NGLOD_ERR_INVALID, "lod=%d", lod);
+    NGLOD_REQUIRE(count == model->level_start[lod + 3] - model->level_start[lod + 2], NGLOD_ERR_INVALID,
+                  "count=%lld is not the number of level-%d voxels (%lld)", (long long)count, lod + 2,
+                  (long long)(model->level_start[lod + 3] - model->level_start[lod + 2]));
+    if (count == 0) return NGLOD_OK;
+    NGLOD_REQUIRE(model->corner_idx && model->parent && chain, NGLOD_ERR_INVALID, "null pointer argument");
+    NGLOD_REQUIRE(aligned(model->corner_idx, 16) && aligned(chain, 16), NGLOD_ERR_ALIGN,
+                  "corner_idx and chain must be 16-byte aligned");
+    chain_build_kernel<<<sgrid(count), 256, 0, (cudaStream_t)stream>>>(
+        reinterpret_cast<const int4 *>(model->corner_idx), model->parent, model->level_start[lod + 2], count, lod,
+        reinterpret_cast<int4 *>(chain));
+    return launch_status("nglod_sparse_build_chain");
 }
 
 extern "C" int nglod_sparse_trace(const nglod_sparse_model *model, int32_t lod, int32_t num_steps, const float *ray_o,

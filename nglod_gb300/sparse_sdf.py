@@ -35,7 +35,12 @@ def _u(t):
 
 
 class SparseSDF:
-    def __init__(self, spc, corner_feats, corner_idx, parent, corner_counts, decoders, feat_dtype, decoder=None):
+    def __init__(self, spc, corner_feats, corner_idx, parent, corner_counts, decoders, feat_dtype, decoder=None,
+                 chains=True):
+        """chains (tensor-core decoder): also keep, per lod, every level-(lod+2)
+        voxel's corner indices of all its ancestors in one row
+        (nglod_sparse_build_chain), which the tensor-core trace reads instead
+        of walking the parent links; results are identical."""
         if decoder is None:
             decoder = "tc" if feat_dtype == _lib.BF16 else "f32"
         if decoder not in ("tc", "f32") or (decoder == "tc" and feat_dtype != _lib.BF16):
@@ -57,6 +62,21 @@ class SparseSDF:
             self.tiles = [pack_decoder_tile(w0, b0).to(dev) for w0, b0, _, _ in decoders]
         self._status = torch.zeros(1, dtype=torch.int32, device=corner_feats.device)
         self._m = self._descriptor()
+        self.chains = []
+        if decoder == "tc" and chains:
+            self._build_chains()
+
+    def _build_chains(self):
+        dev = self.corner_feats.device
+        pyr = self.spc.GetPyramid()
+        lib = _lib.load()
+        for lod in range(self.num_lods):
+            cnt = int(pyr[1, lod + 3] - pyr[1, lod + 2])
+            ch = torch.empty(max(cnt, 1), lod + 1, 8, dtype=torch.int32, device=dev)
+            _lib.check(lib.nglod_sparse_build_chain(self._m, lod, cnt, _u(ch), _lib.stream_ptr(dev)),
+                       "nglod_sparse_build_chain")
+            self.chains.append(ch)
+            self._m.corner_chain[lod] = ch.data_ptr()
 
     # -- construction ----------------------------------------------------------
     @classmethod

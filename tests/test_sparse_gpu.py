@@ -131,6 +131,36 @@ def test_sparse_tc_trace_against_fp64_dense_oracle(scene):
     assert np.median(err) < 1e-3
 
 
+def test_sparse_tc_trace_corner_chains_are_identical(scene):
+    """The tensor-core sparse trace reading each voxel's corner_chain row
+    gives bit-identical x, t, hit and normals to the same trace walking the
+    parent links, and the chain rows hold the ancestors' corner indices."""
+    net, s, _ = scene
+    sp = SparseSDF.from_dense(net, s, precision="bf16", decoder="tc")
+    assert len(sp.chains) == sp.num_lods
+    pyr = s.GetPyramid()
+    lod = 3
+    start, cnt = int(pyr[1, lod + 2]), int(pyr[1, lod + 3] - pyr[1, lod + 2])
+    ci, par = sp.corner_idx.cpu().numpy().reshape(-1, 8), sp.parent.cpu().numpy()
+    ch = sp.chains[lod].cpu().numpy()
+    rng = np.random.default_rng(0)
+    for v in rng.integers(0, cnt, 50):
+        g = start + int(v)
+        for k in range(lod + 1):
+            assert np.array_equal(ch[v, k], ci[g]), (v, k)
+            g = par[g]
+    ro, rd = synthetic.look_at_rays(width=96, height=72)
+    dev = s.GetOctree().device
+    a, _ = sp.render(ro.to(dev), rd.to(dev), lod=lod, num_steps=64)
+    for i in range(sp.num_lods):
+        sp._m.corner_chain[i] = None
+    b, _ = sp.render(ro.to(dev), rd.to(dev), lod=lod, num_steps=64)
+    sp.check_status()
+    assert a[2].sum().item() > 500
+    for u, w in zip(a, b):
+        assert torch.equal(u, w)
+
+
 def test_sparse_vs_dense_tracer(scene):
     """The sparse trace (fp16 export, 50 steps) against the dense float32
     tracer on the same network: same surface within a voxel's reach."""
