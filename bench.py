@@ -12,7 +12,7 @@ one pass over the batch.  ``value`` is queries/s with the points already
 resident in HBM; ``e2e`` is the same metric through the public API with
 host buffers (``Bf16OctreeSDF.sdf_host`` -> ``nglod_sdf_fwd_bf16_host``): the
 points are copied from pinned host memory and the distances copied back inside
-the timed region, in 1M-point chunks whose copies overlap the kernels.
+the timed region, in 256k-point chunks whose copies overlap the kernels.
 ``fp32`` repeats the measurement for the float32 drop-in (``OctreeSDF.sdf``),
 which matches the reference to 1e-5.
 
@@ -236,7 +236,7 @@ def run_ours(args):
 
     # e2e through the public API with host buffers: Bf16OctreeSDF.sdf_host ->
     # nglod_sdf_fwd_bf16_host copies the pinned points in and the distances
-    # out every step, in 1M-point chunks whose copies overlap the kernels.
+    # out every step, in 256k-point chunks whose copies overlap the kernels.
     def e2e_step():
         bnet.sdf_host(x_host, lod=LOD, out=out_host)
 
