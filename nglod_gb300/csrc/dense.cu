@@ -53,18 +53,31 @@ __global__ void __launch_bounds__(256) sdf_fwd_f32_kernel(const nglod_dense_mode
 }
 
 // One feature volume sampled at every point: out[n][C] (FeatureVolume.forward).
+// Cooperative gather (gather_warp_add_f32) of the warp's 32 points; each
+// sample is written straight from the cooperative layout (four whole rows
+// per store instruction).
 __global__ void __launch_bounds__(256) volume_sample_f32_kernel(const float *__restrict__ g, int s,
                                                                 const float *__restrict__ x, int64_t n,
                                                                 float *__restrict__ out) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        float f[kC];
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x + warp * 32; base < n; base += stride) {
+        const int64_t i = base + lane;
+        float px = 0.f, py = 0.f, pz = 0.f;
+        if (i < n) {
+            px = x[3 * i];
+            py = x[3 * i + 1];
+            pz = x[3 * i + 2];
+        }
+        float4 acc[8];
 #pragma unroll
-        for (int c = 0; c < kC; ++c) f[c] = 0.f;
-        gather_add_f32(g, s, x[3 * i], x[3 * i + 1], x[3 * i + 2], f);
-        float4 *o = reinterpret_cast<float4 *>(out + i * kC);
+        for (int p = 0; p < 8; ++p) acc[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+        gather_warp_add_f32(g, s, px, py, pz, lane, acc);
 #pragma unroll
-        for (int q = 0; q < kC / 4; ++q) o[q] = make_float4(f[4 * q], f[4 * q + 1], f[4 * q + 2], f[4 * q + 3]);
+        for (int p = 0; p < 8; ++p) {
+            const int64_t ip = base + 4 * p + (lane >> 3);
+            if (ip < n) reinterpret_cast<float4 *>(out + ip * kC)[lane & 7] = acc[p];
+        }
     }
 }
 

@@ -2,12 +2,12 @@
 // tracer and training kernels.
 //
 // Layout: feature volume l is channel-last [s][s][s][C] (C = 32 floats =
-// 128 B per vertex), so each trilinear corner is eight 16-byte loads of one
-// cache line.  The decoder of one LOD is staged in shared memory as H rows of
-// 36 floats (35 weights of Linear(35, H) followed by its bias; the input
-// vector carries a trailing 1.0) plus the H weights and the bias of
-// Linear(H, 1).  Every thread evaluates whole points, reading the decoder
-// rows as warp-wide broadcasts.
+// 128 B per vertex), so each trilinear corner is one cache line, read by
+// eight lanes with one 16-byte load each.  The decoder of one LOD is staged
+// in shared memory as H rows of 36 floats (35 weights of Linear(35, H)
+// followed by its bias; the input vector carries a trailing 1.0) plus the H
+// weights and the bias of Linear(H, 1).  Every thread decodes whole points,
+// reading the decoder rows as warp-wide broadcasts.
 #pragma once
 
 #include <math.h>
@@ -41,77 +41,22 @@ __device__ __forceinline__ void stage_decoder(float4 *dst, const nglod_dense_mod
     stage_decoder_ptrs(dst, m.hidden_dim, m.w0[l], m.b0[l], m.w1[l], m.b1[l]);
 }
 
-// Adds the trilinear sample of one channel-last float32 volume (s vertices per
-// side) at point p to f.  Same arithmetic as PyTorch's 3-D grid sampler with
-// align_corners=True and padding_mode='border': u = ((p + 1) / 2) * (s - 1)
-// clamped to [0, s - 1], corner weights are products of distances to the
-// opposite corner, corners summed in tnw, tne, tsw, tse, bnw, bne, bsw, bse
-// order.  The far corner index is clamped to s - 1 where u = s - 1; its weight
-// is then exactly 0, as when PyTorch skips the out-of-range corner.
-__device__ __forceinline__ void gather_add_f32(const float *__restrict__ g, int s, float px, float py,
-                                               float pz, float (&f)[kC]) {
-    const float sm1 = (float)(s - 1);
-    float ix = ((px + 1.f) / 2.f) * sm1;
-    float iy = ((py + 1.f) / 2.f) * sm1;
-    float iz = ((pz + 1.f) / 2.f) * sm1;
-    ix = fminf(sm1, fmaxf(ix, 0.f));
-    iy = fminf(sm1, fmaxf(iy, 0.f));
-    iz = fminf(sm1, fmaxf(iz, 0.f));
-    const float x0 = floorf(ix), y0 = floorf(iy), z0 = floorf(iz);
-    const float wx1 = ix - x0, wx0 = (x0 + 1.f) - ix;
-    const float wy1 = iy - y0, wy0 = (y0 + 1.f) - iy;
-    const float wz1 = iz - z0, wz0 = (z0 + 1.f) - iz;
-    const int xi = (int)x0, yi = (int)y0, zi = (int)z0;
-    const int xj = min(xi + 1, s - 1), yj = min(yi + 1, s - 1), zj = min(zi + 1, s - 1);
-    const size_t sy = (size_t)s * kC, sz = (size_t)s * sy;
-    const float4 *c[8];
-    c[0] = reinterpret_cast<const float4 *>(g + zi * sz + yi * sy + xi * kC);
-    c[1] = reinterpret_cast<const float4 *>(g + zi * sz + yi * sy + xj * kC);
-    c[2] = reinterpret_cast<const float4 *>(g + zi * sz + yj * sy + xi * kC);
-    c[3] = reinterpret_cast<const float4 *>(g + zi * sz + yj * sy + xj * kC);
-    c[4] = reinterpret_cast<const float4 *>(g + zj * sz + yi * sy + xi * kC);
-    c[5] = reinterpret_cast<const float4 *>(g + zj * sz + yi * sy + xj * kC);
-    c[6] = reinterpret_cast<const float4 *>(g + zj * sz + yj * sy + xi * kC);
-    c[7] = reinterpret_cast<const float4 *>(g + zj * sz + yj * sy + xj * kC);
-    float w[8];
-    w[0] = wx0 * wy0 * wz0;
-    w[1] = wx1 * wy0 * wz0;
-    w[2] = wx0 * wy1 * wz0;
-    w[3] = wx1 * wy1 * wz0;
-    w[4] = wx0 * wy0 * wz1;
-    w[5] = wx1 * wy0 * wz1;
-    w[6] = wx0 * wy1 * wz1;
-    w[7] = wx1 * wy1 * wz1;
-#pragma unroll
-    for (int q = 0; q < kC / 4; ++q) {
-        float4 v[8];
-#pragma unroll
-        for (int k = 0; k < 8; ++k) v[k] = __ldg(c[k] + q);
-        float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
-#pragma unroll
-        for (int k = 0; k < 8; ++k) {
-            a0 = fmaf(v[k].x, w[k], a0);
-            a1 = fmaf(v[k].y, w[k], a1);
-            a2 = fmaf(v[k].z, w[k], a2);
-            a3 = fmaf(v[k].w, w[k], a3);
-        }
-        f[4 * q + 0] += a0;
-        f[4 * q + 1] += a1;
-        f[4 * q + 2] += a2;
-        f[4 * q + 3] += a3;
-    }
-}
-
-// Warp-cooperative form of gather_add_f32 for the warp's 32 points (lane i
-// owns point i's position).  Each lane computes its own point's corner set
-// (vertex index of corner 0, which neighbours are not clamped, the eight
-// weights); in pass p the eight lanes 8j .. 8j + 7 load the corners of
-// point 4p + j, one float4 (channels 4 (lane % 8) .. +3) each, fetching the
-// corner set by shuffles.  A load instruction then reads four whole 128-byte
-// vertices instead of 16 bytes of 32 different ones.  acc[p] += this lane's
-// four channels of point 4p + lane / 8, with gather_add_f32's arithmetic
-// (same weights, corners summed in the same order), so the sums are
-// identical.
+// Adds the trilinear samples of one channel-last float32 volume (s vertices
+// per side) at the warp's 32 points (lane i owns point i's position).  Same
+// arithmetic as PyTorch's 3-D grid sampler with align_corners=True and
+// padding_mode='border': u = ((p + 1) / 2) * (s - 1) clamped to [0, s - 1],
+// corner weights are products of distances to the opposite corner, corners
+// summed in tnw, tne, tsw, tse, bnw, bne, bsw, bse order from zero per
+// channel, then added to the running sum.  The far corner index is clamped
+// to s - 1 where u = s - 1; its weight is then exactly 0, as when PyTorch
+// skips the out-of-range corner.
+// Cooperative loads: each lane computes its own point's corner set (vertex
+// index of corner 0, which neighbours are not clamped, the eight weights);
+// in pass p the eight lanes 8j .. 8j + 7 load the corners of point 4p + j,
+// one float4 (channels 4 (lane % 8) .. +3) each, fetching the corner set by
+// shuffles, so a load instruction reads four whole 128-byte vertices instead
+// of 16 bytes of 32 different ones.  acc[p] += this lane's four channels of
+// point 4p + lane / 8.
 __device__ __forceinline__ void gather_warp_add_f32(const float *__restrict__ g, int s, float px, float py, float pz,
                                                     int lane, float4 (&acc)[8]) {
     const unsigned FULL = 0xffffffffu;
