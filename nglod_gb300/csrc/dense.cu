@@ -12,7 +12,7 @@ namespace nglod {
 // point owners through a per-warp shared buffer placed after the staged
 // decoders, and each lane decodes its own point.
 template <bool kAll>
-__global__ void __launch_bounds__(256) sdf_fwd_f32_kernel(const nglod_dense_model m, const float *__restrict__ x,
+__global__ void __launch_bounds__(256, kAll ? 2 : 3) sdf_fwd_f32_kernel(const nglod_dense_model m, const float *__restrict__ x,
                                                           int64_t n, int L, float *__restrict__ out) {
     extern __shared__ float4 smem[];
     const int H = m.hidden_dim;
