@@ -67,6 +67,11 @@ __device__ __forceinline__ bool face_straddles(float fi, float fj, float a, floa
     return mn <= 0.f && mx >= 0.f;
 }
 
+// 2^e as a float for -126 <= e <= 127 (exact: the exponent field alone).
+// Multiplying by it equals ldexpf for normal results, as all of them are
+// here (levels <= 15, coordinates >= 0.5 * 2^-15).
+__device__ __forceinline__ float pow2i(int e) { return __int_as_float((127 + e) << 23); }
+
 // The three edge functions (a, b, c per plane) of one ray at one level.
 struct RayFaces {
     float a0, b0, c0, a1, b1, c1, a2, b2, c2;
@@ -83,7 +88,7 @@ __device__ __forceinline__ RayFaces ray_faces(const float *__restrict__ org, con
     const float cx = __fmaf_rn(oy, dz, -__fmul_rn(dy, oz));
     const float cy = __fmaf_rn(oz, dx, -__fmul_rn(dz, ox));
     const float cz = __fmaf_rn(ox, dy, -__fmul_rn(dx, oy));
-    const float s1 = ldexpf(1.f, -level);
+    const float s1 = pow2i(-level);
     const float s2 = __fmul_rn(s1, s1);
     RayFaces f;
     f.a0 = __fmul_rn(-s2, dz);
@@ -122,9 +127,10 @@ __device__ __forceinline__ uint32_t origin_octant(const float *__restrict__ org,
     const float ax = __fmaf_rn(0.5f, org[3 * ridx], 0.5f);
     const float ay = __fmaf_rn(0.5f, org[3 * ridx + 1], 0.5f);
     const float az = __fmaf_rn(0.5f, org[3 * ridx + 2], 0.5f);
-    const float vx = ldexpf((float)p.x + 0.5f, -level);
-    const float vy = ldexpf((float)p.y + 0.5f, -level);
-    const float vz = ldexpf((float)p.z + 0.5f, -level);
+    const float sc = pow2i(-level);
+    const float vx = __fmul_rn((float)p.x + 0.5f, sc);
+    const float vy = __fmul_rn((float)p.y + 0.5f, sc);
+    const float vz = __fmul_rn((float)p.z + 0.5f, sc);
     return (ax > vx ? 4u : 0u) + (ay > vy ? 2u : 0u) + (az > vz ? 1u : 0u);
 }
 
