@@ -11,18 +11,23 @@
 // the point is inside when every line crosses the mesh on both sides of it
 // (Moller-Trumbore, |det| >= 1e-8), and the distance is then negated.
 //
-// GB300 layout: a per-triangle record of 88 floats is precomputed once: the
+// GB300 layout: a per-triangle record of 92 floats is precomputed once: the
 // three vertices, the three edge vectors, the normal, the three edge x
-// normal vectors, the reciprocal squared lengths, and for each of the 13
-// lines the point-independent part of the crossing test (pvec = dir x edge2
-// and 1/det, 0 where |det| < 1e-8).  The distance kernel stages 128 records
-// at a time in shared memory and every thread tests its point against them,
-// keeping the running minimum and two 13-bit crossing masks in registers.
+// normal vectors, the reciprocal squared lengths, for each of the 13 lines
+// the point-independent part of the crossing test (pvec = dir x edge2 and
+// 1/det, 0 where |det| < 1e-8), and a bounding sphere.  The distance kernel
+// stages 128 records at a time in shared memory and every thread tests its
+// point against them, keeping the running minimum and two 13-bit crossing
+// masks in registers.  The sphere culls without changing any result: a
+// triangle whose sphere lies farther than the running minimum cannot lower
+// it, and a line that misses the sphere cannot cross the triangle (both
+// tests with a relative margin far above float rounding).
 #include "common.cuh"
 
 namespace nglod {
 
-constexpr int kTriRec = 88;      // floats per triangle record (352 bytes)
+constexpr int kTriRec = 92;      // floats per triangle record (368 bytes)
+constexpr int kRecSphere = 88;   // bounding sphere: centre x y z, radius
 constexpr int kRecInvDet = 36;   // 1/det of the 13 lines
 constexpr int kRecPvec = 49;     // pvec of the 13 lines
 constexpr int kTriTile = 128;    // triangles per shared-memory tile
@@ -60,7 +65,7 @@ static const float h_stab_dirs[13][3] = {
 
 // record: v0[0..2] v10[3..5] v21[6..8] v02[9..11] nor[12..14] c10[15..17]
 // c21[18..20] c02[21..23] i10 i21 i02 inor [24..27] v1[28..30] v2[31..33]
-// pad[34..35] inv_det[36..48] pvec[49..87]
+// pad[34..35] inv_det[36..48] pvec[49..87] sphere[88..91]
 __global__ void mesh_prepare_kernel(const float *__restrict__ tri, int64_t m, float *__restrict__ rec) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += stride) {
@@ -100,6 +105,16 @@ __global__ void mesh_prepare_kernel(const float *__restrict__ tri, int64_t m, fl
             r[kRecInvDet + d] = (det > -1e-8f && det < 1e-8f) ? 0.f : __fdiv_rn(1.f, det);
             for (int k = 0; k < 3; ++k) r[kRecPvec + 3 * d + k] = pv[k];
         }
+        // bounding sphere about the centroid, radius rounded up
+        float c[3], rad2 = 0.f;
+        for (int k = 0; k < 3; ++k) c[k] = (t[k] + t[3 + k] + t[6 + k]) * (1.f / 3.f);
+        for (int v = 0; v < 3; ++v) {
+            float d2 = 0.f;
+            for (int k = 0; k < 3; ++k) d2 = fmaf(t[3 * v + k] - c[k], t[3 * v + k] - c[k], d2);
+            rad2 = fmaxf(rad2, d2);
+        }
+        for (int k = 0; k < 3; ++k) r[kRecSphere + k] = c[k];
+        r[kRecSphere + 3] = sqrtf(rad2) * 1.0001f + 1e-7f;
     }
 }
 
@@ -120,7 +135,7 @@ __global__ void __launch_bounds__(kTriTile) mesh_sdf_kernel(const float *__restr
             p[1] = pts[3 * i + 1];
             p[2] = pts[3 * i + 2];
         }
-        float mind2 = INFINITY;
+        float mind2 = INFINITY, mind = INFINITY;
         uint32_t pos = 0u, neg = 0u;
         for (int64_t t0 = 0; t0 < m; t0 += kTriTile) {
             const int cnt = (int)(m - t0 < kTriTile ? m - t0 : kTriTile);
@@ -138,7 +153,10 @@ __global__ void __launch_bounds__(kTriTile) mesh_sdf_kernel(const float *__restr
                     p2[k] = p[k] - r[31 + k];
                 }
                 const float *v10 = r + 3, *v21 = r + 6, *v02 = r + 9, *nor = r + 12;
-                if (nor[0] != 0.f || nor[1] != 0.f || nor[2] != 0.f) {
+                const float w[3] = {r[kRecSphere] - p[0], r[kRecSphere + 1] - p[1], r[kRecSphere + 2] - p[2]};
+                const float w2 = dot3(w, w), rho = r[kRecSphere + 3];
+                const float reach = mind + rho;
+                if ((nor[0] != 0.f || nor[1] != 0.f || nor[2] != 0.f) && !(w2 > reach * reach * 1.0001f)) {
                     const float s1 = copysignf(1.f, dot3(r + 15, p0));
                     const float s2 = copysignf(1.f, dot3(r + 18, p1));
                     const float s3 = copysignf(1.f, dot3(r + 21, p2));
@@ -152,9 +170,16 @@ __global__ void __launch_bounds__(kTriTile) mesh_sdf_kernel(const float *__restr
                         const float dn = dot3(nor, p0);
                         d2 = dn * dn * r[27];
                     }
-                    mind2 = fminf(mind2, fmaxf(d2, 0.f));
+                    const float m2 = fminf(mind2, fmaxf(d2, 0.f));
+                    if (m2 < mind2) {
+                        mind2 = m2;
+                        mind = __fsqrt_ru(m2);
+                    }
                 }
-                // crossings of the 13 lines: edge1 = v10, edge2 = -v02, tvec = p0
+                // crossings of the 13 lines: edge1 = v10, edge2 = -v02, tvec = p0.
+                // squared distance of a line from the centre is w2 - (w.d)^2, which
+                // cancels: the margin covers its rounding (a few 1e-7 of w2)
+                const float rho2 = fmaf(rho * rho, 1.0001f, fmaf(w2, 2e-6f, 1e-12f));
                 const float e2v[3] = {-v02[0], -v02[1], -v02[2]};
                 float qvec[3];
                 cross3(p0, v10, qvec);
@@ -164,6 +189,8 @@ __global__ void __launch_bounds__(kTriTile) mesh_sdf_kernel(const float *__restr
                     const float inv_det = r[kRecInvDet + d];
                     if (inv_det == 0.f) continue;
                     const float *dir = c_stab_dirs[d];
+                    const float wd = dot3(w, dir);
+                    if (w2 - wd * wd > rho2) continue;  // the line misses the sphere
                     const float *pvec = r + kRecPvec + 3 * d;
                     const float u = dot3(p0, pvec) * inv_det;
                     if (u < 0.f || u > 1.f) continue;
