@@ -104,20 +104,8 @@ __device__ __forceinline__ void gather_warp_rows(const nglod_bf16_model &m, int 
 
 // Pair lines: vertex (z, y, x) of a volume stored beside its +x neighbour
 // (x + 1 clamped to s - 1) as one 128-byte line of four 32-byte units, unit c
-// = [v(z, y, x) channels 8c..8c+7 | v(z, y, x+1) channels 8c..8c+7].
-struct alignas(32) PairUnit {
-    uint32_t w[8];
-};
-
-// 256-bit read-only load (sm_100+); pair volumes are 32-byte aligned.
-__device__ __forceinline__ PairUnit ld_pair_unit(const PairUnit *p) {
-    PairUnit r;
-    asm("ld.global.nc.v8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
-        : "=r"(r.w[0]), "=r"(r.w[1]), "=r"(r.w[2]), "=r"(r.w[3]), "=r"(r.w[4]), "=r"(r.w[5]), "=r"(r.w[6]),
-          "=r"(r.w[7])
-        : "l"(p));
-    return r;
-}
+// = [v(z, y, x) channels 8c..8c+7 | v(z, y, x+1) channels 8c..8c+7]
+// (PairUnit, ld_pair_unit: bf16_tile.cuh).
 
 // gather_warp_rows<4> over pair volumes for the warp's 8 * NP points (lane
 // i and every lane i + 8 * NP hold point i's position): the four lanes of a

@@ -69,6 +69,22 @@ __device__ __forceinline__ float relu_dot_w1(uint32_t taddr, const float *__rest
     return acc.x + acc.y;
 }
 
+// 32 bytes of bf16 pairs: the two x corners of 8 channels side by side.
+struct alignas(32) PairUnit {
+    uint32_t w[8];
+};
+
+// 256-bit read-only load (sm_100+); the arrays read this way are 32-byte
+// aligned.
+__device__ __forceinline__ PairUnit ld_pair_unit(const PairUnit *p) {
+    PairUnit r;
+    asm("ld.global.nc.v8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=r"(r.w[0]), "=r"(r.w[1]), "=r"(r.w[2]), "=r"(r.w[3]), "=r"(r.w[4]), "=r"(r.w[5]), "=r"(r.w[6]),
+          "=r"(r.w[7])
+        : "l"(p));
+    return r;
+}
+
 // Persistent tracers publish one query point per thread after the fixed
 // layout above.
 constexpr size_t kSmemQ = (kSmemAbort + 4 + 15) & ~(size_t)15;  // float4 query points [128], 16-byte aligned

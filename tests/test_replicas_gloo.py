@@ -39,7 +39,7 @@ def _rank_main(rank, ws, port, out):
 
 def test_max_over_ranks_and_barrier_on_gloo():
     ws = 2
-    out = mp.Manager().dict()
+    out = mp.get_context("spawn").Manager().dict()
     mp.spawn(_rank_main, args=(ws, _free_port(), out), nprocs=ws, join=True)
     assert dict(out) == {0: 1.5 + ws - 1, 1: 1.5 + ws - 1}
 
