@@ -77,6 +77,27 @@ def test_raytrace_bit_exact(cuda, level, targets):
         assert np.array_equal(got, want), target
 
 
+def test_raytrace_bit_exact_at_frame_size(cuda):
+    """The sparse bench's traversal at full size -- 1920x1080 rays into the
+    level-7 octree of the sphere-union surface band, to level 6 (lod 4 + 2,
+    5.1M nuggets) -- bit-exact with the C restatement: every nugget, in the
+    same order."""
+    level = 7
+    vox = _sphere_octree(level)
+    s = spc.SPC.from_voxels(torch.from_numpy(vox.astype(np.int32)).to(cuda), level)
+    pts = s.GetPoints().cpu().numpy()
+    pyr = s.GetPyramid().numpy()
+    prefix = s.GetPrefix().cpu().numpy().view(np.uint32)
+    octree = s.GetOctree().cpu().numpy()
+    ro, rd = synthetic.look_at_rays(width=1920, height=1080)
+    for target in (6,):
+        got = spc.spc_raytrace(s.GetOctree(), s.GetPoints(), s.GetPyramid(), ro.to(cuda), rd.to(cuda),
+                               target).cpu().numpy()
+        want = cref.spc_raytrace(octree, pts, prefix, pyr, level, target, ro.numpy(), rd.numpy())
+        assert got.shape[0] > 1_000_000
+        assert np.array_equal(got, want), target
+
+
 def test_raytrace_capacity_and_empty(cuda):
     level = 5
     s = spc.SPC.from_voxels(torch.from_numpy(_sphere_octree(level).astype(np.int32)).to(cuda), level)
