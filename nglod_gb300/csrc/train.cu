@@ -1,19 +1,21 @@
 // Training kernels of the dense float32 path: forward with saved feature
-// sums, hand-written backward, multi-tensor Adam.
+// sums and ReLU masks, hand-written backward, the L2 loss, multi-tensor Adam.
 //
 // Backward of one training batch (lod_mask = set of LODs with a loss term):
-//   1. sdf_bwd_decoder_kernel, one pass per LOD l in the mask: each thread
-//      owns one point of a 128-point tile, recomputes the decoder's hidden
-//      layer from the saved feature sum, writes dLoss/d(feature sum) for its
-//      point and stores its hidden activations in a shared tile; the block
-//      then reduces the tile into the weight gradients (thread j owns hidden
-//      row j: dW0[j][:], db0[j], dw1[j]), accumulating over all tiles it
-//      visits, and adds its totals to global memory once per LOD.
+//   1. decoder part, per LOD l in the mask:
+//      - hidden_dim 128 with the forward's ReLU masks:
+//        sdf_bwd_decoder_tc_kernel, two tcgen05 products per 128-point tile
+//        (dLoss/d(feature sum) and the weight-gradient accumulator), no
+//        hidden layer recomputed;
+//      - otherwise sdf_bwd_decoder_kernel: each point's hidden layer is
+//        recomputed in float32 in the forward's order, dLoss/d(feature sum)
+//        written, and the block reduces its tiles into the weight gradients.
 //   2. sdf_bwd_scatter_kernel: per point, the gradient reaching volume i is
 //      the suffix sum over mask LODs l >= i of dLoss/d(feature sum l); it is
-//      scattered with the trilinear weights.  The coarsest volumes
-//      (5^3 and 9^3 vertices at base_lod 2) are accumulated in shared memory
-//      per block and flushed once; finer ones use red.global.add.v4.f32.
+//      scattered with the trilinear weights, eight lanes per point.  The
+//      coarsest volumes (5^3 and 9^3 vertices at base_lod 2) are accumulated
+//      in shared memory per block and flushed once; finer ones use
+//      red.global.add.v4.f32.
 #include <cuda_bf16.h>
 
 #include <mutex>
