@@ -7,7 +7,9 @@ b0 / w1 / b1 kept in float32.  ``sdf(x, lod)`` has the semantics of
 OctreeSDF.sdf(x, lod) (sdf-net/lib/models/OctreeSDF.py:94-146) with bf16
 storage and bf16 x bf16 -> fp32 products (b0 enters the product as a bf16
 hi + lo pair); its error against the FP64 oracle
-is measured per LOD by tests/test_bf16_gpu.py and bench.py.
+is measured per LOD by tests/test_bf16_gpu.py and bench.py.  Point queries
+read pair volumes (every vertex beside its +x neighbour, 128-byte lines;
+``pairs=False`` keeps only the vertex volumes), with identical results.
 """
 import ctypes
 

@@ -6,6 +6,9 @@
 // (corner_idx[g]) are blended with trilinear weights computed from the
 // voxel's own integer coordinates, which are the corner coordinates the
 // reference reads from its cc table (solr/sdf/sparse_grid_sample.cuh:52-107).
+// The tensor-core tracer can read the corner indices of every level from a
+// per-voxel chain row instead (corner_chain), so no load waits on a parent
+// index.
 #include <vector>
 
 #include "bf16_tile.cuh"
