@@ -182,6 +182,14 @@ int nglod_sdf_fwd_bf16(const nglod_bf16_model *model, const float *x, int64_t n,
 int nglod_sdf_fwd_bf16_host(const nglod_bf16_model *model, const float *x_host, int64_t n, int32_t lod,
                             float *out_host, int64_t chunk, void *scratch, int32_t *status, nglod_stream_t stream);
 
+/* For tests of the error path: bounds the per-tile tensor-core wait of
+ * later nglod_sdf_fwd_bf16 calls (host setting, all devices) to `polls`
+ * polls of the mbarrier; 0 tests it once without waiting, a negative value
+ * restores the default (2^22 polls).  A wait that gives up sets the call's
+ * status, stops the kernel after letting the issued product finish, and
+ * leaves the context usable.  Not for production use. */
+int nglod_debug_mma_wait_polls(int64_t polls);
+
 /* SphereTracer.forward in the BF16 form: the persistent tracer of
  * nglod_trace with every sdf evaluation (march points and normal taps) done
  * by the bf16 tile kernel above, 128 rays per block evaluated together.

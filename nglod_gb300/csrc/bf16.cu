@@ -325,7 +325,12 @@ struct Bf16Args {
     int L;
     float *out;
     int *status;
+    uint32_t wait_polls;  // bound of the per-tile tensor-core wait (nglod_debug_mma_wait_polls)
 };
+
+// Bound of the per-tile tensor-core wait of nglod_sdf_fwd_bf16 (host side,
+// all devices): kWaitPolls unless a test of the error path lowers it.
+static uint32_t g_bf16_wait_polls = kWaitPolls;
 
 // One 128-point tile per block of four warps: warp w gathers rows 32w ..
 // 32w + 31 (from the vertex volumes, or from pair volumes when kPairs), one
@@ -402,7 +407,7 @@ __global__ void __launch_bounds__(kTP, 4) sdf_fwd_bf16_tc_kernel(const Bf16Args 
                 tc::mma_bf16(tmem, ad, bd, idesc, ks > 0 ? 1u : 0u);
             }
             tc::mma_commit(bar);
-            if (!tc::mbar_wait_bounded(bar, phase, kWaitPolls)) {
+            if (!tc::mbar_wait_bounded(bar, phase, a.wait_polls)) {
                 *abort_flag = 1;
                 atomicExch(a.status, 1);
             }
@@ -736,6 +741,7 @@ static int sdf_fwd_bf16_impl(const nglod_bf16_model *model, const float *x, int6
     a.L = L;
     a.out = out;
     a.status = status;
+    a.wait_polls = g_bf16_wait_polls;
     auto kernel = pairs ? sdf_fwd_bf16_tc_kernel<true> : sdf_fwd_bf16_tc_kernel<false>;
     NGLOD_TRY(cuda_status(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes),
                           "cudaFuncSetAttribute"));
@@ -834,4 +840,11 @@ extern "C" int nglod_trace_bf16(const nglod_bf16_model *model, const nglod_trace
     const int64_t cap = (int64_t)num_sms() * 4;
     trace_bf16_tc_kernel<<<(int)(want < cap ? want : cap), kTP, kSmemBytes, s>>>(a);
     return launch_status("nglod_trace_bf16");
+}
+
+extern "C" int nglod_debug_mma_wait_polls(int64_t polls) {
+    NGLOD_REQUIRE(polls <= (int64_t)kWaitPolls, NGLOD_ERR_INVALID, "polls=%lld above the default %u",
+                  (long long)polls, kWaitPolls);
+    g_bf16_wait_polls = polls < 0 ? kWaitPolls : (uint32_t)polls;
+    return NGLOD_OK;
 }

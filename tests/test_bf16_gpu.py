@@ -184,3 +184,29 @@ def test_pair_volumes_are_built_and_give_identical_results(nets):
     np.testing.assert_allclose(a.cpu().numpy(), emulate(m32, x.cpu().numpy(), bnet.num_lods - 1), atol=2e-4, rtol=0)
     bnet.check_status()
     plain.check_status()
+
+
+def test_tensor_core_wait_timeout_reports_status_and_recovers(nets):
+    """The error path of the bounded tensor-core wait, without a GPU fault:
+    with the wait cut to a single non-blocking test (nglod_debug_mma_wait_polls
+    (0)) the first product of every block is still running when tested, so
+    the call reports a timeout through its status and stops after letting
+    the issued product finish; the next call with the default bound runs
+    normally on the same context and gives the same values as before."""
+    from nglod_gb300 import _lib
+    net, bnet, _, _, _ = nets
+    dev = net.features[0].fm.device
+    lib = _lib.load()
+    x = (torch.rand(100_000, 3, generator=torch.Generator().manual_seed(4)) * 2 - 1).to(dev)
+    good = bnet.sdf(x, lod=2)
+    bnet.check_status()
+    try:
+        _lib.check(lib.nglod_debug_mma_wait_polls(0), "nglod_debug_mma_wait_polls")
+        bnet.sdf(x, lod=2)
+        with pytest.raises(RuntimeError, match="timed out"):
+            bnet.check_status()
+    finally:
+        _lib.check(lib.nglod_debug_mma_wait_polls(-1), "nglod_debug_mma_wait_polls")
+    again = bnet.sdf(x, lod=2)
+    bnet.check_status()
+    assert torch.equal(again, good)
