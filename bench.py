@@ -271,8 +271,9 @@ def run_ours(args):
         "tensor_frac_of_bf16_peak": tc_flop / sec / 1e12 / pk["bf16_tflops"],
         "note": "one launch reads each point once and the 40.4 MB of bf16 pair volumes (each vertex beside "
                 "its +x neighbour, 128-byte lines) from HBM; the corner gathers (2,560 B/query, four whole "
-                "lines per LOD) are served by L2/L1 and bind the kernel; the 35x128 decoder layer runs on "
-                "tcgen05 tensor cores and is a small share of the time",
+                "lines per LOD) are served by L2/L1, and the gather's instruction stream (half of it bf16 "
+                "unpacking) binds the kernel: with every load an L1 hit it still takes 88 % of the time; "
+                "the 35x128 decoder layer runs on tcgen05 tensor cores and is a small share of the time",
     }
     sec32 = ms32 / 1e3
     fp32 = {"value": ws * N_POINTS / sec32, "unit": UNIT, "ms_per_step": ms32, "steps": steps32,
