@@ -74,13 +74,16 @@ class _SdfTrain(torch.autograd.Function):
         gfm = [None] * nl
         gdec = [[None] * 4 for _ in range(nl)]
         for i in range(L + 1):
-            gfm[i] = torch.zeros_like(fms[i], memory_format=CL3D)
+            gfm[i] = torch.empty_like(fms[i], memory_format=CL3D)
             g.grid[i] = gfm[i].data_ptr()
             if (ctx.mask >> i) & 1:
-                gdec[i] = [torch.zeros_like(p) for p in decs[i]]
+                gdec[i] = [torch.empty_like(p) for p in decs[i]]
                 g.w0[i], g.b0[i], g.w1[i], g.b1[i] = [t.data_ptr() for t in gdec[i]]
         dfeat = torch.empty_like(feats)
-        gx = torch.zeros(n, 3, device=dev, dtype=torch.float32) if ctx.x_needs_grad else None
+        gx = torch.empty(n, 3, device=dev, dtype=torch.float32) if ctx.x_needs_grad else None
+        # the kernels add into the gradient buffers: zero them in a few multi-tensor launches
+        torch._foreach_zero_([t for t in gfm[:L + 1]] + [t for d in gdec for t in d if t is not None] +
+                             ([gx] if gx is not None else []))
         _lib.check(_lib.load().nglod_sdf_bwd(m, _lib.ptr(xd), n, ctx.mask, _lib.ptr(gp), _lib.ptr(feats),
                                              _lib.ptr(ctx.relu), _lib.ptr(dfeat), g, _lib.ptr(gx),
                                              _lib.stream_ptr(dev)), "nglod_sdf_bwd")
