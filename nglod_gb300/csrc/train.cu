@@ -27,6 +27,8 @@ namespace nglod {
 
 constexpr int kBT = 128;  // points per backward tile = threads per block
 
+__device__ int32_t g_train_status;  // nonzero: a tensor-core wait of a training kernel gave up
+
 // ---------------------------------------------------------------------------
 // forward for training
 // ---------------------------------------------------------------------------
@@ -79,6 +81,241 @@ __global__ void __launch_bounds__(kFwdTrainThreads, 1)
             }
         }
     }
+}
+
+// ---------------------------------------------------------------------------
+// forward for training, tensor-core form (hidden_dim 128, ReLU masks wanted)
+// ---------------------------------------------------------------------------
+// The decoder's first layer P [128 pts x 128 hid] = IN [pts x 40] . W^T runs
+// on tcgen05 as kind::tf32 products over big / small splits of both
+// operands (x = big + small, big = x with its low 13 mantissa bits cleared;
+// a*b ~ ab*bb + ab*bs + as*bb, relative error about 2^-21, the size of the
+// float32 path's own rounding), accumulated in TMEM; ReLU, the ReLU mask and
+// the 128 -> 1 layer are a float32 epilogue per point.  K order of an IN
+// row: the 32 summed features, x y z, 1 (the b0 column), zeros; W row j:
+// w0[j][3..34], w0[j][0..2], b0[j], zeros.
+// Blocks run LOD by LOD so that each LOD's W tiles are staged once: a
+// block visits the same tiles at every LOD, and the running feature sum of
+// a point is carried through feats (row l-1 is read back by the very lanes
+// that wrote it), which therefore holds every row 0..L.
+namespace fwdtc {
+constexpr int kTP = 128, kH = 128, kK = 40, kKC = kK / 4;   // 32-bit core matrices hold 4 elements along K
+constexpr uint32_t kTileBytes = kTP * kK * 4;               // 20 KB
+constexpr size_t kAB = 0, kAS = kTileBytes, kWB = 2 * kTileBytes, kWS = 3 * kTileBytes;
+constexpr size_t kW1 = 4 * kTileBytes;                        // w1 [128] f32
+constexpr size_t kBar = kW1 + kH * 4, kSlot = kBar + 8, kAbort = kSlot + 4;
+constexpr size_t kSmem = kAbort + 12;
+constexpr uint32_t kPolls = 1u << 22;
+// |P| below which a unit's sign is settled by a float32 evaluation: above the
+// split products' error (about 2^-21 of sum |w x|) for sums up to ~20
+constexpr float kNearZero = 1e-5f;
+static_assert(kTileBytes % 1024 == 0 && kBar % 8 == 0, "shared layout alignment");
+}  // namespace fwdtc
+
+// Byte offset of 32-bit element (row, k) in a K-major tile with kc
+// 16-byte core-matrix columns.
+__host__ __device__ constexpr uint32_t tile_offset32(int row, int k, int kc) {
+    return (uint32_t)(((row / 8) * kc + k / 4) * 128 + (row % 8) * 16 + (k % 4) * 4);
+}
+
+__device__ __forceinline__ float tf32_big(float x) { return __uint_as_float(__float_as_uint(x) & 0xFFFFE000u); }
+
+__device__ __forceinline__ void store_split4(uint8_t *big, uint8_t *small, uint32_t off, float4 v) {
+    const float4 b = make_float4(tf32_big(v.x), tf32_big(v.y), tf32_big(v.z), tf32_big(v.w));
+    *reinterpret_cast<float4 *>(big + off) = b;
+    *reinterpret_cast<float4 *>(small + off) = make_float4(v.x - b.x, v.y - b.y, v.z - b.z, v.w - b.w);
+}
+
+// Hidden unit j's pre-activation for IN row r, in float32 with
+// decode_f32's order (inputs x y z, features, 1; products of even and odd
+// float4 groups summed apart, then added).  The row's values are big + small
+// of the IN tiles, which is exact.
+__device__ __forceinline__ float pre_f32(const uint8_t *smem, const float *__restrict__ w0, const float *__restrict__ b0,
+                                         int r, int j) {
+    using namespace fwdtc;
+    auto in_at = [&](int k) -> float {  // decode_f32's input k
+        const int kk = k < 3 ? 32 + k : (k < 35 ? k - 3 : 35);
+        const uint32_t off = tile_offset32(r, kk, kKC);
+        return *reinterpret_cast<const float *>(smem + kAB + off) + *reinterpret_cast<const float *>(smem + kAS + off);
+    };
+    float a0 = 0.f, a1 = 0.f;
+#pragma unroll 1
+    for (int q = 0; q < 9; ++q) {
+        float t = q & 1 ? a1 : a0;
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const int k = 4 * q + e;
+            t = fmaf(k < 35 ? w0[j * 35 + k] : b0[j], in_at(k), t);
+        }
+        if (q & 1)
+            a1 = t;
+        else
+            a0 = t;
+    }
+    return a0 + a1;
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d),
+        "l"(a), "l"(b), "r"(idesc), "r"(acc)
+        : "memory");
+}
+
+__global__ void __launch_bounds__(fwdtc::kTP, 2)
+    sdf_fwd_train_tc_kernel(const nglod_dense_model m, const float *__restrict__ x, int64_t n, int L, uint32_t mask,
+                            float *__restrict__ preds, float *__restrict__ feats, uint32_t *__restrict__ relu) {
+    using namespace fwdtc;
+    extern __shared__ __align__(1024) uint8_t smem_fw[];
+    uint8_t *smem = smem_fw;
+    float *w1s = reinterpret_cast<float *>(smem + kW1);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + kBar);
+    uint32_t *slot = reinterpret_cast<uint32_t *>(smem + kSlot);
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + kAbort);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    // K columns 36..39 of the IN rows are always zero
+    for (int r = tid; r < kTP; r += kTP) {
+        const uint32_t off = tile_offset32(r, 36, kKC);
+        *reinterpret_cast<float4 *>(smem + kAB + off) = make_float4(0.f, 0.f, 0.f, 0.f);
+        *reinterpret_cast<float4 *>(smem + kAS + off) = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    if (warp == 0) tc::tmem_alloc(slot, kH);
+    if (tid == 0) {
+        tc::mbar_init(bar, 1);
+        *abort_flag = 0;
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = *slot;
+    const uint32_t sbase = tc::smem_addr(smem);
+    const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(kH >> 3) << 17) | ((uint32_t)(kTP >> 4) << 24);
+    const uint32_t trow = (uint32_t)(warp * 32) << 16;
+    uint32_t phase = 0;
+
+#pragma unroll 1
+    for (int l = 0; l <= L && !*abort_flag; ++l) {
+        const bool decode = (mask >> l) & 1u;
+        if (decode) {
+            // W tiles of this LOD (big / small) and w1
+            for (int u = tid; u < kH * kKC; u += kTP) {
+                const int j = u / kKC, kc = u % kKC;
+                float v[4];
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    const int k = kc * 4 + e;
+                    v[e] = k < 32 ? m.w0[l][j * 35 + 3 + k] : k < 35 ? m.w0[l][j * 35 + (k - 32)] : k == 35 ? m.b0[l][j] : 0.f;
+                }
+                store_split4(smem + kWB, smem + kWS, tile_offset32(j, kc * 4, kKC), make_float4(v[0], v[1], v[2], v[3]));
+            }
+            if (tid < kH) w1s[tid] = m.w1[l][tid];
+        }
+        const float b1 = decode ? m.b1[l][0] : 0.f;
+        const int s = volume_side(m, l);
+#pragma unroll 1
+        for (int64_t tile = blockIdx.x; tile * kTP < n; tile += gridDim.x) {
+            const int64_t base = tile * kTP + warp * 32;
+            const int64_t i = base + lane;
+            float px = 0.f, py = 0.f, pz = 0.f;
+            if (i < n) {
+                px = x[3 * i];
+                py = x[3 * i + 1];
+                pz = x[3 * i + 2];
+            }
+            // running sum: LOD l's sample added to row l-1 of feats
+            float4 acc[8];
+#pragma unroll
+            for (int p = 0; p < 8; ++p) {
+                const int64_t ip = base + 4 * p + (lane >> 3);
+                acc[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (l > 0 && ip < n) acc[p] = reinterpret_cast<const float4 *>(feats + ((int64_t)(l - 1) * n + ip) * kC)[lane & 7];
+            }
+            gather_warp_add_f32(static_cast<const float *>(m.grid[l]), s, px, py, pz, lane, acc);
+#pragma unroll
+            for (int p = 0; p < 8; ++p) {
+                const int64_t ip = base + 4 * p + (lane >> 3);
+                if (ip < n) reinterpret_cast<float4 *>(feats + ((int64_t)l * n + ip) * kC)[lane & 7] = acc[p];
+            }
+            if (!decode) continue;
+            // IN rows of the warp's 32 points
+#pragma unroll
+            for (int p = 0; p < 8; ++p)
+                store_split4(smem + kAB, smem + kAS, tile_offset32(warp * 32 + 4 * p + (lane >> 3), 4 * (lane & 7), kKC),
+                             acc[p]);
+            store_split4(smem + kAB, smem + kAS, tile_offset32(warp * 32 + lane, 32, kKC), make_float4(px, py, pz, 1.f));
+            tc::fence_proxy_async_smem();
+            tc::fence_before_sync();
+            __syncthreads();
+            if (tid == 0) {
+                tc::fence_after_sync();
+                const uint64_t ab = tc::smem_desc(sbase + (uint32_t)kAB, 128, kKC * 128);
+                const uint64_t as = tc::smem_desc(sbase + (uint32_t)kAS, 128, kKC * 128);
+                const uint64_t wb = tc::smem_desc(sbase + (uint32_t)kWB, 128, kKC * 128);
+                const uint64_t ws = tc::smem_desc(sbase + (uint32_t)kWS, 128, kKC * 128);
+#pragma unroll
+                for (int t = 0; t < 3; ++t)
+#pragma unroll
+                    for (int ks = 0; ks < kK / 8; ++ks) {
+                        const uint64_t step = (uint64_t)((ks * 256) >> 4);  // 8 tf32 of K = two core matrices
+                        mma_tf32(tmem, (t == 2 ? as : ab) + step, (t == 1 ? ws : wb) + step, idesc,
+                                 (t > 0 || ks > 0) ? 1u : 0u);
+                    }
+                tc::mma_commit(bar);
+                if (!tc::mbar_wait_bounded(bar, phase, kPolls)) {
+                    *abort_flag = 1;
+                    atomicExch(&g_train_status, 1);
+                }
+            }
+            __syncthreads();
+            if (*abort_flag) break;
+            phase ^= 1u;
+            tc::fence_after_sync();
+            // epilogue: row 32 warp + lane = point i.  Units whose product is
+            // within its error bound of zero are evaluated again in float32,
+            // so that the ReLU mask is the float32 path's.
+            float out = 0.f;
+            uint32_t bits[4];
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                float v[32];
+                tc::tmem_load32(tmem + trow + (uint32_t)(32 * c), v);
+                uint32_t b = 0u, near = 0u;
+#pragma unroll
+                for (int e = 0; e < 32; ++e) {
+                    const bool z = fabsf(v[e]) < kNearZero;
+                    near |= (uint32_t)z << e;
+                    out = fmaf(w1s[32 * c + e], z ? 0.f : fmaxf(v[e], 0.f), out);
+                    b |= (uint32_t)(v[e] > 0.f && !z) << e;
+                }
+                while (near) {  // rare: a few units per thousand points
+                    const int e = __ffs(near) - 1;
+                    near &= near - 1u;
+                    const float f = pre_f32(smem, m.w0[l], m.b0[l], warp * 32 + lane, 32 * c + e);
+                    if (f > 0.f) {
+                        out = fmaf(w1s[32 * c + e], f, out);
+                        b |= 1u << e;
+                    }
+                }
+                bits[c] = b;
+            }
+            if (i < n) {
+                const int64_t row = (int64_t)l * n + i;
+                preds[row] = out + b1;
+                reinterpret_cast<uint4 *>(relu)[row] = make_uint4(bits[0], bits[1], bits[2], bits[3]);
+            }
+            tc::fence_before_sync();
+            __syncthreads();
+        }
+        __syncthreads();
+    }
+    if (*abort_flag && tid == 0) tc::mbar_wait_bounded(bar, phase, kPolls);  // let an in-flight product finish
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if (warp == 0) tc::tmem_dealloc(tmem, kH);
 }
 
 // ---------------------------------------------------------------------------
@@ -317,7 +554,6 @@ static_assert(kM % 1024 == 0 && kWH % 1024 == 0 && kBarD % 8 == 0, "shared layou
 static_assert(kSmem <= 227 * 1024, "shared layout fits one block");
 }  // namespace bwdtc
 
-__device__ int32_t g_train_status;  // nonzero: a tensor-core wait of a backward gave up
 
 __device__ __forceinline__ uint32_t bf16x2_bits(__nv_bfloat162 h) { return *reinterpret_cast<uint32_t *>(&h); }
 
@@ -900,6 +1136,15 @@ extern "C" int nglod_sdf_fwd_train(const nglod_dense_model *model, const float *
     NGLOD_REQUIRE(x && preds && feats, NGLOD_ERR_INVALID, "null pointer argument");
     NGLOD_REQUIRE(aligned(feats, 16), NGLOD_ERR_ALIGN, "feats must be 16-byte aligned");
     NGLOD_REQUIRE(!relu_masks || aligned(relu_masks, 16), NGLOD_ERR_ALIGN, "relu_masks must be 16-byte aligned");
+    if (model->hidden_dim == fwdtc::kH && relu_masks) {
+        // tensor-core form: two 128-thread blocks per SM
+        NGLOD_TRY(prepare_smem(sdf_fwd_train_tc_kernel, fwdtc::kSmem));
+        const int64_t tiles = (n + fwdtc::kTP - 1) / fwdtc::kTP;
+        const int64_t cap = (int64_t)num_sms() * 2;
+        sdf_fwd_train_tc_kernel<<<(int)(tiles < cap ? tiles : cap), fwdtc::kTP, fwdtc::kSmem,
+                                  (cudaStream_t)stream>>>(*model, x, n, L, lod_mask, preds, feats, relu_masks);
+        return launch_status("nglod_sdf_fwd_train");
+    }
     const int threads = kFwdTrainThreads;
     // staged decoders, then one [32][kTRow] float transpose buffer per warp
     const size_t smem = (size_t)(L + 1) * decoder_f4(model->hidden_dim) * sizeof(float4) +
