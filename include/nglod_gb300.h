@@ -223,7 +223,13 @@ typedef struct nglod_dense_grads {
  * relu_masks (optional, 16-byte aligned): relu_masks[l][n][(H+31)/32] gets
  * the decoder's ReLU mask (bit j of word j/32: hidden unit j was positive),
  * which nglod_sdf_bwd takes as the ReLU derivative, as autograd takes the
- * forward's saved activation. */
+ * forward's saved activation.  With hidden_dim 128 and relu_masks given,
+ * the decoders run on tcgen05 tensor cores: three TF32 products over
+ * big / small splits of both operands (relative error about 2^-21), and
+ * hidden units whose product lies within 1e-5 of zero evaluated again in
+ * float32, so the ReLU decisions are the float32 path's.  That form writes
+ * every feats row 0..L and reports a tensor-core wait that gives up through
+ * nglod_train_status. */
 int nglod_sdf_fwd_train(const nglod_dense_model *model, const float *x, int64_t n, uint32_t lod_mask,
                         float *preds, float *feats, uint32_t *relu_masks, nglod_stream_t stream);
 
