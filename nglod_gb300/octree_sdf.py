@@ -124,7 +124,10 @@ class OctreeSDF(nn.Module):
         Returns [N, 1] at ``lod`` (0 <= lod < num_lods); otherwise the finest
         prediction, or the list of every LOD's [N, 1] with ``return_lst``.
         Differentiable in the features and decoder weights when autograd
-        needs it.
+        needs it.  That form runs the hidden-128 decoders as split-TF32
+        products on tensor cores: its predictions differ from the float32
+        inference kernels' by rounding (about 2^-21 relative), and its ReLU
+        decisions near zero are taken in float32.
         """
         if lod is None:
             lod = self.lod

@@ -53,8 +53,8 @@ def test_mixed_requests_equal_alone(cuda):
                 assert torch.equal(getattr(tk.result, k), getattr(t2.result, k)), k
             assert tk.result.hit.any()
         else:
-            ref = model.sdf(r.points, lod=r.lod) if isinstance(model, Bf16OctreeSDF) else \
-                model.sdf(r.points, lod=r.lod).detach()
+            with torch.no_grad():  # the inference kernels, as the server runs them
+                ref = model.sdf(r.points, lod=r.lod)
             assert torch.equal(tk.result, ref)
     st = srv.stats()
     assert st["requests"] == len(reqs) and st["p99_ms"] is not None and st["failed"] == 0

@@ -248,3 +248,48 @@ def test_fused_l2_loss_matches_autograd_loss(cuda):
     assert abs(loss.item() - ref.item()) <= 1e-5 * abs(want)
     np.testing.assert_allclose(grad.cpu().numpy(), p.grad.cpu().numpy(), rtol=1e-6, atol=1e-12)
     assert (grad[1] == 0).all() and (grad[3] == 0).all()
+
+
+@pytest.mark.parametrize("n,mask", [(20_001, 0b11111), (4_099, 0b10101), (77, 0b01000)])
+def test_tensor_core_forward_against_fp64_decode(cuda, n, mask):
+    """The training forward at hidden 128 with ReLU masks (split-TF32 products
+    on tcgen05) against a float64 decode of the feature sums it saves: the
+    predictions within 1e-5 of the prediction scale, and every ReLU bit equal
+    to the sign of the float64 pre-activation wherever that lies beyond 1e-6
+    of zero (units nearer zero are settled by a float32 evaluation, whose
+    rounding may differ from float64's)."""
+    from nglod_gb300 import _lib
+    net = seeded_model(num_lods=5, base_lod=2, seed=8).to(cuda)
+    with torch.no_grad():
+        for fv in net.features:
+            fv.fm.normal_(0.0, 0.05)
+    g = torch.Generator(device="cpu").manual_seed(n)
+    x = (torch.rand(n, 3, generator=g) * 2.2 - 1.1).to(cuda)
+    L = mask.bit_length() - 1
+    preds = torch.zeros(L + 1, n, device=cuda)
+    feats = torch.empty(L + 1, n, 32, device=cuda)
+    relu = torch.empty(L + 1, n, 4, device=cuda, dtype=torch.int32)
+    lib = _lib.load()
+    _lib.check(lib.nglod_sdf_fwd_train(net.dense_model(), _lib.ptr(x), n, mask, _lib.ptr(preds), _lib.ptr(feats),
+                                       _lib.ptr(relu), _lib.stream_ptr(cuda)), "nglod_sdf_fwd_train")
+    torch.cuda.synchronize()
+    check_backward_status()
+    xn = x.cpu().double().numpy()
+    fn = feats.cpu().double().numpy()
+    bits = relu.cpu().numpy().view(np.uint32)
+    for l in range(L + 1):
+        if not (mask >> l) & 1:
+            continue
+        lin0, lin1 = net.louts[l][0], net.louts[l][2]
+        w0 = lin0.weight.detach().cpu().double().numpy()
+        b0 = lin0.bias.detach().cpu().double().numpy()
+        w1 = lin1.weight.detach().cpu().double().numpy()[0]
+        b1 = lin1.bias.detach().cpu().double().numpy()[0]
+        pre = np.concatenate([xn, fn[l]], axis=1) @ w0.T + b0
+        want = np.maximum(pre, 0.0) @ w1 + b1
+        got = preds[l].cpu().double().numpy()
+        assert np.abs(got - want).max() <= 1e-5 * np.abs(want).max(), l
+        on = ((bits[l][:, :, None] >> np.arange(32, dtype=np.uint32)) & 1).reshape(n, 128).astype(bool)
+        settled = np.abs(pre) > 1e-6
+        assert ((on == (pre > 0)) | ~settled).all(), l
+        assert settled.mean() > 0.99
