@@ -72,7 +72,7 @@ def parse():
     p.add_argument("--warmup", type=int, default=10)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--no-extras", action="store_true", help="skip the trace and CPU-baseline legs")
-    p.add_argument("--only", choices=["trace", "train", "sparse", "serve", "shade", "mesh"], default=None,
+    p.add_argument("--only", choices=["trace", "summed", "train", "sparse", "serve", "shade", "mesh"], default=None,
                    help="run one extra leg alone (profiling); prints its JSON")
     return p.parse_args()
 
@@ -285,6 +285,7 @@ def run_ours(args):
     extras = {}
     if not args.no_extras:
         extras["trace"] = bench_trace(net, bnet, dev, flush, stream)
+        extras["summed"] = bench_summed(net, bnet, x, dev, flush, stream)
 
     if not args.no_extras:
         extras["serve"] = bench_serve(dev)
@@ -317,6 +318,40 @@ def run_ours(args):
         }
         line.update(extras)
         print(json.dumps(line), flush=True)
+
+
+def bench_summed(net, bnet, x, dev, flush, stream, steps=100):
+    """The BF16 form over LOD-summed volumes (Bf16OctreeSDF(summed=True)):
+    the headline workload with one 8-corner gather per query instead of
+    LOD + 1, against the per-LOD BF16 form on the same points, plus the
+    tracer over the same volumes."""
+    import nglod_gb300 as ng
+    from nglod_gb300 import synthetic
+    from nglod_gb300.bf16 import Bf16OctreeSDF
+    from nglod_gb300.options import default_args
+    sb = Bf16OctreeSDF(net, summed=True)
+    for _ in range(3):
+        got = sb.sdf(x, lod=LOD)
+    torch.cuda.synchronize()
+    ms = time_steps(lambda: sb.sdf(x, lod=LOD), steps, flush, stream) / steps
+    sb.check_status()
+    d = (got - bnet.sdf(x, lod=LOD)).abs()
+    ro, rd = synthetic.look_at_rays(width=TRACE_W, height=TRACE_H)
+    ro, rd = ro.to(dev), rd.to(dev)
+    fused = ng.SphereTracer(default_args(num_steps=TRACE_STEPS))
+    for _ in range(3):
+        rbs = fused(sb, ro, rd)
+    torch.cuda.synchronize()
+    tms = time_steps(lambda: fused(sb, ro, rd), 10, flush, stream) / 10
+    rb16 = fused(bnet, ro, rd)
+    sb.check_status()
+    return {"form": "BF16 over LOD-summed volumes: volume l = sum of the samples of volumes 0..l at LOD l's "
+                    "vertices (float64, one bf16 rounding); a query samples volume LOD alone",
+            "value": N_POINTS / (ms / 1e3), "unit": UNIT, "ms_per_step": ms, "steps": steps,
+            "gathered_bytes_per_query": 8 * 32 * 2,
+            "vs_per_lod_bf16_max_abs": float(d.max().item()), "vs_per_lod_bf16_mean_abs": float(d.mean().item()),
+            "trace_ms": tms, "trace_rays_per_s": ro.shape[0] / (tms / 1e3),
+            "trace_hit_agreement_vs_per_lod_bf16": float((rbs.hit == rb16.hit).float().mean().item())}
 
 
 def bench_trace(net, bnet, dev, flush, stream):
@@ -668,6 +703,16 @@ def run_only(args):
     stream = torch.cuda.current_stream(dev)
     if args.only == "trace":
         out = bench_trace(net, Bf16OctreeSDF(net), dev, flush, stream)
+    elif args.only == "summed":
+        from nglod_gb300 import synthetic
+        x = synthetic.near_surface_query(N_POINTS, *synthetic.sphere_union(1), seed=1).to(dev)
+        bnet = Bf16OctreeSDF(net)
+        for _ in range(3):
+            bnet.sdf(x, lod=LOD)
+        torch.cuda.synchronize()
+        k = max(args.steps, 1) if args.steps != 500 else 100
+        per_lod_ms = time_steps(lambda: bnet.sdf(x, lod=LOD), k, flush, stream) / k
+        out = {"per_lod_bf16_ms": per_lod_ms, **bench_summed(net, bnet, x, dev, flush, stream, steps=k)}
     elif args.only == "train":
         out = bench_train(dev, flush, stream, steps=max(args.steps, 1), warm=max(args.warmup, 1), train_steps=0)
     elif args.only == "sparse":

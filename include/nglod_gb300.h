@@ -155,6 +155,11 @@ typedef struct nglod_bf16_model {
      * (one 128-byte line per vertex and its +x neighbour) instead of grid;
      * results are identical.  NULL: grid is read. */
     const void  *grid_pairs[NGLOD_MAX_LODS];
+    /* Nonzero: grid[l] (and grid_pairs[l]) hold LOD-summed volumes from
+     * nglod_bf16_build_summed, and a query at lod L samples volume L alone
+     * (one gather instead of L + 1).  0: per-LOD volumes, summed per query
+     * as OctreeSDF.sdf does. */
+    int32_t summed;
 } nglod_bf16_model;
 
 /* Pair volume of one bf16 volume grid [s][s][s][32]: pairs [s][s][s][2][32]
@@ -162,6 +167,16 @@ typedef struct nglod_bf16_model {
  * | v(z,y,min(x+1,s-1)) channels 8c..8c+7].  grid 16-byte aligned, pairs
  * 32-byte aligned, s in 2..1025. */
 int nglod_bf16_build_pairs(const void *grid, int32_t s, void *pairs, nglod_stream_t stream);
+
+/* LOD-summed volume `lod` of a float32 model, for nglod_bf16_model with
+ * summed = 1: out[s][s][s][32] bf16 (s = 2^(lod + base_lod) + 1, 16-byte
+ * aligned), vertex v = sum over LODs i <= lod of volume i's trilinear sample
+ * (align_corners, border clamp) at v, computed in float64 and rounded once
+ * to bf16.  Grid spacings halve from LOD to LOD, so each cell of LOD `lod`
+ * lies inside one cell of every coarser grid and a trilinear sample of out
+ * equals the running feature sum of OctreeSDF.sdf (OctreeSDF.py:109-110) up
+ * to rounding.  Reads model->grid[0..lod] only. */
+int nglod_bf16_build_summed(const nglod_dense_model *model, int32_t lod, void *out, nglod_stream_t stream);
 
 #define NGLOD_BF16_TILE_BYTES 12288
 

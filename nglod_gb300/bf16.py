@@ -33,16 +33,35 @@ def pack_decoder_tile(w0, b0):
 class Bf16OctreeSDF:
     """pairs: also keep each volume as a pair volume (every vertex beside
     its +x neighbour, nglod_bf16_build_pairs; twice the volume bytes), which
-    point queries read with whole 128-byte lines; results are identical."""
+    point queries read with whole 128-byte lines; results are identical.
 
-    def __init__(self, net, pairs=True):
+    summed: keep LOD-summed volumes instead of the per-LOD ones
+    (nglod_bf16_build_summed): volume l holds, at each of LOD l's vertices,
+    the sum of the trilinear samples of volumes 0..l there, in float64
+    rounded once to bf16.  Each cell of LOD l lies inside one cell of every
+    coarser grid, so sampling volume l alone gives the running feature sum
+    up to rounding, and a query at lod L gathers one volume instead of
+    L + 1.  Same memory as the per-LOD volumes; a different bf16 rounding of
+    the same features (one rounding of the sum instead of one per LOD)."""
+
+    def __init__(self, net, pairs=True, summed=False):
         _lib.require_cuda(net.features[0].fm)
         dev = net.features[0].fm.device
         self.num_lods = net.num_lods
         self.base_lod = net.base_lod
         self.lod = net.lod
-        self.grids = [fv.fm.detach().to(torch.bfloat16).contiguous(memory_format=torch.channels_last_3d)
-                      for fv in net.features]
+        self.summed = bool(summed)
+        if self.summed:
+            dm = net.dense_model()
+            self.grids = []
+            for i, fv in enumerate(net.features):
+                g = torch.empty_like(fv.fm, dtype=torch.bfloat16, memory_format=torch.channels_last_3d)
+                _lib.check(_lib.load().nglod_bf16_build_summed(dm, i, g.data_ptr(), _lib.stream_ptr(dev)),
+                           "nglod_bf16_build_summed")
+                self.grids.append(g)
+        else:
+            self.grids = [fv.fm.detach().to(torch.bfloat16).contiguous(memory_format=torch.channels_last_3d)
+                          for fv in net.features]
         self.tiles, self.b0, self.w1, self.b1 = [], [], [], []
         for dec in net.louts:
             self.tiles.append(pack_decoder_tile(dec[0].weight, dec[0].bias).to(dev))
@@ -65,6 +84,7 @@ class Bf16OctreeSDF:
                            "nglod_bf16_build_pairs")
                 self.pairs.append(pv)
                 m.grid_pairs[i] = pv.data_ptr()
+        m.summed = int(self.summed)
         self._m = m
         self._status = torch.zeros(1, dtype=torch.int32, device=dev)
 

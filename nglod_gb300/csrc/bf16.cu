@@ -61,7 +61,7 @@ __device__ __forceinline__ void gather_warp_rows(const nglod_bf16_model &m, int 
 #pragma unroll
         for (int c = 0; c < kQ; ++c) acc[p][c] = make_float2(0.f, 0.f);
 #pragma unroll 1
-    for (int l = 0; l <= L; ++l) {
+    for (int l = m.summed ? L : 0; l <= L; ++l) {
         const uint4 *g = static_cast<const uint4 *>(m.grid[l]);  // 4 uint4 per vertex
         const int s = (1 << (l + m.base_lod)) + 1;
         const int sy = s * 4, sz = s * sy;
@@ -126,7 +126,7 @@ __device__ __forceinline__ void gather_warp_pairs(const nglod_bf16_model &m, int
 #pragma unroll
         for (int c = 0; c < 4; ++c) acc[p][c] = make_float2(0.f, 0.f);
 #pragma unroll 1
-    for (int l = 0; l <= L; ++l) {
+    for (int l = m.summed ? L : 0; l <= L; ++l) {
         const PairUnit *g = static_cast<const PairUnit *>(m.grid_pairs[l]) + part;  // 4 units per line
         const int s = (1 << (l + m.base_lod)) + 1;
         const int sy = s * 4, sz = s * sy;
@@ -193,6 +193,43 @@ __global__ void build_pairs_kernel(const uint4 *__restrict__ grid, int s, int64_
         const int c = (int)((i >> 1) & 3), h = (int)(i & 1);
         const int64_t src = v + ((h && (v % s) + 1 < s) ? 1 : 0);
         pairs[i] = grid[4 * src + c];
+    }
+}
+
+// LOD-summed volume L: vertex (z, y, x) of LOD L's grid holds the sum over
+// LODs i <= L of volume i's trilinear sample at that vertex.  Grid spacings
+// halve from LOD to LOD, so the vertex lies at coarse coordinate
+// (x >> (L - i)) + fraction (x mod 2^(L-i)) / 2^(L-i) of volume i, and every
+// cell of LOD L lies inside one cell of each coarser grid: a trilinear
+// function restricted to a sub-box is trilinear, so trilinear sampling of
+// this volume equals the sum of the per-LOD samples (with the same border
+// clamp) up to rounding.  Samples and sum in float64 (dyadic weights, exact
+// products), one rounding to bf16.  Thread per (vertex, channel).
+__global__ void build_summed_kernel(const nglod_dense_model m, int L, int64_t count, __nv_bfloat16 *__restrict__ out) {
+    const int C = m.feature_dim;
+    const int sL = (1 << (L + m.base_lod)) + 1;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < count; t += stride) {
+        const int c = (int)(t % C);
+        const int64_t v = t / C;
+        const int ix = (int)(v % sL), iy = (int)((v / sL) % sL), iz = (int)(v / ((int64_t)sL * sL));
+        double sum = 0.0;
+        for (int i = 0; i <= L; ++i) {
+            const int sh = L - i, s = (1 << (i + m.base_lod)) + 1;
+            const double inv = 1.0 / (double)(1 << sh);
+            const int x0 = ix >> sh, y0 = iy >> sh, z0 = iz >> sh;
+            const double fx = (ix & ((1 << sh) - 1)) * inv, fy = (iy & ((1 << sh) - 1)) * inv,
+                         fz = (iz & ((1 << sh) - 1)) * inv;
+            const int x1 = min(x0 + 1, s - 1), y1 = min(y0 + 1, s - 1), z1 = min(z0 + 1, s - 1);
+            const float *g = static_cast<const float *>(m.grid[i]);
+            auto at = [&](int z, int y, int x) { return (double)g[(((int64_t)z * s + y) * s + x) * C + c]; };
+            const double c00 = at(z0, y0, x0) * (1.0 - fx) + at(z0, y0, x1) * fx;
+            const double c01 = at(z0, y1, x0) * (1.0 - fx) + at(z0, y1, x1) * fx;
+            const double c10 = at(z1, y0, x0) * (1.0 - fx) + at(z1, y0, x1) * fx;
+            const double c11 = at(z1, y1, x0) * (1.0 - fx) + at(z1, y1, x1) * fx;
+            sum += (c00 * (1.0 - fy) + c01 * fy) * (1.0 - fz) + (c10 * (1.0 - fy) + c11 * fy) * fz;
+        }
+        out[t] = __double2bfloat16(sum);
     }
 }
 
@@ -608,7 +645,7 @@ __global__ void __launch_bounds__(kTP, 4) trace_bf16_tc_kernel(const Bf16TraceAr
 #pragma unroll
             for (int c = 0; c < 16; ++c) acc[c] = 0.f;
 #pragma unroll 1
-            for (int l = 0; l <= a.L; ++l)
+            for (int l = a.m.summed ? a.L : 0; l <= a.L; ++l)
                 gather_bf16_half(static_cast<const __nv_bfloat16 *>(a.m.grid[l]), (1 << (l + a.m.base_lod)) + 1, pt.x,
                                  pt.y, pt.z, lane % kLPP, acc);
             write_tile_row_half(sA, row, lane % kLPP, acc, pt.x, pt.y, pt.z);
@@ -761,6 +798,23 @@ extern "C" int nglod_bf16_build_pairs(const void *grid, int32_t s, void *pairs, 
     build_pairs_kernel<<<(int)(want < cap ? want : cap), 256, 0, (cudaStream_t)stream>>>(
         static_cast<const uint4 *>(grid), s, units, static_cast<uint4 *>(pairs));
     return launch_status("nglod_bf16_build_pairs");
+}
+
+extern "C" int nglod_bf16_build_summed(const nglod_dense_model *model, int32_t lod, void *out, nglod_stream_t stream) {
+    NGLOD_REQUIRE(model && out, NGLOD_ERR_INVALID, "null pointer argument");
+    NGLOD_REQUIRE(model->feature_dim == 32, NGLOD_ERR_INVALID, "feature_dim=%d (32 supported)", model->feature_dim);
+    NGLOD_REQUIRE(model->base_lod >= 0 && model->num_lods - 1 + model->base_lod <= 9, NGLOD_ERR_INVALID,
+                  "base_lod=%d num_lods=%d", model->base_lod, model->num_lods);
+    NGLOD_REQUIRE(lod >= 0 && lod < model->num_lods, NGLOD_ERR_INVALID, "lod=%d outside 0..%d", lod,
+                  model->num_lods - 1);
+    for (int l = 0; l <= lod; ++l) NGLOD_REQUIRE(model->grid[l], NGLOD_ERR_INVALID, "volume %d is null", l);
+    NGLOD_REQUIRE(aligned(out, 16), NGLOD_ERR_ALIGN, "out must be 16-byte aligned");
+    const int64_t s = ((int64_t)1 << (lod + model->base_lod)) + 1;
+    const int64_t count = s * s * s * 32;
+    const int64_t want = (count + 255) / 256, cap = (int64_t)num_sms() * 16;
+    build_summed_kernel<<<(int)(want < cap ? want : cap), 256, 0, (cudaStream_t)stream>>>(
+        *model, lod, count, static_cast<__nv_bfloat16 *>(out));
+    return launch_status("nglod_bf16_build_summed");
 }
 
 extern "C" int nglod_sdf_fwd_bf16(const nglod_bf16_model *model, const float *x, int64_t n, int32_t lod, float *out,

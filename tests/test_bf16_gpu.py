@@ -24,14 +24,16 @@ def _bf16(a):
     return r.astype(np.uint32).view(np.float32)
 
 
-def emulate(m, x, lod):
+def emulate(m, x, lod, rounded=False):
     """The BF16 form's arithmetic in numpy: bf16 volumes, fp32 LOD sum rounded
     to bf16, positions and b0 as bf16 hi + lo, bf16 first-layer weights,
-    products accumulated in float64, ReLU / second layer in float32."""
+    products accumulated in float64, ReLU / second layer in float32.
+    rounded: m's volumes already hold bf16 values."""
     x = x.astype(np.float32)
     acc = np.zeros((x.shape[0], 32), np.float32)
     for i in range(lod + 1):
-        acc += dense.feature_volume(_bf16(m["fms"][i]).astype(np.float32), x)
+        fm = m["fms"][i] if rounded else _bf16(m["fms"][i])
+        acc += dense.feature_volume(fm.astype(np.float32), x)
     f = _bf16(acc)
     hi = _bf16(x)
     lo = _bf16(x - hi)
@@ -42,6 +44,28 @@ def emulate(m, x, lod):
     h = f.astype(np.float64) @ w0[:, 3:].T + hi.astype(np.float64) @ w0[:, :3].T + lo.astype(np.float64) @ w0[:, :3].T
     h = np.maximum((h + b0h + b0l).astype(np.float32), 0)
     return (h @ m["w1"][lod].astype(np.float32).T + m["b1"][lod].astype(np.float32))
+
+
+def summed_volume64(m, lod):
+    """LOD-summed volume `lod` in float64, [C, s, s, s]: at every vertex of
+    LOD lod's grid, the sum of the trilinear samples of volumes 0..lod."""
+    s = m["fms"][lod].shape[-1]
+    t = np.linspace(-1.0, 1.0, s)
+    z, y, x = np.meshgrid(t, t, t, indexing="ij")
+    pts = np.stack([x.ravel(), y.ravel(), z.ravel()], axis=1)  # x -> W, y -> H, z -> D
+    acc = np.zeros((pts.shape[0], m["fms"][lod].shape[0]))
+    for i in range(lod + 1):
+        acc += dense.feature_volume(m["fms"][i].astype(np.float64), pts)
+    return acc.T.reshape(-1, s, s, s)
+
+
+def emulate_summed(m, x, lod):
+    """emulate() for Bf16OctreeSDF(summed=True): volume lod = the LOD-summed
+    volume rounded once to bf16, sampled alone."""
+    x = x.astype(np.float32)
+    sv = _bf16(summed_volume64(m, lod).astype(np.float32))
+    one = {"fms": [sv], "w0": [m["w0"][lod]], "b0": [m["b0"][lod]], "w1": [m["w1"][lod]], "b1": [m["b1"][lod]]}
+    return emulate(one, x, 0, rounded=True)
 
 
 @pytest.fixture(scope="module")
@@ -210,3 +234,65 @@ def test_tensor_core_wait_timeout_reports_status_and_recovers(nets):
     again = bnet.sdf(x, lod=2)
     bnet.check_status()
     assert torch.equal(again, good)
+
+
+@pytest.fixture(scope="module")
+def summed(nets):
+    net = nets[0]
+    return Bf16OctreeSDF(net, summed=True)
+
+
+def test_summed_volumes_are_the_float64_sums_rounded_once(nets, summed):
+    """nglod_bf16_build_summed: every value is the float64 LOD sum at that
+    vertex rounded to the nearest bf16 (within half a bf16 ulp, ties either
+    way); the pair volumes are built from the summed volumes."""
+    _, _, m32, _, _ = nets
+    assert summed.summed and len(summed.pairs) == summed.num_lods
+    for lod in range(summed.num_lods):
+        want = summed_volume64(m32, lod)
+        got = summed.grids[lod][0].float().cpu().numpy().astype(np.float64)
+        assert got.shape == want.shape
+        ulp = 2.0 ** (np.floor(np.log2(np.maximum(np.abs(want), 1e-30))) - 7)
+        assert (np.abs(got - want) <= 0.5 * ulp * (1 + 1e-9)).all(), lod
+        if lod == 0:  # LOD 0 alone: the bf16 rounding of the volume itself
+            assert torch.equal(summed.grids[0], nets[1].grids[0])
+
+
+@pytest.mark.parametrize("n", [1, 129, 65_536])
+def test_summed_form_matches_emulation_and_fp64(nets, summed, n):
+    """Queries through LOD-summed volumes (one gather per query) against
+    their numpy emulation (tight) and the FP64 oracle (the per-LOD form's
+    bounds), every LOD, near-surface points plus points outside the box."""
+    net, bnet, m32, m64, (c, r) = nets
+    dev = net.features[0].fm.device
+    x = synthetic.near_surface_query(n, c, r, seed=3)
+    x[: n // 8] *= 1.3
+    report = {}
+    for lod in range(summed.num_lods):
+        got = summed.sdf(x.to(dev), lod=lod).cpu().numpy()
+        np.testing.assert_allclose(got, emulate_summed(m32, x.numpy(), lod), atol=2e-4, rtol=0)
+        err = np.abs(got - dense.sdf(m64, x.numpy().astype(np.float64), lod=lod))
+        report[lod] = (err.max(), err.mean())
+        assert err.max() < 2e-2 and err.mean() < 2e-3, (lod, err.max(), err.mean())
+    summed.check_status()
+    print("summed bf16 error vs fp64 oracle per lod (max, mean):", report)
+
+
+def test_summed_form_trace_against_fp64_oracle(nets, summed):
+    """The BF16 tracer over LOD-summed volumes: same bounds against the FP64
+    oracle trace as the per-LOD form."""
+    from oracle import cref
+    net, _, _, m64, _ = nets
+    dev = net.features[0].fm.device
+    ro, rd = synthetic.look_at_rays(width=96, height=96)
+    rb = ng.SphereTracer(default_args(num_steps=128))(summed, ro.to(dev), rd.to(dev))
+    summed.check_status()
+    x, t, hit, normal = dense.sphere_trace(m64, ro.numpy().astype(np.float64), rd.numpy().astype(np.float64),
+                                           num_steps=128, aabb_fn=lambda o, d: tuple(
+                                               v.astype(np.float64) if v.dtype != bool else v
+                                               for v in cref.aabb(o.astype(np.float32), d.astype(np.float32))))
+    h = rb.hit.cpu().numpy()
+    assert (h == hit).mean() > 0.995
+    both = h & hit
+    err = np.abs(rb.depth.cpu().numpy()[both] - t[both])
+    assert err.mean() < 1e-3 and np.percentile(err, 99) < 5e-3
