@@ -710,7 +710,7 @@ def run_only(args):
         for _ in range(3):
             bnet.sdf(x, lod=LOD)
         torch.cuda.synchronize()
-        k = max(args.steps, 1) if args.steps != 500 else 100
+        k = min(max(args.steps, 1), 100)
         per_lod_ms = time_steps(lambda: bnet.sdf(x, lod=LOD), k, flush, stream) / k
         out = {"per_lod_bf16_ms": per_lod_ms, **bench_summed(net, bnet, x, dev, flush, stream, steps=k)}
     elif args.only == "train":
