@@ -581,6 +581,13 @@ def bench_sparse(net, dev, flush, stream, level=7, lod=4, steps=64):
     sp.check_status()
     sp32.render(ro, rd, lod=lod, num_steps=steps)
     ms32 = time_steps(lambda: sp32.render(ro, rd, lod=lod, num_steps=steps), reps, flush, stream) / reps
+    # LOD-summed corner features: one voxel's corners per query
+    sps = SparseSDF.from_dense(net, s, precision="bf16", summed=True)
+    for _ in range(3):
+        (_, ts, hits, _), _ = sps.render(ro, rd, lod=lod, num_steps=steps)
+    torch.cuda.synchronize()
+    ms_sum = time_steps(lambda: sps.render(ro, rd, lod=lod, num_steps=steps), reps, flush, stream) / reps
+    sps.check_status()
     net.lod = lod
     rb = ng.SphereTracer(default_args(num_steps=128))(net, ro, rd)
     net.lod = None
@@ -591,6 +598,8 @@ def bench_sparse(net, dev, flush, stream, level=7, lod=4, steps=64):
                         f"{steps} steps, bf16 corner features, tcgen05 bf16 decoder",
             "frame_ms": ms, "rays_per_s": TRACE_W * TRACE_H / (ms / 1e3), "traversal_ms": ms_trav,
             "frame_ms_f32_decoder": ms32,
+            "frame_ms_summed": ms_sum,
+            "summed_hit_agreement": float((hits == hit).float().mean().item()),
             "nuggets": int(nug.shape[0]), "setup_s": setup_s,
             "vs_dense_f32": {"hit_agreement": float((hit == rb.hit).float().mean().item()),
                              "depth_median_abs": float((t[both] - rb.depth[both]).abs().median().item()),

@@ -156,7 +156,7 @@ typedef struct nglod_bf16_model {
      * results are identical.  NULL: grid is read. */
     const void  *grid_pairs[NGLOD_MAX_LODS];
     /* Nonzero: grid[l] (and grid_pairs[l]) hold LOD-summed volumes from
-     * nglod_bf16_build_summed, and a query at lod L samples volume L alone
+     * nglod_build_summed_volume, and a query at lod L samples volume L alone
      * (one gather instead of L + 1).  0: per-LOD volumes, summed per query
      * as OctreeSDF.sdf does. */
     int32_t summed;
@@ -168,15 +168,18 @@ typedef struct nglod_bf16_model {
  * 32-byte aligned, s in 2..1025. */
 int nglod_bf16_build_pairs(const void *grid, int32_t s, void *pairs, nglod_stream_t stream);
 
-/* LOD-summed volume `lod` of a float32 model, for nglod_bf16_model with
- * summed = 1: out[s][s][s][32] bf16 (s = 2^(lod + base_lod) + 1, 16-byte
- * aligned), vertex v = sum over LODs i <= lod of volume i's trilinear sample
- * (align_corners, border clamp) at v, computed in float64 and rounded once
- * to bf16.  Grid spacings halve from LOD to LOD, so each cell of LOD `lod`
- * lies inside one cell of every coarser grid and a trilinear sample of out
- * equals the running feature sum of OctreeSDF.sdf (OctreeSDF.py:109-110) up
- * to rounding.  Reads model->grid[0..lod] only. */
-int nglod_bf16_build_summed(const nglod_dense_model *model, int32_t lod, void *out, nglod_stream_t stream);
+/* LOD-summed volume `lod` of a float32 model: out[s][s][s][32] (s =
+ * 2^(lod + base_lod) + 1, 16-byte aligned) of dtype NGLOD_F32 (float) or
+ * NGLOD_BF16, vertex v = sum over LODs i <= lod of volume i's trilinear
+ * sample (align_corners, border clamp) at v, computed in float64 and
+ * rounded once.  Grid spacings halve from LOD to LOD, so each cell of LOD
+ * `lod` lies inside one cell of every coarser grid and a trilinear sample
+ * of out equals the running feature sum of OctreeSDF.sdf
+ * (OctreeSDF.py:109-110) up to rounding.  Reads model->grid[0..lod] only.
+ * bf16 volumes feed nglod_bf16_model with summed = 1; float volumes feed
+ * nglod_sparse_build for nglod_sparse_model with summed = 1. */
+int nglod_build_summed_volume(const nglod_dense_model *model, int32_t lod, int32_t dtype, void *out,
+                              nglod_stream_t stream);
 
 #define NGLOD_BF16_TILE_BYTES 12288
 
@@ -442,6 +445,12 @@ typedef struct nglod_sparse_model {
      * nglod_sparse_trace_tc reads a voxel's corners of every level from its
      * own row instead of walking `parent` (identical results). */
     const int32_t *corner_chain[NGLOD_MAX_LODS];
+    /* Nonzero: corner_feats come from LOD-summed volumes
+     * (nglod_build_summed_volume, then nglod_sparse_build), and every query
+     * at lod L samples the corners of its level-(L+2) voxel alone instead of
+     * adding its ancestors' samples (equal up to rounding: each ancestor
+     * contains the point). */
+    int32_t summed;
 } nglod_sparse_model;
 
 /* SDF::initTrinkets + the corner export of SOL_NGLOD (SDF.cu:141-216,

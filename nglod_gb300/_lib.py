@@ -89,6 +89,7 @@ class SparseModel(ctypes.Structure):
         ("b1", _vp * MAX_LODS),
         ("w0_tile", _vp * MAX_LODS),
         ("corner_chain", _vp * MAX_LODS),
+        ("summed", _i32),
     ]
 
 
@@ -226,7 +227,7 @@ SIGNATURES = {
                                              _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "nglod_bf16_pack_decoder": (ctypes.c_int, [_vp, _vp, _i32, _i32, _vp]),
     "nglod_bf16_build_pairs": (ctypes.c_int, [_vp, _i32, _vp, _vp]),
-    "nglod_bf16_build_summed": (ctypes.c_int, [ctypes.POINTER(DenseModel), _i32, _vp, _vp]),
+    "nglod_build_summed_volume": (ctypes.c_int, [ctypes.POINTER(DenseModel), _i32, _i32, _vp, _vp]),
     "nglod_debug_mma_wait_polls": (ctypes.c_int, [_i64]),
     "nglod_sdf_fwd_bf16": (ctypes.c_int, [ctypes.POINTER(Bf16Model), _vp, _i64, _i32, _vp, _vp, _vp]),
     "nglod_trace_bf16": (ctypes.c_int, [ctypes.POINTER(Bf16Model), ctypes.POINTER(TraceParams), _vp, _vp, _i64,

@@ -36,7 +36,7 @@ class Bf16OctreeSDF:
     point queries read with whole 128-byte lines; results are identical.
 
     summed: keep LOD-summed volumes instead of the per-LOD ones
-    (nglod_bf16_build_summed): volume l holds, at each of LOD l's vertices,
+    (nglod_build_summed_volume): volume l holds, at each of LOD l's vertices,
     the sum of the trilinear samples of volumes 0..l there, in float64
     rounded once to bf16.  Each cell of LOD l lies inside one cell of every
     coarser grid, so sampling volume l alone gives the running feature sum
@@ -56,8 +56,8 @@ class Bf16OctreeSDF:
             self.grids = []
             for i, fv in enumerate(net.features):
                 g = torch.empty_like(fv.fm, dtype=torch.bfloat16, memory_format=torch.channels_last_3d)
-                _lib.check(_lib.load().nglod_bf16_build_summed(dm, i, g.data_ptr(), _lib.stream_ptr(dev)),
-                           "nglod_bf16_build_summed")
+                _lib.check(_lib.load().nglod_build_summed_volume(dm, i, _lib.BF16, g.data_ptr(),
+                                                                 _lib.stream_ptr(dev)), "nglod_build_summed_volume")
                 self.grids.append(g)
         else:
             self.grids = [fv.fm.detach().to(torch.bfloat16).contiguous(memory_format=torch.channels_last_3d)

@@ -8,6 +8,8 @@
 // by tcgen05.mma on 128-point tiles with the accumulator in tensor memory.
 // b0, ReLU and the 128 -> 1 layer are an fp32 epilogue on the TMEM rows.
 #include <cuda_bf16.h>
+
+#include <algorithm>
 #include <string.h>
 
 #include "bf16_tile.cuh"
@@ -204,8 +206,9 @@ __global__ void build_pairs_kernel(const uint4 *__restrict__ grid, int s, int64_
 // function restricted to a sub-box is trilinear, so trilinear sampling of
 // this volume equals the sum of the per-LOD samples (with the same border
 // clamp) up to rounding.  Samples and sum in float64 (dyadic weights, exact
-// products), one rounding to bf16.  Thread per (vertex, channel).
-__global__ void build_summed_kernel(const nglod_dense_model m, int L, int64_t count, __nv_bfloat16 *__restrict__ out) {
+// products), one rounding to T (float or bf16).  Thread per (vertex, channel).
+template <typename T>
+__global__ void build_summed_kernel(const nglod_dense_model m, int L, int64_t count, T *__restrict__ out) {
     const int C = m.feature_dim;
     const int sL = (1 << (L + m.base_lod)) + 1;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -229,7 +232,10 @@ __global__ void build_summed_kernel(const nglod_dense_model m, int L, int64_t co
             const double c11 = at(z1, y1, x0) * (1.0 - fx) + at(z1, y1, x1) * fx;
             sum += (c00 * (1.0 - fy) + c01 * fy) * (1.0 - fz) + (c10 * (1.0 - fy) + c11 * fy) * fz;
         }
-        out[t] = __double2bfloat16(sum);
+        if constexpr (sizeof(T) == 4)
+            out[t] = (float)sum;
+        else
+            out[t] = __double2bfloat16(sum);
     }
 }
 
@@ -800,21 +806,26 @@ extern "C" int nglod_bf16_build_pairs(const void *grid, int32_t s, void *pairs, 
     return launch_status("nglod_bf16_build_pairs");
 }
 
-extern "C" int nglod_bf16_build_summed(const nglod_dense_model *model, int32_t lod, void *out, nglod_stream_t stream) {
+extern "C" int nglod_build_summed_volume(const nglod_dense_model *model, int32_t lod, int32_t dtype, void *out,
+                                         nglod_stream_t stream) {
     NGLOD_REQUIRE(model && out, NGLOD_ERR_INVALID, "null pointer argument");
     NGLOD_REQUIRE(model->feature_dim == 32, NGLOD_ERR_INVALID, "feature_dim=%d (32 supported)", model->feature_dim);
     NGLOD_REQUIRE(model->base_lod >= 0 && model->num_lods - 1 + model->base_lod <= 9, NGLOD_ERR_INVALID,
                   "base_lod=%d num_lods=%d", model->base_lod, model->num_lods);
     NGLOD_REQUIRE(lod >= 0 && lod < model->num_lods, NGLOD_ERR_INVALID, "lod=%d outside 0..%d", lod,
                   model->num_lods - 1);
+    NGLOD_REQUIRE(dtype == NGLOD_F32 || dtype == NGLOD_BF16, NGLOD_ERR_INVALID, "dtype=%d", dtype);
     for (int l = 0; l <= lod; ++l) NGLOD_REQUIRE(model->grid[l], NGLOD_ERR_INVALID, "volume %d is null", l);
     NGLOD_REQUIRE(aligned(out, 16), NGLOD_ERR_ALIGN, "out must be 16-byte aligned");
     const int64_t s = ((int64_t)1 << (lod + model->base_lod)) + 1;
     const int64_t count = s * s * s * 32;
-    const int64_t want = (count + 255) / 256, cap = (int64_t)num_sms() * 16;
-    build_summed_kernel<<<(int)(want < cap ? want : cap), 256, 0, (cudaStream_t)stream>>>(
-        *model, lod, count, static_cast<__nv_bfloat16 *>(out));
-    return launch_status("nglod_bf16_build_summed");
+    const int grid = (int)std::min<int64_t>((count + 255) / 256, (int64_t)num_sms() * 16);
+    if (dtype == NGLOD_F32)
+        build_summed_kernel<float><<<grid, 256, 0, (cudaStream_t)stream>>>(*model, lod, count, static_cast<float *>(out));
+    else
+        build_summed_kernel<__nv_bfloat16>
+            <<<grid, 256, 0, (cudaStream_t)stream>>>(*model, lod, count, static_cast<__nv_bfloat16 *>(out));
+    return launch_status("nglod_build_summed_volume");
 }
 
 extern "C" int nglod_sdf_fwd_bf16(const nglod_bf16_model *model, const float *x, int64_t n, int32_t lod, float *out,

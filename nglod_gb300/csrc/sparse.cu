@@ -60,8 +60,9 @@ __device__ __forceinline__ void sparse_features(const nglod_sparse_model &m, int
 #pragma unroll
     for (int c = 0; c < kC; ++c) f[c] = 0.f;
     const float nx = fmaf(px, 0.5f, 0.5f), ny = fmaf(py, 0.5f, 0.5f), nz = fmaf(pz, 0.5f, 0.5f);
+    const int last = m.summed ? lod + 2 : 2;  // LOD-summed features: the query level alone
 #pragma unroll 1
-    for (int lv = lod + 2; lv >= 2; --lv) {
+    for (int lv = lod + 2; lv >= last; --lv) {
         if (lv != lod + 2) g = m.parent[g];
         const float res = (float)(1 << lv);
         const float ux = nx * res, uy = ny * res, uz = nz * res;
@@ -332,8 +333,9 @@ __device__ __forceinline__ void sparse_features_quarter(const nglod_sparse_model
         na = __ldg(chain);
         nb = __ldg(chain + 1);
     }
+    const int last = m.summed ? lod + 2 : 2;  // LOD-summed features: the query level alone
 #pragma unroll 1
-    for (int lv = lod + 2; lv >= 2; --lv) {
+    for (int lv = lod + 2; lv >= last; --lv) {
         const int k = lod + 2 - lv;
         short4 p;
         int4 ca, cb;
@@ -341,7 +343,7 @@ __device__ __forceinline__ void sparse_features_quarter(const nglod_sparse_model
             p = make_short4((short)(pf.x >> k), (short)(pf.y >> k), (short)(pf.z >> k), 0);
             ca = na;
             cb = nb;
-            if (k < lod) {
+            if (k < lod && !m.summed) {
                 na = __ldg(chain + 2 * k + 2);
                 nb = __ldg(chain + 2 * k + 3);
             }

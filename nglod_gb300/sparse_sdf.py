@@ -36,11 +36,14 @@ def _u(t):
 
 class SparseSDF:
     def __init__(self, spc, corner_feats, corner_idx, parent, corner_counts, decoders, feat_dtype, decoder=None,
-                 chains=True):
+                 chains=True, summed=False):
         """chains (tensor-core decoder): also keep, per lod, every level-(lod+2)
         voxel's corner indices of all its ancestors in one row
         (nglod_sparse_build_chain), which the tensor-core trace reads instead
-        of walking the parent links; results are identical."""
+        of walking the parent links; results are identical.
+
+        summed: corner_feats hold LOD-summed features (from_dense(summed=
+        True)), and a query at lod samples its level-(lod+2) voxel alone."""
         if decoder is None:
             decoder = "tc" if feat_dtype == _lib.BF16 else "f32"
         if decoder not in ("tc", "f32") or (decoder == "tc" and feat_dtype != _lib.BF16):
@@ -53,6 +56,7 @@ class SparseSDF:
         self.corner_counts = list(corner_counts)
         self.decoders = decoders  # list of (w0 [H,35], b0 [H], w1 [1,H], b1 [1]) float32 on device
         self.feat_dtype = feat_dtype
+        self.summed = bool(summed)
         self.num_lods = len(decoders)
         self.hidden_dim = decoders[0][0].shape[0]
         self.tiles = []
@@ -63,7 +67,7 @@ class SparseSDF:
         self._status = torch.zeros(1, dtype=torch.int32, device=corner_feats.device)
         self._m = self._descriptor()
         self.chains = []
-        if decoder == "tc" and chains:
+        if decoder == "tc" and chains and not self.summed:
             self._build_chains()
 
     def _build_chains(self):
@@ -80,15 +84,32 @@ class SparseSDF:
 
     # -- construction ----------------------------------------------------------
     @classmethod
-    def from_dense(cls, net, spc, precision="fp16", half_weights=True, decoder=None):
+    def from_dense(cls, net, spc, precision="fp16", half_weights=True, decoder=None, summed=False):
         """Corner features of every occupied voxel of octree levels 2..num_lods+1
-        taken from net's feature volumes, and net's decoders."""
+        taken from net's feature volumes, and net's decoders.
+
+        summed: take them from net's LOD-summed volumes instead
+        (nglod_build_summed_volume: the sum of the samples of volumes 0..l at
+        LOD l's vertices, float64, one float32 rounding), so that a query at
+        lod samples the corners of its level-(lod+2) voxel alone: each
+        ancestor voxel contains the point, so the ancestors' samples that the
+        reference adds (sparse_grid_sample.cuh:52-107) are already in the
+        corner values, up to rounding."""
         if precision not in ("fp16", "f32", "bf16"):
             raise ValueError("precision must be 'fp16', 'f32' or 'bf16'")
         dev = spc.GetOctree().device
         vols = []
-        for fv in net.features:
-            v = fv.fm.detach().to(dev).float()
+        dm = net.dense_model() if summed else None
+        for i, fv in enumerate(net.features):
+            if summed:
+                _lib.require_cuda(fv.fm)
+                v = torch.empty_like(fv.fm, dtype=torch.float32, memory_format=torch.channels_last_3d)
+                _lib.check(_lib.load().nglod_build_summed_volume(dm, i, _lib.F32, v.data_ptr(),
+                                                                 _lib.stream_ptr(fv.fm.device)),
+                           "nglod_build_summed_volume")
+                v = v.to(dev)
+            else:
+                v = fv.fm.detach().to(dev).float()
             if precision == "fp16":
                 v = v.half().float()
             vols.append(v.contiguous(memory_format=torch.channels_last_3d))
@@ -99,10 +120,11 @@ class SparseSDF:
             if half_weights:
                 ws = [w.half().float() for w in ws]
             decs.append(tuple(w.contiguous() for w in ws))
-        return cls._build(spc, vols, decs, net.base_lod, _lib.BF16 if precision == "bf16" else _lib.F32, decoder)
+        return cls._build(spc, vols, decs, net.base_lod, _lib.BF16 if precision == "bf16" else _lib.F32, decoder,
+                          summed)
 
     @classmethod
-    def _build(cls, spc, vols, decs, base_lod, feat_dtype, decoder=None):
+    def _build(cls, spc, vols, decs, base_lod, feat_dtype, decoder=None, summed=False):
         nl = len(vols)
         dev = spc.GetOctree().device
         level = spc.GetLevel()
@@ -137,7 +159,7 @@ class SparseSDF:
             cf = feats[:total * 32].view(total, 32).clone()
         else:
             cf = feats.view(torch.bfloat16)[:total * 32].view(total, 32).clone()
-        return cls(spc, cf, corner_idx, parent, list(counts), decs, feat_dtype, decoder)
+        return cls(spc, cf, corner_idx, parent, list(counts), decs, feat_dtype, decoder, summed=summed)
 
     @classmethod
     def from_npz(cls, path, device="cuda", precision="f32", decoder=None):
@@ -172,6 +194,8 @@ class SparseSDF:
 
     def save_npz(self, path):
         """The reference's export format (SOL_NGLOD.save, SOL_NGLOD.py:80-100)."""
+        if self.summed:
+            raise ValueError("LOD-summed corner features have no place in the reference's npz format")
         cc = torch.cat([self.corner_coords(i) for i in range(self.num_lods)]).cpu().numpy().astype(np.uint8)
         cf = self.corner_feats.float().cpu().numpy().astype(np.float16)
         stack = lambda k: np.stack([self.decoders[i][k].cpu().numpy().astype(np.float16) for i in range(self.num_lods)])
@@ -195,6 +219,7 @@ class SparseSDF:
             m.w0[i], m.b0[i], m.w1[i], m.b1[i] = w0.data_ptr(), b0.data_ptr(), w1.data_ptr(), b1.data_ptr()
         for i, tile in enumerate(self.tiles):
             m.w0_tile[i] = tile.data_ptr()
+        m.summed = int(self.summed)
         return m
 
     def check_status(self):

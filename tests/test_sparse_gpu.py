@@ -195,3 +195,54 @@ def test_npz_round_trip(scene, tmp_path):
     a, _ = sp.render(ro.to(dev), rd.to(dev), lod=3)
     b, _ = sp2.render(ro.to(dev), rd.to(dev), lod=3)
     assert torch.equal(a[1], b[1]) and torch.equal(a[2], b[2])
+
+
+@pytest.mark.parametrize("lod", [0, 3])
+def test_summed_query_equals_dense_inside_voxels(scene, lod):
+    """LOD-summed corner features (float32): one voxel's corners per query
+    give the dense float32 SDF within rounding at points inside occupied
+    voxels, and NaN at the same points as the per-level form."""
+    net, s, (c, r) = scene
+    sp = SparseSDF.from_dense(net, s, precision="f32", half_weights=False, summed=True)
+    ref = SparseSDF.from_dense(net, s, precision="f32", half_weights=False)
+    assert sp.summed and not sp.chains
+    x = synthetic.near_surface_query(20000, c, r, seed=5).to(s.GetOctree().device)
+    got = sp.forward(x, lod)
+    with torch.no_grad():
+        want = net.sdf(x, lod=lod)
+    inside = ~torch.isnan(got[:, 0])
+    assert torch.equal(inside, ~torch.isnan(ref.forward(x, lod)[:, 0]))
+    assert inside.float().mean() > 0.3
+    assert (got[inside] - want[inside]).abs().max().item() < 1e-5
+    with pytest.raises(ValueError, match="npz"):
+        sp.save_npz("/dev/null")
+
+
+def test_summed_tc_trace_against_fp64_dense_oracle(scene):
+    """The tensor-core sparse trace over LOD-summed bf16 corner features: the
+    same bound against the FP64 dense oracle as the per-level trace, and the
+    per-level trace's hit mask on all but a few rays."""
+    from oracle import cref, dense
+    from tests.helpers import oracle_model
+    net, s, _ = scene
+    sp = SparseSDF.from_dense(net, s, precision="bf16", decoder="tc", half_weights=False, summed=True)
+    per_level = SparseSDF.from_dense(net, s, precision="bf16", decoder="tc", half_weights=False)
+    ro, rd = synthetic.look_at_rays(width=96, height=72)
+    dev = s.GetOctree().device
+    (x, t, hit, normal), _ = sp.render(ro.to(dev), rd.to(dev), lod=3, num_steps=64)
+    (_, t2, hit2, _), _ = per_level.render(ro.to(dev), rd.to(dev), lod=3, num_steps=64)
+    sp.check_status()
+    per_level.check_status()
+    m64 = oracle_model(net, np.float64)
+    xo, to, ho, no = dense.sphere_trace(m64, ro.numpy().astype(np.float64), rd.numpy().astype(np.float64),
+                                        num_steps=128, lod=3, aabb_fn=lambda o, d: tuple(
+                                            v.astype(np.float64) if v.dtype != bool else v
+                                            for v in cref.aabb(o.astype(np.float32), d.astype(np.float32))))
+    h = hit.cpu().numpy()
+    both = h & ho
+    assert both.sum() > 500 and (h == ho).mean() > 0.99
+    err = np.abs(t.cpu().numpy()[both, 0] - to[both, 0])
+    print(f"summed sparse tc trace depth vs fp64 dense: mean {err.mean():.2e} median {np.median(err):.2e} "
+          f"p99 {np.percentile(err, 99):.2e}")
+    assert np.median(err) < 1e-3
+    assert (hit == hit2).float().mean().item() > 0.995
