@@ -23,7 +23,8 @@ def _model(seed, dev):
 
 def test_mixed_requests_equal_alone(cuda):
     f32 = _model(2, cuda)
-    models = [Bf16OctreeSDF(f32), Bf16OctreeSDF(_model(3, cuda)), f32]
+    # a per-LOD BF16 model, a LOD-summed BF16 model and a float32 model
+    models = [Bf16OctreeSDF(f32), Bf16OctreeSDF(_model(3, cuda), summed=True), f32]
     ex = serve.CudaExecutor(models, cuda, num_streams=4)
     budget = serve.RenderRequest(0, 160, 120).nbytes() * 3
     srv = serve.Server(ex, budget)
