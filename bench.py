@@ -72,7 +72,7 @@ def parse():
     p.add_argument("--warmup", type=int, default=10)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--no-extras", action="store_true", help="skip the trace and CPU-baseline legs")
-    p.add_argument("--only", choices=["trace", "summed", "train", "sparse", "serve", "shade", "mesh"], default=None,
+    p.add_argument("--only", choices=["trace", "aabb", "summed", "train", "sparse", "serve", "shade", "mesh"], default=None,
                    help="run one extra leg alone (profiling); prints its JSON")
     return p.parse_args()
 
@@ -352,6 +352,37 @@ def bench_summed(net, bnet, x, dev, flush, stream, steps=100):
             "vs_per_lod_bf16_max_abs": float(d.max().item()), "vs_per_lod_bf16_mean_abs": float(d.mean().item()),
             "trace_ms": tms, "trace_rays_per_s": ro.shape[0] / (tms / 1e3),
             "trace_hit_agreement_vs_per_lod_bf16": float((rbs.hit == rb16.hit).float().mean().item())}
+
+
+def bench_aabb(dev, flush, stream, steps=50):
+    """sol_nglod.aabb (nglod_aabb) on the 1920x1080 camera rays of the trace
+    workload: 24 B in and 17 B out per ray, HBM-bound; L2 flushed between
+    steps."""
+    from nglod_gb300 import _lib, sol_nglod, synthetic
+    ro, rd = synthetic.look_at_rays(width=TRACE_W, height=TRACE_H)
+    ro, rd = ro.to(dev), rd.to(dev)
+    n = ro.shape[0]
+    x = torch.empty_like(ro)
+    t = torch.empty(n, 1, device=dev)
+    hit = torch.empty(n, dtype=torch.bool, device=dev)
+    lib = _lib.load()
+
+    def launch():  # the C entry on preallocated outputs: one kernel
+        _lib.check(lib.nglod_aabb(_lib.ptr(ro), _lib.ptr(rd), n, _lib.ptr(x), _lib.ptr(t), _lib.ptr(hit),
+                                  _lib.stream_ptr(dev)), "nglod_aabb")
+
+    for _ in range(3):
+        launch()
+        sol_nglod.aabb(ro, rd)
+    torch.cuda.synchronize()
+    ms = time_steps(launch, steps, flush, stream) / steps
+    ms_api = time_steps(lambda: sol_nglod.aabb(ro, rd), steps, flush, stream) / steps
+    nbytes = n * (24 + 12 + 4 + 1)
+    pk = peaks()
+    return {"workload": f"sol_nglod.aabb, {n} rays ({TRACE_W}x{TRACE_H} camera (0,0,4) fov 30)",
+            "ms": ms, "rays_per_s": n / (ms / 1e3), "bytes_per_ray": 41, "gbs": nbytes / (ms / 1e3) / 1e9,
+            "hbm_frac": nbytes / (ms / 1e3) / 1e9 / pk["hbm_gbs"], "hits": int(hit.sum().item()),
+            "ms_python_api": ms_api}
 
 
 def bench_trace(net, bnet, dev, flush, stream):
@@ -712,6 +743,8 @@ def run_only(args):
     stream = torch.cuda.current_stream(dev)
     if args.only == "trace":
         out = bench_trace(net, Bf16OctreeSDF(net), dev, flush, stream)
+    elif args.only == "aabb":
+        out = bench_aabb(dev, flush, stream)
     elif args.only == "summed":
         from nglod_gb300 import synthetic
         x = synthetic.near_surface_query(N_POINTS, *synthetic.sphere_union(1), seed=1).to(dev)
