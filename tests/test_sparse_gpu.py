@@ -246,3 +246,21 @@ def test_summed_tc_trace_against_fp64_dense_oracle(scene):
           f"p99 {np.percentile(err, 99):.2e}")
     assert np.median(err) < 1e-3
     assert (hit == hit2).float().mean().item() > 0.995
+
+
+def test_summed_f32_decoder_trace_matches_per_level(scene):
+    """The float32-decoder sparse trace over LOD-summed float32 corner
+    features against the per-level one: same hits on all but a few rays,
+    depths within 1e-4 where both hit."""
+    net, s, _ = scene
+    kw = dict(precision="f32", half_weights=False, decoder="f32")
+    sp = SparseSDF.from_dense(net, s, summed=True, **kw)
+    ref = SparseSDF.from_dense(net, s, **kw)
+    ro, rd = synthetic.look_at_rays(width=96, height=72)
+    dev = s.GetOctree().device
+    (_, t, hit, _), _ = sp.render(ro.to(dev), rd.to(dev), lod=3, num_steps=50)
+    (_, t2, hit2, _), _ = ref.render(ro.to(dev), rd.to(dev), lod=3, num_steps=50)
+    both = hit & hit2
+    assert both.sum().item() > 500
+    assert (hit == hit2).float().mean().item() > 0.999
+    assert np.percentile((t[both] - t2[both]).abs().cpu().numpy(), 99) < 1e-4
