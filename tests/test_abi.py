@@ -119,3 +119,25 @@ def test_bf16_and_training_validation_without_device(built_library):
     for i in range(2):
         g.grid[i] = g.w0[i] = g.b0[i] = g.w1[i] = g.b1[i] = 4096 * (i + 1)
     assert lib.nglod_sdf_bwd(m, fake, 10, 0b11, fake, fake, mis, fake, g, None, None) == -5
+
+
+def test_summed_volume_validation_without_device(built_library):
+    """Argument checks of nglod_build_summed_volume, before any CUDA call."""
+    from nglod_gb300 import _lib
+    lib = _lib.load()
+    m = _lib.DenseModel()
+    m.num_lods, m.base_lod, m.feature_dim, m.hidden_dim = 3, 2, 32, 128
+    for i in range(3):
+        m.grid[i] = 4096 * (i + 1)
+    out = ctypes.c_void_p(1 << 20)
+    assert lib.nglod_build_summed_volume(m, 3, _lib.F32, out, None) == -1  # lod beyond num_lods - 1
+    assert b"lod=3" in lib.nglod_last_error()
+    assert lib.nglod_build_summed_volume(m, 1, 7, out, None) == -1  # dtype
+    assert lib.nglod_build_summed_volume(m, 1, _lib.BF16, ctypes.c_void_p((1 << 20) + 8), None) == -5
+    assert lib.nglod_build_summed_volume(m, 0, _lib.BF16, None, None) == -1
+    m.grid[1] = None
+    assert lib.nglod_build_summed_volume(m, 2, _lib.F32, out, None) == -1
+    assert b"volume 1" in lib.nglod_last_error()
+    m.grid[1] = 8192
+    m.feature_dim = 16
+    assert lib.nglod_build_summed_volume(m, 1, _lib.F32, out, None) == -1
