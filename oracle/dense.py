@@ -76,6 +76,26 @@ def decoder(m, i, ex):
     return h @ m["w1"][i].T + m["b1"][i]
 
 
+def summed_volume(m, lod):
+    """LOD-summed volume ``lod`` [C, s, s, s] in the model's dtype: at every
+    vertex of LOD lod's grid, the running feature sum of ``sdf``
+    (OctreeSDF.py:109-110) there, i.e. the sum over LODs i <= lod of volume
+    i's trilinear sample.  Grid spacings halve from LOD to LOD, so each cell
+    of LOD lod lies inside one cell of every coarser grid, and a trilinear
+    function restricted to a sub-box is trilinear: ``feature_volume`` of this
+    volume gives the running sum at any point up to rounding (the border
+    clamp is the same for every LOD).  The restatement of
+    nglod_build_summed_volume, which computes it on the device in float64."""
+    s = m["fms"][lod].shape[-1]
+    t = np.linspace(-1.0, 1.0, s).astype(m["fms"][lod].dtype)
+    z, y, x = np.meshgrid(t, t, t, indexing="ij")
+    pts = np.stack([x.ravel(), y.ravel(), z.ravel()], axis=1)  # x -> W, y -> H, z -> D
+    acc = 0
+    for i in range(lod + 1):
+        acc = acc + feature_volume(m["fms"][i], pts)
+    return np.ascontiguousarray(acc.T.reshape(-1, s, s, s))
+
+
 def sdf(m, x, lod=None, return_lst=False):
     """``OctreeSDF.sdf(x, lod, return_lst)`` (OctreeSDF.py:94-155).
 

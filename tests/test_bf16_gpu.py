@@ -46,24 +46,11 @@ def emulate(m, x, lod, rounded=False):
     return (h @ m["w1"][lod].astype(np.float32).T + m["b1"][lod].astype(np.float32))
 
 
-def summed_volume64(m, lod):
-    """LOD-summed volume `lod` in float64, [C, s, s, s]: at every vertex of
-    LOD lod's grid, the sum of the trilinear samples of volumes 0..lod."""
-    s = m["fms"][lod].shape[-1]
-    t = np.linspace(-1.0, 1.0, s)
-    z, y, x = np.meshgrid(t, t, t, indexing="ij")
-    pts = np.stack([x.ravel(), y.ravel(), z.ravel()], axis=1)  # x -> W, y -> H, z -> D
-    acc = np.zeros((pts.shape[0], m["fms"][lod].shape[0]))
-    for i in range(lod + 1):
-        acc += dense.feature_volume(m["fms"][i].astype(np.float64), pts)
-    return acc.T.reshape(-1, s, s, s)
-
-
 def emulate_summed(m, x, lod):
     """emulate() for Bf16OctreeSDF(summed=True): volume lod = the LOD-summed
     volume rounded once to bf16, sampled alone."""
     x = x.astype(np.float32)
-    sv = _bf16(summed_volume64(m, lod).astype(np.float32))
+    sv = _bf16(dense.summed_volume(m, lod).astype(np.float32))
     one = {"fms": [sv], "w0": [m["w0"][lod]], "b0": [m["b0"][lod]], "w1": [m["w1"][lod]], "b1": [m["b1"][lod]]}
     return emulate(one, x, 0, rounded=True)
 
@@ -246,10 +233,10 @@ def test_summed_volumes_are_the_float64_sums_rounded_once(nets, summed):
     """nglod_bf16_build_summed: every value is the float64 LOD sum at that
     vertex rounded to the nearest bf16 (within half a bf16 ulp, ties either
     way); the pair volumes are built from the summed volumes."""
-    _, _, m32, _, _ = nets
+    _, _, _, m64, _ = nets
     assert summed.summed and len(summed.pairs) == summed.num_lods
     for lod in range(summed.num_lods):
-        want = summed_volume64(m32, lod)
+        want = dense.summed_volume(m64, lod)
         got = summed.grids[lod][0].float().cpu().numpy().astype(np.float64)
         assert got.shape == want.shape
         ulp = 2.0 ** (np.floor(np.log2(np.maximum(np.abs(want), 1e-30))) - 7)
@@ -270,7 +257,7 @@ def test_summed_form_matches_emulation_and_fp64(nets, summed, n):
     report = {}
     for lod in range(summed.num_lods):
         got = summed.sdf(x.to(dev), lod=lod).cpu().numpy()
-        np.testing.assert_allclose(got, emulate_summed(m32, x.numpy(), lod), atol=2e-4, rtol=0)
+        np.testing.assert_allclose(got, emulate_summed(m64, x.numpy(), lod), atol=2e-4, rtol=0)
         err = np.abs(got - dense.sdf(m64, x.numpy().astype(np.float64), lod=lod))
         report[lod] = (err.max(), err.mean())
         assert err.max() < 2e-2 and err.mean() < 2e-3, (lod, err.max(), err.mean())
