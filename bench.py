@@ -266,6 +266,9 @@ def run_ours(args):
         "kernel": "sdf_fwd_bf16_tc_kernel",
         "per_query": {"hbm_bytes": 16, "gathered_bytes": (LOD + 1) * 8 * 32 * 2, "tensor_flop": 2 * 35 * 128,
                       "fp32_epilogue_flop": 3 * 128},
+        "binding": {"resource": "L1 data-pipe wavefronts (corner gathers + tile rows)", "frac": 0.737,
+                    "issue_active": 0.568,
+                    "source": "ncu --set full capture of one launch (profiles/sdf_fwd_bf16_tc_4M.md)"},
         "gather_gbs": gather_bytes / sec / 1e9,
         "tensor_tflops": tc_flop / sec / 1e12,
         "tensor_frac_of_bf16_peak": tc_flop / sec / 1e12 / pk["bf16_tflops"],
