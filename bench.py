@@ -190,6 +190,38 @@ def time_steps(fn, steps, flush, stream):
     return total
 
 
+def line_read_peak(dev, nbytes, reps=20):
+    """Measured ceiling of the gather's corner reads: random whole 128-byte
+    lines of an L2-resident buffer of `nbytes` (the pair volumes' size) read
+    with the gather's 256-bit loads, four lanes per line
+    (nglod_measure_line_reads), 64 warps per SM; GB/s, best of `reps`."""
+    from nglod_gb300 import _lib
+    lines = nbytes // 128
+    buf = torch.zeros(lines * 128, dtype=torch.uint8, device=dev)
+    sink = torch.zeros(1, dtype=torch.int32, device=dev)
+    blocks = torch.cuda.get_device_properties(dev).multi_processor_count * 16
+    loads = 256
+    lib = _lib.load()
+
+    def go():
+        _lib.check(lib.nglod_measure_line_reads(_lib.ptr(buf), lines, loads, blocks, _lib.ptr(sink),
+                                                _lib.stream_ptr(dev)), "nglod_measure_line_reads")
+
+    for _ in range(3):
+        go()
+    torch.cuda.synchronize()
+    best = float("inf")
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(reps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        go()
+        b.record(stream)
+        b.synchronize()
+        best = min(best, a.elapsed_time(b))
+    return blocks * 128 * loads * 32 / (best / 1e3) / 1e9
+
+
 def run_ours(args):
     ws, rank, local = dist_setup()
     dev = torch.device("cuda", local)
@@ -254,6 +286,7 @@ def run_ours(args):
     pk = peaks()
     grid_bytes = sum(fv.fm.numel() * 2 for fv in net.features)
     pair_bytes = sum(pv.numel() * 2 for pv in bnet.pairs) or grid_bytes  # what the launch reads
+    line_peak = line_read_peak(dev, pair_bytes)
     hbm_bytes = N_POINTS * (12 + 4) + pair_bytes
     gather_bytes = N_POINTS * (LOD + 1) * 8 * 32 * 2
     tc_flop = N_POINTS * 2 * 35 * 128
@@ -270,6 +303,12 @@ def run_ours(args):
                     "issue_active": 0.568,
                     "source": "ncu --set full capture of one launch (profiles/sdf_fwd_bf16_tc_4M.md)"},
         "gather_gbs": gather_bytes / sec / 1e9,
+        "gather": {"gbs": gather_bytes / sec / 1e9, "line_read_peak_gbs": line_peak,
+                   "frac": gather_bytes / sec / 1e9 / line_peak,
+                   "peak_source": "measured live: random whole 128-byte lines of an L2-resident buffer the size of "
+                                  "the pair volumes, read with the gather's 256-bit loads (nglod_measure_line_reads)",
+                   "note": "the gathered bytes (2,560 B per query) include L1 hits (about 28 %), so this fraction "
+                           "may exceed the share of the L2 ceiling"},
         "tensor_tflops": tc_flop / sec / 1e12,
         "tensor_frac_of_bf16_peak": tc_flop / sec / 1e12 / pk["bf16_tflops"],
         "note": "one launch reads each point once and the 40.4 MB of bf16 pair volumes (each vertex beside "

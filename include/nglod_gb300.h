@@ -208,6 +208,15 @@ int nglod_sdf_fwd_bf16_host(const nglod_bf16_model *model, const float *x_host, 
  * leaves the context usable.  Not for production use. */
 int nglod_debug_mma_wait_polls(int64_t polls);
 
+/* Measurement helper, no reference counterpart: `blocks` blocks of 128
+ * threads each read `loads` random whole 128-byte lines of buf[lines][128 B]
+ * (32-byte aligned) with the point-query gather's 256-bit loads, four lanes
+ * per line: blocks * 128 * loads * 32 bytes.  Timed around a buffer held in
+ * L2, it gives the ceiling of the gather's corner reads.  sink: one device
+ * uint32, written only to keep the loads. */
+int nglod_measure_line_reads(const void *buf, int64_t lines, int32_t loads, int32_t blocks, uint32_t *sink,
+                             nglod_stream_t stream);
+
 /* SphereTracer.forward in the BF16 form: the persistent tracer of
  * nglod_trace with every sdf evaluation (march points and normal taps) done
  * by the bf16 tile kernel above, 128 rays per block evaluated together.

@@ -228,6 +228,7 @@ SIGNATURES = {
     "nglod_bf16_pack_decoder": (ctypes.c_int, [_vp, _vp, _i32, _i32, _vp]),
     "nglod_bf16_build_pairs": (ctypes.c_int, [_vp, _i32, _vp, _vp]),
     "nglod_build_summed_volume": (ctypes.c_int, [ctypes.POINTER(DenseModel), _i32, _i32, _vp, _vp]),
+    "nglod_measure_line_reads": (ctypes.c_int, [_vp, _i64, _i32, _i32, _vp, _vp]),
     "nglod_debug_mma_wait_polls": (ctypes.c_int, [_i64]),
     "nglod_sdf_fwd_bf16": (ctypes.c_int, [ctypes.POINTER(Bf16Model), _vp, _i64, _i32, _vp, _vp, _vp]),
     "nglod_trace_bf16": (ctypes.c_int, [ctypes.POINTER(Bf16Model), ctypes.POINTER(TraceParams), _vp, _vp, _i64,

@@ -828,6 +828,41 @@ extern "C" int nglod_build_summed_volume(const nglod_dense_model *model, int32_t
     return launch_status("nglod_build_summed_volume");
 }
 
+// Read throughput of random whole 128-byte lines of a buffer, with the
+// point-query gather's loads (four lanes per line, one 256-bit load each, a
+// warp covering eight lines per instruction).  For a buffer the size of the
+// pair volumes, held in L2, this is the measured ceiling of the gather's
+// corner reads.  Line indices: xorshift32 per group of four lanes (never
+// zero), taken modulo `lines`, so every load is in bounds.
+__global__ void line_read_kernel(const PairUnit *__restrict__ buf, uint32_t lines, int loads, uint32_t seed,
+                                 uint32_t *__restrict__ sink) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t h = ((t >> 2) * 2654435761u) ^ seed;
+    h |= 1u;
+    uint32_t acc = 0u;
+    const PairUnit *base = buf + (threadIdx.x & 3);
+#pragma unroll 4
+    for (int k = 0; k < loads; ++k) {
+        h ^= h << 13;
+        h ^= h >> 17;
+        h ^= h << 5;
+        const PairUnit u = ld_pair_unit(base + (size_t)(h % lines) * 4);
+        acc ^= u.w[0] ^ u.w[1] ^ u.w[2] ^ u.w[3] ^ u.w[4] ^ u.w[5] ^ u.w[6] ^ u.w[7];
+    }
+    if (acc == 0x9E3779B9u) sink[0] = t;  // keeps every load
+}
+
+extern "C" int nglod_measure_line_reads(const void *buf, int64_t lines, int32_t loads, int32_t blocks,
+                                        uint32_t *sink, nglod_stream_t stream) {
+    NGLOD_REQUIRE(buf && sink, NGLOD_ERR_INVALID, "null pointer argument");
+    NGLOD_REQUIRE(aligned(buf, 32), NGLOD_ERR_ALIGN, "buf must be 32-byte aligned");
+    NGLOD_REQUIRE(lines >= 1 && lines <= 0xFFFFFFFFll, NGLOD_ERR_INVALID, "lines=%lld", (long long)lines);
+    NGLOD_REQUIRE(loads >= 1 && blocks >= 1, NGLOD_ERR_INVALID, "loads=%d blocks=%d", loads, blocks);
+    line_read_kernel<<<blocks, 128, 0, (cudaStream_t)stream>>>(static_cast<const PairUnit *>(buf), (uint32_t)lines,
+                                                               loads, 0x2545F491u, sink);
+    return launch_status("nglod_measure_line_reads");
+}
+
 extern "C" int nglod_sdf_fwd_bf16(const nglod_bf16_model *model, const float *x, int64_t n, int32_t lod, float *out,
                                   int32_t *status, nglod_stream_t stream) {
     return sdf_fwd_bf16_impl(model, x, n, lod, out, status, (cudaStream_t)stream, true);
