@@ -141,3 +141,15 @@ def test_summed_volume_validation_without_device(built_library):
     m.grid[1] = 8192
     m.feature_dim = 16
     assert lib.nglod_build_summed_volume(m, 1, _lib.F32, out, None) == -1
+
+
+def test_line_read_probe_validation_without_device(built_library):
+    """Argument checks of nglod_measure_line_reads, before any CUDA call."""
+    from nglod_gb300 import _lib
+    lib = _lib.load()
+    buf, sink = ctypes.c_void_p(1 << 20), ctypes.c_void_p(1 << 21)
+    assert lib.nglod_measure_line_reads(None, 10, 4, 1, sink, None) == -1
+    assert lib.nglod_measure_line_reads(ctypes.c_void_p((1 << 20) + 16), 10, 4, 1, sink, None) == -5
+    assert lib.nglod_measure_line_reads(buf, 0, 4, 1, sink, None) == -1
+    assert lib.nglod_measure_line_reads(buf, 1 << 33, 4, 1, sink, None) == -1
+    assert lib.nglod_measure_line_reads(buf, 10, 0, 1, sink, None) == -1
