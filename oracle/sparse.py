@@ -59,8 +59,12 @@ def build(fms, pts, pyr, num_lods, corner_dtype=np.float32):
             "trink": trink, "parent": parent, "pts": pts, "pyr": pyr}
 
 
-def features(m, lod, g, x):
-    """sparse_grid_sample_kernel: [n, C] feature sums starting in voxels g (global)."""
+def features(m, lod, g, x, summed=False):
+    """sparse_grid_sample_kernel: [n, C] feature sums starting in voxels g (global).
+
+    summed: m's corner features come from LOD-summed volumes
+    (dense.summed_volume), and the sum stops after the query level (the
+    summed form of nglod_sparse_model)."""
     n = x.shape[0]
     C = m["cf"].shape[1]
     out = np.zeros((n, C), f32)
@@ -69,7 +73,8 @@ def features(m, lod, g, x):
     nz = _fma(x[:, 2], 0.5, 0.5)
     g = g.copy()
     cc = m["cc"].astype(f32)
-    for lv in range(lod + 2, 1, -1):
+    last = lod + 2 if summed else 2
+    for lv in range(lod + 2, last - 1, -1):
         if lv != lod + 2:
             g = m["parent"][g]
         res = f32(2 ** lv)
