@@ -279,10 +279,10 @@ int nglod_sdf_bwd(const nglod_dense_model *model, const float *x, int64_t n, uin
                   const float *grad_preds, const float *feats, const uint32_t *relu_masks, float *dfeat_scratch,
                   const nglod_dense_grads *grads, float *grad_x, nglod_stream_t stream);
 
-/* Reads and clears the backward's device status on the current device
+/* Reads and clears the training device status on the current device
  * (synchronous): *status_out = 1 if a bounded tensor-core wait of a
- * nglod_sdf_bwd / nglod_sdf_bwd_noalloc call since the last read gave up
- * (its gradients are incomplete), else 0. */
+ * nglod_sdf_fwd_train, nglod_sdf_bwd or nglod_sdf_bwd_noalloc call since
+ * the last read gave up (its outputs are incomplete), else 0. */
 int nglod_train_status(int32_t *status_out);
 
 /* nglod_sdf_bwd for callers that cannot allocate device memory (a plugin

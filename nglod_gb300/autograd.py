@@ -123,10 +123,11 @@ def sdf_train(net, x, lod, all_lods):
 
 
 def check_backward_status():
-    """Raises if a bounded tensor-core wait of a backward since the last
-    check gave up (its gradients would be incomplete).  Synchronises the
-    device (nglod_train_status)."""
+    """Raises if a bounded tensor-core wait of the training forward or
+    backward since the last check gave up (its predictions or gradients
+    would be incomplete).  Synchronises the device (nglod_train_status)."""
     v = ctypes.c_int32(0)
     _lib.check(_lib.load().nglod_train_status(ctypes.byref(v)), "nglod_train_status")
     if v.value:
-        raise RuntimeError("nglod_sdf_bwd: a bounded tensor-core wait timed out; gradients are incomplete")
+        raise RuntimeError("nglod_sdf_fwd_train / nglod_sdf_bwd: a bounded tensor-core wait timed out; "
+                           "results are incomplete")
