@@ -754,8 +754,9 @@ def run_reference(args):
     net, (c, r) = build_model(None)
     ref = torch_port.RefOctreeSDF({k: v.cpu() for k, v in net.state_dict().items()}, 5)
     x = synthetic.near_surface_query(CPU_SAMPLE, c, r, seed=1)
+    warm = max(1, min(args.warmup, 2))  # bounded: each step is a 262k-point CPU sample
     with torch.no_grad():
-        for _ in range(max(1, min(args.warmup, 2))):
+        for _ in range(warm):
             ref.sdf(x, lod=LOD)
         steps = max(1, min(args.steps, 5))
         t0 = time.perf_counter()
@@ -765,7 +766,7 @@ def run_reference(args):
     value = CPU_SAMPLE * steps / dt
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0, "steps": steps,
-        "warmup": args.warmup, "ms_per_step": dt / steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "warmup": warm, "requested": {"steps": args.steps, "warmup": args.warmup}, "ms_per_step": dt / steps * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": WORKLOAD, "points": N_POINTS, "lod": LOD,
                    "sample_points_per_step": CPU_SAMPLE, "parallelism": "host cores"},
