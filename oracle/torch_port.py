@@ -1,6 +1,6 @@
 """Restatement of the reference's CPU torch path, used as the timed CPU baseline
-(``bench.py --impl reference`` and the ``cpu_baseline`` leg).  TEST/BASELINE
-INFRASTRUCTURE ONLY.
+(``bench.py --impl reference`` and the ``cpu_baseline`` leg).  Test and
+CPU-baseline infrastructure only.
 
 The reference itself cannot be imported where the benchmark runs, so this
 module re-expresses its computation with the same torch operators it calls:
