@@ -375,7 +375,8 @@ def poisson_workload(duration_s, rate_hz, num_models, seed=0, sizes=((256, 256),
 
     Arrivals are a Poisson process; half the requests (by default) are renders
     of a uniformly chosen size at a uniformly chosen LOD, the rest point
-    queries of log-uniform size.  Points are generated lazily by the driver.
+    queries of log-uniform size.  run_workload makes the points when it
+    submits each query.
     """
     rng = np.random.default_rng(seed)
     t = 0.0
