@@ -10,7 +10,6 @@ are torch code on the mesh's device, as the reference's are.  ``load_obj``
 parses Wavefront .obj text itself (vertices, faces triangulated as fans;
 materials are not read), the reference's tinyobjloader being absent.
 """
-import ctypes
 import os
 
 import numpy as np

@@ -25,7 +25,6 @@ tracer constructor that has no such argument.)
 import ctypes
 import math
 
-import numpy as np
 import torch
 
 from . import _lib

@@ -9,7 +9,6 @@ from nglod_gb300 import spc, synthetic
 from nglod_gb300.analytic_init import init_from_sdf
 from nglod_gb300.options import default_args
 from nglod_gb300.sparse_sdf import SparseSDF
-from oracle import dense as odense
 from oracle import sparse as osparse
 from oracle import spc as ospc
 
