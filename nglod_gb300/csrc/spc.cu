@@ -47,11 +47,14 @@ __constant__ uint32_t c_child_order[8] = {order_word(0), order_word(1), order_wo
 // The ray is mapped to [0,1]^3 (o' = o/2 + 1/2, d' = d/2); the voxel (i, j)
 // square of each coordinate plane is tested against the line's 2-D edge
 // function a*i + b*j + c at its four corners.  Arithmetic order: the
-// reference source compiled with nvcc's default contraction, i.e.
-// c0 = fma(a, i, b*j) + c, c1 = c0 + a, c2 = c0 + b, c3 = c1 + b, and
-// o' x d' with each component fma(u, v, -(w*z)).
+// reference source as nvcc contracts it, i.e. c0 = fma(b, j, a*i) + c,
+// c1 = c0 + a, c2 = c0 + b, c3 = c1 + b, and o' x d' with each component
+// fma(u, v, -(w*z)).  This form was pinned against the reference kernel
+// itself: of the nine legal contractions of the two expressions, only this
+// one reproduces all of its decisions on 135M ray/voxel candidates (a
+// 1920x1080 frame through a level-7 octree).
 __device__ __forceinline__ bool face_straddles(float fi, float fj, float a, float b, float c) {
-    const float r0 = __fadd_rn(__fmaf_rn(a, fi, __fmul_rn(b, fj)), c);
+    const float r0 = __fadd_rn(__fmaf_rn(b, fj, __fmul_rn(a, fi)), c);
     const float r1 = __fadd_rn(r0, a);
     const float r2 = __fadd_rn(r0, b);
     const float r3 = __fadd_rn(r1, b);

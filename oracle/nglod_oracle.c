@@ -79,10 +79,13 @@ void oracle_child_order_table(uint8_t *out64) {
         for (int r = 0; r < 8; ++r) out64[8 * c + r] = (uint8_t)child_order(c, r);
 }
 
-/* d_FaceEval (85-105) with nvcc's default contraction of a*i + b*j + c:
- * fma(a, i, b*j) + c; then +a, +b, +b. */
+/* d_FaceEval (85-105) as nvcc contracts a*i + b*j + c in the reference build:
+ * fma(b, j, a*i) + c; then +a, +b, +b.  The contraction was pinned on the GPU
+ * against the reference kernel's own decisions (135M ray/voxel candidates of a
+ * 1920x1080 frame, octree levels 0-7): of the nine legal forms of crs3 and of
+ * this sum, only fma(u, v, -(w*z)) with fma(b, j, a*i) + c agrees with all. */
 static int face_straddles(float fi, float fj, float a, float b, float c) {
-    const float r0 = fmaf(a, fi, b * fj) + c;
+    const float r0 = fmaf(b, fj, a * fi) + c;
     const float r1 = r0 + a;
     const float r2 = r0 + b;
     const float r3 = r1 + b;

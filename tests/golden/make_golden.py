@@ -25,6 +25,17 @@ Fixtures:
   mesh_small.npz   torchgp.normalize, per_face_normals and point_sample
                    (['trace', 'near', 'rand'], torch seed 3) on a procedural
                    icosphere.
+  sol_export_small.npz  SOL_NGLOD(net).save() (sdf-net/lib/models/SOL_NGLOD.py:31-100)
+                   on trace_small's construction at num_lods=3, base_lod=2: the
+                   reference's own sparse export (octree, cc, cf, w0, b0, w1,
+                   b1, pyramid), which sol-renderer's SDF::loadWeights reads.
+                   As shipped, SOL_NGLOD's voxel_sparsify -> sample_surface
+                   builds SphereTracer(device, sol=sol) (renderutils.py:33),
+                   which raises TypeError (BaseTracer has no ``sol``
+                   argument); the generator gives renderutils a factory that
+                   builds the reference SphereTracer from parsed options
+                   instead, and runs sample_surface on the CPU.  Everything
+                   else in the export runs unchanged.
   shade_small.npz  Renderer.shade_tensor with a ground plane, shadow rays and
                    ambient occlusion on trace_small's network, 48x40 rays,
                    matcap shading with nglod_gb300.synthetic.matcap_texture
@@ -230,6 +241,32 @@ def mesh_small():
     np.savez_compressed(os.path.join(HERE, "mesh_small.npz"), **out)
 
 
+def sol_export_small(OctreeSDF, SphereTracer, parse_options):
+    """SOL_NGLOD(net).save() of a 3-LOD network (base_lod 2) holding the
+    sphere-union SDF, run on the CPU."""
+    import lib.renderutils as RU
+    from lib.models.SOL_NGLOD import SOL_NGLOD
+    targs = ref_args(parse_options, num_lods=3, base_lod=2, num_steps=64, min_dis=0.0003, step_size=1.0,
+                     camera_clamp=[-5, 10], grad_method="finitediff")
+    RU.SphereTracer = lambda device, sol=False: SphereTracer(targs)
+    RU.sample_surface.__defaults__ = (False, "cpu")
+    RU.voxel_sparsify.__defaults__ = (False, "cpu")
+    c, r = synthetic.sphere_union(1)
+    torch.manual_seed(0)
+    dropin = DropIn(default_args(num_lods=3, base_lod=2))
+    init_from_sdf(dropin, lambda p: torch.from_numpy(synthetic.sphere_union_sdf(p.numpy(), c, r)), noise=2e-3,
+                  seed=6)
+    with torch.no_grad():
+        for fv in dropin.features:
+            fv.fm[:, 4:] = 0  # keep the fixture small: noise in channels 1-3 only
+    net = OctreeSDF(targs)
+    net.load_state_dict(dropin.state_dict())
+    net.eval()
+    torch.manual_seed(13)  # sample_surface's random rays
+    sol = SOL_NGLOD(net)
+    sol.save(os.path.join(HERE, "sol_export_small.npz"))
+
+
 def coded_volume(s, channels=2):
     c = torch.arange(channels, dtype=torch.float64).view(channels, 1, 1, 1)
     z = torch.arange(s, dtype=torch.float64).view(1, s, 1, 1)
@@ -298,6 +335,7 @@ def main():
     spc_small(spc3d, geoutils, ref_root)
     shade_small(OctreeSDF, SphereTracer, parse_options)
     mesh_small()
+    sol_export_small(OctreeSDF, SphereTracer, parse_options)
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))
