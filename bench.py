@@ -4,44 +4,54 @@
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 Headline workload (``config.workload``): ``OctreeSDF.sdf(x, lod=4)`` of the
-full architecture (5 LODs, 5^3..65^3 volumes, C=32, H=128) on 4,194,304 query
-points, half uniform in [-1,1]^3 and half within 0.02 of the 16-sphere-union
-surface (seed 1), in the BF16 form (bf16 volumes, tcgen05 decoder with fp32
-accumulation) -- the mixed-precision inference configuration.  One step =
-one pass over the batch.  ``value`` is queries/s with the points already
-resident in HBM; ``e2e`` is the same metric through the public API with
-host buffers (``Bf16OctreeSDF.sdf_host`` -> ``nglod_sdf_fwd_bf16_host``): the
-points are copied from pinned host memory and the distances copied back inside
-the timed region, in 256k-point chunks whose copies overlap the kernels.
-``fp32`` repeats the measurement for the float32 drop-in (``OctreeSDF.sdf``),
-which matches the reference to 1e-5.
+float32 drop-in -- the reference's arithmetic and its per-LOD gather, sum and
+decoder -- for the full architecture (5 LODs, 5^3..65^3 volumes, C=32,
+H=128) on 4,194,304 query points, half uniform in [-1,1]^3 and half within
+0.02 of the 16-sphere-union surface (seed 1).  One step = one pass over the
+batch.  ``value`` is queries/s with the points already resident in HBM;
+``e2e`` is the same metric through the public API with host buffers
+(``OctreeSDF.sdf_host`` -> ``nglod_sdf_fwd_host``): the points are copied
+from pinned host memory and the distances copied back inside the timed
+region, in 256k-point chunks whose copies overlap the kernels.  The
+``roofline`` object names the binding one of three live-measured terms of
+``sdf_fwd_f32_kernel``: the corner gathers against a measured line-read
+ceiling, the HBM bytes against the measured copy bandwidth, and the float32
+FLOPs against a measured FMA rate.
 
 The model holds the sphere-union SDF through ``analytic_init`` (deterministic
 and traced with real hits; throughput does not depend on the weights).
 Between timed steps an L2 flush (a 256 MiB write, larger than the 129 MB L2)
 runs outside the timed events.
 
-Extra keys: ``trace`` (sphere tracers at 1920x1080, 64 steps: fused BF16,
-fused float32 and the plain per-step float32 tracer), ``serve`` (the
-continuous-batching server under a Poisson request stream), ``train`` (the
-training step against the reference computation in stock PyTorch ops, then
-2,000 steps and the BF16 form on the trained weights), ``sparse`` (SPC octree
-traversal + sparse BF16 trace of a 1080p frame), ``shade`` (a shaded 1080p
-frame: trace, ground plane, shadow rays, ambient occlusion, matcap),
-``mesh`` (mesh signed distance of 1M points against 20,480 triangles),
-``roofline``,
-``cpu_baseline``, ``clocks``, ``gpu_launches``.  ``--only LEG`` runs one
-extra leg alone (for profiling).
+Extra keys:
+  bf16    the mixed-precision form (bf16 volumes, tcgen05 decoder) on the same
+          4M points, on the weights of 2,000 training steps from seed 1, with
+          each LOD's error against float64 on a 262,144-point sample
+  trace   sphere tracers at 1920x1080, 64 steps: fused BF16, fused float32,
+          the plain per-step float32 tracer and the reference's tracer in
+          stock torch ops, all on the GPU
+  train   the training step against the reference computation in stock
+          PyTorch ops on the same GPU, then the 2,000-step training run
+  serve   the continuous-batching server: 8 models trained on seeds 2..9,
+          a Poisson stream at 200 req/s, and a request-rate sweep to saturation
+  sparse  SPC octree traversal + sparse BF16 trace of a 1080p frame
+  shade   a shaded 1080p frame (trace, ground plane, shadow rays, AO, matcap)
+  summed  the BF16 form over LOD-summed volumes
+  mesh    mesh signed distance of 1M points against 20,480 triangles
+plus ``cpu_baseline``, ``clocks`` and ``gpu_launches``.  ``--only LEG`` runs
+one extra leg alone (for profiling).
 
-``--impl reference`` times the reference's own CPU torch computation (the
-restatement in oracle/torch_port.py, same torch operators) on the host cores
-on a bounded sample of the same workload and prints the same metric.
+``--impl reference`` times the reference's own CPU computation (the
+restatement in oracle/torch_port.py, the same torch operators) on the host
+cores, on the same 4,194,304 points, for the requested steps (within a
+time budget), and prints the same metric.
 
 Several GPUs (torchrun): the path shards only as independent replicas; each
 rank runs the full workload on its own GPU (weak scaling, no collective on
 the data path); rank 0 prints the aggregate.
 """
 import argparse
+import hashlib
 import json
 import os
 import statistics
@@ -60,9 +70,29 @@ LOD = 4
 TRACE_W, TRACE_H, TRACE_STEPS = 1920, 1080, 64
 METRIC = "sdf_queries_per_s"
 UNIT = "queries/s"
-WORKLOAD = "OctreeSDF.sdf(x, lod=4): 5 LODs (5^3..65^3 volumes), C=32, H=128, 4,194,304 points"
+WORKLOAD = ("OctreeSDF.sdf(x, lod=4), float32 drop-in: 5 LODs (5^3..65^3 volumes), C=32, H=128, "
+            "4,194,304 points")
 CPU_SAMPLE = 262_144
+ERR_SAMPLE_STRIDE = 16  # every 16th of the 4M points: 262,144 points, both halves of the distribution
 FLUSH_BYTES = 256 << 20
+REF_TIME_BUDGET_S = 300.0
+TRAIN_STEPS = 2000
+TRAIN_BATCH = 524_288
+
+# Per-query work of OctreeSDF.sdf at lod L (5 LODs at L = 4), float32:
+# HBM: 12 B point in + 4 B distance out (volumes once per launch);
+# gathered corner bytes: 8 corners x 32 channels x 4 B per LOD;
+# FLOP: 2 per corner-channel of the trilinear sums, 2*(35*128 + 128) for the
+# hidden layer with its bias, 2*128 for the output layer.
+F32_GATHER_BYTES = (LOD + 1) * 8 * 32 * 4
+F32_FLOP = (LOD + 1) * 8 * 32 * 2 + 2 * (35 * 128 + 128) + 2 * 128
+
+# DRAM traffic of single ncu captures of the headline kernels on this
+# workload (dram__bytes_read.sum + dram__bytes_write.sum of one launch), with
+# the SHA-256 of the kernel sources they were captured from.  A figure is
+# reported only while those sources are unchanged; otherwise the roofline's
+# traffic is null.
+NCU_CAPTURES = {}
 
 
 def parse():
@@ -71,27 +101,58 @@ def parse():
     p.add_argument("--steps", type=int, default=500)
     p.add_argument("--warmup", type=int, default=10)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    p.add_argument("--no-extras", action="store_true", help="skip the trace and CPU-baseline legs")
-    p.add_argument("--only", choices=["trace", "aabb", "summed", "train", "sparse", "serve", "shade", "mesh"], default=None,
-                   help="run one extra leg alone (profiling); prints its JSON")
+    p.add_argument("--no-extras", action="store_true", help="skip the extra legs and the CPU baseline")
+    p.add_argument("--only", choices=["trace", "aabb", "summed", "train", "sparse", "serve", "shade", "mesh", "bf16"],
+                   default=None, help="run one extra leg alone (profiling); prints its JSON")
     return p.parse_args()
 
 
-# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of
-# sdf_fwd_bf16_tc_kernel on this workload, from the ncu capture summarised in
-# profiles/sdf_fwd_bf16_tc_4M.md (the algorithmic bytes of a launch are
-# 67.1 MB of points and results plus 40.4 MB of bf16 pair volumes; the
-# results still in L2 when the kernel ends are written back later).
-NCU_TRAFFIC_BYTES = 90_623_232 + 10_336_512
-NCU_TRAFFIC_SOURCE = "ncu --set full capture of one launch, 4,194,304 points (profiles/sdf_fwd_bf16_tc_4M.md)"
+def sources_sha(paths):
+    h = hashlib.sha256()
+    for rel in paths:
+        with open(os.path.join(ROOT, rel), "rb") as f:
+            h.update(f.read())
+    return h.hexdigest()
+
+
+def ncu_traffic(kernel, points):
+    """(bytes per launch scaled to `points`, note) from NCU_CAPTURES, or (None, reason)."""
+    rec = NCU_CAPTURES.get(kernel)
+    if rec is None:
+        return None, "no ncu capture recorded for this kernel"
+    if sources_sha(rec["sources"]) != rec["sha256"]:
+        return None, "the kernel sources changed since the ncu capture"
+    return rec["dram_bytes"] * points / rec["points"], rec["how"]
 
 
 def peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
         d = json.load(open(path))
-        return {"hbm_gbs": d["hbm_gbs"], "bf16_tflops": d["bf16_tflops"], "source": "measured"}
-    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "source": "fallback"}
+        return {"hbm_gbs": d["hbm_gbs"], "bf16_tflops": d["bf16_tflops"],
+                "bf16_tflops_sustained": d.get("bf16_tflops_sustained", d["bf16_tflops"]), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0, "source": "fallback"}
+
+
+def roofline(kernel, sec, terms, per_unit, units, traffic=None, traffic_note=None, note=None):
+    """Roofline object of one kernel: `terms` maps a resource name to
+    (algorithmic amount per launch, peak, unit, peak source), each divided by
+    the launch time `sec`; the binding term is the one with the largest
+    fraction of its peak, and the top-level fields are that term's."""
+    tt = {}
+    for name, (amount, peak, unit, src) in terms.items():
+        scale = 1e9 if unit == "GB/s" else 1e12
+        a = amount / sec / scale
+        tt[name] = {"achieved": a, "peak": peak, "unit": unit, "frac": a / peak, "peak_source": src}
+    bind = max(tt, key=lambda k: tt[k]["frac"])
+    out = {"bound": bind, "achieved": tt[bind]["achieved"], "peak": tt[bind]["peak"], "unit": tt[bind]["unit"],
+           "frac": tt[bind]["frac"], "traffic": traffic, "kernel": kernel, "launch_ms": sec * 1e3,
+           "terms": tt, "per_unit": per_unit, "units_per_launch": units}
+    if traffic_note:
+        out["traffic_source"] = traffic_note
+    if note:
+        out["note"] = note
+    return out
 
 
 def dist_setup():
@@ -222,6 +283,57 @@ def line_read_peak(dev, nbytes, reps=20):
     return blocks * 128 * loads * 32 / (best / 1e3) / 1e9
 
 
+def fma_peak(dev, reps=10):
+    """Measured float32 FMA throughput of this device, TFLOP/s (nglod_measure_fma,
+    eight blocks of 256 threads per SM; best of `reps`)."""
+    from nglod_gb300 import _lib
+    sink = torch.zeros(1, device=dev)
+    blocks = torch.cuda.get_device_properties(dev).multi_processor_count * 8
+    iters = 4096
+    lib = _lib.load()
+
+    def go():
+        _lib.check(lib.nglod_measure_fma(iters, blocks, _lib.ptr(sink), _lib.stream_ptr(dev)), "nglod_measure_fma")
+
+    for _ in range(3):
+        go()
+    torch.cuda.synchronize()
+    best = float("inf")
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(reps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        go()
+        b.record(stream)
+        b.synchronize()
+        best = min(best, a.elapsed_time(b))
+    return blocks * 256 * 16 * iters / (best / 1e3) / 1e12
+
+
+def f32_roofline(net, sec, points, dev, line_peak=None, fma_tflops=None):
+    """Roofline of sdf_fwd_f32_kernel at lod 4 over `points` queries."""
+    pk = peaks()
+    grid_bytes = sum(fv.fm.numel() * 4 for fv in net.features)
+    if line_peak is None:
+        line_peak = line_read_peak(dev, grid_bytes)
+    if fma_tflops is None:
+        fma_tflops = fma_peak(dev)
+    traffic, tnote = ncu_traffic("sdf_fwd_f32_kernel", points)
+    terms = {
+        "gather_l2": (points * F32_GATHER_BYTES, line_peak, "GB/s",
+                      "measured live: random whole 128-byte lines of an L2-resident buffer the size of the "
+                      "volumes (nglod_measure_line_reads)"),
+        "hbm": (points * 16 + grid_bytes, pk["hbm_gbs"], "GB/s", f"{pk['source']} hbm_gbs (burst copy)"),
+        "fp32_pipe": (points * F32_FLOP, fma_tflops, "TFLOP/s",
+                      "measured live: float32 FMA chains at full occupancy (nglod_measure_fma)"),
+    }
+    return roofline("sdf_fwd_f32_kernel", sec, terms,
+                    {"hbm_bytes": 16, "gathered_bytes": F32_GATHER_BYTES, "fp32_flop": F32_FLOP},
+                    points, traffic, tnote,
+                    note="one launch reads each point once and the 40.5 MB of float32 volumes from HBM; the "
+                         "corner gathers (5,120 B per query, whole 128-byte vertex lines) are served by L2/L1")
+
+
 def run_ours(args):
     ws, rank, local = dist_setup()
     dev = torch.device("cuda", local)
@@ -229,9 +341,7 @@ def run_ours(args):
     import nglod_gb300 as ng
     from nglod_gb300 import synthetic
     ng.load_library()
-    from nglod_gb300.bf16 import Bf16OctreeSDF
     net, (c, r) = build_model(dev)
-    bnet = Bf16OctreeSDF(net)
     x_host = synthetic.near_surface_query(N_POINTS, c, r, seed=1).pin_memory()
     x = x_host.to(dev)
     out_host = torch.empty(N_POINTS, 1).pin_memory()
@@ -239,15 +349,11 @@ def run_ours(args):
     stream = torch.cuda.current_stream(dev)
 
     def step():
-        return bnet.sdf(x, lod=LOD)
-
-    def step32():
         with torch.no_grad():
             return net.sdf(x, lod=LOD)
 
     for _ in range(max(args.warmup, 3)):
         step()
-        step32()
     torch.cuda.synchronize()
 
     clocks = ClockSampler(local)
@@ -262,15 +368,12 @@ def run_ours(args):
     kern_ms = max_over_ranks(kern_ms, ws, dev)
     ms_per_step = kern_ms / args.steps
     value = ws * N_POINTS / (ms_per_step / 1e3)
-    bnet.check_status()
-    steps32 = max(10, args.steps // 5)
-    ms32 = max_over_ranks(time_steps(step32, steps32, flush, stream), ws, dev) / steps32
 
-    # e2e through the public API with host buffers: Bf16OctreeSDF.sdf_host ->
-    # nglod_sdf_fwd_bf16_host copies the pinned points in and the distances
-    # out every step, in 256k-point chunks whose copies overlap the kernels.
+    # e2e through the public API with host buffers: OctreeSDF.sdf_host ->
+    # nglod_sdf_fwd_host copies the pinned points in and the distances out
+    # every step, in 256k-point chunks whose copies overlap the kernels.
     def e2e_step():
-        bnet.sdf_host(x_host, lod=LOD, out=out_host)
+        net.sdf_host(x_host, lod=LOD, out=out_host)
 
     e2e_steps = min(args.steps, 100)
     for _ in range(3):
@@ -279,62 +382,28 @@ def run_ours(args):
     barrier(ws)
     e2e_ms = time_steps(e2e_step, e2e_steps, flush, stream) / e2e_steps
     e2e_ms = max_over_ranks(e2e_ms, ws, dev)
-    ref = bnet.sdf(x[:4096], lod=LOD)
+    with torch.no_grad():
+        ref = net.sdf(x[:4096], lod=LOD)
     torch.cuda.synchronize()
     assert torch.equal(out_host[:4096].to(dev), ref), "e2e result differs from the resident result"
 
-    pk = peaks()
-    grid_bytes = sum(fv.fm.numel() * 2 for fv in net.features)
-    pair_bytes = sum(pv.numel() * 2 for pv in bnet.pairs) or grid_bytes  # what the launch reads
-    line_peak = line_read_peak(dev, pair_bytes)
-    hbm_bytes = N_POINTS * (12 + 4) + pair_bytes
-    gather_bytes = N_POINTS * (LOD + 1) * 8 * 32 * 2
-    tc_flop = N_POINTS * 2 * 35 * 128
-    sec = ms_per_step / 1e3
-    roofline = {
-        "bound": "hbm", "achieved": hbm_bytes / sec / 1e9, "peak": pk["hbm_gbs"], "unit": "GB/s",
-        "frac": hbm_bytes / sec / 1e9 / pk["hbm_gbs"], "traffic": NCU_TRAFFIC_BYTES,
-        "traffic_source": NCU_TRAFFIC_SOURCE, "algorithmic_bytes": hbm_bytes,
-        "peak_source": f"{pk['source']} hbm_gbs (burst copy)",
-        "kernel": "sdf_fwd_bf16_tc_kernel",
-        "per_query": {"hbm_bytes": 16, "gathered_bytes": (LOD + 1) * 8 * 32 * 2, "tensor_flop": 2 * 35 * 128,
-                      "fp32_epilogue_flop": 3 * 128},
-        "binding": {"resource": "L1 data-pipe wavefronts (corner gathers + tile rows)", "frac": 0.737,
-                    "issue_active": 0.568,
-                    "source": "ncu --set full capture of one launch (profiles/sdf_fwd_bf16_tc_4M.md)"},
-        "gather_gbs": gather_bytes / sec / 1e9,
-        "gather": {"gbs": gather_bytes / sec / 1e9, "line_read_peak_gbs": line_peak,
-                   "frac": gather_bytes / sec / 1e9 / line_peak,
-                   "peak_source": "measured live: random whole 128-byte lines of an L2-resident buffer the size of "
-                                  "the pair volumes, read with the gather's 256-bit loads (nglod_measure_line_reads)",
-                   "note": "the gathered bytes (2,560 B per query) include L1 hits (about 28 %), so this fraction "
-                           "may exceed the share of the L2 ceiling"},
-        "tensor_tflops": tc_flop / sec / 1e12,
-        "tensor_frac_of_bf16_peak": tc_flop / sec / 1e12 / pk["bf16_tflops"],
-        "note": "one launch reads each point once and the 40.4 MB of bf16 pair volumes (each vertex beside "
-                "its +x neighbour, 128-byte lines) from HBM; the corner gathers (2,560 B/query, four whole "
-                "lines per LOD) are served by L2/L1, and the gather's instruction stream (half of it bf16 "
-                "unpacking) binds the kernel: with every load an L1 hit it still takes 88 % of the time; "
-                "the 35x128 decoder layer runs on tcgen05 tensor cores and is a small share of the time",
-    }
-    sec32 = ms32 / 1e3
-    fp32 = {"value": ws * N_POINTS / sec32, "unit": UNIT, "ms_per_step": ms32, "steps": steps32,
-            "kernel": "sdf_fwd_f32_kernel", "parity": "1e-5 abs vs the reference",
-            "gather_gbs": N_POINTS * (LOD + 1) * 8 * 32 * 4 / sec32 / 1e9,
-            "fp32_tflops": N_POINTS * ((LOD + 1) * 8 * 32 * 2 + 2 * (36 * 128 + 128)) / sec32 / 1e12,
-            "hbm_frac": (N_POINTS * 16 + grid_bytes * 2) / sec32 / 1e9 / pk["hbm_gbs"]}
+    line_peak = line_read_peak(dev, sum(fv.fm.numel() * 4 for fv in net.features))
+    fma_tflops = fma_peak(dev)
+    roof = f32_roofline(net, ms_per_step / 1e3, N_POINTS, dev, line_peak, fma_tflops)
+    roof["measured_ceilings"] = {"line_read_gbs": line_peak, "fp32_fma_tflops": fma_tflops}
 
     extras = {}
+    trained = None
     if not args.no_extras:
-        extras["trace"] = bench_trace(net, bnet, dev, flush, stream)
-        extras["summed"] = bench_summed(net, bnet, x, dev, flush, stream)
-
-    if not args.no_extras:
+        extras["train"], trained = bench_train(dev, flush, stream)
+        extras["bf16"] = bench_bf16(trained, x, x_host, c, r, dev, flush, stream, args.steps, line_peak)
+        extras["trace"] = bench_trace(net, dev, flush, stream)
+        extras["summed"] = bench_summed(trained, x, dev, flush, stream)
         extras["serve"] = bench_serve(dev)
-        extras["train"] = bench_train(dev, flush, stream)
         extras["sparse"] = bench_sparse(net, dev, flush, stream)
-        extras["shade"] = bench_shade(net, bnet, dev, flush, stream)
+        extras["shade"] = bench_shade(net, dev, flush, stream)
         extras["mesh"] = bench_mesh(dev, flush, stream)
+        extras["torch_ops_gpu"] = bench_torch_ops_sdf(net, x, dev, flush, stream)
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_extras:
@@ -344,16 +413,16 @@ def run_ours(args):
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": WORKLOAD, "points": N_POINTS, "lod": LOD,
-                       "form": "BF16 (bf16 volumes, tcgen05 bf16 decoder, fp32 accumulate)",
+                       "form": "float32 drop-in (the reference's arithmetic, per-LOD gather and sum)",
                        "point_distribution": "half U[-1,1]^3, half within 0.02 of the 16-sphere union (seed 1)",
                        "l2": "256 MiB flush between timed steps", "parallelism": f"replicas x{ws}"},
-            "e2e": {"value": ws * N_POINTS / (e2e_ms / 1e3), "unit": UNIT,
+            "e2e": {"value": ws * N_POINTS / (e2e_ms / 1e3), "unit": UNIT, "ms_per_step": e2e_ms,
                     "h2d_bytes_per_step": N_POINTS * 12, "d2h_bytes_per_step": N_POINTS * 4},
             "gpu_launches": args.steps,
-            "roofline": roofline,
-            "fp32": fp32,
+            "parity": "1e-5 abs on SDF values vs the reference (tests/test_dense_gpu.py)",
+            "roofline": roof,
             "clocks": clk,
             "cpu_baseline": cpu,
             "wall_s_timed_region": wall,
@@ -362,7 +431,80 @@ def run_ours(args):
         print(json.dumps(line), flush=True)
 
 
-def bench_summed(net, bnet, x, dev, flush, stream, steps=100):
+def bench_torch_ops_sdf(net, x, dev, flush, stream, steps=5):
+    """The reference's OctreeSDF.sdf computation in stock torch operators
+    (F.grid_sample on channel-first volumes, nn.Linear) on the same GPU and
+    points, float32: context for the drop-in's headline."""
+    ref = _TorchOpsOctreeSDF(net).to(dev).eval()
+    with torch.no_grad():
+        for _ in range(2):
+            ref.sdf(x, LOD)
+        torch.cuda.synchronize()
+        ms = time_steps(lambda: ref.sdf(x, LOD), steps, flush, stream) / steps
+    return {"workload": "OctreeSDF.sdf(x, lod=4) in stock torch ops on the GPU, float32, the headline's 4M points",
+            "value": N_POINTS / (ms / 1e3), "unit": UNIT, "ms_per_step": ms}
+
+
+def fp64_errors(net, model, x, lods=range(LOD + 1)):
+    """Max / mean |model.sdf - float64 reference| per LOD on points x: the
+    float64 reference is the reference's computation in torch ops
+    (F.grid_sample, Linear) with float64 volumes and weights on the GPU."""
+    ref = _TorchOpsOctreeSDF(net).to(x.device).double().eval()
+    out = {}
+    with torch.no_grad():
+        for lod in lods:
+            want = ref.sdf(x.double(), lod)
+            d = (model.sdf(x, lod=lod).double() - want).abs()
+            out[str(lod)] = {"max": float(d.max().item()), "mean": float(d.mean().item())}
+    return out
+
+
+def bench_bf16(tnet, x, x_host, c, r, dev, flush, stream, steps, line_peak_f32=None):
+    """The mixed-precision inference form (bf16 volumes, tcgen05 bf16 decoder,
+    fp32 accumulate) on the headline's 4,194,304 points at lod 4, on the
+    weights of 2,000 training steps from seed 1; with each LOD's max and mean
+    error against float64 on every 16th point (262,144 points), beside the
+    float32 drop-in's."""
+    from nglod_gb300.bf16 import Bf16OctreeSDF
+    pk = peaks()
+    bnet = Bf16OctreeSDF(tnet)
+    out_host = torch.empty(N_POINTS, 1).pin_memory()
+    for _ in range(3):
+        bnet.sdf(x, lod=LOD)
+    torch.cuda.synchronize()
+    k = max(10, min(steps, 500))
+    ms = time_steps(lambda: bnet.sdf(x, lod=LOD), k, flush, stream) / k
+    for _ in range(3):
+        bnet.sdf_host(x_host, lod=LOD, out=out_host)
+    torch.cuda.synchronize()
+    ke = min(k, 100)
+    e2e_ms = time_steps(lambda: bnet.sdf_host(x_host, lod=LOD, out=out_host), ke, flush, stream) / ke
+    bnet.check_status()
+    pair_bytes = sum(pv.numel() * 2 for pv in bnet.pairs) or sum(fv.fm.numel() * 2 for fv in tnet.features)
+    line_peak = line_read_peak(dev, pair_bytes)
+    sec = ms / 1e3
+    traffic, tnote = ncu_traffic("sdf_fwd_bf16_tc_kernel", N_POINTS)
+    roof = roofline("sdf_fwd_bf16_tc_kernel", sec, {
+        "gather_l2": (N_POINTS * (LOD + 1) * 8 * 32 * 2, line_peak, "GB/s",
+                      "measured live: random whole 128-byte lines of an L2-resident buffer the size of the pair "
+                      "volumes (nglod_measure_line_reads)"),
+        "hbm": (N_POINTS * 16 + pair_bytes, pk["hbm_gbs"], "GB/s", f"{pk['source']} hbm_gbs (burst copy)"),
+        "tensor": (N_POINTS * 2 * 35 * 128, pk["bf16_tflops"], "TFLOP/s", f"{pk['source']} bf16_tflops (burst)"),
+    }, {"hbm_bytes": 16, "gathered_bytes": (LOD + 1) * 8 * 32 * 2, "tensor_flop": 2 * 35 * 128}, N_POINTS,
+        traffic, tnote)
+    xs = x[::ERR_SAMPLE_STRIDE].contiguous()
+    return {"workload": "Bf16OctreeSDF.sdf(x, lod=4): bf16 volumes, tcgen05 bf16 decoder, fp32 accumulate; the "
+                        "headline's 4,194,304 points; weights of 2,000 training steps from seed 1",
+            "value": N_POINTS / sec, "unit": UNIT, "ms_per_step": ms, "steps": k, "dtype": "bf16",
+            "e2e": {"value": N_POINTS / (e2e_ms / 1e3), "unit": UNIT, "ms_per_step": e2e_ms,
+                    "h2d_bytes_per_step": N_POINTS * 12, "d2h_bytes_per_step": N_POINTS * 4},
+            "roofline": roof,
+            "error_vs_fp64_per_lod": fp64_errors(tnet, bnet, xs),
+            "f32_dropin_error_vs_fp64_per_lod": fp64_errors(tnet, tnet, xs),
+            "error_sample": f"every {ERR_SAMPLE_STRIDE}th point of the 4,194,304 ({xs.shape[0]} points)"}
+
+
+def bench_summed(net, x, dev, flush, stream, steps=100):
     """The BF16 form over LOD-summed volumes (Bf16OctreeSDF(summed=True)):
     the headline workload with one 8-corner gather per query instead of
     LOD + 1, against the per-LOD BF16 form on the same points, plus the
@@ -371,6 +513,7 @@ def bench_summed(net, bnet, x, dev, flush, stream, steps=100):
     from nglod_gb300 import synthetic
     from nglod_gb300.bf16 import Bf16OctreeSDF
     from nglod_gb300.options import default_args
+    bnet = Bf16OctreeSDF(net)
     sb = Bf16OctreeSDF(net, summed=True)
     for _ in range(3):
         got = sb.sdf(x, lod=LOD)
@@ -427,10 +570,18 @@ def bench_aabb(dev, flush, stream, steps=50):
             "ms_python_api": ms_api}
 
 
-def bench_trace(net, bnet, dev, flush, stream):
+def bench_trace(net, dev, flush, stream):
+    """Sphere tracers at 1920x1080, 64 steps, lod None (finest), camera (0,0,4)
+    fov 30: the fused BF16 and float32 tracers, the plain per-step float32
+    tracer (the reference's host loop on our sdf kernel) and the reference's
+    SphereTracer.forward computation in stock torch ops, all on the GPU.  The
+    plain tracer counts the frame's sdf evaluations, the unit of the fused
+    tracers' rooflines."""
     import nglod_gb300 as ng
     from nglod_gb300 import synthetic
+    from nglod_gb300.bf16 import Bf16OctreeSDF
     from nglod_gb300.options import default_args
+    bnet = Bf16OctreeSDF(net)
     ro, rd = synthetic.look_at_rays(width=TRACE_W, height=TRACE_H)
     ro, rd = ro.to(dev), rd.to(dev)
     a = default_args(num_steps=TRACE_STEPS)
@@ -450,8 +601,9 @@ def bench_trace(net, bnet, dev, flush, stream):
     bnet.check_status()
     both = rb.hit & rb16.hit
     derr = (rb.depth[both] - rb16.depth[both]).abs()
-    plain(net, ro, rd)
+    rbp = plain(net, ro, rd)
     torch.cuda.synchronize()
+    evals = int(plain.last_evaluations.item())
     runs = []
     for _ in range(3):  # host-synchronising loop: wall clock, median of three frames
         t0 = time.perf_counter()
@@ -459,16 +611,85 @@ def bench_trace(net, bnet, dev, flush, stream):
         torch.cuda.synchronize()
         runs.append((time.perf_counter() - t0) * 1e3)
     pms = statistics.median(runs)
-    return {"workload": f"SphereTracer {TRACE_W}x{TRACE_H}, {TRACE_STEPS} steps, lod=None (finest), camera (0,0,4) fov 30",
+    # the reference's SphereTracer.forward in stock torch ops on the GPU
+    tnet = _TorchOpsOctreeSDF(net).to(dev).eval()
+    rbt = torch_ops_trace(tnet, ro, rd, LOD, TRACE_STEPS)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    rbt = torch_ops_trace(tnet, ro, rd, LOD, TRACE_STEPS)
+    torch.cuda.synchronize()
+    tms = (time.perf_counter() - t0) * 1e3
+    pk = peaks()
+    line_peak = line_read_peak(dev, sum(fv.fm.numel() * 4 for fv in net.features))
+    fma = fma_peak(dev)
+    roof32 = roofline("trace_f32_kernel", ms / 1e3, {
+        "gather_l2": (evals * F32_GATHER_BYTES, line_peak, "GB/s", "measured live (nglod_measure_line_reads)"),
+        "fp32_pipe": (evals * F32_FLOP, fma, "TFLOP/s", "measured live (nglod_measure_fma)"),
+        "hbm": (n * (24 + 12 + 4 + 12 + 1) + sum(fv.fm.numel() * 4 for fv in net.features), pk["hbm_gbs"], "GB/s",
+                f"{pk['source']} hbm_gbs")},
+        {"sdf_evaluation": {"gathered_bytes": F32_GATHER_BYTES, "fp32_flop": F32_FLOP},
+         "ray": {"hbm_bytes": 24 + 12 + 4 + 12 + 1}}, evals)
+    line_peak16 = line_read_peak(dev, sum(fv.fm.numel() * 2 for fv in net.features))
+    roof16 = roofline("trace_bf16_tc_kernel", ms16 / 1e3, {
+        "gather_l2": (evals * (LOD + 1) * 8 * 32 * 2, line_peak16, "GB/s", "measured live (nglod_measure_line_reads)"),
+        "tensor": (evals * 2 * 35 * 128, pk["bf16_tflops"], "TFLOP/s", f"{pk['source']} bf16_tflops (burst)"),
+        "hbm": (n * (24 + 12 + 4 + 12 + 1) + sum(fv.fm.numel() * 2 for fv in net.features), pk["hbm_gbs"], "GB/s",
+                f"{pk['source']} hbm_gbs")},
+        {"sdf_evaluation": {"gathered_bytes": (LOD + 1) * 8 * 32 * 2, "tensor_flop": 2 * 35 * 128},
+         "ray": {"hbm_bytes": 24 + 12 + 4 + 12 + 1}}, evals)
+    bt = rb.hit & rbt.hit
+    return {"workload": f"SphereTracer {TRACE_W}x{TRACE_H}, {TRACE_STEPS} steps, lod=None (finest), camera (0,0,4) "
+                        "fov 30",
+            "sdf_evaluations_per_frame": evals,
             "fused_f32_rays_per_s": n / (ms / 1e3), "fused_f32_ms": ms,
             "fused_bf16_rays_per_s": n / (ms16 / 1e3), "fused_bf16_ms": ms16,
             "bf16_vs_f32_hit_agreement": float((rb.hit == rb16.hit).float().mean().item()),
             "bf16_vs_f32_depth_mean_abs": float(derr.mean().item()) if derr.numel() else None,
             "plain_f32_rays_per_s": n / (pms / 1e3), "plain_f32_ms": pms, "hits": hits, "kernel_launches_fused": 2,
-            "bf16_over_plain_f32": (n / (ms16 / 1e3)) / (n / (pms / 1e3))}
+            "plain_vs_fused_f32_hit_agreement": float((rb.hit == rbp.hit).float().mean().item()),
+            "torch_ops_f32_ms": tms, "torch_ops_f32_rays_per_s": n / (tms / 1e3),
+            "torch_ops_vs_fused_f32": {"hit_agreement": float((rb.hit == rbt.hit).float().mean().item()),
+                                       "depth_max_abs": float((rb.depth[bt] - rbt.depth[bt]).abs().max().item())
+                                       if bt.any() else None},
+            "bf16_over_plain_f32": pms / ms16, "bf16_over_fused_f32": ms / ms16,
+            "roofline_f32": roof32, "roofline_bf16": roof16}
 
 
-def bench_shade(net, bnet, dev, flush, stream):
+def torch_ops_trace(tnet, ray_o, ray_d, lod, num_steps, min_dis=3e-4, far=10.0):
+    """SphereTracer.forward (sdf-net/lib/tracer/SphereTracer.py:41-132) with
+    the torch-ops OctreeSDF as the network: aabb entry (our kernel, bit-exact
+    with the reference's), then the masked march and finite-difference
+    normals, as the reference runs it on CUDA tensors."""
+    import torch.nn.functional as F
+    from nglod_gb300.sol_nglod import aabb
+    x, t, cond = aabb(ray_o, ray_d)
+    normal = torch.zeros_like(x)
+    with torch.no_grad():
+        d = tnet.sdf(x, lod)
+        dprev = d.clone()
+        hit = torch.zeros_like(d).bool()[:, 0]
+        for _ in range(num_steps):
+            hit = (torch.abs(t) < far)[:, 0]
+            cond = cond & (torch.abs(d) > min_dis)[:, 0]
+            cond = cond & (torch.abs((d + dprev) / 2.0) > min_dis * 3)[:, 0]
+            cond = cond & hit
+            if not cond.any():
+                break
+            x = torch.where(cond.view(-1, 1), torch.addcmul(ray_o, ray_d, t), x)
+            dprev = torch.where(cond.unsqueeze(1), d, dprev)
+            d[cond] = tnet.sdf(x[cond], lod)
+            t = torch.where(cond.view(-1, 1), t + d, t)
+        hit = hit & ~(torch.abs(x) > 1.0).any(dim=-1)
+        xh = x[hit]
+        h = 1.0 / (64.0 * 3.0)
+        eps = torch.eye(3, device=x.device) * h
+        grad = torch.cat([tnet.sdf(xh + eps[k], lod) - tnet.sdf(xh - eps[k], lod) for k in range(3)], dim=-1) / (h * 2)
+        normal[hit] = F.normalize(grad, p=2, dim=-1, eps=1e-5)
+    from nglod_gb300.tracer import RenderBuffer
+    return RenderBuffer(x=x, depth=t, hit=hit, normal=normal)
+
+
+def bench_shade(net, dev, flush, stream):
     """Shaded frame (Renderer.shade_tensor with a ground plane, shadow rays and
     ambient occlusion, matcap colour): 1920x1080, 64 steps, camera (1.6, 1.4,
     3.4) looking at (0, -0.1, 0), fov 35, for the BF16 and float32 networks;
@@ -477,6 +698,8 @@ def bench_shade(net, bnet, dev, flush, stream):
     from nglod_gb300.options import default_args
     from nglod_gb300.renderer import Renderer
     import nglod_gb300 as ng
+    from nglod_gb300.bf16 import Bf16OctreeSDF
+    bnet = Bf16OctreeSDF(net)
     tr = ng.SphereTracer(default_args(num_steps=TRACE_STEPS))
     r = Renderer(tr, args=default_args(render_res=[TRACE_W, TRACE_H], shadow=True, ao=True, ground_height=-0.75))
     f, t, fov = (1.6, 1.4, 3.4), (0.0, -0.1, 0.0), 35.0
@@ -546,16 +769,33 @@ class _TorchOpsOctreeSDF(torch.nn.Module):
                 return d
 
 
-def bench_train(dev, flush, stream, batch=524_288, steps=20, warm=3, train_steps=2000):
+def train_model(seed, dev, steps=TRAIN_STEPS, batch=TRAIN_BATCH, pool_size=8):
+    """A 5-LOD OctreeSDF trained by the project's own kernels as configuration
+    2 prescribes, on the 16-sphere union of `seed`: initial weights from
+    torch seed `seed`, L2 over all LODs, Adam lr 1e-3, `steps` steps over a
+    pool of 524,288-point batches (1/3 uniform, 2/3 surface + N(0, 0.01^2)).
+    Returns (net in eval mode, loss trace)."""
+    import nglod_gb300 as ng
+    from nglod_gb300 import synthetic, trainer
+    from nglod_gb300.options import default_args
+    c, r = synthetic.sphere_union(seed)
+    torch.manual_seed(seed)
+    net = ng.OctreeSDF(default_args(num_lods=5, base_lod=2)).to(dev).train()
+    pool = [synthetic.training_batch(batch, c, r, seed=100 * seed + k) for k in range(pool_size)]
+    pool = [(a.to(dev), b.to(dev)) for a, b in pool]
+    _, losses = trainer.fit(net, pool, steps, lr=1e-3, seed=5 + seed)
+    return net.eval(), losses
+
+
+def bench_train(dev, flush, stream, batch=TRAIN_BATCH, steps=20, warm=3, train_steps=TRAIN_STEPS):
     """Training step of Trainer.step_geometry (L2 over all 5 LODs, Adam 1e-3)
     on a 524,288-point batch of the 16-sphere union (seed 1): ours (fused
     forward over every LOD, hand-written backward, FusedAdam) against the
     reference's computation in stock PyTorch operators on the same GPU.
-    Then 2,000 training steps from seed 1 and the BF16 form's difference to
-    the float32 drop-in per LOD on the trained weights."""
+    Then 2,000 training steps from seed 1 (configuration 3's weights).
+    Returns (leg dict, trained net or None)."""
     import nglod_gb300 as ng
     from nglod_gb300 import synthetic, trainer
-    from nglod_gb300.bf16 import Bf16OctreeSDF
     from nglod_gb300.options import default_args
     c, r = synthetic.sphere_union(1)
     x, g = synthetic.training_batch(batch, c, r, seed=0)
@@ -583,37 +823,40 @@ def bench_train(dev, flush, stream, batch=524_288, steps=20, warm=3, train_steps
     torch.cuda.synchronize()
     ms_ours = time_steps(ours, steps, flush, stream) / steps
     ms_ref = time_steps(theirs, max(3, steps // 4), flush, stream) / max(3, steps // 4)
+    trainer.check_backward_status()
+    pk = peaks()
+    nparams = sum(p.numel() for p in net.parameters())
+    line_peak = line_read_peak(dev, sum(fv.fm.numel() * 4 for fv in net.features))
+    # per point, all 5 LODs in one pass: forward gather 5,120 B and backward
+    # corner scatter 5,120 B (L2); decoder FLOPs 5 x 9,216 forward and about
+    # 86 kFLOP backward; HBM: 16 B of point and target, plus Adam's 28 B per
+    # parameter per step
+    per_pt_flop = 5 * 9216 + 5 * (2 * 35 * 128 + 2 * 128 * 32 + 2 * 128 * 35 + 2 * 128)
+    roof = roofline("training step (sdf_fwd_train_tc + sdf_bwd_decoder_tc + sdf_bwd_scatter + adam)", ms_ours / 1e3, {
+        "gather_l2": (batch * 2 * 5120, line_peak, "GB/s", "measured live (nglod_measure_line_reads)"),
+        "hbm": (batch * 16 + nparams * 28, pk["hbm_gbs"], "GB/s", f"{pk['source']} hbm_gbs"),
+        "tensor": (batch * per_pt_flop, pk["bf16_tflops_sustained"], "TFLOP/s",
+                   f"{pk['source']} bf16_tflops_sustained")},
+        {"point": {"gathered_bytes": 5120, "scattered_bytes": 5120, "decoder_flop": per_pt_flop, "hbm_bytes": 16},
+         "parameter": {"hbm_bytes": 28}}, batch)
     out = {"workload": "Trainer.step_geometry, batch 524,288 (1/3 uniform, 2/3 surface + N(0, 0.01^2)), "
                        "L2 over LOD 0..4, Adam lr 1e-3",
            "ours_ms_per_step": ms_ours, "ours_points_per_s": batch / (ms_ours / 1e3),
            "torch_ops_ms_per_step": ms_ref, "torch_ops_points_per_s": batch / (ms_ref / 1e3),
-           "speedup_vs_torch_ops": ms_ref / ms_ours,
+           "speedup_vs_torch_ops": ms_ref / ms_ours, "roofline": roof,
            "gradient_check": "tests/test_train_gpu.py: 1e-4 relative vs reference autograd, 1e-3 vs FP64 differences"}
     if train_steps == 0:
-        return out
-    # 2,000 steps of configuration 2 from seed 1 (fresh batches every step)
-    torch.manual_seed(1)
-    net = ng.OctreeSDF(default_args(num_lods=5, base_lod=2)).to(dev).train()
+        return out, None
     t0 = time.perf_counter()
-    pool = [synthetic.training_batch(batch, c, r, seed=100 + k) for k in range(8)]
-    pool = [(a.to(dev), b.to(dev)) for a, b in pool]
-    _, losses = trainer.fit(net, pool, train_steps, lr=1e-3, seed=5)
+    tnet, losses = train_model(1, dev, train_steps, batch)
     torch.cuda.synchronize()
     out["train_2000_steps_s"] = time.perf_counter() - t0
     out["train_loss_trace"] = losses
-    net.eval()
-    bnet = Bf16OctreeSDF(net)
-    q = synthetic.near_surface_query(4_194_304, c, r, seed=1).to(dev)
-    errs = {}
+    q = synthetic.near_surface_query(262_144, c, r, seed=1).to(dev)
+    gt = synthetic.sphere_union_sdf(q.double(), c, r).float()[:, None]
     with torch.no_grad():
-        for lod in range(5):
-            d = (bnet.sdf(q, lod=lod) - net.sdf(q, lod=lod)).abs()
-            errs[lod] = {"max": float(d.max().item()), "mean": float(d.mean().item())}
-    out["trained_bf16_vs_f32_per_lod"] = errs
-    gt = synthetic.sphere_union_sdf(q[:262144].double(), c, r).float()[:, None]
-    with torch.no_grad():
-        out["trained_f32_l1_vs_analytic_lod4"] = float((net.sdf(q[:262144], lod=4) - gt).abs().mean().item())
-    return out
+        out["trained_f32_l1_vs_analytic_lod4"] = float((tnet.sdf(q, lod=4) - gt).abs().mean().item())
+    return out, tnet
 
 
 def bench_sparse(net, dev, flush, stream, level=7, lod=4, steps=64):
@@ -664,6 +907,17 @@ def bench_sparse(net, dev, flush, stream, level=7, lod=4, steps=64):
     torch.cuda.synchronize()
     ms_sum = time_steps(lambda: sps.render(ro, rd, lod=lod, num_steps=steps), reps, flush, stream) / reps
     sps.check_status()
+    # traversal roofline: level l's pass reads each level-l nugget (8 B), its
+    # point (8 B), octree byte (1 B) and child prefix (4 B) and the ray
+    # (24 B), and writes 8 B per hit child
+    counts = [int(spc.spc_raytrace(s.GetOctree(), s.GetPoints(), s.GetPyramid(), ro, rd, lv,
+                                   prefix=s.GetPrefix()).shape[0]) for lv in range(lod + 3)]
+    trav_bytes = sum(counts[lv] * (8 + 8 + 1 + 4 + 24) + counts[lv + 1] * 8 for lv in range(lod + 2))
+    pk = peaks()
+    trav_roof = roofline("traverse_decide_kernel + traverse_emit_kernel", ms_trav / 1e3, {
+        "hbm": (trav_bytes, pk["hbm_gbs"], "GB/s", f"{pk['source']} hbm_gbs")},
+        {"nugget_level": {"bytes_in": 8 + 8 + 1 + 4 + 24, "bytes_out_per_hit_child": 8}},
+        sum(counts[:lod + 2]), note="nugget counts per level " + ", ".join(map(str, counts)))
     net.lod = lod
     rb = ng.SphereTracer(default_args(num_steps=128))(net, ro, rd)
     net.lod = None
@@ -676,31 +930,32 @@ def bench_sparse(net, dev, flush, stream, level=7, lod=4, steps=64):
             "frame_ms_f32_decoder": ms32,
             "frame_ms_summed": ms_sum,
             "summed_hit_agreement": float((hits == hit).float().mean().item()),
-            "nuggets": int(nug.shape[0]), "setup_s": setup_s,
+            "nuggets": int(nug.shape[0]), "setup_s": setup_s, "traversal_roofline": trav_roof,
             "vs_dense_f32": {"hit_agreement": float((hit == rb.hit).float().mean().item()),
                              "depth_median_abs": float((t[both] - rb.depth[both]).abs().median().item()),
                              "normal_cos_median": float(cosang.median().item())}}
 
 
-def bench_serve(dev, duration_s=6.0, rate_hz=200.0, num_models=8):
-    """Serving: 8 resident BF16 models (the 16-sphere unions of seeds 2..9 held
-    through analytic_init), a seeded Poisson stream at 200 req/s of renders
-    (256^2, 512^2, 1280x720, 1920x1080, LOD 0-4) and point queries (1e4-1e6
-    points), admitted by the native scheduler (nglod_serve_*) under a 16 GiB
-    HBM budget on 8 slots."""
-    import nglod_gb300 as ng
-    from nglod_gb300 import serve, synthetic
-    from nglod_gb300.analytic_init import init_from_sdf
+def bench_serve(dev, duration_s=6.0, rate_hz=200.0, num_models=8, sweep=(400, 800, 1600, 3200, 6400),
+                sweep_s=2.5, train_steps=TRAIN_STEPS):
+    """Serving: 8 resident BF16 models, each trained by the project's kernels
+    as configuration 2 prescribes on the 16-sphere union of its seed (2..9);
+    a seeded Poisson stream at 200 req/s of renders (256^2, 512^2, 1280x720,
+    1920x1080, LOD 0-4) and point queries (1e4-1e6 points), admitted by the
+    native scheduler (nglod_serve_*) under a 16 GiB HBM budget on 8 slots.
+    Then a rate sweep of the same mix to saturation: per offered rate, the
+    sustained rays/s and queries/s and the p50/p99 latencies, overall and of
+    the 1280x720 renders."""
+    from nglod_gb300 import serve
     from nglod_gb300.bf16 import Bf16OctreeSDF
-    from nglod_gb300.options import default_args
-    models = []
+    t0 = time.perf_counter()
+    models, final_loss = [], []
     for seed in range(2, 2 + num_models):
-        c, r = synthetic.sphere_union(seed)
-        torch.manual_seed(seed)
-        net = ng.OctreeSDF(default_args(num_lods=5, base_lod=2))
-        init_from_sdf(net, lambda p, c=c, r=r: torch.from_numpy(synthetic.sphere_union_sdf(p.numpy(), c, r)),
-                      noise=1e-3, seed=seed)
-        models.append(Bf16OctreeSDF(net.to(dev).eval()))
+        net, losses = train_model(seed, dev, train_steps, pool_size=4)
+        final_loss.append(losses[-1])
+        models.append(Bf16OctreeSDF(net))
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t0
     ex = serve.CudaExecutor(models, dev, num_streams=8)
     gen = torch.Generator(device=dev)
 
@@ -716,8 +971,33 @@ def bench_serve(dev, duration_s=6.0, rate_hz=200.0, num_models=8):
     wl = serve.poisson_workload(duration_s, rate_hz, num_models, seed=7)
     st = serve.run_workload(srv, wl, pts)
     srv.close()
-    st["workload"] = (f"{len(wl)} requests, Poisson {rate_hz:.0f}/s for {duration_s:.0f} s, 8 resident BF16 models; "
-                      "renders 256^2/512^2/1280x720/1920x1080 at LOD 0-4, 64 steps; queries 1e4-1e6 points")
+    st["workload"] = (f"{len(wl)} requests, Poisson {rate_hz:.0f}/s for {duration_s:.0f} s, 8 resident BF16 models "
+                      f"trained {train_steps} steps each on seeds 2..9; renders 256^2/512^2/1280x720/1920x1080 at "
+                      "LOD 0-4, 64 steps; queries 1e4-1e6 points")
+    st["models_train_s"] = train_s
+    st["models_final_loss"] = final_loss
+    rows = []
+    for k, rate in enumerate(sweep):
+        wl = serve.poisson_workload(sweep_s, float(rate), num_models, seed=1000 + k)
+        offered_rays = sum(s_["width"] * s_["height"] for _, s_ in wl if s_["kind"] == "render") / sweep_s
+        offered_q = sum(s_["n"] for _, s_ in wl if s_["kind"] == "query") / sweep_s
+        srv = serve.Server(ex, 16 << 30)
+        r = serve.run_workload(srv, wl, pts)
+        srv.close()
+        hd = r["by_kind"].get("render_1280x720", {})
+        rows.append({"offered_req_per_s": rate, "requests": r["requests"], "failed": r["failed"],
+                     "offered_rays_per_s": offered_rays, "rays_per_s": r["rays_per_s"],
+                     "offered_queries_per_s": offered_q, "queries_per_s": r["queries_per_s"],
+                     "p50_ms": r["p50_ms"], "p99_ms": r["p99_ms"], "p99_1280x720_ms": hd.get("p99_ms"),
+                     "max_concurrent": r["max_concurrent"]})
+        if r["p99_ms"] is not None and r["p99_ms"] > 200.0:
+            break  # far past saturation
+    st["rate_sweep"] = rows
+    ok = [row["offered_req_per_s"] for row in rows
+          if row["p99_1280x720_ms"] is not None and row["p99_1280x720_ms"] < 16.0]
+    st["max_rate_with_1280x720_p99_under_16ms"] = max(ok) if ok else None
+    st["sustained_rays_per_s_max"] = max(row["rays_per_s"] or 0 for row in rows)
+    st["sustained_queries_per_s_max"] = max(row["queries_per_s"] or 0 for row in rows)
     return st
 
 
@@ -744,6 +1024,10 @@ def cpu_baseline(net):
 
 
 def run_reference(args):
+    """The reference's CPU computation (oracle/torch_port.py: OctreeSDF.sdf in
+    the reference's torch operators) on all host cores, on the headline's
+    4,194,304 points per step: W warm-up steps (at most 3) and K timed steps,
+    stopping early only if the timed steps pass REF_TIME_BUDGET_S."""
     ws, rank, _ = dist_setup()
     if rank != 0:
         return
@@ -753,26 +1037,32 @@ def run_reference(args):
     torch.set_num_threads(threads)
     net, (c, r) = build_model(None)
     ref = torch_port.RefOctreeSDF({k: v.cpu() for k, v in net.state_dict().items()}, 5)
-    x = synthetic.near_surface_query(CPU_SAMPLE, c, r, seed=1)
-    warm = max(1, min(args.warmup, 2))  # bounded: each step is a 262k-point CPU sample
+    x = synthetic.near_surface_query(N_POINTS, c, r, seed=1)
+    warm = max(1, min(args.warmup, 3))
     with torch.no_grad():
         for _ in range(warm):
             ref.sdf(x, lod=LOD)
-        steps = max(1, min(args.steps, 5))
+        steps = 0
         t0 = time.perf_counter()
-        for _ in range(steps):
+        while steps < max(1, args.steps):
             ref.sdf(x, lod=LOD)
+            steps += 1
+            if time.perf_counter() - t0 > REF_TIME_BUDGET_S:
+                break
         dt = time.perf_counter() - t0
-    value = CPU_SAMPLE * steps / dt
+    value = N_POINTS * steps / dt
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0, "steps": steps,
-        "warmup": warm, "requested": {"steps": args.steps, "warmup": args.warmup}, "ms_per_step": dt / steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "warmup": warm, "requested": {"steps": args.steps, "warmup": args.warmup},
+        "ms_per_step": dt / steps * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": WORKLOAD, "points": N_POINTS, "lod": LOD,
-                   "sample_points_per_step": CPU_SAMPLE, "parallelism": "host cores"},
+                   "form": "float32 drop-in (the reference's arithmetic, per-LOD gather and sum)",
+                   "point_distribution": "half U[-1,1]^3, half within 0.02 of the 16-sphere union (seed 1)",
+                   "parallelism": f"host cores x{threads}"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{CPU_SAMPLE} points per step of the same workload; the reference's torch "
-                                   f"CPU operators (oracle/torch_port.py)"},
+                         "sample": f"the full {N_POINTS} points per step; the reference's torch CPU operators "
+                                   f"(oracle/torch_port.py), {steps} timed steps"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -782,35 +1072,33 @@ def run_only(args):
     dev = torch.device("cuda", 0)
     torch.cuda.set_device(dev)
     import nglod_gb300 as ng
-    from nglod_gb300.bf16 import Bf16OctreeSDF
+    from nglod_gb300 import synthetic
     ng.load_library()
-    net, _ = build_model(dev)
+    net, (c, r) = build_model(dev)
     flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device=dev)
     stream = torch.cuda.current_stream(dev)
     if args.only == "trace":
-        out = bench_trace(net, Bf16OctreeSDF(net), dev, flush, stream)
+        out = bench_trace(net, dev, flush, stream)
     elif args.only == "aabb":
         out = bench_aabb(dev, flush, stream)
-    elif args.only == "summed":
-        from nglod_gb300 import synthetic
-        x = synthetic.near_surface_query(N_POINTS, *synthetic.sphere_union(1), seed=1).to(dev)
-        bnet = Bf16OctreeSDF(net)
-        for _ in range(3):
-            bnet.sdf(x, lod=LOD)
-        torch.cuda.synchronize()
+    elif args.only in ("summed", "bf16"):
+        x_host = synthetic.near_surface_query(N_POINTS, c, r, seed=1).pin_memory()
+        x = x_host.to(dev)
         k = min(max(args.steps, 1), 100)
-        per_lod_ms = time_steps(lambda: bnet.sdf(x, lod=LOD), k, flush, stream) / k
-        out = {"per_lod_bf16_ms": per_lod_ms, **bench_summed(net, bnet, x, dev, flush, stream, steps=k)}
+        if args.only == "summed":
+            out = bench_summed(net, x, dev, flush, stream, steps=k)
+        else:  # the analytic-init network: same kernels and work as on trained weights
+            out = bench_bf16(net, x, x_host, c, r, dev, flush, stream, k)
     elif args.only == "train":
-        out = bench_train(dev, flush, stream, steps=max(args.steps, 1), warm=max(args.warmup, 1), train_steps=0)
+        out, _ = bench_train(dev, flush, stream, steps=max(args.steps, 1), warm=max(args.warmup, 1), train_steps=0)
     elif args.only == "sparse":
         out = bench_sparse(net, dev, flush, stream)
     elif args.only == "shade":
-        out = bench_shade(net, Bf16OctreeSDF(net), dev, flush, stream)
+        out = bench_shade(net, dev, flush, stream)
     elif args.only == "mesh":
         out = bench_mesh(dev, flush, stream)
     else:
-        out = bench_serve(dev, duration_s=2.0)
+        out = bench_serve(dev, duration_s=2.0, train_steps=200)
     print(json.dumps({"only": args.only, **out}), flush=True)
 
 

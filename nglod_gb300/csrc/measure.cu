@@ -1,0 +1,38 @@
+// Measurement helper for the bench's roofline: the float32 FMA pipe's
+// throughput, measured live on the device the kernels run on (the FMA term
+// of the float32 query kernel is divided by it).
+#include "common.cuh"
+
+namespace nglod {
+
+// Eight independent FMA chains per thread: with 256-thread blocks and eight
+// blocks per SM every scheduler always has an FMA ready, so the loop runs at
+// the pipe's issue rate.  2 * 8 * iters FLOP per thread.
+__global__ void __launch_bounds__(256) fma_rate_kernel(int iters, float seed, float *__restrict__ sink) {
+    float a0 = seed + (float)threadIdx.x, a1 = a0 + 1.f, a2 = a0 + 2.f, a3 = a0 + 3.f;
+    float a4 = a0 + 4.f, a5 = a0 + 5.f, a6 = a0 + 6.f, a7 = a0 + 7.f;
+    const float m = 0.9999999f, c = 1e-7f;
+#pragma unroll 4
+    for (int i = 0; i < iters; ++i) {
+        a0 = __fmaf_rn(a0, m, c);
+        a1 = __fmaf_rn(a1, m, c);
+        a2 = __fmaf_rn(a2, m, c);
+        a3 = __fmaf_rn(a3, m, c);
+        a4 = __fmaf_rn(a4, m, c);
+        a5 = __fmaf_rn(a5, m, c);
+        a6 = __fmaf_rn(a6, m, c);
+        a7 = __fmaf_rn(a7, m, c);
+    }
+    const float s = ((a0 + a1) + (a2 + a3)) + ((a4 + a5) + (a6 + a7));
+    if (s == -1.f) sink[0] = s;  // never true for these inputs; keeps every chain
+}
+
+}  // namespace nglod
+
+extern "C" int nglod_measure_fma(int32_t iters, int32_t blocks, float *sink, nglod_stream_t stream) {
+    using namespace nglod;
+    NGLOD_REQUIRE(sink, NGLOD_ERR_INVALID, "null pointer argument");
+    NGLOD_REQUIRE(iters >= 1 && blocks >= 1, NGLOD_ERR_INVALID, "iters=%d blocks=%d", iters, blocks);
+    fma_rate_kernel<<<blocks, 256, 0, (cudaStream_t)stream>>>(iters, 1.f, sink);
+    return launch_status("nglod_measure_fma");
+}

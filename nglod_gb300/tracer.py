@@ -178,15 +178,32 @@ class PlainSphereTracer(BaseTracer):
     """The reference's host-driven march (SphereTracer.py:41-132) on the GPU.
 
     Every step builds the active mask, synchronises on ``cond.any()``,
-    compacts the active points and calls the float32 sdf kernel on them.
+    compacts the active points and calls the float32 sdf kernel on them: the
+    per-thread decoder form (nglod_sdf_fwd_simt), the arithmetic of the fused
+    float32 tracer, so that the two march identically.
+
+    ``last_evaluations`` (a device int64 tensor) counts the sdf evaluations of
+    the last frame: the first one of every ray, one per ray and march step,
+    and the six finite-difference taps of every hit ray.  The fused tracers
+    march by the same rules, so it is the frame's algorithmic work for them
+    too.
     """
+
+    last_evaluations = None
 
     def forward(self, net, ray_o, ray_d):
         _check_net(net, self.grad_method)
         x, t, cond = aabb(ray_o, ray_d)
         normal = torch.zeros_like(x)
+        evals = torch.full((), x.shape[0], dtype=torch.int64, device=x.device)
+        simt = isinstance(net, OctreeSDF)
+        lod = net.lod if simt and net.lod is not None and 0 <= net.lod < net.num_lods else None
+
+        def f(p):
+            return net._sdf_infer(p, lod, False, simt=True) if simt else net(p)
+
         with torch.no_grad():
-            d = net(x)
+            d = f(x)
             dprev = d.clone()
             hit = torch.zeros_like(d).bool()[:, 0]
             for _ in range(self.num_steps):
@@ -196,14 +213,17 @@ class PlainSphereTracer(BaseTracer):
                 cond = cond & hit
                 if not cond.any():
                     break
+                evals += cond.sum()
                 x = torch.where(cond.view(-1, 1), torch.addcmul(ray_o, ray_d, t), x)
                 dprev = torch.where(cond.unsqueeze(1), d, dprev)
-                d[cond] = net(x[cond]) * self.step_size
+                d[cond] = f(x[cond]) * self.step_size
                 t = torch.where(cond.view(-1, 1), t + d, t)
             hit = hit & ~(torch.abs(x) > 1.0).any(dim=-1)
             xh = x[hit]
+            evals += 6 * xh.shape[0]
             h = 1.0 / (64.0 * 3.0)
             eps = torch.eye(3, device=x.device) * h
-            grad = torch.cat([net(xh + eps[k]) - net(xh - eps[k]) for k in range(3)], dim=-1) / (h * 2.0)
+            grad = torch.cat([f(xh + eps[k]) - f(xh - eps[k]) for k in range(3)], dim=-1) / (h * 2.0)
             normal[hit] = F.normalize(grad, p=2, dim=-1, eps=1e-5)
+        self.last_evaluations = evals
         return RenderBuffer(x=x, depth=t, hit=hit, normal=normal)
