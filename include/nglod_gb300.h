@@ -92,9 +92,26 @@ int nglod_volume_sample(const float *grid, int32_t side, int32_t feature_dim, co
  * BaseLOD.forward (sdf-net/lib/models/BaseLOD.py:37-41).
  * lod in [0, num_lods): out[n] = prediction of that LOD;
  * lod < 0 or >= num_lods: the finest prediction;
- * all_lods != 0: out[num_lods][n] = every LOD's prediction (return_lst). */
+ * all_lods != 0: out[num_lods][n] = every LOD's prediction (return_lst).
+ * Gathers and LOD sums are float32.  For one LOD at hidden_dim 128 the
+ * decoder's feature product runs on the tensor cores as three TF32 products
+ * over big / small splits (relative error about 2^-21 of the dot product,
+ * float32's own size); a bounded wait of that kernel that gives up sets the
+ * flag nglod_dense_status reads.  Other shapes decode per thread in float32. */
 int nglod_sdf_fwd(const nglod_dense_model *model, const float *x, int64_t n,
                   int32_t lod, int32_t all_lods, float *out, nglod_stream_t stream);
+
+/* nglod_sdf_fwd with the per-thread float32 decoder for every shape (the
+ * tensor-core form is not used).  No counterpart in the reference: for
+ * comparisons of the two forms. */
+int nglod_sdf_fwd_simt(const nglod_dense_model *model, const float *x, int64_t n, int32_t lod, int32_t all_lods,
+                       float *out, nglod_stream_t stream);
+
+/* Reads and clears the float32 query's device status on the current device
+ * (synchronous): *status_out = 1 if a bounded tensor-core wait of an
+ * nglod_sdf_fwd call since the last read gave up (its outputs are
+ * incomplete), else 0.  No counterpart in the reference. */
+int nglod_dense_status(int32_t *status_out);
 
 /* nglod_sdf_fwd with the points and results in HOST memory (pinned for the
  * copies to overlap): x_host [n][3], out_host [n].  The points go through a
@@ -201,7 +218,8 @@ int nglod_sdf_fwd_bf16_host(const nglod_bf16_model *model, const float *x_host, 
                             float *out_host, int64_t chunk, void *scratch, int32_t *status, nglod_stream_t stream);
 
 /* For tests of the error path: bounds the per-tile tensor-core wait of
- * later nglod_sdf_fwd_bf16 calls (host setting, all devices) to `polls`
+ * later nglod_sdf_fwd_bf16 and tensor-core nglod_sdf_fwd calls (host
+ * setting, all devices) to `polls`
  * polls of the mbarrier; 0 tests it once without waiting, a negative value
  * restores the default (2^22 polls).  A wait that gives up sets the call's
  * status, stops the kernel after letting the issued product finish, and
@@ -216,6 +234,13 @@ int nglod_debug_mma_wait_polls(int64_t polls);
  * uint32, written only to keep the loads. */
 int nglod_measure_line_reads(const void *buf, int64_t lines, int32_t loads, int32_t blocks, uint32_t *sink,
                              nglod_stream_t stream);
+
+/* Measurement helper, no reference counterpart: `blocks` blocks of 256
+ * threads each run eight independent float32 FMA chains of `iters` steps,
+ * blocks * 256 * 16 * iters FLOP.  Timed, it gives the float32 pipe's
+ * throughput on this device.  sink: one device float, written only to keep
+ * the chains. */
+int nglod_measure_fma(int32_t iters, int32_t blocks, float *sink, nglod_stream_t stream);
 
 /* SphereTracer.forward in the BF16 form: the persistent tracer of
  * nglod_trace with every sdf evaluation (march points and normal taps) done
@@ -294,10 +319,14 @@ int nglod_train_status(int32_t *status_out);
  * Limit: (highest LOD in lod_mask + 1) * n * feature_dim floats must fit in
  * NGLOD_NOALLOC_SCRATCH_BYTES (16 MiB on every GPU that loads the library,
  * held until exit): n <= 26,214 with 5 LODs, 131,072 with one; larger n
- * returns NGLOD_ERR_CAPACITY.  The first call on each device looks up the
- * array's device address (cudaGetSymbolAddress), so make that first call
- * before any stream capture.  All calls share the array: calls that overlap
- * on the GPU race and must be serialised by the caller. */
+ * returns NGLOD_ERR_CAPACITY.  The array's device address belongs to the
+ * CUDA context: every call made outside stream capture looks it up
+ * (cudaGetSymbolAddress) for the current context and caches it per context;
+ * a call made while its stream is capturing uses the cache only.  So make
+ * the first call in each context -- and again after cudaDeviceReset or after
+ * creating a new context -- before any stream capture in it.  All calls
+ * share the array: calls that overlap on the GPU race and must be
+ * serialised by the caller. */
 #define NGLOD_NOALLOC_SCRATCH_BYTES (16u << 20)
 int nglod_sdf_bwd_noalloc(const nglod_dense_model *model, const float *x, int64_t n, uint32_t lod_mask,
                           const float *grad_preds, const float *feats, const uint32_t *relu_masks,

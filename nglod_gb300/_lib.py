@@ -196,6 +196,8 @@ SIGNATURES = {
     "nglod_aabb": (ctypes.c_int, [_vp, _vp, _i64, _vp, _vp, _vp, _vp]),
     "nglod_volume_sample": (ctypes.c_int, [_vp, _i32, _i32, _vp, _i64, _vp, _vp]),
     "nglod_sdf_fwd": (ctypes.c_int, [ctypes.POINTER(DenseModel), _vp, _i64, _i32, _i32, _vp, _vp]),
+    "nglod_sdf_fwd_simt": (ctypes.c_int, [ctypes.POINTER(DenseModel), _vp, _i64, _i32, _i32, _vp, _vp]),
+    "nglod_dense_status": (ctypes.c_int, [_vp]),
     "nglod_trace": (ctypes.c_int, [ctypes.POINTER(DenseModel), ctypes.POINTER(TraceParams), _vp, _vp, _i64,
                                    _vp, _vp, _vp, _vp, _vp, _vp]),
     "nglod_sdf_fwd_train": (ctypes.c_int, [ctypes.POINTER(DenseModel), _vp, _i64, _u32, _vp, _vp, _vp, _vp]),
@@ -229,6 +231,7 @@ SIGNATURES = {
     "nglod_bf16_build_pairs": (ctypes.c_int, [_vp, _i32, _vp, _vp]),
     "nglod_build_summed_volume": (ctypes.c_int, [ctypes.POINTER(DenseModel), _i32, _i32, _vp, _vp]),
     "nglod_measure_line_reads": (ctypes.c_int, [_vp, _i64, _i32, _i32, _vp, _vp]),
+    "nglod_measure_fma": (ctypes.c_int, [_i32, _i32, _vp, _vp]),
     "nglod_debug_mma_wait_polls": (ctypes.c_int, [_i64]),
     "nglod_sdf_fwd_bf16": (ctypes.c_int, [ctypes.POINTER(Bf16Model), _vp, _i64, _i32, _vp, _vp, _vp]),
     "nglod_trace_bf16": (ctypes.c_int, [ctypes.POINTER(Bf16Model), ctypes.POINTER(TraceParams), _vp, _vp, _i64,

@@ -946,5 +946,6 @@ extern "C" int nglod_debug_mma_wait_polls(int64_t polls) {
     NGLOD_REQUIRE(polls <= (int64_t)kWaitPolls, NGLOD_ERR_INVALID, "polls=%lld above the default %u",
                   (long long)polls, kWaitPolls);
     g_bf16_wait_polls = polls < 0 ? kWaitPolls : (uint32_t)polls;
+    set_f32tc_wait_polls(g_bf16_wait_polls);
     return NGLOD_OK;
 }

@@ -22,6 +22,10 @@ inline int launch_status(const char *where) { return cuda_status(cudaGetLastErro
 // Multiprocessor count of the current device (cached per device).
 int num_sms();
 
+// Bound of the tensor-core wait of the float32 query kernel (dense.cu);
+// nglod_debug_mma_wait_polls sets it with the BF16 kernels' bound.
+void set_f32tc_wait_polls(uint32_t polls);
+
 inline bool aligned(const void *p, uintptr_t a) { return (reinterpret_cast<uintptr_t>(p) & (a - 1)) == 0; }
 
 // Host-memory queries: points [n][3] and results [n] in host memory, in

@@ -1,6 +1,7 @@
 // Dense NGLOD path, float32: ray/box entry, fused LOD gather + decoder, and a
 // persistent sphere tracer.  Building blocks live in dense_common.cuh.
 #include "dense_common.cuh"
+#include "tf32_tile.cuh"
 
 namespace nglod {
 
@@ -50,6 +51,166 @@ __global__ void __launch_bounds__(256, kAll ? 2 : 3) sdf_fwd_f32_kernel(const ng
             if (i < n) out[i] = o;
         }
     }
+}
+
+// ---------------------------------------------------------------------------
+// sdf forward, tensor-core form (single LOD, hidden 128)
+// ---------------------------------------------------------------------------
+// The same gather and LOD sum as sdf_fwd_f32_kernel (gather_warp_add_f32, in
+// float32), then the decoder's 32 x 128 feature product on tcgen05 as three
+// TF32 products over big / small splits of both operands (tf32_tile.cuh:
+// relative error about 2^-21 of sum |w f|, the size of float32's rounding),
+// accumulated in TMEM.  The x, y, z and bias terms of the first layer, the
+// ReLU and the 128 -> 1 layer are a float32 epilogue per point.
+//
+// A block of eight warps decodes two 128-point tiles per iteration against
+// one staged weight tile: warps 0-3 fill tile 0, warps 4-7 tile 1 (warp w,
+// lane i owns point 256 q + 32 w + i), one thread issues both tiles' 24
+// MMAs, and each warp reads its rows back from the TMEM lanes of its
+// quadrant (warp % 4) in its tile's 128 columns.  Two blocks per SM hold
+// 2 x 256 TMEM columns, the SM's 512.
+namespace f32tc {
+constexpr int kTP = 128;                      // points per tile (UMMA M)
+constexpr int kTiles = 2;                     // tiles per block iteration
+constexpr int kThreads = kTP * kTiles;        // 256
+constexpr int kH = 128;                       // hidden units (UMMA N)
+constexpr int kK = 32;                        // feature channels along K
+constexpr int kKC = kK / 4;                   // 16-byte core-matrix columns
+constexpr uint32_t kTile = kTP * kK * 4;      // 16 KB
+constexpr size_t kA = 0;                      // tile h: big at kA + 2 h kTile, small after it
+constexpr size_t kW = 2 * kTiles * kTile;     // weights: big, then small
+constexpr size_t kU = kW + 2 * kTile;         // (w0[j][0..2], b0[j]) float4 [kH]
+constexpr size_t kW1 = kU + kH * 16;          // w1 [kH]
+constexpr size_t kBar = kW1 + kH * 4;
+constexpr size_t kSlot = kBar + 8, kAbort = kSlot + 4;
+constexpr size_t kSmem = kAbort + 12;
+constexpr uint32_t kCols = kTiles * kH;       // TMEM columns per block
+static_assert(kTile % 1024 == 0 && kU % 16 == 0 && kBar % 8 == 0, "shared layout alignment");
+static_assert(2 * kSmem <= 227 * 1024, "two blocks per SM");
+}  // namespace f32tc
+
+// Set by a tensor-core wait of sdf_fwd_f32_tc_kernel that gave up; read and
+// cleared by nglod_dense_status.
+__device__ int g_dense_status = 0;
+// Bound of that wait (host side, all devices): kPolls unless a test of the
+// error path lowers it.
+static uint32_t g_f32tc_wait_polls = 1u << 22;
+
+__global__ void __launch_bounds__(f32tc::kThreads, 2)
+    sdf_fwd_f32_tc_kernel(const nglod_dense_model m, const float *__restrict__ x, int64_t n, int L,
+                          float *__restrict__ out, uint32_t polls) {
+    using namespace f32tc;
+    extern __shared__ __align__(1024) uint8_t smem_f32tc[];
+    uint8_t *sm = smem_f32tc;
+    const float4 *su = reinterpret_cast<const float4 *>(sm + kU);
+    const float *sw1 = reinterpret_cast<const float *>(sm + kW1);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(sm + kBar);
+    uint32_t *slot = reinterpret_cast<uint32_t *>(sm + kSlot);
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(sm + kAbort);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int half = warp >> 2, quad = warp & 3;
+
+    // weight tile of LOD L (hidden unit j = row, feature c = K column), split
+    const float *w0 = m.w0[L];
+    for (int u = tid; u < kH * kKC; u += kThreads) {
+        const int j = u / kKC, kc = u % kKC;
+        const float *r = w0 + j * 35 + 3 + 4 * kc;
+        store_split4(sm + kW, sm + kW + kTile, tile_offset32(j, 4 * kc, kKC), make_float4(r[0], r[1], r[2], r[3]));
+    }
+    if (tid < kH) {
+        reinterpret_cast<float4 *>(sm + kU)[tid] =
+            make_float4(w0[tid * 35], w0[tid * 35 + 1], w0[tid * 35 + 2], m.b0[L][tid]);
+        reinterpret_cast<float *>(sm + kW1)[tid] = m.w1[L][tid];
+    }
+    const float b1 = m.b1[L][0];
+    if (warp == 0) tc::tmem_alloc(slot, kCols);
+    if (tid == 0) {
+        tc::mbar_init(bar, 1);
+        *abort_flag = 0;
+    }
+    tc::fence_proxy_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = *slot;
+    const uint32_t sbase = tc::smem_addr(sm);
+    constexpr uint32_t idesc = idesc_tf32_f32(kTP, kH);
+    uint8_t *abig = sm + kA + (size_t)2 * half * kTile;
+    uint8_t *asmall = abig + kTile;
+    const uint32_t taddr = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(half * kH);
+    uint32_t phase = 0;
+
+    for (int64_t q = blockIdx.x; q * kThreads < n; q += gridDim.x) {
+        const int64_t i = q * kThreads + tid;
+        float px = 0.f, py = 0.f, pz = 0.f;
+        if (i < n) {
+            px = x[3 * i];
+            py = x[3 * i + 1];
+            pz = x[3 * i + 2];
+        }
+        // 1. gather: LOD sum of the warp's 32 points, written as tile rows
+        float4 acc[8];
+#pragma unroll
+        for (int p = 0; p < 8; ++p) acc[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll 1
+        for (int l = 0; l <= L; ++l)
+            gather_warp_add_f32(static_cast<const float *>(m.grid[l]), volume_side(m, l), px, py, pz, lane, acc);
+#pragma unroll
+        for (int p = 0; p < 8; ++p)
+            store_split4(abig, asmall, tile_offset32(quad * 32 + 4 * p + (lane >> 3), 4 * (lane & 7), kKC), acc[p]);
+        tc::fence_proxy_async_smem();
+        tc::fence_before_sync();
+        __syncthreads();
+        // 2. one thread issues big*big + big*small + small*big for both tiles
+        if (tid == 0) {
+            tc::fence_after_sync();
+            const uint64_t wb = tc::smem_desc(sbase + (uint32_t)kW, 128, kKC * 128);
+            const uint64_t ws = tc::smem_desc(sbase + (uint32_t)(kW + kTile), 128, kKC * 128);
+#pragma unroll
+            for (int h = 0; h < kTiles; ++h) {
+                const uint64_t ab = tc::smem_desc(sbase + (uint32_t)(kA + 2 * h * kTile), 128, kKC * 128);
+                const uint64_t as = tc::smem_desc(sbase + (uint32_t)(kA + (2 * h + 1) * kTile), 128, kKC * 128);
+#pragma unroll
+                for (int t = 0; t < 3; ++t)
+#pragma unroll
+                    for (int ks = 0; ks < kK / 8; ++ks) {
+                        const uint64_t step = (uint64_t)((ks * 256) >> 4);  // 8 tf32 of K: two core matrices
+                        mma_tf32(tmem + (uint32_t)(h * kH), (t == 2 ? as : ab) + step, (t == 1 ? ws : wb) + step,
+                                 idesc, (t > 0 || ks > 0) ? 1u : 0u);
+                    }
+            }
+            tc::mma_commit(bar);
+            if (!tc::mbar_wait_bounded(bar, phase, polls)) {
+                *abort_flag = 1;
+                atomicExch(&g_dense_status, 1);
+            }
+        }
+        __syncthreads();
+        if (*abort_flag) break;
+        phase ^= 1u;
+        tc::fence_after_sync();
+        // 3. epilogue: x y z and b0 terms, ReLU, the 128 -> 1 layer
+        float o = 0.f;
+#pragma unroll 1
+        for (int c = 0; c < kH / 32; ++c) {
+            float v[32];
+            tc::tmem_load32(taddr + (uint32_t)(32 * c), v);
+#pragma unroll
+            for (int e = 0; e < 32; ++e) {
+                const float4 u = su[32 * c + e];
+                const float z = fmaf(u.x, px, fmaf(u.y, py, fmaf(u.z, pz, v[e] + u.w)));
+                o = fmaf(sw1[32 * c + e], fmaxf(z, 0.f), o);
+            }
+        }
+        if (i < n) out[i] = o + b1;
+        tc::fence_before_sync();
+        __syncthreads();
+    }
+    if (*abort_flag && tid == 0) tc::mbar_wait_bounded(bar, phase, 1u << 22);  // let an in-flight product finish
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if (warp == 0) tc::tmem_dealloc(tmem, kCols);
 }
 
 // One feature volume sampled at every point: out[n][C] (FeatureVolume.forward).
@@ -372,14 +533,25 @@ extern "C" int nglod_volume_sample(const float *grid, int32_t side, int32_t feat
     return launch_status("nglod_volume_sample");
 }
 
-extern "C" int nglod_sdf_fwd(const nglod_dense_model *model, const float *x, int64_t n, int32_t lod,
-                             int32_t all_lods, float *out, nglod_stream_t stream) {
+// The float32 query.  simt: the per-thread decoder (sdf_fwd_f32_kernel)
+// even where the tensor-core form applies.
+static int sdf_fwd_f32(const nglod_dense_model *model, const float *x, int64_t n, int32_t lod, int32_t all_lods,
+                       float *out, cudaStream_t stream, bool simt) {
     NGLOD_REQUIRE(model != nullptr, NGLOD_ERR_INVALID, "model is null");
     const int L = all_lods ? model->num_lods - 1 : resolve_lod(model, lod);
     NGLOD_TRY(check_model(model, L));
     NGLOD_REQUIRE(n >= 0, NGLOD_ERR_INVALID, "n=%lld is negative", (long long)n);
     if (n == 0) return NGLOD_OK;
     NGLOD_REQUIRE(x && out, NGLOD_ERR_INVALID, "null pointer argument");
+    if (!all_lods && !simt && model->hidden_dim == f32tc::kH) {
+        auto k = sdf_fwd_f32_tc_kernel;
+        NGLOD_TRY(prepare_smem(k, f32tc::kSmem));
+        const int64_t want = (n + f32tc::kThreads - 1) / f32tc::kThreads;
+        const int64_t cap = (int64_t)num_sms() * 2;
+        k<<<(int)(want < cap ? want : cap), f32tc::kThreads, f32tc::kSmem, stream>>>(*model, x, n, L, out,
+                                                                                   g_f32tc_wait_polls);
+        return launch_status("nglod_sdf_fwd");
+    }
     const int threads = 256;
     const int ndec = all_lods ? L + 1 : 1;
     // staged decoders, then one [32][kTRow] float transpose buffer per warp
@@ -390,15 +562,37 @@ extern "C" int nglod_sdf_fwd(const nglod_dense_model *model, const float *x, int
         auto k = sdf_fwd_f32_kernel<true>;
         NGLOD_TRY(prepare_smem(k, smem));
         const int64_t cap = resident_blocks(k, threads, smem);
-        k<<<(int)(want < cap ? want : cap), threads, smem, (cudaStream_t)stream>>>(*model, x, n, L, out);
+        k<<<(int)(want < cap ? want : cap), threads, smem, stream>>>(*model, x, n, L, out);
     } else {
         auto k = sdf_fwd_f32_kernel<false>;
         NGLOD_TRY(prepare_smem(k, smem));
         const int64_t cap = resident_blocks(k, threads, smem);
-        k<<<(int)(want < cap ? want : cap), threads, smem, (cudaStream_t)stream>>>(*model, x, n, L, out);
+        k<<<(int)(want < cap ? want : cap), threads, smem, stream>>>(*model, x, n, L, out);
     }
     return launch_status("nglod_sdf_fwd");
 }
+
+extern "C" int nglod_sdf_fwd(const nglod_dense_model *model, const float *x, int64_t n, int32_t lod,
+                             int32_t all_lods, float *out, nglod_stream_t stream) {
+    return sdf_fwd_f32(model, x, n, lod, all_lods, out, (cudaStream_t)stream, false);
+}
+
+extern "C" int nglod_sdf_fwd_simt(const nglod_dense_model *model, const float *x, int64_t n, int32_t lod,
+                                  int32_t all_lods, float *out, nglod_stream_t stream) {
+    return sdf_fwd_f32(model, x, n, lod, all_lods, out, (cudaStream_t)stream, true);
+}
+
+extern "C" int nglod_dense_status(int32_t *status_out) {
+    NGLOD_REQUIRE(status_out != nullptr, NGLOD_ERR_INVALID, "null pointer argument");
+    int32_t v = 0;
+    const int32_t zero = 0;
+    NGLOD_TRY(cuda_status(cudaMemcpyFromSymbol(&v, g_dense_status, sizeof(v)), "nglod_dense_status: read"));
+    NGLOD_TRY(cuda_status(cudaMemcpyToSymbol(g_dense_status, &zero, sizeof(zero)), "nglod_dense_status: reset"));
+    *status_out = v;
+    return NGLOD_OK;
+}
+
+void nglod::set_f32tc_wait_polls(uint32_t polls) { g_f32tc_wait_polls = polls; }
 
 namespace {
 struct F32HostCtx {

@@ -16,12 +16,14 @@
 //      coarsest volumes (5^3 and 9^3 vertices at base_lod 2) are accumulated
 //      in shared memory per block and flushed once; finer ones use
 //      red.global.add.v4.f32.
+#include <cuda.h>
 #include <cuda_bf16.h>
 
 #include <mutex>
 
 #include "dense_common.cuh"
 #include "tc_common.cuh"
+#include "tf32_tile.cuh"
 
 namespace nglod {
 
@@ -112,20 +114,6 @@ constexpr float kNearZero = 1e-5f;
 static_assert(kTileBytes % 1024 == 0 && kBar % 8 == 0, "shared layout alignment");
 }  // namespace fwdtc
 
-// Byte offset of 32-bit element (row, k) in a K-major tile with kc
-// 16-byte core-matrix columns.
-__host__ __device__ constexpr uint32_t tile_offset32(int row, int k, int kc) {
-    return (uint32_t)(((row / 8) * kc + k / 4) * 128 + (row % 8) * 16 + (k % 4) * 4);
-}
-
-__device__ __forceinline__ float tf32_big(float x) { return __uint_as_float(__float_as_uint(x) & 0xFFFFE000u); }
-
-__device__ __forceinline__ void store_split4(uint8_t *big, uint8_t *small, uint32_t off, float4 v) {
-    const float4 b = make_float4(tf32_big(v.x), tf32_big(v.y), tf32_big(v.z), tf32_big(v.w));
-    *reinterpret_cast<float4 *>(big + off) = b;
-    *reinterpret_cast<float4 *>(small + off) = make_float4(v.x - b.x, v.y - b.y, v.z - b.z, v.w - b.w);
-}
-
 // Hidden unit j's pre-activation for IN row r, in float32 with
 // decode_f32's order (inputs x y z, features, 1; products of even and odd
 // float4 groups summed apart, then added).  The row's values are big + small
@@ -153,15 +141,6 @@ __device__ __forceinline__ float pre_f32(const uint8_t *smem, const float *__res
             a0 = t;
     }
     return a0 + a1;
-}
-
-__device__ __forceinline__ void mma_tf32(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "setp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d),
-        "l"(a), "l"(b), "r"(idesc), "r"(acc)
-        : "memory");
 }
 
 __global__ void __launch_bounds__(fwdtc::kTP, 2)
@@ -1285,26 +1264,71 @@ constexpr size_t kNoAllocScratchFloats = (size_t)4 << 20;  // 16 MiB of float32
 
 static __device__ __align__(256) float g_bwd_noalloc_scratch[kNoAllocScratchFloats];
 
-constexpr int kNoAllocMaxDevices = 64;
-static float *g_bwd_noalloc_addr[kNoAllocMaxDevices] = {nullptr};
+// The array has one instance per CUDA context that loads this module, at
+// that context's address.  The address is cached per context, keyed by the
+// CUcontext handle (read through the runtime's driver entry point, so the
+// library needs no link to the driver).  Outside stream capture every call
+// looks the address up again with cudaGetSymbolAddress and refreshes the
+// cache, so a context destroyed and created again at the same handle
+// (cudaDeviceReset, cuCtxDestroy + cuCtxCreate) is picked up by the next
+// call.  A call made while its stream is capturing uses the cache only and
+// fails if the current context has none, so the first call in every context
+// -- and the first call after a reset -- must come before any capture.
+constexpr int kNoAllocMaxContexts = 64;
+struct NoAllocSlot {
+    CUcontext ctx;
+    float *addr;
+};
+static NoAllocSlot g_bwd_noalloc_slots[kNoAllocMaxContexts] = {};
 static std::mutex g_bwd_noalloc_mutex;
 
-// Device address of the array on the current device, looked up on the first
-// call made on that device (the symbol's host-side name is not a device
-// address and must never be passed to a kernel).
-static int noalloc_scratch_address(float **out) {
-    int dev = -1;
-    NGLOD_TRY(cuda_status(cudaGetDevice(&dev), "nglod_sdf_bwd_noalloc: cudaGetDevice"));
-    NGLOD_REQUIRE(dev >= 0 && dev < kNoAllocMaxDevices, NGLOD_ERR_UNSUPPORTED,
-                  "nglod_sdf_bwd_noalloc: device %d beyond the %d supported", dev, kNoAllocMaxDevices);
+using CtxGetCurrentFn = CUresult (*)(CUcontext *);
+
+static int current_context(CUcontext *ctx) {
+    static CtxGetCurrentFn fn = nullptr;
+    if (fn == nullptr) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        NGLOD_TRY(cuda_status(cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q),
+                              "nglod_sdf_bwd_noalloc: cudaGetDriverEntryPointByVersion"));
+        NGLOD_REQUIRE(q == cudaDriverEntryPointSuccess && p != nullptr, NGLOD_ERR_CUDA,
+                      "nglod_sdf_bwd_noalloc: cuCtxGetCurrent not found in the driver");
+        fn = reinterpret_cast<CtxGetCurrentFn>(p);
+    }
+    *ctx = nullptr;
+    NGLOD_REQUIRE(fn(ctx) == CUDA_SUCCESS && *ctx != nullptr, NGLOD_ERR_CUDA,
+                  "nglod_sdf_bwd_noalloc: no current CUDA context");
+    return NGLOD_OK;
+}
+
+// Device address of the array in the current context (the symbol's host-side
+// name is not a device address and must never be passed to a kernel).
+static int noalloc_scratch_address(cudaStream_t stream, float **out) {
+    // a runtime call first: it makes the current device's context current
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    NGLOD_TRY(cuda_status(cudaStreamIsCapturing(stream, &cs), "nglod_sdf_bwd_noalloc: cudaStreamIsCapturing"));
+    CUcontext ctx = nullptr;
+    NGLOD_TRY(current_context(&ctx));
     std::lock_guard<std::mutex> lock(g_bwd_noalloc_mutex);
-    if (g_bwd_noalloc_addr[dev] == nullptr) {
+    int slot = -1, free_slot = -1;
+    for (int i = 0; i < kNoAllocMaxContexts; ++i) {
+        if (g_bwd_noalloc_slots[i].ctx == ctx) slot = i;
+        if (g_bwd_noalloc_slots[i].ctx == nullptr && free_slot < 0) free_slot = i;
+    }
+    if (cs == cudaStreamCaptureStatusNone) {
         void *p = nullptr;
         NGLOD_TRY(cuda_status(cudaGetSymbolAddress(&p, g_bwd_noalloc_scratch),
                               "nglod_sdf_bwd_noalloc: cudaGetSymbolAddress"));
-        g_bwd_noalloc_addr[dev] = static_cast<float *>(p);
+        if (slot < 0) slot = free_slot;
+        NGLOD_REQUIRE(slot >= 0, NGLOD_ERR_UNSUPPORTED, "nglod_sdf_bwd_noalloc: more than %d CUDA contexts",
+                      kNoAllocMaxContexts);
+        g_bwd_noalloc_slots[slot] = {ctx, static_cast<float *>(p)};
+    } else {
+        NGLOD_REQUIRE(slot >= 0, NGLOD_ERR_INVALID,
+                      "nglod_sdf_bwd_noalloc: first call in this CUDA context made during stream capture; "
+                      "call it once outside capture first");
     }
-    *out = g_bwd_noalloc_addr[dev];
+    *out = g_bwd_noalloc_slots[slot].addr;
     return NGLOD_OK;
 }
 
@@ -1330,7 +1354,7 @@ extern "C" int nglod_sdf_bwd_noalloc(const nglod_dense_model *model, const float
                   kNoAllocScratchFloats / per_point);
     if (n == 0) return NGLOD_OK;
     float *scratch = nullptr;
-    NGLOD_TRY(noalloc_scratch_address(&scratch));
+    NGLOD_TRY(noalloc_scratch_address((cudaStream_t)stream, &scratch));
     return nglod_sdf_bwd(model, x, n, lod_mask, grad_preds, feats, relu_masks, scratch, grads, grad_x, stream);
 }
 

@@ -14,6 +14,8 @@ implements outside the hot path (positional / Fourier encoding,
 ``pos_invariant``, ``joint_decoder``, ``interpolate`` -- whose reference path
 raises NameError at OctreeSDF.py:138) raise NotImplementedError.
 """
+import ctypes
+
 import torch
 import torch.nn as nn
 
@@ -124,10 +126,11 @@ class OctreeSDF(nn.Module):
         Returns [N, 1] at ``lod`` (0 <= lod < num_lods); otherwise the finest
         prediction, or the list of every LOD's [N, 1] with ``return_lst``.
         Differentiable in the features and decoder weights when autograd
-        needs it.  That form runs the hidden-128 decoders as split-TF32
-        products on tensor cores: its predictions differ from the float32
-        inference kernels' by rounding (about 2^-21 relative), and its ReLU
-        decisions near zero are taken in float32.
+        needs it.  Both forms gather and sum the features in float32 and, at
+        hidden width 128, run the decoder's first layer on the tensor cores as
+        split-TF32 products (relative error about 2^-21, float32's own size);
+        the training form takes its ReLU decisions near zero in float32.
+        ``check_status()`` reports a bounded tensor-core wait that gave up.
         """
         if lod is None:
             lod = self.lod
@@ -203,8 +206,18 @@ class OctreeSDF(nn.Module):
         m._keep = keep
         return m
 
-    def _sdf_infer(self, x, lod, all_lods):
-        """Forward kernel without autograd: [N, 1], or [num_lods] list of [N, 1]."""
+    def check_status(self):
+        """Raises if a bounded tensor-core wait of an inference call since the
+        last check gave up (nglod_dense_status; reading it synchronises)."""
+        st = ctypes.c_int32(0)
+        _lib.check(_lib.load().nglod_dense_status(ctypes.byref(st)), "nglod_dense_status")
+        if st.value != 0:
+            raise RuntimeError("nglod_sdf_fwd: a bounded tensor-core wait timed out")
+
+    def _sdf_infer(self, x, lod, all_lods, simt=False):
+        """Forward kernel without autograd: [N, 1], or [num_lods] list of [N, 1].
+        simt: the per-thread float32 decoder even where the tensor-core form
+        applies (nglod_sdf_fwd_simt)."""
         _lib.require_cuda(x, self.features[0].fm)
         if x.dim() != 2 or x.shape[1] != 3:
             raise NotImplementedError("OctreeSDF.sdf: only [N, 3] query points are supported")
@@ -215,6 +228,7 @@ class OctreeSDF(nn.Module):
             out = torch.empty(self.num_lods, n, 1, device=x.device, dtype=torch.float32)
         else:
             out = torch.empty(n, 1, device=x.device, dtype=torch.float32)
-        _lib.check(_lib.load().nglod_sdf_fwd(m, _lib.ptr(x), n, -1 if lod is None else lod, 1 if all_lods else 0,
-                                             _lib.ptr(out), _lib.stream_ptr(x.device)), "nglod_sdf_fwd")
+        fn = _lib.load().nglod_sdf_fwd_simt if simt else _lib.load().nglod_sdf_fwd
+        _lib.check(fn(m, _lib.ptr(x), n, -1 if lod is None else lod, 1 if all_lods else 0, _lib.ptr(out),
+                      _lib.stream_ptr(x.device)), "nglod_sdf_fwd")
         return list(out.unbind(0)) if all_lods else out

@@ -196,3 +196,67 @@ def test_frame_size_traces_vs_oracle_on_sampled_rays(cuda):
     assert (hb == h6).mean() >= 0.99
     both = hb & h6
     assert np.abs(b16.depth.cpu().numpy()[pick][both, 0] - t6[both, 0]).mean() <= 1e-3
+
+
+@pytest.fixture(scope="module")
+def full_net(cuda):
+    """The full architecture (5 LODs, 5^3..65^3 volumes, C=32, H=128) holding
+    the sphere-union SDF, and 262,144 query points of the headline's
+    distribution."""
+    c, r = synthetic.sphere_union(1)
+    torch.manual_seed(0)
+    net = ng.OctreeSDF(default_args(num_lods=5, base_lod=2))
+    init_from_sdf(net, lambda p: torch.from_numpy(synthetic.sphere_union_sdf(p.numpy(), c, r)), noise=1e-3, seed=2)
+    x = synthetic.near_surface_query(262_144, c, r, seed=1)
+    return net.to(cuda).eval(), x.to(cuda)
+
+
+def _simt(net, x, lod):
+    from nglod_gb300 import _lib
+    out = torch.empty(x.shape[0], 1, device=x.device)
+    _lib.check(_lib.load().nglod_sdf_fwd_simt(net.dense_model(), _lib.ptr(x), x.shape[0], lod, 0, _lib.ptr(out),
+                                              _lib.stream_ptr(x.device)), "nglod_sdf_fwd_simt")
+    return out
+
+
+@pytest.mark.parametrize("lod", [0, 2, 4])
+def test_tensor_core_f32_query_within_float32_bounds(full_net, lod):
+    """The float32 query's tensor-core form (split-TF32 decoder) against
+    float64 and against the per-thread float32 decoder on 262,144 points: both
+    forms stay within 1e-5 of float64, and within 2e-6 of each other."""
+    net, x = full_net
+    with torch.no_grad():
+        tc = net.sdf(x, lod=lod)
+    net.check_status()
+    simt = _simt(net, x, lod)
+    m64 = oracle_model(net, np.float64)
+    want = dense.sdf(m64, x.cpu().numpy().astype(np.float64), lod=lod)
+    e_tc = np.abs(tc.cpu().numpy().astype(np.float64) - want).max()
+    e_simt = np.abs(simt.cpu().numpy().astype(np.float64) - want).max()
+    assert e_tc < SDF_TOL and e_simt < SDF_TOL, (e_tc, e_simt)
+    assert (tc - simt).abs().max().item() < 2e-6
+
+
+def test_tensor_core_f32_wait_timeout_reports_status_and_recovers(full_net):
+    """The error path of the float32 query's bounded tensor-core wait,
+    without a GPU fault: with the wait cut to one non-blocking test the call
+    reports a timeout through nglod_dense_status, and the next call with the
+    default bound gives the same values as before."""
+    from nglod_gb300 import _lib
+    net, x = full_net
+    lib = _lib.load()
+    with torch.no_grad():
+        good = net.sdf(x, lod=4)
+    net.check_status()
+    try:
+        _lib.check(lib.nglod_debug_mma_wait_polls(0), "nglod_debug_mma_wait_polls")
+        with torch.no_grad():
+            net.sdf(x, lod=4)
+        with pytest.raises(RuntimeError, match="timed out"):
+            net.check_status()
+    finally:
+        _lib.check(lib.nglod_debug_mma_wait_polls(-1), "nglod_debug_mma_wait_polls")
+    with torch.no_grad():
+        again = net.sdf(x, lod=4)
+    net.check_status()
+    assert torch.equal(again, good)

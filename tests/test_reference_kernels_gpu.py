@@ -119,6 +119,10 @@ def test_spc_raytrace_bit_exact_with_reference_kernels_at_frame_size(ref, cuda, 
     assert want.shape[0] > 1_000_000
     assert got.shape == want.shape
     assert torch.equal(got, want)
+    # first-nugget flags of the frame (d_MarkUniqueRays, sdfRenderer.cu:108-120)
+    first = spc.mark_first(got)
+    assert torch.equal(first, ref.mark_unique_rays(want))
+    assert int(first.sum()) == int(torch.unique(want[:, 0]).numel())
 
 
 def test_generate_rays_bit_exact_with_reference_kernel(ref, cuda):

@@ -71,6 +71,11 @@ def _run(net, x, m, feats, relu, gp, mask, noalloc):
                                _lib.ptr(scratch), g, _lib.ptr(gx), _lib.stream_ptr(dev))
     _lib.check(st, "nglod_sdf_bwd_noalloc" if noalloc else "nglod_sdf_bwd")
     torch.cuda.synchronize()
+    # a bounded tensor-core wait that gave up would leave the gradients
+    # incomplete: report that as such, not as a parity mismatch
+    status = ctypes.c_int32(-1)
+    _lib.check(lib.nglod_train_status(ctypes.byref(status)), "nglod_train_status")
+    assert status.value == 0, "a tensor-core wait of the backward gave up"
     bufs["x"] = gx
     return {k: v.cpu().numpy() for k, v in bufs.items()}
 
