@@ -83,9 +83,16 @@ TRAIN_BATCH = 524_288
 # HBM: 12 B point in + 4 B distance out (volumes once per launch);
 # gathered corner bytes: 8 corners x 32 channels x 4 B per LOD;
 # FLOP: 2 per corner-channel of the trilinear sums, 2*(35*128 + 128) for the
-# hidden layer with its bias, 2*128 for the output layer.
+# hidden layer with its bias, 2*128 for the output layer (F32_FLOP, the
+# per-thread decoder's count).  The tensor-core form runs the hidden layer's
+# 32 x 128 feature product as three TF32 products (F32_TC_FLOP on the tensor
+# pipe) and the rest on the float32 pipe (F32_SIMT_FLOP: the trilinear sums
+# and, per hidden unit, x y z and bias terms, ReLU and the output FMA).
 F32_GATHER_BYTES = (LOD + 1) * 8 * 32 * 4
 F32_FLOP = (LOD + 1) * 8 * 32 * 2 + 2 * (35 * 128 + 128) + 2 * 128
+F32_TC_FLOP = 3 * 2 * 32 * 128
+F32_SIMT_FLOP = (LOD + 1) * 8 * 32 * 2 + 128 * (2 * 4 + 2)
+TF32_NOMINAL_TFLOPS = 1100.0
 
 # DRAM traffic of single ncu captures of the headline kernels on this
 # workload (dram__bytes_read.sum + dram__bytes_write.sum of one launch), with
@@ -311,27 +318,32 @@ def fma_peak(dev, reps=10):
 
 
 def f32_roofline(net, sec, points, dev, line_peak=None, fma_tflops=None):
-    """Roofline of sdf_fwd_f32_kernel at lod 4 over `points` queries."""
+    """Roofline of sdf_fwd_f32_tc_kernel (the float32 query at hidden width
+    128) at lod 4 over `points` queries."""
     pk = peaks()
     grid_bytes = sum(fv.fm.numel() * 4 for fv in net.features)
     if line_peak is None:
         line_peak = line_read_peak(dev, grid_bytes)
     if fma_tflops is None:
         fma_tflops = fma_peak(dev)
-    traffic, tnote = ncu_traffic("sdf_fwd_f32_kernel", points)
+    traffic, tnote = ncu_traffic("sdf_fwd_f32_tc_kernel", points)
     terms = {
         "gather_l2": (points * F32_GATHER_BYTES, line_peak, "GB/s",
                       "measured live: random whole 128-byte lines of an L2-resident buffer the size of the "
                       "volumes (nglod_measure_line_reads)"),
         "hbm": (points * 16 + grid_bytes, pk["hbm_gbs"], "GB/s", f"{pk['source']} hbm_gbs (burst copy)"),
-        "fp32_pipe": (points * F32_FLOP, fma_tflops, "TFLOP/s",
+        "fp32_pipe": (points * F32_SIMT_FLOP, fma_tflops, "TFLOP/s",
                       "measured live: float32 FMA chains at full occupancy (nglod_measure_fma)"),
+        "tensor": (points * F32_TC_FLOP, TF32_NOMINAL_TFLOPS, "TFLOP/s",
+                   "nominal dense TF32 (no measured TF32 figure on this pool)"),
     }
-    return roofline("sdf_fwd_f32_kernel", sec, terms,
-                    {"hbm_bytes": 16, "gathered_bytes": F32_GATHER_BYTES, "fp32_flop": F32_FLOP},
+    return roofline("sdf_fwd_f32_tc_kernel", sec, terms,
+                    {"hbm_bytes": 16, "gathered_bytes": F32_GATHER_BYTES, "fp32_pipe_flop": F32_SIMT_FLOP,
+                     "tf32_tensor_flop": F32_TC_FLOP, "algorithmic_fp32_flop": F32_FLOP},
                     points, traffic, tnote,
                     note="one launch reads each point once and the 40.5 MB of float32 volumes from HBM; the "
-                         "corner gathers (5,120 B per query, whole 128-byte vertex lines) are served by L2/L1")
+                         "corner gathers (5,120 B per query, whole 128-byte vertex lines) are served by L2/L1; "
+                         "the decoder's feature product runs as three TF32 products on tcgen05")
 
 
 def run_ours(args):

@@ -76,16 +76,29 @@ constexpr int kThreads = kTP * kTiles;        // 256
 constexpr int kH = 128;                       // hidden units (UMMA N)
 constexpr int kK = 32;                        // feature channels along K
 constexpr int kKC = kK / 4;                   // 16-byte core-matrix columns
+// Point tiles (A) put their K-adjacent core matrices 144 B apart instead of
+// 128 B (the descriptor's LBO): the eight lanes of a quarter warp store one
+// row's eight 16-byte pieces, which then fall in eight different bank
+// groups (at 128 B they would all share four banks).  The weight tile (B) is
+// written once per block and keeps the dense layout.
+constexpr uint32_t kLboA = 144, kSboA = kKC * kLboA;  // 1152 B per 8-row group
+constexpr uint32_t kTileA = (kTP / 8) * kSboA;        // 18 KB
 constexpr uint32_t kTile = kTP * kK * 4;      // 16 KB
-constexpr size_t kA = 0;                      // tile h: big at kA + 2 h kTile, small after it
-constexpr size_t kW = 2 * kTiles * kTile;     // weights: big, then small
+constexpr size_t kA = 0;                      // tile h: big at kA + 2 h kTileA, small after it
+constexpr size_t kW = 2 * kTiles * kTileA;    // weights: big, then small
 constexpr size_t kU = kW + 2 * kTile;         // (w0[j][0..2], b0[j]) float4 [kH]
 constexpr size_t kW1 = kU + kH * 16;          // w1 [kH]
 constexpr size_t kBar = kW1 + kH * 4;
 constexpr size_t kSlot = kBar + 8, kAbort = kSlot + 4;
 constexpr size_t kSmem = kAbort + 12;
 constexpr uint32_t kCols = kTiles * kH;       // TMEM columns per block
-static_assert(kTile % 1024 == 0 && kU % 16 == 0 && kBar % 8 == 0, "shared layout alignment");
+static_assert(kTile % 1024 == 0 && kTileA % 128 == 0 && kW % 1024 == 0 && kU % 16 == 0 && kBar % 8 == 0,
+              "shared layout alignment");
+
+// Byte offset of element (row, k) in a point tile.
+__host__ __device__ constexpr uint32_t a_offset(int row, int k) {
+    return (uint32_t)((row / 8) * kSboA + (k / 4) * kLboA + (row % 8) * 16 + (k % 4) * 4);
+}
 static_assert(2 * kSmem <= 227 * 1024, "two blocks per SM");
 }  // namespace f32tc
 
@@ -135,8 +148,8 @@ __global__ void __launch_bounds__(f32tc::kThreads, 2)
     const uint32_t tmem = *slot;
     const uint32_t sbase = tc::smem_addr(sm);
     constexpr uint32_t idesc = idesc_tf32_f32(kTP, kH);
-    uint8_t *abig = sm + kA + (size_t)2 * half * kTile;
-    uint8_t *asmall = abig + kTile;
+    uint8_t *abig = sm + kA + (size_t)2 * half * kTileA;
+    uint8_t *asmall = abig + kTileA;
     const uint32_t taddr = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(half * kH);
     uint32_t phase = 0;
 
@@ -157,7 +170,7 @@ __global__ void __launch_bounds__(f32tc::kThreads, 2)
             gather_warp_add_f32(static_cast<const float *>(m.grid[l]), volume_side(m, l), px, py, pz, lane, acc);
 #pragma unroll
         for (int p = 0; p < 8; ++p)
-            store_split4(abig, asmall, tile_offset32(quad * 32 + 4 * p + (lane >> 3), 4 * (lane & 7), kKC), acc[p]);
+            store_split4(abig, asmall, a_offset(quad * 32 + 4 * p + (lane >> 3), 4 * (lane & 7)), acc[p]);
         tc::fence_proxy_async_smem();
         tc::fence_before_sync();
         __syncthreads();
@@ -168,14 +181,15 @@ __global__ void __launch_bounds__(f32tc::kThreads, 2)
             const uint64_t ws = tc::smem_desc(sbase + (uint32_t)(kW + kTile), 128, kKC * 128);
 #pragma unroll
             for (int h = 0; h < kTiles; ++h) {
-                const uint64_t ab = tc::smem_desc(sbase + (uint32_t)(kA + 2 * h * kTile), 128, kKC * 128);
-                const uint64_t as = tc::smem_desc(sbase + (uint32_t)(kA + (2 * h + 1) * kTile), 128, kKC * 128);
+                const uint64_t ab = tc::smem_desc(sbase + (uint32_t)(kA + 2 * h * kTileA), kLboA, kSboA);
+                const uint64_t as = tc::smem_desc(sbase + (uint32_t)(kA + (2 * h + 1) * kTileA), kLboA, kSboA);
 #pragma unroll
                 for (int t = 0; t < 3; ++t)
 #pragma unroll
                     for (int ks = 0; ks < kK / 8; ++ks) {
-                        const uint64_t step = (uint64_t)((ks * 256) >> 4);  // 8 tf32 of K: two core matrices
-                        mma_tf32(tmem + (uint32_t)(h * kH), (t == 2 ? as : ab) + step, (t == 1 ? ws : wb) + step,
+                        // 8 tf32 of K: two core matrices of each operand
+                        const uint64_t sa = (uint64_t)((ks * 2 * kLboA) >> 4), sw = (uint64_t)((ks * 256) >> 4);
+                        mma_tf32(tmem + (uint32_t)(h * kH), (t == 2 ? as : ab) + sa, (t == 1 ? ws : wb) + sw,
                                  idesc, (t > 0 || ks > 0) ? 1u : 0u);
                     }
             }

@@ -50,13 +50,15 @@ __device__ __forceinline__ void stage_decoder(float4 *dst, const nglod_dense_mod
 // channel, then added to the running sum.  The far corner index is clamped
 // to s - 1 where u = s - 1; its weight is then exactly 0, as when PyTorch
 // skips the out-of-range corner.
-// Cooperative loads: each lane computes its own point's corner set (vertex
-// index of corner 0, which neighbours are not clamped, the eight weights);
-// in pass p the eight lanes 8j .. 8j + 7 load the corners of point 4p + j,
-// one float4 (channels 4 (lane % 8) .. +3) each, fetching the corner set by
-// shuffles, so a load instruction reads four whole 128-byte vertices instead
-// of 16 bytes of 32 different ones.  acc[p] += this lane's four channels of
-// point 4p + lane / 8.
+// Cooperative loads: in pass p the eight lanes 8j .. 8j + 7 load the
+// corners of point 4p + j, one float4 (channels 4 (lane % 8) .. +3) each, so
+// a load instruction reads four whole 128-byte vertices instead of 16 bytes
+// of 32 different ones.  Each lane computes its own point's clamped grid
+// coordinates; the loading lanes receive them by three shuffles and derive
+// the corner offsets and weights themselves (shuffling the corner index and
+// the eight weights instead takes nine shuffles, which load the shared-memory
+// crossbar the tensor-core kernels also use).  acc[p] += this lane's four
+// channels of point 4p + lane / 8.
 __device__ __forceinline__ void gather_warp_add_f32(const float *__restrict__ g, int s, float px, float py, float pz,
                                                     int lane, float4 (&acc)[8]) {
     const unsigned FULL = 0xffffffffu;
@@ -67,36 +69,33 @@ __device__ __forceinline__ void gather_warp_add_f32(const float *__restrict__ g,
     ix = fminf(sm1, fmaxf(ix, 0.f));
     iy = fminf(sm1, fmaxf(iy, 0.f));
     iz = fminf(sm1, fmaxf(iz, 0.f));
-    const float x0 = floorf(ix), y0 = floorf(iy), z0 = floorf(iz);
-    const float wx1 = ix - x0, wx0 = (x0 + 1.f) - ix;
-    const float wy1 = iy - y0, wy0 = (y0 + 1.f) - iy;
-    const float wz1 = iz - z0, wz0 = (z0 + 1.f) - iz;
-    const int xi = (int)x0, yi = (int)y0, zi = (int)z0;
-    // vertex index < 513^3 < 2^28; bits 28..30: x / y / z neighbour not clamped
-    const uint32_t pk = (uint32_t)((zi * s + yi) * s + xi) | ((uint32_t)(xi + 1 < s) << 28) |
-                        ((uint32_t)(yi + 1 < s) << 29) | ((uint32_t)(zi + 1 < s) << 30);
-    float w[8];
-    w[0] = wx0 * wy0 * wz0;
-    w[1] = wx1 * wy0 * wz0;
-    w[2] = wx0 * wy1 * wz0;
-    w[3] = wx1 * wy1 * wz0;
-    w[4] = wx0 * wy0 * wz1;
-    w[5] = wx1 * wy0 * wz1;
-    w[6] = wx0 * wy1 * wz1;
-    w[7] = wx1 * wy1 * wz1;
     const float4 *g4 = reinterpret_cast<const float4 *>(g) + (lane & 7);  // 8 float4 per vertex
     const int sy = s * 8, sz = s * sy;
 #pragma unroll
     for (int p = 0; p < 8; ++p) {
         const int src = 4 * p + (lane >> 3);
-        const uint32_t q = __shfl_sync(FULL, pk, src);
+        const float qx = __shfl_sync(FULL, ix, src);
+        const float qy = __shfl_sync(FULL, iy, src);
+        const float qz = __shfl_sync(FULL, iz, src);
+        const float x0 = floorf(qx), y0 = floorf(qy), z0 = floorf(qz);
+        const float wx1 = qx - x0, wx0 = (x0 + 1.f) - qx;
+        const float wy1 = qy - y0, wy0 = (y0 + 1.f) - qy;
+        const float wz1 = qz - z0, wz0 = (z0 + 1.f) - qz;
+        const int xi = (int)x0, yi = (int)y0, zi = (int)z0;
         float ws[8];
-#pragma unroll
-        for (int k = 0; k < 8; ++k) ws[k] = __shfl_sync(FULL, w[k], src);
-        const int o0 = (int)(q & 0x0FFFFFFFu) * 8;
-        const int ox = ((q >> 28) & 1u) ? 8 : 0;
-        const int oy = ((q >> 29) & 1u) ? sy : 0;
-        const int oz = ((q >> 30) & 1u) ? sz : 0;
+        ws[0] = wx0 * wy0 * wz0;
+        ws[1] = wx1 * wy0 * wz0;
+        ws[2] = wx0 * wy1 * wz0;
+        ws[3] = wx1 * wy1 * wz0;
+        ws[4] = wx0 * wy0 * wz1;
+        ws[5] = wx1 * wy0 * wz1;
+        ws[6] = wx0 * wy1 * wz1;
+        ws[7] = wx1 * wy1 * wz1;
+        // vertex index < 513^3 < 2^28, float4 offsets < 2^31
+        const int o0 = ((zi * s + yi) * s + xi) * 8;
+        const int ox = xi + 1 < s ? 8 : 0;
+        const int oy = yi + 1 < s ? sy : 0;
+        const int oz = zi + 1 < s ? sz : 0;
         const int o[8] = {o0, o0 + ox, o0 + oy, o0 + oy + ox, o0 + oz, o0 + oz + ox, o0 + oz + oy, o0 + oz + oy + ox};
         float4 v[8];
 #pragma unroll

@@ -15,6 +15,15 @@ from tests.helpers import oracle_model
 
 pytestmark = pytest.mark.gpu
 
+# BF16 error bounds against the FP64 oracle, per LOD 0..4, about twice the
+# errors measured on the GB300 (analytic-init network with noise 1e-2,
+# 65,536 near-surface points): per-LOD volumes max 6.2e-3 / mean 3.6e-4 at
+# LOD 0 down to 5.3e-3 / 3.2e-4; LOD-summed volumes max 7.2e-3 / mean 4.3e-4.
+PER_LOD_MAX = (1.3e-2, 1.2e-2, 1.1e-2, 1.1e-2, 1.1e-2)
+PER_LOD_MEAN = (7.5e-4, 7.0e-4, 6.6e-4, 6.6e-4, 6.6e-4)
+SUMMED_MAX = (1.45e-2, 1.3e-2, 1.4e-2, 1.4e-2, 1.3e-2)
+SUMMED_MEAN = (8.6e-4, 6.8e-4, 6.2e-4, 7.2e-4, 7.6e-4)
+
 
 def _bf16(a):
     """Round float32 array to bfloat16 (round to nearest even), returned as float32."""
@@ -79,7 +88,7 @@ def test_bf16_matches_emulation_and_reports_error(nets):
         ref = dense.sdf(m64, x.numpy().astype(np.float64), lod=lod)
         err = np.abs(got - ref)
         report[lod] = (err.max(), err.mean())
-        assert err.max() < 2e-2 and err.mean() < 2e-3, (lod, err.max(), err.mean())
+        assert err.max() < PER_LOD_MAX[lod] and err.mean() < PER_LOD_MEAN[lod], (lod, err.max(), err.mean())
     bnet.check_status()
     print("bf16 error vs fp64 oracle per lod (max, mean):", report)
 
@@ -101,7 +110,8 @@ def test_bf16_full_size_against_float32_path(nets):
         ref = net.sdf(x, lod=4)
     assert torch.isfinite(got).all()
     d = (got - ref).abs()
-    assert d.max().item() < 2e-2 and d.mean().item() < 2e-3
+    print(f"bf16 vs float32 on 4M points at lod 4: max {d.max().item():.2e} mean {d.mean().item():.2e}")
+    assert d.max().item() < 2e-2 and d.mean().item() < PER_LOD_MEAN[4]
     bnet.check_status()
     assert bnet.sdf(torch.zeros(0, 3, device=dev)).shape == (0, 1)
 
@@ -260,7 +270,7 @@ def test_summed_form_matches_emulation_and_fp64(nets, summed, n):
         np.testing.assert_allclose(got, emulate_summed(m64, x.numpy(), lod), atol=2e-4, rtol=0)
         err = np.abs(got - dense.sdf(m64, x.numpy().astype(np.float64), lod=lod))
         report[lod] = (err.max(), err.mean())
-        assert err.max() < 2e-2 and err.mean() < 2e-3, (lod, err.max(), err.mean())
+        assert err.max() < SUMMED_MAX[lod] and err.mean() < SUMMED_MEAN[lod], (lod, err.max(), err.mean())
     summed.check_status()
     print("summed bf16 error vs fp64 oracle per lod (max, mean):", report)
 

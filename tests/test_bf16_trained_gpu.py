@@ -30,9 +30,19 @@ def trained(cuda):
     return net, Bf16OctreeSDF(net), oracle_model(net, np.float64), (c, r)
 
 
+# Bounds per LOD 0..4, about twice the errors measured on the GB300 on
+# 262,144 points (max 2.6e-3 / 1.7e-3 / 8.0e-4 / 1.1e-3 / 1.1e-3, mean at
+# most 2.2e-4).
+TRAINED_MAX = (5.5e-3, 3.5e-3, 1.7e-3, 2.2e-3, 2.2e-3)
+TRAINED_MEAN = (4.5e-4, 3.7e-4, 2.0e-4, 2.0e-4, 2.3e-4)
+
+
 def test_bf16_error_per_lod_vs_fp64_oracle(trained):
+    """Configuration 3's error statement: BF16 and float32 against the FP64
+    oracle per LOD on the trained network, on every 16th of the 4,194,304
+    query points (262,144 points, both halves of the distribution)."""
     net, bnet, m64, (c, r) = trained
-    x = synthetic.near_surface_query(32768, c, r, seed=1)
+    x = synthetic.near_surface_query(4_194_304, c, r, seed=1)[::16].contiguous()
     xd = x.to(net.features[0].fm.device)
     report = {}
     for lod in range(5):
@@ -45,7 +55,7 @@ def test_bf16_error_per_lod_vs_fp64_oracle(trained):
         report[lod] = {"bf16_max": e16.max(), "bf16_mean": e16.mean(), "f32_max": e32.max()}
         # float32 drop-in: the reference's tolerance; BF16: bounded and stated
         assert e32.max() < 1e-5, (lod, e32.max())
-        assert e16.max() < 2e-2 and e16.mean() < 2e-3, (lod, e16.max(), e16.mean())
+        assert e16.max() < TRAINED_MAX[lod] and e16.mean() < TRAINED_MEAN[lod], (lod, e16.max(), e16.mean())
     bnet.check_status()
     print("trained weights, error vs FP64 oracle per LOD:",
           {k: {kk: f"{vv:.2e}" for kk, vv in v.items()} for k, v in report.items()})
