@@ -88,43 +88,56 @@ __global__ void __launch_bounds__(kFwdTrainThreads, 1)
 // ---------------------------------------------------------------------------
 // forward for training, tensor-core form (hidden_dim 128, ReLU masks wanted)
 // ---------------------------------------------------------------------------
-// The decoder's first layer P [128 pts x 128 hid] = IN [pts x 40] . W^T runs
-// on tcgen05 as kind::tf32 products over big / small splits of both
-// operands (x = big + small, big = x with its low 13 mantissa bits cleared;
-// a*b ~ ab*bb + ab*bs + as*bb, relative error about 2^-21, the size of the
-// float32 path's own rounding), accumulated in TMEM; ReLU, the ReLU mask and
-// the 128 -> 1 layer are a float32 epilogue per point.  K order of an IN
-// row: the 32 summed features, x y z, 1 (the b0 column), zeros; W row j:
-// w0[j][3..34], w0[j][0..2], b0[j], zeros.
-// Blocks run LOD by LOD so that each LOD's W tiles are staged once: a
-// block visits the same tiles at every LOD, and the running feature sum of
-// a point is carried through feats (row l-1 is read back by the very lanes
-// that wrote it), which therefore holds every row 0..L.
+// The decoder's first layer, feature part P [128 pts x 128 hid] =
+// F [pts x 32] . W^T, runs on tcgen05 as kind::tf32 products over big / small
+// splits of both operands (tf32_tile.cuh: relative error about 2^-21, the
+// size of the float32 path's own rounding), accumulated in TMEM.  The x y z
+// and bias terms, ReLU, the ReLU mask and the 128 -> 1 layer are a float32
+// epilogue per point.  Units whose pre-activation lies within the split
+// products' error of zero (a few per thousand points) are evaluated again in
+// float32 with the per-thread decoder's order, so that the saved ReLU mask
+// is the float32 path's decision.
+// A block of eight warps handles two 128-point tiles per iteration against
+// one staged weight tile (the layout of sdf_fwd_f32_tc_kernel: warps 0-3
+// fill tile 0, warps 4-7 tile 1; two blocks per SM hold 2 x 256 TMEM
+// columns).  Blocks run LOD by LOD so that each LOD's weights are staged
+// once: a block visits the same points at every LOD, and the running
+// feature sum of a point is carried through feats (row l-1 is read back by
+// the very lanes that wrote it), which therefore holds every row 0..L.
 namespace fwdtc {
-constexpr int kTP = 128, kH = 128, kK = 40, kKC = kK / 4;   // 32-bit core matrices hold 4 elements along K
-constexpr uint32_t kTileBytes = kTP * kK * 4;               // 20 KB
-constexpr size_t kAB = 0, kAS = kTileBytes, kWB = 2 * kTileBytes, kWS = 3 * kTileBytes;
-constexpr size_t kW1 = 4 * kTileBytes;                        // w1 [128] f32
+constexpr int kTP = 128, kTiles = 2, kThreads = kTP * kTiles, kH = 128, kK = 32, kKC = kK / 4;
+// point tiles: K-adjacent core matrices 144 B apart, so that a quarter warp's
+// eight 16-byte stores of one row hit eight bank groups
+constexpr uint32_t kLboA = 144, kSboA = kKC * kLboA, kTileA = (kTP / 8) * kSboA;  // 18 KB
+constexpr uint32_t kTileW = kH * kK * 4;                                          // 16 KB
+constexpr size_t kA = 0, kW = 2 * kTiles * kTileA, kU = kW + 2 * kTileW, kW1 = kU + kH * 16;
 constexpr size_t kBar = kW1 + kH * 4, kSlot = kBar + 8, kAbort = kSlot + 4;
 constexpr size_t kSmem = kAbort + 12;
+constexpr uint32_t kCols = kTiles * kH;
 constexpr uint32_t kPolls = 1u << 22;
 // |P| below which a unit's sign is settled by a float32 evaluation: above the
 // split products' error (about 2^-21 of sum |w x|) for sums up to ~20
 constexpr float kNearZero = 1e-5f;
-static_assert(kTileBytes % 1024 == 0 && kBar % 8 == 0, "shared layout alignment");
+static_assert(kTileA % 128 == 0 && kW % 1024 == 0 && kU % 16 == 0 && kBar % 8 == 0, "shared layout alignment");
+static_assert(2 * kSmem <= 227 * 1024, "two blocks per SM");
+
+__host__ __device__ constexpr uint32_t a_offset(int row, int k) {
+    return (uint32_t)((row / 8) * kSboA + (k / 4) * kLboA + (row % 8) * 16 + (k % 4) * 4);
+}
 }  // namespace fwdtc
 
-// Hidden unit j's pre-activation for IN row r, in float32 with
+// Hidden unit j's pre-activation for point row r of a tile, in float32 with
 // decode_f32's order (inputs x y z, features, 1; products of even and odd
-// float4 groups summed apart, then added).  The row's values are big + small
-// of the IN tiles, which is exact.
-__device__ __forceinline__ float pre_f32(const uint8_t *smem, const float *__restrict__ w0, const float *__restrict__ b0,
-                                         int r, int j) {
+// float4 groups summed apart, then added).  The features are big + small of
+// the tile, which is exact.
+__device__ __noinline__ float pre_f32(const uint8_t *abig, const uint8_t *asmall, int r, float px, float py,
+                                      float pz, const float *__restrict__ w0, const float *__restrict__ b0, int j) {
     using namespace fwdtc;
     auto in_at = [&](int k) -> float {  // decode_f32's input k
-        const int kk = k < 3 ? 32 + k : (k < 35 ? k - 3 : 35);
-        const uint32_t off = tile_offset32(r, kk, kKC);
-        return *reinterpret_cast<const float *>(smem + kAB + off) + *reinterpret_cast<const float *>(smem + kAS + off);
+        if (k < 3) return k == 0 ? px : (k == 1 ? py : pz);
+        if (k == 35) return 1.f;
+        const uint32_t off = a_offset(r, k - 3);
+        return *reinterpret_cast<const float *>(abig + off) + *reinterpret_cast<const float *>(asmall + off);
     };
     float a0 = 0.f, a1 = 0.f;
 #pragma unroll 1
@@ -143,25 +156,21 @@ __device__ __forceinline__ float pre_f32(const uint8_t *smem, const float *__res
     return a0 + a1;
 }
 
-__global__ void __launch_bounds__(fwdtc::kTP, 2)
+__global__ void __launch_bounds__(fwdtc::kThreads, 2)
     sdf_fwd_train_tc_kernel(const nglod_dense_model m, const float *__restrict__ x, int64_t n, int L, uint32_t mask,
                             float *__restrict__ preds, float *__restrict__ feats, uint32_t *__restrict__ relu) {
     using namespace fwdtc;
     extern __shared__ __align__(1024) uint8_t smem_fw[];
-    uint8_t *smem = smem_fw;
-    float *w1s = reinterpret_cast<float *>(smem + kW1);
-    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + kBar);
-    uint32_t *slot = reinterpret_cast<uint32_t *>(smem + kSlot);
-    volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + kAbort);
+    uint8_t *sm = smem_fw;
+    const float4 *su = reinterpret_cast<const float4 *>(sm + kU);
+    const float *w1s = reinterpret_cast<const float *>(sm + kW1);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(sm + kBar);
+    uint32_t *slot = reinterpret_cast<uint32_t *>(sm + kSlot);
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(sm + kAbort);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int half = warp >> 2, quad = warp & 3;
 
-    // K columns 36..39 of the IN rows are always zero
-    for (int r = tid; r < kTP; r += kTP) {
-        const uint32_t off = tile_offset32(r, 36, kKC);
-        *reinterpret_cast<float4 *>(smem + kAB + off) = make_float4(0.f, 0.f, 0.f, 0.f);
-        *reinterpret_cast<float4 *>(smem + kAS + off) = make_float4(0.f, 0.f, 0.f, 0.f);
-    }
-    if (warp == 0) tc::tmem_alloc(slot, kH);
+    if (warp == 0) tc::tmem_alloc(slot, kCols);
     if (tid == 0) {
         tc::mbar_init(bar, 1);
         *abort_flag = 0;
@@ -170,33 +179,37 @@ __global__ void __launch_bounds__(fwdtc::kTP, 2)
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t tmem = *slot;
-    const uint32_t sbase = tc::smem_addr(smem);
-    const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(kH >> 3) << 17) | ((uint32_t)(kTP >> 4) << 24);
-    const uint32_t trow = (uint32_t)(warp * 32) << 16;
+    const uint32_t sbase = tc::smem_addr(sm);
+    constexpr uint32_t idesc = idesc_tf32_f32(kTP, kH);
+    uint8_t *abig = sm + kA + (size_t)2 * half * kTileA;
+    uint8_t *asmall = abig + kTileA;
+    const uint32_t taddr = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(half * kH);
+    const int row = quad * 32 + lane;  // this thread's point row in its tile
     uint32_t phase = 0;
 
 #pragma unroll 1
     for (int l = 0; l <= L && !*abort_flag; ++l) {
         const bool decode = (mask >> l) & 1u;
         if (decode) {
-            // W tiles of this LOD (big / small) and w1
-            for (int u = tid; u < kH * kKC; u += kTP) {
+            // weights of this LOD: feature part split big / small, x y z and b0, w1
+            const float *w0 = m.w0[l];
+            for (int u = tid; u < kH * kKC; u += kThreads) {
                 const int j = u / kKC, kc = u % kKC;
-                float v[4];
-#pragma unroll
-                for (int e = 0; e < 4; ++e) {
-                    const int k = kc * 4 + e;
-                    v[e] = k < 32 ? m.w0[l][j * 35 + 3 + k] : k < 35 ? m.w0[l][j * 35 + (k - 32)] : k == 35 ? m.b0[l][j] : 0.f;
-                }
-                store_split4(smem + kWB, smem + kWS, tile_offset32(j, kc * 4, kKC), make_float4(v[0], v[1], v[2], v[3]));
+                const float *r = w0 + j * 35 + 3 + 4 * kc;
+                store_split4(sm + kW, sm + kW + kTileW, tile_offset32(j, 4 * kc, kKC),
+                             make_float4(r[0], r[1], r[2], r[3]));
             }
-            if (tid < kH) w1s[tid] = m.w1[l][tid];
+            if (tid < kH) {
+                reinterpret_cast<float4 *>(sm + kU)[tid] =
+                    make_float4(w0[tid * 35], w0[tid * 35 + 1], w0[tid * 35 + 2], m.b0[l][tid]);
+                reinterpret_cast<float *>(sm + kW1)[tid] = m.w1[l][tid];
+            }
         }
         const float b1 = decode ? m.b1[l][0] : 0.f;
         const int s = volume_side(m, l);
 #pragma unroll 1
-        for (int64_t tile = blockIdx.x; tile * kTP < n; tile += gridDim.x) {
-            const int64_t base = tile * kTP + warp * 32;
+        for (int64_t q = blockIdx.x; q * kThreads < n; q += gridDim.x) {
+            const int64_t base = q * kThreads + warp * 32;
             const int64_t i = base + lane;
             float px = 0.f, py = 0.f, pz = 0.f;
             if (i < n) {
@@ -210,7 +223,8 @@ __global__ void __launch_bounds__(fwdtc::kTP, 2)
             for (int p = 0; p < 8; ++p) {
                 const int64_t ip = base + 4 * p + (lane >> 3);
                 acc[p] = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (l > 0 && ip < n) acc[p] = reinterpret_cast<const float4 *>(feats + ((int64_t)(l - 1) * n + ip) * kC)[lane & 7];
+                if (l > 0 && ip < n)
+                    acc[p] = reinterpret_cast<const float4 *>(feats + ((int64_t)(l - 1) * n + ip) * kC)[lane & 7];
             }
             gather_warp_add_f32(static_cast<const float *>(m.grid[l]), s, px, py, pz, lane, acc);
 #pragma unroll
@@ -219,29 +233,29 @@ __global__ void __launch_bounds__(fwdtc::kTP, 2)
                 if (ip < n) reinterpret_cast<float4 *>(feats + ((int64_t)l * n + ip) * kC)[lane & 7] = acc[p];
             }
             if (!decode) continue;
-            // IN rows of the warp's 32 points
 #pragma unroll
             for (int p = 0; p < 8; ++p)
-                store_split4(smem + kAB, smem + kAS, tile_offset32(warp * 32 + 4 * p + (lane >> 3), 4 * (lane & 7), kKC),
-                             acc[p]);
-            store_split4(smem + kAB, smem + kAS, tile_offset32(warp * 32 + lane, 32, kKC), make_float4(px, py, pz, 1.f));
+                store_split4(abig, asmall, a_offset(quad * 32 + 4 * p + (lane >> 3), 4 * (lane & 7)), acc[p]);
             tc::fence_proxy_async_smem();
             tc::fence_before_sync();
             __syncthreads();
             if (tid == 0) {
                 tc::fence_after_sync();
-                const uint64_t ab = tc::smem_desc(sbase + (uint32_t)kAB, 128, kKC * 128);
-                const uint64_t as = tc::smem_desc(sbase + (uint32_t)kAS, 128, kKC * 128);
-                const uint64_t wb = tc::smem_desc(sbase + (uint32_t)kWB, 128, kKC * 128);
-                const uint64_t ws = tc::smem_desc(sbase + (uint32_t)kWS, 128, kKC * 128);
+                const uint64_t wb = tc::smem_desc(sbase + (uint32_t)kW, 128, kKC * 128);
+                const uint64_t ws = tc::smem_desc(sbase + (uint32_t)(kW + kTileW), 128, kKC * 128);
 #pragma unroll
-                for (int t = 0; t < 3; ++t)
+                for (int h = 0; h < kTiles; ++h) {
+                    const uint64_t ab = tc::smem_desc(sbase + (uint32_t)(kA + 2 * h * kTileA), kLboA, kSboA);
+                    const uint64_t as = tc::smem_desc(sbase + (uint32_t)(kA + (2 * h + 1) * kTileA), kLboA, kSboA);
 #pragma unroll
-                    for (int ks = 0; ks < kK / 8; ++ks) {
-                        const uint64_t step = (uint64_t)((ks * 256) >> 4);  // 8 tf32 of K = two core matrices
-                        mma_tf32(tmem, (t == 2 ? as : ab) + step, (t == 1 ? ws : wb) + step, idesc,
-                                 (t > 0 || ks > 0) ? 1u : 0u);
-                    }
+                    for (int t = 0; t < 3; ++t)
+#pragma unroll
+                        for (int ks = 0; ks < kK / 8; ++ks) {
+                            const uint64_t sa = (uint64_t)((ks * 2 * kLboA) >> 4), sw = (uint64_t)((ks * 256) >> 4);
+                            mma_tf32(tmem + (uint32_t)(h * kH), (t == 2 ? as : ab) + sa, (t == 1 ? ws : wb) + sw,
+                                     idesc, (t > 0 || ks > 0) ? 1u : 0u);
+                        }
+                }
                 tc::mma_commit(bar);
                 if (!tc::mbar_wait_bounded(bar, phase, kPolls)) {
                     *abort_flag = 1;
@@ -252,27 +266,27 @@ __global__ void __launch_bounds__(fwdtc::kTP, 2)
             if (*abort_flag) break;
             phase ^= 1u;
             tc::fence_after_sync();
-            // epilogue: row 32 warp + lane = point i.  Units whose product is
-            // within its error bound of zero are evaluated again in float32,
-            // so that the ReLU mask is the float32 path's.
+            // epilogue: this thread's point (row quad * 32 + lane of tile half)
             float out = 0.f;
             uint32_t bits[4];
-#pragma unroll
+#pragma unroll 1
             for (int c = 0; c < 4; ++c) {
                 float v[32];
-                tc::tmem_load32(tmem + trow + (uint32_t)(32 * c), v);
+                tc::tmem_load32(taddr + (uint32_t)(32 * c), v);
                 uint32_t b = 0u, near = 0u;
 #pragma unroll
                 for (int e = 0; e < 32; ++e) {
-                    const bool z = fabsf(v[e]) < kNearZero;
+                    const float4 u = su[32 * c + e];
+                    const float zv = fmaf(u.x, px, fmaf(u.y, py, fmaf(u.z, pz, v[e] + u.w)));
+                    const bool z = fabsf(zv) < kNearZero;
                     near |= (uint32_t)z << e;
-                    out = fmaf(w1s[32 * c + e], z ? 0.f : fmaxf(v[e], 0.f), out);
-                    b |= (uint32_t)(v[e] > 0.f && !z) << e;
+                    out = fmaf(w1s[32 * c + e], z ? 0.f : fmaxf(zv, 0.f), out);
+                    b |= (uint32_t)(zv > 0.f && !z) << e;
                 }
                 while (near) {  // rare: a few units per thousand points
                     const int e = __ffs(near) - 1;
                     near &= near - 1u;
-                    const float f = pre_f32(smem, m.w0[l], m.b0[l], warp * 32 + lane, 32 * c + e);
+                    const float f = pre_f32(abig, asmall, row, px, py, pz, m.w0[l], m.b0[l], 32 * c + e);
                     if (f > 0.f) {
                         out = fmaf(w1s[32 * c + e], f, out);
                         b |= 1u << e;
@@ -281,9 +295,9 @@ __global__ void __launch_bounds__(fwdtc::kTP, 2)
                 bits[c] = b;
             }
             if (i < n) {
-                const int64_t row = (int64_t)l * n + i;
-                preds[row] = out + b1;
-                reinterpret_cast<uint4 *>(relu)[row] = make_uint4(bits[0], bits[1], bits[2], bits[3]);
+                const int64_t r = (int64_t)l * n + i;
+                preds[r] = out + b1;
+                reinterpret_cast<uint4 *>(relu)[r] = make_uint4(bits[0], bits[1], bits[2], bits[3]);
             }
             tc::fence_before_sync();
             __syncthreads();
@@ -294,7 +308,7 @@ __global__ void __launch_bounds__(fwdtc::kTP, 2)
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
-    if (warp == 0) tc::tmem_dealloc(tmem, kH);
+    if (warp == 0) tc::tmem_dealloc(tmem, kCols);
 }
 
 // ---------------------------------------------------------------------------
@@ -1116,11 +1130,11 @@ extern "C" int nglod_sdf_fwd_train(const nglod_dense_model *model, const float *
     NGLOD_REQUIRE(aligned(feats, 16), NGLOD_ERR_ALIGN, "feats must be 16-byte aligned");
     NGLOD_REQUIRE(!relu_masks || aligned(relu_masks, 16), NGLOD_ERR_ALIGN, "relu_masks must be 16-byte aligned");
     if (model->hidden_dim == fwdtc::kH && relu_masks) {
-        // tensor-core form: two 128-thread blocks per SM
+        // tensor-core form: two 256-thread blocks per SM
         NGLOD_TRY(prepare_smem(sdf_fwd_train_tc_kernel, fwdtc::kSmem));
-        const int64_t tiles = (n + fwdtc::kTP - 1) / fwdtc::kTP;
+        const int64_t pairs = (n + fwdtc::kThreads - 1) / fwdtc::kThreads;
         const int64_t cap = (int64_t)num_sms() * 2;
-        sdf_fwd_train_tc_kernel<<<(int)(tiles < cap ? tiles : cap), fwdtc::kTP, fwdtc::kSmem,
+        sdf_fwd_train_tc_kernel<<<(int)(pairs < cap ? pairs : cap), fwdtc::kThreads, fwdtc::kSmem,
                                   (cudaStream_t)stream>>>(*model, x, n, L, lod_mask, preds, feats, relu_masks);
         return launch_status("nglod_sdf_fwd_train");
     }
