@@ -880,15 +880,19 @@ __device__ __forceinline__ void red_add_v4(float *addr, float a, float b, float 
 // floats given by soff[l]); the rest go straight to global memory.  A shared
 // vertex takes kSV = 33 floats (32 channels and a pad word).
 //
-// Each warp handles 32 points at a time, cooperatively: the eight lanes
-// 8j .. 8j + 7 of pass p own channels 4 (lane % 8) .. +3 of point 4p + j.
-// A point's gradient G (suffix sum over the mask LODs l >= i of
-// dLoss/d(feature sum l)) is loaded as whole 128-byte rows, and each
-// corner's 32-channel update is one 128-byte vector reduction
+// Each warp handles 32 points at a time, cooperatively, in eight passes of
+// four points: the eight lanes 8j .. 8j + 7 of pass p own channels
+// 4 (lane % 8) .. +3 of point 4p + j.  Within a pass the LODs run from the
+// finest down, so each lane carries one running gradient G (suffix sum over
+// the mask LODs l >= i of dLoss/d(feature sum l)), loaded as whole 128-byte
+// rows; each corner's 32-channel update is one 128-byte vector reduction
 // (red.global.add.v4.f32 from eight lanes) or 32 consecutive shared-memory
-// atomics.  Corner sets come from the point's own lane by shuffles; the
-// weights are formed as (wx * wy) * wz, as in the forward.
+// atomics.  The eight lanes of a point compute its corner set themselves
+// (no shuffles), with the weights formed as (wx * wy) * wz, as in the
+// forward.  The loop body stays small: the fully unrolled form (all passes
+// of a LOD at once) spent most of its stalls on instruction fetch.
 constexpr int kSV = kC + 1;
+constexpr int kScatterThreads = 512;
 struct ScatterArgs {
     BwdArgs a;
     int smem_levels;
@@ -896,7 +900,7 @@ struct ScatterArgs {
 };
 
 template <bool kGradX>
-__global__ void __launch_bounds__(256) sdf_bwd_scatter_kernel(const ScatterArgs s) {
+__global__ void __launch_bounds__(kScatterThreads, 2) sdf_bwd_scatter_kernel(const ScatterArgs s) {
     extern __shared__ float sacc[];
     const BwdArgs &a = s.a;
     const unsigned FULL = 0xffffffffu;
@@ -906,98 +910,79 @@ __global__ void __launch_bounds__(256) sdf_bwd_scatter_kernel(const ScatterArgs 
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, part = lane & 7;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t base = (int64_t)blockIdx.x * blockDim.x + warp * 32; base < a.n; base += stride) {
-        const int64_t i = base + lane;
-        float px = 0.f, py = 0.f, pz = 0.f;
-        if (i < a.n) {
-            px = a.x[3 * i];
-            py = a.x[3 * i + 1];
-            pz = a.x[3 * i + 2];
-        }
-        float4 G[8];
-        float gxv[8][3];
-#pragma unroll
-        for (int p = 0; p < 8; ++p) {
-            G[p] = make_float4(0.f, 0.f, 0.f, 0.f);
-            gxv[p][0] = gxv[p][1] = gxv[p][2] = 0.f;
-        }
+        // four points per pass, eight lanes per point (lane: channels 4 part .. +3)
 #pragma unroll 1
-        for (int l = a.L; l >= 0; --l) {
-            if ((a.mask >> l) & 1u) {
-#pragma unroll
-                for (int p = 0; p < 8; ++p) {
-                    const int64_t ip = base + 4 * p + (lane >> 3);
-                    if (ip < a.n) {
-                        const float4 v = reinterpret_cast<const float4 *>(a.dfeat + ((int64_t)l * a.n + ip) * kC)[part];
-                        G[p].x += v.x;
-                        G[p].y += v.y;
-                        G[p].z += v.z;
-                        G[p].w += v.w;
-                    }
-                }
+        for (int p = 0; p < 8; ++p) {
+            const int64_t ip = base + 4 * p + (lane >> 3);
+            const bool valid = ip < a.n;
+            float px = 0.f, py = 0.f, pz = 0.f;
+            if (valid) {
+                px = a.x[3 * ip];
+                py = a.x[3 * ip + 1];
+                pz = a.x[3 * ip + 2];
             }
-            // this lane's own point: corner set at LOD l
-            const int sd = volume_side(a.m, l);
-            const float sm1 = (float)(sd - 1);
-            const float rx = ((px + 1.f) / 2.f) * sm1;
-            const float ry = ((py + 1.f) / 2.f) * sm1;
-            const float rz = ((pz + 1.f) / 2.f) * sm1;
-            const float ix = fminf(sm1, fmaxf(rx, 0.f));
-            const float iy = fminf(sm1, fmaxf(ry, 0.f));
-            const float iz = fminf(sm1, fmaxf(rz, 0.f));
-            const float x0 = floorf(ix), y0 = floorf(iy), z0 = floorf(iz);
-            const float wv[6] = {(x0 + 1.f) - ix, ix - x0, (y0 + 1.f) - iy, iy - y0, (z0 + 1.f) - iz, iz - z0};
-            const int xi = (int)x0, yi = (int)y0, zi = (int)z0;
-            // vertex index < 2^28; bits 28..30: x / y / z neighbour not clamped
-            // (the clamp flags of dLoss/dx travel in `edge`)
-            const uint32_t pk = (uint32_t)((zi * sd + yi) * sd + xi) | ((uint32_t)(xi + 1 < sd) << 28) |
-                                ((uint32_t)(yi + 1 < sd) << 29) | ((uint32_t)(zi + 1 < sd) << 30);
-            const uint32_t edge = (uint32_t)(rx <= 0.f || rx >= sm1) | ((uint32_t)(ry <= 0.f || ry >= sm1) << 1) |
-                                  ((uint32_t)(rz <= 0.f || rz >= sm1) << 2);
-            const bool in_smem = l < s.smem_levels;
-            float *gbase = in_smem ? sacc + s.soff[l] : a.g.grid[l];
-            const int vstride = in_smem ? kSV : kC;
-            const float4 *fm = reinterpret_cast<const float4 *>(a.m.grid[l]);
-#pragma unroll
-            for (int p = 0; p < 8; ++p) {
-                const int src = 4 * p + (lane >> 3);
-                const uint32_t q = __shfl_sync(FULL, pk, src);
-                float w6[6];
-#pragma unroll
-                for (int k = 0; k < 6; ++k) w6[k] = __shfl_sync(FULL, wv[k], src);
+            float4 G = make_float4(0.f, 0.f, 0.f, 0.f);
+            float gxv[3] = {0.f, 0.f, 0.f};
+#pragma unroll 1
+            for (int l = a.L; l >= 0; --l) {
+                // G: dLoss / d(feature sum of LODs 0..l) = sum of dfeat over decoded LODs >= l
+                if (valid && ((a.mask >> l) & 1u)) {
+                    const float4 v = reinterpret_cast<const float4 *>(a.dfeat + ((int64_t)l * a.n + ip) * kC)[part];
+                    G.x += v.x;
+                    G.y += v.y;
+                    G.z += v.z;
+                    G.w += v.w;
+                }
+                // the point's corner set at LOD l, in every lane of the point
+                const int sd = volume_side(a.m, l);
+                const float sm1 = (float)(sd - 1);
+                const float rx = ((px + 1.f) / 2.f) * sm1;
+                const float ry = ((py + 1.f) / 2.f) * sm1;
+                const float rz = ((pz + 1.f) / 2.f) * sm1;
+                const float ix = fminf(sm1, fmaxf(rx, 0.f));
+                const float iy = fminf(sm1, fmaxf(ry, 0.f));
+                const float iz = fminf(sm1, fmaxf(rz, 0.f));
+                const float x0 = floorf(ix), y0 = floorf(iy), z0 = floorf(iz);
+                const float w6[6] = {(x0 + 1.f) - ix, ix - x0, (y0 + 1.f) - iy, iy - y0, (z0 + 1.f) - iz, iz - z0};
+                const int xi = (int)x0, yi = (int)y0, zi = (int)z0;
                 const float w[8] = {w6[0] * w6[2] * w6[4], w6[1] * w6[2] * w6[4], w6[0] * w6[3] * w6[4],
                                     w6[1] * w6[3] * w6[4], w6[0] * w6[2] * w6[5], w6[1] * w6[2] * w6[5],
                                     w6[0] * w6[3] * w6[5], w6[1] * w6[3] * w6[5]};
-                const int v0 = (int)(q & 0x0FFFFFFFu);
-                const int ox = ((q >> 28) & 1u) ? 1 : 0;
-                const int oy = ((q >> 29) & 1u) ? sd : 0;
-                const int oz = ((q >> 30) & 1u) ? sd * sd : 0;
+                const int v0 = (zi * sd + yi) * sd + xi;
+                const int ox = xi + 1 < sd ? 1 : 0;
+                const int oy = yi + 1 < sd ? sd : 0;
+                const int oz = zi + 1 < sd ? sd * sd : 0;
                 const int vtx[8] = {v0, v0 + ox, v0 + oy, v0 + oy + ox, v0 + oz, v0 + oz + ox, v0 + oz + oy, v0 + oz + oy + ox};
-                const bool valid = base + src < a.n;
                 if (valid) {
+                    if (l < s.smem_levels) {
+                        float *gbase = sacc + s.soff[l] + 4 * part;
 #pragma unroll
-                    for (int k = 0; k < 8; ++k) {
-                        float *dst = gbase + (size_t)vtx[k] * vstride + 4 * part;
-                        if (in_smem) {
-                            atomicAdd(dst, G[p].x * w[k]);
-                            atomicAdd(dst + 1, G[p].y * w[k]);
-                            atomicAdd(dst + 2, G[p].z * w[k]);
-                            atomicAdd(dst + 3, G[p].w * w[k]);
-                        } else {
-                            red_add_v4(dst, G[p].x * w[k], G[p].y * w[k], G[p].z * w[k], G[p].w * w[k]);
+                        for (int k = 0; k < 8; ++k) {
+                            float *dst = gbase + vtx[k] * kSV;
+                            atomicAdd(dst, G.x * w[k]);
+                            atomicAdd(dst + 1, G.y * w[k]);
+                            atomicAdd(dst + 2, G.z * w[k]);
+                            atomicAdd(dst + 3, G.w * w[k]);
                         }
+                    } else {
+                        float *gbase = a.g.grid[l] + 4 * part;
+#pragma unroll
+                        for (int k = 0; k < 8; ++k)
+                            red_add_v4(gbase + (size_t)vtx[k] * kC, G.x * w[k], G.y * w[k], G.z * w[k], G.w * w[k]);
                     }
                 }
                 if (kGradX) {
                     // d(sample)/du per corner: -/+ the product of the other two axes' weights
                     // (PyTorch's grid_sampler_3d backward), times (s-1)/2, zero where clamped.
+                    const float4 *fm = reinterpret_cast<const float4 *>(a.m.grid[l]);
                     float dot[8];
 #pragma unroll
                     for (int k = 0; k < 8; ++k) {
                         const float4 u = __ldg(fm + (size_t)vtx[k] * (kC / 4) + part);
-                        float t = G[p].x * u.x;
-                        t = fmaf(G[p].y, u.y, t);
-                        t = fmaf(G[p].z, u.z, t);
-                        t = fmaf(G[p].w, u.w, t);
+                        float t = G.x * u.x;
+                        t = fmaf(G.y, u.y, t);
+                        t = fmaf(G.z, u.z, t);
+                        t = fmaf(G.w, u.w, t);
                         t += __shfl_xor_sync(FULL, t, 1);
                         t += __shfl_xor_sync(FULL, t, 2);
                         t += __shfl_xor_sync(FULL, t, 4);
@@ -1012,22 +997,15 @@ __global__ void __launch_bounds__(256) sdf_bwd_scatter_kernel(const ScatterArgs 
                     giz += -dot[0] * wx0 * wy0 - dot[1] * wx1 * wy0 - dot[2] * wx0 * wy1 - dot[3] * wx1 * wy1;
                     giz += dot[4] * wx0 * wy0 + dot[5] * wx1 * wy0 + dot[6] * wx0 * wy1 + dot[7] * wx1 * wy1;
                     const float half = sm1 / 2.f;
-                    const uint32_t e = __shfl_sync(FULL, edge, src);
-                    gxv[p][0] += (e & 1u) ? 0.f : gix * half;
-                    gxv[p][1] += (e & 2u) ? 0.f : giy * half;
-                    gxv[p][2] += (e & 4u) ? 0.f : giz * half;
+                    gxv[0] += (rx <= 0.f || rx >= sm1) ? 0.f : gix * half;
+                    gxv[1] += (ry <= 0.f || ry >= sm1) ? 0.f : giy * half;
+                    gxv[2] += (rz <= 0.f || rz >= sm1) ? 0.f : giz * half;
                 }
             }
-        }
-        if (kGradX && part == 0) {
-#pragma unroll
-            for (int p = 0; p < 8; ++p) {
-                const int64_t ip = base + 4 * p + (lane >> 3);
-                if (ip < a.n) {
-                    a.gx[3 * ip] += gxv[p][0];
-                    a.gx[3 * ip + 1] += gxv[p][1];
-                    a.gx[3 * ip + 2] += gxv[p][2];
-                }
+            if (kGradX && part == 0 && valid) {
+                a.gx[3 * ip] += gxv[0];
+                a.gx[3 * ip + 1] += gxv[1];
+                a.gx[3 * ip + 2] += gxv[2];
             }
         }
     }
@@ -1216,7 +1194,7 @@ extern "C" int nglod_sdf_bwd(const nglod_dense_model *model, const float *x, int
         s.smem_levels = l + 1;
     }
     const size_t smem2 = (size_t)s.soff[s.smem_levels] * sizeof(float);
-    const int threads = 256;
+    const int threads = kScatterThreads;
     const int64_t want = (n + threads - 1) / threads;
     if (grad_x) {
         auto k = sdf_bwd_scatter_kernel<true>;
