@@ -42,6 +42,27 @@ __device__ __forceinline__ void corner_set(int s, float px, float py, float pz, 
     }
 }
 
+// corner_set for a point whose clamped grid coordinates are already known
+// (the same expressions, so the same bits): vertex index of corner 0, the
+// y / z neighbour flags (whether they differ from it) and the weights.
+__device__ __forceinline__ void corner_set_at(int s, float ix, float iy, float iz, int &v0, bool &ny, bool &nz,
+                                              float (&w)[8]) {
+    const float x0 = floorf(ix), y0 = floorf(iy), z0 = floorf(iz);
+    const float wx1 = ix - x0, wx0 = (x0 + 1.f) - ix;
+    const float wy1 = iy - y0, wy0 = (y0 + 1.f) - iy;
+    const float wz1 = iz - z0, wz0 = (z0 + 1.f) - iz;
+    const int xi = (int)x0, yi = (int)y0, zi = (int)z0;
+    v0 = (zi * s + yi) * s + xi;
+    ny = yi + 1 < s;
+    nz = zi + 1 < s;
+    const float wxy[4] = {wx0 * wy0, wx1 * wy0, wx0 * wy1, wx1 * wy1};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        w[k] = wxy[k] * wz0;
+        w[k + 4] = wxy[k] * wz1;
+    }
+}
+
 // Sum over LODs 0..L of the trilinear samples of the 32 points of a warp
 // (lane i owns point i's position).  Each lane computes its own point's
 // corner set once per LOD; the loads are then done by LPP lanes per point
@@ -132,19 +153,26 @@ __device__ __forceinline__ void gather_warp_pairs(const nglod_bf16_model &m, int
         const PairUnit *g = static_cast<const PairUnit *>(m.grid_pairs[l]) + part;  // 4 units per line
         const int s = (1 << (l + m.base_lod)) + 1;
         const int sy = s * 4, sz = s * sy;
-        uint32_t pk;
-        float w[8];
-        corner_set(s, px, py, pz, pk, w);
+        // each lane's own point's clamped grid coordinates; the loading lanes
+        // receive them by three shuffles and derive the corner set themselves
+        // (corner_set's expressions: the same sums as shuffling its results)
+        const float sm1 = (float)(s - 1);
+        const float ix = fminf(sm1, fmaxf(((px + 1.f) / 2.f) * sm1, 0.f));
+        const float iy = fminf(sm1, fmaxf(((py + 1.f) / 2.f) * sm1, 0.f));
+        const float iz = fminf(sm1, fmaxf(((pz + 1.f) / 2.f) * sm1, 0.f));
 #pragma unroll
         for (int p = 0; p < NP; ++p) {
             const int src = p * 8 + (lane >> 2);
-            const uint32_t q = __shfl_sync(FULL, pk, src);
+            const float qx = __shfl_sync(FULL, ix, src);
+            const float qy = __shfl_sync(FULL, iy, src);
+            const float qz = __shfl_sync(FULL, iz, src);
             float ws[8];
-#pragma unroll
-            for (int k = 0; k < 8; ++k) ws[k] = __shfl_sync(FULL, w[k], src);
-            const int o0 = (int)(q & 0x0FFFFFFFu) * 4;
-            const int oy = ((q >> 29) & 1u) ? sy : 0;
-            const int oz = ((q >> 30) & 1u) ? sz : 0;
+            int v0;
+            bool ny, nz;
+            corner_set_at(s, qx, qy, qz, v0, ny, nz, ws);
+            const int o0 = v0 * 4;
+            const int oy = ny ? sy : 0;
+            const int oz = nz ? sz : 0;
             const int o[4] = {o0, o0 + oy, o0 + oz, o0 + oz + oy};
             PairUnit v[4];
 #pragma unroll
@@ -179,10 +207,10 @@ __device__ __forceinline__ void write_pair_rows(uint8_t *sA, int row0, int lane,
         const int row = row0 + p * 8 + (lane >> 2);
         const uint4 f = make_uint4(pack_bf16x2(acc[p][0].x, acc[p][0].y), pack_bf16x2(acc[p][1].x, acc[p][1].y),
                                    pack_bf16x2(acc[p][2].x, acc[p][2].y), pack_bf16x2(acc[p][3].x, acc[p][3].y));
-        *reinterpret_cast<uint4 *>(sA + tc::tile_offset(row, 8 * part, kKC)) = f;
+        *reinterpret_cast<uint4 *>(sA + tile_offset_a(row, 8 * part)) = f;
     }
     if (lane < 8 * NP)
-        *reinterpret_cast<uint4 *>(sA + tc::tile_offset(row0 + lane, 32, kKC)) = position_columns(px, py, pz);
+        *reinterpret_cast<uint4 *>(sA + tile_offset_a(row0 + lane, 32)) = position_columns(px, py, pz);
 }
 
 // Pair volume of a bf16 volume (s vertices per side), in 16-byte units:
@@ -256,10 +284,10 @@ __device__ __forceinline__ void write_warp_rows(uint8_t *sA, int warp, int lane,
                                        pack_bf16x2(acc[p][4 * j + 1].x, acc[p][4 * j + 1].y),
                                        pack_bf16x2(acc[p][4 * j + 2].x, acc[p][4 * j + 2].y),
                                        pack_bf16x2(acc[p][4 * j + 3].x, acc[p][4 * j + 3].y));
-            *reinterpret_cast<uint4 *>(sA + tc::tile_offset(row, 2 * kQ * part + 8 * j, kKC)) = f;
+            *reinterpret_cast<uint4 *>(sA + tile_offset_a(row, 2 * kQ * part + 8 * j)) = f;
         }
     }
-    *reinterpret_cast<uint4 *>(sA + tc::tile_offset(warp * 32 + lane, 32, kKC)) = position_columns(px, py, pz);
+    *reinterpret_cast<uint4 *>(sA + tile_offset_a(warp * 32 + lane, 32)) = position_columns(px, py, pz);
 }
 
 // The tracer's gather: two lanes per point, each computing the corner set
@@ -382,13 +410,17 @@ static uint32_t g_bf16_wait_polls = kWaitPolls;
 template <bool kPairs>
 __global__ void __launch_bounds__(kTP, 4) sdf_fwd_bf16_tc_kernel(const Bf16Args a) {
     extern __shared__ __align__(1024) uint8_t smem[];
-    uint8_t *sA = smem + kSmemA;
-    uint8_t *sB = smem + kSmemB;
-    float *sb0 = reinterpret_cast<float *>(smem + kSmemB0);
-    float *sw1 = reinterpret_cast<float *>(smem + kSmemW1);
-    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + kSmemBar);
-    uint32_t *slot = reinterpret_cast<uint32_t *>(smem + kSmemSlot);
-    volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + kSmemAbort);
+    // the padded point tile (tile_offset_a), then the decoder tile and the rest
+    constexpr size_t qA = 0, qB = kTileBytesA, qB0 = qB + kTileBytes, qW1 = qB0 + kHid * 4, qBar = qW1 + kHid * 4;
+    constexpr size_t qSlot = qBar + 8, qAbort = qSlot + 4;
+    static_assert(qB % 16 == 0 && qBar % 8 == 0 && qAbort + 4 <= kSmemBytes, "point-query shared layout");
+    uint8_t *sA = smem + qA;
+    uint8_t *sB = smem + qB;
+    float *sb0 = reinterpret_cast<float *>(smem + qB0);
+    float *sw1 = reinterpret_cast<float *>(smem + qW1);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + qBar);
+    uint32_t *slot = reinterpret_cast<uint32_t *>(smem + qSlot);
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + qAbort);
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const uint4 *bsrc = static_cast<const uint4 *>(a.m.w0_tile[a.L]);
@@ -399,7 +431,7 @@ __global__ void __launch_bounds__(kTP, 4) sdf_fwd_bf16_tc_kernel(const Bf16Args 
     // K core-matrix column 5 (k 40..47) is always zero.
     for (int i = tid; i < (kTP / 8) * 8; i += kTP) {
         const int grp = i >> 3, r = i & 7;
-        *reinterpret_cast<uint4 *>(sA + (grp * kKC + 5) * 128 + r * 16) = make_uint4(0u, 0u, 0u, 0u);
+        *reinterpret_cast<uint4 *>(sA + grp * kSboA + 5 * kLboA + r * 16) = make_uint4(0u, 0u, 0u, 0u);
     }
     if (warp == 0) tc::tmem_alloc(slot, kHid);
     if (tid == 0) {
@@ -445,7 +477,7 @@ __global__ void __launch_bounds__(kTP, 4) sdf_fwd_bf16_tc_kernel(const Bf16Args 
             tc::fence_after_sync();
 #pragma unroll
             for (int ks = 0; ks < kTK / 16; ++ks) {
-                const uint64_t ad = tc::smem_desc(sa + ks * 256, kLbo, kSbo);
+                const uint64_t ad = tc::smem_desc(sa + ks * 2 * kLboA, kLboA, kSboA);
                 const uint64_t bd = tc::smem_desc(sb + ks * 256, kLbo, kSbo);
                 tc::mma_bf16(tmem, ad, bd, idesc, ks > 0 ? 1u : 0u);
             }

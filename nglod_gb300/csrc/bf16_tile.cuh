@@ -36,6 +36,16 @@ constexpr size_t kSmemBytes = 48 * 1024;
 
 constexpr uint32_t kOneOne = 0x3F803F80u;  // two bf16 1.0: the b0 columns' inputs
 
+// Point tiles of the point-query kernel put their K-adjacent core matrices
+// 160 B apart (the descriptor's LBO) instead of 128 B: a quarter warp then
+// stores its two rows x four 16-byte pieces into eight different bank groups
+// (at 128 B they would share two).
+constexpr uint32_t kLboA = 160, kSboA = kKC * kLboA;  // 960 B per 8-row group
+constexpr uint32_t kTileBytesA = (kTP / 8) * kSboA;   // 15 KB
+__host__ __device__ constexpr uint32_t tile_offset_a(int row, int k) {
+    return (uint32_t)((row / 8) * kSboA + (k / 8) * kLboA + (row % 8) * 16 + (k % 8) * 2);
+}
+
 __device__ __forceinline__ float bf_lo(uint32_t v) { return __uint_as_float(v << 16); }
 __device__ __forceinline__ float bf_hi(uint32_t v) { return __uint_as_float(v & 0xffff0000u); }
 
