@@ -359,9 +359,9 @@ __device__ __forceinline__ void write_tile_row_half(uint8_t *sA, int row, int h,
         const uint4 f = make_uint4(pack_bf16x2(acc[8 * j], acc[8 * j + 1]), pack_bf16x2(acc[8 * j + 2], acc[8 * j + 3]),
                                    pack_bf16x2(acc[8 * j + 4], acc[8 * j + 5]),
                                    pack_bf16x2(acc[8 * j + 6], acc[8 * j + 7]));
-        *reinterpret_cast<uint4 *>(sA + tc::tile_offset(row, kCh * h + 8 * j, kKC)) = f;
+        *reinterpret_cast<uint4 *>(sA + tile_offset_a(row, kCh * h + 8 * j)) = f;
     }
-    if (h == 0) *reinterpret_cast<uint4 *>(sA + tc::tile_offset(row, 32, kKC)) = position_columns(px, py, pz);
+    if (h == 0) *reinterpret_cast<uint4 *>(sA + tile_offset_a(row, 32)) = position_columns(px, py, pz);
 }
 
 // Ray entry into [-1,1]^3 with sol_nglod_kernel.cu:92-150's float arithmetic
@@ -410,17 +410,13 @@ static uint32_t g_bf16_wait_polls = kWaitPolls;
 template <bool kPairs>
 __global__ void __launch_bounds__(kTP, 4) sdf_fwd_bf16_tc_kernel(const Bf16Args a) {
     extern __shared__ __align__(1024) uint8_t smem[];
-    // the padded point tile (tile_offset_a), then the decoder tile and the rest
-    constexpr size_t qA = 0, qB = kTileBytesA, qB0 = qB + kTileBytes, qW1 = qB0 + kHid * 4, qBar = qW1 + kHid * 4;
-    constexpr size_t qSlot = qBar + 8, qAbort = qSlot + 4;
-    static_assert(qB % 16 == 0 && qBar % 8 == 0 && qAbort + 4 <= kSmemBytes, "point-query shared layout");
-    uint8_t *sA = smem + qA;
-    uint8_t *sB = smem + qB;
-    float *sb0 = reinterpret_cast<float *>(smem + qB0);
-    float *sw1 = reinterpret_cast<float *>(smem + qW1);
-    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + qBar);
-    uint32_t *slot = reinterpret_cast<uint32_t *>(smem + qSlot);
-    volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + qAbort);
+    uint8_t *sA = smem + kSmemA;
+    uint8_t *sB = smem + kSmemB;
+    float *sb0 = reinterpret_cast<float *>(smem + kSmemB0);
+    float *sw1 = reinterpret_cast<float *>(smem + kSmemW1);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + kSmemBar);
+    uint32_t *slot = reinterpret_cast<uint32_t *>(smem + kSmemSlot);
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + kSmemAbort);
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const uint4 *bsrc = static_cast<const uint4 *>(a.m.w0_tile[a.L]);
@@ -554,7 +550,7 @@ __global__ void __launch_bounds__(kTP, 4) trace_bf16_tc_kernel(const Bf16TraceAr
     const float b1 = a.m.b1[a.L][0];
     for (int i = tid; i < (kTP / 8) * 8; i += kTP) {
         const int grp = i >> 3, r = i & 7;
-        *reinterpret_cast<uint4 *>(sA + (grp * kKC + 5) * 128 + r * 16) = make_uint4(0u, 0u, 0u, 0u);
+        *reinterpret_cast<uint4 *>(sA + grp * kSboA + 5 * kLboA + r * 16) = make_uint4(0u, 0u, 0u, 0u);
     }
     if (warp == 0) tc::tmem_alloc(slot, kHid);
     if (tid == 0) {
@@ -694,7 +690,7 @@ __global__ void __launch_bounds__(kTP, 4) trace_bf16_tc_kernel(const Bf16TraceAr
             tc::fence_after_sync();
 #pragma unroll
             for (int ks = 0; ks < kTK / 16; ++ks) {
-                const uint64_t ad = tc::smem_desc(sa + ks * 256, kLbo, kSbo);
+                const uint64_t ad = tc::smem_desc(sa + ks * 2 * kLboA, kLboA, kSboA);
                 const uint64_t bd = tc::smem_desc(sb + ks * 256, kLbo, kSbo);
                 tc::mma_bf16(tmem, ad, bd, idesc, ks > 0 ? 1u : 0u);
             }

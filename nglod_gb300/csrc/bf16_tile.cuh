@@ -22,11 +22,22 @@ constexpr uint32_t kTileBytes = kTP * kTK * 2;
 constexpr uint32_t kLbo = 128, kSbo = kKC * 128;
 constexpr uint32_t kWaitPolls = 1u << 22;
 
+// Point tiles (A) put their K-adjacent core matrices 160 B apart (the
+// descriptor's LBO) instead of 128 B: the quarter warps of the tile writers
+// (two rows x four 16-byte pieces, or four rows x two) then store into eight
+// different bank groups (at 128 B they would share two or four).  The
+// decoder tile (B, packed on the host) keeps the dense layout.
+constexpr uint32_t kLboA = 160, kSboA = kKC * kLboA;  // 960 B per 8-row group
+constexpr uint32_t kTileBytesA = (kTP / 8) * kSboA;   // 15 KB
+__host__ __device__ constexpr uint32_t tile_offset_a(int row, int k) {
+    return (uint32_t)((row / 8) * kSboA + (k / 8) * kLboA + (row % 8) * 16 + (k % 8) * 2);
+}
+
 // Dynamic shared memory: A tile | B tile | b0[128] | w1[128] | mbarrier |
 // TMEM slot | abort flag, padded so that at most four blocks share an SM
 // (four x 128 TMEM columns fill the SM's 512).
 constexpr size_t kSmemA = 0;
-constexpr size_t kSmemB = kSmemA + kTileBytes;
+constexpr size_t kSmemB = kSmemA + kTileBytesA;
 constexpr size_t kSmemB0 = kSmemB + kTileBytes;
 constexpr size_t kSmemW1 = kSmemB0 + kHid * 4;
 constexpr size_t kSmemBar = kSmemW1 + kHid * 4;
@@ -36,15 +47,6 @@ constexpr size_t kSmemBytes = 48 * 1024;
 
 constexpr uint32_t kOneOne = 0x3F803F80u;  // two bf16 1.0: the b0 columns' inputs
 
-// Point tiles of the point-query kernel put their K-adjacent core matrices
-// 160 B apart (the descriptor's LBO) instead of 128 B: a quarter warp then
-// stores its two rows x four 16-byte pieces into eight different bank groups
-// (at 128 B they would share two).
-constexpr uint32_t kLboA = 160, kSboA = kKC * kLboA;  // 960 B per 8-row group
-constexpr uint32_t kTileBytesA = (kTP / 8) * kSboA;   // 15 KB
-__host__ __device__ constexpr uint32_t tile_offset_a(int row, int k) {
-    return (uint32_t)((row / 8) * kSboA + (k / 8) * kLboA + (row % 8) * 16 + (k % 8) * 2);
-}
 
 __device__ __forceinline__ float bf_lo(uint32_t v) { return __uint_as_float(v << 16); }
 __device__ __forceinline__ float bf_hi(uint32_t v) { return __uint_as_float(v & 0xffff0000u); }
@@ -99,7 +101,7 @@ __device__ __forceinline__ PairUnit ld_pair_unit(const PairUnit *p) {
 // layout above.
 constexpr size_t kSmemQ = (kSmemAbort + 4 + 15) & ~(size_t)15;  // float4 query points [128], 16-byte aligned
 static_assert(kSmemQ % 16 == 0 && kSmemQ + kTP * 16 <= kSmemBytes, "query-point array layout");
-static_assert(kSmemBar % 8 == 0 && kSmemB % 16 == 0, "barrier / tile alignment");
+static_assert(kSmemBar % 8 == 0 && kSmemB % 16 == 0 && kSmemQ + kTP * 16 <= kSmemBytes, "barrier / tile alignment");
 
 
 }  // namespace nglod

@@ -414,7 +414,7 @@ __global__ void __launch_bounds__(kTP, 4) sparse_trace_tc_kernel(const SparseTcA
     const float b1 = a.m.b1[a.lod][0];
     for (int i = tid; i < (kTP / 8) * 8; i += kTP) {
         const int grp = i >> 3, r = i & 7;
-        *reinterpret_cast<uint4 *>(sA + (grp * kKC + 5) * 128 + r * 16) = make_uint4(0u, 0u, 0u, 0u);
+        *reinterpret_cast<uint4 *>(sA + grp * kSboA + 5 * kLboA + r * 16) = make_uint4(0u, 0u, 0u, 0u);
     }
     if (warp == 0) tc::tmem_alloc(slot, kHid);
     if (tid == 0) {
@@ -556,11 +556,11 @@ __global__ void __launch_bounds__(kTP, 4) sparse_trace_tc_kernel(const SparseTcA
             const float4 pt = qpts[row];
             float f[8];
             sparse_features_quarter<kChain>(a.m, a.lod, (int64_t)__float_as_int(pt.w), pt.x, pt.y, pt.z, q, f);
-            *reinterpret_cast<uint4 *>(sA + tc::tile_offset(row, 8 * q, kKC)) =
+            *reinterpret_cast<uint4 *>(sA + tile_offset_a(row, 8 * q)) =
                 make_uint4(pack_bf16x2(f[0], f[1]), pack_bf16x2(f[2], f[3]), pack_bf16x2(f[4], f[5]),
                            pack_bf16x2(f[6], f[7]));
             if (q == 0)
-                *reinterpret_cast<uint4 *>(sA + tc::tile_offset(row, 32, kKC)) = position_columns(pt.x, pt.y, pt.z);
+                *reinterpret_cast<uint4 *>(sA + tile_offset_a(row, 32)) = position_columns(pt.x, pt.y, pt.z);
         }
         tc::fence_proxy_async_smem();
         __syncthreads();
@@ -568,7 +568,7 @@ __global__ void __launch_bounds__(kTP, 4) sparse_trace_tc_kernel(const SparseTcA
             tc::fence_after_sync();
 #pragma unroll
             for (int ks = 0; ks < kTK / 16; ++ks) {
-                const uint64_t ad = tc::smem_desc(sa + ks * 256, kLbo, kSbo);
+                const uint64_t ad = tc::smem_desc(sa + ks * 2 * kLboA, kLboA, kSboA);
                 const uint64_t bd = tc::smem_desc(sb + ks * 256, kLbo, kSbo);
                 tc::mma_bf16(tmem, ad, bd, idesc, ks > 0 ? 1u : 0u);
             }
