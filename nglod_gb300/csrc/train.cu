@@ -536,8 +536,12 @@ constexpr uint32_t kMBytes = kTP * kH * 2;     // 32 KB
 constexpr size_t kIn = 0;                      // IN: buffer b hi at kIn + 2b * kInBytes, lo after it
 constexpr size_t kM = kIn + 4 * kInBytes;      // M: buffer b hi at kM + 2b * kMBytes, lo after it
 constexpr size_t kWH = kM + 4 * kMBytes, kWL = kWH + kWBytes;  // W1 hi / lo
-constexpr size_t kStage = kWL + kWBytes;       // next tile's feature sums [128][32] f32
-constexpr size_t kStageX = kStage + kTP * 32 * 4;  // and positions [128][3] f32
+// next tile's feature sums [128][32] f32, rows kStageRow float4 apart: nine,
+// so that the eight rows a quarter warp copies or reads fall in eight bank
+// groups (eight float4 apart they would share four banks)
+constexpr int kStageRow = 9;
+constexpr size_t kStage = kWL + kWBytes;
+constexpr size_t kStageX = kStage + kTP * kStageRow * 16;  // and positions [128][3] f32
 constexpr size_t kBarD = kStageX + kTP * 3 * 4;
 constexpr size_t kSlot = kBarD + 8, kAbort = kSlot + 4;
 constexpr size_t kSmem = kAbort + 12;
@@ -608,7 +612,7 @@ __device__ __forceinline__ void stage_tile(const BwdArgs &a, int l, int64_t tile
     const int64_t q = tile * kTP + r;
     if (q < a.n) {
         const float4 *src = reinterpret_cast<const float4 *>(a.feats + ((int64_t)l * a.n + q) * kC);
-        float4 *dst = reinterpret_cast<float4 *>(smem + kStage) + r * 8;
+        float4 *dst = reinterpret_cast<float4 *>(smem + kStage) + r * kStageRow;
 #pragma unroll
         for (int k = 0; k < 4; ++k) cp_async16(dst + 4 * half + k, src + 4 * half + k);
         if (half == 0) {
@@ -630,7 +634,7 @@ __device__ __forceinline__ void fill_in_tile(const BwdArgs &a, int64_t tile, uin
     const float *sx = reinterpret_cast<const float *>(smem + kStageX) + r * 3;
     const float xf[3] = {sx[0], sx[1], sx[2]};
     float4 fr[8];
-    const float4 *sf = reinterpret_cast<const float4 *>(smem + kStage) + r * 8;
+    const float4 *sf = reinterpret_cast<const float4 *>(smem + kStage) + r * kStageRow;
 #pragma unroll
     for (int k = 0; k < 8; ++k) fr[k] = sf[k];
     uint8_t *hi = smem + kIn + (size_t)(2 * buf) * kInBytes, *lo = hi + kInBytes;
