@@ -99,7 +99,19 @@ TF32_NOMINAL_TFLOPS = 1100.0
 # the SHA-256 of the kernel sources they were captured from.  A figure is
 # reported only while those sources are unchanged; otherwise the roofline's
 # traffic is null.
-NCU_CAPTURES = {}
+NCU_CAPTURES = {
+    "sdf_fwd_f32_tc_kernel": {
+        "dram_bytes": 91_318_784 + 11_194_624, "points": N_POINTS,
+        "sources": ["nglod_gb300/csrc/dense.cu", "nglod_gb300/csrc/dense_common.cuh",
+                    "nglod_gb300/csrc/tf32_tile.cuh", "nglod_gb300/csrc/tc_common.cuh"],
+        "sha256": "390c6158788a05ef15a4187d985ef0b2c4deb4d054fc136ddd1d4cb237c4b890",
+        "how": "ncu --set full --clock-control none, one launch at 4,194,304 points (bench --no-extras)"},
+    "sdf_fwd_bf16_tc_kernel": {
+        "dram_bytes": 90_524_160 + 11_049_216, "points": N_POINTS,
+        "sources": ["nglod_gb300/csrc/bf16.cu", "nglod_gb300/csrc/bf16_tile.cuh", "nglod_gb300/csrc/tc_common.cuh"],
+        "sha256": "df7f80a31490e6140ca00f1563d41b5e8e5f2f77ded8375784d5ee72db2176ef",
+        "how": "ncu --set full --clock-control none, one launch at 4,194,304 points (bench --only bf16)"},
+}
 
 
 def parse():
