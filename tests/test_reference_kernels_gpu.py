@@ -37,6 +37,21 @@ def ref(cuda):
     return refkern
 
 
+def _ms(fn, reps=3):
+    """Median CUDA-event time of fn() on the current stream, after one warm-up call."""
+    fn()
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(reps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        fn()
+        b.record()
+        b.synchronize()
+        times.append(a.elapsed_time(b))
+    return sorted(times)[len(times) // 2]
+
+
 def _bits(t):
     return t.contiguous().view(torch.int32) if t.dtype == torch.float32 else t
 
@@ -123,6 +138,10 @@ def test_spc_raytrace_bit_exact_with_reference_kernels_at_frame_size(ref, cuda, 
     first = spc.mark_first(got)
     assert torch.equal(first, ref.mark_unique_rays(want))
     assert int(first.sum()) == int(torch.unique(want[:, 0]).numel())
+    t_ours = _ms(lambda: spc.spc_raytrace(s.GetOctree(), s.GetPoints(), s.GetPyramid(), o, d, target,
+                                          prefix=s.GetPrefix()))
+    t_ref = _ms(lambda: ref.spc_raytrace(s.GetOctree(), s.GetPoints(), s.GetPyramid(), o, d, target))
+    print(f"traversal 1920x1080 to level {target}: ours {t_ours:.3f} ms, reference kernels {t_ref:.3f} ms")
 
 
 def test_generate_rays_bit_exact_with_reference_kernel(ref, cuda):
@@ -173,6 +192,10 @@ def _trace_against_reference(ref, cuda, ours, z, width, height, lod):
     pts = s2.GetPoints()[int(pyr[1, target]):, :3].contiguous()
     xr, tr, hr, nr = sdf_ref.sphere_trace(org, dr, nug, pts, info, lod)
     x, t, hit, normal = ours.sphereTrace(org, dr, nug, None, None, lod)
+    t_ref = _ms(lambda: sdf_ref.sphere_trace(org, dr, nug, pts, info, lod))
+    t_ours = _ms(lambda: ours.sphereTrace(org, dr, nug, None, None, lod))
+    print(f"sparse trace {width}x{height} lod {lod} (float32 decoder): ours {t_ours:.3f} ms, "
+          f"reference kernels + cuBLAS {t_ref:.3f} ms")
     agree = (hit == hr).float().mean().item()
     both = hit & hr
     assert both.sum().item() > 0.05 * hit.numel()
