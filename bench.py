@@ -646,12 +646,15 @@ def bench_trace(net, dev, flush, stream):
     pk = peaks()
     line_peak = line_read_peak(dev, sum(fv.fm.numel() * 4 for fv in net.features))
     fma = fma_peak(dev)
-    roof32 = roofline("trace_f32_kernel", ms / 1e3, {
+    roof32 = roofline("trace_f32_tc_kernel", ms / 1e3, {
         "gather_l2": (evals * F32_GATHER_BYTES, line_peak, "GB/s", "measured live (nglod_measure_line_reads)"),
-        "fp32_pipe": (evals * F32_FLOP, fma, "TFLOP/s", "measured live (nglod_measure_fma)"),
+        "fp32_pipe": (evals * F32_SIMT_FLOP, fma, "TFLOP/s", "measured live (nglod_measure_fma)"),
+        "tensor": (evals * F32_TC_FLOP, TF32_NOMINAL_TFLOPS, "TFLOP/s",
+                   "nominal dense TF32 (no measured TF32 figure on this pool)"),
         "hbm": (n * (24 + 12 + 4 + 12 + 1) + sum(fv.fm.numel() * 4 for fv in net.features), pk["hbm_gbs"], "GB/s",
                 f"{pk['source']} hbm_gbs")},
-        {"sdf_evaluation": {"gathered_bytes": F32_GATHER_BYTES, "fp32_flop": F32_FLOP},
+        {"sdf_evaluation": {"gathered_bytes": F32_GATHER_BYTES, "fp32_pipe_flop": F32_SIMT_FLOP,
+                            "tf32_tensor_flop": F32_TC_FLOP},
          "ray": {"hbm_bytes": 24 + 12 + 4 + 12 + 1}}, evals)
     line_peak16 = line_read_peak(dev, sum(fv.fm.numel() * 2 for fv in net.features))
     roof16 = roofline("trace_bf16_tc_kernel", ms16 / 1e3, {

@@ -109,8 +109,8 @@ int nglod_sdf_fwd_simt(const nglod_dense_model *model, const float *x, int64_t n
 
 /* Reads and clears the float32 query's device status on the current device
  * (synchronous): *status_out = 1 if a bounded tensor-core wait of an
- * nglod_sdf_fwd call since the last read gave up (its outputs are
- * incomplete), else 0.  No counterpart in the reference. */
+ * nglod_sdf_fwd or nglod_trace call since the last read gave up (its outputs
+ * are incomplete), else 0.  No counterpart in the reference. */
 int nglod_dense_status(int32_t *status_out);
 
 /* nglod_sdf_fwd with the points and results in HOST memory (pinned for the
@@ -133,7 +133,9 @@ int nglod_sdf_fwd_host(const nglod_dense_model *model, const float *x_host, int6
  * gradient(method='finitediff') (sdf-net/lib/diffutils.py:61-70).
  * work_counter: one device int64 used to hand rays to warps; the call zeroes
  * it on the stream before the launch.  Outputs x[n][3], t[n], hit[n],
- * normal[n][3] are all written. */
+ * normal[n][3] are all written.  At hidden_dim 128 every sdf evaluation is
+ * nglod_sdf_fwd's tensor-core arithmetic (the same bits at the same point);
+ * a bounded wait that gives up sets the flag nglod_dense_status reads. */
 int nglod_trace(const nglod_dense_model *model, const nglod_trace_params *params,
                 const float *ray_o, const float *ray_d, int64_t n,
                 float *x, float *t, uint8_t *hit, float *normal,

@@ -109,21 +109,14 @@ __device__ int g_dense_status = 0;
 // error path lowers it.
 static uint32_t g_f32tc_wait_polls = 1u << 22;
 
-__global__ void __launch_bounds__(f32tc::kThreads, 2)
-    sdf_fwd_f32_tc_kernel(const nglod_dense_model m, const float *__restrict__ x, int64_t n, int L,
-                          float *__restrict__ out, uint32_t polls) {
+// Block set-up of the tensor-core float32 decode: LOD L's weight tile
+// (feature part, split), x y z and b0 per unit, w1; TMEM columns; the
+// barrier.  Returns the TMEM base address.
+__device__ __forceinline__ uint32_t f32tc_setup(const nglod_dense_model &m, int L, uint8_t *sm, int tid) {
     using namespace f32tc;
-    extern __shared__ __align__(1024) uint8_t smem_f32tc[];
-    uint8_t *sm = smem_f32tc;
-    const float4 *su = reinterpret_cast<const float4 *>(sm + kU);
-    const float *sw1 = reinterpret_cast<const float *>(sm + kW1);
     uint64_t *bar = reinterpret_cast<uint64_t *>(sm + kBar);
     uint32_t *slot = reinterpret_cast<uint32_t *>(sm + kSlot);
     volatile int *abort_flag = reinterpret_cast<volatile int *>(sm + kAbort);
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int half = warp >> 2, quad = warp & 3;
-
-    // weight tile of LOD L (hidden unit j = row, feature c = K column), split
     const float *w0 = m.w0[L];
     for (int u = tid; u < kH * kKC; u += kThreads) {
         const int j = u / kKC, kc = u % kKC;
@@ -135,8 +128,7 @@ __global__ void __launch_bounds__(f32tc::kThreads, 2)
             make_float4(w0[tid * 35], w0[tid * 35 + 1], w0[tid * 35 + 2], m.b0[L][tid]);
         reinterpret_cast<float *>(sm + kW1)[tid] = m.w1[L][tid];
     }
-    const float b1 = m.b1[L][0];
-    if (warp == 0) tc::tmem_alloc(slot, kCols);
+    if ((tid >> 5) == 0) tc::tmem_alloc(slot, kCols);
     if (tid == 0) {
         tc::mbar_init(bar, 1);
         *abort_flag = 0;
@@ -145,14 +137,112 @@ __global__ void __launch_bounds__(f32tc::kThreads, 2)
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
-    const uint32_t tmem = *slot;
-    const uint32_t sbase = tc::smem_addr(sm);
-    constexpr uint32_t idesc = idesc_tf32_f32(kTP, kH);
+    return *slot;
+}
+
+// The sdf of the block's 256 points at LOD L, thread tid owning point
+// (px, py, pz) (warp w fills row 32 (w % 4) + lane of tile w / 4): the
+// warp-cooperative gather and LOD sum, the tile rows, one thread's 24
+// split-TF32 MMAs for both tiles, and this thread's float32 epilogue.  Every
+// thread of the block calls it; false (for all of them) if the bounded
+// tensor-core wait gave up, which also sets g_dense_status.
+__device__ __forceinline__ bool f32tc_decode(const nglod_dense_model &m, int L, float px, float py, float pz,
+                                             uint8_t *sm, uint32_t tmem, uint32_t &phase, uint32_t polls,
+                                             float &out) {
+    using namespace f32tc;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int half = warp >> 2, quad = warp & 3;
+    uint64_t *bar = reinterpret_cast<uint64_t *>(sm + kBar);
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(sm + kAbort);
+    const float4 *su = reinterpret_cast<const float4 *>(sm + kU);
+    const float *sw1 = reinterpret_cast<const float *>(sm + kW1);
     uint8_t *abig = sm + kA + (size_t)2 * half * kTileA;
     uint8_t *asmall = abig + kTileA;
+    // 1. gather: LOD sum of the warp's 32 points, written as tile rows
+    float4 acc[8];
+#pragma unroll
+    for (int p = 0; p < 8; ++p) acc[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll 1
+    for (int l = 0; l <= L; ++l)
+        gather_warp_add_f32(static_cast<const float *>(m.grid[l]), volume_side(m, l), px, py, pz, lane, acc);
+#pragma unroll
+    for (int p = 0; p < 8; ++p)
+        store_split4(abig, asmall, a_offset(quad * 32 + 4 * p + (lane >> 3), 4 * (lane & 7)), acc[p]);
+    tc::fence_proxy_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    // 2. one thread issues big*big + big*small + small*big for both tiles
+    if (tid == 0) {
+        tc::fence_after_sync();
+        const uint32_t sbase = tc::smem_addr(sm);
+        constexpr uint32_t idesc = idesc_tf32_f32(kTP, kH);
+        const uint64_t wb = tc::smem_desc(sbase + (uint32_t)kW, 128, kKC * 128);
+        const uint64_t ws = tc::smem_desc(sbase + (uint32_t)(kW + kTile), 128, kKC * 128);
+#pragma unroll
+        for (int h = 0; h < kTiles; ++h) {
+            const uint64_t ab = tc::smem_desc(sbase + (uint32_t)(kA + 2 * h * kTileA), kLboA, kSboA);
+            const uint64_t as = tc::smem_desc(sbase + (uint32_t)(kA + (2 * h + 1) * kTileA), kLboA, kSboA);
+#pragma unroll
+            for (int t = 0; t < 3; ++t)
+#pragma unroll
+                for (int ks = 0; ks < kK / 8; ++ks) {
+                    // 8 tf32 of K: two core matrices of each operand
+                    const uint64_t sa = (uint64_t)((ks * 2 * kLboA) >> 4), sw = (uint64_t)((ks * 256) >> 4);
+                    mma_tf32(tmem + (uint32_t)(h * kH), (t == 2 ? as : ab) + sa, (t == 1 ? ws : wb) + sw, idesc,
+                             (t > 0 || ks > 0) ? 1u : 0u);
+                }
+        }
+        tc::mma_commit(bar);
+        if (!tc::mbar_wait_bounded(bar, phase, polls)) {
+            *abort_flag = 1;
+            atomicExch(&g_dense_status, 1);
+        }
+    }
+    __syncthreads();
+    if (*abort_flag) return false;
+    phase ^= 1u;
+    tc::fence_after_sync();
+    // 3. epilogue: x y z and b0 terms, ReLU, the 128 -> 1 layer
     const uint32_t taddr = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(half * kH);
-    uint32_t phase = 0;
+    float o = 0.f;
+#pragma unroll 1
+    for (int c = 0; c < kH / 32; ++c) {
+        float v[32];
+        tc::tmem_load32(taddr + (uint32_t)(32 * c), v);
+#pragma unroll
+        for (int e = 0; e < 32; ++e) {
+            const float4 u = su[32 * c + e];
+            const float z = fmaf(u.x, px, fmaf(u.y, py, fmaf(u.z, pz, v[e] + u.w)));
+            o = fmaf(sw1[32 * c + e], fmaxf(z, 0.f), o);
+        }
+    }
+    out = o + m.b1[L][0];
+    tc::fence_before_sync();
+    return true;
+}
 
+// Block teardown: lets an issued product finish after a wait gave up, then
+// frees the TMEM columns.
+__device__ __forceinline__ void f32tc_teardown(uint8_t *sm, uint32_t tmem, uint32_t phase) {
+    using namespace f32tc;
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(sm + kAbort);
+    if (*abort_flag && threadIdx.x == 0)
+        tc::mbar_wait_bounded(reinterpret_cast<uint64_t *>(sm + kBar), phase, 1u << 22);
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if ((threadIdx.x >> 5) == 0) tc::tmem_dealloc(tmem, kCols);
+}
+
+__global__ void __launch_bounds__(f32tc::kThreads, 2)
+    sdf_fwd_f32_tc_kernel(const nglod_dense_model m, const float *__restrict__ x, int64_t n, int L,
+                          float *__restrict__ out, uint32_t polls) {
+    using namespace f32tc;
+    extern __shared__ __align__(1024) uint8_t smem_f32tc[];
+    uint8_t *sm = smem_f32tc;
+    const int tid = threadIdx.x;
+    const uint32_t tmem = f32tc_setup(m, L, sm, tid);
+    uint32_t phase = 0;
     for (int64_t q = blockIdx.x; q * kThreads < n; q += gridDim.x) {
         const int64_t i = q * kThreads + tid;
         float px = 0.f, py = 0.f, pz = 0.f;
@@ -161,70 +251,12 @@ __global__ void __launch_bounds__(f32tc::kThreads, 2)
             py = x[3 * i + 1];
             pz = x[3 * i + 2];
         }
-        // 1. gather: LOD sum of the warp's 32 points, written as tile rows
-        float4 acc[8];
-#pragma unroll
-        for (int p = 0; p < 8; ++p) acc[p] = make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll 1
-        for (int l = 0; l <= L; ++l)
-            gather_warp_add_f32(static_cast<const float *>(m.grid[l]), volume_side(m, l), px, py, pz, lane, acc);
-#pragma unroll
-        for (int p = 0; p < 8; ++p)
-            store_split4(abig, asmall, a_offset(quad * 32 + 4 * p + (lane >> 3), 4 * (lane & 7)), acc[p]);
-        tc::fence_proxy_async_smem();
-        tc::fence_before_sync();
-        __syncthreads();
-        // 2. one thread issues big*big + big*small + small*big for both tiles
-        if (tid == 0) {
-            tc::fence_after_sync();
-            const uint64_t wb = tc::smem_desc(sbase + (uint32_t)kW, 128, kKC * 128);
-            const uint64_t ws = tc::smem_desc(sbase + (uint32_t)(kW + kTile), 128, kKC * 128);
-#pragma unroll
-            for (int h = 0; h < kTiles; ++h) {
-                const uint64_t ab = tc::smem_desc(sbase + (uint32_t)(kA + 2 * h * kTileA), kLboA, kSboA);
-                const uint64_t as = tc::smem_desc(sbase + (uint32_t)(kA + (2 * h + 1) * kTileA), kLboA, kSboA);
-#pragma unroll
-                for (int t = 0; t < 3; ++t)
-#pragma unroll
-                    for (int ks = 0; ks < kK / 8; ++ks) {
-                        // 8 tf32 of K: two core matrices of each operand
-                        const uint64_t sa = (uint64_t)((ks * 2 * kLboA) >> 4), sw = (uint64_t)((ks * 256) >> 4);
-                        mma_tf32(tmem + (uint32_t)(h * kH), (t == 2 ? as : ab) + sa, (t == 1 ? ws : wb) + sw,
-                                 idesc, (t > 0 || ks > 0) ? 1u : 0u);
-                    }
-            }
-            tc::mma_commit(bar);
-            if (!tc::mbar_wait_bounded(bar, phase, polls)) {
-                *abort_flag = 1;
-                atomicExch(&g_dense_status, 1);
-            }
-        }
-        __syncthreads();
-        if (*abort_flag) break;
-        phase ^= 1u;
-        tc::fence_after_sync();
-        // 3. epilogue: x y z and b0 terms, ReLU, the 128 -> 1 layer
-        float o = 0.f;
-#pragma unroll 1
-        for (int c = 0; c < kH / 32; ++c) {
-            float v[32];
-            tc::tmem_load32(taddr + (uint32_t)(32 * c), v);
-#pragma unroll
-            for (int e = 0; e < 32; ++e) {
-                const float4 u = su[32 * c + e];
-                const float z = fmaf(u.x, px, fmaf(u.y, py, fmaf(u.z, pz, v[e] + u.w)));
-                o = fmaf(sw1[32 * c + e], fmaxf(z, 0.f), o);
-            }
-        }
-        if (i < n) out[i] = o + b1;
-        tc::fence_before_sync();
+        float o;
+        if (!f32tc_decode(m, L, px, py, pz, sm, tmem, phase, polls, o)) break;
+        if (i < n) out[i] = o;
         __syncthreads();
     }
-    if (*abort_flag && tid == 0) tc::mbar_wait_bounded(bar, phase, 1u << 22);  // let an in-flight product finish
-    tc::fence_before_sync();
-    __syncthreads();
-    tc::fence_after_sync();
-    if (warp == 0) tc::tmem_dealloc(tmem, kCols);
+    f32tc_teardown(sm, tmem, phase);
 }
 
 // One feature volume sampled at every point: out[n][C] (FeatureVolume.forward).
@@ -512,6 +544,148 @@ __global__ void __launch_bounds__(128) trace_f32_kernel(const TraceArgs a) {
     }
 }
 
+// The persistent float32 tracer with the tensor-core decode (hidden 128):
+// trace_f32_kernel's state machine (SphereTracer.py:74-130) per thread, and
+// every iteration the block's 256 query points (march points or normal taps)
+// evaluated together by f32tc_decode, the float32 query kernel's arithmetic,
+// so each evaluation gives the same bits as nglod_sdf_fwd at that point.
+__global__ void __launch_bounds__(f32tc::kThreads, 2) trace_f32_tc_kernel(const TraceArgs a, uint32_t polls) {
+    extern __shared__ __align__(1024) uint8_t smem_tr[];
+    uint8_t *sm = smem_tr;
+    const uint32_t tmem = f32tc_setup(a.m, a.L, sm, threadIdx.x);
+    uint32_t mphase = 0;
+
+    const unsigned FULL = 0xffffffffu;
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    const float h = 1.0f / 192.0f;
+    const float twoh = (float)(2.0 / 192.0);
+
+    int phase = kNeed, step = 0;
+    int64_t ray = 0;
+    float ox = 0.f, oy = 0.f, oz = 0.f, dx = 0.f, dy = 0.f, dz = 0.f;
+    float xx = 0.f, xy = 0.f, xz = 0.f, t = 0.f, d = 0.f, dprev = 0.f;
+    float g[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    float nx = 0.f, ny = 0.f, nz = 0.f;
+    bool cond = false, hitr = false, hitf = false;
+
+    auto finish = [&]() {
+        hitf = hitr && !(fabsf(xx) > 1.f || fabsf(xy) > 1.f || fabsf(xz) > 1.f);
+        phase = (hitf && a.p.want_normals) ? kTap0 : kDone;
+    };
+    auto march_decide = [&]() {
+        if (step >= a.p.num_steps) {
+            finish();
+            return;
+        }
+        hitr = fabsf(t) < a.p.far_clip;
+        cond = cond && (fabsf(d) > a.p.min_dis) && (fabsf((d + dprev) / 2.f) > a.p.osc_dis) && hitr;
+        if (!cond) {
+            finish();
+            return;
+        }
+        xx = __fadd_rn(ox, __fmul_rn(dx, t));
+        xy = __fadd_rn(oy, __fmul_rn(dy, t));
+        xz = __fadd_rn(oz, __fmul_rn(dz, t));
+        dprev = d;
+        phase = kMarch;
+    };
+
+    for (;;) {
+        for (;;) {
+            if (phase == kDone) {
+                a.x[3 * ray + 0] = xx;
+                a.x[3 * ray + 1] = xy;
+                a.x[3 * ray + 2] = xz;
+                a.t[ray] = t;
+                a.hit[ray] = hitf ? 1 : 0;
+                if (a.normal) {
+                    const bool hn = hitf && a.p.want_normals;
+                    a.normal[3 * ray + 0] = hn ? nx : 0.f;
+                    a.normal[3 * ray + 1] = hn ? ny : 0.f;
+                    a.normal[3 * ray + 2] = hn ? nz : 0.f;
+                }
+                phase = kNeed;
+            }
+            const unsigned need = __ballot_sync(FULL, phase == kNeed);
+            if (need == 0u) break;
+            const int leader = __ffs(need) - 1;
+            unsigned long long base = 0ull;
+            if ((int)lane == leader) base = atomicAdd(a.counter, (unsigned long long)__popc(need));
+            base = __shfl_sync(FULL, base, leader);
+            if (phase == kNeed) {
+                const unsigned long long r = base + (unsigned long long)__popc(need & lt_mask);
+                if (r >= (unsigned long long)a.n) {
+                    phase = kGone;
+                } else {
+                    ray = (int64_t)r;
+                    ox = a.ray_o[3 * ray];
+                    oy = a.ray_o[3 * ray + 1];
+                    oz = a.ray_o[3 * ray + 2];
+                    dx = a.ray_d[3 * ray];
+                    dy = a.ray_d[3 * ray + 1];
+                    dz = a.ray_d[3 * ray + 2];
+                    t = 0.f;
+                    cond = box_entry(ox, oy, oz, dx, dy, dz, t);
+                    xx = cond ? fmaf(dx, t, ox) : ox;
+                    xy = cond ? fmaf(dy, t, oy) : oy;
+                    xz = cond ? fmaf(dz, t, oz) : oz;
+                    step = 0;
+                    hitr = false;
+                    hitf = false;
+                    if (cond)
+                        phase = kEvalInit;
+                    else
+                        march_decide();
+                }
+            }
+        }
+        if (__syncthreads_and(phase == kGone)) break;
+
+        float qx = xx, qy = xy, qz = xz;
+        if (phase >= kTap0 && phase < kDone) {
+            const int k = phase - kTap0;
+            const float e = (k & 1) ? -h : h;
+            if ((k >> 1) == 0) qx = __fadd_rn(xx, e);
+            else if ((k >> 1) == 1) qy = __fadd_rn(xy, e);
+            else qz = __fadd_rn(xz, e);
+        }
+        if (phase == kGone) qx = qy = qz = 0.f;
+        float v;
+        if (!f32tc_decode(a.m, a.L, qx, qy, qz, sm, tmem, mphase, polls, v)) break;
+
+        if (phase == kEvalInit) {
+            d = v;
+            dprev = d;
+            march_decide();
+        } else if (phase == kMarch) {
+            d = v * a.p.step_size;
+            t = t + d;
+            ++step;
+            march_decide();
+        } else if (phase >= kTap0 && phase < kDone) {
+            const int k = phase - kTap0;
+#pragma unroll
+            for (int i = 0; i < 6; ++i)
+                if (i == k) g[i] = v;
+            if (k == 5) {
+                const float gx = (g[0] - g[1]) / twoh;
+                const float gy = (g[2] - g[3]) / twoh;
+                const float gz = (g[4] - g[5]) / twoh;
+                const float nrm = sqrtf(gx * gx + gy * gy + gz * gz);
+                const float den = fmaxf(nrm, 1e-5f);
+                nx = gx / den;
+                ny = gy / den;
+                nz = gz / den;
+                phase = kDone;
+            } else {
+                phase = phase + 1;
+            }
+        }
+    }
+    f32tc_teardown(sm, tmem, mphase);
+}
+
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
@@ -650,14 +824,23 @@ extern "C" int nglod_trace(const nglod_dense_model *model, const nglod_trace_par
     a.hit = hit;
     a.normal = normal;
     a.counter = reinterpret_cast<unsigned long long *>(work_counter);
+    NGLOD_TRY(cuda_status(cudaMemsetAsync(work_counter, 0, sizeof(int64_t), (cudaStream_t)stream),
+                          "nglod_trace counter reset"));
+    if (model->hidden_dim == f32tc::kH) {
+        // tensor-core decode, 256 rays per block, two blocks per SM
+        NGLOD_TRY(prepare_smem(trace_f32_tc_kernel, f32tc::kSmem));
+        const int64_t want = (n + f32tc::kThreads - 1) / f32tc::kThreads;
+        const int64_t cap = (int64_t)num_sms() * 2;
+        trace_f32_tc_kernel<<<(int)(want < cap ? want : cap), f32tc::kThreads, f32tc::kSmem, (cudaStream_t)stream>>>(
+            a, g_f32tc_wait_polls);
+        return launch_status("nglod_trace");
+    }
     const int threads = 128;
     // staged decoder, then one [32][kTRow] float transpose buffer per warp
     const size_t smem = (size_t)decoder_f4(model->hidden_dim) * sizeof(float4) + (size_t)threads * kTRow * sizeof(float);
     NGLOD_TRY(prepare_smem(trace_f32_kernel, smem));
     const int64_t want = (n + threads - 1) / threads;
     const int64_t cap = resident_blocks(trace_f32_kernel, threads, smem);
-    NGLOD_TRY(cuda_status(cudaMemsetAsync(work_counter, 0, sizeof(int64_t), (cudaStream_t)stream),
-                          "nglod_trace counter reset"));
     trace_f32_kernel<<<(int)(want < cap ? want : cap), threads, smem, (cudaStream_t)stream>>>(a);
     return launch_status("nglod_trace");
 }

@@ -178,9 +178,9 @@ class PlainSphereTracer(BaseTracer):
     """The reference's host-driven march (SphereTracer.py:41-132) on the GPU.
 
     Every step builds the active mask, synchronises on ``cond.any()``,
-    compacts the active points and calls the float32 sdf kernel on them: the
-    per-thread decoder form (nglod_sdf_fwd_simt), the arithmetic of the fused
-    float32 tracer, so that the two march identically.
+    compacts the active points and calls the float32 sdf kernel on them
+    (nglod_sdf_fwd), whose arithmetic the fused float32 tracer shares, so
+    that the two march identically.
 
     ``last_evaluations`` (a device int64 tensor) counts the sdf evaluations of
     the last frame: the first one of every ray, one per ray and march step,
@@ -196,11 +196,11 @@ class PlainSphereTracer(BaseTracer):
         x, t, cond = aabb(ray_o, ray_d)
         normal = torch.zeros_like(x)
         evals = torch.full((), x.shape[0], dtype=torch.int64, device=x.device)
-        simt = isinstance(net, OctreeSDF)
-        lod = net.lod if simt and net.lod is not None and 0 <= net.lod < net.num_lods else None
+        dense = isinstance(net, OctreeSDF)
+        lod = net.lod if dense and net.lod is not None and 0 <= net.lod < net.num_lods else None
 
         def f(p):
-            return net._sdf_infer(p, lod, False, simt=True) if simt else net(p)
+            return net._sdf_infer(p, lod, False) if dense else net(p)
 
         with torch.no_grad():
             d = f(x)
