@@ -76,58 +76,109 @@ constexpr int kThreads = kTP * kTiles;        // 256
 constexpr int kH = 128;                       // hidden units (UMMA N)
 constexpr int kK = 32;                        // feature channels along K
 constexpr int kKC = kK / 4;                   // 16-byte core-matrix columns
-// Point tiles (A) put their K-adjacent core matrices 144 B apart instead of
-// 128 B (the descriptor's LBO): the eight lanes of a quarter warp store one
-// row's eight 16-byte pieces, which then fall in eight different bank
-// groups (at 128 B they would all share four banks).  The weight tile (B) is
-// written once per block and keeps the dense layout.
-constexpr uint32_t kLboA = 144, kSboA = kKC * kLboA;  // 1152 B per 8-row group
-constexpr uint32_t kTileA = (kTP / 8) * kSboA;        // 18 KB
-constexpr uint32_t kTile = kTP * kK * 4;      // 16 KB
-constexpr size_t kA = 0;                      // tile h: big at kA + 2 h kTileA, small after it
-constexpr size_t kW = 2 * kTiles * kTileA;    // weights: big, then small
-constexpr size_t kU = kW + 2 * kTile;         // (w0[j][0..2], b0[j]) float4 [kH]
-constexpr size_t kW1 = kU + kH * 16;          // w1 [kH]
+// A point tile holds the first layer's whole input as TF32 parts: the 32
+// summed features, big and small, each a 128 x 32 K-major tile in the
+// 128-byte swizzled layout (tile_offset32_sw128: conflict-free row stores
+// without padding), and a 128 x 8 position tile [x y z big, 1, x y z small,
+// 0].  The weight side (dense K-major) is the feature part big and small and
+// two position tiles, [w_xyz big, b0 big, w_xyz big, 0] and [w_xyz small,
+// b0 small, 0 ...]: their two products with the position tile add
+// p.w + b0 as big*big + small*big + big*small, like the feature part's three
+// products, so the first layer lands in TMEM complete.
+constexpr uint32_t kTileF = kTP * kK * 4;                 // 16 KB
+constexpr uint32_t kTileP = kTP * 8 * 4;                  // 4 KB
+constexpr uint32_t kTileA = 2 * kTileF + kTileP;          // one point tile
+constexpr uint32_t kWBytes = 2 * kTileF + 2 * kTileP;     // the weight side
+constexpr size_t kA = 0;                      // tile h at kA + h kTileA
+constexpr size_t kW = kTiles * kTileA;
+constexpr size_t kW1 = kW + kWBytes;          // w1 [kH]
 constexpr size_t kBar = kW1 + kH * 4;
 constexpr size_t kSlot = kBar + 8, kAbort = kSlot + 4;
 constexpr size_t kSmem = kAbort + 12;
 constexpr uint32_t kCols = kTiles * kH;       // TMEM columns per block
-static_assert(kTile % 1024 == 0 && kTileA % 128 == 0 && kW % 1024 == 0 && kU % 16 == 0 && kBar % 8 == 0,
-              "shared layout alignment");
+static_assert(kTileF % 1024 == 0 && kTileA % 1024 == 0 && kW % 1024 == 0 && kBar % 8 == 0,
+              "swizzled tiles start on 1024-byte boundaries");
+static_assert(2 * (kSmem + 1024) <= 228 * 1024, "two blocks per SM");
 
-// Byte offset of element (row, k) in a point tile.
-__host__ __device__ constexpr uint32_t a_offset(int row, int k) {
-    return (uint32_t)((row / 8) * kSboA + (k / 4) * kLboA + (row % 8) * 16 + (k % 4) * 4);
-}
-static_assert(2 * kSmem <= 227 * 1024, "two blocks per SM");
+// Byte offset of position-tile element (row, k < 8): dense K-major, two
+// core-matrix columns.
+__host__ __device__ constexpr uint32_t pos_offset(int row, int k) { return tile_offset32(row, k, 2); }
 }  // namespace f32tc
 
-// Set by a tensor-core wait of sdf_fwd_f32_tc_kernel that gave up; read and
+// Set by a tensor-core wait of the float32 query or tracer that gave up; read and
 // cleared by nglod_dense_status.
 __device__ int g_dense_status = 0;
 // Bound of that wait (host side, all devices): kPolls unless a test of the
 // error path lowers it.
 static uint32_t g_f32tc_wait_polls = 1u << 22;
 
-// Block set-up of the tensor-core float32 decode: LOD L's weight tile
-// (feature part, split), x y z and b0 per unit, w1; TMEM columns; the
-// barrier.  Returns the TMEM base address.
+// Stages LOD L's decoder for the tensor-core float32 forms at w (the weight
+// side of f32tc: feature part big and small, then the two position tiles)
+// and w1 (w1 [128]).
+__device__ __forceinline__ void stage_tf32_decoder(const nglod_dense_model &m, int L, uint8_t *w, uint8_t *w1, int tid,
+                                                   int nthreads) {
+    using namespace f32tc;
+    const float *w0 = m.w0[L];
+    for (int q = tid; q < kH * kKC; q += nthreads) {
+        const int j = q / kKC, kc = q % kKC;
+        const float *r = w0 + j * 35 + 3 + 4 * kc;
+        store_split4(w, w + kTileF, tile_offset32(j, 4 * kc, kKC), make_float4(r[0], r[1], r[2], r[3]));
+    }
+    for (int j = tid; j < kH; j += nthreads) {
+        const float4 u = make_float4(w0[j * 35], w0[j * 35 + 1], w0[j * 35 + 2], m.b0[L][j]);
+        const float4 ub = make_float4(tf32_big(u.x), tf32_big(u.y), tf32_big(u.z), tf32_big(u.w));
+        uint8_t *pa = w + 2 * kTileF, *pb = pa + kTileP;
+        *reinterpret_cast<float4 *>(pa + pos_offset(j, 0)) = ub;
+        *reinterpret_cast<float4 *>(pa + pos_offset(j, 4)) = make_float4(ub.x, ub.y, ub.z, 0.f);
+        *reinterpret_cast<float4 *>(pb + pos_offset(j, 0)) = make_float4(u.x - ub.x, u.y - ub.y, u.z - ub.z, u.w - ub.w);
+        *reinterpret_cast<float4 *>(pb + pos_offset(j, 4)) = make_float4(0.f, 0.f, 0.f, 0.f);
+        reinterpret_cast<float *>(w1)[j] = m.w1[L][j];
+    }
+}
+
+// The rows of one point tile from a warp's cooperative LOD sums (lane holds
+// channels 4 (lane % 8) .. +3 of row row0 + 4 p + lane / 8 in acc[p]) and
+// from this thread's own point (row row0 + lane).
+__device__ __forceinline__ void store_point_rows(uint8_t *tile, int row0, int lane, const float4 (&acc)[8], float px,
+                                                 float py, float pz) {
+    using namespace f32tc;
+#pragma unroll
+    for (int p = 0; p < 8; ++p)
+        store_split4(tile, tile + kTileF, tile_offset32_sw128(row0 + 4 * p + (lane >> 3), 4 * (lane & 7)), acc[p]);
+    const float bx = tf32_big(px), by = tf32_big(py), bz = tf32_big(pz);
+    uint8_t *pt = tile + 2 * kTileF;
+    *reinterpret_cast<float4 *>(pt + pos_offset(row0 + lane, 0)) = make_float4(bx, by, bz, 1.f);
+    *reinterpret_cast<float4 *>(pt + pos_offset(row0 + lane, 4)) = make_float4(px - bx, py - by, pz - bz, 0.f);
+}
+
+// The first layer of one point tile (shared address a) against the staged
+// weights (shared address w) into TMEM columns d: the feature part's
+// big*big + big*small + small*big over K = 32 (four K steps of eight, 32
+// bytes along the swizzled line), then the two position products.
+__device__ __forceinline__ void issue_first_layer(uint32_t d, uint32_t a, uint32_t w) {
+    using namespace f32tc;
+    constexpr uint32_t idesc = idesc_tf32_f32(kTP, kH);
+    const uint64_t ab = smem_desc_sw128(a), as = smem_desc_sw128(a + kTileF);
+    const uint64_t wb = tc::smem_desc(w, 128, kKC * 128), ws = tc::smem_desc(w + kTileF, 128, kKC * 128);
+#pragma unroll
+    for (int t = 0; t < 3; ++t)
+#pragma unroll
+        for (int ks = 0; ks < kK / 8; ++ks)
+            mma_tf32(d, (t == 2 ? as : ab) + (uint64_t)(ks * 2), (t == 1 ? ws : wb) + (uint64_t)(ks * 16), idesc,
+                     (t > 0 || ks > 0) ? 1u : 0u);
+    const uint64_t ap = tc::smem_desc(a + 2 * kTileF, 128, 256);
+    mma_tf32(d, ap, tc::smem_desc(w + 2 * kTileF, 128, 256), idesc, 1u);
+    mma_tf32(d, ap, tc::smem_desc(w + 2 * kTileF + kTileP, 128, 256), idesc, 1u);
+}
+
+// Block set-up of the tensor-core float32 decode: LOD L's weight side and
+// w1, TMEM columns, the barrier.  Returns the TMEM base address.
 __device__ __forceinline__ uint32_t f32tc_setup(const nglod_dense_model &m, int L, uint8_t *sm, int tid) {
     using namespace f32tc;
     uint64_t *bar = reinterpret_cast<uint64_t *>(sm + kBar);
     uint32_t *slot = reinterpret_cast<uint32_t *>(sm + kSlot);
     volatile int *abort_flag = reinterpret_cast<volatile int *>(sm + kAbort);
-    const float *w0 = m.w0[L];
-    for (int u = tid; u < kH * kKC; u += kThreads) {
-        const int j = u / kKC, kc = u % kKC;
-        const float *r = w0 + j * 35 + 3 + 4 * kc;
-        store_split4(sm + kW, sm + kW + kTile, tile_offset32(j, 4 * kc, kKC), make_float4(r[0], r[1], r[2], r[3]));
-    }
-    if (tid < kH) {
-        reinterpret_cast<float4 *>(sm + kU)[tid] =
-            make_float4(w0[tid * 35], w0[tid * 35 + 1], w0[tid * 35 + 2], m.b0[L][tid]);
-        reinterpret_cast<float *>(sm + kW1)[tid] = m.w1[L][tid];
-    }
+    stage_tf32_decoder(m, L, sm + kW, sm + kW1, tid, kThreads);
     if ((tid >> 5) == 0) tc::tmem_alloc(slot, kCols);
     if (tid == 0) {
         tc::mbar_init(bar, 1);
@@ -142,7 +193,7 @@ __device__ __forceinline__ uint32_t f32tc_setup(const nglod_dense_model &m, int 
 
 // The sdf of the block's 256 points at LOD L, thread tid owning point
 // (px, py, pz) (warp w fills row 32 (w % 4) + lane of tile w / 4): the
-// warp-cooperative gather and LOD sum, the tile rows, one thread's 24
+// warp-cooperative gather and LOD sum, the tile rows, one thread's 28
 // split-TF32 MMAs for both tiles, and this thread's float32 epilogue.  Every
 // thread of the block calls it; false (for all of them) if the bounded
 // tensor-core wait gave up, which also sets g_dense_status.
@@ -154,10 +205,7 @@ __device__ __forceinline__ bool f32tc_decode(const nglod_dense_model &m, int L, 
     const int half = warp >> 2, quad = warp & 3;
     uint64_t *bar = reinterpret_cast<uint64_t *>(sm + kBar);
     volatile int *abort_flag = reinterpret_cast<volatile int *>(sm + kAbort);
-    const float4 *su = reinterpret_cast<const float4 *>(sm + kU);
     const float *sw1 = reinterpret_cast<const float *>(sm + kW1);
-    uint8_t *abig = sm + kA + (size_t)2 * half * kTileA;
-    uint8_t *asmall = abig + kTileA;
     // 1. gather: LOD sum of the warp's 32 points, written as tile rows
     float4 acc[8];
 #pragma unroll
@@ -165,33 +213,17 @@ __device__ __forceinline__ bool f32tc_decode(const nglod_dense_model &m, int L, 
 #pragma unroll 1
     for (int l = 0; l <= L; ++l)
         gather_warp_add_f32(static_cast<const float *>(m.grid[l]), volume_side(m, l), px, py, pz, lane, acc);
-#pragma unroll
-    for (int p = 0; p < 8; ++p)
-        store_split4(abig, asmall, a_offset(quad * 32 + 4 * p + (lane >> 3), 4 * (lane & 7)), acc[p]);
+    store_point_rows(sm + kA + (size_t)half * kTileA, quad * 32, lane, acc, px, py, pz);
     tc::fence_proxy_async_smem();
     tc::fence_before_sync();
     __syncthreads();
-    // 2. one thread issues big*big + big*small + small*big for both tiles
+    // 2. one thread issues both tiles' first layers
     if (tid == 0) {
         tc::fence_after_sync();
         const uint32_t sbase = tc::smem_addr(sm);
-        constexpr uint32_t idesc = idesc_tf32_f32(kTP, kH);
-        const uint64_t wb = tc::smem_desc(sbase + (uint32_t)kW, 128, kKC * 128);
-        const uint64_t ws = tc::smem_desc(sbase + (uint32_t)(kW + kTile), 128, kKC * 128);
 #pragma unroll
-        for (int h = 0; h < kTiles; ++h) {
-            const uint64_t ab = tc::smem_desc(sbase + (uint32_t)(kA + 2 * h * kTileA), kLboA, kSboA);
-            const uint64_t as = tc::smem_desc(sbase + (uint32_t)(kA + (2 * h + 1) * kTileA), kLboA, kSboA);
-#pragma unroll
-            for (int t = 0; t < 3; ++t)
-#pragma unroll
-                for (int ks = 0; ks < kK / 8; ++ks) {
-                    // 8 tf32 of K: two core matrices of each operand
-                    const uint64_t sa = (uint64_t)((ks * 2 * kLboA) >> 4), sw = (uint64_t)((ks * 256) >> 4);
-                    mma_tf32(tmem + (uint32_t)(h * kH), (t == 2 ? as : ab) + sa, (t == 1 ? ws : wb) + sw, idesc,
-                             (t > 0 || ks > 0) ? 1u : 0u);
-                }
-        }
+        for (int h = 0; h < kTiles; ++h)
+            issue_first_layer(tmem + (uint32_t)(h * kH), sbase + (uint32_t)(kA + h * kTileA), sbase + (uint32_t)kW);
         tc::mma_commit(bar);
         if (!tc::mbar_wait_bounded(bar, phase, polls)) {
             *abort_flag = 1;
@@ -202,21 +234,9 @@ __device__ __forceinline__ bool f32tc_decode(const nglod_dense_model &m, int L, 
     if (*abort_flag) return false;
     phase ^= 1u;
     tc::fence_after_sync();
-    // 3. epilogue: x y z and b0 terms, ReLU, the 128 -> 1 layer
+    // 3. epilogue: ReLU and the 128 -> 1 layer on this thread's TMEM row
     const uint32_t taddr = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(half * kH);
-    float o = 0.f;
-#pragma unroll 1
-    for (int c = 0; c < kH / 32; ++c) {
-        float v[32];
-        tc::tmem_load32(taddr + (uint32_t)(32 * c), v);
-#pragma unroll
-        for (int e = 0; e < 32; ++e) {
-            const float4 u = su[32 * c + e];
-            const float z = fmaf(u.x, px, fmaf(u.y, py, fmaf(u.z, pz, v[e] + u.w)));
-            o = fmaf(sw1[32 * c + e], fmaxf(z, 0.f), o);
-        }
-    }
-    out = o + m.b1[L][0];
+    out = relu_dot_w1_f32(taddr, sw1) + m.b1[L][0];
     tc::fence_before_sync();
     return true;
 }
@@ -234,29 +254,183 @@ __device__ __forceinline__ void f32tc_teardown(uint8_t *sm, uint32_t tmem, uint3
     if ((threadIdx.x >> 5) == 0) tc::tmem_dealloc(tmem, kCols);
 }
 
-__global__ void __launch_bounds__(f32tc::kThreads, 2)
-    sdf_fwd_f32_tc_kernel(const nglod_dense_model m, const float *__restrict__ x, int64_t n, int L,
-                          float *__restrict__ out, uint32_t polls) {
-    using namespace f32tc;
-    extern __shared__ __align__(1024) uint8_t smem_f32tc[];
-    uint8_t *sm = smem_f32tc;
-    const int tid = threadIdx.x;
-    const uint32_t tmem = f32tc_setup(m, L, sm, tid);
+// ---------------------------------------------------------------------------
+// sdf forward, tensor-core form with the coarse volumes in shared memory
+// ---------------------------------------------------------------------------
+// The point query of the tensor-core form (the gather, tile rows, product
+// and epilogue of f32tc_decode, bit-identical results) as one persistent
+// 16-warp block per SM.  The leading LODs whose volumes fit beside the tiles
+// (5^3 and 9^3 vertices, 109 KB, at base_lod 2) are copied into shared
+// memory once per block and gathered from there; only the finer LODs' corner
+// lines come through L2.
+//
+// The block is four independent groups of four warps; group g decodes
+// 128-point tiles g, g + 4, ... of the block's share into its own 128 TMEM
+// columns (4 x 128 = the SM's 512).  A group gathers its tile in registers,
+// takes one of two shared point-tile buffers (a lock per buffer), writes the
+// split rows, and its first thread issues the tile's 14 MMAs and waits for
+// them; the buffer is released as soon as the product is done and the group
+// runs its epilogue while the others gather.  Groups meet only at their own
+// named barrier (id 1 + g, 128 threads), never at a block barrier.
+namespace f32st {
+constexpr int kGroups = 4;
+constexpr int kThreads = f32tc::kTP * kGroups;  // 512
+constexpr int kStages = 2;                      // point-tile buffers
+constexpr size_t kA = 0;                        // buffer b at kA + b f32tc::kTileA
+constexpr size_t kW = (size_t)kStages * f32tc::kTileA;
+constexpr size_t kW1 = kW + f32tc::kWBytes;
+constexpr size_t kBar = kW1 + f32tc::kH * 4;    // one mbarrier per group
+constexpr size_t kLock = kBar + 8 * kGroups;    // int per buffer: 1 = taken
+constexpr size_t kSel = kLock + 4 * kStages;    // int per group: its buffer, or -1
+constexpr size_t kOk = kSel + 4 * kGroups;      // int per group: product done
+constexpr size_t kSlot = kOk + 4 * kGroups;
+constexpr size_t kAbort = kSlot + 4;
+constexpr size_t kVol = (kAbort + 4 + 127) & ~(size_t)127;  // staged volumes
+constexpr size_t kSmemMax = 227 * 1024;
+constexpr size_t kVolBudget = kSmemMax - kVol;
+// More than half of an SM's shared memory: one block per SM (its 512 TMEM
+// columns are the SM's whole tensor memory).
+constexpr size_t kSmemMin = 120 * 1024;
+constexpr uint32_t kCols = kGroups * f32tc::kH;
+static_assert(kW % 1024 == 0 && kBar % 8 == 0 && kVol % 128 == 0, "shared layout alignment");
+static_assert(kVol + 109312 <= kSmemMax, "levels 5^3 and 9^3 fit");
+}  // namespace f32st
+
+__device__ __forceinline__ void group_sync(int g) {
+    asm volatile("bar.sync %0, %1;" ::"r"(1 + g), "n"(f32tc::kTP) : "memory");
+}
+
+// Takes a free point-tile buffer; -1 once the block is aborting, or (which
+// also aborts it) if none came free within 2^22 tries.  A buffer is held only
+// from its rows' stores to the end of its product.
+__device__ __forceinline__ int acquire_tile_buffer(int *locks, volatile int *abort_flag) {
+    for (uint32_t k = 0; k < (1u << 22); ++k) {
+        if (*abort_flag) return -1;
+#pragma unroll
+        for (int b = 0; b < f32st::kStages; ++b)
+            if (atomicCAS(&locks[b], 0, 1) == 0) {
+                __threadfence_block();
+                return b;
+            }
+        if (k > 16) __nanosleep(32);
+    }
+    *abort_flag = 1;
+    atomicExch(&g_dense_status, 1);
+    return -1;
+}
+
+__global__ void __launch_bounds__(f32st::kThreads, 1)
+    sdf_fwd_f32_staged_kernel(const nglod_dense_model m, const float *__restrict__ x, int64_t n, int L, int staged,
+                              float *__restrict__ out, uint32_t polls) {
+    using namespace f32st;
+    using f32tc::kH;
+    using f32tc::kTileA;
+    using f32tc::kTP;
+    extern __shared__ __align__(1024) uint8_t smem_f32st[];
+    uint8_t *sm = smem_f32st;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int grp = warp >> 2, quad = warp & 3, gtid = tid & (kTP - 1);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(sm + kBar) + grp;
+    int *locks = reinterpret_cast<int *>(sm + kLock);
+    volatile int *sel = reinterpret_cast<volatile int *>(sm + kSel) + grp;
+    volatile int *okf = reinterpret_cast<volatile int *>(sm + kOk) + grp;
+    uint32_t *slot = reinterpret_cast<uint32_t *>(sm + kSlot);
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(sm + kAbort);
+    const float *sw1 = reinterpret_cast<const float *>(sm + kW1);
+
+    // set-up: decoder, staged volumes, TMEM, barriers and locks
+    stage_tf32_decoder(m, L, sm + kW, sm + kW1, tid, kThreads);
+    {
+        size_t off = kVol;
+        for (int l = 0; l < staged; ++l) {
+            const int s = volume_side(m, l);
+            const int cnt = s * s * s * (kC / 4);
+            const float4 *src = static_cast<const float4 *>(m.grid[l]);
+            float4 *dst = reinterpret_cast<float4 *>(sm + off);
+            for (int q = tid; q < cnt; q += kThreads) dst[q] = __ldg(src + q);
+            off += (size_t)cnt * 16;
+        }
+    }
+    if (warp == 0) tc::tmem_alloc(slot, kCols);
+    if (tid == 0) {
+        for (int g = 0; g < kGroups; ++g) tc::mbar_init(reinterpret_cast<uint64_t *>(sm + kBar) + g, 1);
+        for (int b = 0; b < kStages; ++b) locks[b] = 0;
+        *abort_flag = 0;
+    }
+    tc::fence_proxy_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = *slot;
+    const uint32_t sbase = tc::smem_addr(sm);
+    const uint32_t dcol = tmem + (uint32_t)(grp * kH);
     uint32_t phase = 0;
-    for (int64_t q = blockIdx.x; q * kThreads < n; q += gridDim.x) {
-        const int64_t i = q * kThreads + tid;
+    bool pending = false;  // group leader: an issued product whose completion it did not see
+
+    for (int64_t t = (int64_t)blockIdx.x * kGroups + grp; t * kTP < n; t += (int64_t)gridDim.x * kGroups) {
+        const int64_t i = t * kTP + gtid;
         float px = 0.f, py = 0.f, pz = 0.f;
         if (i < n) {
             px = x[3 * i];
             py = x[3 * i + 1];
             pz = x[3 * i + 2];
         }
-        float o;
-        if (!f32tc_decode(m, L, px, py, pz, sm, tmem, phase, polls, o)) break;
-        if (i < n) out[i] = o;
-        __syncthreads();
+        // 1. gather and LOD sum of the warp's 32 points (rows 32 quad ..)
+        float4 acc[8];
+#pragma unroll
+        for (int p = 0; p < 8; ++p) acc[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+        uint32_t vaddr = sbase + (uint32_t)kVol;
+#pragma unroll 1
+        for (int l = 0; l <= L; ++l) {
+            const int s = volume_side(m, l);
+            if (l < staged) {
+                gather_warp_add_f32_shared(vaddr, s, px, py, pz, lane, acc);
+                vaddr += (uint32_t)(s * s * s) * 128u;
+            } else {
+                gather_warp_add_f32(static_cast<const float *>(m.grid[l]), s, px, py, pz, lane, acc);
+            }
+        }
+        // 2. a point-tile buffer, the split rows
+        if (gtid == 0) *sel = acquire_tile_buffer(locks, abort_flag);
+        group_sync(grp);
+        const int b = *sel;
+        if (b < 0) break;
+        store_point_rows(sm + kA + (size_t)b * kTileA, quad * 32, lane, acc, px, py, pz);
+        tc::fence_proxy_async_smem();
+        tc::fence_before_sync();
+        group_sync(grp);
+        // 3. the leader issues the tile's first layer and waits for it
+        if (gtid == 0) {
+            tc::fence_after_sync();
+            issue_first_layer(dcol, sbase + (uint32_t)(kA + b * kTileA), sbase + (uint32_t)kW);
+            tc::mma_commit(bar);
+            const bool ok = tc::mbar_wait_bounded(bar, phase, polls);
+            if (ok) {
+                __threadfence_block();
+                atomicExch(&locks[b], 0);
+            } else {
+                pending = true;
+                *abort_flag = 1;
+                atomicExch(&g_dense_status, 1);
+            }
+            *okf = ok ? 1 : 0;
+        }
+        group_sync(grp);
+        if (!*okf) break;
+        phase ^= 1u;
+        tc::fence_after_sync();
+        // 4. epilogue on this thread's TMEM row
+        const float o = relu_dot_w1_f32(dcol + ((uint32_t)(quad * 32) << 16), sw1);
+        if (i < n) out[i] = o + m.b1[L][0];
+        tc::fence_before_sync();
     }
-    f32tc_teardown(sm, tmem, phase);
+    // teardown: a product still in flight after a wait gave up finishes
+    // before the columns are freed
+    if (gtid == 0 && pending) tc::mbar_wait_bounded(bar, phase, 1u << 22);
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if (warp == 0) tc::tmem_dealloc(tmem, kCols);
 }
 
 // One feature volume sampled at every point: out[n][C] (FeatureVolume.forward).
@@ -732,12 +906,23 @@ static int sdf_fwd_f32(const nglod_dense_model *model, const float *x, int64_t n
     if (n == 0) return NGLOD_OK;
     NGLOD_REQUIRE(x && out, NGLOD_ERR_INVALID, "null pointer argument");
     if (!all_lods && !simt && model->hidden_dim == f32tc::kH) {
-        auto k = sdf_fwd_f32_tc_kernel;
-        NGLOD_TRY(prepare_smem(k, f32tc::kSmem));
-        const int64_t want = (n + f32tc::kThreads - 1) / f32tc::kThreads;
-        const int64_t cap = (int64_t)num_sms() * 2;
-        k<<<(int)(want < cap ? want : cap), f32tc::kThreads, f32tc::kSmem, stream>>>(*model, x, n, L, out,
-                                                                                   g_f32tc_wait_polls);
+        // the leading volumes that fit beside the tiles are staged
+        int staged = 0;
+        size_t vbytes = 0;
+        for (int l = 0; l <= L; ++l) {
+            const size_t s = (size_t)(1 << (l + model->base_lod)) + 1;
+            if (vbytes + s * s * s * kC * 4 > f32st::kVolBudget) break;
+            vbytes += s * s * s * kC * 4;
+            ++staged;
+        }
+        const size_t smem = f32st::kVol + vbytes < f32st::kSmemMin ? f32st::kSmemMin : f32st::kVol + vbytes;
+        auto k = sdf_fwd_f32_staged_kernel;
+        NGLOD_TRY(prepare_smem(k, smem));
+        const int64_t tiles = (n + f32tc::kTP - 1) / f32tc::kTP;
+        const int64_t want = (tiles + f32st::kGroups - 1) / f32st::kGroups;
+        const int64_t cap = (int64_t)num_sms();
+        k<<<(int)(want < cap ? want : cap), f32st::kThreads, smem, stream>>>(*model, x, n, L, staged, out,
+                                                                           g_f32tc_wait_polls);
         return launch_status("nglod_sdf_fwd");
     }
     const int threads = 256;

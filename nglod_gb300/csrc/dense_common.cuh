@@ -58,9 +58,12 @@ __device__ __forceinline__ void stage_decoder(float4 *dst, const nglod_dense_mod
 // the corner offsets and weights themselves (shuffling the corner index and
 // the eight weights instead takes nine shuffles, which load the shared-memory
 // crossbar the tensor-core kernels also use).  acc[p] += this lane's four
-// channels of point 4p + lane / 8.
-__device__ __forceinline__ void gather_warp_add_f32(const float *__restrict__ g, int s, float px, float py, float pz,
-                                                    int lane, float4 (&acc)[8]) {
+// channels of point 4p + lane / 8.  load(i) returns float4 i of the volume
+// (eight per vertex); gather_warp_add_f32 reads global memory,
+// gather_warp_add_f32_shared a volume staged in shared memory.
+template <typename Load>
+__device__ __forceinline__ void gather_warp_add_f32_by(Load load, int s, float px, float py, float pz, int lane,
+                                                       float4 (&acc)[8]) {
     const unsigned FULL = 0xffffffffu;
     const float sm1 = (float)(s - 1);
     float ix = ((px + 1.f) / 2.f) * sm1;
@@ -69,7 +72,7 @@ __device__ __forceinline__ void gather_warp_add_f32(const float *__restrict__ g,
     ix = fminf(sm1, fmaxf(ix, 0.f));
     iy = fminf(sm1, fmaxf(iy, 0.f));
     iz = fminf(sm1, fmaxf(iz, 0.f));
-    const float4 *g4 = reinterpret_cast<const float4 *>(g) + (lane & 7);  // 8 float4 per vertex
+    const int part = lane & 7;  // this lane's float4 of a vertex
     const int sy = s * 8, sz = s * sy;
 #pragma unroll
     for (int p = 0; p < 8; ++p) {
@@ -99,7 +102,7 @@ __device__ __forceinline__ void gather_warp_add_f32(const float *__restrict__ g,
         const int o[8] = {o0, o0 + ox, o0 + oy, o0 + oy + ox, o0 + oz, o0 + oz + ox, o0 + oz + oy, o0 + oz + oy + ox};
         float4 v[8];
 #pragma unroll
-        for (int k = 0; k < 8; ++k) v[k] = __ldg(g4 + o[k]);
+        for (int k = 0; k < 8; ++k) v[k] = load(o[k] + part);
         float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
@@ -113,6 +116,27 @@ __device__ __forceinline__ void gather_warp_add_f32(const float *__restrict__ g,
         acc[p].z += a2;
         acc[p].w += a3;
     }
+}
+
+__device__ __forceinline__ void gather_warp_add_f32(const float *__restrict__ g, int s, float px, float py, float pz,
+                                                    int lane, float4 (&acc)[8]) {
+    const float4 *g4 = reinterpret_cast<const float4 *>(g);
+    gather_warp_add_f32_by([g4](int i) { return __ldg(g4 + i); }, s, px, py, pz, lane, acc);
+}
+
+// 16-byte load from a shared-memory address.
+__device__ __forceinline__ float4 ld_shared_f4(uint32_t addr) {
+    float4 v;
+    asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "r"(addr));
+    return v;
+}
+
+// The same gather from a volume staged in shared memory at address `base`
+// (channel-last, 128 B per vertex).
+__device__ __forceinline__ void gather_warp_add_f32_shared(uint32_t base, int s, float px, float py, float pz,
+                                                           int lane, float4 (&acc)[8]) {
+    gather_warp_add_f32_by([base](int i) { return ld_shared_f4(base + 16u * (uint32_t)i); }, s, px, py, pz, lane,
+                           acc);
 }
 
 // Row stride (floats) of the per-warp transpose buffer: 36, so that the
