@@ -81,17 +81,21 @@ TRAIN_BATCH = 524_288
 
 # Per-query work of OctreeSDF.sdf at lod L (5 LODs at L = 4), float32:
 # HBM: 12 B point in + 4 B distance out (volumes once per launch);
-# gathered corner bytes: 8 corners x 32 channels x 4 B per LOD;
+# gathered corner bytes: 8 corners x 32 channels x 4 B per LOD, of which the
+# query kernel reads LODs 0 and 1 (5^3 and 9^3 vertices) from shared memory
+# (F32_STAGED_BYTES) and the rest through L2;
 # FLOP: 2 per corner-channel of the trilinear sums, 2*(35*128 + 128) for the
 # hidden layer with its bias, 2*128 for the output layer (F32_FLOP, the
-# per-thread decoder's count).  The tensor-core form runs the hidden layer's
-# 32 x 128 feature product as three TF32 products (F32_TC_FLOP on the tensor
-# pipe) and the rest on the float32 pipe (F32_SIMT_FLOP: the trilinear sums
-# and, per hidden unit, x y z and bias terms, ReLU and the output FMA).
+# per-thread decoder's count).  The tensor-core form runs the whole hidden
+# layer on the tensor pipe (F32_TC_FLOP: the 32 x 128 feature product as
+# three TF32 products and the x y z / bias product over 8 K columns as two)
+# and the rest on the float32 pipe (F32_SIMT_FLOP: the trilinear sums and,
+# per hidden unit, ReLU and the output FMA).
 F32_GATHER_BYTES = (LOD + 1) * 8 * 32 * 4
+F32_STAGED_BYTES = 2 * 8 * 32 * 4
 F32_FLOP = (LOD + 1) * 8 * 32 * 2 + 2 * (35 * 128 + 128) + 2 * 128
-F32_TC_FLOP = 3 * 2 * 32 * 128
-F32_SIMT_FLOP = (LOD + 1) * 8 * 32 * 2 + 128 * (2 * 4 + 2)
+F32_TC_FLOP = 3 * 2 * 32 * 128 + 2 * 2 * 8 * 128
+F32_SIMT_FLOP = (LOD + 1) * 8 * 32 * 2 + 128 * 3
 TF32_NOMINAL_TFLOPS = 1100.0
 
 # DRAM traffic of single ncu captures of the headline kernels on this
@@ -100,7 +104,7 @@ TF32_NOMINAL_TFLOPS = 1100.0
 # reported only while those sources are unchanged; otherwise the roofline's
 # traffic is null.
 NCU_CAPTURES = {
-    "sdf_fwd_f32_tc_kernel": {
+    "sdf_fwd_f32_staged_kernel": {
         "dram_bytes": 91_318_784 + 11_194_624, "points": N_POINTS,
         "sources": ["nglod_gb300/csrc/dense.cu", "nglod_gb300/csrc/dense_common.cuh",
                     "nglod_gb300/csrc/tf32_tile.cuh", "nglod_gb300/csrc/tc_common.cuh"],
@@ -302,6 +306,36 @@ def line_read_peak(dev, nbytes, reps=20):
     return blocks * 128 * loads * 32 / (best / 1e3) / 1e9
 
 
+def smem_read_peak(dev, reps=10):
+    """Measured rate of the SM's shared-memory / L1 data path for the float32
+    gather's line reads: random whole 128-byte lines of a shared-memory
+    buffer, eight lanes per line (nglod_measure_smem_reads), eight blocks of
+    256 threads per SM; GB/s, best of `reps`."""
+    from nglod_gb300 import _lib
+    sink = torch.zeros(1, dtype=torch.int32, device=dev)
+    blocks = torch.cuda.get_device_properties(dev).multi_processor_count * 8
+    loads = 2048
+    lib = _lib.load()
+
+    def go():
+        _lib.check(lib.nglod_measure_smem_reads(loads, blocks, _lib.ptr(sink), _lib.stream_ptr(dev)),
+                   "nglod_measure_smem_reads")
+
+    for _ in range(3):
+        go()
+    torch.cuda.synchronize()
+    best = float("inf")
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(reps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        go()
+        b.record(stream)
+        b.synchronize()
+        best = min(best, a.elapsed_time(b))
+    return blocks * 256 * 16 * loads / (best / 1e3) / 1e9
+
+
 def fma_peak(dev, reps=10):
     """Measured float32 FMA throughput of this device, TFLOP/s (nglod_measure_fma,
     eight blocks of 256 threads per SM; best of `reps`)."""
@@ -329,33 +363,42 @@ def fma_peak(dev, reps=10):
     return blocks * 256 * 16 * iters / (best / 1e3) / 1e12
 
 
-def f32_roofline(net, sec, points, dev, line_peak=None, fma_tflops=None):
-    """Roofline of sdf_fwd_f32_tc_kernel (the float32 query at hidden width
-    128) at lod 4 over `points` queries."""
+def f32_roofline(net, sec, points, dev, line_peak=None, fma_tflops=None, smem_peak=None):
+    """Roofline of sdf_fwd_f32_staged_kernel (the float32 query at hidden
+    width 128) at lod 4 over `points` queries."""
     pk = peaks()
     grid_bytes = sum(fv.fm.numel() * 4 for fv in net.features)
     if line_peak is None:
         line_peak = line_read_peak(dev, grid_bytes)
     if fma_tflops is None:
         fma_tflops = fma_peak(dev)
-    traffic, tnote = ncu_traffic("sdf_fwd_f32_tc_kernel", points)
+    if smem_peak is None:
+        smem_peak = smem_read_peak(dev)
+    traffic, tnote = ncu_traffic("sdf_fwd_f32_staged_kernel", points)
     terms = {
-        "gather_l2": (points * F32_GATHER_BYTES, line_peak, "GB/s",
+        "gather_l2": (points * (F32_GATHER_BYTES - F32_STAGED_BYTES), line_peak, "GB/s",
                       "measured live: random whole 128-byte lines of an L2-resident buffer the size of the "
                       "volumes (nglod_measure_line_reads)"),
+        "data_path": (points * F32_GATHER_BYTES, smem_peak, "GB/s",
+                      "measured live: random whole 128-byte lines of shared memory, eight lanes per line "
+                      "(nglod_measure_smem_reads)"),
         "hbm": (points * 16 + grid_bytes, pk["hbm_gbs"], "GB/s", f"{pk['source']} hbm_gbs (burst copy)"),
         "fp32_pipe": (points * F32_SIMT_FLOP, fma_tflops, "TFLOP/s",
                       "measured live: float32 FMA chains at full occupancy (nglod_measure_fma)"),
         "tensor": (points * F32_TC_FLOP, TF32_NOMINAL_TFLOPS, "TFLOP/s",
                    "nominal dense TF32 (no measured TF32 figure on this pool)"),
     }
-    return roofline("sdf_fwd_f32_tc_kernel", sec, terms,
-                    {"hbm_bytes": 16, "gathered_bytes": F32_GATHER_BYTES, "fp32_pipe_flop": F32_SIMT_FLOP,
+    return roofline("sdf_fwd_f32_staged_kernel", sec, terms,
+                    {"hbm_bytes": 16, "gathered_bytes": F32_GATHER_BYTES,
+                     "gathered_bytes_from_l2": F32_GATHER_BYTES - F32_STAGED_BYTES,
+                     "gathered_bytes_from_shared": F32_STAGED_BYTES, "fp32_pipe_flop": F32_SIMT_FLOP,
                      "tf32_tensor_flop": F32_TC_FLOP, "algorithmic_fp32_flop": F32_FLOP},
                     points, traffic, tnote,
-                    note="one launch reads each point once and the 40.5 MB of float32 volumes from HBM; the "
-                         "corner gathers (5,120 B per query, whole 128-byte vertex lines) are served by L2/L1; "
-                         "the decoder's feature product runs as three TF32 products on tcgen05")
+                    note="one launch reads each point once and the 40.5 MB of float32 volumes from HBM; each "
+                         "block stages the 5^3 and 9^3 volumes (109 KB) in shared memory, and the finer LODs' "
+                         "corner lines (3,072 B per query) come from L2; every corner line (5,120 B per query) "
+                         "passes the SM's shared-memory / L1 data path; the hidden layer runs on tcgen05 as "
+                         "split-TF32 products")
 
 
 def run_ours(args):
@@ -413,8 +456,10 @@ def run_ours(args):
 
     line_peak = line_read_peak(dev, sum(fv.fm.numel() * 4 for fv in net.features))
     fma_tflops = fma_peak(dev)
-    roof = f32_roofline(net, ms_per_step / 1e3, N_POINTS, dev, line_peak, fma_tflops)
-    roof["measured_ceilings"] = {"line_read_gbs": line_peak, "fp32_fma_tflops": fma_tflops}
+    smem_peak = smem_read_peak(dev)
+    roof = f32_roofline(net, ms_per_step / 1e3, N_POINTS, dev, line_peak, fma_tflops, smem_peak)
+    roof["measured_ceilings"] = {"line_read_gbs": line_peak, "fp32_fma_tflops": fma_tflops,
+                                 "smem_line_read_gbs": smem_peak}
 
     extras = {}
     trained = None

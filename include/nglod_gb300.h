@@ -244,6 +244,14 @@ int nglod_measure_line_reads(const void *buf, int64_t lines, int32_t loads, int3
  * the chains. */
 int nglod_measure_fma(int32_t iters, int32_t blocks, float *sink, nglod_stream_t stream);
 
+/* Measurement helper, no reference counterpart: `blocks` blocks of 256
+ * threads each read random whole 128-byte lines of a 32 KB shared-memory
+ * buffer, eight lanes per line with one 16-byte load each, `loads` loads per
+ * thread: blocks * 256 * 16 * loads bytes.  Timed, it gives the rate of the
+ * SM's shared-memory / L1 data path for the float32 gather's line reads.
+ * sink: one device uint32, written only to keep the loads. */
+int nglod_measure_smem_reads(int32_t loads, int32_t blocks, uint32_t *sink, nglod_stream_t stream);
+
 /* SphereTracer.forward in the BF16 form: the persistent tracer of
  * nglod_trace with every sdf evaluation (march points and normal taps) done
  * by the bf16 tile kernel above, 128 rays per block evaluated together.

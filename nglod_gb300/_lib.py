@@ -232,6 +232,7 @@ SIGNATURES = {
     "nglod_build_summed_volume": (ctypes.c_int, [ctypes.POINTER(DenseModel), _i32, _i32, _vp, _vp]),
     "nglod_measure_line_reads": (ctypes.c_int, [_vp, _i64, _i32, _i32, _vp, _vp]),
     "nglod_measure_fma": (ctypes.c_int, [_i32, _i32, _vp, _vp]),
+    "nglod_measure_smem_reads": (ctypes.c_int, [_i32, _i32, _vp, _vp]),
     "nglod_debug_mma_wait_polls": (ctypes.c_int, [_i64]),
     "nglod_sdf_fwd_bf16": (ctypes.c_int, [ctypes.POINTER(Bf16Model), _vp, _i64, _i32, _vp, _vp, _vp]),
     "nglod_trace_bf16": (ctypes.c_int, [ctypes.POINTER(Bf16Model), ctypes.POINTER(TraceParams), _vp, _vp, _i64,

@@ -379,17 +379,16 @@ __global__ void __launch_bounds__(f32st::kThreads, 1)
         float4 acc[8];
 #pragma unroll
         for (int p = 0; p < 8; ++p) acc[p] = make_float4(0.f, 0.f, 0.f, 0.f);
-        uint32_t vaddr = sbase + (uint32_t)kVol;
+        const float4 *vol = reinterpret_cast<const float4 *>(sm + kVol);
 #pragma unroll 1
-        for (int l = 0; l <= L; ++l) {
+        for (int l = 0; l < staged; ++l) {
             const int s = volume_side(m, l);
-            if (l < staged) {
-                gather_warp_add_f32_shared(vaddr, s, px, py, pz, lane, acc);
-                vaddr += (uint32_t)(s * s * s) * 128u;
-            } else {
-                gather_warp_add_f32(static_cast<const float *>(m.grid[l]), s, px, py, pz, lane, acc);
-            }
+            gather_warp_add_f32_shared(vol, s, px, py, pz, lane, acc);
+            vol += s * s * s * (kC / 4);
         }
+#pragma unroll 1
+        for (int l = staged; l <= L; ++l)
+            gather_warp_add_f32(static_cast<const float *>(m.grid[l]), volume_side(m, l), px, py, pz, lane, acc);
         // 2. a point-tile buffer, the split rows
         if (gtid == 0) *sel = acquire_tile_buffer(locks, abort_flag);
         group_sync(grp);

@@ -124,19 +124,11 @@ __device__ __forceinline__ void gather_warp_add_f32(const float *__restrict__ g,
     gather_warp_add_f32_by([g4](int i) { return __ldg(g4 + i); }, s, px, py, pz, lane, acc);
 }
 
-// 16-byte load from a shared-memory address.
-__device__ __forceinline__ float4 ld_shared_f4(uint32_t addr) {
-    float4 v;
-    asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "r"(addr));
-    return v;
-}
-
-// The same gather from a volume staged in shared memory at address `base`
-// (channel-last, 128 B per vertex).
-__device__ __forceinline__ void gather_warp_add_f32_shared(uint32_t base, int s, float px, float py, float pz,
+// The same gather from a volume staged in shared memory (v points into the
+// kernel's shared-memory array; channel-last, 128 B per vertex).
+__device__ __forceinline__ void gather_warp_add_f32_shared(const float4 *v, int s, float px, float py, float pz,
                                                            int lane, float4 (&acc)[8]) {
-    gather_warp_add_f32_by([base](int i) { return ld_shared_f4(base + 16u * (uint32_t)i); }, s, px, py, pz, lane,
-                           acc);
+    gather_warp_add_f32_by([v](int i) { return v[i]; }, s, px, py, pz, lane, acc);
 }
 
 // Row stride (floats) of the per-warp transpose buffer: 36, so that the

@@ -1,6 +1,7 @@
-// Measurement helper for the bench's roofline: the float32 FMA pipe's
-// throughput, measured live on the device the kernels run on (the FMA term
-// of the float32 query kernel is divided by it).
+// Measurement helpers for the bench's roofline, run live on the device the
+// kernels run on: the float32 FMA pipe's throughput (the FMA term of the
+// float32 query kernel is divided by it) and the shared-memory data path's
+// rate for whole-line reads (the term of the gathers served on the SM).
 #include "common.cuh"
 
 namespace nglod {
@@ -27,7 +28,39 @@ __global__ void __launch_bounds__(256) fma_rate_kernel(int iters, float seed, fl
     if (s == -1.f) sink[0] = s;  // never true for these inputs; keeps every chain
 }
 
+// Random whole 128-byte lines of a 32 KB shared-memory buffer, eight lanes
+// per line with one 16-byte load each (the float32 gather's pattern from a
+// staged volume): the rate of the SM's shared-memory / L1 data path for the
+// gather's line reads.  16 * loads bytes per thread.
+constexpr int kSmemLines = 256;
+__global__ void __launch_bounds__(256) smem_line_read_kernel(int loads, uint32_t seed, uint32_t *__restrict__ sink) {
+    __shared__ uint4 buf[kSmemLines * 8];
+    for (int i = threadIdx.x; i < kSmemLines * 8; i += blockDim.x) buf[i] = make_uint4(i, i ^ seed, i + 1, i + 2);
+    __syncthreads();
+    uint32_t h = (((blockIdx.x * blockDim.x + threadIdx.x) >> 3) * 2654435761u) ^ seed;
+    h |= 1u;
+    uint32_t acc = 0u;
+    const uint4 *base = buf + (threadIdx.x & 7);
+#pragma unroll 8
+    for (int k = 0; k < loads; ++k) {
+        h ^= h << 13;
+        h ^= h >> 17;
+        h ^= h << 5;
+        const uint4 u = base[(h % kSmemLines) * 8];
+        acc ^= u.x ^ u.y ^ u.z ^ u.w;
+    }
+    if (acc == 0x9E3779B9u) sink[0] = acc;  // keeps every load
+}
+
 }  // namespace nglod
+
+extern "C" int nglod_measure_smem_reads(int32_t loads, int32_t blocks, uint32_t *sink, nglod_stream_t stream) {
+    using namespace nglod;
+    NGLOD_REQUIRE(sink, NGLOD_ERR_INVALID, "null pointer argument");
+    NGLOD_REQUIRE(loads >= 1 && blocks >= 1, NGLOD_ERR_INVALID, "loads=%d blocks=%d", loads, blocks);
+    smem_line_read_kernel<<<blocks, 256, 0, (cudaStream_t)stream>>>(loads, 0x2545F491u, sink);
+    return launch_status("nglod_measure_smem_reads");
+}
 
 extern "C" int nglod_measure_fma(int32_t iters, int32_t blocks, float *sink, nglod_stream_t stream) {
     using namespace nglod;

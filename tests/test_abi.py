@@ -156,10 +156,14 @@ def test_line_read_probe_validation_without_device(built_library):
 
 
 def test_fma_probe_validation_without_device(built_library):
-    """Argument checks of nglod_measure_fma, before any CUDA call."""
+    """Argument checks of nglod_measure_fma and nglod_measure_smem_reads,
+    before any CUDA call."""
     from nglod_gb300 import _lib
     lib = _lib.load()
     sink = ctypes.c_void_p(1 << 21)
     assert lib.nglod_measure_fma(16, 1, None, None) == -1
     assert lib.nglod_measure_fma(0, 1, sink, None) == -1
     assert lib.nglod_measure_fma(16, 0, sink, None) == -1
+    assert lib.nglod_measure_smem_reads(16, 1, None, None) == -1
+    assert lib.nglod_measure_smem_reads(0, 1, sink, None) == -1
+    assert lib.nglod_measure_smem_reads(16, 0, sink, None) == -1
