@@ -110,7 +110,7 @@ NCU_CAPTURES = {
                     "nglod_gb300/csrc/tf32_tile.cuh", "nglod_gb300/csrc/tc_common.cuh"],
         "sha256": "390c6158788a05ef15a4187d985ef0b2c4deb4d054fc136ddd1d4cb237c4b890",
         "how": "ncu --set full --clock-control none, one launch at 4,194,304 points (bench --no-extras)"},
-    "sdf_fwd_bf16_tc_kernel": {
+    "sdf_fwd_bf16_staged_kernel": {
         "dram_bytes": 90_524_160 + 11_049_216, "points": N_POINTS,
         "sources": ["nglod_gb300/csrc/bf16.cu", "nglod_gb300/csrc/bf16_tile.cuh", "nglod_gb300/csrc/tc_common.cuh"],
         "sha256": "df7f80a31490e6140ca00f1563d41b5e8e5f2f77ded8375784d5ee72db2176ef",
@@ -465,7 +465,7 @@ def run_ours(args):
     trained = None
     if not args.no_extras:
         extras["train"], trained = bench_train(dev, flush, stream)
-        extras["bf16"] = bench_bf16(trained, x, x_host, c, r, dev, flush, stream, args.steps, line_peak)
+        extras["bf16"] = bench_bf16(trained, x, x_host, c, r, dev, flush, stream, args.steps, line_peak, smem_peak)
         extras["trace"] = bench_trace(net, dev, flush, stream)
         extras["summed"] = bench_summed(trained, x, dev, flush, stream)
         extras["serve"] = bench_serve(dev)
@@ -528,7 +528,7 @@ def fp64_errors(net, model, x, lods=range(LOD + 1)):
     return out
 
 
-def bench_bf16(tnet, x, x_host, c, r, dev, flush, stream, steps, line_peak_f32=None):
+def bench_bf16(tnet, x, x_host, c, r, dev, flush, stream, steps, line_peak_f32=None, smem_peak=None):
     """The mixed-precision inference form (bf16 volumes, tcgen05 bf16 decoder,
     fp32 accumulate) on the headline's 4,194,304 points at lod 4, on the
     weights of 2,000 training steps from seed 1; with each LOD's max and mean
@@ -551,16 +551,25 @@ def bench_bf16(tnet, x, x_host, c, r, dev, flush, stream, steps, line_peak_f32=N
     bnet.check_status()
     pair_bytes = sum(pv.numel() * 2 for pv in bnet.pairs) or sum(fv.fm.numel() * 2 for fv in tnet.features)
     line_peak = line_read_peak(dev, pair_bytes)
+    if smem_peak is None:
+        smem_peak = smem_read_peak(dev)
     sec = ms / 1e3
-    traffic, tnote = ncu_traffic("sdf_fwd_bf16_tc_kernel", N_POINTS)
-    roof = roofline("sdf_fwd_bf16_tc_kernel", sec, {
-        "gather_l2": (N_POINTS * (LOD + 1) * 8 * 32 * 2, line_peak, "GB/s",
+    gathered = (LOD + 1) * 8 * 32 * 2  # four 128-byte pair lines per LOD
+    staged = 2 * 8 * 32 * 2            # LODs 0 and 1 from shared memory
+    traffic, tnote = ncu_traffic("sdf_fwd_bf16_staged_kernel", N_POINTS)
+    roof = roofline("sdf_fwd_bf16_staged_kernel", sec, {
+        "gather_l2": (N_POINTS * (gathered - staged), line_peak, "GB/s",
                       "measured live: random whole 128-byte lines of an L2-resident buffer the size of the pair "
                       "volumes (nglod_measure_line_reads)"),
+        "data_path": (N_POINTS * gathered, smem_peak, "GB/s",
+                      "measured live: random whole 128-byte lines of shared memory (nglod_measure_smem_reads)"),
         "hbm": (N_POINTS * 16 + pair_bytes, pk["hbm_gbs"], "GB/s", f"{pk['source']} hbm_gbs (burst copy)"),
         "tensor": (N_POINTS * 2 * 35 * 128, pk["bf16_tflops"], "TFLOP/s", f"{pk['source']} bf16_tflops (burst)"),
-    }, {"hbm_bytes": 16, "gathered_bytes": (LOD + 1) * 8 * 32 * 2, "tensor_flop": 2 * 35 * 128}, N_POINTS,
-        traffic, tnote)
+    }, {"hbm_bytes": 16, "gathered_bytes": gathered, "gathered_bytes_from_l2": gathered - staged,
+        "gathered_bytes_from_shared": staged, "tensor_flop": 2 * 35 * 128}, N_POINTS,
+        traffic, tnote,
+        note="each block stages the 5^3 and 9^3 pair volumes (109 KB) in shared memory; LODs 2..4 come from L2 "
+             "as whole 128-byte pair lines")
     xs = x[::ERR_SAMPLE_STRIDE].contiguous()
     return {"workload": "Bf16OctreeSDF.sdf(x, lod=4): bf16 volumes, tcgen05 bf16 decoder, fp32 accumulate; the "
                         "headline's 4,194,304 points; weights of 2,000 training steps from seed 1",

@@ -139,60 +139,85 @@ __device__ __forceinline__ void gather_warp_rows(const nglod_bf16_model &m, int 
 // over eight lines and made the kernel twice as slow.)  Each lane holds both x corners of its 8
 // channels, and the eight weighted corners are summed in the same order
 // (tnw..bse) as gather_warp_rows, so the two give identical sums.
+template <int NP, typename Load>
+__device__ __forceinline__ void pairs_add_level(int s, float px, float py, float pz, int lane, float2 (&acc)[NP][4],
+                                                Load load) {
+    const unsigned FULL = 0xffffffffu;
+    const int sy = s * 4, sz = s * sy;
+    // each lane's own point's clamped grid coordinates; the loading lanes
+    // receive them by three shuffles and derive the corner set themselves
+    // (corner_set's expressions: the same sums as shuffling its results)
+    const float sm1 = (float)(s - 1);
+    const float ix = fminf(sm1, fmaxf(((px + 1.f) / 2.f) * sm1, 0.f));
+    const float iy = fminf(sm1, fmaxf(((py + 1.f) / 2.f) * sm1, 0.f));
+    const float iz = fminf(sm1, fmaxf(((pz + 1.f) / 2.f) * sm1, 0.f));
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+        const int src = p * 8 + (lane >> 2);
+        const float qx = __shfl_sync(FULL, ix, src);
+        const float qy = __shfl_sync(FULL, iy, src);
+        const float qz = __shfl_sync(FULL, iz, src);
+        float ws[8];
+        int v0;
+        bool ny, nz;
+        corner_set_at(s, qx, qy, qz, v0, ny, nz, ws);
+        const int o0 = v0 * 4;
+        const int oy = ny ? sy : 0;
+        const int oz = nz ? sz : 0;
+        const int o[4] = {o0, o0 + oy, o0 + oz, o0 + oz + oy};
+        PairUnit v[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) v[j] = load(o[j]);
+        float2 a2[4] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+#pragma unroll
+            for (int x = 0; x < 2; ++x) {
+                const float2 w2 = make_float2(ws[2 * j + x], ws[2 * j + x]);
+#pragma unroll
+                for (int c = 0; c < 4; ++c)
+                    a2[c] = __ffma2_rn(make_float2(bf_lo(v[j].w[4 * x + c]), bf_hi(v[j].w[4 * x + c])), w2, a2[c]);
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < 4; ++c) acc[p][c] = __fadd2_rn(acc[p][c], a2[c]);
+    }
+}
+
 template <int NP>
 __device__ __forceinline__ void gather_warp_pairs(const nglod_bf16_model &m, int L, float px, float py, float pz,
                                                   int lane, float2 (&acc)[NP][4]) {
-    const unsigned FULL = 0xffffffffu;
-    const int part = lane & 3;
 #pragma unroll
     for (int p = 0; p < NP; ++p)
 #pragma unroll
         for (int c = 0; c < 4; ++c) acc[p][c] = make_float2(0.f, 0.f);
 #pragma unroll 1
     for (int l = m.summed ? L : 0; l <= L; ++l) {
-        const PairUnit *g = static_cast<const PairUnit *>(m.grid_pairs[l]) + part;  // 4 units per line
-        const int s = (1 << (l + m.base_lod)) + 1;
-        const int sy = s * 4, sz = s * sy;
-        // each lane's own point's clamped grid coordinates; the loading lanes
-        // receive them by three shuffles and derive the corner set themselves
-        // (corner_set's expressions: the same sums as shuffling its results)
-        const float sm1 = (float)(s - 1);
-        const float ix = fminf(sm1, fmaxf(((px + 1.f) / 2.f) * sm1, 0.f));
-        const float iy = fminf(sm1, fmaxf(((py + 1.f) / 2.f) * sm1, 0.f));
-        const float iz = fminf(sm1, fmaxf(((pz + 1.f) / 2.f) * sm1, 0.f));
-#pragma unroll
-        for (int p = 0; p < NP; ++p) {
-            const int src = p * 8 + (lane >> 2);
-            const float qx = __shfl_sync(FULL, ix, src);
-            const float qy = __shfl_sync(FULL, iy, src);
-            const float qz = __shfl_sync(FULL, iz, src);
-            float ws[8];
-            int v0;
-            bool ny, nz;
-            corner_set_at(s, qx, qy, qz, v0, ny, nz, ws);
-            const int o0 = v0 * 4;
-            const int oy = ny ? sy : 0;
-            const int oz = nz ? sz : 0;
-            const int o[4] = {o0, o0 + oy, o0 + oz, o0 + oz + oy};
-            PairUnit v[4];
-#pragma unroll
-            for (int j = 0; j < 4; ++j) v[j] = ld_pair_unit(g + o[j]);
-            float2 a2[4] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f),
-                            make_float2(0.f, 0.f)};
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-#pragma unroll
-                for (int x = 0; x < 2; ++x) {
-                    const float2 w2 = make_float2(ws[2 * j + x], ws[2 * j + x]);
-#pragma unroll
-                    for (int c = 0; c < 4; ++c)
-                        a2[c] = __ffma2_rn(make_float2(bf_lo(v[j].w[4 * x + c]), bf_hi(v[j].w[4 * x + c])), w2, a2[c]);
-                }
-            }
-#pragma unroll
-            for (int c = 0; c < 4; ++c) acc[p][c] = __fadd2_rn(acc[p][c], a2[c]);
-        }
+        const PairUnit *g = static_cast<const PairUnit *>(m.grid_pairs[l]) + (lane & 3);  // 4 units per line
+        pairs_add_level<NP>((1 << (l + m.base_lod)) + 1, px, py, pz, lane, acc,
+                            [g](int o) { return ld_pair_unit(g + o); });
     }
+}
+
+// This lane's 32-byte unit of a pair line staged in shared memory (u: the
+// unit's two 16-byte halves, x corner 0 then 1), read as two 16-byte loads.
+// The lanes of odd points of a load instruction (hs = 1) read the x = 1 half
+// first, so that the two points of each quarter warp cover all 32 banks
+// (reading the x = 0 halves together would leave half of them idle and take
+// twice the wavefronts); the halves are put back in order with selects.
+__device__ __forceinline__ PairUnit lds_pair_unit(const uint4 *u, int hs) {
+    const uint4 a = u[hs], b = u[hs ^ 1];
+    const uint4 x0 = hs ? b : a, x1 = hs ? a : b;
+    PairUnit r;
+    r.w[0] = x0.x;
+    r.w[1] = x0.y;
+    r.w[2] = x0.z;
+    r.w[3] = x0.w;
+    r.w[4] = x1.x;
+    r.w[5] = x1.y;
+    r.w[6] = x1.z;
+    r.w[7] = x1.w;
+    return r;
 }
 
 // Writes the tile rows row0 .. row0 + 8 * NP - 1 of gather_warp_pairs<NP>:
@@ -403,11 +428,10 @@ struct Bf16Args {
 // all devices): kWaitPolls unless a test of the error path lowers it.
 static uint32_t g_bf16_wait_polls = kWaitPolls;
 
-// One 128-point tile per block of four warps: warp w gathers rows 32w ..
-// 32w + 31 (from the vertex volumes, or from pair volumes when kPairs), one
+// One 128-point tile per block of four warps (models without pair
+// volumes): warp w gathers rows 32w .. 32w + 31 from the vertex volumes, one
 // thread issues the MMA, and thread (w, lane) runs the epilogue of TMEM lane
 // / row 32w + lane.
-template <bool kPairs>
 __global__ void __launch_bounds__(kTP, 4) sdf_fwd_bf16_tc_kernel(const Bf16Args a) {
     extern __shared__ __align__(1024) uint8_t smem[];
     uint8_t *sA = smem + kSmemA;
@@ -443,7 +467,7 @@ __global__ void __launch_bounds__(kTP, 4) sdf_fwd_bf16_tc_kernel(const Bf16Args 
     const uint32_t idesc = tc::idesc_bf16_f32(kTP, kHid);
     uint32_t phase = 0;
     // unsorted query points: four lanes per point load (one load instruction
-    // covers a point's 64-byte vertex, or its 128-byte pair line)
+    // covers a point's 64-byte vertex)
     constexpr int kLPP = 4;
 
     for (int64_t tile = blockIdx.x; tile * kTP < a.n; tile += gridDim.x) {
@@ -456,15 +480,9 @@ __global__ void __launch_bounds__(kTP, 4) sdf_fwd_bf16_tc_kernel(const Bf16Args 
                 py = a.x[3 * gi + 1];
                 pz = a.x[3 * gi + 2];
             }
-            if constexpr (kPairs) {
-                float2 acc[4][4];
-                gather_warp_pairs<4>(a.m, a.L, px, py, pz, lane, acc);
-                write_pair_rows<4>(sA, warp * 32, lane, acc, px, py, pz);
-            } else {
-                float2 acc[kLPP][16 / kLPP];
-                gather_warp_rows<kLPP>(a.m, a.L, px, py, pz, lane, acc);
-                write_warp_rows<kLPP>(sA, warp, lane, acc, px, py, pz);
-            }
+            float2 acc[kLPP][16 / kLPP];
+            gather_warp_rows<kLPP>(a.m, a.L, px, py, pz, lane, acc);
+            write_warp_rows<kLPP>(sA, warp, lane, acc, px, py, pz);
         }
         tc::fence_proxy_async_smem();
         __syncthreads();
@@ -503,6 +521,171 @@ __global__ void __launch_bounds__(kTP, 4) sdf_fwd_bf16_tc_kernel(const Bf16Args 
     if (warp == 0) tc::tmem_dealloc(tmem, kHid);
 }
 
+
+// ---------------------------------------------------------------------------
+// point query over pair volumes: persistent, coarse volumes in shared memory
+// ---------------------------------------------------------------------------
+// One 16-warp block per SM.  The leading pair volumes that fit (5^3 and 9^3
+// vertices, 109 KB, at base_lod 2) are copied into shared memory once per
+// block; the finer levels come through L2 with 32-byte loads.  The block is
+// four independent groups of four warps, each with its own point tile and
+// its own 128 TMEM columns (4 x 128 = the SM's 512): a group gathers 128
+// points, writes their rows, its first thread issues the three K steps and
+// waits, and the group runs the epilogue while the other groups gather.
+// Groups meet only at their own named barrier (id 1 + g, 128 threads).
+// Same arithmetic as sdf_fwd_bf16_tc_kernel over vertex volumes (identical
+// results).
+namespace b16st {
+constexpr int kGroups = 4;
+constexpr int kThreads = kTP * kGroups;  // 512
+constexpr size_t kA = 0;                 // group g's point tile at kA + g kTileBytesA
+constexpr size_t kB = kA + (size_t)kGroups * kTileBytesA;
+constexpr size_t kW1 = kB + kTileBytes;
+constexpr size_t kBar = kW1 + kHid * 4;  // one mbarrier per group
+constexpr size_t kOk = kBar + 8 * kGroups;
+constexpr size_t kSlot = kOk + 4 * kGroups;
+constexpr size_t kAbort = kSlot + 4;
+constexpr size_t kVol = (kAbort + 4 + 127) & ~(size_t)127;
+constexpr size_t kSmemMax = 227 * 1024;
+constexpr size_t kVolBudget = kSmemMax - kVol;
+// more than half of an SM's shared memory: one block (512 TMEM columns) per SM
+constexpr size_t kSmemMin = 120 * 1024;
+constexpr uint32_t kCols = kGroups * kHid;
+static_assert(kB % 16 == 0 && kBar % 8 == 0 && kVol % 128 == 0, "shared layout alignment");
+static_assert(kVol + 109312 <= kSmemMax, "pair levels 5^3 and 9^3 fit");
+}  // namespace b16st
+
+__device__ __forceinline__ void b16_group_sync(int g) {
+    asm volatile("bar.sync %0, %1;" ::"r"(1 + g), "n"(kTP) : "memory");
+}
+
+// Levels first .. first + nstaged - 1 are staged (in that order) in shared
+// memory; first = L for LOD-summed models, else 0.
+__global__ void __launch_bounds__(b16st::kThreads, 1)
+    sdf_fwd_bf16_staged_kernel(const Bf16Args a, int first, int nstaged) {
+    using namespace b16st;
+    extern __shared__ __align__(1024) uint8_t smem_b16st[];
+    uint8_t *sm = smem_b16st;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int grp = warp >> 2, quad = warp & 3, gtid = tid & (kTP - 1);
+    uint8_t *sA = sm + kA + (size_t)grp * kTileBytesA;
+    const float *sw1 = reinterpret_cast<const float *>(sm + kW1);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(sm + kBar) + grp;
+    volatile int *okf = reinterpret_cast<volatile int *>(sm + kOk) + grp;
+    uint32_t *slot = reinterpret_cast<uint32_t *>(sm + kSlot);
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(sm + kAbort);
+    const int L = a.L;
+
+    // set-up: decoder tile, w1, the zero K columns 40..47 of the point
+    // tiles, the staged pair volumes, TMEM, barriers
+    const uint4 *bsrc = static_cast<const uint4 *>(a.m.w0_tile[L]);
+    for (int i = tid; i < (int)(kTileBytes / 16); i += kThreads) reinterpret_cast<uint4 *>(sm + kB)[i] = bsrc[i];
+    if (tid < kHid) reinterpret_cast<float *>(sm + kW1)[tid] = a.m.w1[L][tid];
+    const float b1 = a.m.b1[L][0];
+    for (int i = tid; i < kGroups * (kTP / 8) * 8; i += kThreads) {
+        const int g = i / ((kTP / 8) * 8), r8 = (i >> 3) % (kTP / 8), r = i & 7;
+        *reinterpret_cast<uint4 *>(sm + kA + (size_t)g * kTileBytesA + r8 * kSboA + 5 * kLboA + r * 16) =
+            make_uint4(0u, 0u, 0u, 0u);
+    }
+    {
+        size_t off = kVol;
+        for (int l = first; l < first + nstaged; ++l) {
+            const int s = (1 << (l + a.m.base_lod)) + 1;
+            const int cnt = s * s * s * 8;  // 16-byte pieces
+            const uint4 *src = static_cast<const uint4 *>(a.m.grid_pairs[l]);
+            uint4 *dst = reinterpret_cast<uint4 *>(sm + off);
+            for (int q = tid; q < cnt; q += kThreads) dst[q] = src[q];
+            off += (size_t)cnt * 16;
+        }
+    }
+    if (warp == 0) tc::tmem_alloc(slot, kCols);
+    if (tid == 0) {
+        for (int g = 0; g < kGroups; ++g) tc::mbar_init(reinterpret_cast<uint64_t *>(sm + kBar) + g, 1);
+        *abort_flag = 0;
+    }
+    tc::fence_proxy_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = *slot;
+    const uint32_t dcol = tmem + (uint32_t)(grp * kHid);
+    const uint32_t sa = tc::smem_addr(sA), sb = tc::smem_addr(sm + kB);
+    const uint32_t idesc = tc::idesc_bf16_f32(kTP, kHid);
+    const int part = lane & 3, hs = (lane >> 2) & 1;
+    uint32_t phase = 0;
+    bool pending = false;  // group leader: an issued product whose completion it did not see
+
+    for (int64_t t = (int64_t)blockIdx.x * kGroups + grp; t * kTP < a.n; t += (int64_t)gridDim.x * kGroups) {
+        const int64_t gi = t * kTP + gtid;
+        float px = 0.f, py = 0.f, pz = 0.f;
+        if (gi < a.n) {
+            px = a.x[3 * gi];
+            py = a.x[3 * gi + 1];
+            pz = a.x[3 * gi + 2];
+        }
+        // 1. gather: the warp's 32 points (rows 32 quad ..), staged levels
+        // from shared memory, the rest from the pair volumes in global memory
+        float2 acc[4][4];
+#pragma unroll
+        for (int p = 0; p < 4; ++p)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) acc[p][c] = make_float2(0.f, 0.f);
+        const uint4 *vol = reinterpret_cast<const uint4 *>(sm + kVol) + 2 * part;  // 8 pieces per line
+#pragma unroll 1
+        for (int l = first; l < first + nstaged; ++l) {
+            const int s = (1 << (l + a.m.base_lod)) + 1;
+            pairs_add_level<4>(s, px, py, pz, lane, acc, [vol, hs](int o) { return lds_pair_unit(vol + 2 * o, hs); });
+            vol += s * s * s * 8;
+        }
+#pragma unroll 1
+        for (int l = first + nstaged; l <= L; ++l) {
+            const PairUnit *g = static_cast<const PairUnit *>(a.m.grid_pairs[l]) + part;
+            pairs_add_level<4>((1 << (l + a.m.base_lod)) + 1, px, py, pz, lane, acc,
+                               [g](int o) { return ld_pair_unit(g + o); });
+        }
+        write_pair_rows<4>(sA, quad * 32, lane, acc, px, py, pz);
+        tc::fence_proxy_async_smem();
+        tc::fence_before_sync();
+        b16_group_sync(grp);
+        // 2. the group's first thread issues the three K steps and waits (not
+        // once another group's wait gave up: the group then stops)
+        if (gtid == 0) {
+            bool ok = false;
+            if (!*abort_flag) {
+                tc::fence_after_sync();
+#pragma unroll
+                for (int ks = 0; ks < kTK / 16; ++ks) {
+                    const uint64_t ad = tc::smem_desc(sa + ks * 2 * kLboA, kLboA, kSboA);
+                    const uint64_t bd = tc::smem_desc(sb + ks * 256, kLbo, kSbo);
+                    tc::mma_bf16(dcol, ad, bd, idesc, ks > 0 ? 1u : 0u);
+                }
+                tc::mma_commit(bar);
+                ok = tc::mbar_wait_bounded(bar, phase, a.wait_polls);
+                if (!ok) {
+                    pending = true;
+                    *abort_flag = 1;
+                    atomicExch(a.status, 1);
+                }
+            }
+            *okf = ok ? 1 : 0;
+        }
+        b16_group_sync(grp);
+        if (!*okf) break;
+        phase ^= 1u;
+        tc::fence_after_sync();
+        // 3. epilogue on this thread's TMEM row
+        const float o = relu_dot_w1(dcol + ((uint32_t)(quad * 32) << 16), sw1);
+        if (gi < a.n) a.out[gi] = o + b1;
+        tc::fence_before_sync();
+    }
+    // teardown: a product still in flight after a wait gave up finishes
+    // before the columns are freed
+    if (gtid == 0 && pending) tc::mbar_wait_bounded(bar, phase, kWaitPolls);
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if (warp == 0) tc::tmem_dealloc(tmem, kCols);
+}
 
 // ---------------------------------------------------------------------------
 // persistent BF16 sphere tracer
@@ -813,12 +996,32 @@ static int sdf_fwd_bf16_impl(const nglod_bf16_model *model, const float *x, int6
     a.out = out;
     a.status = status;
     a.wait_polls = g_bf16_wait_polls;
-    auto kernel = pairs ? sdf_fwd_bf16_tc_kernel<true> : sdf_fwd_bf16_tc_kernel<false>;
-    NGLOD_TRY(cuda_status(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes),
-                          "cudaFuncSetAttribute"));
     const int64_t tiles = (n + kTP - 1) / kTP;
+    if (pairs) {
+        // the leading pair volumes that fit beside the tiles are staged
+        const int first = model->summed ? L : 0;
+        int nstaged = 0;
+        size_t vbytes = 0;
+        for (int l = first; l <= L; ++l) {
+            const size_t sd = (size_t)(1 << (l + model->base_lod)) + 1;
+            if (vbytes + sd * sd * sd * 128 > b16st::kVolBudget) break;
+            vbytes += sd * sd * sd * 128;
+            ++nstaged;
+        }
+        const size_t smem = b16st::kVol + vbytes < b16st::kSmemMin ? b16st::kSmemMin : b16st::kVol + vbytes;
+        NGLOD_TRY(cuda_status(cudaFuncSetAttribute(sdf_fwd_bf16_staged_kernel,
+                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                              "cudaFuncSetAttribute"));
+        const int64_t want = (tiles + b16st::kGroups - 1) / b16st::kGroups;
+        const int64_t cap = (int64_t)num_sms();
+        sdf_fwd_bf16_staged_kernel<<<(int)(want < cap ? want : cap), b16st::kThreads, smem, s>>>(a, first, nstaged);
+        return launch_status("nglod_sdf_fwd_bf16");
+    }
+    NGLOD_TRY(cuda_status(cudaFuncSetAttribute(sdf_fwd_bf16_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)kSmemBytes),
+                          "cudaFuncSetAttribute"));
     const int64_t cap = (int64_t)num_sms() * 4;
-    kernel<<<(int)(tiles < cap ? tiles : cap), kTP, kSmemBytes, s>>>(a);
+    sdf_fwd_bf16_tc_kernel<<<(int)(tiles < cap ? tiles : cap), kTP, kSmemBytes, s>>>(a);
     return launch_status("nglod_sdf_fwd_bf16");
 }
 
