@@ -554,8 +554,8 @@ def bench_bf16(tnet, x, x_host, c, r, dev, flush, stream, steps, line_peak_f32=N
     if smem_peak is None:
         smem_peak = smem_read_peak(dev)
     sec = ms / 1e3
-    gathered = (LOD + 1) * 8 * 32 * 2  # four 128-byte pair lines per LOD
-    staged = 2 * 8 * 32 * 2            # LODs 0 and 1 from shared memory
+    gathered = (LOD + 1) * 8 * 32 * 2  # 8 corners x 64 B per LOD (four 128-byte pair lines from L2)
+    staged = 2 * 8 * 32 * 2            # LODs 0 and 1: eight 64-byte vertices each, from shared memory
     traffic, tnote = ncu_traffic("sdf_fwd_bf16_staged_kernel", N_POINTS)
     roof = roofline("sdf_fwd_bf16_staged_kernel", sec, {
         "gather_l2": (N_POINTS * (gathered - staged), line_peak, "GB/s",
@@ -568,8 +568,8 @@ def bench_bf16(tnet, x, x_host, c, r, dev, flush, stream, steps, line_peak_f32=N
     }, {"hbm_bytes": 16, "gathered_bytes": gathered, "gathered_bytes_from_l2": gathered - staged,
         "gathered_bytes_from_shared": staged, "tensor_flop": 2 * 35 * 128}, N_POINTS,
         traffic, tnote,
-        note="each block stages the 5^3 and 9^3 pair volumes (109 KB) in shared memory; LODs 2..4 come from L2 "
-             "as whole 128-byte pair lines")
+        note="each block stages the 5^3 and 9^3 bf16 vertex volumes (55 KB) in shared memory; LODs 2..4 come "
+             "from L2 as whole 128-byte pair lines")
     xs = x[::ERR_SAMPLE_STRIDE].contiguous()
     return {"workload": "Bf16OctreeSDF.sdf(x, lod=4): bf16 volumes, tcgen05 bf16 decoder, fp32 accumulate; the "
                         "headline's 4,194,304 points; weights of 2,000 training steps from seed 1",

@@ -44,15 +44,16 @@ __device__ __forceinline__ void corner_set(int s, float px, float py, float pz, 
 
 // corner_set for a point whose clamped grid coordinates are already known
 // (the same expressions, so the same bits): vertex index of corner 0, the
-// y / z neighbour flags (whether they differ from it) and the weights.
-__device__ __forceinline__ void corner_set_at(int s, float ix, float iy, float iz, int &v0, bool &ny, bool &nz,
-                                              float (&w)[8]) {
+// x / y / z neighbour flags (whether they differ from it) and the weights.
+__device__ __forceinline__ void corner_set_at(int s, float ix, float iy, float iz, int &v0, bool &nx, bool &ny,
+                                              bool &nz, float (&w)[8]) {
     const float x0 = floorf(ix), y0 = floorf(iy), z0 = floorf(iz);
     const float wx1 = ix - x0, wx0 = (x0 + 1.f) - ix;
     const float wy1 = iy - y0, wy0 = (y0 + 1.f) - iy;
     const float wz1 = iz - z0, wz0 = (z0 + 1.f) - iz;
     const int xi = (int)x0, yi = (int)y0, zi = (int)z0;
     v0 = (zi * s + yi) * s + xi;
+    nx = xi + 1 < s;
     ny = yi + 1 < s;
     nz = zi + 1 < s;
     const float wxy[4] = {wx0 * wy0, wx1 * wy0, wx0 * wy1, wx1 * wy1};
@@ -159,8 +160,8 @@ __device__ __forceinline__ void pairs_add_level(int s, float px, float py, float
         const float qz = __shfl_sync(FULL, iz, src);
         float ws[8];
         int v0;
-        bool ny, nz;
-        corner_set_at(s, qx, qy, qz, v0, ny, nz, ws);
+        bool nx, ny, nz;  // the pair line holds the x neighbour already
+        corner_set_at(s, qx, qy, qz, v0, nx, ny, nz, ws);
         const int o0 = v0 * 4;
         const int oy = ny ? sy : 0;
         const int oz = nz ? sz : 0;
@@ -199,25 +200,51 @@ __device__ __forceinline__ void gather_warp_pairs(const nglod_bf16_model &m, int
     }
 }
 
-// This lane's 32-byte unit of a pair line staged in shared memory (u: the
-// unit's two 16-byte halves, x corner 0 then 1), read as two 16-byte loads.
-// The lanes of odd points of a load instruction (hs = 1) read the x = 1 half
-// first, so that the two points of each quarter warp cover all 32 banks
-// (reading the x = 0 halves together would leave half of them idle and take
-// twice the wavefronts); the halves are put back in order with selects.
-__device__ __forceinline__ PairUnit lds_pair_unit(const uint4 *u, int hs) {
-    const uint4 a = u[hs], b = u[hs ^ 1];
-    const uint4 x0 = hs ? b : a, x1 = hs ? a : b;
-    PairUnit r;
-    r.w[0] = x0.x;
-    r.w[1] = x0.y;
-    r.w[2] = x0.z;
-    r.w[3] = x0.w;
-    r.w[4] = x1.x;
-    r.w[5] = x1.y;
-    r.w[6] = x1.z;
-    r.w[7] = x1.w;
-    return r;
+// pairs_add_level's sums over a vertex volume (four 16-byte pieces per
+// vertex; load(o) returns piece o of this lane's part): the eight corners are
+// separate loads, summed in the same order (tnw..bse) with the same weights,
+// so the results are identical.  Used for the volumes staged in shared
+// memory, where the 64-byte vertices need no selects to spread a load
+// instruction over the banks.
+template <int NP, typename Load>
+__device__ __forceinline__ void verts_add_level(int s, float px, float py, float pz, int lane, float2 (&acc)[NP][4],
+                                                Load load) {
+    const unsigned FULL = 0xffffffffu;
+    const int sy = s * 4, sz = s * sy;
+    const float sm1 = (float)(s - 1);
+    const float ix = fminf(sm1, fmaxf(((px + 1.f) / 2.f) * sm1, 0.f));
+    const float iy = fminf(sm1, fmaxf(((py + 1.f) / 2.f) * sm1, 0.f));
+    const float iz = fminf(sm1, fmaxf(((pz + 1.f) / 2.f) * sm1, 0.f));
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+        const int src = p * 8 + (lane >> 2);
+        const float qx = __shfl_sync(FULL, ix, src);
+        const float qy = __shfl_sync(FULL, iy, src);
+        const float qz = __shfl_sync(FULL, iz, src);
+        float ws[8];
+        int v0;
+        bool nx, ny, nz;
+        corner_set_at(s, qx, qy, qz, v0, nx, ny, nz, ws);
+        const int o0 = v0 * 4;
+        const int ox = nx ? 4 : 0;
+        const int oy = ny ? sy : 0;
+        const int oz = nz ? sz : 0;
+        const int o[8] = {o0, o0 + ox, o0 + oy, o0 + oy + ox, o0 + oz, o0 + oz + ox, o0 + oz + oy, o0 + oz + oy + ox};
+        uint4 v[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) v[k] = load(o[k]);
+        float2 a2[4] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const float2 w2 = make_float2(ws[k], ws[k]);
+            a2[0] = __ffma2_rn(make_float2(bf_lo(v[k].x), bf_hi(v[k].x)), w2, a2[0]);
+            a2[1] = __ffma2_rn(make_float2(bf_lo(v[k].y), bf_hi(v[k].y)), w2, a2[1]);
+            a2[2] = __ffma2_rn(make_float2(bf_lo(v[k].z), bf_hi(v[k].z)), w2, a2[2]);
+            a2[3] = __ffma2_rn(make_float2(bf_lo(v[k].w), bf_hi(v[k].w)), w2, a2[3]);
+        }
+#pragma unroll
+        for (int c = 0; c < 4; ++c) acc[p][c] = __fadd2_rn(acc[p][c], a2[c]);
+    }
 }
 
 // Writes the tile rows row0 .. row0 + 8 * NP - 1 of gather_warp_pairs<NP>:
@@ -525,9 +552,11 @@ __global__ void __launch_bounds__(kTP, 4) sdf_fwd_bf16_tc_kernel(const Bf16Args 
 // ---------------------------------------------------------------------------
 // point query over pair volumes: persistent, coarse volumes in shared memory
 // ---------------------------------------------------------------------------
-// One 16-warp block per SM.  The leading pair volumes that fit (5^3 and 9^3
-// vertices, 109 KB, at base_lod 2) are copied into shared memory once per
-// block; the finer levels come through L2 with 32-byte loads.  The block is
+// One 16-warp block per SM.  The leading volumes that fit (5^3 and 9^3
+// vertices, 55 KB as bf16 vertex volumes, at base_lod 2) are copied into
+// shared memory once per block and gathered corner by corner
+// (verts_add_level); the finer levels come through L2 as pair lines with
+// 32-byte loads.  The block is
 // four independent groups of four warps, each with its own point tile and
 // its own 128 TMEM columns (4 x 128 = the SM's 512): a group gathers 128
 // points, writes their rows, its first thread issues the three K steps and
@@ -552,7 +581,7 @@ constexpr size_t kVolBudget = kSmemMax - kVol;
 constexpr size_t kSmemMin = 120 * 1024;
 constexpr uint32_t kCols = kGroups * kHid;
 static_assert(kB % 16 == 0 && kBar % 8 == 0 && kVol % 128 == 0, "shared layout alignment");
-static_assert(kVol + 109312 <= kSmemMax, "pair levels 5^3 and 9^3 fit");
+static_assert(kVol + 54656 <= kSmemMax, "levels 5^3 and 9^3 fit");
 }  // namespace b16st
 
 __device__ __forceinline__ void b16_group_sync(int g) {
@@ -591,8 +620,8 @@ __global__ void __launch_bounds__(b16st::kThreads, 1)
         size_t off = kVol;
         for (int l = first; l < first + nstaged; ++l) {
             const int s = (1 << (l + a.m.base_lod)) + 1;
-            const int cnt = s * s * s * 8;  // 16-byte pieces
-            const uint4 *src = static_cast<const uint4 *>(a.m.grid_pairs[l]);
+            const int cnt = s * s * s * 4;  // 16-byte pieces
+            const uint4 *src = static_cast<const uint4 *>(a.m.grid[l]);
             uint4 *dst = reinterpret_cast<uint4 *>(sm + off);
             for (int q = tid; q < cnt; q += kThreads) dst[q] = src[q];
             off += (size_t)cnt * 16;
@@ -611,7 +640,7 @@ __global__ void __launch_bounds__(b16st::kThreads, 1)
     const uint32_t dcol = tmem + (uint32_t)(grp * kHid);
     const uint32_t sa = tc::smem_addr(sA), sb = tc::smem_addr(sm + kB);
     const uint32_t idesc = tc::idesc_bf16_f32(kTP, kHid);
-    const int part = lane & 3, hs = (lane >> 2) & 1;
+    const int part = lane & 3;
     uint32_t phase = 0;
     bool pending = false;  // group leader: an issued product whose completion it did not see
 
@@ -630,12 +659,12 @@ __global__ void __launch_bounds__(b16st::kThreads, 1)
         for (int p = 0; p < 4; ++p)
 #pragma unroll
             for (int c = 0; c < 4; ++c) acc[p][c] = make_float2(0.f, 0.f);
-        const uint4 *vol = reinterpret_cast<const uint4 *>(sm + kVol) + 2 * part;  // 8 pieces per line
+        const uint4 *vol = reinterpret_cast<const uint4 *>(sm + kVol) + part;  // 4 pieces per vertex
 #pragma unroll 1
         for (int l = first; l < first + nstaged; ++l) {
             const int s = (1 << (l + a.m.base_lod)) + 1;
-            pairs_add_level<4>(s, px, py, pz, lane, acc, [vol, hs](int o) { return lds_pair_unit(vol + 2 * o, hs); });
-            vol += s * s * s * 8;
+            verts_add_level<4>(s, px, py, pz, lane, acc, [vol](int o) { return vol[o]; });
+            vol += s * s * s * 4;
         }
 #pragma unroll 1
         for (int l = first + nstaged; l <= L; ++l) {
@@ -1004,8 +1033,8 @@ static int sdf_fwd_bf16_impl(const nglod_bf16_model *model, const float *x, int6
         size_t vbytes = 0;
         for (int l = first; l <= L; ++l) {
             const size_t sd = (size_t)(1 << (l + model->base_lod)) + 1;
-            if (vbytes + sd * sd * sd * 128 > b16st::kVolBudget) break;
-            vbytes += sd * sd * sd * 128;
+            if (vbytes + sd * sd * sd * 64 > b16st::kVolBudget) break;
+            vbytes += sd * sd * sd * 64;
             ++nstaged;
         }
         const size_t smem = b16st::kVol + vbytes < b16st::kSmemMin ? b16st::kSmemMin : b16st::kVol + vbytes;
