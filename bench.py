@@ -105,15 +105,15 @@ TF32_NOMINAL_TFLOPS = 1100.0
 # traffic is null.
 NCU_CAPTURES = {
     "sdf_fwd_f32_staged_kernel": {
-        "dram_bytes": 91_318_784 + 11_194_624, "points": N_POINTS,
+        "dram_bytes": 91_279_872 + 10_913_024, "points": N_POINTS,
         "sources": ["nglod_gb300/csrc/dense.cu", "nglod_gb300/csrc/dense_common.cuh",
                     "nglod_gb300/csrc/tf32_tile.cuh", "nglod_gb300/csrc/tc_common.cuh"],
-        "sha256": "390c6158788a05ef15a4187d985ef0b2c4deb4d054fc136ddd1d4cb237c4b890",
+        "sha256": "36751d5dec46f13ed4a96cf9d6022884916da915a48fc829ea124017e0c87260",
         "how": "ncu --set full --clock-control none, one launch at 4,194,304 points (bench --no-extras)"},
     "sdf_fwd_bf16_staged_kernel": {
-        "dram_bytes": 90_524_160 + 11_049_216, "points": N_POINTS,
+        "dram_bytes": 90_247_168 + 10_010_368, "points": N_POINTS,
         "sources": ["nglod_gb300/csrc/bf16.cu", "nglod_gb300/csrc/bf16_tile.cuh", "nglod_gb300/csrc/tc_common.cuh"],
-        "sha256": "df7f80a31490e6140ca00f1563d41b5e8e5f2f77ded8375784d5ee72db2176ef",
+        "sha256": "dc15f91c3edeacffdc46a26102f70997d66fdf032c0b4f4930d55b34f08a0f92",
         "how": "ncu --set full --clock-control none, one launch at 4,194,304 points (bench --only bf16)"},
 }
 
