@@ -995,7 +995,7 @@ def bench_sparse(net, dev, flush, stream, level=7, lod=4, steps=64):
                                    prefix=s.GetPrefix()).shape[0]) for lv in range(lod + 3)]
     trav_bytes = sum(counts[lv] * (8 + 8 + 1 + 4 + 24) + counts[lv + 1] * 8 for lv in range(lod + 2))
     pk = peaks()
-    trav_roof = roofline("traverse_decide_kernel + traverse_emit_kernel", ms_trav / 1e3, {
+    trav_roof = roofline("traverse_level_kernel (one launch per level)", ms_trav / 1e3, {
         "hbm": (trav_bytes, pk["hbm_gbs"], "GB/s", f"{pk['source']} hbm_gbs")},
         {"nugget_level": {"bytes_in": 8 + 8 + 1 + 4 + 24, "bytes_out_per_hit_child": 8}},
         sum(counts[:lod + 2]), note="nugget counts per level " + ", ".join(map(str, counts)))

@@ -408,9 +408,13 @@ int nglod_spc_decode(const uint8_t *octree, int64_t osize, int16_t *points, int6
  * index) of every voxel at target_level the ray's line passes through, per
  * ray front to back, rays in order -- bit-exact with the reference.  All
  * levels run on the device with no host round trip.
- * nuggets_a/nuggets_b: two int32 [capacity][2] buffers; info, partials:
- * uint32 [capacity] and [capacity/1024 + 2]; ctrl: int64
- * [NGLOD_SPC_CTRL_WORDS] device.
+ * nuggets_a/nuggets_b: two int32 [capacity][2] buffers; info: uint32
+ * [max(capacity, 1024)], 8-byte aligned (chunk tickets and scan states);
+ * partials: uint32 [capacity/1024 + 2] (not used by this entry point; kept
+ * for the signature); ctrl: int64 [NGLOD_SPC_CTRL_WORDS] device.
+ * One launch per level: each 1024-nugget chunk finds its output offset by
+ * a bounded look-back over the preceding chunks (NGLOD_ERR_CUDA if a wait
+ * gave up).
  * On return (the call synchronises once) *count = number of nuggets and
  * *result_buffer = 0 (nuggets_a) or 1 (nuggets_b) holds them.  More than
  * `capacity` nuggets at any level: NGLOD_ERR_CAPACITY (the reference

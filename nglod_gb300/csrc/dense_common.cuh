@@ -58,12 +58,9 @@ __device__ __forceinline__ void stage_decoder(float4 *dst, const nglod_dense_mod
 // the corner offsets and weights themselves (shuffling the corner index and
 // the eight weights instead takes nine shuffles, which load the shared-memory
 // crossbar the tensor-core kernels also use).  acc[p] += this lane's four
-// channels of point 4p + lane / 8.  load(i) returns float4 i of the volume
-// (eight per vertex); gather_warp_add_f32 reads global memory,
-// gather_warp_add_f32_shared a volume staged in shared memory.
-template <typename Load>
-__device__ __forceinline__ void gather_warp_add_f32_by(Load load, int s, float px, float py, float pz, int lane,
-                                                       float4 (&acc)[8]) {
+// channels of point 4p + lane / 8.
+__device__ __forceinline__ void gather_warp_add_f32(const float *__restrict__ g, int s, float px, float py, float pz,
+                                                    int lane, float4 (&acc)[8]) {
     const unsigned FULL = 0xffffffffu;
     const float sm1 = (float)(s - 1);
     float ix = ((px + 1.f) / 2.f) * sm1;
@@ -72,7 +69,7 @@ __device__ __forceinline__ void gather_warp_add_f32_by(Load load, int s, float p
     ix = fminf(sm1, fmaxf(ix, 0.f));
     iy = fminf(sm1, fmaxf(iy, 0.f));
     iz = fminf(sm1, fmaxf(iz, 0.f));
-    const int part = lane & 7;  // this lane's float4 of a vertex
+    const float4 *g4 = reinterpret_cast<const float4 *>(g) + (lane & 7);  // 8 float4 per vertex
     const int sy = s * 8, sz = s * sy;
 #pragma unroll
     for (int p = 0; p < 8; ++p) {
@@ -102,7 +99,7 @@ __device__ __forceinline__ void gather_warp_add_f32_by(Load load, int s, float p
         const int o[8] = {o0, o0 + ox, o0 + oy, o0 + oy + ox, o0 + oz, o0 + oz + ox, o0 + oz + oy, o0 + oz + oy + ox};
         float4 v[8];
 #pragma unroll
-        for (int k = 0; k < 8; ++k) v[k] = load(o[k] + part);
+        for (int k = 0; k < 8; ++k) v[k] = __ldg(g4 + o[k]);
         float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
@@ -118,17 +115,62 @@ __device__ __forceinline__ void gather_warp_add_f32_by(Load load, int s, float p
     }
 }
 
-__device__ __forceinline__ void gather_warp_add_f32(const float *__restrict__ g, int s, float px, float py, float pz,
-                                                    int lane, float4 (&acc)[8]) {
-    const float4 *g4 = reinterpret_cast<const float4 *>(g);
-    gather_warp_add_f32_by([g4](int i) { return __ldg(g4 + i); }, s, px, py, pz, lane, acc);
-}
-
-// The same gather from a volume staged in shared memory (v points into the
-// kernel's shared-memory array; channel-last, 128 B per vertex).
+// gather_warp_add_f32 over a volume staged in shared memory (v points into
+// the kernel's shared-memory array; channel-last, 128 B per vertex): the same
+// expressions in the same order, so the same sums.
 __device__ __forceinline__ void gather_warp_add_f32_shared(const float4 *v, int s, float px, float py, float pz,
                                                            int lane, float4 (&acc)[8]) {
-    gather_warp_add_f32_by([v](int i) { return v[i]; }, s, px, py, pz, lane, acc);
+    const unsigned FULL = 0xffffffffu;
+    const float sm1 = (float)(s - 1);
+    float ix = ((px + 1.f) / 2.f) * sm1;
+    float iy = ((py + 1.f) / 2.f) * sm1;
+    float iz = ((pz + 1.f) / 2.f) * sm1;
+    ix = fminf(sm1, fmaxf(ix, 0.f));
+    iy = fminf(sm1, fmaxf(iy, 0.f));
+    iz = fminf(sm1, fmaxf(iz, 0.f));
+    const float4 *g4 = v + (lane & 7);  // 8 float4 per vertex
+    const int sy = s * 8, sz = s * sy;
+#pragma unroll
+    for (int p = 0; p < 8; ++p) {
+        const int src = 4 * p + (lane >> 3);
+        const float qx = __shfl_sync(FULL, ix, src);
+        const float qy = __shfl_sync(FULL, iy, src);
+        const float qz = __shfl_sync(FULL, iz, src);
+        const float x0 = floorf(qx), y0 = floorf(qy), z0 = floorf(qz);
+        const float wx1 = qx - x0, wx0 = (x0 + 1.f) - qx;
+        const float wy1 = qy - y0, wy0 = (y0 + 1.f) - qy;
+        const float wz1 = qz - z0, wz0 = (z0 + 1.f) - qz;
+        const int xi = (int)x0, yi = (int)y0, zi = (int)z0;
+        float ws[8];
+        ws[0] = wx0 * wy0 * wz0;
+        ws[1] = wx1 * wy0 * wz0;
+        ws[2] = wx0 * wy1 * wz0;
+        ws[3] = wx1 * wy1 * wz0;
+        ws[4] = wx0 * wy0 * wz1;
+        ws[5] = wx1 * wy0 * wz1;
+        ws[6] = wx0 * wy1 * wz1;
+        ws[7] = wx1 * wy1 * wz1;
+        const int o0 = ((zi * s + yi) * s + xi) * 8;
+        const int ox = xi + 1 < s ? 8 : 0;
+        const int oy = yi + 1 < s ? sy : 0;
+        const int oz = zi + 1 < s ? sz : 0;
+        const int o[8] = {o0, o0 + ox, o0 + oy, o0 + oy + ox, o0 + oz, o0 + oz + ox, o0 + oz + oy, o0 + oz + oy + ox};
+        float4 vv[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) vv[k] = g4[o[k]];
+        float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            a0 = fmaf(vv[k].x, ws[k], a0);
+            a1 = fmaf(vv[k].y, ws[k], a1);
+            a2 = fmaf(vv[k].z, ws[k], a2);
+            a3 = fmaf(vv[k].w, ws[k], a3);
+        }
+        acc[p].x += a0;
+        acc[p].y += a1;
+        acc[p].z += a2;
+        acc[p].w += a3;
+    }
 }
 
 // Row stride (floats) of the per-warp transpose buffer: 36, so that the

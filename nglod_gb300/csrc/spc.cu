@@ -138,17 +138,26 @@ __device__ __forceinline__ uint32_t origin_octant(const float *__restrict__ org,
 }
 
 // ---------------------------------------------------------------------------
-// traversal kernels
+// traversal kernel
 // ---------------------------------------------------------------------------
 // Level l's pass turns the nuggets of level l (voxels the ray is known to
 // hit; at level 0 every ray with the root, tested here) into the nuggets of
 // level l+1: the children of each voxel that are occupied and hit by the
-// ray, nearest first.  "decide" tests the children and stores per nugget
-// the hit mask (bits 0-7, by child index) and the origin octant (bits 8-10);
-// "emit" writes the children of the mask in the octant's order.  Both
-// produce the reference's nuggets exactly: the reference emits every
+// ray, nearest first.  One launch per level, one 1024-nugget chunk per block
+// iteration: the block tests its nuggets' children (hit mask and origin
+// octant per nugget, kept in registers), scans the hit counts, finds the
+// chunk's output offset by a decoupled look-back over the preceding chunks'
+// published counts, and writes the hit children in the octant's order.
+// This produces the reference's nuggets exactly: the reference emits every
 // occupied child and drops the missed ones at the next level, which leaves
 // the same children in the same order.
+//
+// Chunks are taken in ticket order (one atomic per block iteration), so a
+// chunk's predecessors belong to blocks that are already running and
+// publish their counts without waiting on anything; the look-back reads 32
+// predecessors' states per step, each wait is bounded (kLookbackPolls), and
+// a wait that gives up raises the status (kStatusLookback) instead of
+// hanging.
 struct TraverseArgs {
     const uint8_t *octree;
     const short4 *points;  // all levels
@@ -157,8 +166,8 @@ struct TraverseArgs {
     const float *dir;
     const int2 *in;  // nuggets of this level (unused at level 0)
     int2 *out;
-    uint32_t *info;
-    uint32_t *partials;
+    unsigned long long *state;  // this level's chunk states
+    uint32_t *ticket;           // this level's chunk ticket
     int64_t *ctrl;
     int64_t capacity;
     int level;       // current level
@@ -167,29 +176,58 @@ struct TraverseArgs {
     int64_t off1;    // ... of the next level's
 };
 
+// Chunk state word: flag in bits 32-33 (kStateCount: the chunk's own hit
+// count; kStatePrefix: its inclusive prefix), the value in bits 0-31.
+constexpr unsigned long long kStateCount = 1ull << 32, kStatePrefix = 2ull << 32;
+constexpr uint32_t kLookbackPolls = 1u << 22;
+constexpr int64_t kStatusLookback = 2;
+// Scratch of nglod_spc_raytrace in its `info` buffer: 16 tickets, then the
+// chunk states of each pass.
+constexpr int64_t kTicketBytes = 64;
+inline int64_t state_words(int64_t capacity) { return (capacity + kChunk - 1) / kChunk + 1; }
+
 __device__ __forceinline__ int2 nugget_at(const TraverseArgs &a, int64_t i) {
     if (a.level == 0) return make_int2((int)i, 0);
     return a.in[i];
 }
 
-__global__ void __launch_bounds__(kChunk) traverse_decide_kernel(const TraverseArgs a) {
+__global__ void __launch_bounds__(kChunk, 2) traverse_level_kernel(const TraverseArgs a) {
     __shared__ uint32_t s_warp[33];
-    if (a.ctrl[kCtrlStatus] != 0) return;
+    __shared__ uint32_t s_order[8];
+    __shared__ int64_t s_chunk;
+    __shared__ uint32_t s_excl;
+    if (threadIdx.x < 8) s_order[threadIdx.x] = c_child_order[threadIdx.x];
     const int64_t count = a.ctrl[kCtrlCount + a.level];
     const int64_t nchunks = (count + kChunk - 1) / kChunk;
-    for (int64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
+    // an empty level has no last chunk to write the next level's count
+    if (nchunks == 0 && blockIdx.x == 0 && threadIdx.x == 0) a.ctrl[kCtrlCount + a.level + 1] = 0;
+    volatile unsigned long long *st = a.state;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const int64_t c = (int64_t)atomicAdd(a.ticket, 1u);
+            // after a raised status (an earlier level overflowed, or a wait
+            // gave up) nothing more is read or written
+            s_chunk = *(volatile int64_t *)(a.ctrl + kCtrlStatus) != 0 ? nchunks : c;
+        }
+        __syncthreads();
+        const int64_t c = s_chunk;
+        if (c >= nchunks) break;
+        // 1. decide: the hit mask (bits 0-7, by child index) and the origin
+        // octant (bits 8-10) of this thread's nugget
         const int64_t i = c * kChunk + threadIdx.x;
-        uint32_t v = 0;
+        uint32_t inf = 0;
+        int2 nug = make_int2(0, 0);
+        uint32_t o = 0;
+        int64_t node = 0;
         if (i < count) {
-            const int2 nug = nugget_at(a, i);
-            const int64_t node = a.off0 + nug.y;
+            nug = nugget_at(a, i);
+            node = a.off0 + nug.y;
             const short4 p = a.points[node];
-            uint32_t inf = 0;
             if (a.level > 0 || ray_hits_voxel(a.org, a.dir, (uint32_t)nug.x, p, 0)) {
                 if (a.level == a.target) {
                     inf = 1u;
                 } else {
-                    const uint32_t o = a.octree[node];
+                    o = a.octree[node];
                     const RayFaces f = ray_faces(a.org, a.dir, (uint32_t)nug.x, a.level + 1);
                     const float bx = (float)(2 * (int)p.x), by = (float)(2 * (int)p.y), bz = (float)(2 * (int)p.z);
 #pragma unroll
@@ -201,44 +239,80 @@ __global__ void __launch_bounds__(kChunk) traverse_decide_kernel(const TraverseA
                     inf |= origin_octant(a.org, (uint32_t)nug.x, p, a.level) << 8;
                 }
             }
-            a.info[i] = inf;
-            v = (uint32_t)__popc(inf & 0xffu);
         }
-        const uint32_t s = block_sum(v, s_warp);
-        if (threadIdx.x == 0) a.partials[c] = s;
-    }
-}
-
-__global__ void __launch_bounds__(kChunk) traverse_emit_kernel(const TraverseArgs a) {
-    __shared__ uint32_t s_warp[33];
-    __shared__ uint32_t s_order[8];
-    if (threadIdx.x < 8) s_order[threadIdx.x] = c_child_order[threadIdx.x];
-    __syncthreads();
-    if (a.ctrl[kCtrlStatus] != 0) return;
-    const int64_t count = a.ctrl[kCtrlCount + a.level];
-    const int64_t nchunks = (count + kChunk - 1) / kChunk;
-    for (int64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
-        const int64_t i = c * kChunk + threadIdx.x;
-        const uint32_t inf = i < count ? a.info[i] : 0u;
         const uint32_t v = (uint32_t)__popc(inf & 0xffu);
         uint32_t tot;
         const uint32_t ex = block_exclusive_scan(v, s_warp, &tot);
-        if (v == 0) continue;
-        int64_t pos = (int64_t)a.partials[c] + ex;
-        const int2 nug = nugget_at(a, i);
-        if (a.level == a.target) {
-            a.out[pos] = nug;
-            continue;
-        }
-        const int64_t node = a.off0 + nug.y;
-        const uint32_t o = a.octree[node];
-        const int64_t first = (int64_t)a.prefix[node] - a.off1;
-        uint32_t ord = s_order[inf >> 8];
+        // 2. the chunk's offset: publish its count, then warp 0 adds the
+        // predecessors' counts 32 chunks at a time, back to the nearest chunk
+        // that has published its inclusive prefix
+        if (threadIdx.x < 32) {
+            const int lane = threadIdx.x;
+            uint32_t excl = 0;
+            if (c == 0) {
+                if (lane == 0) st[0] = kStatePrefix | tot;
+            } else {
+                if (lane == 0) st[c] = kStateCount | tot;
+                int64_t k = c - 1;
+                uint32_t polls = 0;
+                bool failed = false;
+                for (;;) {
+                    const int64_t idx = k - lane;
+                    unsigned long long w = kStatePrefix;  // before chunk 0: an empty prefix
+                    if (idx >= 0) w = st[idx];
+                    const unsigned pmask = __ballot_sync(0xffffffffu, (w & kStatePrefix) != 0);
+                    const unsigned dmask = __ballot_sync(0xffffffffu, (w & (kStatePrefix | kStateCount)) != 0);
+                    const int jp = pmask ? __ffs(pmask) - 1 : 32;  // nearest inclusive prefix
+                    const unsigned need = jp == 32 ? 0xffffffffu : (2u << jp) - 1u;
+                    if ((dmask & need) == need) {
+                        uint32_t val = lane <= jp ? (uint32_t)w : 0u;
 #pragma unroll
-        for (int r = 0; r < 8; ++r, ord >>= 3) {
-            const uint32_t j = ord & 7u;
-            if (inf & (1u << j)) a.out[pos++] = make_int2(nug.x, (int)(first + __popc(o & ((2u << j) - 1u))));
+                        for (int o = 16; o > 0; o >>= 1) val += __shfl_xor_sync(0xffffffffu, val, o);
+                        excl += val;
+                        if (jp < 32) break;
+                        k -= 32;
+                        polls = 0;
+                    } else if (++polls > kLookbackPolls) {
+                        failed = true;
+                        break;
+                    } else if (polls > 32) {
+                        __nanosleep(64);
+                    }
+                }
+                if (lane == 0) {
+                    if (failed)
+                        atomicExch(reinterpret_cast<unsigned long long *>(a.ctrl + kCtrlStatus),
+                                   (unsigned long long)kStatusLookback);
+                    st[c] = kStatePrefix | (excl + tot);
+                }
+            }
+            if (lane == 0) {
+                s_excl = excl;
+                if (c == nchunks - 1) {
+                    const int64_t total = (int64_t)excl + tot;
+                    a.ctrl[kCtrlCount + a.level + 1] = total;
+                    if (total > a.capacity)
+                        atomicExch(reinterpret_cast<unsigned long long *>(a.ctrl + kCtrlStatus), 1ull);
+                }
+            }
         }
+        __syncthreads();
+        // 3. emit the hit children nearest first (nothing beyond the capacity)
+        int64_t pos = (int64_t)s_excl + ex;
+        if (v != 0 && pos + v <= a.capacity) {
+            if (a.level == a.target) {
+                a.out[pos] = nug;
+            } else {
+                const int64_t first = (int64_t)a.prefix[node] - a.off1;
+                uint32_t ord = s_order[inf >> 8];
+#pragma unroll
+                for (int r = 0; r < 8; ++r, ord >>= 3) {
+                    const uint32_t j = ord & 7u;
+                    if (inf & (1u << j)) a.out[pos++] = make_int2(nug.x, (int)(first + __popc(o & ((2u << j) - 1u))));
+                }
+            }
+        }
+        __syncthreads();  // s_chunk, s_excl and s_warp are reused by the next chunk
     }
 }
 
@@ -635,26 +709,31 @@ extern "C" int nglod_spc_raytrace(const uint8_t *octree, const int16_t *points, 
     *result_buffer = passes % 2;
     *count = 0;
     if (n_rays == 0) return NGLOD_OK;
-    NGLOD_REQUIRE(octree && points && prefix && org && dir && nuggets_a && nuggets_b && info && partials && ctrl,
+    NGLOD_REQUIRE(octree && points && prefix && org && dir && nuggets_a && nuggets_b && info && ctrl,
                   NGLOD_ERR_INVALID, "null pointer argument");
     NGLOD_REQUIRE(aligned(points, 8) && aligned(nuggets_a, 8) && aligned(nuggets_b, 8) && aligned(ctrl, 8),
                   NGLOD_ERR_ALIGN, "points, nuggets and ctrl must be 8-byte aligned");
+    NGLOD_REQUIRE(aligned(info, 8), NGLOD_ERR_ALIGN, "info must be 8-byte aligned");
     cudaStream_t s = (cudaStream_t)stream;
     int64_t init[kCtrlCount + 1] = {0, 0, 0, 0, n_rays};
     NGLOD_TRY(cuda_status(cudaMemcpyAsync(ctrl, init, sizeof(init), cudaMemcpyHostToDevice, s), "raytrace copy"));
+    // tickets and chunk states of every pass start at zero
+    const int64_t nstate = state_words(capacity);
+    NGLOD_TRY(cuda_status(cudaMemsetAsync(info, 0, (size_t)(kTicketBytes + passes * nstate * 8), s),
+                          "raytrace scratch"));
     TraverseArgs a;
     a.octree = octree;
     a.points = reinterpret_cast<const short4 *>(points);
     a.prefix = prefix;
     a.org = org;
     a.dir = dir;
-    a.info = info;
-    a.partials = partials;
     a.ctrl = ctrl;
     a.capacity = capacity;
     a.target = target_level;
     const int32_t *psum = pyramid_host + (level + 2);
     int2 *buf[2] = {reinterpret_cast<int2 *>(nuggets_a), reinterpret_cast<int2 *>(nuggets_b)};
+    unsigned long long *states =
+        reinterpret_cast<unsigned long long *>(reinterpret_cast<uint8_t *>(info) + kTicketBytes);
     const int grid = grid_for((capacity + kChunk - 1) / kChunk);
     for (int l = 0; l < passes; ++l) {
         a.level = l;
@@ -662,10 +741,9 @@ extern "C" int nglod_spc_raytrace(const uint8_t *octree, const int16_t *points, 
         a.off1 = psum[l + 1];
         a.in = buf[l % 2];
         a.out = buf[(l + 1) % 2];
-        traverse_decide_kernel<<<grid, kChunk, 0, s>>>(a);
-        scan_chunk_counts_kernel<<<1, kChunk, 0, s>>>(partials, ctrl + kCtrlCount + l, ctrl + kCtrlCount + l + 1,
-                                                      capacity, ctrl + kCtrlStatus);
-        traverse_emit_kernel<<<grid, kChunk, 0, s>>>(a);
+        a.state = states + l * nstate;
+        a.ticket = info + l;
+        traverse_level_kernel<<<grid, kChunk, 0, s>>>(a);
     }
     NGLOD_TRY(launch_status("nglod_spc_raytrace"));
     int64_t res[kCtrlCount + kMaxSpcLevels + 1];
@@ -673,6 +751,8 @@ extern "C" int nglod_spc_raytrace(const uint8_t *octree, const int16_t *points, 
                                           cudaMemcpyDeviceToHost, s),
                           "raytrace copy"));
     NGLOD_TRY(cuda_status(cudaStreamSynchronize(s), "raytrace sync"));
+    NGLOD_REQUIRE(res[kCtrlStatus] != kStatusLookback, NGLOD_ERR_CUDA,
+                  "spc_raytrace: a chunk's wait for its predecessors gave up");
     NGLOD_REQUIRE(res[kCtrlStatus] == 0, NGLOD_ERR_CAPACITY,
                   "spc_raytrace: more than capacity=%lld nuggets at some level", (long long)capacity);
     *count = res[kCtrlCount + passes];

@@ -182,7 +182,7 @@ def spc_raytrace(octree, points, pyramid, Org, Dir, targetLevel, prefix=None, ca
     while True:
         a = torch.empty(capacity, 2, dtype=torch.int32, device=dev)
         b = torch.empty(capacity, 2, dtype=torch.int32, device=dev)
-        info = torch.empty(capacity, dtype=torch.int32, device=dev)
+        info = torch.empty(max(capacity, 1024), dtype=torch.int32, device=dev)
         partials = torch.empty(capacity // 1024 + 2, dtype=torch.int32, device=dev)
         ctrl = torch.empty(CTRL_WORDS, dtype=torch.int64, device=dev)
         count = ctypes.c_int64(0)

@@ -112,7 +112,7 @@ def test_raytrace_capacity_and_empty(cuda):
     lib = _lib.load()
     cap = o.shape[0]
     bufs = [torch.empty(cap, 2, dtype=torch.int32, device=cuda) for _ in range(2)]
-    info = torch.empty(cap, dtype=torch.int32, device=cuda)
+    info = torch.empty(max(cap, 1024), dtype=torch.int32, device=cuda)
     parts = torch.empty(cap // 1024 + 2, dtype=torch.int32, device=cuda)
     ctrl = torch.empty(spc.CTRL_WORDS, dtype=torch.int64, device=cuda)
     import ctypes
