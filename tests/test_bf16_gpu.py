@@ -11,7 +11,7 @@ from nglod_gb300.analytic_init import init_from_sdf
 from nglod_gb300.bf16 import Bf16OctreeSDF
 from nglod_gb300.options import default_args
 from oracle import dense
-from tests.helpers import oracle_model
+from tests.helpers import seeded_model, oracle_model
 
 pytestmark = pytest.mark.gpu
 
@@ -204,6 +204,28 @@ def test_pair_volumes_are_built_and_give_identical_results(nets):
         assert torch.equal(a, b), (lod, (a - b).abs().max().item())
     np.testing.assert_allclose(a.cpu().numpy(), emulate(m32, x.cpu().numpy(), bnet.num_lods - 1), atol=2e-4, rtol=0)
     bnet.check_status()
+    plain.check_status()
+
+
+@pytest.mark.parametrize("base_lod,num_lods", [(1, 4), (3, 3), (4, 2)])
+def test_staged_query_variants_equal_the_vertex_kernel(cuda, base_lod, num_lods):
+    """The persistent BF16 query stages the leading vertex volumes that fit
+    in shared memory (three at base_lod 1: 3^3, 5^3, 9^3; one at base_lod 3;
+    none at base_lod 4) and reads the rest as pair lines; at every lod its
+    results equal the vertex-volume kernel's bit for bit (same corner order
+    and weights), on ragged sizes and points outside the box."""
+    net = seeded_model(num_lods=num_lods, base_lod=base_lod, seed=base_lod).to(cuda)
+    staged = Bf16OctreeSDF(net)
+    plain = Bf16OctreeSDF(net, pairs=False)
+    assert staged.pairs and not plain.pairs
+    gen = torch.Generator().manual_seed(5 + base_lod)
+    for n in [1, 127, 129, 513, 40_001]:
+        x = (torch.rand(n, 3, generator=gen) * 2.4 - 1.2).to(cuda)
+        for lod in range(num_lods):
+            a = staged.sdf(x, lod=lod)
+            b = plain.sdf(x, lod=lod)
+            assert torch.equal(a, b), (n, lod, (a - b).abs().max().item())
+    staged.check_status()
     plain.check_status()
 
 

@@ -237,6 +237,29 @@ def test_tensor_core_f32_query_within_float32_bounds(full_net, lod):
     assert (tc - simt).abs().max().item() < 2e-6
 
 
+@pytest.mark.parametrize("base_lod,num_lods,lod", [(1, 4, 3), (2, 2, 1), (3, 3, 2), (2, 5, 0), (4, 2, 1)])
+def test_tensor_core_f32_query_staging_variants(cuda, base_lod, num_lods, lod):
+    """The persistent float32 query stages the leading volumes that fit in
+    shared memory beside its tiles: three levels at base_lod 1 (3^3, 5^3,
+    9^3), two at base_lod 2, one at base_lod 3 (9^3; 17^3 does not fit), none
+    at base_lod 4, only LOD 0 when lod = 0.  Each variant against the
+    per-thread float32 decoder and float64, on ragged sizes (partial last
+    tile, fewer tiles than groups, points outside the box)."""
+    net = seeded_model(num_lods=num_lods, base_lod=base_lod, seed=base_lod).to(cuda)
+    m64 = oracle_model(net.cpu(), np.float64)
+    net.to(cuda)
+    gen = torch.Generator().manual_seed(11 + base_lod)
+    for n in [1, 127, 129, 513, 70_001]:
+        x = (torch.rand(n, 3, generator=gen) * 2.4 - 1.2).to(cuda)
+        with torch.no_grad():
+            tc = net.sdf(x, lod=lod)
+        net.check_status()
+        simt = _simt(net, x, lod)
+        want = dense.sdf(m64, x.cpu().numpy().astype(np.float64), lod=lod)
+        assert np.abs(tc.cpu().numpy().astype(np.float64) - want).max() < SDF_TOL, n
+        assert (tc - simt).abs().max().item() < 2e-6, n
+
+
 def test_tensor_core_f32_wait_timeout_reports_status_and_recovers(full_net):
     """The error path of the float32 query's bounded tensor-core wait,
     without a GPU fault: with the wait cut to one non-blocking test the call
