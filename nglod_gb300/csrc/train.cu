@@ -23,7 +23,7 @@
 
 #include "dense_common.cuh"
 #include "tc_common.cuh"
-#include "tf32_tile.cuh"
+#include "f32_tile.cuh"
 
 namespace nglod {
 
@@ -88,29 +88,31 @@ __global__ void __launch_bounds__(kFwdTrainThreads, 1)
 // ---------------------------------------------------------------------------
 // forward for training, tensor-core form (hidden_dim 128, ReLU masks wanted)
 // ---------------------------------------------------------------------------
-// The decoder's first layer, feature part P [128 pts x 128 hid] =
-// F [pts x 32] . W^T, runs on tcgen05 as kind::tf32 products over big / small
-// splits of both operands (tf32_tile.cuh: relative error about 2^-21, the
-// size of the float32 path's own rounding), accumulated in TMEM.  The x y z
-// and bias terms, ReLU, the ReLU mask and the 128 -> 1 layer are a float32
-// epilogue per point.  Units whose pre-activation lies within the split
-// products' error of zero (a few per thousand points) are evaluated again in
-// float32 with the per-thread decoder's order, so that the saved ReLU mask
-// is the float32 path's decision.
+// The decoder's first layer, P [128 pts x 128 hid] = [F, x y z, 1] . [W, b0]^T,
+// runs on tcgen05 as kind::tf32 products over big / small splits of both
+// operands (the point tiles of f32_tile.cuh: relative error about 2^-21, the
+// size of the float32 path's own rounding), accumulated in TMEM.  ReLU, the
+// ReLU mask and the 128 -> 1 layer are a float32 epilogue per point.  Units
+// whose pre-activation lies within the split products' error of zero (a few
+// per thousand points) are evaluated again in float32 with the per-thread
+// decoder's order, so that the saved ReLU mask is the float32 path's
+// decision.
 // A block of eight warps handles two 128-point tiles per iteration against
-// one staged weight tile (the layout of sdf_fwd_f32_tc_kernel: warps 0-3
+// one staged weight tile (the layout of the fused float32 tracer: warps 0-3
 // fill tile 0, warps 4-7 tile 1; two blocks per SM hold 2 x 256 TMEM
 // columns).  Blocks run LOD by LOD so that each LOD's weights are staged
 // once: a block visits the same points at every LOD, and the running
 // feature sum of a point is carried through feats (row l-1 is read back by
 // the very lanes that wrote it), which therefore holds every row 0..L.
 namespace fwdtc {
-constexpr int kTP = 128, kTiles = 2, kThreads = kTP * kTiles, kH = 128, kK = 32, kKC = kK / 4;
-// point tiles: K-adjacent core matrices 144 B apart, so that a quarter warp's
-// eight 16-byte stores of one row hit eight bank groups
-constexpr uint32_t kLboA = 144, kSboA = kKC * kLboA, kTileA = (kTP / 8) * kSboA;  // 18 KB
-constexpr uint32_t kTileW = kH * kK * 4;                                          // 16 KB
-constexpr size_t kA = 0, kW = 2 * kTiles * kTileA, kU = kW + 2 * kTileW, kW1 = kU + kH * 16;
+using f32tile::kH;
+using f32tile::kK;
+using f32tile::kTileA;
+using f32tile::kTileF;
+using f32tile::kTP;
+using f32tile::kWBytes;
+constexpr int kTiles = 2, kThreads = kTP * kTiles;
+constexpr size_t kA = 0, kW = kTiles * kTileA, kW1 = kW + kWBytes;
 constexpr size_t kBar = kW1 + kH * 4, kSlot = kBar + 8, kAbort = kSlot + 4;
 constexpr size_t kSmem = kAbort + 12;
 constexpr uint32_t kCols = kTiles * kH;
@@ -118,26 +120,22 @@ constexpr uint32_t kPolls = 1u << 22;
 // |P| below which a unit's sign is settled by a float32 evaluation: above the
 // split products' error (about 2^-21 of sum |w x|) for sums up to ~20
 constexpr float kNearZero = 1e-5f;
-static_assert(kTileA % 128 == 0 && kW % 1024 == 0 && kU % 16 == 0 && kBar % 8 == 0, "shared layout alignment");
-static_assert(2 * kSmem <= 227 * 1024, "two blocks per SM");
-
-__host__ __device__ constexpr uint32_t a_offset(int row, int k) {
-    return (uint32_t)((row / 8) * kSboA + (k / 4) * kLboA + (row % 8) * 16 + (k % 4) * 4);
-}
+static_assert(kW % 1024 == 0 && kBar % 8 == 0, "shared layout alignment");
+static_assert(2 * (kSmem + 1024) <= 228 * 1024, "two blocks per SM");
 }  // namespace fwdtc
 
-// Hidden unit j's pre-activation for point row r of a tile, in float32 with
-// decode_f32's order (inputs x y z, features, 1; products of even and odd
-// float4 groups summed apart, then added).  The features are big + small of
-// the tile, which is exact.
-__device__ __noinline__ float pre_f32(const uint8_t *abig, const uint8_t *asmall, int r, float px, float py,
-                                      float pz, const float *__restrict__ w0, const float *__restrict__ b0, int j) {
+// Hidden unit j's pre-activation for point row r of a point tile, in
+// float32 with decode_f32's order (inputs x y z, features, 1; products of
+// even and odd float4 groups summed apart, then added).  The features are
+// big + small of the tile, which is exact.
+__device__ __noinline__ float pre_f32(const uint8_t *tile, int r, float px, float py, float pz,
+                                      const float *__restrict__ w0, const float *__restrict__ b0, int j) {
     using namespace fwdtc;
     auto in_at = [&](int k) -> float {  // decode_f32's input k
         if (k < 3) return k == 0 ? px : (k == 1 ? py : pz);
         if (k == 35) return 1.f;
-        const uint32_t off = a_offset(r, k - 3);
-        return *reinterpret_cast<const float *>(abig + off) + *reinterpret_cast<const float *>(asmall + off);
+        const uint32_t off = tile_offset32_sw128(r, k - 3);
+        return *reinterpret_cast<const float *>(tile + off) + *reinterpret_cast<const float *>(tile + kTileF + off);
     };
     float a0 = 0.f, a1 = 0.f;
 #pragma unroll 1
@@ -162,7 +160,6 @@ __global__ void __launch_bounds__(fwdtc::kThreads, 2)
     using namespace fwdtc;
     extern __shared__ __align__(1024) uint8_t smem_fw[];
     uint8_t *sm = smem_fw;
-    const float4 *su = reinterpret_cast<const float4 *>(sm + kU);
     const float *w1s = reinterpret_cast<const float *>(sm + kW1);
     uint64_t *bar = reinterpret_cast<uint64_t *>(sm + kBar);
     uint32_t *slot = reinterpret_cast<uint32_t *>(sm + kSlot);
@@ -180,9 +177,7 @@ __global__ void __launch_bounds__(fwdtc::kThreads, 2)
     tc::fence_after_sync();
     const uint32_t tmem = *slot;
     const uint32_t sbase = tc::smem_addr(sm);
-    constexpr uint32_t idesc = idesc_tf32_f32(kTP, kH);
-    uint8_t *abig = sm + kA + (size_t)2 * half * kTileA;
-    uint8_t *asmall = abig + kTileA;
+    uint8_t *tile = sm + kA + (size_t)half * kTileA;
     const uint32_t taddr = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(half * kH);
     const int row = quad * 32 + lane;  // this thread's point row in its tile
     uint32_t phase = 0;
@@ -190,21 +185,9 @@ __global__ void __launch_bounds__(fwdtc::kThreads, 2)
 #pragma unroll 1
     for (int l = 0; l <= L && !*abort_flag; ++l) {
         const bool decode = (mask >> l) & 1u;
-        if (decode) {
-            // weights of this LOD: feature part split big / small, x y z and b0, w1
-            const float *w0 = m.w0[l];
-            for (int u = tid; u < kH * kKC; u += kThreads) {
-                const int j = u / kKC, kc = u % kKC;
-                const float *r = w0 + j * 35 + 3 + 4 * kc;
-                store_split4(sm + kW, sm + kW + kTileW, tile_offset32(j, 4 * kc, kKC),
-                             make_float4(r[0], r[1], r[2], r[3]));
-            }
-            if (tid < kH) {
-                reinterpret_cast<float4 *>(sm + kU)[tid] =
-                    make_float4(w0[tid * 35], w0[tid * 35 + 1], w0[tid * 35 + 2], m.b0[l][tid]);
-                reinterpret_cast<float *>(sm + kW1)[tid] = m.w1[l][tid];
-            }
-        }
+        // this LOD's decoder (the weight side of the point tiles, w1); the
+        // previous LOD's products all completed before its last barrier
+        if (decode) stage_tf32_decoder(m, l, sm + kW, sm + kW1, tid, kThreads);
         const float b1 = decode ? m.b1[l][0] : 0.f;
         const int s = volume_side(m, l);
 #pragma unroll 1
@@ -233,29 +216,16 @@ __global__ void __launch_bounds__(fwdtc::kThreads, 2)
                 if (ip < n) reinterpret_cast<float4 *>(feats + ((int64_t)l * n + ip) * kC)[lane & 7] = acc[p];
             }
             if (!decode) continue;
-#pragma unroll
-            for (int p = 0; p < 8; ++p)
-                store_split4(abig, asmall, a_offset(quad * 32 + 4 * p + (lane >> 3), 4 * (lane & 7)), acc[p]);
+            store_point_rows(tile, quad * 32, lane, acc, px, py, pz);
             tc::fence_proxy_async_smem();
             tc::fence_before_sync();
             __syncthreads();
             if (tid == 0) {
                 tc::fence_after_sync();
-                const uint64_t wb = tc::smem_desc(sbase + (uint32_t)kW, 128, kKC * 128);
-                const uint64_t ws = tc::smem_desc(sbase + (uint32_t)(kW + kTileW), 128, kKC * 128);
 #pragma unroll
-                for (int h = 0; h < kTiles; ++h) {
-                    const uint64_t ab = tc::smem_desc(sbase + (uint32_t)(kA + 2 * h * kTileA), kLboA, kSboA);
-                    const uint64_t as = tc::smem_desc(sbase + (uint32_t)(kA + (2 * h + 1) * kTileA), kLboA, kSboA);
-#pragma unroll
-                    for (int t = 0; t < 3; ++t)
-#pragma unroll
-                        for (int ks = 0; ks < kK / 8; ++ks) {
-                            const uint64_t sa = (uint64_t)((ks * 2 * kLboA) >> 4), sw = (uint64_t)((ks * 256) >> 4);
-                            mma_tf32(tmem + (uint32_t)(h * kH), (t == 2 ? as : ab) + sa, (t == 1 ? ws : wb) + sw,
-                                     idesc, (t > 0 || ks > 0) ? 1u : 0u);
-                        }
-                }
+                for (int h = 0; h < kTiles; ++h)
+                    issue_first_layer(tmem + (uint32_t)(h * kH), sbase + (uint32_t)(kA + h * kTileA),
+                                      sbase + (uint32_t)kW);
                 tc::mma_commit(bar);
                 if (!tc::mbar_wait_bounded(bar, phase, kPolls)) {
                     *abort_flag = 1;
@@ -276,8 +246,7 @@ __global__ void __launch_bounds__(fwdtc::kThreads, 2)
                 uint32_t b = 0u, near = 0u;
 #pragma unroll
                 for (int e = 0; e < 32; ++e) {
-                    const float4 u = su[32 * c + e];
-                    const float zv = fmaf(u.x, px, fmaf(u.y, py, fmaf(u.z, pz, v[e] + u.w)));
+                    const float zv = v[e];
                     const bool z = fabsf(zv) < kNearZero;
                     near |= (uint32_t)z << e;
                     out = fmaf(w1s[32 * c + e], z ? 0.f : fmaxf(zv, 0.f), out);
@@ -286,7 +255,7 @@ __global__ void __launch_bounds__(fwdtc::kThreads, 2)
                 while (near) {  // rare: a few units per thousand points
                     const int e = __ffs(near) - 1;
                     near &= near - 1u;
-                    const float f = pre_f32(abig, asmall, row, px, py, pz, m.w0[l], m.b0[l], 32 * c + e);
+                    const float f = pre_f32(tile, row, px, py, pz, m.w0[l], m.b0[l], 32 * c + e);
                     if (f > 0.f) {
                         out = fmaf(w1s[32 * c + e], f, out);
                         b |= 1u << e;
