@@ -12,7 +12,7 @@ batch.  ``value`` is queries/s with the points already resident in HBM;
 ``e2e`` is the same metric through the public API with host buffers
 (``OctreeSDF.sdf_host`` -> ``nglod_sdf_fwd_host``): the points are copied
 from pinned host memory and the distances copied back inside the timed
-region, in 256k-point chunks whose copies overlap the kernels.  The
+region, in 512k-point chunks whose copies overlap the kernels.  The
 ``roofline`` object names the binding one of three live-measured terms of
 ``sdf_fwd_f32_kernel``: the corner gathers against a measured line-read
 ceiling, the HBM bytes against the measured copy bandwidth, and the float32
@@ -438,7 +438,7 @@ def run_ours(args):
 
     # e2e through the public API with host buffers: OctreeSDF.sdf_host ->
     # nglod_sdf_fwd_host copies the pinned points in and the distances out
-    # every step, in 256k-point chunks whose copies overlap the kernels.
+    # every step, in 512k-point chunks whose copies overlap the kernels.
     def e2e_step():
         net.sdf_host(x_host, lod=LOD, out=out_host)
 

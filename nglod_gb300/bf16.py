@@ -99,7 +99,7 @@ class Bf16OctreeSDF:
                    "nglod_sdf_fwd_bf16")
         return out
 
-    def sdf_host(self, x_host, lod=None, out=None, chunk=1 << 18):
+    def sdf_host(self, x_host, lod=None, out=None, chunk=1 << 19):
         """sdf of points in host memory ([n, 3] float32; pinned for overlap)
         into host memory ([n, 1] float32, returned): chunks are copied in,
         evaluated and copied out on three streams joined into the current

@@ -153,7 +153,7 @@ class OctreeSDF(nn.Module):
         return preds if return_lst else preds[-1]
 
     @torch.no_grad()
-    def sdf_host(self, x_host, lod=None, out=None, chunk=1 << 18):
+    def sdf_host(self, x_host, lod=None, out=None, chunk=1 << 19):
         """Inference sdf of points in host memory ([n, 3] float32; pinned for
         overlap) into host memory ([n, 1], returned), pipelined in chunks on
         three streams joined into the current one (nglod_sdf_fwd_host).  The
