@@ -319,8 +319,11 @@ __global__ void chain_build_kernel(const int4 *__restrict__ corner_idx, const in
 template <bool kChain>
 __device__ __forceinline__ void sparse_features_quarter(const nglod_sparse_model &m, int lod, int64_t g, float px,
                                                         float py, float pz, int q, float (&f)[8]) {
+    // channel pairs (2c, 2c + 1) in one packed FMA: each lane of it is the
+    // same float32 FMA as before, in the same corner order
+    float2 f2[4];
 #pragma unroll
-    for (int c = 0; c < 8; ++c) f[c] = 0.f;
+    for (int c = 0; c < 4; ++c) f2[c] = make_float2(0.f, 0.f);
     const float nx = fmaf(px, 0.5f, 0.5f), ny = fmaf(py, 0.5f, 0.5f), nz = fmaf(pz, 0.5f, 0.5f);
     const uint4 *feats = static_cast<const uint4 *>(m.corner_feats) + q;  // 4 uint4 per corner row
     const short4 pf = reinterpret_cast<const short4 *>(m.points)[g];
@@ -370,15 +373,17 @@ __device__ __forceinline__ void sparse_features_quarter(const nglod_sparse_model
         for (int k = 0; k < 8; ++k) {
             const int bx = k & 1, by = (k >> 1) & 1, bz = k >> 2;
             const float w = (wz[bz] * wy[by]) * wx[bx];
-            f[0] = fmaf(bf16_lo(v[k].x), w, f[0]);
-            f[1] = fmaf(bf16_hi(v[k].x), w, f[1]);
-            f[2] = fmaf(bf16_lo(v[k].y), w, f[2]);
-            f[3] = fmaf(bf16_hi(v[k].y), w, f[3]);
-            f[4] = fmaf(bf16_lo(v[k].z), w, f[4]);
-            f[5] = fmaf(bf16_hi(v[k].z), w, f[5]);
-            f[6] = fmaf(bf16_lo(v[k].w), w, f[6]);
-            f[7] = fmaf(bf16_hi(v[k].w), w, f[7]);
+            const float2 w2 = make_float2(w, w);
+            f2[0] = __ffma2_rn(make_float2(bf16_lo(v[k].x), bf16_hi(v[k].x)), w2, f2[0]);
+            f2[1] = __ffma2_rn(make_float2(bf16_lo(v[k].y), bf16_hi(v[k].y)), w2, f2[1]);
+            f2[2] = __ffma2_rn(make_float2(bf16_lo(v[k].z), bf16_hi(v[k].z)), w2, f2[2]);
+            f2[3] = __ffma2_rn(make_float2(bf16_lo(v[k].w), bf16_hi(v[k].w)), w2, f2[3]);
         }
+    }
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        f[2 * c] = f2[c].x;
+        f[2 * c + 1] = f2[c].y;
     }
 }
 

@@ -191,19 +191,50 @@ __device__ __forceinline__ int2 nugget_at(const TraverseArgs &a, int64_t i) {
     return a.in[i];
 }
 
-__global__ void __launch_bounds__(kChunk, 2) traverse_level_kernel(const TraverseArgs a) {
-    __shared__ uint32_t s_warp[33];
+// One nugget's decision: the hit mask (bits 0-7, by child index) and the
+// origin octant (bits 8-10); its octree byte and point index for the emit.
+__device__ __forceinline__ uint32_t decide_nugget(const TraverseArgs &a, int2 nug, uint32_t &o, int64_t &node) {
+    node = a.off0 + nug.y;
+    const short4 p = a.points[node];
+    uint32_t inf = 0;
+    if (a.level > 0 || ray_hits_voxel(a.org, a.dir, (uint32_t)nug.x, p, 0)) {
+        if (a.level == a.target) {
+            inf = 1u;
+        } else {
+            o = a.octree[node];
+            const RayFaces f = ray_faces(a.org, a.dir, (uint32_t)nug.x, a.level + 1);
+            const float bx = (float)(2 * (int)p.x), by = (float)(2 * (int)p.y), bz = (float)(2 * (int)p.z);
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                if (!(o & (1u << j))) continue;
+                if (faces_hit(f, bx + (float)((j >> 2) & 1), by + (float)((j >> 1) & 1), bz + (float)(j & 1)))
+                    inf |= 1u << j;
+            }
+            inf |= origin_octant(a.org, (uint32_t)nug.x, p, a.level) << 8;
+        }
+    }
+    return inf;
+}
+
+// 256 threads per block, four consecutive nuggets of a 1024-nugget chunk
+// per thread (decided one after the other, so a warp's divergence averages
+// over four decisions, and a chunk costs a 256-thread scan).
+constexpr int kTravThreads = 256, kTravPer = kChunk / kTravThreads;
+
+__global__ void __launch_bounds__(kTravThreads, 4) traverse_level_kernel(const TraverseArgs a) {
+    __shared__ uint32_t s_warp[kTravThreads / 32 + 1];
     __shared__ uint32_t s_order[8];
     __shared__ int64_t s_chunk;
     __shared__ uint32_t s_excl;
-    if (threadIdx.x < 8) s_order[threadIdx.x] = c_child_order[threadIdx.x];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid < 8) s_order[tid] = c_child_order[tid];
     const int64_t count = a.ctrl[kCtrlCount + a.level];
     const int64_t nchunks = (count + kChunk - 1) / kChunk;
     // an empty level has no last chunk to write the next level's count
-    if (nchunks == 0 && blockIdx.x == 0 && threadIdx.x == 0) a.ctrl[kCtrlCount + a.level + 1] = 0;
+    if (nchunks == 0 && blockIdx.x == 0 && tid == 0) a.ctrl[kCtrlCount + a.level + 1] = 0;
     volatile unsigned long long *st = a.state;
     for (;;) {
-        if (threadIdx.x == 0) {
+        if (tid == 0) {
             const int64_t c = (int64_t)atomicAdd(a.ticket, 1u);
             // after a raised status (an earlier level overflowed, or a wait
             // gave up) nothing more is read or written
@@ -212,42 +243,51 @@ __global__ void __launch_bounds__(kChunk, 2) traverse_level_kernel(const Travers
         __syncthreads();
         const int64_t c = s_chunk;
         if (c >= nchunks) break;
-        // 1. decide: the hit mask (bits 0-7, by child index) and the origin
-        // octant (bits 8-10) of this thread's nugget
-        const int64_t i = c * kChunk + threadIdx.x;
-        uint32_t inf = 0;
-        int2 nug = make_int2(0, 0);
-        uint32_t o = 0;
-        int64_t node = 0;
-        if (i < count) {
-            nug = nugget_at(a, i);
-            node = a.off0 + nug.y;
-            const short4 p = a.points[node];
-            if (a.level > 0 || ray_hits_voxel(a.org, a.dir, (uint32_t)nug.x, p, 0)) {
-                if (a.level == a.target) {
-                    inf = 1u;
-                } else {
-                    o = a.octree[node];
-                    const RayFaces f = ray_faces(a.org, a.dir, (uint32_t)nug.x, a.level + 1);
-                    const float bx = (float)(2 * (int)p.x), by = (float)(2 * (int)p.y), bz = (float)(2 * (int)p.z);
+        // 1. decide this thread's four nuggets
+        const int64_t i0 = c * kChunk + (int64_t)tid * kTravPer;
+        uint32_t inf[kTravPer], oct[kTravPer];
+        int2 nug[kTravPer];
+        int64_t node[kTravPer];
+        uint32_t v = 0;
 #pragma unroll
-                    for (int j = 0; j < 8; ++j) {
-                        if (!(o & (1u << j))) continue;
-                        if (faces_hit(f, bx + (float)((j >> 2) & 1), by + (float)((j >> 1) & 1), bz + (float)(j & 1)))
-                            inf |= 1u << j;
-                    }
-                    inf |= origin_octant(a.org, (uint32_t)nug.x, p, a.level) << 8;
-                }
+        for (int e = 0; e < kTravPer; ++e) {
+            inf[e] = 0;
+            oct[e] = 0;
+            node[e] = 0;
+            nug[e] = make_int2(0, 0);
+            if (i0 + e < count) {
+                nug[e] = nugget_at(a, i0 + e);
+                inf[e] = decide_nugget(a, nug[e], oct[e], node[e]);
             }
+            v += (uint32_t)__popc(inf[e] & 0xffu);
         }
-        const uint32_t v = (uint32_t)__popc(inf & 0xffu);
-        uint32_t tot;
-        const uint32_t ex = block_exclusive_scan(v, s_warp, &tot);
-        // 2. the chunk's offset: publish its count, then warp 0 adds the
+        // 2. exclusive scan of the threads' hit counts
+        uint32_t x = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) s_warp[warp] = x;
+        __syncthreads();
+        if (warp == 0) {
+            const uint32_t w = lane < kTravThreads / 32 ? s_warp[lane] : 0u;
+            uint32_t wi = w;
+#pragma unroll
+            for (int o = 1; o < kTravThreads / 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, wi, o);
+                if (lane >= o) wi += y;
+            }
+            if (lane < kTravThreads / 32) s_warp[lane] = wi - w;  // exclusive prefix of warp totals
+            if (lane == kTravThreads / 32 - 1) s_warp[kTravThreads / 32] = wi;
+        }
+        __syncthreads();
+        const uint32_t ex = s_warp[warp] + x - v;
+        const uint32_t tot = s_warp[kTravThreads / 32];
+        // 3. the chunk's offset: publish its count, then warp 0 adds the
         // predecessors' counts 32 chunks at a time, back to the nearest chunk
         // that has published its inclusive prefix
-        if (threadIdx.x < 32) {
-            const int lane = threadIdx.x;
+        if (warp == 0) {
             uint32_t excl = 0;
             if (c == 0) {
                 if (lane == 0) st[0] = kStatePrefix | tot;
@@ -297,18 +337,23 @@ __global__ void __launch_bounds__(kChunk, 2) traverse_level_kernel(const Travers
             }
         }
         __syncthreads();
-        // 3. emit the hit children nearest first (nothing beyond the capacity)
+        // 4. emit the hit children nearest first (nothing beyond the capacity)
         int64_t pos = (int64_t)s_excl + ex;
         if (v != 0 && pos + v <= a.capacity) {
-            if (a.level == a.target) {
-                a.out[pos] = nug;
-            } else {
-                const int64_t first = (int64_t)a.prefix[node] - a.off1;
-                uint32_t ord = s_order[inf >> 8];
+#pragma unroll
+            for (int e = 0; e < kTravPer; ++e) {
+                if (!(inf[e] & 0xffu)) continue;
+                if (a.level == a.target) {
+                    a.out[pos++] = nug[e];
+                    continue;
+                }
+                const int64_t first = (int64_t)a.prefix[node[e]] - a.off1;
+                uint32_t ord = s_order[inf[e] >> 8];
 #pragma unroll
                 for (int r = 0; r < 8; ++r, ord >>= 3) {
                     const uint32_t j = ord & 7u;
-                    if (inf & (1u << j)) a.out[pos++] = make_int2(nug.x, (int)(first + __popc(o & ((2u << j) - 1u))));
+                    if (inf[e] & (1u << j))
+                        a.out[pos++] = make_int2(nug[e].x, (int)(first + __popc(oct[e] & ((2u << j) - 1u))));
                 }
             }
         }
@@ -734,7 +779,8 @@ extern "C" int nglod_spc_raytrace(const uint8_t *octree, const int16_t *points, 
     int2 *buf[2] = {reinterpret_cast<int2 *>(nuggets_a), reinterpret_cast<int2 *>(nuggets_b)};
     unsigned long long *states =
         reinterpret_cast<unsigned long long *>(reinterpret_cast<uint8_t *>(info) + kTicketBytes);
-    const int grid = grid_for((capacity + kChunk - 1) / kChunk);
+    const int64_t chunks = (capacity + kChunk - 1) / kChunk, cap = (int64_t)num_sms() * 8;
+    const int grid = (int)(chunks < cap ? chunks : cap);
     for (int l = 0; l < passes; ++l) {
         a.level = l;
         a.off0 = psum[l];
@@ -743,7 +789,7 @@ extern "C" int nglod_spc_raytrace(const uint8_t *octree, const int16_t *points, 
         a.out = buf[(l + 1) % 2];
         a.state = states + l * nstate;
         a.ticket = info + l;
-        traverse_level_kernel<<<grid, kChunk, 0, s>>>(a);
+        traverse_level_kernel<<<grid, kTravThreads, 0, s>>>(a);
     }
     NGLOD_TRY(launch_status("nglod_spc_raytrace"));
     int64_t res[kCtrlCount + kMaxSpcLevels + 1];
