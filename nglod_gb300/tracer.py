@@ -126,6 +126,60 @@ def _check_net(net, grad_method):
         raise NotImplementedError(f"grad_method={grad_method!r}: the fused tracer computes 'finitediff' normals")
 
 
+def _sdf_fn(net):
+    """The network's sdf at its current lod through the library's query
+    kernels (the reference calls ``net(x)``)."""
+    if isinstance(net, OctreeSDF):
+        lod = net.lod if net.lod is not None and 0 <= net.lod < net.num_lods else None
+        return lambda p: net._sdf_infer(p, lod, False)
+    return lambda p: net(p)
+
+
+def get_min(tracer, net, ray_o, ray_d):
+    """SphereTracer.get_min (sdf-net/lib/tracer/SphereTracer.py:134-218): the
+    march of ``forward`` with the reference's get_min rules, and per ray the
+    point of the smallest sdf seen (``min_x``).  Its rules, kept as they are:
+    every ray marches from the start (``cond`` is recomputed each step from
+    |d|, the oscillation test and |t| < far, not carried over), including rays
+    that miss the box (they start at their origin, t = 0); ``min_x`` takes the
+    point the step just moved to wherever the previous step's d is below the
+    running minimum; hit rays get the finite-difference gradient, not
+    normalised.  Each step's evaluations go through the library's sdf kernel
+    on the compacted active points.  The reference builds its result with
+    ``RenderBuffer(..., minx=minx)``, a keyword its RenderBuffer does not have
+    (the field is ``min_x``), so as shipped it raises TypeError on its last
+    line; this returns the buffer with ``min_x`` set."""
+    _check_net(net, tracer.grad_method)
+    f = _sdf_fn(net)
+    x, t, hit = aabb(ray_o, ray_d)
+    normal = torch.zeros_like(x)
+    with torch.no_grad():
+        d = f(x)
+        dprev = d.clone()
+        mind = d.clone()
+        minx = x.clone()
+        for _ in range(tracer.num_steps):
+            hit = (torch.abs(t) < tracer.camera_clamp[1])[:, 0]
+            cond = (torch.abs(d) > tracer.min_dis)[:, 0]
+            cond = cond & (torch.abs((d + dprev) / 2.0) > tracer.min_dis * 3)[:, 0]
+            cond = cond & hit
+            if not cond.any():
+                break
+            x = torch.where(cond.view(-1, 1), torch.addcmul(ray_o, ray_d, t), x)
+            new_mins = (d < mind)[..., 0]
+            mind[new_mins] = d[new_mins]
+            minx[new_mins] = x[new_mins]
+            dprev = torch.where(cond.unsqueeze(1), d, dprev)
+            d[cond] = f(x[cond]) * tracer.step_size
+            t = torch.where(cond.view(-1, 1), t + d, t)
+        hit = hit & ~(torch.abs(x) > 1.0).any(dim=-1)
+        xh = x[hit]
+        h = 1.0 / (64.0 * 3.0)
+        eps = torch.eye(3, device=x.device) * h
+        normal[hit] = torch.cat([f(xh + eps[k]) - f(xh - eps[k]) for k in range(3)], dim=-1) / (h * 2.0)
+    return RenderBuffer(x=x, depth=t, hit=hit, normal=normal, min_x=minx)
+
+
 class SphereTracer(BaseTracer):
     """Persistent fused sphere tracer (one kernel launch per call).
 
@@ -133,6 +187,9 @@ class SphereTracer(BaseTracer):
     (the BF16 form) by ``nglod_trace_bf16``, which evaluates 128 rays per
     block on the tensor cores.
     """
+
+    def get_min(self, net, ray_o, ray_d):
+        return get_min(self, net, ray_o, ray_d)
 
     def forward(self, net, ray_o, ray_d):
         _check_net(net, self.grad_method)
@@ -190,6 +247,9 @@ class PlainSphereTracer(BaseTracer):
     """
 
     last_evaluations = None
+
+    def get_min(self, net, ray_o, ray_d):
+        return get_min(self, net, ray_o, ray_d)
 
     def forward(self, net, ray_o, ray_d):
         _check_net(net, self.grad_method)

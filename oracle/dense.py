@@ -170,6 +170,51 @@ def normalize(v, eps=1e-5):
     return v / np.maximum(n, v.dtype.type(eps))
 
 
+def get_min(m, ray_o, ray_d, lod=None, num_steps=128, min_dis=3e-4, step_size=1.0, camera_clamp=(-5.0, 10.0),
+            aabb_fn=aabb):
+    """``SphereTracer.get_min(net, ray_o, ray_d)`` (tracer/SphereTracer.py:134-218).
+
+    Returns (x, t, hit, normal, min_x).  Its rules: ``cond`` is recomputed
+    every step (|d|, oscillation, |t| < far) without the aabb mask, so rays
+    that miss the box march from their origins; before each step's update,
+    min_x takes the new point wherever the previous d is below the running
+    minimum; normals are the finite-difference gradient, not normalised.
+    """
+    dt = m["fms"][0].dtype
+    o = np.asarray(ray_o).astype(dt)
+    dr = np.asarray(ray_d).astype(dt)
+    net = lambda p: sdf(m, p, lod=lod)
+    x, t, _ = aabb_fn(o, dr)
+    x = x.astype(dt)
+    t = t.astype(dt)
+    normal = np.zeros_like(x)
+    d = net(x)
+    dprev = d.copy()
+    mind = d.copy()
+    minx = x.copy()
+    hit = np.zeros(o.shape[0], dtype=bool)
+    far = dt.type(camera_clamp[1])
+    md = dt.type(min_dis)
+    for _ in range(num_steps):
+        hit = np.abs(t[:, 0]) < far
+        cond = np.abs(d[:, 0]) > md
+        cond = cond & (np.abs((d[:, 0] + dprev[:, 0]) / dt.type(2)) > md * dt.type(3))
+        cond = cond & hit
+        if not cond.any():
+            break
+        x = np.where(cond[:, None], o + dr * t, x)
+        new = d[:, 0] < mind[:, 0]
+        mind[new] = d[new]
+        minx[new] = x[new]
+        dprev = np.where(cond[:, None], d, dprev)
+        d[cond] = net(x[cond]) * dt.type(step_size)
+        t = np.where(cond[:, None], t + d, t)
+    hit = hit & ~(np.abs(x) > 1).any(axis=-1)
+    if hit.any():
+        normal[hit] = finitediff_gradient(net, x[hit])
+    return x, t, hit, normal, minx
+
+
 def sphere_trace(m, ray_o, ray_d, lod=None, num_steps=128, min_dis=3e-4, step_size=1.0,
                  camera_clamp=(-5.0, 10.0), aabb_fn=aabb):
     """``SphereTracer.forward(net, ray_o, ray_d)`` (tracer/SphereTracer.py:41-132).

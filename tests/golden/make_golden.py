@@ -36,6 +36,11 @@ Fixtures:
                    builds the reference SphereTracer from parsed options
                    instead, and runs sample_surface on the CPU.  Everything
                    else in the export runs unchanged.
+  get_min_small.npz  SphereTracer.get_min on trace_small's network and rays
+                   (lod None): x, depth, hit, unnormalised normals and min_x.
+                   As shipped, get_min's last line passes ``minx=`` to
+                   RenderBuffer, whose field is ``min_x``, and raises
+                   TypeError; the generator maps the keyword.
   shade_small.npz  Renderer.shade_tensor with a ground plane, shadow rays and
                    ambient occlusion on trace_small's network, 48x40 rays,
                    matcap shading with nglod_gb300.synthetic.matcap_texture
@@ -195,6 +200,33 @@ def trace_small(OctreeSDF, SphereTracer, parse_options):
     np.savez_compressed(os.path.join(HERE, "trace_small.npz"), **out)
 
 
+def get_min_small(OctreeSDF, SphereTracer, parse_options):
+    """SphereTracer.get_min on trace_small's network and rays (lod None).  As
+    shipped, get_min ends with RenderBuffer(..., minx=minx), a keyword the
+    reference's RenderBuffer does not have (its field is min_x), and raises
+    TypeError; the generator gives the tracer module a RenderBuffer factory
+    that takes ``minx`` as ``min_x``.  The march itself runs unchanged."""
+    ST = sys.modules["lib.tracer.SphereTracer"]
+    RB = ST.RenderBuffer
+    net, args = trace_small_net(OctreeSDF, parse_options)
+    ro, rd = synthetic.look_at_rays(width=40, height=40)
+    extra_o = torch.tensor([[0, 0, 0], [0.5, 0.2, -0.3], [3, 3, 3], [0, 0, 4], [1, 0, 0], [0, 2, 0],
+                            [-0.2, 0.1, 1.0]], dtype=torch.float32)
+    extra_d = torch.tensor([[1, 0, 0], [0, 0, 1], [1, 0, 0], [0, 0, -1], [-1, 0, 0], [0, -1, 0],
+                            [0, 0, -1]], dtype=torch.float32)
+    ro = torch.cat([ro, extra_o])
+    rd = torch.cat([rd, extra_d])
+    ST.RenderBuffer = lambda minx=None, **k: RB(min_x=minx, **k)
+    try:
+        rb = SphereTracer(args).get_min(net, ro, rd)
+    finally:
+        ST.RenderBuffer = RB
+    out = {"ray_o": ro.numpy(), "ray_d": rd.numpy(), "x": rb.x.detach().numpy(),
+           "depth": rb.depth.detach().numpy(), "hit": rb.hit.numpy(), "normal": rb.normal.detach().numpy(),
+           "min_x": rb.min_x.detach().numpy(), "num_steps": np.array(int(args.num_steps))}
+    np.savez_compressed(os.path.join(HERE, "get_min_small.npz"), **out)
+
+
 def shade_small(OctreeSDF, SphereTracer, parse_options):
     import lib.renderer as R
     W, H = 48, 40
@@ -327,15 +359,22 @@ def spc_small(spc3d, geoutils, ref_root):
 
 
 def main():
+    """make_golden.py [REFERENCE_ROOT [FIXTURE ...]]: all fixtures, or only the
+    named ones (e.g. get_min_small)."""
     ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    only = set(sys.argv[2:])
     OctreeSDF, SphereTracer, parse_options, spc3d, geoutils = import_reference(ref_root)
     torch.set_num_threads(max(1, os.cpu_count() or 1))
-    dense_small(OctreeSDF, parse_options)
-    trace_small(OctreeSDF, SphereTracer, parse_options)
-    spc_small(spc3d, geoutils, ref_root)
-    shade_small(OctreeSDF, SphereTracer, parse_options)
-    mesh_small()
-    sol_export_small(OctreeSDF, SphereTracer, parse_options)
+    jobs = [("dense_small", lambda: dense_small(OctreeSDF, parse_options)),
+            ("trace_small", lambda: trace_small(OctreeSDF, SphereTracer, parse_options)),
+            ("get_min_small", lambda: get_min_small(OctreeSDF, SphereTracer, parse_options)),
+            ("spc_small", lambda: spc_small(spc3d, geoutils, ref_root)),
+            ("shade_small", lambda: shade_small(OctreeSDF, SphereTracer, parse_options)),
+            ("mesh_small", mesh_small),
+            ("sol_export_small", lambda: sol_export_small(OctreeSDF, SphereTracer, parse_options))]
+    for name, job in jobs:
+        if not only or name in only:
+            job()
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

@@ -133,6 +133,28 @@ def test_trace_matches_reference_golden(golden, cuda, name, lod, tracer_cls):
     assert rb.hit[-7].item() and rb.depth[-7, 0].item() == 0.0
 
 
+@pytest.mark.parametrize("tracer_cls", [ng.SphereTracer, ng.PlainSphereTracer])
+def test_get_min_matches_reference_golden(golden, cuda, tracer_cls):
+    """SphereTracer.get_min against the reference's own get_min on
+    trace_small's network (tests/golden/get_min_small.npz): hit mask, depth
+    and final point at the trace tolerances, the unnormalised finite-difference
+    normals at 1e-3, and the minimum-sdf points min_x at the depth tolerance."""
+    fx = golden("get_min_small")
+    tr = golden("trace_small")
+    net = model_from_fixture(tr, 2, 3, device=cuda)
+    net.lod = None
+    tracer = tracer_cls(default_args(num_steps=int(fx["num_steps"])))
+    rb = tracer.get_min(net, torch.from_numpy(fx["ray_o"]).to(cuda), torch.from_numpy(fx["ray_d"]).to(cuda))
+    h = rb.hit.cpu().numpy()
+    assert (h == fx["hit"]).mean() >= 0.9999
+    both = h & fx["hit"]
+    np.testing.assert_allclose(rb.depth.cpu().numpy(), fx["depth"], atol=DEPTH_TOL, rtol=1e-4)
+    np.testing.assert_allclose(rb.x.cpu().numpy(), fx["x"], atol=DEPTH_TOL, rtol=0)
+    np.testing.assert_allclose(rb.min_x.cpu().numpy(), fx["min_x"], atol=DEPTH_TOL, rtol=0)
+    np.testing.assert_allclose(rb.normal.cpu().numpy()[both], fx["normal"][both], atol=1e-3, rtol=0)
+    assert (rb.normal.cpu().numpy()[~h] == 0).all()
+
+
 def test_trace_full_model_vs_oracle(cuda):
     """5-LOD network holding the seed-1 sphere union; 96x96 camera, 128 steps."""
     c, r = synthetic.sphere_union(1)

@@ -55,6 +55,25 @@ def test_aabb_oracles_agree_and_edge_cases():
     assert (xc[miss] == o[miss]).all() and (tc[miss] == 0).all()
 
 
+def test_get_min_matches_reference(golden):
+    """The oracle's get_min against the reference's own SphereTracer.get_min
+    (tests/golden/get_min_small.npz) on trace_small's network."""
+    fx = golden("get_min_small")
+    net = model_from_fixture(golden("trace_small"), 2, 3)
+    m = oracle_model(net, np.float32)
+    x, t, hit, normal, minx = dense.get_min(m, fx["ray_o"], fx["ray_d"], num_steps=int(fx["num_steps"]),
+                                            aabb_fn=cref.aabb)
+    assert (hit == fx["hit"]).mean() >= 0.9999
+    both = hit & fx["hit"]
+    np.testing.assert_allclose(t, fx["depth"], atol=DEPTH_TOL, rtol=1e-4)
+    np.testing.assert_allclose(minx, fx["min_x"], atol=DEPTH_TOL, rtol=0)
+    np.testing.assert_allclose(normal[both], fx["normal"][both], atol=1e-3, rtol=0)
+    # rays that miss the box march from their origins under get_min's rules
+    _, _, in_box = cref.aabb(fx["ray_o"], fx["ray_d"])
+    moved = np.abs(fx["x"] - fx["ray_o"]).max(axis=1) > 0
+    assert (~in_box).sum() > 0 and moved[~in_box].all()
+
+
 @pytest.mark.parametrize("name,lod", [("lodNone", None), ("lod0", 0)])
 def test_sphere_trace_matches_reference(golden, name, lod):
     fx = golden("trace_small")
