@@ -148,9 +148,12 @@ def test_get_min_matches_reference_golden(golden, cuda, tracer_cls):
     h = rb.hit.cpu().numpy()
     assert (h == fx["hit"]).mean() >= 0.9999
     both = h & fx["hit"]
-    np.testing.assert_allclose(rb.depth.cpu().numpy(), fx["depth"], atol=DEPTH_TOL, rtol=1e-4)
-    np.testing.assert_allclose(rb.x.cpu().numpy(), fx["x"], atol=DEPTH_TOL, rtol=0)
-    np.testing.assert_allclose(rb.min_x.cpu().numpy(), fx["min_x"], atol=DEPTH_TOL, rtol=0)
+    # hit rays at the depth bar; rays that march out to the far clip carry
+    # their steps' float32 rounding, bounded relatively (as for forward)
+    for got, want in [(rb.depth, fx["depth"]), (rb.x, fx["x"]), (rb.min_x, fx["min_x"])]:
+        got = got.cpu().numpy()
+        np.testing.assert_allclose(got[both], want[both], atol=DEPTH_TOL, rtol=0)
+        np.testing.assert_allclose(got[~both], want[~both], atol=DEPTH_TOL, rtol=1e-4)
     np.testing.assert_allclose(rb.normal.cpu().numpy()[both], fx["normal"][both], atol=1e-3, rtol=0)
     assert (rb.normal.cpu().numpy()[~h] == 0).all()
 

@@ -65,8 +65,9 @@ def test_get_min_matches_reference(golden):
                                             aabb_fn=cref.aabb)
     assert (hit == fx["hit"]).mean() >= 0.9999
     both = hit & fx["hit"]
-    np.testing.assert_allclose(t, fx["depth"], atol=DEPTH_TOL, rtol=1e-4)
-    np.testing.assert_allclose(minx, fx["min_x"], atol=DEPTH_TOL, rtol=0)
+    for got, want in [(t, fx["depth"]), (x, fx["x"]), (minx, fx["min_x"])]:
+        np.testing.assert_allclose(got[both], want[both], atol=DEPTH_TOL, rtol=0)
+        np.testing.assert_allclose(got[~both], want[~both], atol=DEPTH_TOL, rtol=1e-4)
     np.testing.assert_allclose(normal[both], fx["normal"][both], atol=1e-3, rtol=0)
     # rays that miss the box march from their origins under get_min's rules
     _, _, in_box = cref.aabb(fx["ray_o"], fx["ray_d"])
