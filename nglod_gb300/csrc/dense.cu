@@ -192,11 +192,13 @@ __device__ __forceinline__ void f32tc_teardown(uint8_t *sm, uint32_t tmem, uint3
 // The block is four independent groups of four warps; group g decodes
 // 128-point tiles g, g + 4, ... of the block's share into its own 128 TMEM
 // columns (4 x 128 = the SM's 512).  A group gathers its tile in registers,
-// takes one of two shared point-tile buffers (a lock per buffer), writes the
-// split rows, and its first thread issues the tile's 14 MMAs and waits for
-// them; the buffer is released as soon as the product is done and the group
-// runs its epilogue while the others gather.  Groups meet only at their own
-// named barrier (id 1 + g, 128 threads), never at a block barrier.
+// takes one of two shared point-tile buffers, writes the split rows, and its
+// first thread issues the tile's 14 MMAs; the group then gathers its next
+// tile while the product runs, and only then reads the product back for the
+// epilogue.  A buffer's lock covers its rows' stores and the issue; its
+// next taker waits on the buffer's mbarrier for the product.  Groups meet
+// only at their own named barrier (id 1 + g, 128 threads), never at a block
+// barrier.
 namespace f32st {
 constexpr int kGroups = 4;
 constexpr int kThreads = f32tc::kTP * kGroups;  // 512
@@ -204,9 +206,11 @@ constexpr int kStages = 2;                      // point-tile buffers
 constexpr size_t kA = 0;                        // buffer b at kA + b f32tc::kTileA
 constexpr size_t kW = (size_t)kStages * f32tc::kTileA;
 constexpr size_t kW1 = kW + f32tc::kWBytes;
-constexpr size_t kBar = kW1 + f32tc::kH * 4;    // one mbarrier per group
-constexpr size_t kLock = kBar + 8 * kGroups;    // int per buffer: 1 = taken
-constexpr size_t kSel = kLock + 4 * kStages;    // int per group: its buffer, or -1
+constexpr size_t kBar = kW1 + f32tc::kH * 4;    // one mbarrier per group: its product done
+constexpr size_t kFree = kBar + 8 * kGroups;    // one mbarrier per buffer: its last product done
+constexpr size_t kLock = kFree + 8 * kStages;   // int per buffer: 1 = taken
+constexpr size_t kUses = kLock + 4 * kStages;   // uint32 per buffer: products issued on it
+constexpr size_t kSel = kUses + 4 * kStages;    // int per group: its buffer, or -1
 constexpr size_t kOk = kSel + 4 * kGroups;      // int per group: product done
 constexpr size_t kSlot = kOk + 4 * kGroups;
 constexpr size_t kAbort = kSlot + 4;
@@ -217,7 +221,7 @@ constexpr size_t kVolBudget = kSmemMax - kVol;
 // columns are the SM's whole tensor memory).
 constexpr size_t kSmemMin = 120 * 1024;
 constexpr uint32_t kCols = kGroups * f32tc::kH;
-static_assert(kW % 1024 == 0 && kBar % 8 == 0 && kVol % 128 == 0, "shared layout alignment");
+static_assert(kW % 1024 == 0 && kBar % 8 == 0 && kFree % 8 == 0 && kVol % 128 == 0, "shared layout alignment");
 static_assert(kVol + 109312 <= kSmemMax, "levels 5^3 and 9^3 fit");
 }  // namespace f32st
 
@@ -225,16 +229,30 @@ __device__ __forceinline__ void group_sync(int g) {
     asm volatile("bar.sync %0, %1;" ::"r"(1 + g), "n"(f32tc::kTP) : "memory");
 }
 
-// Takes a free point-tile buffer; -1 once the block is aborting, or (which
-// also aborts it) if none came free within 2^22 tries.  A buffer is held only
-// from its rows' stores to the end of its product.
-__device__ __forceinline__ int acquire_tile_buffer(int *locks, volatile int *abort_flag) {
+// Takes a point-tile buffer whose last product has completed; -1 once the
+// block is aborting, or (which also aborts it) if none came free within the
+// bounds.  A buffer's lock covers only its rows' stores and the issue of its
+// product; the next taker waits on the buffer's mbarrier for that product
+// (uses: products issued on the buffer so far; the use before it completed
+// before it was issued, so the barrier's parity is unambiguous).
+__device__ __forceinline__ int acquire_tile_buffer(uint8_t *sm, uint32_t polls, volatile int *abort_flag) {
+    using namespace f32st;
+    int *locks = reinterpret_cast<int *>(sm + kLock);
+    const uint32_t *uses = reinterpret_cast<const uint32_t *>(sm + kUses);
     for (uint32_t k = 0; k < (1u << 22); ++k) {
         if (*abort_flag) return -1;
 #pragma unroll
-        for (int b = 0; b < f32st::kStages; ++b)
+        for (int b = 0; b < kStages; ++b)
             if (atomicCAS(&locks[b], 0, 1) == 0) {
                 __threadfence_block();
+                const uint32_t u = uses[b];
+                if (u > 0 && !tc::mbar_wait_bounded(reinterpret_cast<uint64_t *>(sm + kFree) + b, (u - 1) & 1u, polls)) {
+                    // the buffer's last product did not finish: the block
+                    // stops (the buffer stays locked)
+                    *abort_flag = 1;
+                    atomicExch(&g_dense_status, 1);
+                    return -1;
+                }
                 return b;
             }
         if (k > 16) __nanosleep(32);
@@ -256,7 +274,9 @@ __global__ void __launch_bounds__(f32st::kThreads, 1)
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int grp = warp >> 2, quad = warp & 3, gtid = tid & (kTP - 1);
     uint64_t *bar = reinterpret_cast<uint64_t *>(sm + kBar) + grp;
+    uint64_t *freeb = reinterpret_cast<uint64_t *>(sm + kFree);
     int *locks = reinterpret_cast<int *>(sm + kLock);
+    uint32_t *uses = reinterpret_cast<uint32_t *>(sm + kUses);
     volatile int *sel = reinterpret_cast<volatile int *>(sm + kSel) + grp;
     volatile int *okf = reinterpret_cast<volatile int *>(sm + kOk) + grp;
     uint32_t *slot = reinterpret_cast<uint32_t *>(sm + kSlot);
@@ -279,7 +299,11 @@ __global__ void __launch_bounds__(f32st::kThreads, 1)
     if (warp == 0) tc::tmem_alloc(slot, kCols);
     if (tid == 0) {
         for (int g = 0; g < kGroups; ++g) tc::mbar_init(reinterpret_cast<uint64_t *>(sm + kBar) + g, 1);
-        for (int b = 0; b < kStages; ++b) locks[b] = 0;
+        for (int b = 0; b < kStages; ++b) {
+            tc::mbar_init(freeb + b, 1);
+            locks[b] = 0;
+            uses[b] = 0;
+        }
         *abort_flag = 0;
     }
     tc::fence_proxy_async_smem();
@@ -289,33 +313,64 @@ __global__ void __launch_bounds__(f32st::kThreads, 1)
     const uint32_t tmem = *slot;
     const uint32_t sbase = tc::smem_addr(sm);
     const uint32_t dcol = tmem + (uint32_t)(grp * kH);
+    const float b1 = m.b1[L][0];
     uint32_t phase = 0;
     bool pending = false;  // group leader: an issued product whose completion it did not see
+    bool prev = false;     // the group has a tile whose epilogue is still to run
+    int64_t prev_i = 0;    // that tile's point of this thread
 
-    for (int64_t t = (int64_t)blockIdx.x * kGroups + grp; t * kTP < n; t += (int64_t)gridDim.x * kGroups) {
+    // Software-pipelined per group: the product of tile k runs while the
+    // group gathers tile k + 1; then tile k's epilogue, then tile k + 1's
+    // rows and product.
+    for (int64_t t = (int64_t)blockIdx.x * kGroups + grp;; t += (int64_t)gridDim.x * kGroups) {
+        const bool has = t * kTP < n;
         const int64_t i = t * kTP + gtid;
         float px = 0.f, py = 0.f, pz = 0.f;
-        if (i < n) {
-            px = x[3 * i];
-            py = x[3 * i + 1];
-            pz = x[3 * i + 2];
-        }
-        // 1. gather and LOD sum of the warp's 32 points (rows 32 quad ..)
         float4 acc[8];
 #pragma unroll
         for (int p = 0; p < 8; ++p) acc[p] = make_float4(0.f, 0.f, 0.f, 0.f);
-        const float4 *vol = reinterpret_cast<const float4 *>(sm + kVol);
+        if (has) {
+            if (i < n) {
+                px = x[3 * i];
+                py = x[3 * i + 1];
+                pz = x[3 * i + 2];
+            }
+            // 1. gather and LOD sum of the warp's 32 points (rows 32 quad ..)
+            const float4 *vol = reinterpret_cast<const float4 *>(sm + kVol);
 #pragma unroll 1
-        for (int l = 0; l < staged; ++l) {
-            const int s = volume_side(m, l);
-            gather_warp_add_f32_shared(vol, s, px, py, pz, lane, acc);
-            vol += s * s * s * (kC / 4);
+            for (int l = 0; l < staged; ++l) {
+                const int s = volume_side(m, l);
+                gather_warp_add_f32_shared(vol, s, px, py, pz, lane, acc);
+                vol += s * s * s * (kC / 4);
+            }
+#pragma unroll 1
+            for (int l = staged; l <= L; ++l)
+                gather_warp_add_f32(static_cast<const float *>(m.grid[l]), volume_side(m, l), px, py, pz, lane, acc);
         }
-#pragma unroll 1
-        for (int l = staged; l <= L; ++l)
-            gather_warp_add_f32(static_cast<const float *>(m.grid[l]), volume_side(m, l), px, py, pz, lane, acc);
-        // 2. a point-tile buffer, the split rows
-        if (gtid == 0) *sel = acquire_tile_buffer(locks, abort_flag);
+        // 2. the previous tile's epilogue, once its product is done
+        if (prev) {
+            if (gtid == 0) {
+                const bool ok = tc::mbar_wait_bounded(bar, phase, polls);
+                if (ok) {
+                    pending = false;
+                } else {
+                    *abort_flag = 1;
+                    atomicExch(&g_dense_status, 1);
+                }
+                *okf = ok ? 1 : 0;
+            }
+            group_sync(grp);
+            if (!*okf) break;
+            phase ^= 1u;
+            tc::fence_after_sync();
+            const float o = relu_dot_w1_f32(dcol + ((uint32_t)(quad * 32) << 16), sw1);
+            if (prev_i < n) out[prev_i] = o + b1;
+            tc::fence_before_sync();
+            prev = false;
+        }
+        if (!has) break;
+        // 3. a point-tile buffer whose last product is done, the split rows
+        if (gtid == 0) *sel = acquire_tile_buffer(sm, polls, abort_flag);
         group_sync(grp);
         const int b = *sel;
         if (b < 0) break;
@@ -323,30 +378,28 @@ __global__ void __launch_bounds__(f32st::kThreads, 1)
         tc::fence_proxy_async_smem();
         tc::fence_before_sync();
         group_sync(grp);
-        // 3. the leader issues the tile's first layer and waits for it
+        // 4. the leader issues the tile's first layer; its completion arrives
+        // on the group's barrier and on the buffer's, and the buffer's lock is
+        // released at once
         if (gtid == 0) {
             tc::fence_after_sync();
             issue_first_layer(dcol, sbase + (uint32_t)(kA + b * kTileA), sbase + (uint32_t)kW);
             tc::mma_commit(bar);
-            const bool ok = tc::mbar_wait_bounded(bar, phase, polls);
-            if (ok) {
-                __threadfence_block();
-                atomicExch(&locks[b], 0);
-            } else {
-                pending = true;
+            tc::mma_commit(freeb + b);
+            pending = true;
+            // A wait bound of 0 (nglod_debug_mma_wait_polls) cuts every wait
+            // to one non-blocking test; the product is tested right after its
+            // issue, where it is still running, so the error path runs.
+            if (polls == 0 && !tc::mbar_test(bar, phase)) {
                 *abort_flag = 1;
                 atomicExch(&g_dense_status, 1);
             }
-            *okf = ok ? 1 : 0;
+            uses[b] += 1;
+            __threadfence_block();
+            atomicExch(&locks[b], 0);
         }
-        group_sync(grp);
-        if (!*okf) break;
-        phase ^= 1u;
-        tc::fence_after_sync();
-        // 4. epilogue on this thread's TMEM row
-        const float o = relu_dot_w1_f32(dcol + ((uint32_t)(quad * 32) << 16), sw1);
-        if (i < n) out[i] = o + m.b1[L][0];
-        tc::fence_before_sync();
+        prev = true;
+        prev_i = i;
     }
     // teardown: a product still in flight after a wait gave up finishes
     // before the columns are freed
