@@ -105,10 +105,11 @@ TF32_NOMINAL_TFLOPS = 1100.0
 # traffic is null.
 NCU_CAPTURES = {
     "sdf_fwd_f32_staged_kernel": {
-        "dram_bytes": 91_279_872 + 10_913_024, "points": N_POINTS,
+        "dram_bytes": 91_242_496 + 10_955_264, "points": N_POINTS,
         "sources": ["nglod_gb300/csrc/dense.cu", "nglod_gb300/csrc/dense_common.cuh",
-                    "nglod_gb300/csrc/tf32_tile.cuh", "nglod_gb300/csrc/tc_common.cuh"],
-        "sha256": "36751d5dec46f13ed4a96cf9d6022884916da915a48fc829ea124017e0c87260",
+                    "nglod_gb300/csrc/f32_tile.cuh", "nglod_gb300/csrc/tf32_tile.cuh",
+                    "nglod_gb300/csrc/tc_common.cuh"],
+        "sha256": "01e0389b43152b90da9edd90f39da63396df2372e9a768657baf839275f78827",
         "how": "ncu --set full --clock-control none, one launch at 4,194,304 points (bench --no-extras)"},
     "sdf_fwd_bf16_staged_kernel": {
         "dram_bytes": 90_247_168 + 10_010_368, "points": N_POINTS,
