@@ -93,11 +93,13 @@ int nglod_volume_sample(const float *grid, int32_t side, int32_t feature_dim, co
  * lod in [0, num_lods): out[n] = prediction of that LOD;
  * lod < 0 or >= num_lods: the finest prediction;
  * all_lods != 0: out[num_lods][n] = every LOD's prediction (return_lst).
- * Gathers and LOD sums are float32.  For one LOD at hidden_dim 128 the
- * decoder's feature product runs on the tensor cores as three TF32 products
- * over big / small splits (relative error about 2^-21 of the dot product,
- * float32's own size); a bounded wait of that kernel that gives up sets the
- * flag nglod_dense_status reads.  Other shapes decode per thread in float32. */
+ * Gathers and LOD sums are float32.  For one LOD at hidden_dim 128 a
+ * persistent kernel (one block per SM, the leading volumes that fit copied
+ * into shared memory) runs the decoder's first layer, features, x y z and
+ * bias, on the tensor cores as split-TF32 products (relative error about
+ * 2^-21 of the dot product, float32's own size); a bounded wait of that
+ * kernel that gives up sets the flag nglod_dense_status reads.  Other shapes
+ * decode per thread in float32. */
 int nglod_sdf_fwd(const nglod_dense_model *model, const float *x, int64_t n,
                   int32_t lod, int32_t all_lods, float *out, nglod_stream_t stream);
 
@@ -219,13 +221,15 @@ int nglod_sdf_fwd_bf16(const nglod_bf16_model *model, const float *x, int64_t n,
 int nglod_sdf_fwd_bf16_host(const nglod_bf16_model *model, const float *x_host, int64_t n, int32_t lod,
                             float *out_host, int64_t chunk, void *scratch, int32_t *status, nglod_stream_t stream);
 
-/* For tests of the error path: bounds the per-tile tensor-core wait of
- * later nglod_sdf_fwd_bf16 and tensor-core nglod_sdf_fwd calls (host
- * setting, all devices) to `polls`
- * polls of the mbarrier; 0 tests it once without waiting, a negative value
- * restores the default (2^22 polls).  A wait that gives up sets the call's
- * status, stops the kernel after letting the issued product finish, and
- * leaves the context usable.  Not for production use. */
+/* For tests of the error path: bounds the per-tile tensor-core waits of
+ * later nglod_sdf_fwd_bf16 and tensor-core nglod_sdf_fwd / nglod_trace calls
+ * (host setting, all devices) to `polls` polls of the mbarrier; 0 tests it
+ * once without waiting (the float32 query, whose groups read a tile's
+ * product back only after gathering their next tile, then also tests each
+ * product right after issuing it), a negative value restores the default
+ * (2^22 polls).  A wait that gives up sets the call's status, stops the
+ * kernel after letting the issued product finish, and leaves the context
+ * usable.  Not for production use. */
 int nglod_debug_mma_wait_polls(int64_t polls);
 
 /* Measurement helper, no reference counterpart: `blocks` blocks of 128
