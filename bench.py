@@ -10,13 +10,17 @@ H=128) on 4,194,304 query points, half uniform in [-1,1]^3 and half within
 0.02 of the 16-sphere-union surface (seed 1).  One step = one pass over the
 batch.  ``value`` is queries/s with the points already resident in HBM;
 ``e2e`` is the same metric through the public API with host buffers
-(``OctreeSDF.sdf_host`` -> ``nglod_sdf_fwd_host``): the points are copied
-from pinned host memory and the distances copied back inside the timed
-region, in 512k-point chunks whose copies overlap the kernels.  The
-``roofline`` object names the binding one of three live-measured terms of
-``sdf_fwd_f32_kernel``: the corner gathers against a measured line-read
-ceiling, the HBM bytes against the measured copy bandwidth, and the float32
-FLOPs against a measured FMA rate.
+(``OctreeSDF.sdf_host`` -> ``nglod_sdf_fwd_host``) inside the timed region:
+the points are pinned host memory and the distances go to pinned host
+memory; since both are mapped, the query kernel itself reads the points and
+writes the distances over the GPU's host link (NVLink-C2C on GB300) in one
+launch, with no staging copies (other host memory goes through chunked
+copies that overlap the kernels).  The ``roofline`` object names the
+binding one of five live-measured terms of ``sdf_fwd_f32_staged_kernel``:
+the corner lines served by L2 against a measured line-read ceiling, all
+corner lines against a measured shared-memory line-read rate, the HBM bytes
+against the measured copy bandwidth, the float32 FLOPs against a measured
+FMA rate, and the TF32 products against the nominal tensor rate.
 
 The model holds the sphere-union SDF through ``analytic_init`` (deterministic
 and traced with real hits; throughput does not depend on the weights).
@@ -438,8 +442,9 @@ def run_ours(args):
     value = ws * N_POINTS / (ms_per_step / 1e3)
 
     # e2e through the public API with host buffers: OctreeSDF.sdf_host ->
-    # nglod_sdf_fwd_host copies the pinned points in and the distances out
-    # every step, in 512k-point chunks whose copies overlap the kernels.
+    # nglod_sdf_fwd_host; the points and distances are pinned (mapped) host
+    # memory, which the query kernel reads and writes over the host link
+    # every step.
     def e2e_step():
         net.sdf_host(x_host, lod=LOD, out=out_host)
 
@@ -489,6 +494,8 @@ def run_ours(args):
                        "point_distribution": "half U[-1,1]^3, half within 0.02 of the 16-sphere union (seed 1)",
                        "l2": "256 MiB flush between timed steps", "parallelism": f"replicas x{ws}"},
             "e2e": {"value": ws * N_POINTS / (e2e_ms / 1e3), "unit": UNIT, "ms_per_step": e2e_ms,
+                    "transfer": "points read from and distances written to pinned, mapped host memory by the "
+                                "query kernel over the host link (NVLink-C2C), every step",
                     "h2d_bytes_per_step": N_POINTS * 12, "d2h_bytes_per_step": N_POINTS * 4},
             "gpu_launches": args.steps,
             "parity": "1e-5 abs on SDF values vs the reference (tests/test_dense_gpu.py)",
@@ -576,6 +583,8 @@ def bench_bf16(tnet, x, x_host, c, r, dev, flush, stream, steps, line_peak_f32=N
                         "headline's 4,194,304 points; weights of 2,000 training steps from seed 1",
             "value": N_POINTS / sec, "unit": UNIT, "ms_per_step": ms, "steps": k, "dtype": "bf16",
             "e2e": {"value": N_POINTS / (e2e_ms / 1e3), "unit": UNIT, "ms_per_step": e2e_ms,
+                    "transfer": "points read from and distances written to pinned, mapped host memory by the "
+                                "query kernel over the host link (NVLink-C2C), every step",
                     "h2d_bytes_per_step": N_POINTS * 12, "d2h_bytes_per_step": N_POINTS * 4},
             "roofline": roof,
             "error_vs_fp64_per_lod": fp64_errors(tnet, bnet, xs),

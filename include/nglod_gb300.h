@@ -115,10 +115,12 @@ int nglod_sdf_fwd_simt(const nglod_dense_model *model, const float *x, int64_t n
  * are incomplete), else 0.  No counterpart in the reference. */
 int nglod_dense_status(int32_t *status_out);
 
-/* nglod_sdf_fwd with the points and results in HOST memory (pinned for the
- * copies to overlap): x_host [n][3], out_host [n].  The points go through a
- * device staging area in chunks of `chunk` points; chunk i's copy in,
- * kernel and copy out run on one of three streams (the caller's and two
+/* nglod_sdf_fwd with the points and results in HOST memory: x_host [n][3],
+ * out_host [n].  When both are pinned and mapped (cudaHostAlloc,
+ * cudaHostRegister; PyTorch's pin_memory), one kernel launch reads the points
+ * and writes the results over the host link itself.  Otherwise the points go
+ * through a device staging area in chunks of `chunk` points; chunk i's copy
+ * in, kernel and copy out run on one of three streams (the caller's and two
  * library streams forked from and joined back into it), so the copies of
  * one chunk overlap the kernels of the others.  scratch: device buffer of
  * nglod_host_query_scratch_bytes(chunk) bytes, 256-byte aligned.  Queued on

@@ -644,13 +644,29 @@ __global__ void __launch_bounds__(b16st::kThreads, 1)
     uint32_t phase = 0;
     bool pending = false;  // group leader: an issued product whose completion it did not see
 
-    for (int64_t t = (int64_t)blockIdx.x * kGroups + grp; t * kTP < a.n; t += (int64_t)gridDim.x * kGroups) {
+    const int64_t stride = (int64_t)gridDim.x * kGroups;
+    // this thread's point of the group's next tile, loaded one tile ahead (the
+    // points may be host memory read over the host link)
+    float nx = 0.f, ny = 0.f, nz = 0.f;
+    {
+        const int64_t i0 = ((int64_t)blockIdx.x * kGroups + grp) * kTP + gtid;
+        if (i0 < a.n) {
+            nx = a.x[3 * i0];
+            ny = a.x[3 * i0 + 1];
+            nz = a.x[3 * i0 + 2];
+        }
+    }
+    for (int64_t t = (int64_t)blockIdx.x * kGroups + grp; t * kTP < a.n; t += stride) {
         const int64_t gi = t * kTP + gtid;
-        float px = 0.f, py = 0.f, pz = 0.f;
-        if (gi < a.n) {
-            px = a.x[3 * gi];
-            py = a.x[3 * gi + 1];
-            pz = a.x[3 * gi + 2];
+        const float px = nx, py = ny, pz = nz;
+        {
+            const int64_t in = gi + stride * kTP;
+            nx = ny = nz = 0.f;
+            if (in < a.n) {
+                nx = a.x[3 * in];
+                ny = a.x[3 * in + 1];
+                nz = a.x[3 * in + 2];
+            }
         }
         // 1. gather: the warp's 32 points (rows 32 quad ..), staged levels
         // from shared memory, the rest from the pair volumes in global memory

@@ -28,12 +28,14 @@ void set_f32tc_wait_polls(uint32_t polls);
 
 inline bool aligned(const void *p, uintptr_t a) { return (reinterpret_cast<uintptr_t>(p) & (a - 1)) == 0; }
 
-// Host-memory queries: points [n][3] and results [n] in host memory, in
-// chunks through a device staging area of kHostStages buffers; chunk i runs
-// H2D -> kernel -> D2H on stage i % kHostStages, whose stream is the
-// caller's (stage 0) or one of the library's helper streams of the current
-// device, forked from and joined back into the caller's stream, so that the
-// copies of one chunk overlap the kernels of the others.
+// Host-memory queries: points [n][3] and results [n] in host memory.  When
+// both are pinned and mapped, one kernel launch reads and writes them over
+// the host link directly.  Otherwise they go in chunks through a device
+// staging area of kHostStages buffers; chunk i runs H2D -> kernel -> D2H on
+// stage i % kHostStages, whose stream is the caller's (stage 0) or one of
+// the library's helper streams of the current device, forked from and
+// joined back into the caller's stream, so that the copies of one chunk
+// overlap the kernels of the others.
 constexpr int kHostStages = 3;
 int64_t host_stage_bytes(int64_t chunk);
 // launch(x_dev, m, out_dev, stream) queues one chunk's kernel.

@@ -322,19 +322,35 @@ __global__ void __launch_bounds__(f32st::kThreads, 1)
     // Software-pipelined per group: the product of tile k runs while the
     // group gathers tile k + 1; then tile k's epilogue, then tile k + 1's
     // rows and product.
-    for (int64_t t = (int64_t)blockIdx.x * kGroups + grp;; t += (int64_t)gridDim.x * kGroups) {
+    const int64_t stride = (int64_t)gridDim.x * kGroups;
+    // this thread's point of the group's next tile, loaded one tile ahead (the
+    // points may be host memory read over the host link)
+    float nx = 0.f, ny = 0.f, nz = 0.f;
+    {
+        const int64_t i0 = ((int64_t)blockIdx.x * kGroups + grp) * kTP + gtid;
+        if (i0 < n) {
+            nx = x[3 * i0];
+            ny = x[3 * i0 + 1];
+            nz = x[3 * i0 + 2];
+        }
+    }
+    for (int64_t t = (int64_t)blockIdx.x * kGroups + grp;; t += stride) {
         const bool has = t * kTP < n;
         const int64_t i = t * kTP + gtid;
-        float px = 0.f, py = 0.f, pz = 0.f;
+        const float px = nx, py = ny, pz = nz;
+        {
+            const int64_t in = i + stride * kTP;
+            nx = ny = nz = 0.f;
+            if (in < n) {
+                nx = x[3 * in];
+                ny = x[3 * in + 1];
+                nz = x[3 * in + 2];
+            }
+        }
         float4 acc[8];
 #pragma unroll
         for (int p = 0; p < 8; ++p) acc[p] = make_float4(0.f, 0.f, 0.f, 0.f);
         if (has) {
-            if (i < n) {
-                px = x[3 * i];
-                py = x[3 * i + 1];
-                pz = x[3 * i + 2];
-            }
             // 1. gather and LOD sum of the warp's 32 points (rows 32 quad ..)
             const float4 *vol = reinterpret_cast<const float4 *>(sm + kVol);
 #pragma unroll 1

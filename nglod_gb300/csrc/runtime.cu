@@ -53,12 +53,29 @@ int64_t host_stage_bytes(int64_t chunk) {
     return kHostStages * (xs + os);
 }
 
+// The device address of host memory the GPU reads and writes directly
+// (pinned and mapped: cudaHostAlloc, cudaHostRegister), else null.
+static void *mapped_host(const void *p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 int host_query_pipeline(const float *x_host, int64_t n, float *out_host, int64_t chunk, void *scratch,
                         cudaStream_t stream, HostChunkLaunch launch, const void *ctx) {
     NGLOD_REQUIRE(n >= 0 && chunk >= 1, NGLOD_ERR_INVALID, "n=%lld, chunk=%lld", (long long)n, (long long)chunk);
     if (n == 0) return NGLOD_OK;
     NGLOD_REQUIRE(x_host && out_host && scratch, NGLOD_ERR_INVALID, "null pointer argument");
     NGLOD_REQUIRE(aligned(scratch, 256), NGLOD_ERR_ALIGN, "scratch must be 256-byte aligned");
+    // Pinned, mapped host buffers: the kernel reads the points and writes
+    // the results over the host link itself, in one launch, with no staging
+    // copies.
+    const float *x_map = static_cast<const float *>(mapped_host(x_host));
+    float *out_map = static_cast<float *>(mapped_host(out_host));
+    if (x_map && out_map) return launch(ctx, x_map, n, out_map, stream);
     int dev = 0;
     NGLOD_TRY(cuda_status(cudaGetDevice(&dev), "host query: device"));
     NGLOD_REQUIRE(dev >= 0 && dev < 64, NGLOD_ERR_UNSUPPORTED, "device %d", dev);
