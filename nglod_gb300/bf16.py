@@ -100,11 +100,13 @@ class Bf16OctreeSDF:
         return out
 
     def sdf_host(self, x_host, lod=None, out=None, chunk=1 << 19):
-        """sdf of points in host memory ([n, 3] float32; pinned for overlap)
-        into host memory ([n, 1] float32, returned): chunks are copied in,
-        evaluated and copied out on three streams joined into the current
-        one (nglod_sdf_fwd_bf16_host).  The result is complete once the
-        current stream's work is (e.g. after torch.cuda.synchronize())."""
+        """sdf of points in host memory ([n, 3] float32) into host memory
+        ([n, 1] float32, returned) through nglod_sdf_fwd_bf16_host: pinned
+        points and results are read and written by the query kernel itself
+        over the host link; other host memory is copied in, evaluated and
+        copied out in chunks on three streams joined into the current one.
+        The result is complete once the current stream's work is (e.g. after
+        torch.cuda.synchronize())."""
         if lod is None:
             lod = self.lod
         if x_host.is_cuda or x_host.dtype != torch.float32 or not x_host.is_contiguous():

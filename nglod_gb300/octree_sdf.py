@@ -154,10 +154,12 @@ class OctreeSDF(nn.Module):
 
     @torch.no_grad()
     def sdf_host(self, x_host, lod=None, out=None, chunk=1 << 19):
-        """Inference sdf of points in host memory ([n, 3] float32; pinned for
-        overlap) into host memory ([n, 1], returned), pipelined in chunks on
-        three streams joined into the current one (nglod_sdf_fwd_host).  The
-        result is complete once the current stream's work is."""
+        """Inference sdf of points in host memory ([n, 3] float32) into host
+        memory ([n, 1], returned; pinned when allocated here) through
+        nglod_sdf_fwd_host: pinned points and results are read and written by
+        the query kernel itself over the host link, other host memory goes
+        in chunks pipelined on three streams joined into the current one.
+        The result is complete once the current stream's work is."""
         if lod is None:
             lod = self.lod
         if x_host.is_cuda or x_host.dtype != torch.float32 or not x_host.is_contiguous():

@@ -156,15 +156,21 @@ def test_bf16_trace_matches_fp32_trace_semantics(nets):
     assert abs(r16.depth[2, 0].item() - r32.depth[2, 0].item()) < 5e-3
 
 
+@pytest.mark.parametrize("pinned", [True, False])
 @pytest.mark.parametrize("n,chunk", [(0, 1000), (1, 1000), (9999, 1000), (300_001, 65_536), (1_048_576, 1 << 20)])
-def test_host_memory_queries_equal_device_queries(nets, n, chunk):
-    """sdf_host (host points in, host distances out, chunks pipelined on three
-    streams) gives bitwise the device path's values, BF16 and float32 forms."""
+def test_host_memory_queries_equal_device_queries(nets, n, chunk, pinned):
+    """sdf_host gives bitwise the device path's values, BF16 and float32
+    forms: with pinned host buffers the query kernel reads and writes them
+    itself; with pageable ones they go in chunks pipelined on three streams."""
     net, bnet, _, _, _ = nets
     dev = net.features[0].fm.device
-    x = (torch.rand(n, 3) * 2.2 - 1.1).pin_memory()
-    got16 = bnet.sdf_host(x, lod=4, chunk=chunk)
-    got32 = net.sdf_host(x, lod=3, chunk=chunk)
+    x = torch.rand(n, 3) * 2.2 - 1.1
+    if pinned:
+        x = x.pin_memory()
+    out16 = torch.empty(n, 1, pin_memory=pinned)
+    out32 = torch.empty(n, 1, pin_memory=pinned)
+    got16 = bnet.sdf_host(x, lod=4, chunk=chunk, out=out16)
+    got32 = net.sdf_host(x, lod=3, chunk=chunk, out=out32)
     torch.cuda.synchronize()
     bnet.check_status()
     assert got16.shape == (n, 1) and got32.shape == (n, 1)
