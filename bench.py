@@ -109,16 +109,16 @@ TF32_NOMINAL_TFLOPS = 1100.0
 # traffic is null.
 NCU_CAPTURES = {
     "sdf_fwd_f32_staged_kernel": {
-        "dram_bytes": 91_242_496 + 10_955_264, "points": N_POINTS,
+        "dram_bytes": 91_286_016 + 10_711_552, "points": N_POINTS,
         "sources": ["nglod_gb300/csrc/dense.cu", "nglod_gb300/csrc/dense_common.cuh",
                     "nglod_gb300/csrc/f32_tile.cuh", "nglod_gb300/csrc/tf32_tile.cuh",
                     "nglod_gb300/csrc/tc_common.cuh"],
-        "sha256": "01e0389b43152b90da9edd90f39da63396df2372e9a768657baf839275f78827",
+        "sha256": "0d28d5300def798633dc4289e33b49a8306193d23d25db07d87da1c717bae5ea",
         "how": "ncu --set full --clock-control none, one launch at 4,194,304 points (bench --no-extras)"},
     "sdf_fwd_bf16_staged_kernel": {
-        "dram_bytes": 90_247_168 + 10_010_368, "points": N_POINTS,
+        "dram_bytes": 90_247_424 + 9_916_928, "points": N_POINTS,
         "sources": ["nglod_gb300/csrc/bf16.cu", "nglod_gb300/csrc/bf16_tile.cuh", "nglod_gb300/csrc/tc_common.cuh"],
-        "sha256": "dc15f91c3edeacffdc46a26102f70997d66fdf032c0b4f4930d55b34f08a0f92",
+        "sha256": "80899c5c6f67d3ee412d70d7c37812a9992049b143c3fe08e41d55c09fe56fca",
         "how": "ncu --set full --clock-control none, one launch at 4,194,304 points (bench --only bf16)"},
 }
 
