@@ -58,6 +58,7 @@ import argparse
 import hashlib
 import json
 import os
+import re
 import statistics
 import subprocess
 import sys
@@ -104,21 +105,21 @@ TF32_NOMINAL_TFLOPS = 1100.0
 
 # DRAM traffic of single ncu captures of the headline kernels on this
 # workload (dram__bytes_read.sum + dram__bytes_write.sum of one launch), with
-# the SHA-256 of the kernel sources they were captured from.  A figure is
-# reported only while those sources are unchanged; otherwise the roofline's
-# traffic is null.
+# the SHA-256 of the code of the kernel sources they were captured from
+# (comments and blank space removed).  A figure is reported only while that
+# code is unchanged; otherwise the roofline's traffic is null.
 NCU_CAPTURES = {
     "sdf_fwd_f32_staged_kernel": {
         "dram_bytes": 91_286_016 + 10_711_552, "points": N_POINTS,
         "sources": ["nglod_gb300/csrc/dense.cu", "nglod_gb300/csrc/dense_common.cuh",
                     "nglod_gb300/csrc/f32_tile.cuh", "nglod_gb300/csrc/tf32_tile.cuh",
                     "nglod_gb300/csrc/tc_common.cuh"],
-        "sha256": "0d28d5300def798633dc4289e33b49a8306193d23d25db07d87da1c717bae5ea",
+        "sha256": "7dafd1797f6f76c6432432f23b8d2c19bb3d461d3c54282d3642bf09845f3570",
         "how": "ncu --set full --clock-control none, one launch at 4,194,304 points (bench --no-extras)"},
     "sdf_fwd_bf16_staged_kernel": {
         "dram_bytes": 90_247_424 + 9_916_928, "points": N_POINTS,
         "sources": ["nglod_gb300/csrc/bf16.cu", "nglod_gb300/csrc/bf16_tile.cuh", "nglod_gb300/csrc/tc_common.cuh"],
-        "sha256": "80899c5c6f67d3ee412d70d7c37812a9992049b143c3fe08e41d55c09fe56fca",
+        "sha256": "b54b66dcdfe53ee43b86a2d0c18ba0dee16557d6d7f3934768752cc63c4824c5",
         "how": "ncu --set full --clock-control none, one launch at 4,194,304 points (bench --only bf16)"},
 }
 
@@ -135,11 +136,21 @@ def parse():
     return p.parse_args()
 
 
+def code_text(src):
+    """C/C++/CUDA source without comments and blank space: what a capture's
+    validity depends on (a comment edit leaves the compiled kernel as it
+    was).  String literals in these sources hold no comment markers."""
+    src = re.sub(r"/\*.*?\*/", " ", src, flags=re.S)
+    src = re.sub(r"//[^\n]*", " ", src)
+    return " ".join(src.split())
+
+
 def sources_sha(paths):
+    """SHA-256 of the code (comments and blank space removed) of `paths`."""
     h = hashlib.sha256()
     for rel in paths:
-        with open(os.path.join(ROOT, rel), "rb") as f:
-            h.update(f.read())
+        with open(os.path.join(ROOT, rel), encoding="utf-8") as f:
+            h.update(code_text(f.read()).encode())
     return h.hexdigest()
 
 

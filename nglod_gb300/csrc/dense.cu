@@ -54,21 +54,22 @@ __global__ void __launch_bounds__(256, kAll ? 2 : 3) sdf_fwd_f32_kernel(const ng
 }
 
 // ---------------------------------------------------------------------------
-// sdf forward, tensor-core form (single LOD, hidden 128)
+// tensor-core decode of the float32 tracer (single LOD, hidden 128)
 // ---------------------------------------------------------------------------
 // The same gather and LOD sum as sdf_fwd_f32_kernel (gather_warp_add_f32, in
-// float32), then the decoder's 32 x 128 feature product on tcgen05 as three
-// TF32 products over big / small splits of both operands (tf32_tile.cuh:
-// relative error about 2^-21 of sum |w f|, the size of float32's rounding),
-// accumulated in TMEM.  The x, y, z and bias terms of the first layer, the
-// ReLU and the 128 -> 1 layer are a float32 epilogue per point.
+// float32), then the decoder's first layer on tcgen05 as split-TF32 products
+// over big / small parts of both operands (f32_tile.cuh, tf32_tile.cuh:
+// relative error about 2^-21 of sum |w x|, the size of float32's rounding),
+// accumulated in TMEM; the ReLU and the 128 -> 1 layer are a float32
+// epilogue per point.
 //
 // A block of eight warps decodes two 128-point tiles per iteration against
-// one staged weight tile: warps 0-3 fill tile 0, warps 4-7 tile 1 (warp w,
-// lane i owns point 256 q + 32 w + i), one thread issues both tiles' 24
-// MMAs, and each warp reads its rows back from the TMEM lanes of its
-// quadrant (warp % 4) in its tile's 128 columns.  Two blocks per SM hold
-// 2 x 256 TMEM columns, the SM's 512.
+// one staged weight side: warps 0-3 fill tile 0, warps 4-7 tile 1 (warp w,
+// lane i owns point 32 w + i of the block's 256), one thread issues both
+// tiles' 28 MMAs, and each warp reads its rows back from the TMEM lanes of
+// its quadrant (warp % 4) in its tile's 128 columns.  Two blocks per SM hold
+// 2 x 256 TMEM columns, the SM's 512.  The point query runs the same rows,
+// products and epilogue in the persistent kernel below.
 namespace f32tc {
 using f32tile::kTP;
 using f32tile::kH;
