@@ -204,11 +204,23 @@ __device__ __forceinline__ uint32_t decide_nugget(const TraverseArgs &a, int2 nu
             o = a.octree[node];
             const RayFaces f = ray_faces(a.org, a.dir, (uint32_t)nug.x, a.level + 1);
             const float bx = (float)(2 * (int)p.x), by = (float)(2 * (int)p.y), bz = (float)(2 * (int)p.z);
+            // A child's three plane tests depend on two of its three
+            // coordinates each, so the eight children need twelve distinct
+            // tests (the same expressions on the same inputs as testing
+            // every child alone); all twelve run, without branches.
+            uint32_t m0 = 0, m1 = 0, m2 = 0;
+#pragma unroll
+            for (int u = 0; u < 2; ++u)
+#pragma unroll
+                for (int w = 0; w < 2; ++w) {
+                    m0 |= (uint32_t)face_straddles(by + (float)u, bz + (float)w, f.a0, f.b0, f.c0) << (2 * u + w);
+                    m1 |= (uint32_t)face_straddles(bx + (float)u, bz + (float)w, f.a1, f.b1, f.c1) << (2 * u + w);
+                    m2 |= (uint32_t)face_straddles(bx + (float)u, by + (float)w, f.a2, f.b2, f.c2) << (2 * u + w);
+                }
 #pragma unroll
             for (int j = 0; j < 8; ++j) {
-                if (!(o & (1u << j))) continue;
-                if (faces_hit(f, bx + (float)((j >> 2) & 1), by + (float)((j >> 1) & 1), bz + (float)(j & 1)))
-                    inf |= 1u << j;
+                const int dx = (j >> 2) & 1, dy = (j >> 1) & 1, dz = j & 1;
+                inf |= ((o >> j) & (m0 >> (2 * dy + dz)) & (m1 >> (2 * dx + dz)) & (m2 >> (2 * dx + dy)) & 1u) << j;
             }
             inf |= origin_octant(a.org, (uint32_t)nug.x, p, a.level) << 8;
         }
