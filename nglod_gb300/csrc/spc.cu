@@ -53,20 +53,18 @@ __constant__ uint32_t c_child_order[8] = {order_word(0), order_word(1), order_wo
 // itself: of the nine legal contractions of the two expressions, only this
 // one reproduces all of its decisions on 135M ray/voxel candidates (a
 // 1920x1080 frame through a level-7 octree).
+// The reference keeps a running min (from 1) and max (from -1) of the four
+// corner values, skipping NaNs, and tests min <= 0 and max >= 0; that is
+// "some value <= 0 and some value >= 0", which fminf / fmaxf (a NaN operand
+// yields the other one; all NaN gives NaN, which fails both tests) decide in
+// six min / max operations.
 __device__ __forceinline__ bool face_straddles(float fi, float fj, float a, float b, float c) {
     const float r0 = __fadd_rn(__fmaf_rn(b, fj, __fmul_rn(a, fi)), c);
     const float r1 = __fadd_rn(r0, a);
     const float r2 = __fadd_rn(r0, b);
     const float r3 = __fadd_rn(r1, b);
-    float mn = 1.f, mx = -1.f;
-    mn = r0 < mn ? r0 : mn;
-    mx = r0 > mx ? r0 : mx;
-    mn = r1 < mn ? r1 : mn;
-    mx = r1 > mx ? r1 : mx;
-    mn = r2 < mn ? r2 : mn;
-    mx = r2 > mx ? r2 : mx;
-    mn = r3 < mn ? r3 : mn;
-    mx = r3 > mx ? r3 : mx;
+    const float mn = fminf(fminf(r0, r1), fminf(r2, r3));
+    const float mx = fmaxf(fmaxf(r0, r1), fmaxf(r2, r3));
     return mn <= 0.f && mx >= 0.f;
 }
 
