@@ -502,9 +502,9 @@ constexpr int kThreads = 256;
 constexpr uint32_t kInBytes = kTP * kK1 * 2;   // 12 KB
 constexpr uint32_t kWBytes = kH * kK1 * 2;     // 12 KB
 constexpr uint32_t kMBytes = kTP * kH * 2;     // 32 KB
-constexpr size_t kIn = 0;                      // IN: buffer b hi at kIn + 2b * kInBytes, lo after it
-constexpr size_t kM = kIn + 4 * kInBytes;      // M: buffer b hi at kM + 2b * kMBytes, lo after it
-constexpr size_t kWH = kM + 4 * kMBytes, kWL = kWH + kWBytes;  // W1 hi / lo
+constexpr size_t kIn = 0;                      // g . IN: buffer b hi at kIn + 2b * kInBytes, lo after it
+constexpr size_t kM = kIn + 4 * kInBytes;      // ReLU mask (bf16 1 / 0): buffer b at kM + b * kMBytes
+constexpr size_t kWH = kM + 2 * kMBytes, kWL = kWH + kWBytes;  // W1 hi / lo
 // next tile's feature sums [128][32] f32, rows kStageRow float4 apart: nine,
 // so that the eight rows a quarter warp copies or reads fall in eight bank
 // groups (eight float4 apart they would share four banks)
@@ -542,19 +542,20 @@ __device__ __forceinline__ float in_column(int c, const float (&xf)[3], const fl
     return c == 35 ? 1.f : 0.f;
 }
 
-// Columns 24 HALF .. 24 HALF + 23 of IN row r (hi and lo tiles); rows of
-// points past the end are zero.
+// Columns 24 HALF .. 24 HALF + 23 of row r of g . IN (hi and lo tiles: the
+// point's dLoss/dpred times its decoder input); rows of points past the end
+// are zero.
 template <int HALF>
 __device__ __forceinline__ void fill_in_row(uint8_t *in_hi, uint8_t *in_lo, int r, const float (&xf)[3],
-                                            const float4 (&fr)[8], bool valid) {
+                                            const float4 (&fr)[8], bool valid, float g) {
 #pragma unroll
     for (int cc = 0; cc < 3; ++cc) {
         const int c0 = HALF * 24 + cc * 8;
         uint32_t h[4], lo[4];
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-            const float v0 = valid ? in_column(c0 + 2 * k, xf, fr) : 0.f;
-            const float v1 = valid ? in_column(c0 + 2 * k + 1, xf, fr) : 0.f;
+            const float v0 = valid ? g * in_column(c0 + 2 * k, xf, fr) : 0.f;
+            const float v1 = valid ? g * in_column(c0 + 2 * k + 1, xf, fr) : 0.f;
             split_bf16x2(v0, v1, h[k], lo[k]);
         }
         const uint32_t off = tc::tile_offset(r, c0, bwdtc::kKC1);
@@ -596,7 +597,8 @@ __device__ __forceinline__ void stage_tile(const BwdArgs &a, int l, int64_t tile
 // IN rows of `tile` (staged by stage_tile, copies complete and visible) into
 // IN buffer `buf`: thread (r, half) fills columns 24 half .. 24 half + 23 of
 // row r.
-__device__ __forceinline__ void fill_in_tile(const BwdArgs &a, int64_t tile, uint8_t *smem, int buf, int tid) {
+__device__ __forceinline__ void fill_in_tile(const BwdArgs &a, int64_t tile, uint8_t *smem, int buf, int tid,
+                                             float g) {
     using namespace bwdtc;
     const int r = tid & (kTP - 1), half = tid >> 7;
     const bool valid = tile * kTP + r < a.n;
@@ -608,50 +610,41 @@ __device__ __forceinline__ void fill_in_tile(const BwdArgs &a, int64_t tile, uin
     for (int k = 0; k < 8; ++k) fr[k] = sf[k];
     uint8_t *hi = smem + kIn + (size_t)(2 * buf) * kInBytes, *lo = hi + kInBytes;
     if (half == 0)
-        fill_in_row<0>(hi, lo, r, xf, fr, valid);
+        fill_in_row<0>(hi, lo, r, xf, fr, valid, g);
     else
-        fill_in_row<1>(hi, lo, r, xf, fr, valid);
+        fill_in_row<1>(hi, lo, r, xf, fr, valid, g);
 }
 
-// M row `row` (columns 64 hf .. 64 hf + 63) of buffer `buf`: g where the
-// 64 mask bits `bits` are set, else 0, as bf16 hi / lo.
-__device__ __forceinline__ void fill_m_row(uint8_t *smem, int buf, int row, int hf, float g, uint2 bits) {
+// Mask row `row` (columns 64 hf .. 64 hf + 63) of buffer `buf`: bf16 1.0
+// where the 64 mask bits `bits` are set, else 0 (exact in bf16).
+__device__ __forceinline__ void fill_m_row(uint8_t *smem, int buf, int row, int hf, uint2 bits) {
     using namespace bwdtc;
-    const __nv_bfloat16 gh = __float2bfloat16_rn(g);
-    const __nv_bfloat16 gl = __float2bfloat16_rn(g - __bfloat162float(gh));
-    const uint32_t uh = *reinterpret_cast<const uint16_t *>(&gh), ul = *reinterpret_cast<const uint16_t *>(&gl);
-    uint8_t *mh = smem + kM + (size_t)(2 * buf) * kMBytes, *ml = mh + kMBytes;
+    uint8_t *mt = smem + kM + (size_t)buf * kMBytes;
 #pragma unroll
     for (int u = 0; u < 8; ++u) {  // 8 columns per 16-byte store
         const uint32_t b8 = ((u < 4 ? bits.x : bits.y) >> (8 * (u & 3))) & 0xFFu;
-        uint32_t h[4], lo[4];
+        uint32_t h[4];
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const uint32_t m0 = (b8 >> (2 * k)) & 1u, m1 = (b8 >> (2 * k + 1)) & 1u;
-            h[k] = (m0 ? uh : 0u) | (m1 ? uh << 16 : 0u);
-            lo[k] = (m0 ? ul : 0u) | (m1 ? ul << 16 : 0u);
-        }
-        const uint32_t off = tc::tile_offset(row, 64 * hf + 8 * u, kKCH);
-        *reinterpret_cast<uint4 *>(mh + off) = make_uint4(h[0], h[1], h[2], h[3]);
-        *reinterpret_cast<uint4 *>(ml + off) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
+        for (int k = 0; k < 4; ++k)
+            h[k] = ((b8 >> (2 * k)) & 1u ? 0x3F80u : 0u) | ((b8 >> (2 * k + 1)) & 1u ? 0x3F800000u : 0u);
+        *reinterpret_cast<uint4 *>(mt + tc::tile_offset(row, 64 * hf + 8 * u, kKCH)) = make_uint4(h[0], h[1], h[2], h[3]);
     }
 }
 
-// Thread 0 issues the three-term product D (+)= A . B over KSTEPS K steps
-// of 16 (A, B descriptors advanced by a_step / b_step bytes per step); the
-// descriptors of hi and lo differ only in their start address.
+// Thread 0 issues D (+)= A . (B_hi + B_lo) over KSTEPS K steps of 16, for an
+// A that bf16 holds exactly (the 1 / 0 mask).
 template <int KSTEPS>
-__device__ __forceinline__ void mma3(uint32_t d, uint32_t a_hi, uint32_t a_lo, uint32_t b_hi, uint32_t b_lo,
-                                     uint32_t a_lbo, uint32_t a_sbo, uint32_t a_step, uint32_t b_lbo,
-                                     uint32_t b_sbo, uint32_t b_step, uint32_t idesc, bool accumulate) {
-    const uint64_t ah = tc::smem_desc(a_hi, a_lbo, a_sbo), al = tc::smem_desc(a_lo, a_lbo, a_sbo);
+__device__ __forceinline__ void mma2(uint32_t d, uint32_t a, uint32_t b_hi, uint32_t b_lo, uint32_t a_lbo,
+                                     uint32_t a_sbo, uint32_t a_step, uint32_t b_lbo, uint32_t b_sbo,
+                                     uint32_t b_step, uint32_t idesc, bool accumulate) {
+    const uint64_t ad0 = tc::smem_desc(a, a_lbo, a_sbo);
     const uint64_t bh = tc::smem_desc(b_hi, b_lbo, b_sbo), bl = tc::smem_desc(b_lo, b_lbo, b_sbo);
 #pragma unroll
-    for (int t = 0; t < 3; ++t)
+    for (int t = 0; t < 2; ++t)
 #pragma unroll
         for (int ks = 0; ks < KSTEPS; ++ks) {
             // start address >> 4 sits in the descriptor's low bits
-            const uint64_t ad = (t == 2 ? al : ah) + (uint64_t)((ks * a_step) >> 4);
+            const uint64_t ad = ad0 + (uint64_t)((ks * a_step) >> 4);
             const uint64_t bd = (t == 1 ? bl : bh) + (uint64_t)((ks * b_step) >> 4);
             tc::mma_bf16(d, ad, bd, idesc, (accumulate || t > 0 || ks > 0) ? 1u : 0u);
         }
@@ -706,21 +699,21 @@ __global__ void __launch_bounds__(bwdtc::kThreads, 1) sdf_bwd_decoder_tc_kernel(
             *reinterpret_cast<uint4 *>(smem + kWL + off) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
         }
         float gsum = 0.f;
+        float g_cur = 0.f;  // dLoss/dpred of this thread's row of the current tile
         stage_tile(a, l, tile, smem, tid);
         {
             const int64_t qg = tile * kTP + ql;
-            float g = 0.f;
             uint2 rm = make_uint2(0u, 0u);
             if (qg < a.n) {
-                g = a.gpred[(int64_t)l * a.n + qg];
+                g_cur = a.gpred[(int64_t)l * a.n + qg];
                 rm = reinterpret_cast<const uint2 *>(a.relu + ((int64_t)l * a.n + qg) * (kH / 32))[hf];
             }
-            fill_m_row(smem, 0, ql, hf, g, rm);
-            if (hf == 0) gsum += g;
+            fill_m_row(smem, 0, ql, hf, rm);
+            if (hf == 0) gsum += g_cur;
         }
         cp_async_wait_all();
         __syncthreads();
-        fill_in_tile(a, tile, smem, 0, tid);
+        fill_in_tile(a, tile, smem, 0, tid, g_cur);
         bool first = true;
         int buf = 0;
 
@@ -728,36 +721,37 @@ __global__ void __launch_bounds__(bwdtc::kThreads, 1) sdf_bwd_decoder_tc_kernel(
         for (; tile * kTP < a.n; tile += gridDim.x, buf ^= 1) {
             const int64_t next = tile + gridDim.x;
             const bool has_next = next * kTP < a.n;
-            // 1. rows of this tile are in buffer `buf`: dIN = M . W1, E += M^T . IN
+            // 1. rows of this tile are in buffer `buf`: dIN = g (Mask . W1) (g
+            // in the epilogue), E += Mask^T . (g IN)
             tc::fence_proxy_async_smem();
             tc::fence_before_sync();
             __syncthreads();
             if (tid == 0) {
                 tc::fence_after_sync();
-                const uint32_t mh = sbase + (uint32_t)(kM + 2 * buf * kMBytes), ml = mh + kMBytes;
+                const uint32_t mt = sbase + (uint32_t)(kM + buf * kMBytes);
                 const uint32_t ih = sbase + (uint32_t)(kIn + 2 * buf * kInBytes), il = ih + kInBytes;
-                mma3<kH / 16>(tmem + kColDin, mh, ml, sbase + (uint32_t)kWH, sbase + (uint32_t)kWL, 128, kKCH * 128,
-                              256, kKC1 * 128, 128, 2 * kKC1 * 128, id2, false);
-                mma3<kTP / 16>(tmem + kColE, mh, ml, ih, il, kKCH * 128, 128, 2 * kKCH * 128, kKC1 * 128, 128,
+                mma2<kH / 16>(tmem + kColDin, mt, sbase + (uint32_t)kWH, sbase + (uint32_t)kWL, 128, kKCH * 128, 256,
+                              kKC1 * 128, 128, 2 * kKC1 * 128, id2, false);
+                mma2<kTP / 16>(tmem + kColE, mt, ih, il, kKCH * 128, 128, 2 * kKCH * 128, kKC1 * 128, 128,
                                2 * kKC1 * 128, id3, !first);
                 tc::mma_commit(barD);
             }
             first = false;
             // 2. the next tile's rows into the other buffer while those run
+            float g_next = 0.f;
             if (has_next) {
                 stage_tile(a, l, next, smem, tid);
                 const int64_t qn = next * kTP + ql;
-                float g = 0.f;
                 uint2 rm = make_uint2(0u, 0u);
                 if (qn < a.n) {
-                    g = a.gpred[(int64_t)l * a.n + qn];
+                    g_next = a.gpred[(int64_t)l * a.n + qn];
                     rm = reinterpret_cast<const uint2 *>(a.relu + ((int64_t)l * a.n + qn) * (kH / 32))[hf];
                 }
-                fill_m_row(smem, buf ^ 1, ql, hf, g, rm);
-                if (hf == 0) gsum += g;
+                fill_m_row(smem, buf ^ 1, ql, hf, rm);
+                if (hf == 0) gsum += g_next;
                 cp_async_wait_all();
                 __syncthreads();
-                fill_in_tile(a, next, smem, buf ^ 1, tid);
+                fill_in_tile(a, next, smem, buf ^ 1, tid, g_next);
             }
             // 3. wait for the products, then dLoss/d(feature sum) and the
             // decoder's dLoss/dx of row ql
@@ -775,6 +769,8 @@ __global__ void __launch_bounds__(bwdtc::kThreads, 1) sdf_bwd_decoder_tc_kernel(
                 const int64_t qg = tile * kTP + ql;
                 float v[32];
                 tc::tmem_load32(tmem + trow + kColDin + (uint32_t)(32 * hf), v);
+#pragma unroll
+                for (int k = 0; k < 32; ++k) v[k] *= g_cur;
                 if (qg < a.n) {
                     float *o = a.dfeat + ((int64_t)l * a.n + qg) * kC;
                     if (hf == 0) {
@@ -795,6 +791,7 @@ __global__ void __launch_bounds__(bwdtc::kThreads, 1) sdf_bwd_decoder_tc_kernel(
                     }
                 }
             }
+            g_cur = g_next;
         }
         if (*abort_flag) break;
         // LOD totals from E (TMEM row j = ql): dW0 = w1 E, db0 = w1 E[:, 35],
