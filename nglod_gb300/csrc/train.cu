@@ -482,19 +482,22 @@ __global__ void __launch_bounds__(kBThreads, 2) sdf_bwd_decoder_kernel(const Bwd
 // with M[q][j] = g[q] mask[q][j], W1[j][c] = w1[j] W[j][c] and
 // E[j][c] = sum_q M[q][j] IN[q][c]; IN row of a point = x y z, the 32
 // summed features, 1 (the b0 column), zeros; W row j = w0[j][0..34], b0[j].
-// So per 128-point tile two products run on tcgen05, each as three bf16
-// MMAs over hi / lo splits (a*b ~ ah*bh + ah*bl + al*bh, relative error
-// about 2^-16 before the fp32 accumulation in TMEM):
-//   dIN [128 pts x 48]  = M [pts x 128 hid] . W1          (TMEM cols 0..47)
-//   E   [128 hid x 48] += M^T [hid x pts] . IN            (cols 64..111,
+// Since M = diag(g) Mask with Mask the 1 / 0 ReLU mask, exact in bf16, per
+// 128-point tile two products run on tcgen05, each as two bf16 MMAs against
+// the hi / lo split of the other operand (relative error about 2^-16 before
+// the fp32 accumulation in TMEM):
+//   dIN [128 pts x 48]  = Mask [pts x 128 hid] . W1, times g per point in
+//                         the epilogue                       (TMEM cols 0..47)
+//   E   [128 hid x 48] += Mask^T [hid x pts] . (g IN)        (cols 64..111,
 //                         summed over all tiles of a LOD)
-// and the hidden layer is never recomputed.  M and IN tiles are written
-// once in the K-major core-matrix layout and read by the second product
-// through MN-major descriptors (the same 8 x 16 B core matrices: for a
-// no-swizzle MN-major operand LBO is the stride between K-adjacent core
-// matrices and SBO the stride between MN-adjacent ones).  Both are double
-// buffered: the next tile's rows (its feature sums staged by cp.async) are
-// written while the tensor core works on this tile's.
+// and the hidden layer is never recomputed.  Mask and g IN tiles are
+// written once in the K-major core-matrix layout and read by the second
+// product through MN-major descriptors (the same 8 x 16 B core matrices: for
+// a no-swizzle MN-major operand LBO is the stride between K-adjacent core
+// matrices and SBO the stride between MN-adjacent ones).  One operand buffer
+// per block (100 KB), two blocks per SM: the next tile's feature sums are
+// staged by cp.async while this tile's products and epilogue run, and the
+// other block works while one waits.
 // ---------------------------------------------------------------------------
 namespace bwdtc {
 constexpr int kTP = 128, kH = 128, kK1 = 48, kKC1 = kK1 / 8, kKCH = kH / 8;
@@ -502,10 +505,10 @@ constexpr int kThreads = 256;
 constexpr uint32_t kInBytes = kTP * kK1 * 2;   // 12 KB
 constexpr uint32_t kWBytes = kH * kK1 * 2;     // 12 KB
 constexpr uint32_t kMBytes = kTP * kH * 2;     // 32 KB
-constexpr size_t kIn = 0;                      // g . IN: buffer b hi at kIn + 2b * kInBytes, lo after it
-constexpr size_t kM = kIn + 4 * kInBytes;      // ReLU mask (bf16 1 / 0): buffer b at kM + b * kMBytes
-constexpr size_t kWH = kM + 2 * kMBytes, kWL = kWH + kWBytes;  // W1 hi / lo
-// next tile's feature sums [128][32] f32, rows kStageRow float4 apart: nine,
+constexpr size_t kIn = 0;                      // g . IN: hi at kIn, lo after it
+constexpr size_t kM = kIn + 2 * kInBytes;      // ReLU mask (bf16 1 / 0)
+constexpr size_t kWH = kM + kMBytes, kWL = kWH + kWBytes;  // W1 hi / lo
+// a tile's feature sums [128][32] f32, rows kStageRow float4 apart: nine,
 // so that the eight rows a quarter warp copies or reads fall in eight bank
 // groups (eight float4 apart they would share four banks)
 constexpr int kStageRow = 9;
@@ -517,7 +520,7 @@ constexpr size_t kSmem = kAbort + 12;
 constexpr uint32_t kColDin = 0, kColE = 64, kCols = 128;
 constexpr uint32_t kPolls = 1u << 22;
 static_assert(kM % 1024 == 0 && kWH % 1024 == 0 && kBarD % 8 == 0, "shared layout alignment");
-static_assert(kSmem <= 227 * 1024, "shared layout fits one block");
+static_assert(2 * (kSmem + 1024) <= 228 * 1024, "two blocks per SM");
 }  // namespace bwdtc
 
 
@@ -650,7 +653,7 @@ __device__ __forceinline__ void mma2(uint32_t d, uint32_t a, uint32_t b_hi, uint
         }
 }
 
-__global__ void __launch_bounds__(bwdtc::kThreads, 1) sdf_bwd_decoder_tc_kernel(const BwdArgs a) {
+__global__ void __launch_bounds__(bwdtc::kThreads, 2) sdf_bwd_decoder_tc_kernel(const BwdArgs a) {
     using namespace bwdtc;
     extern __shared__ __align__(1024) uint8_t smem_tc[];
     uint8_t *smem = smem_tc;
@@ -700,36 +703,48 @@ __global__ void __launch_bounds__(bwdtc::kThreads, 1) sdf_bwd_decoder_tc_kernel(
         }
         float gsum = 0.f;
         float g_cur = 0.f;  // dLoss/dpred of this thread's row of the current tile
+        uint2 rm_cur = make_uint2(0u, 0u);
         stage_tile(a, l, tile, smem, tid);
         {
             const int64_t qg = tile * kTP + ql;
-            uint2 rm = make_uint2(0u, 0u);
             if (qg < a.n) {
                 g_cur = a.gpred[(int64_t)l * a.n + qg];
-                rm = reinterpret_cast<const uint2 *>(a.relu + ((int64_t)l * a.n + qg) * (kH / 32))[hf];
+                rm_cur = reinterpret_cast<const uint2 *>(a.relu + ((int64_t)l * a.n + qg) * (kH / 32))[hf];
             }
-            fill_m_row(smem, 0, ql, hf, rm);
-            if (hf == 0) gsum += g_cur;
         }
-        cp_async_wait_all();
-        __syncthreads();
-        fill_in_tile(a, tile, smem, 0, tid, g_cur);
         bool first = true;
-        int buf = 0;
 
 #pragma unroll 1
-        for (; tile * kTP < a.n; tile += gridDim.x, buf ^= 1) {
+        for (; tile * kTP < a.n; tile += gridDim.x) {
             const int64_t next = tile + gridDim.x;
             const bool has_next = next * kTP < a.n;
-            // 1. rows of this tile are in buffer `buf`: dIN = g (Mask . W1) (g
-            // in the epilogue), E += Mask^T . (g IN)
+            // 1. this tile's rows into the operand buffer (its last products
+            // completed before the previous epilogue)
+            fill_m_row(smem, 0, ql, hf, rm_cur);
+            if (hf == 0) gsum += g_cur;
+            cp_async_wait_all();
+            __syncthreads();
+            fill_in_tile(a, tile, smem, 0, tid, g_cur);
             tc::fence_proxy_async_smem();
             tc::fence_before_sync();
             __syncthreads();
+            // 2. the next tile's feature sums and its g and mask start loading
+            // while the products run: dIN = g (Mask . W1) (g in the
+            // epilogue), E += Mask^T . (g IN)
+            float g_next = 0.f;
+            uint2 rm_next = make_uint2(0u, 0u);
+            if (has_next) {
+                stage_tile(a, l, next, smem, tid);
+                const int64_t qn = next * kTP + ql;
+                if (qn < a.n) {
+                    g_next = a.gpred[(int64_t)l * a.n + qn];
+                    rm_next = reinterpret_cast<const uint2 *>(a.relu + ((int64_t)l * a.n + qn) * (kH / 32))[hf];
+                }
+            }
             if (tid == 0) {
                 tc::fence_after_sync();
-                const uint32_t mt = sbase + (uint32_t)(kM + buf * kMBytes);
-                const uint32_t ih = sbase + (uint32_t)(kIn + 2 * buf * kInBytes), il = ih + kInBytes;
+                const uint32_t mt = sbase + (uint32_t)kM;
+                const uint32_t ih = sbase + (uint32_t)kIn, il = ih + kInBytes;
                 mma2<kH / 16>(tmem + kColDin, mt, sbase + (uint32_t)kWH, sbase + (uint32_t)kWL, 128, kKCH * 128, 256,
                               kKC1 * 128, 128, 2 * kKC1 * 128, id2, false);
                 mma2<kTP / 16>(tmem + kColE, mt, ih, il, kKCH * 128, 128, 2 * kKCH * 128, kKC1 * 128, 128,
@@ -737,22 +752,6 @@ __global__ void __launch_bounds__(bwdtc::kThreads, 1) sdf_bwd_decoder_tc_kernel(
                 tc::mma_commit(barD);
             }
             first = false;
-            // 2. the next tile's rows into the other buffer while those run
-            float g_next = 0.f;
-            if (has_next) {
-                stage_tile(a, l, next, smem, tid);
-                const int64_t qn = next * kTP + ql;
-                uint2 rm = make_uint2(0u, 0u);
-                if (qn < a.n) {
-                    g_next = a.gpred[(int64_t)l * a.n + qn];
-                    rm = reinterpret_cast<const uint2 *>(a.relu + ((int64_t)l * a.n + qn) * (kH / 32))[hf];
-                }
-                fill_m_row(smem, buf ^ 1, ql, hf, rm);
-                if (hf == 0) gsum += g_next;
-                cp_async_wait_all();
-                __syncthreads();
-                fill_in_tile(a, next, smem, buf ^ 1, tid, g_next);
-            }
             // 3. wait for the products, then dLoss/d(feature sum) and the
             // decoder's dLoss/dx of row ql
             if (tid == 0) {
@@ -792,6 +791,7 @@ __global__ void __launch_bounds__(bwdtc::kThreads, 1) sdf_bwd_decoder_tc_kernel(
                 }
             }
             g_cur = g_next;
+            rm_cur = rm_next;
         }
         if (*abort_flag) break;
         // LOD totals from E (TMEM row j = ql): dW0 = w1 E, db0 = w1 E[:, 35],
@@ -1136,10 +1136,10 @@ extern "C" int nglod_sdf_bwd(const nglod_dense_model *model, const float *x, int
     a.gx = grad_x;
 
     if (model->hidden_dim == bwdtc::kH && relu_masks) {
-        // tensor-core form: one block of 256 threads per SM
+        // tensor-core form: two blocks of 256 threads per SM
         NGLOD_TRY(prepare_smem(sdf_bwd_decoder_tc_kernel, bwdtc::kSmem));
         const int64_t tiles = (n + bwdtc::kTP - 1) / bwdtc::kTP;
-        const int64_t cap1 = num_sms();
+        const int64_t cap1 = (int64_t)num_sms() * 2;
         sdf_bwd_decoder_tc_kernel<<<(int)(tiles < cap1 ? tiles : cap1), bwdtc::kThreads, bwdtc::kSmem,
                                     (cudaStream_t)stream>>>(a);
     } else {
