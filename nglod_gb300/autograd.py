@@ -39,7 +39,9 @@ class _SdfTrain(torch.autograd.Function):
         xd = x.detach().float().contiguous()
         n = xd.shape[0]
         dev = xd.device
-        preds = torch.zeros(L + 1, n, 1, device=dev, dtype=torch.float32)
+        # the forward writes every row in the mask; rows outside it stay zero
+        alloc = torch.empty if mask == (1 << (L + 1)) - 1 else torch.zeros
+        preds = alloc(L + 1, n, 1, device=dev, dtype=torch.float32)
         feats = torch.empty(L + 1, n, net.fdim, device=dev, dtype=torch.float32)
         # ReLU masks of the forward: the tensor-core backward (hidden_dim 128) takes them as the
         # ReLU derivative; other widths recompute the hidden layer

@@ -997,25 +997,31 @@ __global__ void __launch_bounds__(kScatterThreads, 2) sdf_bwd_scatter_kernel(con
 // ---------------------------------------------------------------------------
 // preds [rows][n], gts [n]: loss = sum over l in mask, q of (preds - gts)^2
 // / n, accumulated in float64 (block partial sums, one double atomic per
-// block); grad[l][q] = 2 (preds - gts) / n for l in mask, else 0.
+// block); grad[l][q] = 2 (preds - gts) / n for l in mask, else 0.  One
+// thread takes a point and loads its gt and every row's prediction before
+// using them (rows <= NGLOD_MAX_LODS loads in flight per thread).
 __global__ void __launch_bounds__(256) l2_loss_kernel(const float *__restrict__ preds, const float *__restrict__ gts,
                                                       int64_t n, int rows, uint32_t mask, double *loss,
                                                       float *__restrict__ grad) {
     __shared__ double part[8];
     const float scale = 2.f / (float)n;
     double acc = 0.0;
-    const int64_t total = (int64_t)rows * n;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += stride) {
-        const int l = (int)(e / n);
-        const int64_t q = e - (int64_t)l * n;
-        const bool on = (mask >> l) & 1u;
-        const float p = preds[e], g = gts[q];
-        if (on) {
-            const double d = (double)p - (double)g;
-            acc += d * d;
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += stride) {
+        const float g = gts[q];
+        float p[NGLOD_MAX_LODS];
+#pragma unroll
+        for (int l = 0; l < NGLOD_MAX_LODS; ++l) p[l] = l < rows ? preds[(int64_t)l * n + q] : 0.f;
+#pragma unroll
+        for (int l = 0; l < NGLOD_MAX_LODS; ++l) {
+            if (l >= rows) break;
+            const bool on = (mask >> l) & 1u;
+            if (on) {
+                const double d = (double)p[l] - (double)g;
+                acc += d * d;
+            }
+            grad[(int64_t)l * n + q] = on ? (p[l] - g) * scale : 0.f;
         }
-        grad[e] = on ? (p - g) * scale : 0.f;
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
@@ -1032,22 +1038,46 @@ __global__ void __launch_bounds__(256) l2_loss_kernel(const float *__restrict__ 
 // ---------------------------------------------------------------------------
 // Adam
 // ---------------------------------------------------------------------------
+// One element of the update (torch.optim.Adam's single-tensor order).
+__device__ __forceinline__ void adam_update(float &p, float g, float &m, float &v, float lr_over_bc1, float beta2,
+                                            float one_m_b1, float one_m_b2, float bc2_sqrt, float eps, float wd) {
+    if (wd != 0.f) g = g + wd * p;
+    // torch.lerp with weight < 0.5: m + w * (g - m)
+    m = m + one_m_b1 * (g - m);
+    v = v * beta2;
+    v = v + (one_m_b2 * g) * g;
+    const float denom = sqrtf(v) / bc2_sqrt + eps;
+    p = p + (-lr_over_bc1) * (m / denom);
+}
+
+// blockIdx.y selects the tensor.  Tensors whose four arrays start on 16-byte
+// boundaries go four elements per thread and access; the rest of each
+// tensor (its last numel % 4 elements, or all of an unaligned one) one.
 __global__ void __launch_bounds__(256) adam_kernel(const nglod_adam_tensor *__restrict__ tab, float lr_over_bc1,
-                                                   float beta1, float beta2, float one_m_b1, float one_m_b2,
-                                                   float bc2_sqrt, float eps, float wd) {
+                                                   float beta2, float one_m_b1, float one_m_b2, float bc2_sqrt,
+                                                   float eps, float wd) {
     const nglod_adam_tensor t = tab[blockIdx.y];
+    const int64_t first = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < t.numel; i += stride) {
-        float g = t.grad[i];
-        float p = t.param[i];
-        if (wd != 0.f) g = g + wd * p;
-        float m = t.exp_avg[i];
-        // torch.lerp with weight < 0.5: m + w * (g - m)
-        m = m + one_m_b1 * (g - m);
-        float v = t.exp_avg_sq[i] * beta2;
-        v = v + (one_m_b2 * g) * g;
-        const float denom = sqrtf(v) / bc2_sqrt + eps;
-        p = p + (-lr_over_bc1) * (m / denom);
+    const uintptr_t bits = reinterpret_cast<uintptr_t>(t.param) | reinterpret_cast<uintptr_t>(t.grad) |
+                           reinterpret_cast<uintptr_t>(t.exp_avg) | reinterpret_cast<uintptr_t>(t.exp_avg_sq);
+    const int64_t nv = (bits & 15u) == 0 ? t.numel / 4 : 0;
+    for (int64_t i = first; i < nv; i += stride) {
+        const float4 g = reinterpret_cast<const float4 *>(t.grad)[i];
+        float4 p = reinterpret_cast<const float4 *>(t.param)[i];
+        float4 m = reinterpret_cast<const float4 *>(t.exp_avg)[i];
+        float4 v = reinterpret_cast<const float4 *>(t.exp_avg_sq)[i];
+        adam_update(p.x, g.x, m.x, v.x, lr_over_bc1, beta2, one_m_b1, one_m_b2, bc2_sqrt, eps, wd);
+        adam_update(p.y, g.y, m.y, v.y, lr_over_bc1, beta2, one_m_b1, one_m_b2, bc2_sqrt, eps, wd);
+        adam_update(p.z, g.z, m.z, v.z, lr_over_bc1, beta2, one_m_b1, one_m_b2, bc2_sqrt, eps, wd);
+        adam_update(p.w, g.w, m.w, v.w, lr_over_bc1, beta2, one_m_b1, one_m_b2, bc2_sqrt, eps, wd);
+        reinterpret_cast<float4 *>(t.exp_avg)[i] = m;
+        reinterpret_cast<float4 *>(t.exp_avg_sq)[i] = v;
+        reinterpret_cast<float4 *>(t.param)[i] = p;
+    }
+    for (int64_t i = 4 * nv + first; i < t.numel; i += stride) {
+        float p = t.param[i], m = t.exp_avg[i], v = t.exp_avg_sq[i];
+        adam_update(p, t.grad[i], m, v, lr_over_bc1, beta2, one_m_b1, one_m_b2, bc2_sqrt, eps, wd);
         t.exp_avg[i] = m;
         t.exp_avg_sq[i] = v;
         t.param[i] = p;
@@ -1190,11 +1220,11 @@ extern "C" int nglod_adam_step(const nglod_adam_tensor *tensors, int32_t count, 
     const double bc1 = 1.0 - pow((double)beta1, (double)step);
     const double bc2 = 1.0 - pow((double)beta2, (double)step);
     const int threads = 256;
-    int64_t bx = (max_numel + threads - 1) / threads;
+    int64_t bx = (max_numel + 4 * threads - 1) / (4 * threads);
     const int64_t cap = (int64_t)num_sms() * 8;
     if (bx > cap) bx = cap;
     dim3 grid((unsigned)bx, (unsigned)count);
-    adam_kernel<<<grid, threads, 0, (cudaStream_t)stream>>>(tensors, (float)((double)lr / bc1), beta1, beta2,
+    adam_kernel<<<grid, threads, 0, (cudaStream_t)stream>>>(tensors, (float)((double)lr / bc1), beta2,
                                                             (float)(1.0 - (double)beta1), (float)(1.0 - (double)beta2),
                                                             (float)sqrt(bc2), eps, weight_decay);
     return launch_status("nglod_adam_step");
@@ -1340,8 +1370,7 @@ extern "C" int nglod_l2_loss(const float *preds, const float *gts, int64_t n, in
     if (n == 0) return NGLOD_OK;
     NGLOD_REQUIRE(preds && gts && grad_preds, NGLOD_ERR_INVALID, "null pointer argument");
     const int threads = 256;
-    const int64_t total = (int64_t)rows * n;
-    const int64_t want = (total + threads - 1) / threads, cap = (int64_t)num_sms() * 8;
+    const int64_t want = (n + threads - 1) / threads, cap = (int64_t)num_sms() * 8;
     l2_loss_kernel<<<(int)(want < cap ? want : cap), threads, 0, s>>>(preds, gts, n, rows, lod_mask, loss_out,
                                                                       grad_preds);
     return launch_status("nglod_l2_loss");

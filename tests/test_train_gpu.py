@@ -145,19 +145,25 @@ def test_fused_adam_matches_torch_adam(cuda):
     p2 = p1.clone()
     q1 = torch.randn(5, 32, 9, 9, 9, device=cuda).contiguous(memory_format=torch.channels_last_3d)
     q2 = q1.clone()
-    a = trainer.FusedAdam([p1, q1], lr=1e-3)
-    b = torch.optim.Adam([p2, q2], lr=1e-3, foreach=False)
-    for p in (p1, p2, q1, q2):
+    # a length that is not a multiple of 4, and a tensor 4 bytes off a
+    # 16-byte boundary: the kernel's one-element path
+    r1 = torch.randn(1001, 3, device=cuda)
+    r2 = r1.clone()
+    u1 = torch.randn(4001, device=cuda)[1:]
+    u2 = u1.clone()
+    assert u1.data_ptr() % 16 != 0
+    a = trainer.FusedAdam([p1, q1, r1, u1], lr=1e-3)
+    b = torch.optim.Adam([p2, q2, r2, u2], lr=1e-3, foreach=False)
+    for p in (p1, p2, q1, q2, r1, r2, u1, u2):
         p.requires_grad_(True)
     for s in range(5):
-        g = torch.randn_like(p1)
-        h = torch.randn_like(q1)
-        p1.grad, p2.grad = g.clone(), g.clone()
-        q1.grad, q2.grad = h.clone(), h.clone()
+        for x1, x2 in ((p1, p2), (q1, q2), (r1, r2), (u1, u2)):
+            g = torch.randn_like(x1)
+            x1.grad, x2.grad = g.clone(), g.clone()
         a.step()
         b.step()
-    assert (p1 - p2).abs().max().item() < 1e-6
-    assert (q1 - q2).abs().max().item() < 1e-6
+    for x1, x2 in ((p1, p2), (q1, q2), (r1, r2), (u1, u2)):
+        assert (x1 - x2).abs().max().item() < 1e-6
 
 
 def test_training_reduces_loss(cuda):
