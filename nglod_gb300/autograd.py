@@ -22,10 +22,12 @@ def _model_from_params(net, fms, decs):
     m.feature_dim = net.fdim
     m.hidden_dim = net.hidden_dim
     m.grid_dtype = _lib.F32
-    for i, fm in enumerate(fms):
-        m.grid[i] = fm.data_ptr()
-    for i, (w0, b0, w1, b1) in enumerate(decs):
-        m.w0[i], m.b0[i], m.w1[i], m.b1[i] = w0.data_ptr(), b0.data_ptr(), w1.data_ptr(), b1.data_ptr()
+    m.grid[:len(fms)] = [fm.data_ptr() for fm in fms]
+    k = len(decs)
+    m.w0[:k] = [d[0].data_ptr() for d in decs]
+    m.b0[:k] = [d[1].data_ptr() for d in decs]
+    m.w1[:k] = [d[2].data_ptr() for d in decs]
+    m.b1[:k] = [d[3].data_ptr() for d in decs]
     return m
 
 
@@ -34,8 +36,9 @@ class _SdfTrain(torch.autograd.Function):
     def forward(ctx, x, mask, net, *params):
         nl = net.num_lods
         L = mask.bit_length() - 1
-        fms = [_as_cl3d(p.detach()) for p in params[:nl]]
-        decs = [tuple(p.detach().contiguous() for p in params[nl + 4 * i: nl + 4 * i + 4]) for i in range(nl)]
+        # grad mode is off here: the parameters are used and saved as they are
+        fms = [_as_cl3d(p) for p in params[:nl]]
+        decs = [tuple(p.contiguous() for p in params[nl + 4 * i: nl + 4 * i + 4]) for i in range(nl)]
         xd = x.detach().float().contiguous()
         n = xd.shape[0]
         dev = xd.device
@@ -95,9 +98,14 @@ class _SdfTrain(torch.autograd.Function):
 
 
 def train_params(net):
-    ps = [fv.fm for fv in net.features]
-    for dec in net.louts:
-        ps += [dec[0].weight, dec[0].bias, dec[2].weight, dec[2].bias]
+    """features.{i}.fm, then louts.{i}.{0,2}.{weight,bias} of every LOD, read
+    from the modules' parameter tables (nn.Sequential indexing and
+    Module.__getattr__ cost more host time than the rest of a step's
+    launch path)."""
+    ps = [fv._parameters["fm"] for fv in net.features._modules.values()]
+    for dec in net.louts._modules.values():
+        l0, l2 = dec._modules["0"]._parameters, dec._modules["2"]._parameters
+        ps += [l0["weight"], l0["bias"], l2["weight"], l2["bias"]]
     return ps
 
 

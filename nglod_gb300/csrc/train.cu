@@ -995,17 +995,40 @@ __global__ void __launch_bounds__(kScatterThreads, 2) sdf_bwd_scatter_kernel(con
 // ---------------------------------------------------------------------------
 // L2 loss of Trainer.step_geometry and its gradient in one pass
 // ---------------------------------------------------------------------------
+// Error-free transformations in float32 (Knuth's TwoSum; Dekker's product
+// with one FMA), in round-to-nearest intrinsics so that no step is fused.
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// (ah, al) += (xh, xl) for float-float values of one sign: about 2^-46
+// relative error per addition, ah the float nearest to the pair's sum.
+__device__ __forceinline__ void ff_add(float &ah, float &al, float xh, float xl) {
+    float s, e;
+    two_sum(ah, xh, s, e);
+    e = __fadd_rn(e, __fadd_rn(al, xl));
+    ah = __fadd_rn(s, e);
+    al = __fsub_rn(e, __fsub_rn(ah, s));
+}
+
 // preds [rows][n], gts [n]: loss = sum over l in mask, q of (preds - gts)^2
-// / n, accumulated in float64 (block partial sums, one double atomic per
-// block); grad[l][q] = 2 (preds - gts) / n for l in mask, else 0.  One
-// thread takes a point and loads its gt and every row's prediction before
-// using them (rows <= NGLOD_MAX_LODS loads in flight per thread).
+// / n to float64 accuracy; grad[l][q] = 2 (preds - gts) / n for l in mask,
+// else 0.  One thread takes a point and loads its gt and every row's
+// prediction before using them (rows <= NGLOD_MAX_LODS loads in flight).
+// The squares are summed as float-float pairs in float32 arithmetic, whose
+// rate is far above float64's on this part: p - g = s + e exactly (TwoSum),
+// (p - g)^2 = s*s (an exact pair through one FMA) + 2 s e, dropping e*e
+// (below 2^-48 of s*s), so a term is exact to about 2^-46 while
+// 2^-63 < |p - g| < 2^63.  Each warp's pair goes to float64 once; block
+// sums in float64, one double atomic per block.
 __global__ void __launch_bounds__(256) l2_loss_kernel(const float *__restrict__ preds, const float *__restrict__ gts,
                                                       int64_t n, int rows, uint32_t mask, double *loss,
                                                       float *__restrict__ grad) {
     __shared__ double part[8];
     const float scale = 2.f / (float)n;
-    double acc = 0.0;
+    float ah = 0.f, al = 0.f;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += stride) {
         const float g = gts[q];
@@ -1017,16 +1040,23 @@ __global__ void __launch_bounds__(256) l2_loss_kernel(const float *__restrict__ 
             if (l >= rows) break;
             const bool on = (mask >> l) & 1u;
             if (on) {
-                const double d = (double)p[l] - (double)g;
-                acc += d * d;
+                float d, e;
+                two_sum(p[l], -g, d, e);
+                const float sq = __fmul_rn(d, d);
+                const float sq_err = fmaf(d, d, -sq);
+                ff_add(ah, al, sq, __fadd_rn(sq_err, __fmul_rn(__fmul_rn(2.f, d), e)));
             }
             grad[(int64_t)l * n + q] = on ? (p[l] - g) * scale : 0.f;
         }
     }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    for (int o = 16; o > 0; o >>= 1) {
+        const float xh = __shfl_xor_sync(0xffffffffu, ah, o);
+        const float xl = __shfl_xor_sync(0xffffffffu, al, o);
+        ff_add(ah, al, xh, xl);
+    }
     const int warp = threadIdx.x >> 5;
-    if ((threadIdx.x & 31) == 0) part[warp] = acc;
+    if ((threadIdx.x & 31) == 0) part[warp] = (double)ah + (double)al;
     __syncthreads();
     if (threadIdx.x == 0) {
         double t = 0.0;

@@ -125,8 +125,10 @@ def step_geometry(net, optimizer, pts, gts, loss_lods=None):
     same values as l2_loss(...).backward()."""
     if loss_lods is None:
         loss_lods = list(range(net.num_lods))
-    net.zero_grad()
     preds = sdf_train_stacked(net, pts)
+    # after the forward's launch (which reads no gradient), so that the
+    # device starts on the step sooner
+    net.zero_grad()
     loss, grad = fused_l2_loss(preds, gts, loss_lods)
     preds.backward(grad)
     optimizer.step()
