@@ -30,6 +30,28 @@ def test_full_architecture_parameters():
     assert net.louts[4][0].weight.shape == (128, 35)
 
 
+def test_training_parameter_list_and_model_descriptor():
+    """The training path's parameter list (read from the modules' parameter
+    tables) is the reference's parameters, in the order the autograd function
+    takes them, and the kernels' model descriptor holds their addresses."""
+    from nglod_gb300 import autograd
+    net = seeded_model(num_lods=5, base_lod=2, seed=0)
+    ps = autograd.train_params(net)
+    want = [fv.fm for fv in net.features]
+    for dec in net.louts:
+        want += [dec[0].weight, dec[0].bias, dec[2].weight, dec[2].bias]
+    assert len(ps) == len(want) == 25 and all(a is b for a, b in zip(ps, want))
+    assert [id(p) for p in ps] == [id(p) for p in net.parameters()]
+    fms, decs = ps[:5], [tuple(ps[5 + 4 * i: 9 + 4 * i]) for i in range(5)]
+    m = autograd._model_from_params(net, fms, decs)
+    assert (m.num_lods, m.base_lod, m.feature_dim, m.hidden_dim) == (5, 2, 32, 128)
+    for i in range(5):
+        assert m.grid[i] == fms[i].data_ptr()
+        assert (m.w0[i], m.b0[i], m.w1[i], m.b1[i]) == tuple(t.data_ptr() for t in decs[i])
+    for i in range(5, len(m.grid)):
+        assert not m.grid[i] and not m.w0[i] and not m.b1[i]
+
+
 def test_cpu_tensors_are_rejected():
     net = seeded_model(num_lods=2)
     with torch.no_grad(), pytest.raises(RuntimeError, match="CUDA tensors only"):
