@@ -351,7 +351,8 @@ int nglod_sdf_bwd_noalloc(const nglod_dense_model *model, const float *x, int64_
 /* The loss of Trainer.step_geometry (sdf-net/lib/trainer.py:325-336) over
  * preds[rows][n] (rows = highest LOD + 1, as nglod_sdf_fwd_train writes them)
  * and gts[n]: *loss_out = sum over LODs l in lod_mask of
- * ((preds[l] - gts)^2).sum() / n, reduced in float64 on the device; and its
+ * ((preds[l] - gts)^2).sum() / n to float64 accuracy (float-float partial
+ * sums in float32 arithmetic, float64 across warps and blocks); and its
  * gradient grad_preds[l][q] = 2 (preds[l][q] - gts[q]) / n for l in the mask,
  * 0 for the other rows (the grad_preds of nglod_sdf_bwd).  One launch. */
 int nglod_l2_loss(const float *preds, const float *gts, int64_t n, int32_t rows, uint32_t lod_mask,
