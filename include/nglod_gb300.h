@@ -425,7 +425,8 @@ int nglod_spc_decode(const uint8_t *octree, int64_t osize, int16_t *points, int6
  * On return (the call synchronises once) *count = number of nuggets and
  * *result_buffer = 0 (nuggets_a) or 1 (nuggets_b) holds them.  More than
  * `capacity` nuggets at any level: NGLOD_ERR_CAPACITY (the reference
- * truncated silently). */
+ * truncated silently).  capacity < 2^29, so that a level's count (at most
+ * eight children per nugget) stays below 2^32. */
 /* Exclusive prefix sums of child counts over all octree bytes:
  * prefix[k] = sum of popcount(octree[i]) for i < k, k in [0, osize]; the
  * table the reference recomputes on every spc_raytrace call with CUB

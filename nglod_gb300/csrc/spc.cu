@@ -753,8 +753,10 @@ extern "C" int nglod_spc_raytrace(const uint8_t *octree, const int16_t *points, 
                   kMaxSpcLevels);
     NGLOD_REQUIRE(target_level >= 0 && target_level <= level, NGLOD_ERR_INVALID,
                   "target_level=%d outside [0, level=%d]", target_level, level);
-    NGLOD_REQUIRE(n_rays >= 0 && n_rays <= capacity && capacity <= ((int64_t)1 << 31) - 1, NGLOD_ERR_CAPACITY,
-                  "n_rays=%lld must not exceed capacity=%lld (< 2^31)", (long long)n_rays, (long long)capacity);
+    // a level's hit count is at most 8 x capacity (eight children per
+    // nugget) and the chunk states hold it in 32 bits
+    NGLOD_REQUIRE(n_rays >= 0 && n_rays <= capacity && capacity < ((int64_t)1 << 29), NGLOD_ERR_CAPACITY,
+                  "n_rays=%lld must not exceed capacity=%lld (< 2^29)", (long long)n_rays, (long long)capacity);
     NGLOD_REQUIRE(pyramid_host && count && result_buffer, NGLOD_ERR_INVALID, "null pointer argument");
     NGLOD_REQUIRE(pyramid_host[level + 1] == 0 && pyramid_host[level + 2] == 0, NGLOD_ERR_INVALID,
                   "bad pyramid table (the reference's 'bad spc table3' check)");

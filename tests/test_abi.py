@@ -82,6 +82,18 @@ def test_validation_errors_without_device(built_library):
         getattr(m, k)[0] = getattr(m, k)[1] = 256
     assert lib.nglod_trace(m, p, None, None, 0, None, None, None, None, None, None) == -1
     assert b"num_steps" in lib.nglod_last_error()
+    # traversal capacity: below 2^29, so that a level's count fits the 32-bit chunk states
+    import ctypes
+    pyr = (ctypes.c_int32 * 32)()
+    cnt, rb = ctypes.c_int64(0), ctypes.c_int32(0)
+
+    def raytrace(capacity):
+        return lib.nglod_spc_raytrace(None, None, None, pyr, 7, 7, None, None, 10, None, None, capacity, None, None,
+                                      None, ctypes.byref(cnt), ctypes.byref(rb), None)
+    assert raytrace(1 << 29) == -4
+    assert b"2^29" in lib.nglod_last_error()
+    assert raytrace((1 << 29) - 1) == -1  # past the capacity check: the null octree
+    assert raytrace(5) == -4  # fewer nuggets than rays
 
 
 def test_python_shim_raises_on_status():
