@@ -12,7 +12,7 @@ import ctypes
 import torch
 
 from . import _lib
-from .octree_sdf import CL3D, _as_cl3d
+from .octree_sdf import CL3D, _as_cl3d, param_list
 
 
 def _model_from_params(net, fms, decs):
@@ -98,15 +98,9 @@ class _SdfTrain(torch.autograd.Function):
 
 
 def train_params(net):
-    """features.{i}.fm, then louts.{i}.{0,2}.{weight,bias} of every LOD, read
-    from the modules' parameter tables (nn.Sequential indexing and
-    Module.__getattr__ cost more host time than the rest of a step's
-    launch path)."""
-    ps = [fv._parameters["fm"] for fv in net.features._modules.values()]
-    for dec in net.louts._modules.values():
-        l0, l2 = dec._modules["0"]._parameters, dec._modules["2"]._parameters
-        ps += [l0["weight"], l0["bias"], l2["weight"], l2["bias"]]
-    return ps
+    """The parameters the training kernels take, in their order
+    (octree_sdf.param_list)."""
+    return param_list(net)
 
 
 def sdf_train_stacked(net, x):

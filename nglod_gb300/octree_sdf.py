@@ -36,6 +36,18 @@ def _as_cl3d(t):
     return t if t.is_contiguous(memory_format=CL3D) else t.contiguous(memory_format=CL3D)
 
 
+def param_list(net):
+    """features.{i}.fm, then louts.{i}.{0,2}.{weight,bias} of every LOD, read
+    from the modules' parameter tables (nn.Sequential indexing and
+    Module.__getattr__ cost more host time than the rest of a call's launch
+    path)."""
+    ps = [fv._parameters["fm"] for fv in net.features._modules.values()]
+    for dec in net.louts._modules.values():
+        l0, l2 = dec._modules["0"]._parameters, dec._modules["2"]._parameters
+        ps += [l0["weight"], l0["bias"], l2["weight"], l2["bias"]]
+    return ps
+
+
 class FeatureVolume(nn.Module):
     """Feature grid of (fsize+1)^3 vertices x fdim channels (OctreeSDF.py:38-57)."""
 
@@ -187,24 +199,27 @@ class OctreeSDF(nn.Module):
         m.hidden_dim = self.hidden_dim
         m.grid_dtype = _lib.F32
         keep = []
-        for i in range(self.num_lods):
-            fm = self.features[i].fm
+        nl = self.num_lods
+        ps = param_list(self)
+        grids = []
+        for fm in ps[:nl]:
             if fm.dtype != torch.float32:
                 raise RuntimeError("nglod_gb300 float32 path: parameters must be float32")
             if not fm.is_contiguous(memory_format=CL3D):
                 fm = _as_cl3d(fm.detach())
                 keep.append(fm)
-            lin0, lin1 = self.louts[i][0], self.louts[i][2]
-            ws = [lin0.weight, lin0.bias, lin1.weight, lin1.bias]
-            for j, w in enumerate(ws):
-                if not w.is_contiguous():
-                    ws[j] = w.detach().contiguous()
-                    keep.append(ws[j])
-            m.grid[i] = fm.data_ptr()
-            m.w0[i] = ws[0].data_ptr()
-            m.b0[i] = ws[1].data_ptr()
-            m.w1[i] = ws[2].data_ptr()
-            m.b1[i] = ws[3].data_ptr()
+            grids.append(fm.data_ptr())
+        ws = []
+        for w in ps[nl:]:
+            if not w.is_contiguous():
+                w = w.detach().contiguous()
+                keep.append(w)
+            ws.append(w.data_ptr())
+        m.grid[:nl] = grids
+        m.w0[:nl] = ws[0::4]
+        m.b0[:nl] = ws[1::4]
+        m.w1[:nl] = ws[2::4]
+        m.b1[:nl] = ws[3::4]
         m._keep = keep
         return m
 

@@ -52,6 +52,31 @@ def test_training_parameter_list_and_model_descriptor():
         assert not m.grid[i] and not m.w0[i] and not m.b1[i]
 
 
+def test_dense_model_descriptor():
+    """OctreeSDF.dense_model: the volumes' and decoders' addresses per LOD, and
+    contiguous copies (kept alive by the descriptor) of parameters that are
+    not in the kernels' layout."""
+    net = seeded_model(num_lods=3, base_lod=2, seed=1)
+    w = net.louts[1][0].weight
+    w.data = w.data.t().contiguous().t()  # same values, transposed strides
+    fm = net.features[2].fm
+    fm.data = fm.data.contiguous()  # channel-first instead of channels_last_3d
+    m = net.dense_model()
+    assert (m.num_lods, m.base_lod, m.feature_dim, m.hidden_dim) == (3, 2, 32, 128)
+    assert len(m._keep) == 2
+    wc = next(t for t in m._keep if t.dim() == 2)
+    fc = next(t for t in m._keep if t.dim() == 5)
+    assert torch.equal(wc, w) and wc.is_contiguous()
+    assert torch.equal(fc, fm) and fc.is_contiguous(memory_format=torch.channels_last_3d)
+    for i in range(3):
+        dec = net.louts[i]
+        assert m.grid[i] == (fc if i == 2 else net.features[i].fm).data_ptr()
+        assert m.w0[i] == (wc if i == 1 else dec[0].weight).data_ptr()
+        assert (m.b0[i], m.w1[i], m.b1[i]) == (dec[0].bias.data_ptr(), dec[2].weight.data_ptr(),
+                                               dec[2].bias.data_ptr())
+    assert not m.grid[3] and not m.w0[3]
+
+
 def test_cpu_tensors_are_rejected():
     net = seeded_model(num_lods=2)
     with torch.no_grad(), pytest.raises(RuntimeError, match="CUDA tensors only"):
